@@ -1,0 +1,560 @@
+// C ABI of the GB300 gravity backend (include/gtc.h).
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gtc.h"
+#include "pipeline.cuh"
+
+static_assert(sizeof(gtc_float4) == 16 && alignof(gtc_float4) == 16, "float4 layout");
+static_assert(sizeof(gtc_kernel_params) == 32, "GTParams layout");
+static_assert(sizeof(gtc_cell) == 48, "GTCell layout");
+static_assert(sizeof(gtc_group) == 32, "GTGroup layout");
+
+struct gtc_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {};
+  std::string error;
+  gtc_stats stats{};
+  gtc::Workspace ws;
+  gtc::Scalars *host_sc = nullptr;  // pinned
+  gtc::DeviceBuffer counter;        // evaluator work queue
+  gtc::DeviceBuffer sample_scratch; // FP64 sample partial sums
+  bool have_group = false;
+  gtc::SolverParams last{};
+};
+
+namespace gtc {
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line) {
+  std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" +
+                    cudaGetErrorString(e) + ") in " + what + " at " + file + ":" +
+                    std::to_string(line);
+  if (e == cudaErrorMemoryAllocation) throw OutOfMemory(msg);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) throw RuntimeError(msg);
+  throw RuntimeError(msg);
+}
+
+void DeviceBuffer::ensure(std::size_t want) {
+  if (want <= bytes && ptr) return;
+  release();
+  const std::size_t grown = want + want / 8 + 256;
+  void *p = nullptr;
+  const cudaError_t e = cudaMalloc(&p, grown);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw OutOfMemory("device allocation of " + std::to_string(grown) + " bytes failed: " +
+                      cudaGetErrorString(e));
+  }
+  ptr = p;
+  bytes = grown;
+}
+
+void DeviceBuffer::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+void Workspace::release_all() {
+  DeviceBuffer *all[] = {&pos, &mass, &acc, &pot, &key0, &key0_alt, &idx, &idx_alt, &key1,
+                         &key2, &tiny, &lcp, &leafdepth, &count, &count_scan, &flags,
+                         &flags_scan, &tpos, &tmass, &bodies, &out, &dpos, &dkey, &dkey_alt,
+                         &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
+                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &walk, &cells,
+                         &gbegin, &gend, &gbox, &gcells, &gbodies, &gcell_off, &gbody_off,
+                         &groups, &cell_list, &body_list, &root, &bbox_part, &scalars, &scan_tmp,
+                         &radix.counts, &radix.scan_tmp};
+  for (DeviceBuffer *b : all) b->release();
+}
+
+}  // namespace gtc
+
+namespace {
+
+using gtc::u32;
+using gtc::u64;
+
+thread_local std::string g_create_error;
+
+template <class F>
+gtc_status guarded(gtc_context *ctx, F &&f) {
+  if (!ctx) return GTC_INVALID_ARGUMENT;
+  try {
+    GTC_CUDA(cudaSetDevice(ctx->device));
+    f();
+    ctx->error.clear();
+    return GTC_OK;
+  } catch (const gtc::InvalidArgument &e) {
+    ctx->error = e.what();
+    return GTC_INVALID_ARGUMENT;
+  } catch (const gtc::OutOfMemory &e) {
+    ctx->error = e.what();
+    return GTC_OUT_OF_MEMORY;
+  } catch (const std::bad_alloc &) {
+    ctx->error = "host allocation failed";
+    return GTC_OUT_OF_MEMORY;
+  } catch (const std::exception &e) {
+    ctx->error = e.what();
+    return GTC_RUNTIME_ERROR;
+  }
+}
+
+gtc::SolverParams check_params(const gtc_gravity_params *gp, bool group) {
+  if (!gp) throw gtc::InvalidArgument("gravity parameters are required");
+  gtc::SolverParams sp{gp->G, gp->theta, gp->eps, gp->quadrupole != 0 ? 1 : 0,
+                       gp->group_size, std::max(1, gp->leaf_size), gp->pack < 0 ? 1 : gp->pack,
+                       gp->criterion};
+  if (group) {
+    if (sp.group_size < 1) throw gtc::InvalidArgument("group_size must be at least 1");
+    if (sp.group_size > gtc::kMaxGroupSize)
+      throw gtc::InvalidArgument("group_size can be at most 32 on cuda");
+    if (!(sp.theta > 0)) throw gtc::InvalidArgument("theta must be positive");
+    if (sp.criterion != GTC_CRITERION_THETA && sp.criterion != GTC_CRITERION_LEARNED)
+      throw gtc::InvalidArgument("unknown opening criterion");
+    if (sp.criterion == GTC_CRITERION_LEARNED)
+      throw gtc::InvalidArgument("the learned criterion needs a trained model (none loaded)");
+  }
+  return sp;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  GTC_CUDA(cudaEventElapsedTime(&ms, a, b));
+  return ms;
+}
+
+// The grouped solver on device arrays (caller order in and out).
+void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
+                 const gtc::SolverParams &sp, double *acc, double *pot) {
+  if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the 32 bit GPU indices");
+  cudaStream_t s = ctx->stream;
+  gtc::Workspace &ws = ctx->ws;
+  ctx->have_group = false;
+  ctx->stats = gtc_stats{};
+  if (n == 0) {
+    ws.n = ws.n_nodes = ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
+    ctx->have_group = true;
+    ctx->last = sp;
+    return;
+  }
+  GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
+  gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
+  GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
+  gtc::build_lists(ws, sp, s, ctx->host_sc);
+  GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
+  if (n > 0) {
+    ws.out.ensure(n * sizeof(float4));
+    ctx->counter.ensure(sizeof(u32));
+    gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
+                        ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
+                        static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
+                        sp.quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+    gtc::scatter_results(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, s);
+  }
+  GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
+  GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
+                           cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  if (ctx->host_sc->error != 0)
+    throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                            std::to_string(ctx->host_sc->error) + ")");
+  gtc_stats &st = ctx->stats;
+  st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
+  st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+  st.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+  st.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+  if (n > 0) {
+    const gtc::Scalars &h = *ctx->host_sc;
+    st.cell_interactions = h.cell_interactions;
+    st.body_interactions = h.body_interactions;
+    st.max_list = h.max_list;
+    st.max_group = h.max_group;
+    st.depth = h.depth;
+  }
+  st.n_cell_list = ws.n_cell_list;
+  st.n_body_list = ws.n_body_list;
+  st.n_nodes = static_cast<u32>(ws.n_nodes);
+  st.n_groups = static_cast<u32>(ws.n_groups);
+  ctx->have_group = true;
+  ctx->last = sp;
+}
+
+void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
+                  const gtc::SolverParams &sp, double *acc, double *pot) {
+  if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the CUDA kernels");
+  cudaStream_t s = ctx->stream;
+  gtc::Workspace &ws = ctx->ws;
+  ctx->stats = gtc_stats{};
+  GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
+  if (n > 0) {
+    gtc::pack_bodies_bbox(ws, pos, mass, n, s);
+    ws.out.ensure(n * sizeof(float4));
+    GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
+    gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), static_cast<float>(sp.G),
+                     static_cast<float>(sp.eps * sp.eps), ws.out.as<float4>(), s);
+  } else {
+    GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
+  }
+  GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  ctx->stats.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+  ctx->stats.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+  ctx->stats.body_interactions = n > 0 ? n * (n - 1) : 0;
+}
+
+}  // namespace
+
+namespace gtc {
+// Caller-order scatter for the direct path (identity order).
+__global__ void k_unpack_direct(const float4 *out, u32 n, double *acc, double *pot) {
+  const u32 i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const float4 o = out[i];
+  acc[3ull * i] = o.x;
+  acc[3ull * i + 1] = o.y;
+  acc[3ull * i + 2] = o.z;
+  pot[i] = o.w;
+}
+}  // namespace gtc
+
+extern "C" {
+
+const char *gtc_status_name(gtc_status s) {
+  switch (s) {
+    case GTC_OK: return "ok";
+    case GTC_INVALID_ARGUMENT: return "invalid argument";
+    case GTC_RUNTIME_ERROR: return "runtime error";
+    case GTC_NO_DEVICE: return "no device";
+    case GTC_OUT_OF_MEMORY: return "out of memory";
+  }
+  return "unknown";
+}
+
+gtc_status gtc_create(gtc_context **out, int device) {
+  if (!out) return GTC_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    (void)cudaGetLastError();
+    g_create_error = std::string("cuda: no GPU device available") +
+                     (e != cudaSuccess ? std::string(" (") + cudaGetErrorString(e) + ")" : "");
+    return GTC_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) {
+    g_create_error = "cuda: device index out of range";
+    return GTC_INVALID_ARGUMENT;
+  }
+  gtc_context *ctx = new (std::nothrow) gtc_context;
+  if (!ctx) return GTC_OUT_OF_MEMORY;
+  ctx->device = device;
+  try {
+    GTC_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop{};
+    GTC_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10)
+      throw gtc::RuntimeError(std::string("cuda: this build needs an sm_103 GPU, found ") +
+                              prop.name);
+    GTC_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    for (auto &ev : ctx->ev) GTC_CUDA(cudaEventCreate(&ev));
+    GTC_CUDA(cudaHostAlloc(&ctx->host_sc, sizeof(gtc::Scalars), cudaHostAllocDefault));
+    std::memset(ctx->host_sc, 0, sizeof(gtc::Scalars));
+  } catch (const std::exception &ex) {
+    g_create_error = ex.what();
+    gtc_destroy(ctx);
+    return GTC_RUNTIME_ERROR;
+  }
+  *out = ctx;
+  return GTC_OK;
+}
+
+void gtc_destroy(gtc_context *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->ws.release_all();
+  ctx->counter.release();
+  ctx->sample_scratch.release();
+  for (auto &ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *gtc_last_error(const gtc_context *ctx) {
+  return ctx ? ctx->error.c_str() : g_create_error.c_str();
+}
+
+void *gtc_stream(gtc_context *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
+gtc_status gtc_direct(gtc_context *ctx, const gtc_float4 *bodies, const gtc_kernel_params *p,
+                      gtc_float4 *out) {
+  return guarded(ctx, [&] {
+    if (!p) throw gtc::InvalidArgument("kernel parameters are required");
+    const u64 n = p->n;
+    if (n == 0) return;
+    if (!bodies || !out) throw gtc::InvalidArgument("bodies and out are required");
+    cudaStream_t s = ctx->stream;
+    gtc::Workspace &ws = ctx->ws;
+    ws.bodies.ensure(n * 16);
+    ws.out.ensure(n * 16);
+    GTC_CUDA(cudaMemcpyAsync(ws.bodies.ptr, bodies, n * 16, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
+    gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), p->G, p->eps2,
+                     ws.out.as<float4>(), s);
+    GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
+    GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    ctx->stats = gtc_stats{};
+    ctx->stats.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+    ctx->stats.total_ms = ctx->stats.evaluate_ms;
+    ctx->stats.body_interactions = n * (n - 1);
+  });
+}
+
+gtc_status gtc_tree(gtc_context *ctx, const gtc_float4 *bodies, const gtc_cell *cells,
+                    uint32_t n_cells, const uint32_t *cell_list, uint64_t n_cell_list,
+                    const uint32_t *body_list, uint64_t n_body_list, const gtc_group *groups,
+                    const gtc_kernel_params *p, gtc_float4 *out) {
+  return guarded(ctx, [&] {
+    if (!p) throw gtc::InvalidArgument("kernel parameters are required");
+    const u64 n = p->n, ng = p->n_groups;
+    if (n == 0 || ng == 0) return;
+    if (!bodies || !groups || !out || (n_cells && !cells) || (n_cell_list && !cell_list) ||
+        (n_body_list && !body_list))
+      throw gtc::InvalidArgument("cuda tree: missing array");
+    // The checks the reference makes (metal_backend.mm:218-223), plus bounds
+    // on every index, so that no kernel reads outside the arrays.
+    for (u64 g = 0; g < ng; ++g) {
+      const gtc_group &G = groups[g];
+      if (G.end < G.begin || G.end > n)
+        throw gtc::InvalidArgument("cuda tree: a group's targets are out of range");
+      if (G.end - G.begin > static_cast<u32>(gtc::kMaxGroupSize))
+        throw gtc::InvalidArgument("cuda tree: a group has more than 32 targets");
+      if (G.cell_end < G.cell_begin || G.cell_end > n_cell_list || G.body_end < G.body_begin ||
+          G.body_end > n_body_list)
+        throw gtc::InvalidArgument("cuda tree: a group's list range is out of range");
+    }
+    for (u64 k = 0; k < n_cell_list; ++k)
+      if (cell_list[k] >= n_cells) throw gtc::InvalidArgument("cuda tree: cell index out of range");
+    for (u64 k = 0; k < n_body_list; ++k)
+      if (body_list[k] >= n) throw gtc::InvalidArgument("cuda tree: body index out of range");
+    cudaStream_t s = ctx->stream;
+    gtc::Workspace &ws = ctx->ws;
+    ws.bodies.ensure(n * 16);
+    ws.out.ensure(n * 16);
+    ws.cells.ensure(std::max<u64>(1, n_cells) * 48);
+    ws.cell_list.ensure(std::max<u64>(1, n_cell_list) * 4);
+    ws.body_list.ensure(std::max<u64>(1, n_body_list) * 4);
+    ws.groups.ensure(ng * 32);
+    GTC_CUDA(cudaMemcpyAsync(ws.bodies.ptr, bodies, n * 16, cudaMemcpyHostToDevice, s));
+    if (n_cells) GTC_CUDA(cudaMemcpyAsync(ws.cells.ptr, cells, n_cells * 48ull, cudaMemcpyHostToDevice, s));
+    if (n_cell_list)
+      GTC_CUDA(cudaMemcpyAsync(ws.cell_list.ptr, cell_list, n_cell_list * 4, cudaMemcpyHostToDevice, s));
+    if (n_body_list)
+      GTC_CUDA(cudaMemcpyAsync(ws.body_list.ptr, body_list, n_body_list * 4, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemcpyAsync(ws.groups.ptr, groups, ng * 32, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemsetAsync(ws.out.ptr, 0, n * 16, s));
+    ctx->counter.ensure(sizeof(u32));
+    GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
+    gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
+                        ws.body_list.as<u32>(), ws.groups.as<uint4>(), ng, p->G, p->eps2,
+                        p->quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+    GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
+    GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    ctx->have_group = false;
+    ctx->stats = gtc_stats{};
+    ctx->stats.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+    ctx->stats.total_ms = ctx->stats.evaluate_ms;
+  });
+}
+
+gtc_status gtc_group_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                  uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                  double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, true);
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    group_force(ctx, pos, mass, n, sp, acc, pot);
+  });
+}
+
+gtc_status gtc_group_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                           const gtc_gravity_params *gp, double *acc, double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, true);
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    gtc::Workspace &ws = ctx->ws;
+    cudaStream_t s = ctx->stream;
+    const u64 nn = std::max<u64>(n, 1);
+    ws.pos.ensure(nn * 24);
+    ws.mass.ensure(nn * 8);
+    ws.acc.ensure(nn * 24);
+    ws.pot.ensure(nn * 8);
+    if (n) {
+      GTC_CUDA(cudaMemcpyAsync(ws.pos.ptr, pos, n * 24, cudaMemcpyHostToDevice, s));
+      GTC_CUDA(cudaMemcpyAsync(ws.mass.ptr, mass, n * 8, cudaMemcpyHostToDevice, s));
+    }
+    group_force(ctx, ws.pos.as<double>(), ws.mass.as<double>(), n, sp, ws.acc.as<double>(),
+                ws.pot.as<double>());
+    if (n) {
+      GTC_CUDA(cudaMemcpyAsync(acc, ws.acc.ptr, n * 24, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(pot, ws.pot.ptr, n * 8, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+    }
+  });
+}
+
+gtc_status gtc_direct_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                   uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                   double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, false);
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    direct_force(ctx, pos, mass, n, sp, acc, pot);
+    if (n) {
+      gtc::k_unpack_direct<<<gtc::ceil_div(n, 256), 256, 0, ctx->stream>>>(
+          ctx->ws.out.as<float4>(), static_cast<u32>(n), acc, pot);
+      GTC_LAUNCH_CHECK();
+      GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+  });
+}
+
+gtc_status gtc_direct_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                            const gtc_gravity_params *gp, double *acc, double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, false);
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    gtc::Workspace &ws = ctx->ws;
+    cudaStream_t s = ctx->stream;
+    const u64 nn = std::max<u64>(n, 1);
+    ws.pos.ensure(nn * 24);
+    ws.mass.ensure(nn * 8);
+    ws.acc.ensure(nn * 24);
+    ws.pot.ensure(nn * 8);
+    if (n) {
+      GTC_CUDA(cudaMemcpyAsync(ws.pos.ptr, pos, n * 24, cudaMemcpyHostToDevice, s));
+      GTC_CUDA(cudaMemcpyAsync(ws.mass.ptr, mass, n * 8, cudaMemcpyHostToDevice, s));
+    }
+    direct_force(ctx, ws.pos.as<double>(), ws.mass.as<double>(), n, sp, ws.acc.as<double>(),
+                 ws.pot.as<double>());
+    if (n) {
+      gtc::k_unpack_direct<<<gtc::ceil_div(n, 256), 256, 0, s>>>(
+          ws.out.as<float4>(), static_cast<u32>(n), ws.acc.as<double>(), ws.pot.as<double>());
+      GTC_LAUNCH_CHECK();
+      GTC_CUDA(cudaMemcpyAsync(acc, ws.acc.ptr, n * 24, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(pot, ws.pot.ptr, n * 8, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+    }
+  });
+}
+
+gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const double *mass,
+                                  uint64_t n, const uint64_t *idx, uint64_t m, double G,
+                                  double eps, double *acc, double *pot) {
+  return guarded(ctx, [&] {
+    if (m > 0 && (!pos || !mass || !idx || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, idx, acc and pot are required");
+    gtc::direct_fp64_sample(pos, mass, n, idx, m, G, eps, acc, pot, ctx->sample_scratch,
+                            ctx->stream);
+    GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out) {
+  if (!ctx || !out) return GTC_INVALID_ARGUMENT;
+  *out = ctx->stats;
+  return GTC_OK;
+}
+
+gtc_status gtc_group_sizes(const gtc_context *ctx, uint64_t *n_bodies, uint64_t *n_nodes,
+                           uint64_t *n_groups, uint64_t *n_cell_list, uint64_t *n_body_list) {
+  if (!ctx) return GTC_INVALID_ARGUMENT;
+  const bool ok = ctx->have_group;
+  if (n_bodies) *n_bodies = ok ? ctx->ws.n : 0;
+  if (n_nodes) *n_nodes = ok ? ctx->ws.n_nodes : 0;
+  if (n_groups) *n_groups = ok ? ctx->ws.n_groups : 0;
+  if (n_cell_list) *n_cell_list = ok ? ctx->ws.n_cell_list : 0;
+  if (n_body_list) *n_body_list = ok ? ctx->ws.n_body_list : 0;
+  return ok ? GTC_OK : GTC_INVALID_ARGUMENT;
+}
+
+gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
+                            gtc_float4 *bodies, gtc_cell *cells, gtc_group *groups,
+                            uint32_t *cell_list, uint32_t *body_list, gtc_float4 *out) {
+  return guarded(ctx, [&] {
+    if (!ctx->have_group) throw gtc::InvalidArgument("no grouped solve to export");
+    gtc::Workspace &ws = ctx->ws;
+    const u64 n = ws.n, m = ws.n_nodes;
+    auto get = [&](void *dst, const gtc::DeviceBuffer &src, u64 bytes) {
+      if (dst && bytes) GTC_CUDA(cudaMemcpy(dst, src.ptr, bytes, cudaMemcpyDeviceToHost));
+    };
+    GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (nodes && m) {
+      std::vector<double2> geom(2 * m), mom(2 * m);
+      std::vector<double2> quad(3 * m);
+      std::vector<double> delta(m);
+      std::vector<u32> nb(m), ne(m), sk(m), par(m);
+      std::vector<gtc::u8> dep(m), nch(m);
+      get(geom.data(), ws.geom, 2 * m * sizeof(double2));
+      get(mom.data(), ws.mom, 2 * m * sizeof(double2));
+      get(quad.data(), ws.quad, 3 * m * sizeof(double2));
+      get(delta.data(), ws.delta, m * 8);
+      get(nb.data(), ws.nbegin, m * 4);
+      get(ne.data(), ws.nend, m * 4);
+      get(sk.data(), ws.skip, m * 4);
+      get(par.data(), ws.parent, m * 4);
+      get(dep.data(), ws.depth, m);
+      get(nch.data(), ws.nchild, m);
+      for (u64 p = 0; p < m; ++p) {
+        gtc_node &o = nodes[p];
+        o.center[0] = geom[2 * p].x;
+        o.center[1] = geom[2 * p].y;
+        o.center[2] = geom[2 * p + 1].x;
+        o.half = geom[2 * p + 1].y;
+        o.com[0] = mom[2 * p].x;
+        o.com[1] = mom[2 * p].y;
+        o.com[2] = mom[2 * p + 1].x;
+        o.mass = mom[2 * p + 1].y;
+        o.quad[0] = quad[3 * p].x;
+        o.quad[1] = quad[3 * p].y;
+        o.quad[2] = quad[3 * p + 1].x;
+        o.quad[3] = quad[3 * p + 1].y;
+        o.quad[4] = quad[3 * p + 2].x;
+        o.quad[5] = quad[3 * p + 2].y;
+        o.delta = delta[p];
+        o.begin = nb[p];
+        o.end = ne[p];
+        o.skip = sk[p];
+        o.parent = par[p];
+        o.depth = dep[p];
+        o.n_children = nch[p];
+      }
+    }
+    if (order && n) {
+      std::vector<u32> idx(n);
+      get(idx.data(), ws.idx, n * 4);
+      for (u64 k = 0; k < n; ++k) order[k] = idx[k];
+    }
+    get(bodies, ws.bodies, n * 16);
+    get(cells, ws.cells, m * 48);
+    get(groups, ws.groups, ws.n_groups * 32);
+    get(cell_list, ws.cell_list, ws.n_cell_list * 4);
+    get(body_list, ws.body_list, ws.n_body_list * 4);
+    get(out, ws.out, n * 16);
+  });
+}
+
+}  // extern "C"

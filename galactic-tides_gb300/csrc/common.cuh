@@ -1,0 +1,75 @@
+// Shared declarations of the GB300 gravity backend (libgtc.so).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace gtc {
+
+using u8 = std::uint8_t;
+using u32 = std::uint32_t;
+using u64 = std::uint64_t;
+
+// ----------------------------------------------------------------- errors
+// Host code throws these; the C ABI layer turns them into gtc_status codes.
+struct InvalidArgument : std::invalid_argument {
+  using std::invalid_argument::invalid_argument;
+};
+struct RuntimeError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct OutOfMemory : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line);
+
+#define GTC_CUDA(call)                                                       \
+  do {                                                                       \
+    cudaError_t gtc_e_ = (call);                                             \
+    if (gtc_e_ != cudaSuccess) ::gtc::throw_cuda(gtc_e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define GTC_LAUNCH_CHECK() GTC_CUDA(cudaGetLastError())
+
+// ------------------------------------------------------- device buffers
+// Grow-only device allocation, kept between calls.
+struct DeviceBuffer {
+  void *ptr = nullptr;
+  std::size_t bytes = 0;
+  void ensure(std::size_t want);
+  void release();
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+
+inline u32 ceil_div(u64 a, u64 b) { return static_cast<u32>((a + b - 1) / b); }
+
+// --------------------------------------------------------------- scans
+// Exclusive prefix sums over n elements on `s`. `tmp` is grown as needed.
+// The total is written to *total_dev (device memory, may be null).
+void exclusive_scan_u32(const u32 *in, u32 *out, u64 n, u32 *total_dev, DeviceBuffer &tmp,
+                        cudaStream_t s);
+void exclusive_scan_u64(const u64 *in, u64 *out, u64 n, u64 *total_dev, DeviceBuffer &tmp,
+                        cudaStream_t s);
+
+// ---------------------------------------------------------- radix sort
+// Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the
+// key. The sorted pairs end up back in keys/vals; alt_* are scratch of n
+// elements each.
+struct RadixScratch {
+  DeviceBuffer counts, scan_tmp;
+};
+void radix_sort_pairs(u64 *keys, u32 *vals, u64 *alt_keys, u32 *alt_vals, u32 n, int bits,
+                      RadixScratch &scratch, cudaStream_t s);
+
+// ------------------------------------------------------- warp helpers
+constexpr unsigned kFullMask = 0xffffffffu;
+
+}  // namespace gtc

@@ -1,0 +1,179 @@
+// Warp-per-group evaluation of grouped interaction lists, FP32.
+//
+// Same arithmetic as the reference's shared kernels (gt_body / gt_cell,
+// include/galactic_tides/kernels/gravity_kernels.h:71-135) and the same
+// order -- all cells in list order, then all bodies in list order, skipping
+// the target itself (gt_group_accel, :162-170) -- with FMA contraction and
+// the SFU reciprocal square root (rsqrtf) instead of 1/sqrt.
+//
+// Lane l of a warp owns target begin + l of its group. The warp walks the
+// list 32 entries at a time: each lane loads one entry (coalesced index
+// load, then one 48-byte cell or 16-byte body), scales its mass and
+// quadrupole by G once, and stages it in shared memory; then every lane
+// reads the 32 staged entries back as broadcast loads (one shared-memory
+// transaction serves the whole warp) and accumulates. The body index of
+// each staged entry is passed round with __shfl_sync for the self test.
+// Groups are handed out to warps by an atomic counter, so a warp that drew
+// a long list does not hold back the others' next groups.
+
+#include <algorithm>
+
+#include "pipeline.cuh"
+
+namespace gtc {
+namespace {
+
+constexpr int kWarpsPerBlock = 4;
+constexpr int kT = 32 * kWarpsPerBlock;
+
+struct Staged {
+  float4 cm;   // com (rel. origin), G * mass
+  float4 q0;   // G * (xx, yy, zz, xy)
+  float4 q1;   // G * (xz, yz, -, -)
+};
+
+template <bool kQuad>
+__device__ __forceinline__ void add_cell(float px, float py, float pz, const Staged &c, float eps2,
+                                         float &ax, float &ay, float &az, float &pot) {
+  const float dx = px - c.cm.x, dy = py - c.cm.y, dz = pz - c.cm.z;
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+  const float inv = rsqrtf(r2);
+  const float inv2 = inv * inv;
+  const float inv3 = inv * inv2;
+  const float gm3 = c.cm.w * inv3;
+  ax = fmaf(-gm3, dx, ax);
+  ay = fmaf(-gm3, dy, ay);
+  az = fmaf(-gm3, dz, az);
+  pot = fmaf(-c.cm.w, inv, pot);
+  if (kQuad) {
+    const float qx = fmaf(c.q0.x, dx, fmaf(c.q0.w, dy, c.q1.x * dz));
+    const float qy = fmaf(c.q0.w, dx, fmaf(c.q0.y, dy, c.q1.y * dz));
+    const float qz = fmaf(c.q1.x, dx, fmaf(c.q1.y, dy, c.q0.z * dz));
+    const float rqr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+    const float inv5 = inv3 * inv2;
+    const float inv7 = inv5 * inv2;
+    const float u = 2.5f * rqr * inv7;
+    ax = fmaf(qx, inv5, fmaf(-u, dx, ax));
+    ay = fmaf(qy, inv5, fmaf(-u, dy, ay));
+    az = fmaf(qz, inv5, fmaf(-u, dz, az));
+    pot = fmaf(-0.5f * rqr, inv5, pot);
+  }
+}
+
+template <bool kQuad>
+__global__ void __launch_bounds__(kT)
+    k_eval(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
+           const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
+           const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
+           float4 *__restrict__ out, u32 *next_group) {
+  __shared__ Staged sc[kWarpsPerBlock][32];
+  __shared__ float4 sb[kWarpsPerBlock][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    u32 g = 0;
+    if (lane == 0) g = atomicAdd(next_group, 1u);
+    g = __shfl_sync(kFullMask, g, 0);
+    if (g >= ngroups) return;
+    const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
+    const u32 i = ga.x + lane;
+    const bool active = i < ga.y;
+    const float4 bi = active ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
+
+    for (u32 base = ga.z; base < ga.w; base += 32) {
+      const u32 k = base + lane;
+      if (k < ga.w) {
+        const u64 c = cell_list[k];
+        const float4 c0 = __ldg(&cells[3 * c]);
+        Staged st;
+        st.cm = make_float4(c0.x, c0.y, c0.z, G * c0.w);
+        if (kQuad) {
+          const float4 c1 = __ldg(&cells[3 * c + 1]), c2 = __ldg(&cells[3 * c + 2]);
+          st.q0 = make_float4(G * c1.x, G * c1.y, G * c1.z, G * c1.w);
+          st.q1 = make_float4(G * c2.x, G * c2.y, 0.f, 0.f);
+        }
+        sc[warp][lane] = st;
+      }
+      __syncwarp();
+      const u32 cnt = min(32u, ga.w - base);
+      for (u32 t = 0; t < cnt; ++t) add_cell<kQuad>(bi.x, bi.y, bi.z, sc[warp][t], eps2, ax, ay, az, pot);
+      __syncwarp();
+    }
+
+    for (u32 base = gb.x; base < gb.y; base += 32) {
+      const u32 k = base + lane;
+      u32 j = 0xffffffffu;
+      if (k < gb.y) {
+        j = body_list[k];
+        const float4 b = __ldg(&bodies[j]);
+        sb[warp][lane] = make_float4(b.x, b.y, b.z, G * b.w);
+      }
+      __syncwarp();
+      const u32 cnt = min(32u, gb.y - base);
+      for (u32 t = 0; t < cnt; ++t) {
+        const u32 jt = __shfl_sync(kFullMask, j, t);
+        const float4 b = sb[warp][t];
+        const bool self = jt == i;
+        const float dx = bi.x - b.x, dy = bi.y - b.y, dz = bi.z - b.z;
+        const float r2 = self ? 1.0f : fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        const float inv = rsqrtf(r2);
+        const float gm = (self ? 0.0f : b.w) * inv;
+        const float gm3 = gm * inv * inv;
+        ax = fmaf(-gm3, dx, ax);
+        ay = fmaf(-gm3, dy, ay);
+        az = fmaf(-gm3, dz, az);
+        pot -= gm;
+      }
+      __syncwarp();
+    }
+    if (active) out[i] = make_float4(ax, ay, az, pot);
+  }
+}
+
+// Tree order -> caller order, FP32 -> FP64 (gravity_backends.cpp:132-136).
+__global__ void __launch_bounds__(256)
+    k_scatter(const float4 *out, const u32 *order, u32 n, double *acc, double *pot) {
+  const u32 k = blockIdx.x * 256 + threadIdx.x;
+  if (k >= n) return;
+  const float4 o = out[k];
+  const u64 i = order[k];
+  acc[3 * i] = o.x;
+  acc[3 * i + 1] = o.y;
+  acc[3 * i + 2] = o.z;
+  pot[i] = o.w;
+}
+
+}  // namespace
+
+void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                    const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
+                    bool quadrupole, float4 *out, u32 *counter, cudaStream_t s) {
+  if (n_groups == 0) return;
+  GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
+  int dev = 0, sms = 0, per_sm = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (quadrupole)
+    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<true>, kT, 0));
+  else
+    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<false>, kT, 0));
+  const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
+  const u32 ng = static_cast<u32>(n_groups);
+  if (quadrupole)
+    k_eval<true><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups, ng, G, eps2, out,
+                                     counter);
+  else
+    k_eval<false><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups, ng, G, eps2, out,
+                                      counter);
+  GTC_LAUNCH_CHECK();
+}
+
+void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
+                     cudaStream_t s) {
+  if (n == 0) return;
+  k_scatter<<<ceil_div(n, 256), 256, 0, s>>>(out, order, static_cast<u32>(n), acc, pot);
+  GTC_LAUNCH_CHECK();
+}
+
+}  // namespace gtc

@@ -1,0 +1,274 @@
+// Group choice and grouped walk on the device, producing the reference's
+// lists exactly (src/group_lists.cpp:65-207). Compiled with -fmad=false: the
+// FP64 opening test rounds every product and sum separately, as the
+// reference's x86-64 build does, so every accept/open decision matches.
+//
+// Groups. The reference visits the tree depth first and emits, for every
+// node with more than group_size bodies, its children in order: small ones
+// (merged with their preceding small siblings while the run fits, when
+// packing), large leaves cut into chunks, large inner nodes recursed into.
+// Each such node's contribution depends only on its own children, so one
+// thread per node marks where its groups start in tree order; a scan turns
+// the marks into the group array, which comes out in tree order as in the
+// reference.
+//
+// Walk. One thread per group traverses the nodes in their stored order
+// (the order the reference's stack pops them): accept -> record and jump to
+// the node's skip link, leaf -> record its bodies and jump, otherwise step
+// to the next node (its last child). A counting pass sizes the lists; after
+// the offsets are scanned a second pass writes them.
+
+#include <algorithm>
+
+#include "pipeline.cuh"
+
+namespace gtc {
+namespace {
+
+constexpr int kT = 256;
+
+struct NodeView {
+  const u32 *nbegin, *nend, *skip;
+  const u8 *isleaf;
+};
+
+__global__ void __launch_bounds__(kT)
+    k_group_marks(NodeView nv, u32 m, u32 n, u32 gs, int pack, u32 *mark) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  const u32 size = nv.nend[p] - nv.nbegin[p];
+  if (p == 0 && (size <= gs || nv.isleaf[0])) {
+    for (u32 c = 0; c < n; c += gs) mark[c] = 1;
+    return;
+  }
+  if (nv.isleaf[p] || size <= gs) return;
+  // children, last octant first
+  u32 ch[8];
+  int nc = 0;
+  for (u32 c = p + 1; c < nv.skip[p] && nc < 8; c = nv.skip[c]) ch[nc++] = c;
+  bool open = false;
+  u32 run_begin = 0, run_end = 0;
+  for (int j = nc - 1; j >= 0; --j) {
+    const u32 c = ch[j];
+    const u32 cb = nv.nbegin[c], ce = nv.nend[c], cc = ce - cb;
+    if (cc <= gs) {
+      if (pack && open && (run_end - run_begin) + cc <= gs) {
+        run_end = ce;
+      } else {
+        if (open) mark[run_begin] = 1;
+        run_begin = cb;
+        run_end = ce;
+        open = true;
+      }
+    } else {
+      if (open) mark[run_begin] = 1;
+      open = false;
+      if (nv.isleaf[c])
+        for (u32 x = cb; x < ce; x += gs) mark[x] = 1;
+    }
+  }
+  if (open) mark[run_begin] = 1;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_group_ranges(const u32 *mark, const u32 *scan, u32 n, u32 *gbegin, u32 *gend) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b >= n || !mark[b]) return;
+  const u32 g = scan[b];
+  gbegin[g] = b;
+  if (g > 0) gend[g - 1] = b;
+}
+
+__global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
+  if (sc->n_groups > 0) gend[sc->n_groups - 1] = n;
+}
+
+// Group bounding box (group_lists.cpp:125-131): centre and half-extent.
+__global__ void __launch_bounds__(kT)
+    k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos, double *gbox) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= ng) return;
+  const u32 b0 = gbegin[g], b1 = gend[g];
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) lo[a] = hi[a] = tpos[3ull * b0 + a];
+  for (u32 k = b0; k < b1; ++k)
+    for (int a = 0; a < 3; ++a) {
+      const double v = tpos[3ull * k + a];
+      lo[a] = v < lo[a] ? v : lo[a];
+      hi[a] = hi[a] < v ? v : hi[a];
+    }
+  for (int a = 0; a < 3; ++a) {
+    gbox[6ull * g + a] = (lo[a] + hi[a]) * 0.5;
+    gbox[6ull * g + 3 + a] = (hi[a] - lo[a]) * 0.5;
+  }
+}
+
+// The opening test of group_lists.cpp:145-154 for one node.
+__device__ __forceinline__ bool accept(const WalkRec &r, const double *gc, const double *gh) {
+  bool overlap = true;
+  double d2 = 0.0;
+  if (fabs(r.cx - gc[0]) > r.slack + gh[0]) overlap = false;
+  double d = fabs(r.mx - gc[0]) - gh[0];
+  if (d > 0) d2 += d * d;
+  if (fabs(r.cy - gc[1]) > r.slack + gh[1]) overlap = false;
+  d = fabs(r.my - gc[1]) - gh[1];
+  if (d > 0) d2 += d * d;
+  if (fabs(r.cz - gc[2]) > r.slack + gh[2]) overlap = false;
+  d = fabs(r.mz - gc[2]) - gh[2];
+  if (d > 0) d2 += d * d;
+  return !overlap && d2 > r.crit2;
+}
+
+__device__ __forceinline__ WalkRec load_rec(const WalkRec *w, u32 i) {
+  const double2 *p = reinterpret_cast<const double2 *>(w + i);
+  const double2 a0 = __ldg(p), a1 = __ldg(p + 1), b0 = __ldg(p + 2), b1 = __ldg(p + 3);
+  const uint4 c = __ldg(reinterpret_cast<const uint4 *>(p + 4));
+  WalkRec r;
+  r.cx = a0.x;
+  r.cy = a0.y;
+  r.cz = a1.x;
+  r.slack = a1.y;
+  r.mx = b0.x;
+  r.my = b0.y;
+  r.mz = b1.x;
+  r.crit2 = b1.y;
+  r.skip = c.x;
+  r.nbody = c.y;
+  r.begin = c.z;
+  r.leaf = c.w;
+  return r;
+}
+
+struct WalkOut {
+  u64 *ncells, *nbodies;          // count pass
+  const u64 *cell_off, *body_off; // fill pass
+  u32 *cell_list, *body_list;
+  uint4 *groups;
+};
+
+template <bool kFill>
+__global__ void __launch_bounds__(kT)
+    k_walk(const WalkRec *walk, u32 m, const u32 *gbegin, const u32 *gend, const double *gbox,
+           u32 ng, WalkOut out, Scalars *sc) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= ng) return;
+  double gc[3], gh[3];
+  for (int a = 0; a < 3; ++a) {
+    gc[a] = gbox[6ull * g + a];
+    gh[a] = gbox[6ull * g + 3 + a];
+  }
+  u32 *cl = nullptr, *bl = nullptr;
+  if (kFill) {
+    cl = out.cell_list + out.cell_off[g];
+    bl = out.body_list + out.body_off[g];
+  }
+  u32 nc = 0, nb = 0;
+  u32 i = 0;
+  while (i < m) {
+    const WalkRec r = load_rec(walk, i);
+    if (accept(r, gc, gh)) {
+      if (r.nbody <= kFewBodies) {
+        if (kFill)
+          for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
+        nb += r.nbody;
+      } else {
+        if (kFill) cl[nc] = i;
+        ++nc;
+      }
+      if (r.skip <= i) break;  // malformed tree: never loop
+      i = r.skip;
+    } else if (r.leaf) {
+      if (kFill)
+        for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
+      nb += r.nbody;
+      if (r.skip <= i) break;
+      i = r.skip;
+    } else {
+      ++i;
+    }
+  }
+  if (i < m) atomicOr(&sc->error, 1u);
+  const u32 t = gend[g] - gbegin[g];
+  if (kFill) {
+    const u64 c0 = out.cell_off[g], b0 = out.body_off[g];
+    out.groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0),
+                                      static_cast<u32>(c0 + nc));
+    out.groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + nb), 0u, 0u);
+  } else {
+    out.ncells[g] = nc;
+    out.nbodies[g] = nb;
+    atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t) * nc);
+    atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t) * nb - t);
+    atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
+    atomicMax(&sc->max_group, t);
+  }
+}
+
+void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
+  GTC_CUDA(cudaMemcpyAsync(host, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host) {
+  const u64 n = ws.n;
+  ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
+  if (n == 0) return;
+  const u32 n32 = static_cast<u32>(n), m = static_cast<u32>(ws.n_nodes);
+  const u32 gs = static_cast<u32>(sp.group_size);
+  Scalars *sc = ws.scalars.as<Scalars>();
+  ws.flags.ensure(n * 4);
+  ws.flags_scan.ensure(n * 4);
+  u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
+  GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
+  NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
+  k_group_marks<<<ceil_div(m, kT), kT, 0, s>>>(nv, m, n32, gs, sp.pack, mark);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u32(mark, mscan, n, &sc->n_groups, ws.scan_tmp, s);
+  // group ranges (the count is at most n; sized for n so no read-back is needed)
+  ws.gbegin.ensure(n * 4);
+  ws.gend.ensure(n * 4);
+  ws.gbox.ensure(n * 48);
+  ws.gcells.ensure(n * 8);
+  ws.gbodies.ensure(n * 8);
+  ws.gcell_off.ensure(n * 8);
+  ws.gbody_off.ensure(n * 8);
+  ws.groups.ensure(n * 32);
+  u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
+  k_group_ranges<<<ceil_div(n, kT), kT, 0, s>>>(mark, mscan, n32, gbegin, gend);
+  GTC_LAUNCH_CHECK();
+  k_last_end<<<1, 1, 0, s>>>(sc, n32, gend);
+  GTC_LAUNCH_CHECK();
+  GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
+  read_scalars(ws, host, s);
+  const u32 ng = host->n_groups;
+  ws.n_groups = ng;
+  const u32 gb = ceil_div(ng, kT);
+  k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.gbox.as<double>());
+  GTC_LAUNCH_CHECK();
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.gcell_off.as<u64>(),
+             ws.gbody_off.as<u64>(), nullptr, nullptr, ws.groups.as<uint4>()};
+  k_walk<false><<<gb, kT, 0, s>>>(ws.walk.as<WalkRec>(), m, gbegin, gend, ws.gbox.as<double>(), ng,
+                                  wo, sc);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u64(ws.gcells.as<u64>(), ws.gcell_off.as<u64>(), ng, &sc->n_cell_list,
+                     ws.scan_tmp, s);
+  exclusive_scan_u64(ws.gbodies.as<u64>(), ws.gbody_off.as<u64>(), ng, &sc->n_body_list,
+                     ws.scan_tmp, s);
+  read_scalars(ws, host, s);
+  if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
+    throw RuntimeError("interaction lists too long for 32 bit offsets");
+  ws.n_cell_list = host->n_cell_list;
+  ws.n_body_list = host->n_body_list;
+  ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
+  ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
+  wo.cell_list = ws.cell_list.as<u32>();
+  wo.body_list = ws.body_list.as<u32>();
+  k_walk<true><<<gb, kT, 0, s>>>(ws.walk.as<WalkRec>(), m, gbegin, gend, ws.gbox.as<double>(), ng,
+                                 wo, sc);
+  GTC_LAUNCH_CHECK();
+}
+
+}  // namespace gtc

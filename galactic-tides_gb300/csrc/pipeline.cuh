@@ -1,0 +1,115 @@
+// The device-resident grouped solver: workspace and stage entry points.
+//
+// Data layout in HBM (N bodies, M tree nodes, G groups):
+//   per body   pos/mass (caller order, FP64), sort keys (up to three 63-bit
+//              words of octant digits), tree-order permutation, tree-order
+//              FP64 positions/masses, FP32 bodies (float4), FP32 output.
+//   per node   geometry (centre, half), FP64 moments (com, mass, quadrupole,
+//              delta), range [begin, end), skip, parent, depth, and the packed
+//              FP32 cell (48 B) and FP64 walk record (80 B) the kernels read.
+//   per group  target range, FP64 bounding box, list offsets, GTGroup.
+//   lists      cell_list / body_list, uint32 node / body indices.
+// Nodes are numbered in the reference walk's visiting order (root, then the
+// children's subtrees last octant first), which makes the grouped walk a
+// stackless forward scan with skip links.
+#pragma once
+
+#include "common.cuh"
+
+namespace gtc {
+
+constexpr int kMaxDepth = 60;     // depth cap of the reference octree (octree.cpp:18)
+constexpr int kLevelsPerWord = 21;
+constexpr u32 kFewBodies = 2;     // accepted cells this small go on the body list (group_lists.h:58)
+constexpr int kMaxGroupSize = 32;
+
+// Root cube: the reference's bounding-box rule (octree.cpp:184-198) and the
+// half side of a node at every depth (each child halves its parent's side).
+struct TreeRoot {
+  double lo[3], hi[3];
+  double center[3];
+  double half_at[kMaxDepth + 1];
+};
+
+// What the grouped walk reads per node, 80 bytes.
+struct alignas(16) WalkRec {
+  double cx, cy, cz, slack;  // slack = half * 1.0001 (group_lists.cpp:147)
+  double mx, my, mz, crit2;  // crit = 2 half / theta + delta (group_lists.cpp:59-60)
+  u32 skip, nbody, begin, leaf;
+};
+
+struct SolverParams {
+  double G, theta, eps;
+  int quadrupole, group_size, leaf_size, pack, criterion;
+};
+
+struct Workspace {
+  // bodies
+  DeviceBuffer pos, mass;                 // staged caller input (host calls)
+  DeviceBuffer acc, pot;                  // staged caller output (host calls)
+  DeviceBuffer key0, key0_alt, idx, idx_alt, key1, key2, tiny;
+  DeviceBuffer lcp, leafdepth, count, count_scan, flags, flags_scan;
+  DeviceBuffer tpos, tmass, bodies, out;
+  // deep rounds
+  DeviceBuffer dpos, dkey, dkey_alt, drec, drec_alt, dseg, dtmp;
+  // nodes
+  DeviceBuffer geom, mom, quad, delta, nbegin, nend, skip, parent, depth, nchild, isleaf,
+      arrive, walk, cells;
+  // groups and lists
+  DeviceBuffer gbegin, gend, gbox, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
+      body_list;
+  // scalars and reductions
+  DeviceBuffer root, bbox_part, scalars;
+  DeviceBuffer scan_tmp;
+  RadixScratch radix;
+
+  // host-side view of the last build
+  u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
+  int key_words = 1;
+  void release_all();
+};
+
+// Device scalars written by the stages, read back once per call.
+struct Scalars {
+  u32 deep;               // bodies whose leaf lies below the key words so far
+  u32 n_nodes;
+  u32 n_groups;
+  u32 depth;              // deepest leaf
+  u64 n_cell_list, n_body_list;
+  unsigned long long cell_interactions, body_interactions, max_list;
+  u32 max_group;
+  u32 aux;                // scratch count (deep-round segments)
+  u32 error;              // device-detected failure code (0 = none)
+};
+
+// Stage 1: octree on the device. pos (N x 3) and mass in caller order.
+// Fills geometry, moments, ranges, the tree-order permutation (idx), the
+// FP32 bodies and cells and the walk records. Returns the node count.
+// `host` is pinned memory the device scalars are read back into.
+void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
+                const SolverParams &sp, cudaStream_t s, Scalars *host);
+
+// Stage 2: groups (with sibling packing) and the grouped walk; fills groups,
+// cell_list and body_list and the interaction counters.
+void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host);
+
+// Stage 3: warp-per-group evaluation of the lists into ws.out (tree order),
+// then the scatter into acc/pot in caller order (FP64).
+// `counter` is one device word the kernel's work queue uses.
+void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                    const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
+                    bool quadrupole, float4 *out, u32 *counter, cudaStream_t s);
+void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
+                     cudaStream_t s);
+
+// Direct summation kernels.
+void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, cudaStream_t s);
+void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
+                        double G, double eps, double *acc, double *pot, DeviceBuffer &scratch,
+                        cudaStream_t s);
+// float4 bodies relative to the bounding-box centre (gravity_backends.cpp:15-23, :62).
+void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 n,
+                      cudaStream_t s);
+void bbox_root(Workspace &ws, const double *pos, u64 n, cudaStream_t s);
+
+}  // namespace gtc

@@ -1,0 +1,742 @@
+// Octree build on the device, bit-identical to the reference's CPU build
+// (src/octree.cpp:169-273). Compiled with -fmad=false: every FP64 product
+// and sum below rounds separately, as in the reference's x86-64 build.
+//
+// The reference splits a node at its centre c (body goes up on an axis when
+// p >= c) and makes each child's centre c +- h/2, recursively, with a stable
+// counting sort. Here every body replays that chain of comparisons and
+// additions on its own, writing the octant of every level as a 3-bit digit
+// of a key (21 levels per 64-bit word), and one stable radix sort of the
+// keys reproduces the reference's tree order. The tree's shape follows from
+// the sorted keys alone:
+//   * lcp(a, b): the number of leading levels two bodies share;
+//   * a node of depth d holds more than L = leaf_size bodies iff some run of
+//     L+1 consecutive sorted bodies shares d levels, so a body's leaf depth is
+//     1 + max lcp over the L+1 windows that contain it, capped by depth 60 and
+//     by the reference's "tiny node" rule (octree.cpp:40-44);
+//   * the nodes that end at sorted position b are the depths
+//     lcp(b, b+1) < d <= leafdepth(b).
+// Numbering nodes by (end descending, depth ascending) gives exactly the
+// order in which the reference's group walk pops them (group_lists.cpp:
+// 141-164), so each node's subtree is a contiguous index range and a
+// "skip" link replaces the walk's stack. Bodies deeper than 21 levels (dense
+// clumps, coincident points) get further key words in up to two more rounds,
+// sorted within their depth-21 (or 42) node.
+//
+// Inside a leaf the reference keeps bodies in input order (its sort is
+// stable and leaves are not split further), so each leaf's range is put back
+// in input order before the moments are taken. Moments are FP64, leaves
+// summed in tree order and parents from their children in octant order
+// (octree.cpp:46-102), bottom-up with one arrival counter per node.
+
+#include <algorithm>
+#include <cstddef>
+
+#include "pipeline.cuh"
+
+namespace gtc {
+namespace {
+
+constexpr int kT = 256;
+constexpr u8 kNoTiny = 255;
+
+struct Dbl4 {
+  double x, y, z, w;
+};
+__device__ __forceinline__ Dbl4 make_dbl4(double x, double y, double z, double w) {
+  return Dbl4{x, y, z, w};
+}
+
+struct KeyView {
+  const u64 *w0, *w1, *w2;
+  int words;
+};
+
+__device__ __forceinline__ int word_lcp(u64 a, u64 b, int levels) {
+  const u64 x = a ^ b;
+  if (x == 0) return levels;
+  const int q = (__clzll(static_cast<long long>(x)) - 1) / 3;
+  return q < levels ? q : levels;
+}
+
+// Levels shared by the bodies at sorted positions a and b.
+__device__ __forceinline__ int lcp(const KeyView &kv, u32 a, u32 b) {
+  int l = word_lcp(kv.w0[a], kv.w0[b], kLevelsPerWord);
+  if (l < kLevelsPerWord || kv.words == 1) return l;
+  l = word_lcp(kv.w1[a], kv.w1[b], kLevelsPerWord);
+  if (l < kLevelsPerWord || kv.words == 2) return kLevelsPerWord + l;
+  return 2 * kLevelsPerWord + word_lcp(kv.w2[a], kv.w2[b], kMaxDepth - 2 * kLevelsPerWord);
+}
+
+// Octant digit of level `lvl` (1-based) of the body at sorted position b.
+__device__ __forceinline__ int digit(const KeyView &kv, u32 b, int lvl) {
+  const int w = (lvl - 1) / kLevelsPerWord, q = (lvl - 1) % kLevelsPerWord;
+  const u64 word = w == 0 ? kv.w0[b] : (w == 1 ? kv.w1[b] : kv.w2[b]);
+  return static_cast<int>((word >> (60 - 3 * q)) & 7u);
+}
+
+// The reference's "tiny" leaf rule (octree.cpp:43).
+__device__ __forceinline__ bool tiny_node(double h, double cx, double cy, double cz) {
+  return h < 1e-12 * (fabs(cx) + fabs(cy) + fabs(cz) + 1e-300);
+}
+
+__device__ __forceinline__ void step_centre(double &cx, double &cy, double &cz, int o, double h) {
+  cx = cx + ((o & 1) ? h : -h);  // octree.cpp:131-132
+  cy = cy + ((o & 2) ? h : -h);
+  cz = cz + ((o & 4) ? h : -h);
+}
+
+// ------------------------------------------------------------ bounding box
+
+__global__ void __launch_bounds__(kT) k_bbox_partial(const double *pos, u64 n, double *part) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (u64 i = blockIdx.x * static_cast<u64>(kT) + threadIdx.x; i < n;
+       i += static_cast<u64>(gridDim.x) * kT) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double v = pos[3 * i + a];
+      lo[a] = fmin(lo[a], v);
+      hi[a] = fmax(hi[a], v);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = fmin(lo[a], __shfl_xor_sync(kFullMask, lo[a], o));
+      hi[a] = fmax(hi[a], __shfl_xor_sync(kFullMask, hi[a], o));
+    }
+  __shared__ double s[kT / 32][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int a = 0; a < 3; ++a) {
+      s[warp][a] = lo[a];
+      s[warp][3 + a] = hi[a];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = s[0][threadIdx.x];
+    for (int w = 1; w < kT / 32; ++w)
+      v = threadIdx.x < 3 ? fmin(v, s[w][threadIdx.x]) : fmax(v, s[w][threadIdx.x]);
+    part[6 * blockIdx.x + threadIdx.x] = v;
+  }
+}
+
+// Root cube from the reduced box (octree.cpp:184-198), one thread.
+__global__ void k_root(const double *part, int nparts, TreeRoot *root) {
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = part[a];
+    hi[a] = part[3 + a];
+  }
+  for (int p = 1; p < nparts; ++p)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = fmin(lo[a], part[6 * p + a]);
+      hi[a] = fmax(hi[a], part[6 * p + 3 + a]);
+    }
+  double half = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    root->lo[a] = lo[a];
+    root->hi[a] = hi[a];
+    root->center[a] = (lo[a] + hi[a]) * 0.5;
+    const double e = 0.5 * (hi[a] - lo[a]);
+    half = half < e ? e : half;
+  }
+  half = half * (1.0 + 1e-9) + 1e-300;
+  root->half_at[0] = half;
+  for (int d = 0; d < kMaxDepth; ++d) root->half_at[d + 1] = 0.5 * root->half_at[d];
+}
+
+// ------------------------------------------------------------------- keys
+
+// First key word: levels 1..21 from the root; records the first depth whose
+// node is "tiny" (a leaf whatever its count). Digits below a tiny node are 0,
+// so bodies of such a leaf stay in input order through the sort.
+__global__ void __launch_bounds__(kT)
+    k_keys(const double *pos, u32 n, const TreeRoot *root, u64 *key, u32 *idx, u8 *tiny) {
+  __shared__ double half_at[kLevelsPerWord + 1];
+  __shared__ double c0[3];
+  if (threadIdx.x <= kLevelsPerWord) half_at[threadIdx.x] = root->half_at[threadIdx.x];
+  if (threadIdx.x < 3) c0[threadIdx.x] = root->center[threadIdx.x];
+  __syncthreads();
+  const u32 i = blockIdx.x * kT + threadIdx.x;
+  if (i >= n) return;
+  const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
+  double cx = c0[0], cy = c0[1], cz = c0[2];
+  u64 k = 0;
+  int t = kNoTiny;
+  for (int d = 0; d < kLevelsPerWord; ++d) {
+    if (t == kNoTiny && tiny_node(half_at[d], cx, cy, cz)) t = d;
+    int o = (x >= cx ? 1 : 0) | (y >= cy ? 2 : 0) | (z >= cz ? 4 : 0);
+    if (t != kNoTiny) o = 0;
+    k = (k << 3) | static_cast<u64>(o);
+    step_centre(cx, cy, cz, o, half_at[d + 1]);
+  }
+  if (t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz)) t = kLevelsPerWord;
+  key[i] = k;
+  idx[i] = i;
+  tiny[i] = static_cast<u8>(t);
+}
+
+// Per sorted position: levels shared with the next body, and the leaf depth.
+__global__ void __launch_bounds__(kT)
+    k_levels(KeyView kv, const u32 *idx, const u8 *tiny, u32 n, int L, signed char *lcp_next,
+             u8 *leafdepth, Scalars *sc) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b >= n) return;
+  lcp_next[b] = static_cast<signed char>(b + 1 < n ? lcp(kv, b, b + 1) : -1);
+  int w = -1;
+  if (n > static_cast<u32>(L)) {
+    const u32 lo = b >= static_cast<u32>(L) ? b - L : 0;
+    const u32 hi = min(b, n - 1 - L);
+    for (u32 i = lo; i <= hi; ++i) w = max(w, lcp(kv, i, i + L));
+  }
+  int ld = min(w + 1, kMaxDepth);
+  ld = min(ld, static_cast<int>(tiny[idx[b]]));
+  leafdepth[b] = static_cast<u8>(ld);
+  if (ld > kLevelsPerWord * kv.words) atomicAdd(&sc->deep, 1u);
+  atomicMax(&sc->depth, static_cast<u32>(ld));
+}
+
+// ------------------------------------------------------- deeper key words
+
+__global__ void __launch_bounds__(kT)
+    k_deep_flags(const u8 *leafdepth, u32 n, int limit, u32 *flag) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b < n) flag[b] = leafdepth[b] > limit ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_compact(const u32 *flag, const u32 *scan, u32 n, u32 *out) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b < n && flag[b]) out[scan[b]] = b;
+}
+
+// Next key word for the deep bodies: replay the path to depth 21*words from
+// the root with the existing digits, then record up to 21 more levels.
+__global__ void __launch_bounds__(kT)
+    k_deep_keys(KeyView kv, const u32 *dpos, u32 nd, const u32 *idx, const double *pos,
+                const TreeRoot *root, u8 *tiny, u64 *word, u32 *rec, u32 *didx) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= nd) return;
+  const u32 b = dpos[k];
+  const u32 i = idx[b];
+  const int base = kLevelsPerWord * kv.words;
+  double cx = root->center[0], cy = root->center[1], cz = root->center[2];
+  for (int lvl = 1; lvl <= base; ++lvl) step_centre(cx, cy, cz, digit(kv, b, lvl), root->half_at[lvl]);
+  const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
+  const int levels = min(kLevelsPerWord, kMaxDepth - base);
+  int t = tiny[i];
+  u64 w = 0;
+  for (int q = 0; q < levels; ++q) {
+    const int d = base + q;  // depth of the node being split
+    if (q > 0 && t == kNoTiny && tiny_node(root->half_at[d], cx, cy, cz)) t = d;
+    int o = (x >= cx ? 1 : 0) | (y >= cy ? 2 : 0) | (z >= cz ? 4 : 0);
+    if (t != kNoTiny) o = 0;
+    w = (w << 3) | static_cast<u64>(o);
+    step_centre(cx, cy, cz, o, root->half_at[d + 1]);
+  }
+  if (t == kNoTiny && tiny_node(root->half_at[base + levels], cx, cy, cz)) t = base + levels;
+  w <<= 3 * (kLevelsPerWord - levels);
+  tiny[i] = static_cast<u8>(t);
+  word[k] = w;
+  rec[k] = k;
+  didx[k] = i;
+}
+
+// Segment of each deep record: a new segment starts where the existing key
+// words change (a different depth-21*words node).
+__global__ void __launch_bounds__(kT)
+    k_deep_segments(KeyView kv, const u32 *dpos, u32 nd, u32 *flag) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= nd) return;
+  bool start = k == 0;
+  if (!start) {
+    const u32 a = dpos[k - 1], b = dpos[k];
+    start = kv.w0[a] != kv.w0[b] || (kv.words > 1 && kv.w1[a] != kv.w1[b]);
+  }
+  flag[k] = start ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_seg_keys(const u32 *rec, const u32 *seg_scan, const u32 *seg_flag, u32 nd, u64 *key) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= nd) return;
+  const u32 r = rec[k];
+  key[k] = seg_scan[r] + seg_flag[r];  // 1-based segment number
+}
+
+// Puts the deep records back into their positions, now ordered by (segment,
+// new word, input order).
+__global__ void __launch_bounds__(kT)
+    k_deep_scatter(const u32 *dpos, const u32 *rec, const u32 *didx, const u64 *word, u32 nd,
+                   u32 *idx, u64 *word_out) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= nd) return;
+  const u32 r = rec[k];
+  idx[dpos[k]] = didx[r];
+  word_out[dpos[k]] = word[r];
+}
+
+// ------------------------------------------------------------------ nodes
+
+__global__ void __launch_bounds__(kT)
+    k_node_count(const signed char *lcp_next, const u8 *leafdepth, u32 n, u32 *count) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b < n) count[b] = static_cast<u32>(max(0, static_cast<int>(leafdepth[b]) - lcp_next[b]));
+}
+
+// Writes the nodes ending at sorted position b, shallowest first.
+__global__ void __launch_bounds__(kT)
+    k_nodes(KeyView kv, const signed char *lcp_next, const u8 *leafdepth, const u32 *count,
+            const u32 *count_scan, u32 n, const Scalars *sc, const TreeRoot *root, double2 *geom,
+            u32 *nbegin, u32 *nend, u32 *skip, u8 *depth, u8 *isleaf) {
+  const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (b >= n) return;
+  const u32 c = count[b];
+  if (c == 0) return;
+  const u32 total = sc->n_nodes;
+  const u32 first = total - count_scan[b] - c;  // nodes ending after b come first
+  const int d0 = lcp_next[b] + 1, ld = leafdepth[b];
+  double cx = root->center[0], cy = root->center[1], cz = root->center[2];
+  for (int d = 0; d <= ld; ++d) {
+    if (d > 0) step_centre(cx, cy, cz, digit(kv, b, d), root->half_at[d]);
+    if (d < d0) continue;
+    const u32 p = first + static_cast<u32>(d - d0);
+    // first body of the node: smallest b0 sharing d levels with b
+    u32 lo = 0, hi = b;
+    if (d > 0)
+      while (lo < hi) {
+        const u32 mid = lo + (hi - lo) / 2;
+        if (lcp(kv, mid, b) >= d) hi = mid;
+        else lo = mid + 1;
+      }
+    geom[2 * p] = make_double2(cx, cy);
+    geom[2 * p + 1] = make_double2(cz, root->half_at[d]);
+    nbegin[p] = lo;
+    nend[p] = b + 1;
+    skip[p] = total - count_scan[lo];
+    depth[p] = static_cast<u8>(d);
+    isleaf[p] = d == ld ? 1 : 0;
+  }
+}
+
+// Children of a node are p+1, skip[p+1], ... (last octant first) up to skip[p].
+__device__ __forceinline__ int children_of(u32 p, const u32 *skip, u32 ch[8]) {
+  int k = 0;
+  for (u32 c = p + 1; c < skip[p] && k < 8; c = skip[c]) ch[k++] = c;
+  return k;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_children(const u32 *skip, const u8 *isleaf, u32 m, u32 *parent, u8 *nchild) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  if (p == 0) parent[0] = 0xffffffffu;
+  if (isleaf[p]) {
+    nchild[p] = 0;
+    return;
+  }
+  u32 ch[8];
+  const int k = children_of(p, skip, ch);
+  nchild[p] = static_cast<u8>(k);
+  for (int j = 0; j < k; ++j) parent[ch[j]] = p;
+}
+
+// Input order inside each leaf (the reference never splits a leaf's range).
+__global__ void __launch_bounds__(kT)
+    k_leaf_order(const u8 *isleaf, const u32 *nbegin, const u32 *nend, u32 m, u32 *idx) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m || !isleaf[p]) return;
+  const u32 b0 = nbegin[p], b1 = nend[p];
+  for (u32 i = b0 + 1; i < b1; ++i) {
+    const u32 v = idx[i];
+    u32 j = i;
+    while (j > b0 && idx[j - 1] > v) {
+      idx[j] = idx[j - 1];
+      --j;
+    }
+    idx[j] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_tree_order(const double *pos, const double *mass, const u32 *idx, u32 n, double *tpos,
+                 double *tmass) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= n) return;
+  const u64 i = idx[k];
+  tpos[3ull * k] = pos[3 * i];
+  tpos[3ull * k + 1] = pos[3 * i + 1];
+  tpos[3ull * k + 2] = pos[3 * i + 2];
+  tmass[k] = mass[i];
+}
+
+// ---------------------------------------------------------------- moments
+
+struct MomentArrays {
+  const double2 *geom;   // 2 per node: (cx, cy), (cz, half)
+  const u32 *nbegin, *nend, *skip, *parent;
+  const u8 *nchild;
+  const double *tpos, *tmass;
+  double2 *mom;     // 2 per node: (mx, my), (mz, mass)
+  double2 *quad;    // 3 x double2 per node: xx yy | zz xy | xz yz
+  double *delta;
+  u32 *arrive;
+  u32 *error;
+};
+
+__device__ __forceinline__ Dbl4 load_pair(const double2 *a, u32 p) {
+  const double2 u = a[2 * p], v = a[2 * p + 1];
+  return make_dbl4(u.x, u.y, v.x, v.y);
+}
+
+// Uncached (L2) read of a child's moments written by another thread.
+__device__ __forceinline__ Dbl4 load_pair_cg(const double2 *a, u32 p) {
+  const double2 u = __ldcg(&a[2 * p]), v = __ldcg(&a[2 * p + 1]);
+  return make_dbl4(u.x, u.y, v.x, v.y);
+}
+
+__device__ __forceinline__ void store_pair(double2 *a, u32 p, double x, double y, double z,
+                                           double w) {
+  a[2 * p] = make_double2(x, y);
+  a[2 * p + 1] = make_double2(z, w);
+}
+
+__device__ void leaf_moments(const MomentArrays &a, u32 p) {  // octree.cpp:46-72
+  const Dbl4 g = load_pair(a.geom, p);
+  const u32 b0 = a.nbegin[p], b1 = a.nend[p];
+  double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+  for (u32 k = b0; k < b1; ++k) {
+    const double mi = a.tmass[k];
+    m += mi;
+    cx += mi * a.tpos[3ull * k];
+    cy += mi * a.tpos[3ull * k + 1];
+    cz += mi * a.tpos[3ull * k + 2];
+  }
+  if (m > 0) {
+    cx = cx / m;
+    cy = cy / m;
+    cz = cz / m;
+  } else {
+    cx = g.x;
+    cy = g.y;
+    cz = g.z;
+  }
+  double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
+  for (u32 k = b0; k < b1; ++k) {
+    const double mi = a.tmass[k];
+    const double dx = a.tpos[3ull * k] - cx, dy = a.tpos[3ull * k + 1] - cy,
+                 dz = a.tpos[3ull * k + 2] - cz;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    q0 += mi * (3 * dx * dx - r2);
+    q1 += mi * (3 * dy * dy - r2);
+    q2 += mi * (3 * dz * dz - r2);
+    q3 += mi * 3 * dx * dy;
+    q4 += mi * 3 * dx * dz;
+    q5 += mi * 3 * dy * dz;
+  }
+  store_pair(a.mom, p, cx, cy, cz, m);
+  a.quad[3 * p] = make_double2(q0, q1);
+  a.quad[3 * p + 1] = make_double2(q2, q3);
+  a.quad[3 * p + 2] = make_double2(q4, q5);
+  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
+  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+__device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-102
+  const Dbl4 g = load_pair(a.geom, p);
+  u32 ch[8];
+  const int nc = children_of(p, a.skip, ch);  // last octant first
+  double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+  for (int j = nc - 1; j >= 0; --j) {
+    const Dbl4 c = load_pair_cg(a.mom, ch[j]);
+    m += c.w;
+    cx += c.w * c.x;
+    cy += c.w * c.y;
+    cz += c.w * c.z;
+  }
+  if (m > 0) {
+    cx = cx / m;
+    cy = cy / m;
+    cz = cz / m;
+  } else {
+    cx = g.x;
+    cy = g.y;
+    cz = g.z;
+  }
+  double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
+  for (int j = nc - 1; j >= 0; --j) {
+    const Dbl4 c = load_pair_cg(a.mom, ch[j]);
+    const double2 qa = __ldcg(&a.quad[3 * ch[j]]), qb = __ldcg(&a.quad[3 * ch[j] + 1]),
+                  qc = __ldcg(&a.quad[3 * ch[j] + 2]);
+    const double dx = c.x - cx, dy = c.y - cy, dz = c.z - cz;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    q0 += qa.x + c.w * (3 * dx * dx - r2);
+    q1 += qa.y + c.w * (3 * dy * dy - r2);
+    q2 += qb.x + c.w * (3 * dz * dz - r2);
+    q3 += qb.y + c.w * 3 * dx * dy;
+    q4 += qc.x + c.w * 3 * dx * dz;
+    q5 += qc.y + c.w * 3 * dy * dz;
+  }
+  store_pair(a.mom, p, cx, cy, cz, m);
+  a.quad[3 * p] = make_double2(q0, q1);
+  a.quad[3 * p + 1] = make_double2(q2, q3);
+  a.quad[3 * p + 2] = make_double2(q4, q5);
+  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
+  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+// One thread per leaf; the last child to finish carries on with its parent.
+__global__ void __launch_bounds__(kT) k_moments(MomentArrays a, const u8 *isleaf, u32 m) {
+  const u32 p0 = blockIdx.x * kT + threadIdx.x;
+  if (p0 >= m || !isleaf[p0]) return;
+  leaf_moments(a, p0);
+  u32 p = p0;
+  for (int level = 0; p != 0; ++level) {
+    const u32 up = a.parent[p];
+    if (up >= m || level > kMaxDepth) {  // malformed tree: record and stop
+      atomicOr(a.error, 2u);
+      return;
+    }
+    __threadfence();
+    const u32 before = atomicAdd(&a.arrive[up], 1u);
+    if (before + 1 != a.nchild[up]) return;
+    __threadfence();
+    node_moments(a, up);
+    p = up;
+  }
+}
+
+// --------------------------------------------------------------- packing
+
+// FP64 walk record and FP32 cell of every node (group_lists.cpp:52-61).
+__global__ void __launch_bounds__(kT)
+    k_pack_nodes(const double2 *geom, const double2 *mom, const double2 *quad,
+                 const double *delta, const u32 *nbegin, const u32 *nend, const u32 *skip,
+                 const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta, WalkRec *walk,
+                 float4 *cells) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  const Dbl4 g = load_pair(geom, p), c = load_pair(mom, p);
+  const double crit = 2.0 * g.w * inv_theta + delta[p];
+  WalkRec r;
+  r.cx = g.x;
+  r.cy = g.y;
+  r.cz = g.z;
+  r.slack = g.w * 1.0001;
+  r.mx = c.x;
+  r.my = c.y;
+  r.mz = c.z;
+  r.crit2 = crit * crit;
+  r.skip = skip[p];
+  r.nbody = nend[p] - nbegin[p];
+  r.begin = nbegin[p];
+  r.leaf = isleaf[p];
+  walk[p] = r;
+  const double ox = root->center[0], oy = root->center[1], oz = root->center[2];
+  const double2 qa = quad[3 * p], qb = quad[3 * p + 1], qc = quad[3 * p + 2];
+  cells[3 * p] = make_float4(static_cast<float>(c.x - ox), static_cast<float>(c.y - oy),
+                             static_cast<float>(c.z - oz), static_cast<float>(c.w));
+  cells[3 * p + 1] = make_float4(static_cast<float>(qa.x), static_cast<float>(qa.y),
+                                 static_cast<float>(qb.x), static_cast<float>(qb.y));
+  cells[3 * p + 2] = make_float4(static_cast<float>(qc.x), static_cast<float>(qc.y), 0.0f, 0.0f);
+}
+
+// FP32 bodies relative to `origin` (group_lists.cpp:46-50, gravity_backends.cpp:15-23).
+__global__ void __launch_bounds__(kT)
+    k_pack_bodies(const double *tpos, const double *tmass, u32 n, const double *origin,
+                  float4 *bodies) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= n) return;
+  bodies[k] = make_float4(static_cast<float>(tpos[3ull * k] - origin[0]),
+                          static_cast<float>(tpos[3ull * k + 1] - origin[1]),
+                          static_cast<float>(tpos[3ull * k + 2] - origin[2]),
+                          static_cast<float>(tmass[k]));
+}
+
+const double *root_centre(const TreeRoot *root) {
+  return reinterpret_cast<const double *>(reinterpret_cast<const char *>(root) +
+                                          offsetof(TreeRoot, center));
+}
+
+void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
+  GTC_CUDA(cudaMemcpyAsync(host, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+void bbox_root(Workspace &ws, const double *pos, u64 n, cudaStream_t s) {
+  const u32 nparts = std::min<u32>(1024, std::max<u32>(1, ceil_div(n, kT)));
+  ws.bbox_part.ensure(6 * sizeof(double) * nparts);
+  ws.root.ensure(sizeof(TreeRoot));
+  k_bbox_partial<<<nparts, kT, 0, s>>>(pos, n, ws.bbox_part.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_root<<<1, 1, 0, s>>>(ws.bbox_part.as<double>(), static_cast<int>(nparts), ws.root.as<TreeRoot>());
+  GTC_LAUNCH_CHECK();
+}
+
+void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 n,
+                      cudaStream_t s) {
+  bbox_root(ws, pos, n, s);
+  ws.bodies.ensure(n * sizeof(float4));
+  const TreeRoot *root = ws.root.as<TreeRoot>();
+  k_pack_bodies<<<ceil_div(n, kT), kT, 0, s>>>(pos, mass, static_cast<u32>(n),
+                                               root_centre(root), ws.bodies.as<float4>());
+  GTC_LAUNCH_CHECK();
+}
+
+void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
+                const SolverParams &sp, cudaStream_t s, Scalars *host) {
+  ws.n = n;
+  ws.n_nodes = 0;
+  ws.key_words = 1;
+  if (n == 0) return;
+  const u32 n32 = static_cast<u32>(n);
+  const u32 nb = ceil_div(n, kT);
+  const int L = std::max(1, sp.leaf_size);
+
+  ws.key0.ensure(n * 8);
+  ws.key0_alt.ensure(n * 8);
+  ws.idx.ensure(n * 4);
+  ws.idx_alt.ensure(n * 4);
+  ws.tiny.ensure(n);
+  ws.lcp.ensure(n);
+  ws.leafdepth.ensure(n);
+  ws.count.ensure(n * 4);
+  ws.count_scan.ensure(n * 4);
+  ws.tpos.ensure(n * 24);
+  ws.tmass.ensure(n * 8);
+  ws.bodies.ensure(n * sizeof(float4));
+  ws.scalars.ensure(sizeof(Scalars));
+  Scalars *sc = ws.scalars.as<Scalars>();
+  GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
+
+  bbox_root(ws, pos, n, s);
+  const TreeRoot *root = ws.root.as<TreeRoot>();
+  u64 *key0 = ws.key0.as<u64>();
+  u32 *idx = ws.idx.as<u32>();
+  u8 *tiny = ws.tiny.as<u8>();
+  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny);
+  GTC_LAUNCH_CHECK();
+  radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
+
+  KeyView kv{key0, nullptr, nullptr, 1};
+  signed char *lcp_next = ws.lcp.as<signed char>();
+  u8 *leafdepth = ws.leafdepth.as<u8>();
+  k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
+  GTC_LAUNCH_CHECK();
+  read_scalars(ws, host, s);
+
+  // Deeper key words for bodies whose leaves lie below the words so far.
+  while (host->deep > 0 && kv.words < 3) {
+    const int limit = kLevelsPerWord * kv.words;
+    DeviceBuffer &wbuf = kv.words == 1 ? ws.key1 : ws.key2;
+    wbuf.ensure(n * 8);
+    GTC_CUDA(cudaMemsetAsync(wbuf.ptr, 0, n * 8, s));
+    ws.flags.ensure(n * 4);
+    ws.flags_scan.ensure(n * 4);
+    u32 *flag = ws.flags.as<u32>(), *fscan = ws.flags_scan.as<u32>();
+    k_deep_flags<<<nb, kT, 0, s>>>(leafdepth, n32, limit, flag);
+    GTC_LAUNCH_CHECK();
+    exclusive_scan_u32(flag, fscan, n, &sc->deep, ws.scan_tmp, s);
+    read_scalars(ws, host, s);
+    const u32 nd = host->deep;
+    ws.dpos.ensure(nd * 4ull);
+    ws.dkey.ensure(nd * 8ull);
+    ws.dkey_alt.ensure(nd * 8ull);
+    ws.drec.ensure(nd * 4ull);
+    ws.drec_alt.ensure(nd * 4ull);
+    const u64 idx_bytes = (nd * 4ull + 15) & ~15ull;
+    ws.dtmp.ensure(idx_bytes + nd * 8ull);
+    u32 *dpos = ws.dpos.as<u32>(), *drec = ws.drec.as<u32>();
+    u32 *didx = ws.dtmp.as<u32>();
+    u64 *dword = reinterpret_cast<u64 *>(ws.dtmp.as<char>() + idx_bytes);
+    const u32 ndb = ceil_div(nd, kT);
+    k_compact<<<nb, kT, 0, s>>>(flag, fscan, n32, dpos);
+    GTC_LAUNCH_CHECK();
+    k_deep_keys<<<ndb, kT, 0, s>>>(kv, dpos, nd, idx, pos, root, tiny, dword, drec, didx);
+    GTC_LAUNCH_CHECK();
+    // order records by (segment, new word, input order): sort by the word,
+    // then stably by segment number
+    u64 *dkey = ws.dkey.as<u64>();
+    GTC_CUDA(cudaMemcpyAsync(dkey, dword, nd * 8ull, cudaMemcpyDeviceToDevice, s));
+    radix_sort_pairs(dkey, drec, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), nd, 63, ws.radix, s);
+    u32 *sflag = ws.flags.as<u32>(), *sscan = ws.flags_scan.as<u32>();
+    k_deep_segments<<<ndb, kT, 0, s>>>(kv, dpos, nd, sflag);
+    GTC_LAUNCH_CHECK();
+    exclusive_scan_u32(sflag, sscan, nd, &sc->aux, ws.scan_tmp, s);
+    read_scalars(ws, host, s);
+    int seg_bits = 1;
+    while (seg_bits < 32 && (1ull << seg_bits) <= host->aux) ++seg_bits;
+    k_seg_keys<<<ndb, kT, 0, s>>>(drec, sscan, sflag, nd, dkey);
+    GTC_LAUNCH_CHECK();
+    radix_sort_pairs(dkey, drec, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), nd, seg_bits,
+                     ws.radix, s);
+    k_deep_scatter<<<ndb, kT, 0, s>>>(dpos, drec, didx, dword, nd, idx, wbuf.as<u64>());
+    GTC_LAUNCH_CHECK();
+    if (kv.words == 1) kv.w1 = ws.key1.as<u64>();
+    else kv.w2 = ws.key2.as<u64>();
+    kv.words += 1;
+    GTC_CUDA(cudaMemsetAsync(&sc->deep, 0, sizeof(u32), s));
+    k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
+    GTC_LAUNCH_CHECK();
+    read_scalars(ws, host, s);
+  }
+  if (host->deep > 0) throw RuntimeError("octree deeper than the depth cap");
+  ws.key_words = kv.words;
+
+  // Node numbering: count the nodes ending at each sorted position.
+  u32 *count = ws.count.as<u32>(), *cscan = ws.count_scan.as<u32>();
+  k_node_count<<<nb, kT, 0, s>>>(lcp_next, leafdepth, n32, count);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u32(count, cscan, n, &sc->n_nodes, ws.scan_tmp, s);
+  read_scalars(ws, host, s);
+  const u32 m = host->n_nodes;
+  ws.n_nodes = m;
+  ws.geom.ensure(m * 2 * sizeof(double2));
+  ws.mom.ensure(m * 2 * sizeof(double2));
+  ws.quad.ensure(m * 3 * sizeof(double2));
+  ws.delta.ensure(m * 8ull);
+  ws.nbegin.ensure(m * 4ull);
+  ws.nend.ensure(m * 4ull);
+  ws.skip.ensure(m * 4ull);
+  ws.parent.ensure(m * 4ull);
+  ws.depth.ensure(m);
+  ws.nchild.ensure(m);
+  ws.isleaf.ensure(m);
+  ws.arrive.ensure(m * 4ull);
+  ws.walk.ensure(m * sizeof(WalkRec));
+  ws.cells.ensure(m * 3 * sizeof(float4));
+  const u32 mb = ceil_div(m, kT);
+
+  k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
+                            ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>());
+  GTC_LAUNCH_CHECK();
+  k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, ws.parent.as<u32>(),
+                               ws.nchild.as<u8>());
+  GTC_LAUNCH_CHECK();
+  k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), m, idx);
+  GTC_LAUNCH_CHECK();
+  k_tree_order<<<nb, kT, 0, s>>>(pos, mass, idx, n32, ws.tpos.as<double>(), ws.tmass.as<double>());
+  GTC_LAUNCH_CHECK();
+
+  GTC_CUDA(cudaMemsetAsync(ws.arrive.ptr, 0, m * 4ull, s));
+  MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                  ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
+                  ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
+                  ws.quad.as<double2>(), ws.delta.as<double>(), ws.arrive.as<u32>(), &sc->error};
+  k_moments<<<mb, kT, 0, s>>>(ma, ws.isleaf.as<u8>(), m);
+  GTC_LAUNCH_CHECK();
+  k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
+                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
+                                 1.0 / sp.theta, ws.walk.as<WalkRec>(), ws.cells.as<float4>());
+  GTC_LAUNCH_CHECK();
+  k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
+                                  root_centre(root), ws.bodies.as<float4>());
+  GTC_LAUNCH_CHECK();
+}
+
+}  // namespace gtc

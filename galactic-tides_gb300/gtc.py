@@ -1,0 +1,244 @@
+"""ctypes binding of the C ABI in include/gtc.h (libgtc.so, built in-tree).
+
+The Python face of the CUDA backend: the same calls a C++ caller makes
+through gtc.hpp, with numpy arrays on the host and raw device pointers for
+the ``*_device`` forms. Errors raise ``GtcInvalidArgument`` (a ValueError,
+the reference's std::invalid_argument) or ``GtcError`` (a RuntimeError, the
+reference's std::runtime_error). There is no CPU fallback: if libgtc.so is
+missing, importing this module fails.
+"""
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "libgtc.so"
+
+GTC_OK, GTC_INVALID_ARGUMENT, GTC_RUNTIME_ERROR, GTC_NO_DEVICE, GTC_OUT_OF_MEMORY = range(5)
+CRITERION_THETA, CRITERION_LEARNED = 0, 1
+
+
+class GtcError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+class GtcInvalidArgument(GtcError, ValueError):
+    pass
+
+
+class GravityParams(C.Structure):
+    _fields_ = [("G", C.c_double), ("theta", C.c_double), ("eps", C.c_double),
+                ("quadrupole", C.c_int32), ("group_size", C.c_int32), ("leaf_size", C.c_int32),
+                ("pack", C.c_int32), ("criterion", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class KernelParams(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("n_groups", C.c_uint32), ("G", C.c_float),
+                ("eps2", C.c_float), ("quadrupole", C.c_uint32), ("pad", C.c_uint32 * 3)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("tree_ms", C.c_double), ("lists_ms", C.c_double), ("evaluate_ms", C.c_double),
+                ("total_ms", C.c_double), ("cell_interactions", C.c_uint64),
+                ("body_interactions", C.c_uint64), ("max_list", C.c_uint64),
+                ("n_cell_list", C.c_uint64), ("n_body_list", C.c_uint64),
+                ("n_nodes", C.c_uint32), ("n_groups", C.c_uint32), ("max_group", C.c_uint32),
+                ("depth", C.c_uint32)]
+
+
+NODE_DTYPE = np.dtype([
+    ("center", "<f8", 3), ("half", "<f8"), ("com", "<f8", 3), ("mass", "<f8"),
+    ("quad", "<f8", 6), ("delta", "<f8"), ("begin", "<u4"), ("end", "<u4"), ("skip", "<u4"),
+    ("parent", "<u4"), ("depth", "<i4"), ("n_children", "<i4")])
+assert NODE_DTYPE.itemsize == 144
+
+assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 88
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built: run __graft_entry__.build() (make -C "
+                          "galactic-tides_gb300)")
+    lib = C.CDLL(str(LIB_PATH))
+    V, I, U32, U64, D = C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_double
+    P = C.c_void_p
+    sig = {
+        "gtc_create": (I, [C.POINTER(V), I]),
+        "gtc_destroy": (None, [V]),
+        "gtc_last_error": (C.c_char_p, [V]),
+        "gtc_status_name": (C.c_char_p, [I]),
+        "gtc_stream": (V, [V]),
+        "gtc_direct": (I, [V, P, C.POINTER(KernelParams), P]),
+        "gtc_tree": (I, [V, P, P, U32, P, U64, P, U64, P, C.POINTER(KernelParams), P]),
+        "gtc_group_force": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
+        "gtc_group_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
+        "gtc_direct_force": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
+        "gtc_direct_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
+        "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
+        "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
+        "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
+        "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def gravity_params(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8,
+                   pack=True, criterion=CRITERION_THETA):
+    return GravityParams(G, theta, eps, int(quadrupole), group_size, leaf_size, int(pack),
+                         criterion, (C.c_int32 * 3)(0, 0, 0))
+
+
+class Context:
+    """One gtc_context: a device, a CUDA stream, and buffers reused between calls."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        rc = lib.gtc_create(C.byref(h), device)
+        if rc != GTC_OK:
+            raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(
+                rc, lib.gtc_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib.gtc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != GTC_OK:
+            msg = lib.gtc_last_error(self.h).decode()
+            raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(rc, msg)
+
+    @property
+    def stream(self):
+        """The context's cudaStream_t as an integer handle."""
+        return lib.gtc_stream(self.h)
+
+    # ---- reference-facing calls with host arrays -----------------------------
+
+    def group_force(self, pos, mass, **kw):
+        """GroupTreeGravity(Device::CUDA).compute: host arrays in, (acc, pot) out."""
+        pos = _f64(pos, (-1, 3))
+        mass = _f64(mass)
+        n = mass.shape[0]
+        acc = np.empty((n, 3))
+        pot = np.empty(n)
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_group_force(self.h, _ptr(pos), _ptr(mass), n, C.byref(gp),
+                                        _ptr(acc), _ptr(pot)))
+        return acc, pot
+
+    def direct_force(self, pos, mass, **kw):
+        """DirectGravity(Device::CUDA).compute: FP32 direct sum, host arrays."""
+        pos = _f64(pos, (-1, 3))
+        mass = _f64(mass)
+        n = mass.shape[0]
+        acc = np.empty((n, 3))
+        pot = np.empty(n)
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_direct_force(self.h, _ptr(pos), _ptr(mass), n, C.byref(gp),
+                                         _ptr(acc), _ptr(pot)))
+        return acc, pot
+
+    def direct(self, bodies, G=1.0, eps2=0.0):
+        """metal::Context::direct: float4 bodies -> float4 (ax, ay, az, pot)."""
+        bodies = np.ascontiguousarray(bodies, dtype=np.float32).reshape(-1, 4)
+        n = bodies.shape[0]
+        out = np.empty((n, 4), np.float32)
+        kp = KernelParams(n, 0, G, eps2, 0, (C.c_uint32 * 3)())
+        self._check(lib.gtc_direct(self.h, _ptr(bodies), C.byref(kp), _ptr(out)))
+        return out
+
+    def tree(self, bodies, cells, cell_list, body_list, groups, G=1.0, eps2=0.0,
+             quadrupole=True, n_groups=None):
+        """metal::Context::tree: evaluate given grouped lists -> float4 per body (tree order)."""
+        bodies = np.ascontiguousarray(bodies, dtype=np.float32).reshape(-1, 4)
+        cells = np.ascontiguousarray(cells, dtype=np.float32).reshape(-1, 12)
+        cl = np.ascontiguousarray(cell_list, dtype=np.uint32)
+        bl = np.ascontiguousarray(body_list, dtype=np.uint32)
+        groups = np.ascontiguousarray(groups, dtype=np.uint32).reshape(-1, 8)
+        n = bodies.shape[0]
+        ng = groups.shape[0] if n_groups is None else n_groups
+        out = np.empty((n, 4), np.float32)
+        kp = KernelParams(n, ng, G, eps2, int(quadrupole), (C.c_uint32 * 3)())
+        self._check(lib.gtc_tree(self.h, _ptr(bodies), _ptr(cells), cells.shape[0], _ptr(cl),
+                                 cl.shape[0], _ptr(bl), bl.shape[0], _ptr(groups), C.byref(kp),
+                                 _ptr(out)))
+        return out
+
+    # ---- device-pointer forms ------------------------------------------------
+
+    def group_force_device(self, pos_ptr, mass_ptr, n, acc_ptr, pot_ptr, **kw):
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_group_force_device(self.h, pos_ptr, mass_ptr, n, C.byref(gp),
+                                               acc_ptr, pot_ptr))
+
+    def direct_force_device(self, pos_ptr, mass_ptr, n, acc_ptr, pot_ptr, **kw):
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_direct_force_device(self.h, pos_ptr, mass_ptr, n, C.byref(gp),
+                                                acc_ptr, pot_ptr))
+
+    def direct_fp64_device(self, pos_ptr, mass_ptr, n, idx_ptr, m, acc_ptr, pot_ptr, G=1.0,
+                           eps=0.025):
+        self._check(lib.gtc_direct_fp64_device(self.h, pos_ptr, mass_ptr, n, idx_ptr, m, G, eps,
+                                               acc_ptr, pot_ptr))
+
+    # ---- introspection -----------------------------------------------------
+
+    def stats(self):
+        st = Stats()
+        self._check(lib.gtc_get_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def export(self):
+        """Tree, groups and lists of the last group_force, as numpy arrays."""
+        sz = [C.c_uint64() for _ in range(5)]
+        self._check(lib.gtc_group_sizes(self.h, *[C.byref(x) for x in sz]))
+        n, m, ng, ncl, nbl = (x.value for x in sz)
+        nodes = np.zeros(m, NODE_DTYPE)
+        order = np.zeros(n, np.uint64)
+        bodies = np.zeros((n, 4), np.float32)
+        cells = np.zeros((m, 12), np.float32)
+        groups = np.zeros((ng, 8), np.uint32)
+        cl = np.zeros(ncl, np.uint32)
+        bl = np.zeros(nbl, np.uint32)
+        out = np.zeros((n, 4), np.float32)
+        self._check(lib.gtc_group_export(self.h, _ptr(nodes), _ptr(order), _ptr(bodies),
+                                         _ptr(cells), _ptr(groups), _ptr(cl), _ptr(bl),
+                                         _ptr(out)))
+        return dict(nodes=nodes, order=order, bodies=bodies, cells=cells, groups=groups,
+                    cell_list=cl, body_list=bl, out=out)

@@ -1,0 +1,213 @@
+/*
+ * gtc.h -- C ABI of the GB300 gravity backend (libgtc.so).
+ *
+ * This is the drop-in boundary for `device = cuda` behind the reference's
+ * gravity/device selection (src/gravity_backends.cpp:139-173). It replaces
+ * the Metal context (include/galactic_tides/metal_backend.h:25-54) for the
+ * two kernels, and additionally runs the whole grouped solver -- tree build,
+ * grouped walk and list evaluation, which the reference does on the host
+ * (src/octree.cpp:169-273, src/group_lists.cpp:18-207) -- on the device.
+ *
+ * Plain C: pointers, sizes and POD structs. Structs that the reference's
+ * kernels read have the reference's byte layout (the sizes are the ones
+ * static_assert'ed at src/metal/metal_backend.mm:21-24).
+ *
+ * Errors: every call returns a gtc_status; gtc_last_error() gives the message.
+ * The C++ wrapper (galactic-tides_gb300/host/gtc.hpp) turns
+ * GTC_INVALID_ARGUMENT into std::invalid_argument and every other failure
+ * into std::runtime_error, the exception types the reference uses for the
+ * same conditions (gravity_backends.cpp:93-96, metal_backend.mm:206,218-223,
+ * 260, group_lists.cpp:25-26,182-183, metal_stub.cpp:15-19).
+ *
+ * Threading: a context is used from one host thread at a time and owns one
+ * CUDA stream and the device buffers it reuses between calls (so calls after
+ * the first allocate nothing unless the problem grows), as the reference's
+ * Metal context reuses its bindings (metal_backend.mm:58-104).
+ */
+#ifndef GTC_H
+#define GTC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#define GTC_ALIGN16 alignas(16)
+#else
+#define GTC_ALIGN16 _Alignas(16)
+#endif
+
+typedef enum gtc_status {
+  GTC_OK = 0,
+  GTC_INVALID_ARGUMENT = 1, /* bad sizes or parameters: std::invalid_argument */
+  GTC_RUNTIME_ERROR = 2,    /* device failure, 32-bit overflow: std::runtime_error */
+  GTC_NO_DEVICE = 3,        /* no usable GB300: std::runtime_error */
+  GTC_OUT_OF_MEMORY = 4     /* device allocation failed: std::runtime_error */
+} gtc_status;
+
+typedef struct gtc_context gtc_context;
+
+/* kern::float4 (gravity_kernels.h:33-35): 16 bytes, 16-byte aligned. */
+typedef struct gtc_float4 {
+  GTC_ALIGN16 float x;
+  float y, z, w;
+} gtc_float4;
+
+/* kern::GTParams (gravity_kernels.h:51-60): 32 bytes, passed by value to
+ * the kernels. n = bodies, n_groups = groups (tree kernel), eps2 = softening
+ * squared, quadrupole = 1 to include cell quadrupoles. */
+typedef struct gtc_kernel_params {
+  uint32_t n;
+  uint32_t n_groups;
+  float G;
+  float eps2;
+  uint32_t quadrupole;
+  uint32_t pad0, pad1, pad2;
+} gtc_kernel_params;
+
+/* kern::GTCell (gravity_kernels.h:87-91): centre of mass and mass, then the
+ * traceless quadrupole (xx, yy, zz, xy) and (xz, yz, 0, 0). 48 bytes. */
+typedef struct gtc_cell {
+  gtc_float4 com_mass;
+  gtc_float4 q0;
+  gtc_float4 q1;
+} gtc_cell;
+
+/* kern::GTGroup (gravity_kernels.h:96-105): targets [begin, end) in tree
+ * order, cells cell_list[cell_begin, cell_end), bodies
+ * body_list[body_begin, body_end). 32 bytes. */
+typedef struct gtc_group {
+  uint32_t begin, end;
+  uint32_t cell_begin, cell_end;
+  uint32_t body_begin, body_end;
+  uint32_t pad0, pad1;
+} gtc_group;
+
+/* Opening criteria for the grouped walk. */
+#define GTC_CRITERION_THETA 0   /* the reference's box test (group_lists.cpp:147-154) */
+#define GTC_CRITERION_LEARNED 1 /* learned error model, theta test as fallback */
+
+/* GravityParams (octree.h:13-18) plus the make_gravity keys that shape the
+ * grouped solver (gravity_backends.cpp:154-160, group_lists.h:64-65). */
+typedef struct gtc_gravity_params {
+  double G;           /* default 1 */
+  double theta;       /* opening angle */
+  double eps;         /* Plummer softening length */
+  int32_t quadrupole; /* 1: accepted cells carry quadrupoles */
+  int32_t group_size; /* 1..32 on the device (GT_SIMD_WIDTH, gravity_backends.cpp:94-96) */
+  int32_t leaf_size;  /* bucket size of the octree (default 8) */
+  int32_t pack;       /* 1: merge small sibling groups (the device default), 0: do not */
+  int32_t criterion;  /* GTC_CRITERION_* */
+  int32_t reserved[3];
+} gtc_gravity_params;
+
+/* GroupTreeGravity::Timings (gravity_backends.h:54-58) and the GroupLists
+ * counters (group_lists.h:45-49) of the last call. Times are device times
+ * from CUDA events, in milliseconds. */
+typedef struct gtc_stats {
+  double tree_ms;      /* bounding box, keys, sort, topology, moments, packing */
+  double lists_ms;     /* group choice, grouped walk, list offsets */
+  double evaluate_ms;  /* list (or direct) evaluation and scatter */
+  double total_ms;
+  uint64_t cell_interactions; /* summed over targets (group_lists.cpp:197-199) */
+  uint64_t body_interactions;
+  uint64_t max_list;          /* longest list, cells + bodies */
+  uint64_t n_cell_list, n_body_list;
+  uint32_t n_nodes, n_groups, max_group, depth;
+} gtc_stats;
+
+/* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
+ * none). Replaces metal::Context::Context (metal_backend.mm:122-160). */
+gtc_status gtc_create(gtc_context **ctx, int device);
+void gtc_destroy(gtc_context *ctx);
+/* Message of the last failed call on ctx (or of gtc_create when ctx is NULL). */
+const char *gtc_last_error(const gtc_context *ctx);
+const char *gtc_status_name(gtc_status s);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order their own work against it. */
+void *gtc_stream(gtc_context *ctx);
+
+/* out[i] = (ax, ay, az, potential) of body i against every other, FP32.
+ * Host arrays of p->n bodies. Replaces metal::Context::direct
+ * (metal_backend.h:39-41, metal_backend.mm:175-207). */
+gtc_status gtc_direct(gtc_context *ctx, const gtc_float4 *bodies, const gtc_kernel_params *p,
+                      gtc_float4 *out);
+
+/* Evaluates grouped interaction lists: out[i] for every body i in tree
+ * order, one group per warp. p->n and p->n_groups must match the arrays and
+ * no group may have more than 32 targets (GTC_INVALID_ARGUMENT otherwise).
+ * Host arrays. Replaces metal::Context::tree (metal_backend.h:43-49,
+ * metal_backend.mm:209-261). */
+gtc_status gtc_tree(gtc_context *ctx, const gtc_float4 *bodies, const gtc_cell *cells,
+                    uint32_t n_cells, const uint32_t *cell_list, uint64_t n_cell_list,
+                    const uint32_t *body_list, uint64_t n_body_list, const gtc_group *groups,
+                    const gtc_kernel_params *p, gtc_float4 *out);
+
+/* GroupTreeGravity::compute (gravity_backends.cpp:109-137) entirely on the
+ * device: octree with FP64 moments, grouped walk, FP32 list evaluation and
+ * scatter back to the caller's order. pos holds n (x, y, z) doubles -- the
+ * memory of a std::vector<Vec3> -- and mass n doubles; acc receives n
+ * (x, y, z) and pot n. Host pointers; copies are part of the call. */
+gtc_status gtc_group_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                           const gtc_gravity_params *gp, double *acc, double *pot);
+
+/* The same with device pointers, enqueued on the context's stream. */
+gtc_status gtc_group_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                  uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                  double *pot);
+
+/* DirectGravity::compute with the device (gravity_backends.cpp:53-68):
+ * bodies packed relative to the bounding-box centre, FP32 tiled kernel,
+ * results in the caller's order. Host pointers. */
+gtc_status gtc_direct_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                            const gtc_gravity_params *gp, double *acc, double *pot);
+gtc_status gtc_direct_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                   uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                   double *pot);
+
+/* FP64 direct summation for the m targets idx[0..m) against all n bodies:
+ * compute_gravity_direct (src/gravity.cpp:28-45) on a sample, as the
+ * reference bench's accuracy judge (apps/galactic_tides_bench.cpp:74-95).
+ * Device pointers; acc m x 3, pot m. */
+gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const double *mass,
+                                  uint64_t n, const uint64_t *idx, uint64_t m, double G,
+                                  double eps, double *acc, double *pot);
+
+gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
+
+/* ---- exports of the last gtc_group_force*, for parity checks ------------ */
+
+/* One node of the device octree. Nodes are numbered in the order the
+ * reference's walk visits them (depth first, children last octant first), so
+ * node `skip` is the first node after this node's subtree. The fields of
+ * Octree::Node (octree.h:52-63) are all here; children are the nodes
+ * i+1, skip[i+1], ... up to skip[i] (last octant first). */
+typedef struct gtc_node {
+  double center[3];
+  double half;
+  double com[3];
+  double mass;
+  double quad[6];
+  double delta;
+  uint32_t begin, end;
+  uint32_t skip;
+  uint32_t parent;
+  int32_t depth;
+  int32_t n_children;
+} gtc_node;
+
+/* Sizes of the last group call's tree and lists (for sizing the export). */
+gtc_status gtc_group_sizes(const gtc_context *ctx, uint64_t *n_bodies, uint64_t *n_nodes,
+                           uint64_t *n_groups, uint64_t *n_cell_list, uint64_t *n_body_list);
+/* Copies the tree (NULL to skip any array): nodes, order (tree position ->
+ * caller index), the FP32 bodies and cells the evaluator read, the groups
+ * and both lists, the tree-order evaluator output. */
+gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
+                            gtc_float4 *bodies, gtc_cell *cells, gtc_group *groups,
+                            uint32_t *cell_list, uint32_t *body_list, gtc_float4 *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GTC_H */

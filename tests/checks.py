@@ -1,0 +1,77 @@
+"""Comparisons between the device build and the oracle / reference.
+
+Node numbering differs by design (the device numbers nodes in walk order,
+the reference appends children blocks as it splits, and its parallel build
+depends on the thread count), so nodes are compared by identity: a node is
+fixed by its first body and its depth, since a node and its only child share
+a range but not a depth.
+"""
+
+import numpy as np
+
+
+def ref_depths(nodes):
+    """Depth of every node of a reference-layout tree (children after parents)."""
+    depth = np.zeros(len(nodes), np.int64)
+    fc = nodes["first_child"].astype(np.int64)
+    nc = nodes["n_children"].astype(np.int64)
+    for i in range(len(nodes)):
+        if nc[i] > 0:
+            depth[fc[i]:fc[i] + nc[i]] = depth[i] + 1
+    return depth
+
+
+def node_keys(begin, depth):
+    return (np.asarray(begin, np.int64) << 7) | np.asarray(depth, np.int64)
+
+
+def compare_trees(dev_nodes, ref_nodes):
+    """Returns a list of mismatch descriptions (empty when identical)."""
+    bad = []
+    if len(dev_nodes) != len(ref_nodes):
+        return [f"node count {len(dev_nodes)} != {len(ref_nodes)}"]
+    rd = ref_depths(ref_nodes)
+    dk = node_keys(dev_nodes["begin"], dev_nodes["depth"])
+    rk = node_keys(ref_nodes["begin"], rd)
+    di, ri = np.argsort(dk), np.argsort(rk)
+    if not np.array_equal(dk[di], rk[ri]):
+        return ["node sets differ"]
+    d, r = dev_nodes[di], ref_nodes[ri]
+    for f in ("end", "half", "center", "com", "mass", "quad", "delta"):
+        if not np.array_equal(d[f], r[f]):
+            k = np.nonzero(np.any((d[f] != r[f]).reshape(len(d), -1), axis=1))[0]
+            bad.append(f"{f}: {len(k)} nodes differ, first at begin={d['begin'][k[0]]}")
+    leaf_d = d["n_children"] == 0
+    leaf_r = r["n_children"] == 0
+    if not np.array_equal(leaf_d, leaf_r) or not np.array_equal(d["n_children"], r["n_children"]):
+        bad.append("children counts differ")
+    return bad
+
+
+def compare_lists(dev, dev_nodes, ref_lists, ref_nodes):
+    """Groups, and every group's cell and body list in order."""
+    bad = []
+    g_d, g_r = dev["groups"], ref_lists.groups
+    if g_d.shape != g_r.shape:
+        return [f"group count {len(g_d)} != {len(g_r)}"]
+    if not np.array_equal(g_d[:, :6], g_r[:, :6]):
+        k = np.nonzero(np.any(g_d[:, :6] != g_r[:, :6], axis=1))[0]
+        bad.append(f"{len(k)} group records differ, first {k[0]}: {g_d[k[0]]} vs {g_r[k[0]]}")
+    if not np.array_equal(dev["body_list"], ref_lists.body_list):
+        bad.append("body lists differ")
+    dkey = node_keys(dev_nodes["begin"], dev_nodes["depth"])
+    rkey = node_keys(ref_nodes["begin"], ref_depths(ref_nodes))
+    if len(dev["cell_list"]) != len(ref_lists.cell_list) or not np.array_equal(
+            dkey[dev["cell_list"]], rkey[ref_lists.cell_list]):
+        bad.append("cell lists differ")
+    return bad
+
+
+def rel_errors(acc, ref):
+    return np.linalg.norm(acc - ref, axis=1) / np.linalg.norm(ref, axis=1)
+
+
+def scatter(tree_order_vals, order):
+    out = np.zeros_like(tree_order_vals)
+    out[np.asarray(order, np.int64)] = tree_order_vals
+    return out
