@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the grouped gravity solver on one GB300.
+
+Workload (the reference's headline metric at N = 2,000,000): one full force
+evaluation -- octree build with FP64 moments, grouped walk, FP32 list
+evaluation, scatter -- of a Hernquist galaxy (disk 40 %, bulge 13 %, halo
+47 %, seed 1), theta = 0.75, group_size = 32, leaf_size = 8, softening 0.025,
+quadrupoles on, sibling packing on. A "step" is one force evaluation.
+
+  value   ms per force evaluation, inputs resident in HBM, CUDA events on the
+          solver's stream around each call, L2 flushed (256 MiB write) before
+          every timed call, mean over the timed steps;
+  e2e     the same through the public host-array call (gtc_group_force):
+          pinned host positions/masses in, accelerations/potentials out;
+  roofline  the list-evaluation kernel: algorithmic FP32 flops (20 per body
+          interaction, 64 per quadrupole cell interaction) / its event time,
+          against this GPU's FP32 FMA peak measured in the same run;
+  accuracy  p99 and median of |a - a_FP64| / |a_FP64| on the reference
+          bench's 4096-particle sample, FP64 direct sums on the device;
+  cpu_baseline  the oracle's restatement of the reference's OpenMP group and
+          tree solvers on this machine's host cores, one evaluation each.
+
+--impl reference times the reference's own CPU solver on the host cores
+(its build when present, else the oracle restatement) on the same workload.
+"""
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8)
+METRIC = "ms/force-eval at N=2M (grouped walk, theta=0.75)"
+WORKLOAD = "hernquist-galaxy N=2M, group solver theta=0.75 gs=32 leaf=8 eps=0.025 quadrupole"
+FLOPS_BODY, FLOPS_CELL_QUAD, FLOPS_CELL_MONO = 20, 64, 21
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=2_000_000)
+    ap.add_argument("--sample", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-steps", action="store_true",
+                    help="warm-up and timed steps only (for profiler launch lists)")
+    return ap.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def read_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()), "measured"
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed loop runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        time.sleep(0.15)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def galaxy(n):
+    import __graft_entry__
+    gtc = __graft_entry__.load_package().gtc
+    pos, vel, mass, _ = gtc.make_galaxy(n, seed=1)
+    return pos, vel, mass
+
+
+def cpu_group_ms(pos, mass, use_ref):
+    """One evaluation (after one warm-up) of the reference's CPU group solver."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import native
+    if use_ref:
+        impl = native.Ref()
+        impl.group_force(pos, mass, pack=False, **SOLVER)
+        t0 = time.perf_counter()
+        _, _, tm = impl.group_force(pos, mass, pack=False, **SOLVER)
+        return (time.perf_counter() - t0) * 1e3, tm
+    impl = native.Oracle()
+    impl.group_force(pos, mass, pack=False, **SOLVER)
+    t0 = time.perf_counter()
+    _, _, tm = impl.group_force(pos, mass, pack=False, **SOLVER)
+    return (time.perf_counter() - t0) * 1e3, tm
+
+
+def cpu_tree_ms(pos, mass):
+    sys.path.insert(0, str(ROOT / "tests"))
+    import native
+    kw = {k: v for k, v in SOLVER.items() if k != "group_size"}
+    t0 = time.perf_counter()
+    _, _, st = native.Oracle().tree_force(pos, mass, **kw)
+    return (time.perf_counter() - t0) * 1e3, st
+
+
+def run_reference(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "tests"))
+    import native
+    use_ref = native.have_ref()
+    impl = native.Ref() if use_ref else native.Oracle()
+    pos, _, mass = galaxy(args.n)
+    for _ in range(min(args.warmup, 1)):
+        impl.group_force(pos, mass, pack=False, **SOLVER)
+    times, budget, t_start = [], 150.0, time.perf_counter()
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, tm = impl.group_force(pos, mass, pack=False, **SOLVER)
+        times.append((time.perf_counter() - t0) * 1e3)
+        if time.perf_counter() - t_start > budget:
+            break
+    ms = statistics.mean(times)
+    cores = os.cpu_count()
+    kind = "reference" if use_ref else "port"
+    sample = (f"{len(times)} full force evaluations at N={args.n} "
+              f"(warm-up {min(args.warmup, 1)}), group solver unpacked (the reference's CPU "
+              f"default), OpenMP over {cores} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
+            "n_gpus": world, "steps": len(times), "warmup": min(args.warmup, 1),
+            "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 tree+lists, f32 evaluation",
+            "data": "synthetic (Hernquist galaxy, seed 1)",
+            "config": {"workload": WORKLOAD, "n": args.n, "parallelism": "openmp host"},
+            "breakdown_ms": {"tree": tm["tree"] * 1e3, "lists": tm["lists"] * 1e3,
+                             "evaluate": tm["evaluate"] * 1e3},
+            "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    rank, local_rank, world = dist_info()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    gtc = __graft_entry__.load_package().gtc
+    ctx = gtc.Context(local_rank)
+    n = args.n
+    pos, _, mass = galaxy(n)
+
+    dev = torch.device("cuda", local_rank)
+    dpos = torch.from_numpy(pos).to(dev)
+    dmass = torch.from_numpy(mass).to(dev)
+    dacc = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    dpot = torch.empty(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    def step():
+        ctx.group_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                               dpot.data_ptr(), pack=True, **SOLVER)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    stats = []
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            stats.append(ctx.stats())
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    times = [a.elapsed_time(b) for a, b in ev]
+    total = sum(times)
+    if world > 1:
+        t = torch.tensor([total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+    ms = total / args.steps
+    value = ms / world  # replicas: force evaluations of the whole job per ms
+
+    if args.only_steps:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(value, 4), "unit": "ms",
+                              "n": n, "steps": args.steps, "only_steps": True}), flush=True)
+        ctx.close()
+        return
+    st = stats[-1]
+    mean = lambda key: statistics.mean(s[key] for s in stats)
+    cell_int, body_int = st["cell_interactions"], st["body_interactions"]
+    fl_cell = FLOPS_CELL_QUAD if SOLVER["quadrupole"] else FLOPS_CELL_MONO
+    flops = FLOPS_BODY * body_int + fl_cell * cell_int
+    kernel_ms = mean("eval_kernel_ms")
+    launches = sum(s["kernel_launches"] for s in stats)
+
+    # accuracy against FP64 direct sums on the reference bench's sample
+    idx = gtc.sample_indices(n, args.sample, 1)
+    didx = torch.from_numpy(idx.astype(np.int64)).to(dev)
+    racc = torch.empty((len(idx), 3), dtype=torch.float64, device=dev)
+    rpot = torch.empty(len(idx), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    ctx.direct_fp64_device(dpos.data_ptr(), dmass.data_ptr(), n, didx.data_ptr(), len(idx),
+                           racc.data_ptr(), rpot.data_ptr(), G=SOLVER["G"], eps=SOLVER["eps"])
+    ref = racc.cpu().numpy()
+    got = dacc.cpu().numpy()[idx.astype(np.int64)]
+    err = np.sort(np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1))
+    p99, med = float(err[len(err) * 99 // 100]), float(err[len(err) // 2])
+
+    # end to end through the host-array call, pinned buffers
+    hpos = torch.from_numpy(pos).pin_memory().numpy()
+    hmass = torch.from_numpy(mass).pin_memory().numpy()
+    hacc = torch.empty((n, 3), dtype=torch.float64).pin_memory().numpy()
+    hpot = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    import ctypes
+    gp = gtc.gravity_params(pack=True, **SOLVER)
+
+    def e2e_step():
+        rc = gtc.lib.gtc_group_force(ctx.h, hpos.ctypes.data, hmass.ctypes.data, n,
+                                     ctypes.byref(gp), hacc.ctypes.data, hpot.ctypes.data)
+        ctx._check(rc)
+
+    e2e_step()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+
+    peak_fp32 = ctx.fp32_peak_tflops()
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    traffic = None
+    tf = ROOT / "profiles" / "evaluate_traffic.json"
+    if tf.exists():
+        try:
+            t = json.loads(tf.read_text())
+            traffic = float(t["dram_bytes_per_launch"]) * n / float(t["n"])
+        except Exception:
+            traffic = None
+    peaks, peak_src = read_peaks()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import native
+        use_ref = native.have_ref()
+        g_ms, g_tm = cpu_group_ms(pos, mass, use_ref)
+        t_ms, t_st = cpu_tree_ms(pos, mass)
+        cores = os.cpu_count()
+        cpu = {"value": round(g_ms, 2), "unit": "ms", "cores": cores,
+               "kind": "reference" if use_ref else "port",
+               "sample": (f"1 full force evaluation at N={n} after 1 warm-up: the reference's "
+                          f"OpenMP group solver (unpacked, its CPU default) over {cores} threads"),
+               "group_breakdown_ms": {"tree": g_tm["tree"] * 1e3, "lists": g_tm["lists"] * 1e3,
+                                      "evaluate": g_tm["evaluate"] * 1e3},
+               "tree_cpu_ms": round(t_ms, 2),
+               "tree_cpu_interactions_per_particle": (t_st[0] + t_st[1]) / n}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "ms", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 tree+walk, f32 evaluation", "data": "synthetic (Hernquist galaxy, seed 1)",
+            "config": {"workload": WORKLOAD, "n": n, "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "l2": "256 MiB flush before every timed step; working set > L2"},
+            "breakdown_ms": {"tree": round(mean("tree_ms"), 4), "lists": round(mean("lists_ms"), 4),
+                             "evaluate": round(mean("evaluate_ms"), 4),
+                             "evaluate_kernel": round(kernel_ms, 4)},
+            "interactions": {"cell": cell_int, "body": body_int,
+                             "per_particle": (cell_int + body_int) / n,
+                             "per_s": (cell_int + body_int) / (ms * 1e-3)},
+            "accuracy": {"p99": p99, "median": med, "sample": len(idx), "judge": "fp64 direct"},
+            "tree": {"nodes": st["n_nodes"], "groups": st["n_groups"], "depth": st["depth"],
+                     "max_list": st["max_list"], "mean_fill": n / max(1, st["n_groups"])},
+            "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": n * 32,
+                    "d2h_bytes_per_step": n * 32, "steps": e2e_steps},
+            "roofline": {"kernel": "k_eval (warp-per-group list evaluation)", "bound": "fp32",
+                         "achieved": round(achieved, 3), "peak": round(peak_fp32, 3),
+                         "unit": "TFLOP/s", "frac": round(achieved / peak_fp32, 4),
+                         "traffic": traffic,
+                         "peak_source": "FP32 FMA throughput measured in this run by a dense FMA "
+                                        "kernel on every SM (no FP32 figure in MEASURED_PEAKS.json)",
+                         "flops_per_launch": flops},
+            "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
+                      "source": peak_src},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+            "learned": None,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,6 +1,7 @@
 // C ABI of the GB300 gravity backend (include/gtc.h).
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 #include <string>
@@ -17,7 +18,7 @@ static_assert(sizeof(gtc_group) == 32, "GTGroup layout");
 struct gtc_context {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {};
+  cudaEvent_t ev[6] = {};
   std::string error;
   gtc_stats stats{};
   gtc::Workspace ws;
@@ -29,6 +30,12 @@ struct gtc_context {
 };
 
 namespace gtc {
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 [[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line) {
   std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" +
@@ -136,6 +143,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   gtc::Workspace &ws = ctx->ws;
   ctx->have_group = false;
   ctx->stats = gtc_stats{};
+  const unsigned long long launches0 = gtc::launches_so_far();
   if (n == 0) {
     ws.n = ws.n_nodes = ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
     ctx->have_group = true;
@@ -150,10 +158,12 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   if (n > 0) {
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
+    GTC_CUDA(cudaEventRecord(ctx->ev[4], s));
     gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
                         ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
                         static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
                         sp.quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+    GTC_CUDA(cudaEventRecord(ctx->ev[5], s));
     gtc::scatter_results(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, s);
   }
   GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
@@ -168,6 +178,8 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
   st.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
   st.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+  st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
+  st.kernel_launches = gtc::launches_so_far() - launches0;
   if (n > 0) {
     const gtc::Scalars &h = *ctx->host_sc;
     st.cell_interactions = h.cell_interactions;
@@ -190,6 +202,7 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
   cudaStream_t s = ctx->stream;
   gtc::Workspace &ws = ctx->ws;
   ctx->stats = gtc_stats{};
+  const unsigned long long launches0 = gtc::launches_so_far();
   GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
   if (n > 0) {
     gtc::pack_bodies_bbox(ws, pos, mass, n, s);
@@ -203,8 +216,10 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
   GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
   GTC_CUDA(cudaStreamSynchronize(s));
   ctx->stats.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+  ctx->stats.eval_kernel_ms = ctx->stats.evaluate_ms;
   ctx->stats.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
   ctx->stats.body_interactions = n > 0 ? n * (n - 1) : 0;
+  ctx->stats.kernel_launches = gtc::launches_so_far() - launches0;
 }
 
 }  // namespace
@@ -470,6 +485,13 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
     gtc::direct_fp64_sample(pos, mass, n, idx, m, G, eps, acc, pot, ctx->sample_scratch,
                             ctx->stream);
     GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops) {
+  return guarded(ctx, [&] {
+    if (!tflops) throw gtc::InvalidArgument("tflops is required");
+    *tflops = gtc::fp32_peak_tflops(ctx->stream);
   });
 }
 

@@ -34,7 +34,14 @@ struct OutOfMemory : std::runtime_error {
     if (gtc_e_ != cudaSuccess) ::gtc::throw_cuda(gtc_e_, #call, __FILE__, __LINE__); \
   } while (0)
 
-#define GTC_LAUNCH_CHECK() GTC_CUDA(cudaGetLastError())
+// Every kernel launch is followed by GTC_LAUNCH_CHECK(), which also counts it.
+void count_launch();
+#define GTC_LAUNCH_CHECK()            \
+  do {                                \
+    GTC_CUDA(cudaGetLastError());     \
+    ::gtc::count_launch();            \
+  } while (0)
+unsigned long long launches_so_far();
 
 // ------------------------------------------------------- device buffers
 // Grow-only device allocation, kept between calls.

@@ -181,3 +181,54 @@ void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 
 }
 
 }  // namespace gtc
+
+namespace gtc {
+namespace {
+
+// Eight independent FMA chains per thread, long enough to hide latency.
+__global__ void __launch_bounds__(256) k_fma_peak(float *sink, int iters, float a, float b) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-3f + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678f) sink[threadIdx.x] = s;  // keeps the chains live
+}
+
+}  // namespace
+
+double fp32_peak_tflops(cudaStream_t s) {
+  int dev = 0, sms = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  DeviceBuffer sink;
+  sink.ensure(256 * sizeof(float));
+  const int iters = 1 << 14;
+  const u32 blocks = static_cast<u32>(sms) * 8;
+  cudaEvent_t a, b;
+  GTC_CUDA(cudaEventCreate(&a));
+  GTC_CUDA(cudaEventCreate(&b));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    GTC_CUDA(cudaEventRecord(a, s));
+    k_fma_peak<<<blocks, 256, 0, s>>>(sink.as<float>(), iters, 0.999f, 1e-3f);
+    GTC_LAUNCH_CHECK();
+    GTC_CUDA(cudaEventRecord(b, s));
+    GTC_CUDA(cudaEventSynchronize(b));
+    float ms = 0.f;
+    GTC_CUDA(cudaEventElapsedTime(&ms, a, b));
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  sink.release();
+  const double flops = 2.0 * 8.0 * iters * 256.0 * blocks;
+  return flops / (best * 1e-3) / 1e12;
+}
+
+}  // namespace gtc

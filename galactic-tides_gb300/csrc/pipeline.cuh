@@ -112,4 +112,7 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
                       cudaStream_t s);
 void bbox_root(Workspace &ws, const double *pos, u64 n, cudaStream_t s);
 
+// FP32 FMA throughput of the device (TFLOP/s), by a dense FMA kernel on every SM.
+double fp32_peak_tflops(cudaStream_t s);
+
 }  // namespace gtc

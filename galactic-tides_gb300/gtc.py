@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 LIB_PATH = HERE / "libgtc.so"
+ICS_PATH = HERE / "libgtc_ics.so"
 
 GTC_OK, GTC_INVALID_ARGUMENT, GTC_RUNTIME_ERROR, GTC_NO_DEVICE, GTC_OUT_OF_MEMORY = range(5)
 CRITERION_THETA, CRITERION_LEARNED = 0, 1
@@ -47,7 +48,8 @@ class Stats(C.Structure):
                 ("body_interactions", C.c_uint64), ("max_list", C.c_uint64),
                 ("n_cell_list", C.c_uint64), ("n_body_list", C.c_uint64),
                 ("n_nodes", C.c_uint32), ("n_groups", C.c_uint32), ("max_group", C.c_uint32),
-                ("depth", C.c_uint32)]
+                ("depth", C.c_uint32), ("eval_kernel_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
 
 
 NODE_DTYPE = np.dtype([
@@ -56,7 +58,7 @@ NODE_DTYPE = np.dtype([
     ("parent", "<u4"), ("depth", "<i4"), ("n_children", "<i4")])
 assert NODE_DTYPE.itemsize == 144
 
-assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 88
+assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 104
 
 
 def _load():
@@ -80,6 +82,7 @@ def _load():
         "gtc_direct_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
+        "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -219,6 +222,11 @@ class Context:
 
     # ---- introspection -----------------------------------------------------
 
+    def fp32_peak_tflops(self):
+        v = C.c_double()
+        self._check(lib.gtc_measure_fp32_peak(self.h, C.byref(v)))
+        return v.value
+
     def stats(self):
         st = Stats()
         self._check(lib.gtc_get_stats(self.h, C.byref(st)))
@@ -242,3 +250,62 @@ class Context:
                                          _ptr(out)))
         return dict(nodes=nodes, order=order, bodies=bodies, cells=cells, groups=groups,
                     cell_list=cl, body_list=bl, out=out)
+
+
+# ---- synthetic galaxies (host/galaxy.h, libgtc_ics.so) ----------------------
+
+class GalaxyModel(C.Structure):
+    _fields_ = [("G", C.c_double), ("disk_n", C.c_uint64), ("bulge_n", C.c_uint64),
+                ("halo_n", C.c_uint64), ("disk_mass", C.c_double), ("disk_h", C.c_double),
+                ("disk_z0", C.c_double), ("disk_rmax", C.c_double), ("disk_Q", C.c_double),
+                ("disk_Q_radius", C.c_double), ("bulge_mass", C.c_double),
+                ("bulge_a", C.c_double), ("bulge_rmax", C.c_double), ("halo_mass", C.c_double),
+                ("halo_core", C.c_double), ("halo_cutoff", C.c_double),
+                ("halo_rmax", C.c_double), ("vesc_fraction", C.c_double), ("seed", C.c_uint64)]
+
+
+_ics = None
+
+
+def _ics_lib():
+    global _ics
+    if _ics is None:
+        if not ICS_PATH.exists():
+            raise ImportError(f"{ICS_PATH} is not built (make -C galactic-tides_gb300)")
+        _ics = C.CDLL(str(ICS_PATH))
+        _ics.gtc_galaxy_default.restype = None
+        _ics.gtc_galaxy_default.argtypes = [C.POINTER(GalaxyModel), C.c_uint64, C.c_uint64]
+        _ics.gtc_make_galaxy.restype = C.c_int
+        _ics.gtc_make_galaxy.argtypes = [C.POINTER(GalaxyModel)] + [C.c_void_p] * 4
+        _ics.gtc_sample_indices.restype = None
+        _ics.gtc_sample_indices.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
+    return _ics
+
+
+def galaxy_model(n, seed=1, **fields):
+    """The benchmark galaxy model for n particles; keyword fields override."""
+    m = GalaxyModel()
+    _ics_lib().gtc_galaxy_default(C.byref(m), n, seed)
+    for k, v in fields.items():
+        setattr(m, k, v)
+    return m
+
+
+def make_galaxy(n=None, seed=1, model=None, **fields):
+    """-> pos (n,3), vel (n,3), mass (n,), type (n,) of a Hernquist galaxy."""
+    m = model if model is not None else galaxy_model(n, seed, **fields)
+    tot = m.disk_n + m.bulge_n + m.halo_n
+    pos = np.empty((tot, 3))
+    vel = np.empty((tot, 3))
+    mass = np.empty(tot)
+    typ = np.empty(tot, np.int32)
+    if _ics_lib().gtc_make_galaxy(C.byref(m), _ptr(pos), _ptr(vel), _ptr(mass), _ptr(typ)):
+        raise ValueError("invalid galaxy model")
+    return pos, vel, mass, typ
+
+
+def sample_indices(n, m=4096, seed=1):
+    """The reference bench's accuracy sample: mt19937_64(seed) shuffle, first m."""
+    out = np.empty(min(n, m), np.uint64)
+    _ics_lib().gtc_sample_indices(n, m, seed, _ptr(out))
+    return out

@@ -114,6 +114,8 @@ typedef struct gtc_stats {
   uint64_t max_list;          /* longest list, cells + bodies */
   uint64_t n_cell_list, n_body_list;
   uint32_t n_nodes, n_groups, max_group, depth;
+  double eval_kernel_ms;      /* the list (or direct) evaluation kernel alone */
+  uint64_t kernel_launches;   /* kernels this call launched */
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
@@ -174,6 +176,12 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
                                   double eps, double *acc, double *pot);
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
+
+/* ---- diagnostics (no reference counterpart) ----------------------------- */
+
+/* Measured FP32 FMA throughput of this GPU in TFLOP/s (one FMA = 2 flops):
+ * the roofline denominator for the FP32 evaluation kernels. */
+gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops);
 
 /* ---- exports of the last gtc_group_force*, for parity checks ------------ */
 
