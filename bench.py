@@ -340,7 +340,8 @@ def main():
                              "per_s": (cell_int + body_int) / (ms * 1e-3)},
             "accuracy": {"p99": p99, "median": med, "sample": len(idx), "judge": "fp64 direct"},
             "tree": {"nodes": st["n_nodes"], "groups": st["n_groups"], "depth": st["depth"],
-                     "max_list": st["max_list"], "mean_fill": n / max(1, st["n_groups"])},
+                     "max_list": st["max_list"], "mean_fill": n / max(1, st["n_groups"]),
+                     "walk_tests_fp64": st["walk_tests_fp64"]},
             "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": n * 32,
                     "d2h_bytes_per_step": n * 32, "steps": e2e_steps},
             "roofline": {"kernel": "k_eval (warp-per-group list evaluation)", "bound": "fp32",

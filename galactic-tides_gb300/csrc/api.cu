@@ -72,8 +72,8 @@ void Workspace::release_all() {
                          &key2, &tiny, &lcp, &leafdepth, &count, &count_scan, &flags,
                          &flags_scan, &tpos, &tmass, &bodies, &out, &dpos, &dkey, &dkey_alt,
                          &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
-                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &walk, &cells,
-                         &gbegin, &gend, &gbox, &gcells, &gbodies, &gcell_off, &gbody_off,
+                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &walk32, &walk64, &cells,
+                         &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
                          &groups, &cell_list, &body_list, &root, &bbox_part, &scalars, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
@@ -187,6 +187,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     st.max_list = h.max_list;
     st.max_group = h.max_group;
     st.depth = h.depth;
+    st.walk_tests_fp64 = h.fp64_tests;
   }
   st.n_cell_list = ws.n_cell_list;
   st.n_body_list = ws.n_body_list;

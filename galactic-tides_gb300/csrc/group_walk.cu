@@ -83,9 +83,12 @@ __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
   if (sc->n_groups > 0) gend[sc->n_groups - 1] = n;
 }
 
-// Group bounding box (group_lists.cpp:125-131): centre and half-extent.
+// Group bounding box (group_lists.cpp:125-131): centre and half-extent in
+// FP64, and the same in FP32 with the centre taken relative to the root
+// centre (the frame of the FP32 walk records).
 __global__ void __launch_bounds__(kT)
-    k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos, double *gbox) {
+    k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos,
+                const TreeRoot *root, double *gbox, float *gboxf) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (g >= ng) return;
   const u32 b0 = gbegin[g], b1 = gend[g];
@@ -98,13 +101,17 @@ __global__ void __launch_bounds__(kT)
       hi[a] = hi[a] < v ? v : hi[a];
     }
   for (int a = 0; a < 3; ++a) {
-    gbox[6ull * g + a] = (lo[a] + hi[a]) * 0.5;
-    gbox[6ull * g + 3 + a] = (hi[a] - lo[a]) * 0.5;
+    const double c = (lo[a] + hi[a]) * 0.5, h = (hi[a] - lo[a]) * 0.5;
+    gbox[6ull * g + a] = c;
+    gbox[6ull * g + 3 + a] = h;
+    gboxf[6ull * g + a] = static_cast<float>(c - root->center[a]);
+    gboxf[6ull * g + 3 + a] = static_cast<float>(h);
   }
 }
 
-// The opening test of group_lists.cpp:145-154 for one node.
-__device__ __forceinline__ bool accept(const WalkRec &r, const double *gc, const double *gh) {
+// The opening test of group_lists.cpp:145-154 for one node, in FP64 exactly
+// as the reference computes it.
+__device__ __forceinline__ bool accept64(const WalkRec64 &r, const double *gc, const double *gh) {
   bool overlap = true;
   double d2 = 0.0;
   if (fabs(r.cx - gc[0]) > r.slack + gh[0]) overlap = false;
@@ -119,24 +126,67 @@ __device__ __forceinline__ bool accept(const WalkRec &r, const double *gc, const
   return !overlap && d2 > r.crit2;
 }
 
-__device__ __forceinline__ WalkRec load_rec(const WalkRec *w, u32 i) {
-  const double2 *p = reinterpret_cast<const double2 *>(w + i);
-  const double2 a0 = __ldg(p), a1 = __ldg(p + 1), b0 = __ldg(p + 2), b1 = __ldg(p + 3);
-  const uint4 c = __ldg(reinterpret_cast<const uint4 *>(p + 4));
-  WalkRec r;
-  r.cx = a0.x;
-  r.cy = a0.y;
-  r.cz = a1.x;
-  r.slack = a1.y;
-  r.mx = b0.x;
-  r.my = b0.y;
-  r.mz = b1.x;
-  r.crit2 = b1.y;
+// The same test in FP32 with a rigorous error bound. Every FP32 input is the
+// FP64 quantity rounded once (relative error 2^-24), and each FP32 result
+// below is within a few 2^-24 of the value computed from the exact inputs;
+// the band kBand = 2^-20 (relative to the magnitudes involved) is several
+// times wider than all of that plus the FP64 roundings. A comparison whose
+// two sides are further apart than the band has the same outcome in FP64;
+// otherwise the result is "undecided" and the caller runs the FP64 test.
+// Returns 1 accept, 0 open, 2 undecided. NaNs come out undecided.
+constexpr float kBand = 1.0f / (1 << 20);
+
+__device__ __forceinline__ int accept32(const WalkRec32 &r, const float *gf, const float *hf) {
+  // overlap: on every axis |c - g| <= slack + gh (group_lists.cpp:147)
+  int separated = 0, within = 0;
+  float lo2 = 0.f, hi2 = 0.f;
+  const float c[3] = {r.cx, r.cy, r.cz}, mm[3] = {r.mx, r.my, r.mz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float x = fabsf(c[a] - gf[a]), y = r.slack + hf[a];
+    const float e = kBand * (fabsf(c[a]) + fabsf(gf[a]) + x + y);
+    separated |= x > y + e;
+    within += x < y - e;
+    // distance from the box to the centre of mass (group_lists.cpp:150-151)
+    const float d = fabsf(mm[a] - gf[a]) - hf[a];
+    const float ed = kBand * (fabsf(mm[a]) + fabsf(gf[a]) + hf[a] + fabsf(d));
+    const float dl = d - ed, dh = d + ed;
+    lo2 += dl > 0.f ? dl * dl : 0.f;
+    hi2 += dh > 0.f ? dh * dh : 0.f;
+  }
+  lo2 *= 1.f - 4.f * kBand;
+  hi2 *= 1.f + 4.f * kBand;
+  const float c2 = r.crit2;
+  if (within == 3) return 0;                       // overlaps: opened
+  if (hi2 < c2 * (1.f - 4.f * kBand)) return 0;    // too close: opened
+  if (separated && lo2 > c2 * (1.f + 4.f * kBand)) return 1;
+  return 2;
+}
+
+__device__ __forceinline__ WalkRec32 load32(const WalkRec32 *w, u32 i) {
+  const float4 *p = reinterpret_cast<const float4 *>(w + i);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  const uint4 c = __ldg(reinterpret_cast<const uint4 *>(p + 2));
+  WalkRec32 r;
+  r.cx = a.x;
+  r.cy = a.y;
+  r.cz = a.z;
+  r.slack = a.w;
+  r.mx = b.x;
+  r.my = b.y;
+  r.mz = b.z;
+  r.crit2 = b.w;
   r.skip = c.x;
   r.nbody = c.y;
   r.begin = c.z;
   r.leaf = c.w;
   return r;
+}
+
+__device__ __forceinline__ WalkRec64 load64(const WalkRec64 *w, u32 i) {
+  const double2 *p = reinterpret_cast<const double2 *>(w + i);
+  const double2 a0 = __ldg(p), a1 = __ldg(p + 1), b0 = __ldg(p + 2), b1 = __ldg(p + 3);
+  return WalkRec64{a0.x, a0.y, a1.x, a1.y, b0.x, b0.y, b1.x, b1.y};
 }
 
 struct WalkOut {
@@ -148,44 +198,48 @@ struct WalkOut {
 
 template <bool kFill>
 __global__ void __launch_bounds__(kT)
-    k_walk(const WalkRec *walk, u32 m, const u32 *gbegin, const u32 *gend, const double *gbox,
-           u32 ng, WalkOut out, Scalars *sc) {
+    k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, u32 m, const u32 *gbegin,
+           const u32 *gend, const double *gbox, const float *gboxf, u32 ng, WalkOut out,
+           Scalars *sc) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (g >= ng) return;
-  double gc[3], gh[3];
+  float gf[3], hf[3];
   for (int a = 0; a < 3; ++a) {
-    gc[a] = gbox[6ull * g + a];
-    gh[a] = gbox[6ull * g + 3 + a];
+    gf[a] = gboxf[6ull * g + a];
+    hf[a] = gboxf[6ull * g + 3 + a];
   }
   u32 *cl = nullptr, *bl = nullptr;
   if (kFill) {
     cl = out.cell_list + out.cell_off[g];
     bl = out.body_list + out.body_off[g];
   }
-  u32 nc = 0, nb = 0;
+  u32 nc = 0, nb = 0, exact = 0;
   u32 i = 0;
   while (i < m) {
-    const WalkRec r = load_rec(walk, i);
-    if (accept(r, gc, gh)) {
-      if (r.nbody <= kFewBodies) {
-        if (kFill)
-          for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
-        nb += r.nbody;
-      } else {
-        if (kFill) cl[nc] = i;
-        ++nc;
+    const WalkRec32 r = load32(walk32, i);
+    int verdict = accept32(r, gf, hf);
+    if (verdict == 2) {
+      double gc[3], gh[3];
+      for (int a = 0; a < 3; ++a) {
+        gc[a] = gbox[6ull * g + a];
+        gh[a] = gbox[6ull * g + 3 + a];
       }
-      if (r.skip <= i) break;  // malformed tree: never loop
-      i = r.skip;
-    } else if (r.leaf) {
+      verdict = accept64(load64(walk64, i), gc, gh) ? 1 : 0;
+      ++exact;
+    }
+    if (verdict == 1 && r.nbody > kFewBodies) {
+      if (kFill) cl[nc] = i;
+      ++nc;
+    } else if (verdict == 1 || r.leaf) {
       if (kFill)
         for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
       nb += r.nbody;
-      if (r.skip <= i) break;
-      i = r.skip;
     } else {
       ++i;
+      continue;
     }
+    if (r.skip <= i) break;  // malformed tree: never loop
+    i = r.skip;
   }
   if (i < m) atomicOr(&sc->error, 1u);
   const u32 t = gend[g] - gbegin[g];
@@ -201,6 +255,7 @@ __global__ void __launch_bounds__(kT)
     atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t) * nb - t);
     atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
     atomicMax(&sc->max_group, t);
+    if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
   }
 }
 
@@ -230,6 +285,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gbegin.ensure(n * 4);
   ws.gend.ensure(n * 4);
   ws.gbox.ensure(n * 48);
+  ws.gboxf.ensure(n * 24);
   ws.gcells.ensure(n * 8);
   ws.gbodies.ensure(n * 8);
   ws.gcell_off.ensure(n * 8);
@@ -246,12 +302,14 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u32 ng = host->n_groups;
   ws.n_groups = ng;
   const u32 gb = ceil_div(ng, kT);
-  k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.gbox.as<double>());
+  k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
+                                ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.gcell_off.as<u64>(),
              ws.gbody_off.as<u64>(), nullptr, nullptr, ws.groups.as<uint4>()};
-  k_walk<false><<<gb, kT, 0, s>>>(ws.walk.as<WalkRec>(), m, gbegin, gend, ws.gbox.as<double>(), ng,
-                                  wo, sc);
+  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
+  k_walk<false><<<gb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), m, gbegin,
+                                  gend, ws.gbox.as<double>(), ws.gboxf.as<float>(), ng, wo, sc);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u64(ws.gcells.as<u64>(), ws.gcell_off.as<u64>(), ng, &sc->n_cell_list,
                      ws.scan_tmp, s);
@@ -266,8 +324,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   wo.cell_list = ws.cell_list.as<u32>();
   wo.body_list = ws.body_list.as<u32>();
-  k_walk<true><<<gb, kT, 0, s>>>(ws.walk.as<WalkRec>(), m, gbegin, gend, ws.gbox.as<double>(), ng,
-                                 wo, sc);
+  k_walk<true><<<gb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), m, gbegin,
+                                 gend, ws.gbox.as<double>(), ws.gboxf.as<float>(), ng, wo, sc);
   GTC_LAUNCH_CHECK();
 }
 

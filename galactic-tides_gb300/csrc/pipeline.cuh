@@ -31,11 +31,17 @@ struct TreeRoot {
   double half_at[kMaxDepth + 1];
 };
 
-// What the grouped walk reads per node, 80 bytes.
-struct alignas(16) WalkRec {
+// What the grouped walk reads per node. The FP32 record decides almost every
+// opening test; the FP64 record (the reference's exact quantities) settles
+// the few tests the FP32 record cannot decide with certainty.
+struct alignas(16) WalkRec32 {
+  float cx, cy, cz, slack;   // centre relative to the root centre; half * 1.0001
+  float mx, my, mz, crit2;   // centre of mass relative to the root centre; crit^2
+  u32 skip, nbody, begin, leaf;
+};
+struct alignas(16) WalkRec64 {
   double cx, cy, cz, slack;  // slack = half * 1.0001 (group_lists.cpp:147)
   double mx, my, mz, crit2;  // crit = 2 half / theta + delta (group_lists.cpp:59-60)
-  u32 skip, nbody, begin, leaf;
 };
 
 struct SolverParams {
@@ -54,9 +60,9 @@ struct Workspace {
   DeviceBuffer dpos, dkey, dkey_alt, drec, drec_alt, dseg, dtmp;
   // nodes
   DeviceBuffer geom, mom, quad, delta, nbegin, nend, skip, parent, depth, nchild, isleaf,
-      arrive, walk, cells;
+      arrive, walk32, walk64, cells;
   // groups and lists
-  DeviceBuffer gbegin, gend, gbox, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
+  DeviceBuffer gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
       body_list;
   // scalars and reductions
   DeviceBuffer root, bbox_part, scalars;
@@ -78,7 +84,8 @@ struct Scalars {
   u64 n_cell_list, n_body_list;
   unsigned long long cell_interactions, body_interactions, max_list;
   u32 max_group;
-  u32 aux;                // scratch count (deep-round segments)
+  u32 aux;
+  unsigned long long fp64_tests;  // opening tests the FP32 bounds left undecided                // scratch count (deep-round segments)
   u32 error;              // device-detected failure code (0 = none)
 };
 

@@ -121,18 +121,39 @@ __global__ void __launch_bounds__(kT) k_bbox_partial(const double *pos, u64 n, d
   }
 }
 
-// Root cube from the reduced box (octree.cpp:184-198), one thread.
-__global__ void k_root(const double *part, int nparts, TreeRoot *root) {
+// Root cube from the reduced box (octree.cpp:184-198); min/max are exact in
+// any order, so the partial boxes are reduced by the whole block.
+__global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, TreeRoot *root) {
+  double v[6];
+  for (int a = 0; a < 3; ++a) {
+    v[a] = INFINITY;
+    v[3 + a] = -INFINITY;
+  }
+  for (int p = threadIdx.x; p < nparts; p += kT)
+    for (int a = 0; a < 3; ++a) {
+      v[a] = fmin(v[a], part[6 * p + a]);
+      v[3 + a] = fmax(v[3 + a], part[6 * p + 3 + a]);
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      v[a] = fmin(v[a], __shfl_xor_sync(kFullMask, v[a], o));
+      v[3 + a] = fmax(v[3 + a], __shfl_xor_sync(kFullMask, v[3 + a], o));
+    }
+  __shared__ double s[kT / 32][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int a = 0; a < 6; ++a) s[warp][a] = v[a];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   double lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
-    lo[a] = part[a];
-    hi[a] = part[3 + a];
-  }
-  for (int p = 1; p < nparts; ++p)
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = fmin(lo[a], part[6 * p + a]);
-      hi[a] = fmax(hi[a], part[6 * p + 3 + a]);
+    lo[a] = s[0][a];
+    hi[a] = s[0][3 + a];
+    for (int w = 1; w < kT / 32; ++w) {
+      lo[a] = fmin(lo[a], s[w][a]);
+      hi[a] = fmax(hi[a], s[w][3 + a]);
     }
+  }
   double half = 0.0;
   for (int a = 0; a < 3; ++a) {
     root->lo[a] = lo[a];
@@ -509,17 +530,18 @@ __global__ void __launch_bounds__(kT) k_moments(MomentArrays a, const u8 *isleaf
 
 // --------------------------------------------------------------- packing
 
-// FP64 walk record and FP32 cell of every node (group_lists.cpp:52-61).
+// Walk records (FP32 and FP64) and FP32 cell of every node
+// (group_lists.cpp:52-61).
 __global__ void __launch_bounds__(kT)
     k_pack_nodes(const double2 *geom, const double2 *mom, const double2 *quad,
                  const double *delta, const u32 *nbegin, const u32 *nend, const u32 *skip,
-                 const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta, WalkRec *walk,
-                 float4 *cells) {
+                 const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta,
+                 WalkRec32 *walk32, WalkRec64 *walk64, float4 *cells) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p >= m) return;
   const Dbl4 g = load_pair(geom, p), c = load_pair(mom, p);
   const double crit = 2.0 * g.w * inv_theta + delta[p];
-  WalkRec r;
+  WalkRec64 r;
   r.cx = g.x;
   r.cy = g.y;
   r.cz = g.z;
@@ -528,12 +550,22 @@ __global__ void __launch_bounds__(kT)
   r.my = c.y;
   r.mz = c.z;
   r.crit2 = crit * crit;
-  r.skip = skip[p];
-  r.nbody = nend[p] - nbegin[p];
-  r.begin = nbegin[p];
-  r.leaf = isleaf[p];
-  walk[p] = r;
+  walk64[p] = r;
   const double ox = root->center[0], oy = root->center[1], oz = root->center[2];
+  WalkRec32 f;
+  f.cx = static_cast<float>(g.x - ox);
+  f.cy = static_cast<float>(g.y - oy);
+  f.cz = static_cast<float>(g.z - oz);
+  f.slack = static_cast<float>(r.slack);
+  f.mx = static_cast<float>(c.x - ox);
+  f.my = static_cast<float>(c.y - oy);
+  f.mz = static_cast<float>(c.z - oz);
+  f.crit2 = static_cast<float>(r.crit2);
+  f.skip = skip[p];
+  f.nbody = nend[p] - nbegin[p];
+  f.begin = nbegin[p];
+  f.leaf = isleaf[p];
+  walk32[p] = f;
   const double2 qa = quad[3 * p], qb = quad[3 * p + 1], qc = quad[3 * p + 2];
   cells[3 * p] = make_float4(static_cast<float>(c.x - ox), static_cast<float>(c.y - oy),
                              static_cast<float>(c.z - oz), static_cast<float>(c.w));
@@ -572,7 +604,7 @@ void bbox_root(Workspace &ws, const double *pos, u64 n, cudaStream_t s) {
   ws.root.ensure(sizeof(TreeRoot));
   k_bbox_partial<<<nparts, kT, 0, s>>>(pos, n, ws.bbox_part.as<double>());
   GTC_LAUNCH_CHECK();
-  k_root<<<1, 1, 0, s>>>(ws.bbox_part.as<double>(), static_cast<int>(nparts), ws.root.as<TreeRoot>());
+  k_root<<<1, kT, 0, s>>>(ws.bbox_part.as<double>(), static_cast<int>(nparts), ws.root.as<TreeRoot>());
   GTC_LAUNCH_CHECK();
 }
 
@@ -706,7 +738,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   ws.nchild.ensure(m);
   ws.isleaf.ensure(m);
   ws.arrive.ensure(m * 4ull);
-  ws.walk.ensure(m * sizeof(WalkRec));
+  ws.walk32.ensure(m * sizeof(WalkRec32));
+  ws.walk64.ensure(m * sizeof(WalkRec64));
   ws.cells.ensure(m * 3 * sizeof(float4));
   const u32 mb = ceil_div(m, kT);
 
@@ -732,7 +765,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
                                  ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                                  ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
-                                 1.0 / sp.theta, ws.walk.as<WalkRec>(), ws.cells.as<float4>());
+                                 1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
+                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>());
   GTC_LAUNCH_CHECK();
   k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
                                   root_centre(root), ws.bodies.as<float4>());

@@ -49,7 +49,7 @@ class Stats(C.Structure):
                 ("n_cell_list", C.c_uint64), ("n_body_list", C.c_uint64),
                 ("n_nodes", C.c_uint32), ("n_groups", C.c_uint32), ("max_group", C.c_uint32),
                 ("depth", C.c_uint32), ("eval_kernel_ms", C.c_double),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("walk_tests_fp64", C.c_uint64)]
 
 
 NODE_DTYPE = np.dtype([
@@ -58,7 +58,7 @@ NODE_DTYPE = np.dtype([
     ("parent", "<u4"), ("depth", "<i4"), ("n_children", "<i4")])
 assert NODE_DTYPE.itemsize == 144
 
-assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 104
+assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 112
 
 
 def _load():

@@ -116,6 +116,7 @@ typedef struct gtc_stats {
   uint32_t n_nodes, n_groups, max_group, depth;
   double eval_kernel_ms;      /* the list (or direct) evaluation kernel alone */
   uint64_t kernel_launches;   /* kernels this call launched */
+  uint64_t walk_tests_fp64;   /* opening tests decided in FP64 (FP32 bound undecided) */
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
