@@ -75,3 +75,77 @@ def scatter(tree_order_vals, order):
     out = np.zeros_like(tree_order_vals)
     out[np.asarray(order, np.int64)] = tree_order_vals
     return out
+
+
+# ---- the reference's list invariants (tests/test_gpu_kernels.cpp:109-168) ----
+
+def check_lists(node_begin, node_end, groups, cell_list, body_list, n, group_size):
+    """Groups tile [0, n) in order and have 1..group_size targets; every body is
+    covered exactly once by each group's list (a cell covers all its bodies);
+    no accepted cell contains one of the group's targets. Returns the number
+    of violations."""
+    bad = 0
+    nxt = 0
+    for g in groups:
+        if g[0] != nxt or g[1] <= g[0] or g[1] - g[0] > group_size:
+            bad += 1
+        nxt = g[1]
+    bad += int(nxt != n)
+    nb = np.asarray(node_begin, np.int64)
+    ne = np.asarray(node_end, np.int64)
+    for g in groups:
+        cov = np.zeros(n + 1, np.int64)
+        cells = np.asarray(cell_list[g[2]:g[3]], np.int64)
+        b, e = nb[cells], ne[cells]
+        bad += int(np.count_nonzero((b < g[1]) & (g[0] < e)))
+        np.add.at(cov, b, 1)
+        np.add.at(cov, e, -1)
+        cov = np.cumsum(cov)[:n]
+        np.add.at(cov, np.asarray(body_list[g[4]:g[5]], np.int64), 1)
+        bad += int(np.count_nonzero(cov != 1))
+    return bad
+
+
+def check_packing(node_begin, node_end, children, groups):
+    """Packing only merges siblings: every group is a whole node, a chunk of a
+    leaf, or a run of consecutive children of the deepest node containing it.
+    `children(p)` lists p's children. Returns the number of violations."""
+    bad = 0
+    for g in groups:
+        p = 0
+        while True:
+            for c in children(p):
+                if node_begin[c] <= g[0] and g[1] <= node_end[c]:
+                    p = c
+                    break
+            else:
+                break
+        if node_begin[p] == g[0] and node_end[p] == g[1]:
+            continue
+        ch = children(p)
+        if not ch:
+            continue
+        starts = any(node_begin[c] == g[0] for c in ch)
+        ends = any(node_end[c] == g[1] for c in ch)
+        bad += int(not (starts and ends))
+    return bad
+
+
+def ref_children(nodes):
+    fc, nc = nodes["first_child"], nodes["n_children"]
+    return lambda p: list(range(int(fc[p]), int(fc[p]) + int(nc[p]))) if nc[p] > 0 else []
+
+
+def dev_children(nodes):
+    skip = nodes["skip"]
+    nch = nodes["n_children"]
+
+    def children(p):
+        if nch[p] == 0:
+            return []
+        out, c = [], p + 1
+        while c < skip[p]:
+            out.append(c)
+            c = int(skip[c])
+        return out[::-1]
+    return children
