@@ -170,6 +170,8 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
                            cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
+  if (ctx->host_sc->error & 4u)
+    throw gtc::InvalidArgument("cuda: positions must be finite");
   if (ctx->host_sc->error != 0)
     throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
                             std::to_string(ctx->host_sc->error) + ")");

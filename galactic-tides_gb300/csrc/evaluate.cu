@@ -40,27 +40,37 @@ __device__ __forceinline__ void add_cell(float px, float py, float pz, const Sta
   const float inv = rsqrtf(r2);
   const float inv2 = inv * inv;
   const float inv3 = inv * inv2;
-  const float gm3 = c.cm.w * inv3;
-  ax = fmaf(-gm3, dx, ax);
-  ay = fmaf(-gm3, dy, ay);
-  az = fmaf(-gm3, dz, az);
-  pot = fmaf(-c.cm.w, inv, pot);
   if (kQuad) {
+    // a = -G m d / r^3 + G Q d / r^5 - 5/2 G (d.Q.d) d / r^7, with G folded
+    // into m and Q: the monopole and quadrupole terms along d share one FMA
+    // per axis.
     const float qx = fmaf(c.q0.x, dx, fmaf(c.q0.w, dy, c.q1.x * dz));
     const float qy = fmaf(c.q0.w, dx, fmaf(c.q0.y, dy, c.q1.y * dz));
     const float qz = fmaf(c.q1.x, dx, fmaf(c.q1.y, dy, c.q0.z * dz));
     const float rqr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
     const float inv5 = inv3 * inv2;
     const float inv7 = inv5 * inv2;
-    const float u = 2.5f * rqr * inv7;
-    ax = fmaf(qx, inv5, fmaf(-u, dx, ax));
-    ay = fmaf(qy, inv5, fmaf(-u, dy, ay));
-    az = fmaf(qz, inv5, fmaf(-u, dz, az));
-    pot = fmaf(-0.5f * rqr, inv5, pot);
+    const float along = fmaf(-2.5f * rqr, inv7, -c.cm.w * inv3);
+    ax = fmaf(along, dx, fmaf(qx, inv5, ax));
+    ay = fmaf(along, dy, fmaf(qy, inv5, ay));
+    az = fmaf(along, dz, fmaf(qz, inv5, az));
+    pot = fmaf(-c.cm.w, inv, fmaf(-0.5f * rqr, inv5, pot));
+  } else {
+    const float gm3 = c.cm.w * inv3;
+    ax = fmaf(-gm3, dx, ax);
+    ay = fmaf(-gm3, dy, ay);
+    az = fmaf(-gm3, dz, az);
+    pot = fmaf(-c.cm.w, inv, pot);
   }
 }
 
-template <bool kQuad>
+// kSoft: eps2 > 0. Every target appears exactly once in its own group's body
+// list (each body is covered once and no accepted cell holds a target), and
+// with softening its self term adds exactly zero acceleration (d = 0) and a
+// known -G m_i / eps to the potential, so the loop needs no self test and
+// the self potential is taken back out at the end. Without softening the
+// self term is singular and each entry is tested as in the reference.
+template <bool kQuad, bool kSoft>
 __global__ void __launch_bounds__(kT)
     k_eval(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
            const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
@@ -111,13 +121,17 @@ __global__ void __launch_bounds__(kT)
       __syncwarp();
       const u32 cnt = min(32u, gb.y - base);
       for (u32 t = 0; t < cnt; ++t) {
-        const u32 jt = __shfl_sync(kFullMask, j, t);
         const float4 b = sb[warp][t];
-        const bool self = jt == i;
         const float dx = bi.x - b.x, dy = bi.y - b.y, dz = bi.z - b.z;
-        const float r2 = self ? 1.0f : fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        float w = b.w;
+        if (!kSoft) {
+          const bool self = __shfl_sync(kFullMask, j, t) == i;
+          r2 = self ? 1.0f : r2;
+          w = self ? 0.0f : w;
+        }
         const float inv = rsqrtf(r2);
-        const float gm = (self ? 0.0f : b.w) * inv;
+        const float gm = w * inv;
         const float gm3 = gm * inv * inv;
         ax = fmaf(-gm3, dx, ax);
         ay = fmaf(-gm3, dy, ay);
@@ -126,6 +140,7 @@ __global__ void __launch_bounds__(kT)
       }
       __syncwarp();
     }
+    if (kSoft) pot += G * bi.w * rsqrtf(eps2);  // the self term, added once above
     if (active) out[i] = make_float4(ax, ay, az, pot);
   }
 }
@@ -143,6 +158,21 @@ __global__ void __launch_bounds__(256)
   pot[i] = o.w;
 }
 
+template <bool kQuad, bool kSoft>
+void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                 const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
+                 float4 *out, u32 *counter, cudaStream_t s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<kQuad, kSoft>, kT, 0));
+  const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
+  k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
+                                           static_cast<u32>(n_groups), G, eps2, out, counter);
+  GTC_LAUNCH_CHECK();
+}
+
 }  // namespace
 
 void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
@@ -150,23 +180,15 @@ void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_l
                     bool quadrupole, float4 *out, u32 *counter, cudaStream_t s) {
   if (n_groups == 0) return;
   GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
-  int dev = 0, sms = 0, per_sm = 0;
-  GTC_CUDA(cudaGetDevice(&dev));
-  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (quadrupole)
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<true>, kT, 0));
+  const bool soft = eps2 > 0.0f;
+  if (quadrupole && soft)
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+  else if (quadrupole)
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+  else if (soft)
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
   else
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<false>, kT, 0));
-  const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
-  const u32 ng = static_cast<u32>(n_groups);
-  if (quadrupole)
-    k_eval<true><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups, ng, G, eps2, out,
-                                     counter);
-  else
-    k_eval<false><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups, ng, G, eps2, out,
-                                      counter);
-  GTC_LAUNCH_CHECK();
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
 }
 
 void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,

@@ -169,11 +169,26 @@ __global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, Tre
 
 // ------------------------------------------------------------------- keys
 
+// Order-preserving image of a double for integer comparison: a >= b exactly
+// when key(a) >= key(b), for finite a, b (-0.0 is taken as +0.0).
+__device__ __forceinline__ u64 order_key(double v) {
+  u64 b = static_cast<u64>(__double_as_longlong(v));
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 // First key word: levels 1..21 from the root; records the first depth whose
 // node is "tiny" (a leaf whatever its count). Digits below a tiny node are 0,
 // so bodies of such a leaf stay in input order through the sort.
+//
+// A node holding body p has |centre|_1 <= |p|_1 + 3 half (plus rounding), so
+// it can only be tiny once half < 1e-12 (|p|_1 + 3 half + 1e-300), i.e. once
+// half < ~1.0000001e-12 (|p|_1 + 1e-300). Levels whose half is at least
+// twice that bound skip the exact FP64 test; the comparison of two positive
+// doubles is done on their bit patterns.
 __global__ void __launch_bounds__(kT)
-    k_keys(const double *pos, u32 n, const TreeRoot *root, u64 *key, u32 *idx, u8 *tiny) {
+    k_keys(const double *pos, u32 n, const TreeRoot *root, u64 *key, u32 *idx, u8 *tiny,
+           u32 *error) {
   __shared__ double half_at[kLevelsPerWord + 1];
   __shared__ double c0[3];
   if (threadIdx.x <= kLevelsPerWord) half_at[threadIdx.x] = root->half_at[threadIdx.x];
@@ -182,12 +197,19 @@ __global__ void __launch_bounds__(kT)
   const u32 i = blockIdx.x * kT + threadIdx.x;
   if (i >= n) return;
   const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
+  if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicOr(error, 4u);
+  const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
+  const long long maybe_tiny =
+      __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
   double cx = c0[0], cy = c0[1], cz = c0[2];
   u64 k = 0;
   int t = kNoTiny;
   for (int d = 0; d < kLevelsPerWord; ++d) {
-    if (t == kNoTiny && tiny_node(half_at[d], cx, cy, cz)) t = d;
-    int o = (x >= cx ? 1 : 0) | (y >= cy ? 2 : 0) | (z >= cz ? 4 : 0);
+    if (t == kNoTiny && __double_as_longlong(half_at[d]) < maybe_tiny &&
+        tiny_node(half_at[d], cx, cy, cz))
+      t = d;
+    int o = (kx >= order_key(cx) ? 1 : 0) | (ky >= order_key(cy) ? 2 : 0) |
+            (kz >= order_key(cz) ? 4 : 0);
     if (t != kNoTiny) o = 0;
     k = (k << 3) | static_cast<u64>(o);
     step_centre(cx, cy, cz, o, half_at[d + 1]);
@@ -649,7 +671,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny);
+  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
   radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
 

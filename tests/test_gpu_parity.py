@@ -172,3 +172,23 @@ def test_fp64_sample_kernel(ctx, oracle):
     err = rel_errors(da.cpu().numpy(), racc)
     assert err.max() < 1e-12
     assert np.abs(dpot.cpu().numpy() / rpot - 1).max() < 1e-12
+
+
+def test_rejects_non_finite_positions(ctx, gtc):
+    pos, mass = lopsided_sphere(1000, 3)
+    pos[17, 1] = np.nan
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.group_force(pos, mass)
+    pos[17, 1] = np.inf
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.group_force(pos, mass)
+    pos, mass = lopsided_sphere(1000, 3)   # the context stays usable
+    acc, _ = ctx.group_force(pos, mass)
+    assert np.all(np.isfinite(acc))
+
+
+def test_unsoftened_self_exclusion(ctx, oracle):
+    """eps = 0: the evaluator tests every body entry against the target."""
+    pos, mass = lopsided_sphere(2000, 8)
+    err, _ = solve_and_compare(ctx, oracle, pos, mass, theta=0.7, gs=32, pack=True, eps=0.0)
+    assert np.all(np.isfinite(err)) and np.median(err) < 1e-5
