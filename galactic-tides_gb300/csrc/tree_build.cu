@@ -681,6 +681,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
   GTC_LAUNCH_CHECK();
   read_scalars(ws, host, s);
+  if (host->error & 4u) throw InvalidArgument("cuda: positions must be finite");
 
   // Deeper key words for bodies whose leaves lie below the words so far.
   while (host->deep > 0 && kv.words < 3) {
