@@ -72,11 +72,13 @@ void Workspace::release_all() {
                          &key2, &tiny, &lcp, &leafdepth, &count, &count_scan, &flags,
                          &flags_scan, &tpos, &tmass, &bodies, &out, &dpos, &dkey, &dkey_alt,
                          &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
-                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &walk32, &walk64, &cells,
-                         &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
+                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &bucket, &walk32, &walk64, &cells,
+                         &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
                          &groups, &cell_list, &body_list, &root, &bbox_part, &scalars, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
+  if (host_words) cudaFreeHost(host_words);
+  host_words = nullptr;
 }
 
 }  // namespace gtc

@@ -189,20 +189,49 @@ __device__ __forceinline__ WalkRec64 load64(const WalkRec64 *w, u32 i) {
   return WalkRec64{a0.x, a0.y, a1.x, a1.y, b0.x, b0.y, b1.x, b1.y};
 }
 
-struct WalkOut {
-  u64 *ncells, *nbodies;          // count pass
-  const u64 *cell_off, *body_off; // fill pass
-  u32 *cell_list, *body_list;
-  uint4 *groups;
+// One walk task: the subtree under `root`, reached through `anc` (the root's
+// ancestor at depth 1, or kNone when root is shallower). The reference's
+// walk visits the subtrees in node order, so a group's list is its tasks'
+// lists concatenated in task order. When the ancestor is accepted the
+// subtree is never entered and only the task first under the ancestor in
+// node order (root == anc + 1, the ancestor's last-octant child) emits it.
+struct Task {
+  u32 root, anc, first, pad;
 };
+constexpr u32 kNone = 0xffffffffu;
+
+struct WalkOut {
+  u64 *ncells, *nbodies;          // count pass, [group * ntasks + task]
+  const u64 *cell_off, *body_off; // fill pass, same indexing
+  u32 *cell_list, *body_list;
+};
+
+__device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk64, u32 i,
+                                      const float *gf, const float *hf, const double *gbox,
+                                      u32 g, u32 &exact) {
+  int verdict = accept32(r, gf, hf);
+  if (verdict == 2) {
+    double gc[3], gh[3];
+    for (int a = 0; a < 3; ++a) {
+      gc[a] = gbox[6ull * g + a];
+      gh[a] = gbox[6ull * g + 3 + a];
+    }
+    verdict = accept64(load64(walk64, i), gc, gh) ? 1 : 0;
+    ++exact;
+  }
+  return verdict;
+}
 
 template <bool kFill>
 __global__ void __launch_bounds__(kT)
-    k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, u32 m, const u32 *gbegin,
-           const u32 *gend, const double *gbox, const float *gboxf, u32 ng, WalkOut out,
+    k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
+           const float *gboxf, u32 ng, const Task *tasks, u32 ntasks, WalkOut out,
            Scalars *sc) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
+  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (tid >= static_cast<u64>(ng) * ntasks) return;
+  // consecutive threads: consecutive groups on the same task (similar walks)
+  const u32 t = static_cast<u32>(tid / ng), g = static_cast<u32>(tid % ng);
+  const u64 slot = static_cast<u64>(g) * ntasks + t;
   float gf[3], hf[3];
   for (int a = 0; a < 3; ++a) {
     gf[a] = gboxf[6ull * g + a];
@@ -210,53 +239,94 @@ __global__ void __launch_bounds__(kT)
   }
   u32 *cl = nullptr, *bl = nullptr;
   if (kFill) {
-    cl = out.cell_list + out.cell_off[g];
-    bl = out.body_list + out.body_off[g];
+    cl = out.cell_list + out.cell_off[slot];
+    bl = out.body_list + out.body_off[slot];
   }
   u32 nc = 0, nb = 0, exact = 0;
-  u32 i = 0;
-  while (i < m) {
-    const WalkRec32 r = load32(walk32, i);
-    int verdict = accept32(r, gf, hf);
-    if (verdict == 2) {
-      double gc[3], gh[3];
-      for (int a = 0; a < 3; ++a) {
-        gc[a] = gbox[6ull * g + a];
-        gh[a] = gbox[6ull * g + 3 + a];
-      }
-      verdict = accept64(load64(walk64, i), gc, gh) ? 1 : 0;
-      ++exact;
-    }
+  const Task task = tasks[t];
+  auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     if (verdict == 1 && r.nbody > kFewBodies) {
       if (kFill) cl[nc] = i;
       ++nc;
-    } else if (verdict == 1 || r.leaf) {
+    } else {
       if (kFill)
         for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
       nb += r.nbody;
-    } else {
-      ++i;
-      continue;
     }
-    if (r.skip <= i) break;  // malformed tree: never loop
-    i = r.skip;
+  };
+  bool enter = true;
+  if (task.anc != kNone) {
+    const WalkRec32 a = load32(walk32, task.anc);
+    if (decide(a, walk64, task.anc, gf, hf, gbox, g, exact) == 1) {
+      if (task.first) take(a, task.anc, 1);
+      enter = false;
+    }
   }
-  if (i < m) atomicOr(&sc->error, 1u);
-  const u32 t = gend[g] - gbegin[g];
-  if (kFill) {
-    const u64 c0 = out.cell_off[g], b0 = out.body_off[g];
-    out.groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0),
-                                      static_cast<u32>(c0 + nc));
-    out.groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + nb), 0u, 0u);
-  } else {
-    out.ncells[g] = nc;
-    out.nbodies[g] = nb;
-    atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t) * nc);
-    atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t) * nb - t);
-    atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
-    atomicMax(&sc->max_group, t);
+  if (enter) {
+    u32 i = task.root;
+    const u32 end = load32(walk32, task.root).skip;
+    while (i < end) {
+      const WalkRec32 r = load32(walk32, i);
+      const int verdict = decide(r, walk64, i, gf, hf, gbox, g, exact);
+      if (verdict == 1 || r.leaf) {
+        take(r, i, verdict);
+        if (r.skip <= i) {  // malformed tree: never loop
+          atomicOr(&sc->error, 1u);
+          break;
+        }
+        i = r.skip;
+      } else {
+        ++i;
+      }
+    }
+  }
+  if (!kFill) {
+    out.ncells[slot] = nc;
+    out.nbodies[slot] = nb;
     if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
   }
+}
+
+// Walk tasks: nodes at depth kSplitDepth, and leaves above it, in node order.
+constexpr int kSplitDepth = 2;
+
+__global__ void __launch_bounds__(kT)
+    k_task_flags(const u8 *depth, const u8 *isleaf, u32 m, u32 *flag) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  flag[p] = (depth[p] == kSplitDepth || (isleaf[p] && depth[p] < kSplitDepth)) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_task_fill(const u32 *flag, const u32 *scan, const u8 *depth, const u32 *parent, u32 m,
+                Task *tasks) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m || !flag[p]) return;
+  Task t{p, kNone, 0u, 0u};
+  if (depth[p] == kSplitDepth) {
+    t.anc = parent[p];
+    t.first = p == t.anc + 1 ? 1u : 0u;
+  }
+  tasks[scan[p]] = t;
+}
+
+// GTGroup records from the per-task offsets, and the list counters.
+__global__ void __launch_bounds__(kT)
+    k_group_records(const u32 *gbegin, const u32 *gend, u32 ng, u32 ntasks, const u64 *cell_off,
+                    const u64 *body_off, uint4 *groups, Scalars *sc) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= ng) return;
+  const u64 c0 = cell_off[static_cast<u64>(g) * ntasks],
+            c1 = cell_off[static_cast<u64>(g + 1) * ntasks];
+  const u64 b0 = body_off[static_cast<u64>(g) * ntasks],
+            b1 = body_off[static_cast<u64>(g + 1) * ntasks];
+  groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c1));
+  groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b1), 0u, 0u);
+  const u64 t = gend[g] - gbegin[g], nc = c1 - c0, nb = b1 - b0;
+  atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
+  atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
+  atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
+  atomicMax(&sc->max_group, static_cast<u32>(t));
 }
 
 void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
@@ -273,23 +343,30 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u32 n32 = static_cast<u32>(n), m = static_cast<u32>(ws.n_nodes);
   const u32 gs = static_cast<u32>(sp.group_size);
   Scalars *sc = ws.scalars.as<Scalars>();
-  ws.flags.ensure(n * 4);
-  ws.flags_scan.ensure(n * 4);
+  ws.flags.ensure(std::max<u64>(n, m) * 4);
+  ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
   u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
+  const u32 mb = ceil_div(m, kT);
+
+  // walk tasks (their count is read back with the group count)
+  ws.tasks.ensure(m * sizeof(Task));
+  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, mark);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u32(mark, mscan, m, &sc->aux, ws.scan_tmp, s);
+  k_task_fill<<<mb, kT, 0, s>>>(mark, mscan, ws.depth.as<u8>(), ws.parent.as<u32>(), m,
+                                ws.tasks.as<Task>());
+  GTC_LAUNCH_CHECK();
+
+  // groups
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
   NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
-  k_group_marks<<<ceil_div(m, kT), kT, 0, s>>>(nv, m, n32, gs, sp.pack, mark);
+  k_group_marks<<<mb, kT, 0, s>>>(nv, m, n32, gs, sp.pack, mark);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(mark, mscan, n, &sc->n_groups, ws.scan_tmp, s);
-  // group ranges (the count is at most n; sized for n so no read-back is needed)
   ws.gbegin.ensure(n * 4);
   ws.gend.ensure(n * 4);
   ws.gbox.ensure(n * 48);
   ws.gboxf.ensure(n * 24);
-  ws.gcells.ensure(n * 8);
-  ws.gbodies.ensure(n * 8);
-  ws.gcell_off.ensure(n * 8);
-  ws.gbody_off.ensure(n * 8);
   ws.groups.ensure(n * 32);
   u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
   k_group_ranges<<<ceil_div(n, kT), kT, 0, s>>>(mark, mscan, n32, gbegin, gend);
@@ -298,23 +375,35 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_LAUNCH_CHECK();
   GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
   read_scalars(ws, host, s);
-  const u32 ng = host->n_groups;
+  const u32 ng = host->n_groups, ntasks = host->aux;
   ws.n_groups = ng;
   const u32 gb = ceil_div(ng, kT);
   k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.gcell_off.as<u64>(),
-             ws.gbody_off.as<u64>(), nullptr, nullptr, ws.groups.as<uint4>()};
-  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
-  k_walk<false><<<gb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), m, gbegin,
-                                  gend, ws.gbox.as<double>(), ws.gboxf.as<float>(), ng, wo, sc);
+
+  // count pass, offsets, fill pass
+  const u64 slots = static_cast<u64>(ng) * ntasks;
+  ws.gcells.ensure(slots * 8);
+  ws.gbodies.ensure(slots * 8);
+  ws.gcell_off.ensure((slots + 1) * 8);
+  ws.gbody_off.ensure((slots + 1) * 8);
+  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr};
+  const u32 tb = ceil_div(slots, kT);
+  k_walk<false><<<tb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), ng,
+                                  ws.tasks.as<Task>(), ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
-  exclusive_scan_u64(ws.gcells.as<u64>(), ws.gcell_off.as<u64>(), ng, &sc->n_cell_list,
-                     ws.scan_tmp, s);
-  exclusive_scan_u64(ws.gbodies.as<u64>(), ws.gbody_off.as<u64>(), ng, &sc->n_body_list,
-                     ws.scan_tmp, s);
+  exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
+  exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, slots, body_off + slots, ws.scan_tmp, s);
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + slots, 8, cudaMemcpyDeviceToDevice, s));
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + slots, 8, cudaMemcpyDeviceToDevice, s));
+  k_group_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, ntasks, cell_off, body_off,
+                                    ws.groups.as<uint4>(), sc);
+  GTC_LAUNCH_CHECK();
   read_scalars(ws, host, s);
   if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
     throw RuntimeError("interaction lists too long for 32 bit offsets");
@@ -324,8 +413,9 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   wo.cell_list = ws.cell_list.as<u32>();
   wo.body_list = ws.body_list.as<u32>();
-  k_walk<true><<<gb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), m, gbegin,
-                                 gend, ws.gbox.as<double>(), ws.gboxf.as<float>(), ng, wo, sc);
+  k_walk<true><<<tb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), ng,
+                                 ws.tasks.as<Task>(), ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
 }
 

@@ -60,9 +60,9 @@ struct Workspace {
   DeviceBuffer dpos, dkey, dkey_alt, drec, drec_alt, dseg, dtmp;
   // nodes
   DeviceBuffer geom, mom, quad, delta, nbegin, nend, skip, parent, depth, nchild, isleaf,
-      arrive, walk32, walk64, cells;
+      arrive, bucket, walk32, walk64, cells;
   // groups and lists
-  DeviceBuffer gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
+  DeviceBuffer tasks, gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
       body_list;
   // scalars and reductions
   DeviceBuffer root, bbox_part, scalars;
@@ -72,6 +72,7 @@ struct Workspace {
   // host-side view of the last build
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
+  u32 *host_words = nullptr;  // pinned, for small read-backs
   void release_all();
 };
 

@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cstddef>
+#include <cstring>
 
 #include "pipeline.cuh"
 
@@ -424,18 +425,10 @@ struct MomentArrays {
   double2 *mom;     // 2 per node: (mx, my), (mz, mass)
   double2 *quad;    // 3 x double2 per node: xx yy | zz xy | xz yz
   double *delta;
-  u32 *arrive;
-  u32 *error;
 };
 
 __device__ __forceinline__ Dbl4 load_pair(const double2 *a, u32 p) {
   const double2 u = a[2 * p], v = a[2 * p + 1];
-  return make_dbl4(u.x, u.y, v.x, v.y);
-}
-
-// Uncached (L2) read of a child's moments written by another thread.
-__device__ __forceinline__ Dbl4 load_pair_cg(const double2 *a, u32 p) {
-  const double2 u = __ldcg(&a[2 * p]), v = __ldcg(&a[2 * p + 1]);
   return make_dbl4(u.x, u.y, v.x, v.y);
 }
 
@@ -492,7 +485,7 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
   const int nc = children_of(p, a.skip, ch);  // last octant first
   double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
   for (int j = nc - 1; j >= 0; --j) {
-    const Dbl4 c = load_pair_cg(a.mom, ch[j]);
+    const Dbl4 c = load_pair(a.mom, ch[j]);
     m += c.w;
     cx += c.w * c.x;
     cy += c.w * c.y;
@@ -509,9 +502,8 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
   }
   double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
   for (int j = nc - 1; j >= 0; --j) {
-    const Dbl4 c = load_pair_cg(a.mom, ch[j]);
-    const double2 qa = __ldcg(&a.quad[3 * ch[j]]), qb = __ldcg(&a.quad[3 * ch[j] + 1]),
-                  qc = __ldcg(&a.quad[3 * ch[j] + 2]);
+    const Dbl4 c = load_pair(a.mom, ch[j]);
+    const double2 qa = a.quad[3 * ch[j]], qb = a.quad[3 * ch[j] + 1], qc = a.quad[3 * ch[j] + 2];
     const double dx = c.x - cx, dy = c.y - cy, dz = c.z - cz;
     const double r2 = dx * dx + dy * dy + dz * dz;
     q0 += qa.x + c.w * (3 * dx * dx - r2);
@@ -529,25 +521,50 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
   a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
 }
 
-// One thread per leaf; the last child to finish carries on with its parent.
-__global__ void __launch_bounds__(kT) k_moments(MomentArrays a, const u8 *isleaf, u32 m) {
-  const u32 p0 = blockIdx.x * kT + threadIdx.x;
-  if (p0 >= m || !isleaf[p0]) return;
-  leaf_moments(a, p0);
-  u32 p = p0;
-  for (int level = 0; p != 0; ++level) {
-    const u32 up = a.parent[p];
-    if (up >= m || level > kMaxDepth) {  // malformed tree: record and stop
-      atomicOr(a.error, 2u);
-      return;
-    }
-    __threadfence();
-    const u32 before = atomicAdd(&a.arrive[up], 1u);
-    if (before + 1 != a.nchild[up]) return;
-    __threadfence();
-    node_moments(a, up);
-    p = up;
+// Moments bottom-up, one launch per depth: leaves first (any depth), then
+// the inner nodes of each depth from the deepest up, so every node's
+// children are complete when it is combined. Nodes are bucketed by depth
+// (bucket kLeafBucket holds the leaves); the order inside a bucket does not
+// matter, each node's sums run in the reference's order.
+constexpr int kLeafBucket = kMaxDepth + 1;
+constexpr int kBuckets = kMaxDepth + 2;
+
+__global__ void __launch_bounds__(kT)
+    k_bucket_count(const u8 *depth, const u8 *isleaf, u32 m, u32 *count) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p < m) atomicAdd(&count[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+}
+
+// offsets[b] = start of bucket b; also clears the fill counters.
+__global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill) {
+  if (threadIdx.x != 0) return;
+  u32 run = 0;
+  for (int b = 0; b < kBuckets; ++b) {
+    offset[b] = run;
+    run += count[b];
+    fill[b] = 0;
   }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_bucket_fill(const u8 *depth, const u8 *isleaf, u32 m, const u32 *offset, u32 *fill,
+                  u32 *bucket) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  const int b = isleaf[p] ? kLeafBucket : depth[p];
+  bucket[offset[b] + atomicAdd(&fill[b], 1u)] = p;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_leaf_moments(MomentArrays a, const u32 *bucket, u32 count) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k < count) leaf_moments(a, bucket[k]);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_node_moments(MomentArrays a, const u32 *bucket, u32 count) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k < count) node_moments(a, bucket[k]);
 }
 
 // --------------------------------------------------------------- packing
@@ -606,6 +623,15 @@ __global__ void __launch_bounds__(kT)
                           static_cast<float>(tpos[3ull * k + 1] - origin[1]),
                           static_cast<float>(tpos[3ull * k + 2] - origin[2]),
                           static_cast<float>(tmass[k]));
+}
+
+// Pinned host words for small read-backs (kept in the workspace).
+u32 *host_meta(Workspace &ws) {
+  if (!ws.host_words) {
+    GTC_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ws.host_words), 256 * sizeof(u32),
+                           cudaHostAllocDefault));
+  }
+  return ws.host_words;
 }
 
 const double *root_centre(const TreeRoot *root) {
@@ -760,7 +786,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   ws.depth.ensure(m);
   ws.nchild.ensure(m);
   ws.isleaf.ensure(m);
-  ws.arrive.ensure(m * 4ull);
+  ws.arrive.ensure(3 * kBuckets * sizeof(u32));
+  ws.bucket.ensure(m * 4ull);
   ws.walk32.ensure(m * sizeof(WalkRec32));
   ws.walk64.ensure(m * sizeof(WalkRec64));
   ws.cells.ensure(m * 3 * sizeof(float4));
@@ -778,13 +805,37 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   k_tree_order<<<nb, kT, 0, s>>>(pos, mass, idx, n32, ws.tpos.as<double>(), ws.tmass.as<double>());
   GTC_LAUNCH_CHECK();
 
-  GTC_CUDA(cudaMemsetAsync(ws.arrive.ptr, 0, m * 4ull, s));
+  // moments, one depth at a time from the leaves up
+  u32 *meta = ws.arrive.as<u32>();  // count[kBuckets], offset[kBuckets], fill[kBuckets]
+  u32 *bucket = ws.bucket.as<u32>();
+  GTC_CUDA(cudaMemsetAsync(meta, 0, kBuckets * sizeof(u32), s));
+  k_bucket_count<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, meta);
+  GTC_LAUNCH_CHECK();
+  k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets);
+  GTC_LAUNCH_CHECK();
+  k_bucket_fill<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, meta + kBuckets,
+                                  meta + 2 * kBuckets, bucket);
+  GTC_LAUNCH_CHECK();
+  u32 counts[2 * kBuckets];
+  GTC_CUDA(cudaMemcpyAsync(host_meta(ws), meta, 2 * kBuckets * sizeof(u32),
+                           cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(counts, host_meta(ws), sizeof counts);
   MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
                   ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
-                  ws.quad.as<double2>(), ws.delta.as<double>(), ws.arrive.as<u32>(), &sc->error};
-  k_moments<<<mb, kT, 0, s>>>(ma, ws.isleaf.as<u8>(), m);
-  GTC_LAUNCH_CHECK();
+                  ws.quad.as<double2>(), ws.delta.as<double>()};
+  {
+    const u32 c = counts[kLeafBucket], o = counts[kBuckets + kLeafBucket];
+    if (c) k_leaf_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
+    GTC_LAUNCH_CHECK();
+  }
+  for (int d = kMaxDepth; d >= 0; --d) {
+    const u32 c = counts[d], o = counts[kBuckets + d];
+    if (!c) continue;
+    k_node_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
+    GTC_LAUNCH_CHECK();
+  }
   k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
                                  ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                                  ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
