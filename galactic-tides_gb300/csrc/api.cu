@@ -493,6 +493,18 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
   });
 }
 
+gtc_status gtc_set_option(gtc_context *ctx, const char *name, int64_t value) {
+  return guarded(ctx, [&] {
+    const std::string key = name ? name : "";
+    if (key == "walk_split_depth") {
+      if (value < 0 || value > 2) throw gtc::InvalidArgument("walk_split_depth must be 0, 1 or 2");
+      ctx->ws.walk_split_depth = static_cast<int>(value);
+    } else {
+      throw gtc::InvalidArgument("unknown option '" + key + "'");
+    }
+  });
+}
+
 gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops) {
   return guarded(ctx, [&] {
     if (!tflops) throw gtc::InvalidArgument("tflops is required");

@@ -89,6 +89,7 @@ __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
 __global__ void __launch_bounds__(kT)
     k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos,
                 const TreeRoot *root, double *gbox, float *gboxf) {
+  // gboxf per group: centre (3), half-extent (3), magnitude bound, pad
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (g >= ng) return;
   const u32 b0 = gbegin[g], b1 = gend[g];
@@ -100,13 +101,19 @@ __global__ void __launch_bounds__(kT)
       lo[a] = v < lo[a] ? v : lo[a];
       hi[a] = hi[a] < v ? v : hi[a];
     }
+  float gmax = 0.f, hmax = 0.f;
   for (int a = 0; a < 3; ++a) {
     const double c = (lo[a] + hi[a]) * 0.5, h = (hi[a] - lo[a]) * 0.5;
     gbox[6ull * g + a] = c;
     gbox[6ull * g + 3 + a] = h;
-    gboxf[6ull * g + a] = static_cast<float>(c - root->center[a]);
-    gboxf[6ull * g + 3 + a] = static_cast<float>(h);
+    const float cf = static_cast<float>(c - root->center[a]), hf = static_cast<float>(h);
+    gboxf[8ull * g + a] = cf;
+    gboxf[8ull * g + 3 + a] = hf;
+    gmax = fmaxf(gmax, fabsf(cf));
+    hmax = fmaxf(hmax, hf);
   }
+  gboxf[8ull * g + 6] = (gmax + hmax) * (1.0f + 1.0f / (1 << 20));
+  gboxf[8ull * g + 7] = 0.f;
 }
 
 // The opening test of group_lists.cpp:145-154 for one node, in FP64 exactly
@@ -126,40 +133,39 @@ __device__ __forceinline__ bool accept64(const WalkRec64 &r, const double *gc, c
   return !overlap && d2 > r.crit2;
 }
 
-// The same test in FP32 with a rigorous error bound. Every FP32 input is the
-// FP64 quantity rounded once (relative error 2^-24), and each FP32 result
-// below is within a few 2^-24 of the value computed from the exact inputs;
-// the band kBand = 2^-20 (relative to the magnitudes involved) is several
-// times wider than all of that plus the FP64 roundings. A comparison whose
-// two sides are further apart than the band has the same outcome in FP64;
-// otherwise the result is "undecided" and the caller runs the FP64 test.
-// Returns 1 accept, 0 open, 2 undecided. NaNs come out undecided.
+// The same test in FP32 with a rigorous error band. Every FP32 input is the
+// FP64 quantity (relative to the root centre) rounded once; the node record
+// carries B_n >= all its |values| + slack and the group B_g >= max|centre| +
+// max half-extent, so every quantity compared below is at most ~2 (B_n + B_g)
+// in size and each FP32 result is within 5 * 2^-24 (B_n + B_g) of the value
+// from the exact inputs (more than the FP64 roundings too). The band
+// E = 2^-20 (B_n + B_g) is over three times that: a comparison whose sides
+// differ by more than E has the FP64 outcome; otherwise the caller runs the
+// FP64 test. Returns 1 accept, 0 open, 2 undecided (NaNs end up undecided).
 constexpr float kBand = 1.0f / (1 << 20);
 
-__device__ __forceinline__ int accept32(const WalkRec32 &r, const float *gf, const float *hf) {
-  // overlap: on every axis |c - g| <= slack + gh (group_lists.cpp:147)
-  int separated = 0, within = 0;
+__device__ __forceinline__ int accept32(const WalkRec32 &r, const float *gf, const float *hf,
+                                        float gbound) {
+  const float e = kBand * (r.bound + gbound);
+  bool separated = false, within = true;
   float lo2 = 0.f, hi2 = 0.f;
   const float c[3] = {r.cx, r.cy, r.cz}, mm[3] = {r.mx, r.my, r.mz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
+    // overlap: on every axis |c - g| <= slack + gh (group_lists.cpp:147)
     const float x = fabsf(c[a] - gf[a]), y = r.slack + hf[a];
-    const float e = kBand * (fabsf(c[a]) + fabsf(gf[a]) + x + y);
     separated |= x > y + e;
-    within += x < y - e;
+    within &= x < y - e;
     // distance from the box to the centre of mass (group_lists.cpp:150-151)
     const float d = fabsf(mm[a] - gf[a]) - hf[a];
-    const float ed = kBand * (fabsf(mm[a]) + fabsf(gf[a]) + hf[a] + fabsf(d));
-    const float dl = d - ed, dh = d + ed;
-    lo2 += dl > 0.f ? dl * dl : 0.f;
-    hi2 += dh > 0.f ? dh * dh : 0.f;
+    const float dl = fmaxf(d - e, 0.f), dh = fmaxf(d + e, 0.f);
+    lo2 = fmaf(dl, dl, lo2);
+    hi2 = fmaf(dh, dh, hi2);
   }
-  lo2 *= 1.f - 4.f * kBand;
-  hi2 *= 1.f + 4.f * kBand;
   const float c2 = r.crit2;
-  if (within == 3) return 0;                       // overlaps: opened
-  if (hi2 < c2 * (1.f - 4.f * kBand)) return 0;    // too close: opened
-  if (separated && lo2 > c2 * (1.f + 4.f * kBand)) return 1;
+  if (within) return 0;                                      // overlaps: opened
+  if (hi2 * (1.f + 4.f * kBand) < c2 * (1.f - 4.f * kBand)) return 0;  // too close
+  if (separated && lo2 * (1.f - 4.f * kBand) > c2 * (1.f + 4.f * kBand)) return 1;
   return 2;
 }
 
@@ -177,9 +183,9 @@ __device__ __forceinline__ WalkRec32 load32(const WalkRec32 *w, u32 i) {
   r.mz = b.z;
   r.crit2 = b.w;
   r.skip = c.x;
-  r.nbody = c.y;
+  r.nbody_leaf = c.y;
   r.begin = c.z;
-  r.leaf = c.w;
+  r.bound = __uint_as_float(c.w);
   return r;
 }
 
@@ -207,9 +213,9 @@ struct WalkOut {
 };
 
 __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk64, u32 i,
-                                      const float *gf, const float *hf, const double *gbox,
-                                      u32 g, u32 &exact) {
-  int verdict = accept32(r, gf, hf);
+                                      const float *gf, const float *hf, float gbound,
+                                      const double *gbox, u32 g, u32 &exact) {
+  int verdict = accept32(r, gf, hf, gbound);
   if (verdict == 2) {
     double gc[3], gh[3];
     for (int a = 0; a < 3; ++a) {
@@ -232,11 +238,10 @@ __global__ void __launch_bounds__(kT)
   // consecutive threads: consecutive groups on the same task (similar walks)
   const u32 t = static_cast<u32>(tid / ng), g = static_cast<u32>(tid % ng);
   const u64 slot = static_cast<u64>(g) * ntasks + t;
-  float gf[3], hf[3];
-  for (int a = 0; a < 3; ++a) {
-    gf[a] = gboxf[6ull * g + a];
-    hf[a] = gboxf[6ull * g + 3 + a];
-  }
+  const float4 b0 = reinterpret_cast<const float4 *>(gboxf)[2ull * g],
+               b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
+  const float gf[3] = {b0.x, b0.y, b0.z}, hf[3] = {b0.w, b1.x, b1.y};
+  const float gbound = b1.z;
   u32 *cl = nullptr, *bl = nullptr;
   if (kFill) {
     cl = out.cell_list + out.cell_off[slot];
@@ -245,19 +250,20 @@ __global__ void __launch_bounds__(kT)
   u32 nc = 0, nb = 0, exact = 0;
   const Task task = tasks[t];
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
-    if (verdict == 1 && r.nbody > kFewBodies) {
+    const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+    if (verdict == 1 && nbody > kFewBodies) {
       if (kFill) cl[nc] = i;
       ++nc;
     } else {
       if (kFill)
-        for (u32 j = 0; j < r.nbody; ++j) bl[nb + j] = r.begin + j;
-      nb += r.nbody;
+        for (u32 j = 0; j < nbody; ++j) bl[nb + j] = r.begin + j;
+      nb += nbody;
     }
   };
   bool enter = true;
   if (task.anc != kNone) {
     const WalkRec32 a = load32(walk32, task.anc);
-    if (decide(a, walk64, task.anc, gf, hf, gbox, g, exact) == 1) {
+    if (decide(a, walk64, task.anc, gf, hf, gbound, gbox, g, exact) == 1) {
       if (task.first) take(a, task.anc, 1);
       enter = false;
     }
@@ -267,8 +273,8 @@ __global__ void __launch_bounds__(kT)
     const u32 end = load32(walk32, task.root).skip;
     while (i < end) {
       const WalkRec32 r = load32(walk32, i);
-      const int verdict = decide(r, walk64, i, gf, hf, gbox, g, exact);
-      if (verdict == 1 || r.leaf) {
+      const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
+      if (verdict == 1 || (r.nbody_leaf >> 31)) {
         take(r, i, verdict);
         if (r.skip <= i) {  // malformed tree: never loop
           atomicOr(&sc->error, 1u);
@@ -287,14 +293,14 @@ __global__ void __launch_bounds__(kT)
   }
 }
 
-// Walk tasks: nodes at depth kSplitDepth, and leaves above it, in node order.
-constexpr int kSplitDepth = 2;
-
+// Walk tasks: nodes at depth `split` (0..2), and leaves above it, in node
+// order. The root is never accepted (every group lies inside it), so only a
+// depth-2 task has an ancestor to test.
 __global__ void __launch_bounds__(kT)
-    k_task_flags(const u8 *depth, const u8 *isleaf, u32 m, u32 *flag) {
+    k_task_flags(const u8 *depth, const u8 *isleaf, u32 m, int split, u32 *flag) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p >= m) return;
-  flag[p] = (depth[p] == kSplitDepth || (isleaf[p] && depth[p] < kSplitDepth)) ? 1u : 0u;
+  flag[p] = (depth[p] == split || (isleaf[p] && depth[p] < split)) ? 1u : 0u;
 }
 
 __global__ void __launch_bounds__(kT)
@@ -303,7 +309,7 @@ __global__ void __launch_bounds__(kT)
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p >= m || !flag[p]) return;
   Task t{p, kNone, 0u, 0u};
-  if (depth[p] == kSplitDepth) {
+  if (depth[p] == 2) {
     t.anc = parent[p];
     t.first = p == t.anc + 1 ? 1u : 0u;
   }
@@ -350,7 +356,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
 
   // walk tasks (their count is read back with the group count)
   ws.tasks.ensure(m * sizeof(Task));
-  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, mark);
+  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, ws.walk_split_depth,
+                                 mark);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(mark, mscan, m, &sc->aux, ws.scan_tmp, s);
   k_task_fill<<<mb, kT, 0, s>>>(mark, mscan, ws.depth.as<u8>(), ws.parent.as<u32>(), m,
@@ -366,7 +373,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gbegin.ensure(n * 4);
   ws.gend.ensure(n * 4);
   ws.gbox.ensure(n * 48);
-  ws.gboxf.ensure(n * 24);
+  ws.gboxf.ensure(n * 32);
   ws.groups.ensure(n * 32);
   u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
   k_group_ranges<<<ceil_div(n, kT), kT, 0, s>>>(mark, mscan, n32, gbegin, gend);

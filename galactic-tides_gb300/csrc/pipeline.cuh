@@ -37,7 +37,10 @@ struct TreeRoot {
 struct alignas(16) WalkRec32 {
   float cx, cy, cz, slack;   // centre relative to the root centre; half * 1.0001
   float mx, my, mz, crit2;   // centre of mass relative to the root centre; crit^2
-  u32 skip, nbody, begin, leaf;
+  u32 skip;                  // first node after this node's subtree
+  u32 nbody_leaf;            // bodies in the node | 0x80000000 for a leaf
+  u32 begin;                 // first body (tree order)
+  float bound;               // >= every |value| above plus slack (error bound scale)
 };
 struct alignas(16) WalkRec64 {
   double cx, cy, cz, slack;  // slack = half * 1.0001 (group_lists.cpp:147)
@@ -73,6 +76,7 @@ struct Workspace {
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
   u32 *host_words = nullptr;  // pinned, for small read-backs
+  int walk_split_depth = 2;   // tuning: subtree depth of the walk tasks (0..2)
   void release_all();
 };
 

@@ -529,10 +529,17 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
 constexpr int kLeafBucket = kMaxDepth + 1;
 constexpr int kBuckets = kMaxDepth + 2;
 
+// Per-block histograms in shared memory, one global atomic per bucket.
 __global__ void __launch_bounds__(kT)
     k_bucket_count(const u8 *depth, const u8 *isleaf, u32 m, u32 *count) {
+  __shared__ u32 h[kBuckets];
+  for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
+  __syncthreads();
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p < m) atomicAdd(&count[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+  if (p < m) atomicAdd(&h[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kBuckets; b += kT)
+    if (h[b]) atomicAdd(&count[b], h[b]);
 }
 
 // offsets[b] = start of bucket b; also clears the fill counters.
@@ -546,13 +553,25 @@ __global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill) {
   }
 }
 
+// Each block reserves one range per bucket, then places its nodes in it.
 __global__ void __launch_bounds__(kT)
     k_bucket_fill(const u8 *depth, const u8 *isleaf, u32 m, const u32 *offset, u32 *fill,
                   u32 *bucket) {
+  __shared__ u32 h[kBuckets], base[kBuckets];
+  for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
+  __syncthreads();
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p >= m) return;
-  const int b = isleaf[p] ? kLeafBucket : depth[p];
-  bucket[offset[b] + atomicAdd(&fill[b], 1u)] = p;
+  int b = -1;
+  u32 local = 0;
+  if (p < m) {
+    b = isleaf[p] ? kLeafBucket : depth[p];
+    local = atomicAdd(&h[b], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kBuckets; k += kT)
+    base[k] = h[k] ? offset[k] + atomicAdd(&fill[k], h[k]) : 0;
+  __syncthreads();
+  if (b >= 0) bucket[base[b] + local] = p;
 }
 
 __global__ void __launch_bounds__(kT)
@@ -601,9 +620,12 @@ __global__ void __launch_bounds__(kT)
   f.mz = static_cast<float>(c.z - oz);
   f.crit2 = static_cast<float>(r.crit2);
   f.skip = skip[p];
-  f.nbody = nend[p] - nbegin[p];
+  f.nbody_leaf = (nend[p] - nbegin[p]) | (isleaf[p] ? 0x80000000u : 0u);
   f.begin = nbegin[p];
-  f.leaf = isleaf[p];
+  // magnitude bound of this record's FP32 values, rounded up
+  const float mag = fmaxf(fmaxf(fmaxf(fabsf(f.cx), fabsf(f.cy)), fmaxf(fabsf(f.cz), fabsf(f.mx))),
+                          fmaxf(fabsf(f.my), fabsf(f.mz)));
+  f.bound = (mag + f.slack) * (1.0f + 1.0f / (1 << 20));
   walk32[p] = f;
   const double2 qa = quad[3 * p], qb = quad[3 * p + 1], qc = quad[3 * p + 2];
   cells[3 * p] = make_float4(static_cast<float>(c.x - ox), static_cast<float>(c.y - oy),

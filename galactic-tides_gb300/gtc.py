@@ -83,6 +83,7 @@ def _load():
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
+        "gtc_set_option": (I, [V, C.c_char_p, C.c_int64]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -221,6 +222,9 @@ class Context:
                                                acc_ptr, pot_ptr))
 
     # ---- introspection -----------------------------------------------------
+
+    def set_option(self, name, value):
+        self._check(lib.gtc_set_option(self.h, name.encode(), int(value)))
 
     def fp32_peak_tflops(self):
         v = C.c_double()

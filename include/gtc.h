@@ -178,7 +178,13 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
 
-/* ---- diagnostics (no reference counterpart) ----------------------------- */
+/* ---- tuning and diagnostics (no reference counterpart) ------------------ */
+
+/* Sets a tuning option of the context (results do not depend on them):
+ *   "walk_split_depth"  0, 1 or 2 (default 2): each group's walk runs as
+ *                       independent tasks, one per subtree at this depth.
+ * GTC_INVALID_ARGUMENT for an unknown name or a value out of range. */
+gtc_status gtc_set_option(gtc_context *ctx, const char *name, int64_t value);
 
 /* Measured FP32 FMA throughput of this GPU in TFLOP/s (one FMA = 2 flops):
  * the roofline denominator for the FP32 evaluation kernels. */
