@@ -76,7 +76,7 @@ struct Workspace {
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
   u32 *host_words = nullptr;  // pinned, for small read-backs
-  int walk_split_depth = 2;   // tuning: subtree depth of the walk tasks (0..2)
+  int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
   void release_all();
 };
 
