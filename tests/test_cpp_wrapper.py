@@ -1,0 +1,48 @@
+"""The C++ wrapper (galactic-tides_gb300/host/gtc.hpp): a C++ program in the
+reference's test style, built with g++ against libgtc.so and the oracle, run
+on the GPU; and, where the reference's headers are present, a compile check of
+the drop-in backend shown in INTEGRATION.md against them."""
+
+import pathlib
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+PKG = ROOT / "galactic-tides_gb300"
+REF_INCLUDE = pathlib.Path("/root/reference/include")
+
+
+def compile_cpp(src, out, extra=()):
+    cmd = ["g++", "-std=c++17", "-O2", str(src), "-o", str(out), f"-I{ROOT / 'include'}",
+           f"-I{PKG / 'host'}", f"-L{PKG}", "-lgtc", f"-Wl,-rpath,{PKG}", *extra]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+
+
+@pytest.mark.gpu
+def test_cpp_wrapper_program(tmp_path):
+    exe = tmp_path / "test_host_wrapper"
+    compile_cpp(ROOT / "tests" / "cpp" / "test_host_wrapper.cpp", exe,
+                [f"-L{ROOT / 'oracle'}", "-loracle", f"-Wl,-rpath,{ROOT / 'oracle'}"])
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all checks passed" in r.stdout
+
+
+@pytest.mark.skipif(not (REF_INCLUDE / "galactic_tides" / "integrator.h").exists(),
+                    reason="needs the reference's headers")
+def test_integration_snippet_compiles_against_reference(tmp_path):
+    """The CudaGroupGravity / CudaDirectGravity classes of INTEGRATION.md,
+    compiled against the reference's own ForceModel and Particles."""
+    text = (ROOT / "INTEGRATION.md").read_text()
+    start = text.index("```cpp\n// gravity_backends_cuda.cpp") + len("```cpp\n")
+    code = text[start:text.index("```", start)]
+    src = tmp_path / "gravity_backends_cuda.cpp"
+    src.write_text(code)
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    cmd = ["g++", "-std=c++17", "-c", str(src), "-o", str(tmp_path / "x.o"),
+           f"-I{REF_INCLUDE}", f"-I{ROOT / 'include'}", f"-I{PKG / 'host'}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
