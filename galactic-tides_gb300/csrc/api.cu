@@ -230,6 +230,8 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
 }  // namespace
 
 namespace gtc {
+void set_contextless_error(const std::string &msg) { g_create_error = msg; }
+
 // Caller-order scatter for the direct path (identity order).
 __global__ void k_unpack_direct(const float4 *out, u32 n, double *acc, double *pot) {
   const u32 i = blockIdx.x * 256 + threadIdx.x;

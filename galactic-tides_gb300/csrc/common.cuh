@@ -43,6 +43,9 @@ void count_launch();
   } while (0)
 unsigned long long launches_so_far();
 
+// Message returned by gtc_last_error(NULL) (calls made without a context).
+void set_contextless_error(const std::string &msg);
+
 // ------------------------------------------------------- device buffers
 // Grow-only device allocation, kept between calls.
 struct DeviceBuffer {

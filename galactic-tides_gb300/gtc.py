@@ -84,6 +84,7 @@ def _load():
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
         "gtc_set_option": (I, [V, C.c_char_p, C.c_int64]),
+        "gtc_direct_fp64_noalloc": (I, [P, P, U64, P, U64, D, D, P, P, V]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -112,6 +113,18 @@ def gravity_params(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32,
                    pack=True, criterion=CRITERION_THETA):
     return GravityParams(G, theta, eps, int(quadrupole), group_size, leaf_size, int(pack),
                          criterion, (C.c_int32 * 3)(0, 0, 0))
+
+
+def direct_fp64_noalloc(pos_ptr, mass_ptr, n, idx_ptr, m, acc_ptr, pot_ptr, G=1.0, eps=0.025,
+                        stream=None):
+    """gtc_direct_fp64_noalloc: FP64 sampled sums with no allocation and no
+    context, enqueued on `stream` (a cudaStream_t handle, None for the default
+    stream); the caller synchronizes."""
+    rc = lib.gtc_direct_fp64_noalloc(pos_ptr, mass_ptr, n, idx_ptr, m, G, eps, acc_ptr, pot_ptr,
+                                     stream)
+    if rc != GTC_OK:
+        raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(
+            rc, lib.gtc_last_error(None).decode())
 
 
 class Context:

@@ -123,7 +123,8 @@ typedef struct gtc_stats {
  * none). Replaces metal::Context::Context (metal_backend.mm:122-160). */
 gtc_status gtc_create(gtc_context **ctx, int device);
 void gtc_destroy(gtc_context *ctx);
-/* Message of the last failed call on ctx (or of gtc_create when ctx is NULL). */
+/* Message of the last failed call on ctx; with ctx NULL, of the last failed
+ * call made without a context (gtc_create, gtc_direct_fp64_noalloc). */
 const char *gtc_last_error(const gtc_context *ctx);
 const char *gtc_status_name(gtc_status s);
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
@@ -175,6 +176,25 @@ gtc_status gtc_direct_force_device(gtc_context *ctx, const double *pos, const do
 gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const double *mass,
                                   uint64_t n, const uint64_t *idx, uint64_t m, double G,
                                   double eps, double *acc, double *pot);
+
+/* The same FP64 sampled sums for callers that cannot allocate device memory:
+ * code inside another framework whose caching allocator has reserved the
+ * GPU's memory (a cudaMalloc of ours would fail or fragment that pool), and
+ * timing-critical loops where cudaMalloc/cudaFree would synchronize the
+ * device. No reference counterpart. Needs no context and allocates nothing:
+ * the per-slice partial sums live in one fixed 8 MiB device array inside
+ * libgtc.so, held by every GPU that loads the library until exit. At most
+ * 262144 sample targets (m); larger m is refused (GTC_INVALID_ARGUMENT).
+ * idx values must be < n. Enqueued on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) without waiting; the results are ready when the
+ * stream reaches that point. The first call on a device looks up the array's
+ * address (once per device, on the current device): make it before any
+ * stream capture. All calls share the array and it keeps the last call's
+ * contents (each call writes every slot it reads, nothing needs clearing);
+ * calls that overlap on the GPU race on it. Errors: gtc_last_error(NULL). */
+gtc_status gtc_direct_fp64_noalloc(const double *pos, const double *mass, uint64_t n,
+                                   const uint64_t *idx, uint64_t m, double G, double eps,
+                                   double *acc, double *pot, void *stream);
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
 
