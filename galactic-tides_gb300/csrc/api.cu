@@ -2,32 +2,19 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "../../include/gtc.h"
-#include "pipeline.cuh"
+#include "context.cuh"
 
 static_assert(sizeof(gtc_float4) == 16 && alignof(gtc_float4) == 16, "float4 layout");
 static_assert(sizeof(gtc_kernel_params) == 32, "GTParams layout");
 static_assert(sizeof(gtc_cell) == 48, "GTCell layout");
 static_assert(sizeof(gtc_group) == 32, "GTGroup layout");
-
-struct gtc_context {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[6] = {};
-  std::string error;
-  gtc_stats stats{};
-  gtc::Workspace ws;
-  gtc::Scalars *host_sc = nullptr;  // pinned
-  gtc::DeviceBuffer counter;        // evaluator work queue
-  gtc::DeviceBuffer sample_scratch; // FP64 sample partial sums
-  bool have_group = false;
-  gtc::SolverParams last{};
-};
 
 namespace gtc {
 
@@ -117,7 +104,7 @@ gtc::SolverParams check_params(const gtc_gravity_params *gp, bool group) {
   if (!gp) throw gtc::InvalidArgument("gravity parameters are required");
   gtc::SolverParams sp{gp->G, gp->theta, gp->eps, gp->quadrupole != 0 ? 1 : 0,
                        gp->group_size, std::max(1, gp->leaf_size), gp->pack < 0 ? 1 : gp->pack,
-                       gp->criterion};
+                       gp->criterion, gp->alpha};
   if (group) {
     if (sp.group_size < 1) throw gtc::InvalidArgument("group_size must be at least 1");
     if (sp.group_size > gtc::kMaxGroupSize)
@@ -125,8 +112,8 @@ gtc::SolverParams check_params(const gtc_gravity_params *gp, bool group) {
     if (!(sp.theta > 0)) throw gtc::InvalidArgument("theta must be positive");
     if (sp.criterion != GTC_CRITERION_THETA && sp.criterion != GTC_CRITERION_LEARNED)
       throw gtc::InvalidArgument("unknown opening criterion");
-    if (sp.criterion == GTC_CRITERION_LEARNED)
-      throw gtc::InvalidArgument("the learned criterion needs a trained model (none loaded)");
+    if (sp.criterion == GTC_CRITERION_LEARNED && !(sp.alpha > 0 && std::isfinite(sp.alpha)))
+      throw gtc::InvalidArgument("the learned criterion needs a positive alpha");
   }
   return sp;
 }
@@ -152,10 +139,33 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     ctx->last = sp;
     return;
   }
+  // The learned walk needs a model and |a| of a previous solve of the same
+  // bodies; otherwise the theta walk runs (the fallback).
+  const bool learned = sp.criterion == GTC_CRITERION_LEARNED && ctx->have_model &&
+                       ctx->prev_n == n;
   GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
   gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
   GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
-  gtc::build_lists(ws, sp, s, ctx->host_sc);
+  if (learned) {
+    gtc::learned_node_features(ws, ctx->cfeat, s);
+    gtc::LearnedWalk lw;
+    lw.net = ctx->net.as<gtc::LearnedNet>();
+    lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
+    lw.gtol = &ctx->gtol;
+    lw.scratch = &ctx->walk_scratch;
+    lw.lane_cells = &ctx->lane_cells;
+    lw.lane_runs = &ctx->lane_runs;
+    lw.split_depth = ctx->learned_split;
+    lw.prev_amag = ctx->prev_amag.as<float>();
+    lw.alpha = sp.alpha;
+    lw.G = sp.G;
+    lw.inv_theta_guard = static_cast<float>(1.0 / ctx->guard_theta);
+    lw.band = ctx->band_override >= 0 ? static_cast<float>(ctx->band_override) : ctx->model_band;
+    lw.batch_min = ctx->batch_min;
+    gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
+  } else {
+    gtc::build_lists(ws, sp, s, ctx->host_sc);
+  }
   GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
   if (n > 0) {
     ws.out.ensure(n * sizeof(float4));
@@ -167,6 +177,11 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
                         sp.quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
     GTC_CUDA(cudaEventRecord(ctx->ev[5], s));
     gtc::scatter_results(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, s);
+    if (ctx->have_model) {  // |a| for the next learned solve
+      ctx->prev_amag.ensure(n * sizeof(float));
+      gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
+                               ctx->prev_amag.as<float>(), s);
+    }
   }
   GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
   GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
@@ -174,6 +189,8 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   GTC_CUDA(cudaStreamSynchronize(s));
   if (ctx->host_sc->error & 4u)
     throw gtc::InvalidArgument("cuda: positions must be finite");
+  if (ctx->host_sc->error & 8u)
+    throw gtc::RuntimeError("cuda: the learned walk's count and fill passes disagree");
   if (ctx->host_sc->error != 0)
     throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
                             std::to_string(ctx->host_sc->error) + ")");
@@ -192,7 +209,11 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     st.max_group = h.max_group;
     st.depth = h.depth;
     st.walk_tests_fp64 = h.fp64_tests;
+    st.mlp_rows = h.mlp_rows;
+    st.mlp_batches = h.mlp_batches;
   }
+  st.criterion_used = learned ? GTC_CRITERION_LEARNED : GTC_CRITERION_THETA;
+  ctx->prev_n = ctx->have_model ? n : 0;
   st.n_cell_list = ws.n_cell_list;
   st.n_body_list = ws.n_body_list;
   st.n_nodes = static_cast<u32>(ws.n_nodes);
@@ -302,6 +323,11 @@ void gtc_destroy(gtc_context *ctx) {
   ctx->ws.release_all();
   ctx->counter.release();
   ctx->sample_scratch.release();
+  for (gtc::DeviceBuffer *b : {&ctx->samples.feat, &ctx->samples.label, &ctx->samples.pair,
+                               &ctx->model, &ctx->net,
+                               &ctx->train_scratch, &ctx->cfeat, &ctx->gtol, &ctx->walk_scratch,
+                               &ctx->prev_amag})
+    b->release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
@@ -495,12 +521,27 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
   });
 }
 
-gtc_status gtc_set_option(gtc_context *ctx, const char *name, int64_t value) {
+gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
   return guarded(ctx, [&] {
     const std::string key = name ? name : "";
+    if (!std::isfinite(value)) throw gtc::InvalidArgument("option values must be finite");
     if (key == "walk_split_depth") {
-      if (value < 0 || value > 2) throw gtc::InvalidArgument("walk_split_depth must be 0, 1 or 2");
+      if (value != std::floor(value) || value < 0 || value > 2)
+        throw gtc::InvalidArgument("walk_split_depth must be 0, 1 or 2");
       ctx->ws.walk_split_depth = static_cast<int>(value);
+    } else if (key == "learned_guard_theta") {
+      if (!(value > 0)) throw gtc::InvalidArgument("learned_guard_theta must be positive");
+      ctx->guard_theta = value;
+    } else if (key == "learned_band") {
+      ctx->band_override = value;
+    } else if (key == "learned_split_depth") {
+      if (value != std::floor(value) || value < 0 || value > 3)
+        throw gtc::InvalidArgument("learned_split_depth must be 0..3");
+      ctx->learned_split = static_cast<int>(value);
+    } else if (key == "learned_batch_min") {
+      if (value != std::floor(value) || value < 1 || value > 32)
+        throw gtc::InvalidArgument("learned_batch_min must be 1..32");
+      ctx->batch_min = static_cast<int>(value);
     } else {
       throw gtc::InvalidArgument("unknown option '" + key + "'");
     }
@@ -511,6 +552,171 @@ gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops) {
   return guarded(ctx, [&] {
     if (!tflops) throw gtc::InvalidArgument("tflops is required");
     *tflops = gtc::fp32_peak_tflops(ctx->stream);
+  });
+}
+
+// ---------------------------------------------------- learned criterion
+
+gtc_status gtc_learned_add_samples(gtc_context *ctx, const double *pos, const double *mass,
+                                   uint64_t n, const gtc_gravity_params *gp, double theta_gen,
+                                   double theta_guard, uint64_t max_new,
+                                   uint32_t max_cell_bodies, uint64_t *added) {
+  return guarded(ctx, [&] {
+    if (!added) throw gtc::InvalidArgument("added is required");
+    *added = 0;
+    if (!gp) throw gtc::InvalidArgument("gravity parameters are required");
+    gtc_gravity_params p = *gp;
+    p.criterion = GTC_CRITERION_THETA;  // the groups come from the theta walk's set-up
+    const gtc::SolverParams sp = check_params(&p, true);
+    if (!(theta_gen > 0) || !(theta_guard > 0))
+      throw gtc::InvalidArgument("theta_gen and theta_guard must be positive");
+    if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the 32 bit GPU indices");
+    if (n == 0) return;
+    if (!pos || !mass) throw gtc::InvalidArgument("pos and mass are required");
+    gtc::Workspace &ws = ctx->ws;
+    cudaStream_t s = ctx->stream;
+    ws.pos.ensure(n * 24);
+    ws.mass.ensure(n * 8);
+    GTC_CUDA(cudaMemcpyAsync(ws.pos.ptr, pos, n * 24, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemcpyAsync(ws.mass.ptr, mass, n * 8, cudaMemcpyHostToDevice, s));
+    ctx->have_group = false;
+    gtc::learned_add_samples(ctx, ws.pos.as<double>(), ws.mass.as<double>(), n, sp, theta_gen,
+                             theta_guard, max_new, max_cell_bodies, added);
+    if (ctx->host_sc->error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
+  });
+}
+
+gtc_status gtc_learned_sample_count(const gtc_context *ctx, uint64_t *count) {
+  if (!ctx || !count) return GTC_INVALID_ARGUMENT;
+  *count = ctx->samples.count;
+  return GTC_OK;
+}
+
+gtc_status gtc_learned_export_samples(gtc_context *ctx, uint64_t first, uint64_t count,
+                                      float *feat, float *label, uint32_t *pairs) {
+  return guarded(ctx, [&] {
+    const gtc::LearnedSet &set = ctx->samples;
+    if (first > set.count || count > set.count - first)
+      throw gtc::InvalidArgument("sample range out of bounds");
+    if (count == 0) return;
+    cudaStream_t s = ctx->stream;
+    if (feat)
+      GTC_CUDA(cudaMemcpyAsync(feat, set.feat.as<float>() + first * gtc::kFeat,
+                               count * gtc::kFeat * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (label)
+      GTC_CUDA(cudaMemcpyAsync(label, set.label.as<float>() + first, count * sizeof(float),
+                               cudaMemcpyDeviceToHost, s));
+    if (pairs)
+      GTC_CUDA(cudaMemcpyAsync(pairs, set.pair.as<uint2>() + first, count * sizeof(uint2),
+                               cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+gtc_status gtc_learned_clear_samples(gtc_context *ctx) {
+  return guarded(ctx, [&] { ctx->samples.count = 0; });
+}
+
+gtc_status gtc_learned_train(gtc_context *ctx, uint64_t steps, uint32_t batch, float lr,
+                             uint64_t seed, int init, double *loss) {
+  return guarded(ctx, [&] {
+    const gtc::LearnedSet &set = ctx->samples;
+    if (set.count == 0) throw gtc::InvalidArgument("no training samples");
+    if (batch == 0 || batch > (1u << 20)) throw gtc::InvalidArgument("batch must be 1..2^20");
+    if (!(lr >= 0) || !std::isfinite(lr)) throw gtc::InvalidArgument("lr must be finite and >= 0");
+    if (init || !ctx->have_model) gtc::learned_init_model(ctx, seed);
+    const double l = gtc::learned_train_on(ctx, set.feat.as<float>(), set.label.as<float>(),
+                                           set.count, steps, batch, lr, seed, nullptr, nullptr);
+    gtc::learned_update_band(ctx, 0.999);
+    if (loss) *loss = l;
+  });
+}
+
+gtc_status gtc_learned_gradient(gtc_context *ctx, const float *model, const float *feat,
+                                const float *label, uint32_t n, float *grad, double *loss) {
+  return guarded(ctx, [&] {
+    if (!model || !grad || (n && (!feat || !label)))
+      throw gtc::InvalidArgument("model, feat, label and grad are required");
+    if (n == 0 || n > (1u << 20)) throw gtc::InvalidArgument("n must be 1..2^20");
+    cudaStream_t s = ctx->stream;
+    std::vector<float> saved;
+    const bool had = ctx->have_model;
+    if (had) {
+      saved.resize(gtc::kModelFloats);
+      GTC_CUDA(cudaMemcpyAsync(saved.data(), ctx->model.ptr, gtc::kModelFloats * sizeof(float),
+                               cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+    }
+    gtc::DeviceBuffer f, l, idx;
+    struct Release {
+      gtc::DeviceBuffer *b[3];
+      ~Release() {
+        for (gtc::DeviceBuffer *x : b) x->release();
+      }
+    } release{{&f, &l, &idx}};
+    f.ensure(static_cast<u64>(n) * gtc::kFeat * sizeof(float));
+    l.ensure(static_cast<u64>(n) * sizeof(float));
+    idx.ensure(static_cast<u64>(n) * sizeof(u32));
+    std::vector<u32> order(n);
+    for (u32 i = 0; i < n; ++i) order[i] = i;
+    GTC_CUDA(cudaMemcpyAsync(f.ptr, feat, static_cast<u64>(n) * gtc::kFeat * sizeof(float),
+                             cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemcpyAsync(l.ptr, label, static_cast<u64>(n) * sizeof(float),
+                             cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaMemcpyAsync(idx.ptr, order.data(), static_cast<u64>(n) * sizeof(u32),
+                             cudaMemcpyHostToDevice, s));
+    gtc::learned_set_model(ctx, model);
+    double lv = 0;
+    try {
+      lv = gtc::learned_train_on(ctx, f.as<float>(), l.as<float>(), n, 1, n, 0.f, 0,
+                                 idx.as<u32>(), grad);
+    } catch (...) {
+      if (had) gtc::learned_set_model(ctx, saved.data());
+      else ctx->have_model = false;
+      throw;
+    }
+    if (had) gtc::learned_set_model(ctx, saved.data());
+    else ctx->have_model = false;
+    if (loss) *loss = lv;
+  });
+}
+
+gtc_status gtc_learned_set_model(gtc_context *ctx, const float *model) {
+  return guarded(ctx, [&] {
+    if (!model) throw gtc::InvalidArgument("model is required");
+    gtc::learned_set_model(ctx, model);
+  });
+}
+
+gtc_status gtc_learned_get_model(gtc_context *ctx, float *model) {
+  return guarded(ctx, [&] {
+    if (!model) throw gtc::InvalidArgument("model is required");
+    if (!ctx->have_model) throw gtc::InvalidArgument("the context has no model");
+    GTC_CUDA(cudaMemcpyAsync(model, ctx->model.ptr, gtc::kModelFloats * sizeof(float),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+gtc_status gtc_learned_predict(gtc_context *ctx, const float *feat, uint64_t n, float *pred) {
+  return guarded(ctx, [&] {
+    if (n == 0) return;
+    if (!feat || !pred) throw gtc::InvalidArgument("feat and pred are required");
+    if (!ctx->have_model) throw gtc::InvalidArgument("the context has no model");
+    cudaStream_t s = ctx->stream;
+    gtc::DeviceBuffer f, p;
+    struct Release {
+      gtc::DeviceBuffer *b[2];
+      ~Release() {
+        for (gtc::DeviceBuffer *x : b) x->release();
+      }
+    } release{{&f, &p}};
+    f.ensure(n * gtc::kFeat * sizeof(float));
+    p.ensure(n * sizeof(float));
+    GTC_CUDA(cudaMemcpyAsync(f.ptr, feat, n * gtc::kFeat * sizeof(float), cudaMemcpyHostToDevice, s));
+    gtc::learned_predict(ctx->net.as<gtc::LearnedNet>(), f.as<float>(), n, p.as<float>(), s);
+    GTC_CUDA(cudaMemcpyAsync(pred, p.ptr, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
   });
 }
 

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 
+#include "learned.cuh"
 #include "pipeline.cuh"
 
 namespace gtc {
@@ -342,7 +343,8 @@ void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
 
 }  // namespace
 
-void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host) {
+void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host,
+                 const LearnedWalk *lw) {
   const u64 n = ws.n;
   ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
   if (n == 0) return;
@@ -356,8 +358,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
 
   // walk tasks (their count is read back with the group count)
   ws.tasks.ensure(m * sizeof(Task));
-  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, ws.walk_split_depth,
-                                 mark);
+  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m,
+                                 lw ? lw->split_depth : ws.walk_split_depth, mark);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(mark, mscan, m, &sc->aux, ws.scan_tmp, s);
   k_task_fill<<<mb, kT, 0, s>>>(mark, mscan, ws.depth.as<u8>(), ws.parent.as<u32>(), m,
@@ -382,7 +384,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_LAUNCH_CHECK();
   GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
-  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, 3 * sizeof(unsigned long long), s));
   read_scalars(ws, host, s);
   const u32 ng = host->n_groups, ntasks = host->aux;
   ws.n_groups = ng;
@@ -390,6 +392,11 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
+  if (lw) {
+    learned_group_tolerances(ws, *lw, ng, s);
+    learned_build_lists(ws, *lw, ng, ntasks, host, s);
+    return;
+  }
 
   // count pass, offsets, fill pass
   const u64 slots = static_cast<u64>(ng) * ntasks;

@@ -50,6 +50,7 @@ struct alignas(16) WalkRec64 {
 struct SolverParams {
   double G, theta, eps;
   int quadrupole, group_size, leaf_size, pack, criterion;
+  double alpha;  // learned criterion's tolerance
 };
 
 struct Workspace {
@@ -90,7 +91,11 @@ struct Scalars {
   unsigned long long cell_interactions, body_interactions, max_list;
   u32 max_group;
   u32 aux;
-  unsigned long long fp64_tests;  // opening tests the FP32 bounds left undecided                // scratch count (deep-round segments)
+  unsigned long long fp64_tests;  // opening tests the FP32 bounds left undecided
+  unsigned long long mlp_rows;    // learned walk: rows the MLP decided
+  unsigned long long mlp_batches; // learned walk: warp inferences
+  unsigned long long walk_items; // learned walk: next item to take
+  u32 list_overflow;      // learned walk: a lane's region overflowed
   u32 error;              // device-detected failure code (0 = none)
 };
 
@@ -101,9 +106,13 @@ struct Scalars {
 void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                 const SolverParams &sp, cudaStream_t s, Scalars *host);
 
+struct LearnedWalk;
+
 // Stage 2: groups (with sibling packing) and the grouped walk; fills groups,
-// cell_list and body_list and the interaction counters.
-void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host);
+// cell_list and body_list and the interaction counters. With `lw` the walk
+// decides by the learned criterion instead of the opening angle.
+void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host,
+                 const LearnedWalk *lw = nullptr);
 
 // Stage 3: warp-per-group evaluation of the lists into ws.out (tree order),
 // then the scatter into acc/pot in caller order (FP64).

@@ -34,7 +34,8 @@ class GtcInvalidArgument(GtcError, ValueError):
 class GravityParams(C.Structure):
     _fields_ = [("G", C.c_double), ("theta", C.c_double), ("eps", C.c_double),
                 ("quadrupole", C.c_int32), ("group_size", C.c_int32), ("leaf_size", C.c_int32),
-                ("pack", C.c_int32), ("criterion", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("pack", C.c_int32), ("criterion", C.c_int32), ("reserved", C.c_int32),
+                ("alpha", C.c_double)]
 
 
 class KernelParams(C.Structure):
@@ -49,7 +50,9 @@ class Stats(C.Structure):
                 ("n_cell_list", C.c_uint64), ("n_body_list", C.c_uint64),
                 ("n_nodes", C.c_uint32), ("n_groups", C.c_uint32), ("max_group", C.c_uint32),
                 ("depth", C.c_uint32), ("eval_kernel_ms", C.c_double),
-                ("kernel_launches", C.c_uint64), ("walk_tests_fp64", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("walk_tests_fp64", C.c_uint64),
+                ("mlp_rows", C.c_uint64), ("mlp_batches", C.c_uint64),
+                ("criterion_used", C.c_uint32), ("pad", C.c_uint32)]
 
 
 NODE_DTYPE = np.dtype([
@@ -58,7 +61,11 @@ NODE_DTYPE = np.dtype([
     ("parent", "<u4"), ("depth", "<i4"), ("n_children", "<i4")])
 assert NODE_DTYPE.itemsize == 144
 
-assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 112
+assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 136
+
+# Learned criterion model: W1[6][64], b1[64], W2[64][64], b2[64], W3[64], b3,
+# then feature mean[6], std[6], y_mean, y_std, band (include/gtc.h).
+LEARNED_FEATURES, LEARNED_PARAMS, LEARNED_MODEL_FLOATS = 6, 4673, 4688
 
 
 def _load():
@@ -83,7 +90,17 @@ def _load():
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
-        "gtc_set_option": (I, [V, C.c_char_p, C.c_int64]),
+        "gtc_set_option": (I, [V, C.c_char_p, D]),
+        "gtc_learned_add_samples": (I, [V, P, P, U64, C.POINTER(GravityParams), D, D, U64, U32,
+                                        C.POINTER(C.c_uint64)]),
+        "gtc_learned_sample_count": (I, [V, C.POINTER(C.c_uint64)]),
+        "gtc_learned_export_samples": (I, [V, U64, U64, P, P, P]),
+        "gtc_learned_clear_samples": (I, [V]),
+        "gtc_learned_train": (I, [V, U64, U32, C.c_float, U64, I, C.POINTER(C.c_double)]),
+        "gtc_learned_gradient": (I, [V, P, P, P, U32, P, C.POINTER(C.c_double)]),
+        "gtc_learned_set_model": (I, [V, P]),
+        "gtc_learned_get_model": (I, [V, P]),
+        "gtc_learned_predict": (I, [V, P, U64, P]),
         "gtc_direct_fp64_noalloc": (I, [P, P, U64, P, U64, D, D, P, P, V]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
@@ -110,9 +127,9 @@ def _f64(a, shape=None):
 
 
 def gravity_params(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8,
-                   pack=True, criterion=CRITERION_THETA):
+                   pack=True, criterion=CRITERION_THETA, alpha=0.0):
     return GravityParams(G, theta, eps, int(quadrupole), group_size, leaf_size, int(pack),
-                         criterion, (C.c_int32 * 3)(0, 0, 0))
+                         criterion, 0, alpha)
 
 
 def direct_fp64_noalloc(pos_ptr, mass_ptr, n, idx_ptr, m, acc_ptr, pot_ptr, G=1.0, eps=0.025,
@@ -237,7 +254,74 @@ class Context:
     # ---- introspection -----------------------------------------------------
 
     def set_option(self, name, value):
-        self._check(lib.gtc_set_option(self.h, name.encode(), int(value)))
+        self._check(lib.gtc_set_option(self.h, name.encode(), float(value)))
+
+    # ---- learned opening criterion -------------------------------------------
+
+    def learned_add_samples(self, pos, mass, theta_gen=0.5, theta_guard=1.5, max_new=1 << 20,
+                            max_cell_bodies=8192, **kw):
+        """Labelled (group, cell) samples from these bodies -> number added."""
+        pos = _f64(pos, (-1, 3))
+        mass = _f64(mass)
+        gp = gravity_params(**kw)
+        added = C.c_uint64()
+        self._check(lib.gtc_learned_add_samples(self.h, _ptr(pos), _ptr(mass), mass.shape[0],
+                                                C.byref(gp), theta_gen, theta_guard, max_new,
+                                                max_cell_bodies, C.byref(added)))
+        return added.value
+
+    def learned_sample_count(self):
+        v = C.c_uint64()
+        self._check(lib.gtc_learned_sample_count(self.h, C.byref(v)))
+        return v.value
+
+    def learned_samples(self, first=0, count=None):
+        """-> (features (count, 6), labels (count,), (group, node) pairs (count, 2))."""
+        if count is None:
+            count = self.learned_sample_count() - first
+        feat = np.empty((count, LEARNED_FEATURES), np.float32)
+        label = np.empty(count, np.float32)
+        pairs = np.empty((count, 2), np.uint32)
+        self._check(lib.gtc_learned_export_samples(self.h, first, count, _ptr(feat),
+                                                   _ptr(label), _ptr(pairs)))
+        return feat, label, pairs
+
+    def learned_clear_samples(self):
+        self._check(lib.gtc_learned_clear_samples(self.h))
+
+    def learned_train(self, steps, batch=4096, lr=1e-3, seed=1, init=False):
+        loss = C.c_double()
+        self._check(lib.gtc_learned_train(self.h, steps, batch, lr, seed, int(init),
+                                          C.byref(loss)))
+        return loss.value
+
+    def learned_gradient(self, model, feat, label):
+        """Gradient (LEARNED_PARAMS,) and loss of `model` on the given samples."""
+        model = np.ascontiguousarray(model, np.float32)
+        feat = np.ascontiguousarray(feat, np.float32).reshape(-1, LEARNED_FEATURES)
+        label = np.ascontiguousarray(label, np.float32)
+        grad = np.empty(LEARNED_PARAMS, np.float32)
+        loss = C.c_double()
+        self._check(lib.gtc_learned_gradient(self.h, _ptr(model), _ptr(feat), _ptr(label),
+                                             label.shape[0], _ptr(grad), C.byref(loss)))
+        return grad, loss.value
+
+    def learned_set_model(self, model):
+        model = np.ascontiguousarray(model, np.float32)
+        if model.shape != (LEARNED_MODEL_FLOATS,):
+            raise ValueError(f"a model has {LEARNED_MODEL_FLOATS} floats")
+        self._check(lib.gtc_learned_set_model(self.h, _ptr(model)))
+
+    def learned_get_model(self):
+        model = np.empty(LEARNED_MODEL_FLOATS, np.float32)
+        self._check(lib.gtc_learned_get_model(self.h, _ptr(model)))
+        return model
+
+    def learned_predict(self, feat):
+        feat = np.ascontiguousarray(feat, np.float32).reshape(-1, LEARNED_FEATURES)
+        pred = np.empty(feat.shape[0], np.float32)
+        self._check(lib.gtc_learned_predict(self.h, _ptr(feat), feat.shape[0], _ptr(pred)))
+        return pred
 
     def fp32_peak_tflops(self):
         v = C.c_double()

@@ -85,7 +85,7 @@ typedef struct gtc_group {
 
 /* Opening criteria for the grouped walk. */
 #define GTC_CRITERION_THETA 0   /* the reference's box test (group_lists.cpp:147-154) */
-#define GTC_CRITERION_LEARNED 1 /* learned error model, theta test as fallback */
+#define GTC_CRITERION_LEARNED 1 /* learned error model, theta test as fallback (below) */
 
 /* GravityParams (octree.h:13-18) plus the make_gravity keys that shape the
  * grouped solver (gravity_backends.cpp:154-160, group_lists.h:64-65). */
@@ -98,7 +98,9 @@ typedef struct gtc_gravity_params {
   int32_t leaf_size;  /* bucket size of the octree (default 8) */
   int32_t pack;       /* 1: merge small sibling groups (the device default), 0: do not */
   int32_t criterion;  /* GTC_CRITERION_* */
-  int32_t reserved[3];
+  int32_t reserved;
+  double alpha;       /* learned criterion: per-cell error tolerance relative to the
+                         group's smallest |a| (ignored by the theta criterion) */
 } gtc_gravity_params;
 
 /* GroupTreeGravity::Timings (gravity_backends.h:54-58) and the GroupLists
@@ -117,6 +119,10 @@ typedef struct gtc_stats {
   double eval_kernel_ms;      /* the list (or direct) evaluation kernel alone */
   uint64_t kernel_launches;   /* kernels this call launched */
   uint64_t walk_tests_fp64;   /* opening tests decided in FP64 (FP32 bound undecided) */
+  uint64_t mlp_rows;          /* learned walk: opening tests the network decided */
+  uint64_t mlp_batches;       /* learned walk: warp-wide network evaluations */
+  uint32_t criterion_used;    /* GTC_CRITERION_* the walk actually used */
+  uint32_t pad;
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
@@ -200,16 +206,98 @@ gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
 
 /* ---- tuning and diagnostics (no reference counterpart) ------------------ */
 
-/* Sets a tuning option of the context (results do not depend on them):
- *   "walk_split_depth"  0, 1 or 2 (default 0): each group's walk runs as
- *                       independent tasks, one per subtree at this depth
- *                       (0: one task per group; measured fastest on GB300).
+/* Sets an option of the context:
+ *   "walk_split_depth"   0, 1 or 2 (default 0): each group's walk runs as
+ *                        independent tasks, one per subtree at this depth
+ *                        (0: one task per group; measured fastest on GB300).
+ *                        Results do not depend on it.
+ *   "learned_guard_theta" > 0 (default 1.5): the learned walk opens every
+ *                        cell closer than 2 h / guard + delta (the theta
+ *                        test with this angle guards the network).
+ *   "learned_band"       >= 0 log2 units, or < 0 for the model's own band
+ *                        (default): tests whose error prior lies further than
+ *                        this from the tolerance skip the network.
+ *   "learned_batch_min"  1..32 (default 16): waiting lanes of a warp that
+ *                        trigger a network evaluation.
+ *   "learned_split_depth" 0..3 (default 2): the learned walk runs each group
+ *                        as independent tasks, one per subtree at this depth
+ *                        (the nodes above it are opened for every group).
  * GTC_INVALID_ARGUMENT for an unknown name or a value out of range. */
-gtc_status gtc_set_option(gtc_context *ctx, const char *name, int64_t value);
+gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value);
 
 /* Measured FP32 FMA throughput of this GPU in TFLOP/s (one FMA = 2 flops):
  * the roofline denominator for the FP32 evaluation kernels. */
 gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops);
+
+/* ---- learned opening criterion (no reference counterpart) ---------------
+ *
+ * Replaces the accept test of the grouped walk (group_lists.cpp:147-154)
+ * when gtc_gravity_params.criterion is GTC_CRITERION_LEARNED. A 6-64-64-1
+ * ReLU network corrects a physical prior for the force error that accepting
+ * a cell would cause for a group (log2 of the largest |a_multipole - a_exact|
+ * over the group's targets, in units of G M_total / L^2, L the root
+ * half-size):
+ *   prediction = prior + y_mean + y_std * net((f - mean) / std)
+ *   prior      = log2(2 * 3^1.5) + f3 + 3 f1 - 5 f2
+ * with features f0 log2(group half-extent / L), f1 log2(cell half-size / L),
+ * f2 log2(distance from the group box to the cell's centre of mass / L),
+ * f3 log2(cell mass / M_total), f4 log2(|Q| / (M L^2)), f5 delta / half.
+ * A cell is accepted when the prediction is below
+ * log2(alpha * a_g * L^2 / (G M_total)), a_g = max(min |a|, mean |a| / 2)
+ * over the group's targets, |a| from the context's previous solve of the
+ * same bodies (caller order). Cells inside the guard (learned_guard_theta) are always opened.
+ * The walk runs the network in BF16 on the tensor cores (mma.sync), FP32
+ * accumulation.
+ * Fallback: with no model, or no previous solve of the same n, the call runs
+ * the theta walk (gtc_stats.criterion_used says which ran). Every solve of a
+ * context with a model records |a| for the next.
+ *
+ * Model layout (GTC_LEARNED_MODEL_FLOATS floats): W1[6][64], b1[64],
+ * W2[64][64], b2[64], W3[64], b3 (W[in][out]), then mean[6], std[6], y_mean,
+ * y_std, band (log2 units; tests whose centred prior, prior + y_mean, lies
+ * further than band from the tolerance are decided by it alone). */
+#define GTC_LEARNED_FEATURES 6
+#define GTC_LEARNED_PARAMS 4673
+#define GTC_LEARNED_MODEL_FLOATS 4688
+
+/* Training samples from the bodies (host arrays): builds the tree and groups
+ * with gp, walks sampled groups with opening angle theta_gen and labels every
+ * visited cell of more than two bodies beyond the guard angle theta_guard
+ * by FP64 direct summation over its bodies (cells of more than
+ * max_cell_bodies bodies are skipped). Appends at most max_new samples;
+ * *added receives the count. */
+gtc_status gtc_learned_add_samples(gtc_context *ctx, const double *pos, const double *mass,
+                                   uint64_t n, const gtc_gravity_params *gp, double theta_gen,
+                                   double theta_guard, uint64_t max_new,
+                                   uint32_t max_cell_bodies, uint64_t *added);
+gtc_status gtc_learned_sample_count(const gtc_context *ctx, uint64_t *count);
+/* Copies samples [first, first + count) (NULL to skip an array): feat
+ * count x 6, label count, pairs count x 2 = (group, node) in the tree and
+ * groups of the call that made the sample (gtc_group_export numbering when
+ * the same bodies and parameters are solved with the theta criterion). */
+gtc_status gtc_learned_export_samples(gtc_context *ctx, uint64_t first, uint64_t count,
+                                      float *feat, float *label, uint32_t *pairs);
+gtc_status gtc_learned_clear_samples(gtc_context *ctx);
+
+/* Trains the context's model on its samples with the project's own kernels:
+ * `steps` Adam steps (learning rate lr) on random minibatches of `batch`
+ * samples, mean squared error of the correction in normalised units. With
+ * init = 1 first sets the normalisation from the samples and draws new
+ * weights from `seed`. Afterwards sets the band to the 0.999 quantile of
+ * |y_std net| over the samples. *loss: the last minibatch's loss. */
+gtc_status gtc_learned_train(gtc_context *ctx, uint64_t steps, uint32_t batch, float lr,
+                             uint64_t seed, int init, double *loss);
+/* Gradient of the mean squared error of the given model (host,
+ * GTC_LEARNED_MODEL_FLOATS) on n given samples (host), by the training
+ * kernels: grad (GTC_LEARNED_PARAMS floats) and *loss. The context's own
+ * model is left as it was. */
+gtc_status gtc_learned_gradient(gtc_context *ctx, const float *model, const float *feat,
+                                const float *label, uint32_t n, float *grad, double *loss);
+gtc_status gtc_learned_set_model(gtc_context *ctx, const float *model);
+gtc_status gtc_learned_get_model(gtc_context *ctx, float *model);
+/* The walk's BF16 tensor-core inference on n given feature rows (host):
+ * pred[i] = predicted log2 error. */
+gtc_status gtc_learned_predict(gtc_context *ctx, const float *feat, uint64_t n, float *pred);
 
 /* ---- exports of the last gtc_group_force*, for parity checks ------------ */
 
