@@ -1,0 +1,115 @@
+#!/usr/bin/env python
+"""Trains the learned opening criterion on the GPU and writes the model.
+
+  python galactic-tides_gb300/train_criterion.py [--out DIR]
+
+Samples: (group, cell) pairs of Hernquist galaxies at N = 50k, 200k and 2M
+(the benchmark galaxy model, seeds other than the benchmark's seed 1),
+labelled by FP64 direct summation on the device (gtc_learned_add_samples).
+Training: Adam on the project's own forward/backward kernels
+(gtc_learned_train), then the band. Calibration: on a 2M galaxy of another
+seed, the largest alpha on a grid whose p99 force error against FP64 direct
+(4096-particle sample) is no worse than the plain theta = 0.75 walk's.
+
+Writes criterion_model.f32 (GTC_LEARNED_MODEL_FLOATS little-endian floats,
+the layout of include/gtc.h) and criterion_model.json (how it was made).
+"""
+
+import argparse
+import json
+import pathlib
+import sys
+import time
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+
+SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8,
+              pack=True)
+SAMPLE_SETS = [(50_000, s) for s in range(11, 19)] + [(200_000, s) for s in range(21, 25)] + \
+              [(2_000_000, s) for s in (31, 32)]
+SCHEDULE = [(12_000, 8192, 1e-3), (8_000, 8192, 3e-4), (4_000, 16384, 1e-4)]
+ALPHAS = [0.0008, 0.001, 0.0012, 0.0014, 0.0016, 0.0018, 0.002]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=str(HERE))
+    ap.add_argument("--max-per-galaxy", type=int, default=4_000_000)
+    ap.add_argument("--calib-n", type=int, default=2_000_000)
+    args = ap.parse_args()
+    import torch
+    import __graft_entry__
+    gtc = __graft_entry__.load_package().gtc
+    log = lambda *a: print(*a, flush=True)
+    ctx = gtc.Context(0)
+    t0 = time.time()
+    sets = []
+    for n, seed in SAMPLE_SETS:
+        pos, _, mass, _ = gtc.make_galaxy(n, seed=seed)
+        k = ctx.learned_add_samples(pos, mass, theta_gen=0.5, theta_guard=1.5,
+                                    max_new=args.max_per_galaxy, max_cell_bodies=16384, **SOLVER)
+        sets.append(dict(n=n, seed=seed, samples=k))
+        log(f"samples N={n} seed={seed}: {k}")
+    total = ctx.learned_sample_count()
+    t_samples = time.time() - t0
+    t1 = time.time()
+    losses = [ctx.learned_train(1, batch=8192, lr=0.0, seed=1, init=True)]
+    for k, (steps, batch, lr) in enumerate(SCHEDULE):
+        losses.append(ctx.learned_train(steps, batch=batch, lr=lr, seed=2 + k))
+    torch.cuda.synchronize()
+    t_train = time.time() - t1
+    model = ctx.learned_get_model()
+    log(f"{total} samples in {t_samples:.1f} s, training {t_train:.1f} s, losses {losses}, "
+        f"band {model[-1]}")
+
+    # calibration of alpha on a galaxy the bench does not use
+    n = args.calib_n
+    pos, _, mass, _ = gtc.make_galaxy(n, seed=7)
+    idx = gtc.sample_indices(n, 4096, 2).astype(np.int64)
+    dev = torch.device("cuda", 0)
+    dpos, dmass = torch.from_numpy(pos).to(dev), torch.from_numpy(mass).to(dev)
+    didx = torch.from_numpy(idx).to(dev)
+    racc = torch.empty((len(idx), 3), dtype=torch.float64, device=dev)
+    rpot = torch.empty(len(idx), dtype=torch.float64, device=dev)
+    ctx.direct_fp64_device(dpos.data_ptr(), dmass.data_ptr(), n, didx.data_ptr(), len(idx),
+                           racc.data_ptr(), rpot.data_ptr(), G=1.0, eps=0.025)
+    ref = racc.cpu().numpy()
+
+    def p99(acc):
+        e = np.linalg.norm(acc[idx] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        return float(np.percentile(e, 99))
+
+    with gtc.Context(0) as plain:
+        acc, _ = plain.group_force(pos, mass, **SOLVER)
+        st = plain.stats()
+    base = dict(p99=p99(acc), interactions=st["cell_interactions"] + st["body_interactions"])
+    table = []
+    for a in ALPHAS:
+        kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=a)
+        ctx.group_force(pos, mass, **kw)
+        acc, _ = ctx.group_force(pos, mass, **kw)
+        st = ctx.stats()
+        table.append(dict(alpha=a, p99=p99(acc),
+                          interactions=st["cell_interactions"] + st["body_interactions"]))
+        log(table[-1])
+    ok = [r for r in table if r["p99"] <= base["p99"]]
+    alpha = max(r["alpha"] for r in ok) if ok else min(ALPHAS)
+    out = pathlib.Path(args.out)
+    out.mkdir(parents=True, exist_ok=True)
+    model.astype("<f4").tofile(out / "criterion_model.f32")
+    info = dict(model_floats=int(model.shape[0]), samples=int(total), sample_sets=sets,
+                theta_gen=0.5, theta_guard=1.5, max_cell_bodies=16384,
+                schedule=[dict(steps=s, batch=b, lr=lr) for s, b, lr in SCHEDULE],
+                losses=losses, band=float(model[-1]), train_seconds=round(t_train, 2),
+                sample_seconds=round(t_samples, 2), alpha=alpha,
+                calibration=dict(n=n, galaxy_seed=7, sample_seed=2, sample=len(idx),
+                                 plain_theta_0_75=base, learned=table))
+    (out / "criterion_model.json").write_text(json.dumps(info, indent=1) + "\n")
+    log(f"alpha = {alpha}; wrote {out / 'criterion_model.f32'}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,293 @@
+"""The learned opening criterion: the training kernels' gradients against the
+FP64 oracle, the labels against FP64 direct sums, the walk's BF16 inference,
+the lists' invariants, the fallback to the theta walk, and what the trained
+network gains over the plain theta = 0.75 walk."""
+
+import json
+import pathlib
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "oracle"))
+import learned_oracle as lo  # noqa: E402
+
+from checks import rel_errors  # noqa: E402
+
+SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8,
+              pack=True)
+MODEL = ROOT / "galactic-tides_gb300" / "criterion_model.f32"
+MODEL_INFO = ROOT / "galactic-tides_gb300" / "criterion_model.json"
+
+
+def random_model(seed=3, scale=0.25):
+    rng = np.random.default_rng(seed)
+    m = np.zeros(lo.MODEL_FLOATS)
+    m[:lo.PARAMS] = rng.normal(0.0, scale, lo.PARAMS)
+    m[lo.OFF_MEAN:lo.OFF_STD] = [-6.4, -3.8, -1.2, -10.5, -8.5, 0.38]
+    m[lo.OFF_STD:lo.OFF_YMEAN] = [1.8, 0.8, 0.6, 1.7, 1.6, 0.2]
+    m[lo.OFF_YMEAN], m[lo.OFF_YSTD], m[lo.OFF_BAND] = -4.7, 1.05, 3.0
+    return m.astype(np.float32)
+
+
+def random_samples(model, n, seed=4):
+    rng = np.random.default_rng(seed)
+    p = lo.unpack(model)
+    feat = (p["mean"] + p["std"] * rng.normal(size=(n, lo.FEAT))).astype(np.float32)
+    label = (lo.prior(feat) - 4.7 + rng.normal(size=n)).astype(np.float32)
+    return feat, label
+
+
+# ---------------------------------------------------------------- CPU only
+
+def test_oracle_gradient_matches_finite_differences():
+    model = random_model().astype(np.float64)
+    feat, label = random_samples(model, 64)
+    _, g = lo.loss_and_grad(model, feat, label)
+    rng = np.random.default_rng(5)
+    for k in rng.choice(lo.PARAMS, 60, replace=False):
+        h = 1e-6
+        mp, mm = model.copy(), model.copy()
+        mp[k] += h
+        mm[k] -= h
+        fd = (lo.loss_and_grad(mp, feat, label)[0] - lo.loss_and_grad(mm, feat, label)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])) + 1e-8, k
+
+
+def test_oracle_bf16_rounding():
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0, 65504.0])
+    r = lo.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0  # tie to even
+    assert r[2] == 1.0078125
+    assert abs(r[3] + 3.140625) < 1e-12 and r[4] == 0.0
+    assert np.all(np.abs(r - x) <= np.abs(x) * 2.0 ** -8)
+
+
+def test_committed_model_is_well_formed():
+    m = np.fromfile(MODEL, dtype="<f4")
+    assert m.shape == (lo.MODEL_FLOATS,)
+    assert np.all(np.isfinite(m))
+    assert np.all(m[lo.OFF_STD:lo.OFF_YMEAN] > 0) and m[lo.OFF_YSTD] > 0
+    assert 0 <= m[lo.OFF_BAND] < 32
+    info = json.loads(MODEL_INFO.read_text())
+    assert info["model_floats"] == lo.MODEL_FLOATS and info["alpha"] > 0
+
+
+# ---------------------------------------------------------------- GPU
+
+gpu = pytest.mark.gpu
+
+
+@gpu
+def test_training_gradient_matches_oracle(ctx):
+    model = random_model()
+    feat, label = random_samples(model, 1000)
+    grad, loss = ctx.learned_gradient(model, feat, label)
+    want_loss, want = lo.loss_and_grad(model.astype(np.float64), feat, label)
+    assert abs(loss - want_loss) <= 1e-5 * want_loss
+    scale = np.abs(want).max()
+    assert np.abs(grad - want).max() <= 2e-5 * scale
+    cos = float(grad @ want / (np.linalg.norm(grad) * np.linalg.norm(want)))
+    assert cos > 1 - 1e-8
+
+
+@gpu
+def test_gradient_leaves_the_context_model(ctx):
+    model = random_model(seed=11)
+    ctx.learned_set_model(model)
+    feat, label = random_samples(model, 300)
+    ctx.learned_gradient(random_model(seed=12), feat, label)
+    assert np.array_equal(ctx.learned_get_model(), model)
+
+
+@gpu
+def test_walk_inference_matches_oracle(ctx):
+    model = random_model(seed=7, scale=0.2)
+    ctx.learned_set_model(model)
+    feat, _ = random_samples(model, 5000, seed=8)
+    got = ctx.learned_predict(feat)
+    emu = lo.predict_bf16(model, feat)
+    exact = lo.predict(model, feat)
+    d = np.abs(got - emu)
+    assert np.median(d) < 2e-3 and d.max() < 0.05
+    assert np.abs(got - exact).max() < 0.3
+
+
+@gpu
+def test_labels_and_features_match_oracle(ctx, gtc):
+    pos, _, mass, _ = gtc.make_galaxy(20_000, seed=3)
+    ctx.learned_clear_samples()
+    added = ctx.learned_add_samples(pos, mass, theta_gen=0.5, theta_guard=1.5, max_new=4000,
+                                    max_cell_bodies=4096, **SOLVER)
+    assert 1000 < added <= 4000
+    feat, label, pairs = ctx.learned_samples()
+    assert feat.shape == (added, 6) and np.all(np.isfinite(feat)) and np.all(np.isfinite(label))
+    # the same tree and groups, exported from a theta solve of the same bodies
+    ctx.group_force(pos, mass, **SOLVER)
+    dev = ctx.export()
+    nodes, order, groups = dev["nodes"], dev["order"].astype(np.int64), dev["groups"]
+    tpos, tmass = pos[order], mass[order]
+    L, mtot = nodes[0]["half"], nodes[0]["mass"]
+    rng = np.random.default_rng(1)
+    for k in rng.choice(added, 150, replace=False):
+        g, p = int(pairs[k, 0]), int(pairs[k, 1])
+        nd = nodes[p]
+        tg = tpos[groups[g, 0]:groups[g, 1]]
+        want = lo.pair_label(tg, tpos[nd["begin"]:nd["end"]], tmass[nd["begin"]:nd["end"]],
+                             nd["com"], nd["mass"], nd["quad"], 1.0, 0.025 ** 2, L, mtot)
+        assert abs(label[k] - want) < 2e-3, (k, label[k], want)
+        lo_, hi_ = tg.min(0), tg.max(0)
+        c, h = (lo_ + hi_) / 2, (hi_ - lo_) / 2
+        dist = np.linalg.norm(np.maximum(np.abs(nd["com"] - c) - h, 0.0))
+        wf = lo.pair_features(h, dist, nd["half"], nd["mass"], lo.quad_norm(nd["quad"]),
+                              nd["delta"], L, mtot)
+        # FP32 positions relative to the root centre: the distance carries
+        # an absolute error of about 1e-7 L
+        tol = np.full(6, 2e-3)
+        tol[2] += 1e-6 * L / max(dist, 1e-12)
+        assert np.all(np.abs(feat[k] - wf) <= tol), (k, feat[k], wf)
+        assert nd["end"] - nd["begin"] > lo.FEW_BODIES
+        assert groups[g, 1] <= nd["begin"] or nd["end"] <= groups[g, 0]
+
+
+@gpu
+def test_training_reduces_the_loss(ctx, gtc):
+    ctx.learned_clear_samples()
+    for seed in (1, 2):
+        pos, _, mass, _ = gtc.make_galaxy(50_000, seed=seed)
+        ctx.learned_add_samples(pos, mass, max_new=400_000, **SOLVER)
+    first = ctx.learned_train(1, batch=4096, lr=0.0, seed=1, init=True)
+    ctx.learned_train(1500, batch=4096, lr=1e-3, seed=2)
+    after = ctx.learned_train(200, batch=8192, lr=1e-4, seed=3)
+    assert after < 0.8 * first
+    model = ctx.learned_get_model()
+    assert 0 < model[lo.OFF_BAND] < 32
+    # deterministic: the same steps from the same start give the same model
+    ctx.learned_train(1, batch=4096, lr=0.0, seed=1, init=True)
+    ctx.learned_train(1500, batch=4096, lr=1e-3, seed=2)
+    ctx.learned_train(200, batch=8192, lr=1e-4, seed=3)
+    assert np.array_equal(ctx.learned_get_model(), model)
+
+
+def _learned_ctx(gtc):
+    c = gtc.Context(0)
+    c.learned_set_model(np.fromfile(MODEL, dtype="<f4"))
+    return c
+
+
+def _check_list_invariants(dev, n, max_groups=300):
+    """Every body once per group, no accepted cell holding a target."""
+    nodes, groups = dev["nodes"], dev["groups"]
+    cl, bl = dev["cell_list"].astype(np.int64), dev["body_list"].astype(np.int64)
+    step = max(1, len(groups) // max_groups)
+    for g in range(0, len(groups), step):
+        b0, b1, c0, c1, l0, l1 = (int(v) for v in groups[g, :6])
+        cover = np.zeros(n + 1, np.int64)
+        cells = cl[c0:c1]
+        np.add.at(cover, nodes["begin"][cells], 1)
+        np.add.at(cover, nodes["end"][cells], -1)
+        cover = np.cumsum(cover)[:n]
+        np.add.at(cover, bl[l0:l1], 1)
+        assert np.all(cover == 1), g
+        assert np.all((nodes["end"][cells] <= b0) | (nodes["begin"][cells] >= b1)), g
+        assert np.all(nodes["end"][cells] - nodes["begin"][cells] > lo.FEW_BODIES)
+
+
+@gpu
+def test_fallback_then_learned_lists_are_valid(gtc):
+    pos, _, mass, _ = gtc.make_galaxy(30_000, seed=5)
+    kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.002)
+    with gtc.Context(0) as plain:
+        want, _ = plain.group_force(pos, mass, **SOLVER)
+    with _learned_ctx(gtc) as c:
+        # no previous solve: the theta walk runs, exactly the plain result
+        acc0, _ = c.group_force(pos, mass, **kw)
+        assert c.stats()["criterion_used"] == gtc.CRITERION_THETA
+        assert np.array_equal(acc0, want)
+        acc1, _ = c.group_force(pos, mass, **kw)
+        st = c.stats()
+        assert st["criterion_used"] == gtc.CRITERION_LEARNED
+        assert st["mlp_rows"] > 0 and st["mlp_batches"] > 0
+        _check_list_invariants(c.export(), len(mass))
+        # a different number of bodies has no previous |a|: theta again
+        c.group_force(pos[:20_000], mass[:20_000], **kw)
+        assert c.stats()["criterion_used"] == gtc.CRITERION_THETA
+    with _learned_ctx(gtc) as c:  # the same calls again: bitwise the same forces
+        c.group_force(pos, mass, **kw)
+        again, _ = c.group_force(pos, mass, **kw)
+        assert np.array_equal(again, acc1)
+    with gtc.Context(0) as c:  # no model: theta
+        c.group_force(pos, mass, **kw)
+        c.group_force(pos, mass, **kw)
+        assert c.stats()["criterion_used"] == gtc.CRITERION_THETA
+
+
+@gpu
+def test_band_only_skips_the_network_where_it_cannot_change_the_decision(gtc):
+    pos, _, mass, _ = gtc.make_galaxy(100_000, seed=6)
+    kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
+    with _learned_ctx(gtc) as c:
+        c.group_force(pos, mass, **kw)
+        c.set_option("learned_band", 1e6)  # the network decides every guarded test
+        full, _ = c.group_force(pos, mass, **kw)
+        s_full = c.stats()
+        c.set_option("learned_band", -1)  # the model's band
+        band, _ = c.group_force(pos, mass, **kw)
+        s_band = c.stats()
+    assert s_band["mlp_rows"] < s_full["mlp_rows"]
+    tot = lambda s: s["cell_interactions"] + s["body_interactions"]
+    assert abs(tot(s_band) / tot(s_full) - 1) < 0.01
+    assert np.median(rel_errors(band, full)) < 1e-6
+
+
+@gpu
+def test_learned_gains_over_plain_theta(ctx, gtc):
+    """The trained network against the method without it (theta = 0.75): at
+    no worse p99 force error against FP64 direct, far fewer interactions."""
+    n = 200_000
+    pos, _, mass, _ = gtc.make_galaxy(n, seed=1)
+    idx = gtc.sample_indices(n, 1024, 1).astype(np.int64)
+    import torch
+    dev = torch.device("cuda", 0)
+    dpos, dmass = torch.from_numpy(pos).to(dev), torch.from_numpy(mass).to(dev)
+    didx = torch.from_numpy(idx).to(dev)
+    racc = torch.empty((len(idx), 3), dtype=torch.float64, device=dev)
+    rpot = torch.empty(len(idx), dtype=torch.float64, device=dev)
+    ctx.direct_fp64_device(dpos.data_ptr(), dmass.data_ptr(), n, didx.data_ptr(), len(idx),
+                           racc.data_ptr(), rpot.data_ptr(), G=1.0, eps=0.025)
+    ref = racc.cpu().numpy()
+
+    def p99(acc):
+        return float(np.percentile(rel_errors(acc[idx], ref), 99))
+
+    with gtc.Context(0) as plain:
+        acc_p, _ = plain.group_force(pos, mass, **SOLVER)
+        s_p = plain.stats()
+    with _learned_ctx(gtc) as c:
+        kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.001)
+        c.group_force(pos, mass, **kw)
+        acc_l, _ = c.group_force(pos, mass, **kw)
+        s_l = c.stats()
+    inter = lambda s: s["cell_interactions"] + s["body_interactions"]
+    assert s_l["criterion_used"] == gtc.CRITERION_LEARNED
+    assert p99(acc_l) <= p99(acc_p)
+    assert inter(s_l) < 0.6 * inter(s_p)
+
+
+@gpu
+def test_invalid_learned_arguments(ctx, gtc):
+    pos, _, mass, _ = gtc.make_galaxy(2000, seed=1)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.group_force(pos, mass, **dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0))
+    bad = random_model()
+    bad[lo.OFF_STD] = 0.0
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.learned_set_model(bad)
+    with pytest.raises(ValueError):
+        ctx.learned_set_model(bad[:10])
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_batch_min", 0)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_split_depth", 7)
