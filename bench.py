@@ -18,7 +18,12 @@ quadrupoles on, sibling packing on. A "step" is one force evaluation.
   accuracy  p99 and median of |a - a_FP64| / |a_FP64| on the reference
           bench's 4096-particle sample, FP64 direct sums on the device;
   cpu_baseline  the oracle's restatement of the reference's OpenMP group and
-          tree solvers on this machine's host cores, one evaluation each.
+          tree solvers on this machine's host cores, one evaluation each;
+  learned   the same workload with the learned opening criterion (the
+          committed model, alpha calibrated on another galaxy by the training
+          script), timed the same way after warm-up solves that supply the
+          previous accelerations it needs: ms, breakdown, interactions, p99 on
+          the same sample, and its ratio to the plain theta = 0.75 value.
 
 --impl reference times the reference's own CPU solver on the host cores
 (its build when present, else the oracle restatement) on the same workload.
@@ -39,7 +44,9 @@ ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf_size=8)
-METRIC = "ms/force-eval at N=2M (grouped walk, theta=0.75)"
+METRIC = "ms/force-eval at N=2M, p99 err vs FP64 direct; learned vs plain \u03b8=0.75 on GB300"
+MODEL = ROOT / "galactic-tides_gb300" / "criterion_model.f32"
+MODEL_INFO = ROOT / "galactic-tides_gb300" / "criterion_model.json"
 WORKLOAD = "hernquist-galaxy N=2M, group solver theta=0.75 gs=32 leaf=8 eps=0.025 quadrupole"
 FLOPS_BODY, FLOPS_CELL_QUAD, FLOPS_CELL_MONO = 20, 64, 21
 
@@ -53,6 +60,8 @@ def parse():
     ap.add_argument("--n", type=int, default=2_000_000)
     ap.add_argument("--sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-criterion measurement")
     ap.add_argument("--only-steps", action="store_true",
                     help="warm-up and timed steps only (for profiler launch lists)")
     return ap.parse_args()
@@ -190,6 +199,58 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, ref, plain_ms,
+                    device):
+    """The learned criterion on the same bodies, timed like the plain solver."""
+    import torch
+    info = json.loads(MODEL_INFO.read_text())
+    alpha = float(info["alpha"])
+    lctx = gtc.Context(device)
+    lctx.learned_set_model(np.fromfile(MODEL, dtype="<f4"))
+
+    def step():
+        lctx.group_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                                dpot.data_ptr(), pack=True, criterion=gtc.CRITERION_LEARNED,
+                                alpha=alpha, **SOLVER)
+
+    for _ in range(max(3, args.warmup) + 1):  # the first is the theta fallback
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    stats = []
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            stats.append(lctx.stats())
+    torch.cuda.synchronize()
+    lms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    got = dacc.cpu().numpy()[idx.astype(np.int64)]
+    err = np.sort(np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1))
+    st = stats[-1]
+    mean = lambda key: statistics.mean(s[key] for s in stats)
+    model = np.fromfile(MODEL, dtype="<f4")
+    lctx.close()
+    return {"ms": round(lms, 4), "ratio_vs_plain": round(lms / plain_ms, 4),
+            "criterion_used": "learned" if st["criterion_used"] == gtc.CRITERION_LEARNED else "theta",
+            "breakdown_ms": {"tree": round(mean("tree_ms"), 4), "lists": round(mean("lists_ms"), 4),
+                             "evaluate": round(mean("evaluate_ms"), 4),
+                             "evaluate_kernel": round(mean("eval_kernel_ms"), 4)},
+            "interactions": {"cell": st["cell_interactions"], "body": st["body_interactions"],
+                             "per_particle": (st["cell_interactions"] + st["body_interactions"]) / n},
+            "accuracy": {"p99": float(err[len(err) * 99 // 100]),
+                         "median": float(err[len(err) // 2]), "sample": len(idx),
+                         "judge": "fp64 direct"},
+            "network_rows": st["mlp_rows"], "network_batches": st["mlp_batches"],
+            "alpha": alpha, "band": float(model[-1]),
+            "model": "galactic-tides_gb300/criterion_model.f32 (6-64-64-1, BF16 inference)",
+            "alpha_source": "largest alpha with p99 <= plain theta=0.75 on a 2M galaxy of seed 7",
+            "gpu_launches": sum(s["kernel_launches"] for s in stats)}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -295,6 +356,10 @@ def main():
         e2e_step()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
 
+    learned = None
+    if not args.no_learned and MODEL.exists():
+        learned = measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, ref,
+                                  ms, local_rank)
     peak_fp32 = ctx.fp32_peak_tflops()
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     traffic = None
@@ -356,7 +421,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,
-            "learned": None,
+            "learned": learned,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

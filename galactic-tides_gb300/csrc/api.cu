@@ -152,16 +152,14 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.net = ctx->net.as<gtc::LearnedNet>();
     lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
     lw.gtol = &ctx->gtol;
-    lw.scratch = &ctx->walk_scratch;
-    lw.lane_cells = &ctx->lane_cells;
-    lw.lane_runs = &ctx->lane_runs;
+    lw.scratch = &ctx->lscratch;
     lw.split_depth = ctx->learned_split;
+    lw.y_mean = ctx->model_ymean;
     lw.prev_amag = ctx->prev_amag.as<float>();
     lw.alpha = sp.alpha;
     lw.G = sp.G;
     lw.inv_theta_guard = static_cast<float>(1.0 / ctx->guard_theta);
     lw.band = ctx->band_override >= 0 ? static_cast<float>(ctx->band_override) : ctx->model_band;
-    lw.batch_min = ctx->batch_min;
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
     gtc::build_lists(ws, sp, s, ctx->host_sc);
@@ -325,9 +323,9 @@ void gtc_destroy(gtc_context *ctx) {
   ctx->sample_scratch.release();
   for (gtc::DeviceBuffer *b : {&ctx->samples.feat, &ctx->samples.label, &ctx->samples.pair,
                                &ctx->model, &ctx->net,
-                               &ctx->train_scratch, &ctx->cfeat, &ctx->gtol, &ctx->walk_scratch,
-                               &ctx->prev_amag})
+                               &ctx->train_scratch, &ctx->cfeat, &ctx->gtol, &ctx->prev_amag})
     b->release();
+  ctx->lscratch.release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
@@ -538,10 +536,6 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
       if (value != std::floor(value) || value < 0 || value > 3)
         throw gtc::InvalidArgument("learned_split_depth must be 0..3");
       ctx->learned_split = static_cast<int>(value);
-    } else if (key == "learned_batch_min") {
-      if (value != std::floor(value) || value < 1 || value > 32)
-        throw gtc::InvalidArgument("learned_batch_min must be 1..32");
-      ctx->batch_min = static_cast<int>(value);
     } else {
       throw gtc::InvalidArgument("unknown option '" + key + "'");
     }
@@ -627,7 +621,7 @@ gtc_status gtc_learned_train(gtc_context *ctx, uint64_t steps, uint32_t batch, f
     if (init || !ctx->have_model) gtc::learned_init_model(ctx, seed);
     const double l = gtc::learned_train_on(ctx, set.feat.as<float>(), set.label.as<float>(),
                                            set.count, steps, batch, lr, seed, nullptr, nullptr);
-    gtc::learned_update_band(ctx, 0.999);
+    gtc::learned_update_band(ctx, 0.99);
     if (loss) *loss = l;
   });
 }

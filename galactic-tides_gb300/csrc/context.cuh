@@ -25,16 +25,15 @@ struct gtc_context {
   gtc::DeviceBuffer net;            // LearnedNet: the model in tensor-core layout
   bool have_model = false;
   float model_band = 1e30f;         // the model's band (host copy)
+  float model_ymean = 0.f;          // the model's y_mean (host copy)
   gtc::DeviceBuffer train_scratch;  // per-block partial gradients, Adam moments, losses
   gtc::DeviceBuffer cfeat, gtol;    // per-node features, per-group tolerances
-  gtc::DeviceBuffer walk_scratch;   // the learned walk's per-lane list scratch
+  gtc::LearnedScratch lscratch;     // the learned walk's rounds
   gtc::DeviceBuffer prev_amag;      // |a| per body (caller order) of the last solve
   gtc::u64 prev_n = 0;              // bodies in prev_amag (0: none)
   double guard_theta = 1.5;         // options of the learned walk
   double band_override = -1.0;      // < 0: the model's band
-  int batch_min = 16;
-  int learned_split = 2;            // learned walk tasks: subtrees at this depth
-  gtc::u32 lane_cells = 1024, lane_runs = 256;  // learned walk lane regions (grown as needed)
+  int learned_split = 1;            // learned walk tasks: subtrees at this depth
 };
 
 namespace gtc {

@@ -525,6 +525,7 @@ void learned_set_model(gtc_context *ctx, const float *host_model) {
   learned_prepare_net(ctx->model.as<float>(), ctx->net.as<LearnedNet>(), s);
   GTC_CUDA(cudaStreamSynchronize(s));
   ctx->model_band = host_model[kOffBand];
+  ctx->model_ymean = host_model[kOffYMean];
   ctx->have_model = true;
 }
 

@@ -93,19 +93,34 @@ struct alignas(16) LearnedNet {
   float b3, y_mean, y_std, band;
 };
 
+// Device memory of the learned walk, kept between calls.
+struct LearnedScratch {
+  DeviceBuffer seg;                 // per item: two uint4 records (items_cap each)
+  DeviceBuffer regions, lane_fill;  // the lanes' list regions and how full they are
+  DeviceBuffer gstart, pcount, poff, base;
+  DeviceBuffer q[2], dec[2];        // deferred pairs and the network's decisions
+  u64 items_cap = 0;
+  u32 lane_cells = 1024, lane_runs = 256, lane_pend = 256;  // grown when outgrown
+  void release() {
+    for (DeviceBuffer *b : {&seg, &regions, &lane_fill, &gstart, &pcount, &poff, &base, &q[0],
+                            &q[1], &dec[0], &dec[1]})
+      b->release();
+    items_cap = 0;
+  }
+};
+
 // What the learned walk needs besides the tree and the groups.
 struct LearnedWalk {
   const LearnedNet *net = nullptr;  // device
   const CellFeat *cfeat = nullptr;  // per node (device)
   DeviceBuffer *gtol = nullptr;     // per group (f0, tolerance), filled by build_lists
-  DeviceBuffer *scratch = nullptr;  // items' segments and the lanes' list regions
-  u32 *lane_cells = nullptr, *lane_runs = nullptr;  // region sizes (grown when outgrown)
-  int split_depth = 2;              // tasks: the subtrees at this depth
+  LearnedScratch *scratch = nullptr;
+  int split_depth = 1;              // tasks: the subtrees at this depth
   const float *prev_amag = nullptr; // |a| per body in caller order (device)
   double alpha = 0.02, G = 1.0;
   float inv_theta_guard = 1.f / 1.5f;
   float band = 3.f;                 // log2 units; 0: prior only; huge: the MLP decides all
-  int batch_min = 16;               // waiting lanes that trigger a warp inference
+  float y_mean = 0.f;               // the model's mean correction (centres the prior)
 };
 
 // Per-node features (after build_tree).

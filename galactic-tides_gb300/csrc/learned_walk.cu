@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include "learned.cuh"
 
@@ -40,73 +41,67 @@ __device__ __forceinline__ u32 pack_bf16(float lo, float hi) {
 // The MLP for the 32 rows of `rows` (per row: the six normalised features
 // and a constant 1 as BF16 pairs). Every lane of the warp must call it; lane
 // L gets the network output (normalised units) of row L. The two 16-row
-// tiles go through the layers together: each B fragment is loaded once for
-// both, and the two accumulator chains interleave.
-__device__ __forceinline__ float warp_mlp(const uint4 *rows, const u32 (&w1)[8], const uint2 *w2,
+// tiles run one after the other, which keeps the walk's register count low
+// (more warps in flight to hide its memory latency); the B fragments come
+// from shared memory.
+__device__ __forceinline__ float warp_mlp(const uint4 *rows, const u32 *w1, const uint2 *w2,
                                           const float *b2, const float *w3, float b3, int lane) {
   const int g = lane >> 2, t = lane & 3;
-  const u32 a00 = reinterpret_cast<const u32 *>(&rows[g])[t];
-  const u32 a01 = reinterpret_cast<const u32 *>(&rows[g + 8])[t];
-  const u32 a10 = reinterpret_cast<const u32 *>(&rows[16 + g])[t];
-  const u32 a11 = reinterpret_cast<const u32 *>(&rows[24 + g])[t];
-  u32 A0[4][4], A1[4][4];
+  float o[4];
 #pragma unroll
-  for (int j = 0; j < 8; j += 2) {
-    float c0[4] = {0.f, 0.f, 0.f, 0.f}, e0[4] = {0.f, 0.f, 0.f, 0.f};
-    float c1[4] = {0.f, 0.f, 0.f, 0.f}, e1[4] = {0.f, 0.f, 0.f, 0.f};
-    mma_bf16(c0, a00, a01, 0u, 0u, w1[j], 0u);
-    mma_bf16(c1, a10, a11, 0u, 0u, w1[j], 0u);
-    mma_bf16(e0, a00, a01, 0u, 0u, w1[j + 1], 0u);
-    mma_bf16(e1, a10, a11, 0u, 0u, w1[j + 1], 0u);
-    A0[j / 2][0] = pack_bf16(fmaxf(c0[0], 0.f), fmaxf(c0[1], 0.f));
-    A0[j / 2][1] = pack_bf16(fmaxf(c0[2], 0.f), fmaxf(c0[3], 0.f));
-    A0[j / 2][2] = pack_bf16(fmaxf(e0[0], 0.f), fmaxf(e0[1], 0.f));
-    A0[j / 2][3] = pack_bf16(fmaxf(e0[2], 0.f), fmaxf(e0[3], 0.f));
-    A1[j / 2][0] = pack_bf16(fmaxf(c1[0], 0.f), fmaxf(c1[1], 0.f));
-    A1[j / 2][1] = pack_bf16(fmaxf(c1[2], 0.f), fmaxf(c1[3], 0.f));
-    A1[j / 2][2] = pack_bf16(fmaxf(e1[0], 0.f), fmaxf(e1[1], 0.f));
-    A1[j / 2][3] = pack_bf16(fmaxf(e1[2], 0.f), fmaxf(e1[3], 0.f));
-  }
-  float s00 = 0.f, s01 = 0.f, s10 = 0.f, s11 = 0.f;
+  for (int mt = 0; mt < 2; ++mt) {
+    const u32 a0 = reinterpret_cast<const u32 *>(&rows[mt * 16 + g])[t];
+    const u32 a1 = reinterpret_cast<const u32 *>(&rows[mt * 16 + g + 8])[t];
+    u32 A[4][4];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float2 bb = *reinterpret_cast<const float2 *>(&b2[8 * j + 2 * t]);
-    float c0[4] = {bb.x, bb.y, bb.x, bb.y}, c1[4] = {bb.x, bb.y, bb.x, bb.y};
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      const uint2 b = w2[(kk * 8 + j) * 32 + lane];
-      mma_bf16(c0, A0[kk][0], A0[kk][1], A0[kk][2], A0[kk][3], b.x, b.y);
-      mma_bf16(c1, A1[kk][0], A1[kk][1], A1[kk][2], A1[kk][3], b.x, b.y);
+    for (int j = 0; j < 8; j += 2) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f}, e[4] = {0.f, 0.f, 0.f, 0.f};
+      mma_bf16(c, a0, a1, 0u, 0u, w1[j * 32 + lane], 0u);
+      mma_bf16(e, a0, a1, 0u, 0u, w1[(j + 1) * 32 + lane], 0u);
+      A[j / 2][0] = pack_bf16(fmaxf(c[0], 0.f), fmaxf(c[1], 0.f));
+      A[j / 2][1] = pack_bf16(fmaxf(c[2], 0.f), fmaxf(c[3], 0.f));
+      A[j / 2][2] = pack_bf16(fmaxf(e[0], 0.f), fmaxf(e[1], 0.f));
+      A[j / 2][3] = pack_bf16(fmaxf(e[2], 0.f), fmaxf(e[3], 0.f));
     }
-    const float2 w = *reinterpret_cast<const float2 *>(&w3[8 * j + 2 * t]);
-    s00 = fmaf(fmaxf(c0[0], 0.f), w.x, fmaf(fmaxf(c0[1], 0.f), w.y, s00));
-    s01 = fmaf(fmaxf(c0[2], 0.f), w.x, fmaf(fmaxf(c0[3], 0.f), w.y, s01));
-    s10 = fmaf(fmaxf(c1[0], 0.f), w.x, fmaf(fmaxf(c1[1], 0.f), w.y, s10));
-    s11 = fmaf(fmaxf(c1[2], 0.f), w.x, fmaf(fmaxf(c1[3], 0.f), w.y, s11));
-  }
+    float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-  for (int o = 1; o <= 2; o <<= 1) {
-    s00 += __shfl_xor_sync(kFullMask, s00, o);
-    s01 += __shfl_xor_sync(kFullMask, s01, o);
-    s10 += __shfl_xor_sync(kFullMask, s10, o);
-    s11 += __shfl_xor_sync(kFullMask, s11, o);
+    for (int j = 0; j < 8; ++j) {
+      const float2 bb = *reinterpret_cast<const float2 *>(&b2[8 * j + 2 * t]);
+      float c[4] = {bb.x, bb.y, bb.x, bb.y};
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint2 b = w2[(kk * 8 + j) * 32 + lane];
+        mma_bf16(c, A[kk][0], A[kk][1], A[kk][2], A[kk][3], b.x, b.y);
+      }
+      const float2 w = *reinterpret_cast<const float2 *>(&w3[8 * j + 2 * t]);
+      s0 = fmaf(fmaxf(c[0], 0.f), w.x, fmaf(fmaxf(c[1], 0.f), w.y, s0));
+      s1 = fmaf(fmaxf(c[2], 0.f), w.x, fmaf(fmaxf(c[3], 0.f), w.y, s1));
+    }
+    s0 += __shfl_xor_sync(kFullMask, s0, 1);
+    s0 += __shfl_xor_sync(kFullMask, s0, 2);
+    s1 += __shfl_xor_sync(kFullMask, s1, 1);
+    s1 += __shfl_xor_sync(kFullMask, s1, 2);
+    o[2 * mt] = s0;      // row mt*16 + g
+    o[2 * mt + 1] = s1;  // row mt*16 + g + 8
   }
-  // quad q holds rows q, q + 8, 16 + q, 24 + q; row L is in quad L % 8
+  // row L lives in quad L % 8 as o[L / 8]
   const int src = (lane & 7) << 2, h = lane >> 3;
-  const float v0 = __shfl_sync(kFullMask, s00, src), v1 = __shfl_sync(kFullMask, s01, src),
-              v2 = __shfl_sync(kFullMask, s10, src), v3 = __shfl_sync(kFullMask, s11, src);
+  const float v0 = __shfl_sync(kFullMask, o[0], src), v1 = __shfl_sync(kFullMask, o[1], src),
+              v2 = __shfl_sync(kFullMask, o[2], src), v3 = __shfl_sync(kFullMask, o[3], src);
   return (h == 0 ? v0 : h == 1 ? v1 : h == 2 ? v2 : v3) + b3;
 }
 
 // The block's copy of what every lane reads per inference.
 struct NetShared {
   uint2 w2[4 * 8 * 32];
+  u32 w1[8 * 32];
   float b2[kHid], w3[kHid];
   float mean[kFeat], inv_std[kFeat];
 };
 
 __device__ __forceinline__ void load_net(const LearnedNet *net, NetShared &s) {
   for (int k = threadIdx.x; k < 4 * 8 * 32; k += blockDim.x) s.w2[k] = net->w2[k];
+  for (int k = threadIdx.x; k < 8 * 32; k += blockDim.x) s.w1[k] = net->w1[k];
   for (int k = threadIdx.x; k < kHid; k += blockDim.x) {
     s.b2[k] = net->b2[k];
     s.w3[k] = net->w3[k];
@@ -230,13 +225,25 @@ __device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
   return r;
 }
 
-// Work items of the learned walk: (task, group) pairs, item k = t * ng + g.
-// A task is a subtree (the nodes at the split depth, and leaves above it, in
-// node order); the nodes above the split depth are opened for every group.
-// Each lane appends the lists of its items to its own region (cells, and
-// runs of bodies (first, count)); a gather pass concatenates a group's
-// items in task order into the group's lists.
-constexpr u32 kNoItem = 0xffffffffu;
+// The learned walk runs in rounds. Round 0's items are (task, group) pairs:
+// a task is a subtree (the nodes at the split depth, and leaves above it, in
+// node order) and the nodes above the split depth are opened for every
+// group. A walk decides what the guard and the prior settle and defers the
+// rest, the (group, cell) pairs whose centred prior lies within the band of
+// the group's tolerance, skipping their subtrees. A dense kernel then runs
+// the network on all deferred pairs at once, 32 rows per warp on the tensor
+// cores, and the next round's items are those pairs with the network's
+// decision: accept the cell, or walk its children (deferring again). The
+// walk kernel itself carries no network and few registers, so many warps
+// hide its memory latency, and the network's latency is off its path.
+//
+// Each lane appends what its items produce to its own region: accepted
+// cells, runs of bodies (first, count) and deferred nodes. A gather pass
+// concatenates a group's items in (round, item) order into the group's
+// lists. Item storage is grouped by group: round 0 item (t, g) is stored at
+// g * ntasks + t, and the deferred pairs of a round keep that order.
+constexpr u64 kNoItem = ~0ull;
+constexpr int kMaxRounds = kMaxDepth + 4;
 
 struct LArgs {
   const WalkRec32 *walk32;
@@ -246,61 +253,40 @@ struct LArgs {
   const float *gboxf;
   const float2 *gtol;
   u32 ng;
-  u64 nitems;
-  const LearnedNet *net;
+  u32 round;
+  u64 nitems;              // items of this round
+  u64 item_base;           // global index of the round's first item
+  const uint2 *qitems;     // rounds > 0: (group, node) of each item
+  const u8 *qdec;          // rounds > 0: the network's decision (1: accept)
   const TreeRoot *root;
   const double2 *mom;
-  float inv_theta_guard, band;
-  int batch_min;
-  u32 lane_cells, lane_runs;  // capacity of each lane's region
+  float inv_theta_guard, band, y_mean;
+  u32 lane_cells, lane_runs, lane_pend;  // capacity of each lane's regions
   u32 *reg_cells;
   uint2 *reg_runs;
+  u32 *reg_pend;
+  u32 *lane_fill;          // per lane: cells, runs, deferred used so far
   uint4 *seg;              // per item: first cell, cells, first run, runs (region indices)
-  u32 *seg_bodies;         // per item: bodies
+  uint4 *seg2;             // per item: first deferred, deferred, bodies, 0
+  u32 *pcount;             // per item of the round (storage order): deferred
   Scalars *sc;
 };
 
-// The learned walk. Each lane walks one item at a time in the plain walk's
-// node order (a forward scan with skip links) and takes the next item as
-// soon as it is done (one counter), so the lanes of a warp stay busy until
-// the work runs out, and no group's walk is longer than its longest task.
-// Per visited node:
-//   overlap, or inside the guard (2 h / theta_guard + delta) -> opened
-//   guarded with two bodies or fewer                           -> accepted (bodies, exact)
-//   centred prior below tau - band -> accepted; above tau + band -> opened
-//   otherwise the lane waits for the network.
-// A waiting lane keeps its node while the others walk on; the warp runs the
-// network once `batch_min` lanes wait, or every active lane does. A row's
-// result does not depend on the other rows, so the decisions do not depend
-// on the schedule.
-// kNet = false: band 0, the prior decides every test and the kernel carries
-// no network (fewer registers, more warps in flight).
-template <bool kNet>
-__global__ void __launch_bounds__(kT) k_lwalk(LArgs a) {
-  __shared__ NetShared sn;
-  __shared__ uint4 rows[kT / 32][kNet ? 32 : 1];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  u32 w1[8];
-  if (kNet) {
-    load_net(a.net, sn);
-    rows[warp][lane] = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) w1[j] = a.net->w1[j * 32 + lane];
-  }
-  const float b3 = a.net->b3, y_mean = a.net->y_mean, inv_y_std = 1.f / a.net->y_std;
-  __syncthreads();
+__global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
+  const int lane = threadIdx.x & 31;
   const FeatScale fs = scale_of(a.root, a.mom);
   const u64 gtid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  u32 lc = a.lane_fill[3 * gtid], lr = a.lane_fill[3 * gtid + 1], lp = a.lane_fill[3 * gtid + 2];
   u32 *reg_c = a.reg_cells + gtid * a.lane_cells;
   uint2 *reg_r = a.reg_runs + gtid * a.lane_runs;
+  u32 *reg_p = a.reg_pend + gtid * a.lane_pend;
   Scalars *sc = a.sc;
 
-  u64 item = kNoItem;
-  u32 i = 0, end = 0, lc = 0, lr = 0, c0i = 0, r0i = 0, nb = 0;
-  bool exhausted = false, waiting = false;
-  float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f}, f0 = 0.f, tau = 0.f, thr = 0.f;
-  WalkRec32 r{};
-  unsigned long long rows_run = 0, batches = 0;
+  u64 item = kNoItem, store = 0;
+  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0;
+  int pre = -1;  // the network's decision on a deferred item's node
+  bool exhausted = false;
+  float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f}, tau = 0.f;
   while (true) {
     // idle lanes take the next items (one atomic per warp)
     const bool want = item == kNoItem && !exhausted;
@@ -308,7 +294,8 @@ __global__ void __launch_bounds__(kT) k_lwalk(LArgs a) {
     if (wantm) {
       const int leader = __ffs(wantm) - 1;
       unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&sc->walk_items, static_cast<unsigned long long>(__popc(wantm)));
+      if (lane == leader)
+        base = atomicAdd(&sc->walk_items, static_cast<unsigned long long>(__popc(wantm)));
       base = __shfl_sync(kFullMask, base, leader);
       if (want) {
         const u64 k = base + __popc(wantm & ((1u << lane) - 1u));
@@ -316,7 +303,21 @@ __global__ void __launch_bounds__(kT) k_lwalk(LArgs a) {
           exhausted = true;
         } else {
           item = k;
-          const u32 t = static_cast<u32>(k / a.ng), g = static_cast<u32>(k % a.ng);
+          u32 g;
+          if (a.round == 0) {
+            const u32 t = static_cast<u32>(k / a.ng);
+            g = static_cast<u32>(k % a.ng);
+            store = static_cast<u64>(g) * a.ntasks + t;
+            i = a.tasks[t].x;
+            pre = -1;
+          } else {
+            const uint2 q = a.qitems[k];
+            g = q.x;
+            i = q.y;
+            store = k;
+            pre = a.qdec[k];
+          }
+          end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.walk32 + i) + 2).x);
           const float4 b0 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g],
                        b1 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g + 1];
           gf[0] = b0.x;
@@ -325,24 +326,24 @@ __global__ void __launch_bounds__(kT) k_lwalk(LArgs a) {
           hf[0] = b0.w;
           hf[1] = b1.x;
           hf[2] = b1.y;
-          const float2 gt = a.gtol[g];
-          f0 = gt.x;
-          tau = gt.y;
-          i = a.tasks[t].x;
-          end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.walk32 + i) + 2).x);
+          tau = a.gtol[g].y;
           c0i = lc;
           r0i = lr;
+          p0i = lp;
           nb = 0;
         }
       }
     }
-    const bool active = item != kNoItem;
-    const unsigned act = __ballot_sync(kFullMask, active);
-    if (act == 0) break;
+    if (__ballot_sync(kFullMask, item != kNoItem) == 0) break;
+    if (item == kNoItem) continue;  // the lanes meet again at the next ballot
 
-    int verdict = -1;
-    if (active && !waiting) {
-      r = load_rec(a.walk32, i);
+    const WalkRec32 r = load_rec(a.walk32, i);
+    const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+    int verdict;  // 0 open, 1 accept, 2 defer
+    if (pre >= 0) {
+      verdict = pre;
+      pre = -1;
+    } else {
       const float4 c0 = __ldg(reinterpret_cast<const float4 *>(a.cfeat + i));
       // the reference's overlap test (group_lists.cpp:147), in FP32
       const bool overlap = fabsf(r.cx - gf[0]) <= r.slack + hf[0] &&
@@ -353,88 +354,137 @@ __global__ void __launch_bounds__(kT) k_lwalk(LArgs a) {
                   dz = fmaxf(fabsf(r.mz - gf[2]) - hf[2], 0.f);
       const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       const float crit = fmaf(2.f * c0.x, a.inv_theta_guard, c0.y);
-      const u32 nbody = r.nbody_leaf & 0x7fffffffu;
       if (overlap || !(d2 > crit * crit)) {
         verdict = 0;
       } else if (nbody <= kFewBodies) {
         verdict = 1;
       } else {
-        const float f2 = distance_feature(d2, fs);
-        const float e = prior_log2err(c0.z, f2) + y_mean;  // centred prior
-        if (!kNet) {
-          verdict = e < tau ? 1 : 0;
-        } else if (e < tau - a.band) {
-          verdict = 1;
-        } else if (e > tau + a.band) {
-          verdict = 0;
-        } else {
-          const float4 c1 = __ldg(reinterpret_cast<const float4 *>(a.cfeat + i) + 1);
-          const float f[kFeat] = {f0, c0.w, f2, c1.x, c1.y, c1.z};
-          rows[warp][lane] = feature_row(f, sn);
-          thr = (tau - e) * inv_y_std;
-          waiting = true;
-        }
+        const float e = prior_log2err(c0.z, distance_feature(d2, fs)) + a.y_mean;
+        verdict = e < tau - a.band ? 1 : e > tau + a.band ? 0 : 2;
       }
     }
-    const unsigned wm = kNet ? __ballot_sync(kFullMask, waiting) : 0u;
-    if (kNet && wm != 0 && (__popc(wm) >= a.batch_min || wm == act)) {
-      __syncwarp();
-      const float y = warp_mlp(rows[warp], w1, sn.w2, sn.b2, sn.w3, b3, lane);
-      if (waiting) {
-        verdict = y < thr ? 1 : 0;
-        waiting = false;
-      }
-      rows_run += __popc(wm);
-      ++batches;
-      __syncwarp();
+    if (verdict == 2) {
+      if (lp < a.lane_pend) reg_p[lp] = i;
+      ++lp;
+    } else if (verdict == 1 && nbody > kFewBodies) {
+      if (lc < a.lane_cells) reg_c[lc] = i;
+      ++lc;
+    } else if (verdict == 1 || (r.nbody_leaf >> 31)) {
+      if (lr < a.lane_runs) reg_r[lr] = make_uint2(r.begin, nbody);
+      ++lr;
+      nb += nbody;
     }
-
-    if (verdict >= 0) {
-      const u32 nbody = r.nbody_leaf & 0x7fffffffu;
-      if (verdict == 1 || (r.nbody_leaf >> 31)) {
-        if (verdict == 1 && nbody > kFewBodies) {
-          if (lc < a.lane_cells) reg_c[lc] = i;
-          ++lc;
-        } else {
-          if (lr < a.lane_runs) reg_r[lr] = make_uint2(r.begin, nbody);
-          ++lr;
-          nb += nbody;
-        }
-        if (r.skip <= i) {  // malformed tree: never loop
-          atomicOr(&sc->error, 1u);
-          i = end;
-        } else {
-          i = r.skip;
-        }
+    if (verdict != 0 || (r.nbody_leaf >> 31)) {
+      if (r.skip <= i) {  // malformed tree: never loop
+        atomicOr(&sc->error, 1u);
+        i = end;
       } else {
-        ++i;
+        i = r.skip;
       }
-      if (i >= end) {  // the item is done
-        a.seg[item] = make_uint4(static_cast<u32>(gtid * a.lane_cells + c0i), lc - c0i,
-                                 static_cast<u32>(gtid * a.lane_runs + r0i), lr - r0i);
-        a.seg_bodies[item] = nb;
-        item = kNoItem;
-      }
+    } else {
+      ++i;
+    }
+    if (i >= end) {  // the item is done
+      const u64 gi = a.item_base + store;
+      a.seg[gi] = make_uint4(static_cast<u32>(gtid * a.lane_cells + c0i), lc - c0i,
+                             static_cast<u32>(gtid * a.lane_runs + r0i), lr - r0i);
+      a.seg2[gi] = make_uint4(static_cast<u32>(gtid * a.lane_pend + p0i), lp - p0i, nb, 0u);
+      a.pcount[store] = lp - p0i;
+      item = kNoItem;
     }
   }
-  if (lc > a.lane_cells || lr > a.lane_runs) atomicOr(&sc->list_overflow, 1u);
-  if (lane == 0 && batches) {
-    atomicAdd(&sc->mlp_rows, rows_run);
-    atomicAdd(&sc->mlp_batches, batches);
-  }
+  a.lane_fill[3 * gtid] = lc;
+  a.lane_fill[3 * gtid + 1] = lr;
+  a.lane_fill[3 * gtid + 2] = lp;
+  if (lc > a.lane_cells || lr > a.lane_runs || lp > a.lane_pend) atomicOr(&sc->list_overflow, 1u);
 }
+
+// Start of every group's deferred pairs in the next round's item order
+// (round 0 items of group g start at g * ntasks; later rounds' at the
+// previous round's starts), from the exclusive scan of the deferred counts.
+__global__ void __launch_bounds__(kT)
+    k_lgstart(u32 round, u32 ng, u32 ntasks, const u32 *poff, const u32 *prev, u32 *out) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g > ng) return;
+  const u64 first = round == 0 ? static_cast<u64>(g) * ntasks : prev[g];
+  out[g] = poff[first];
+}
+
+// The deferred pairs of a round, in storage order, as the next round's items.
+__global__ void __launch_bounds__(kT)
+    k_lcompact(u32 round, u64 nitems, u64 item_base, u32 ntasks, const uint2 *qitems,
+               const uint4 *seg2, const u32 *poff, const u32 *reg_pend, uint2 *next) {
+  const u64 j = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (j >= nitems) return;
+  const uint4 s2 = seg2[item_base + j];
+  if (s2.y == 0) return;
+  const u32 g = round == 0 ? static_cast<u32>(j / ntasks) : qitems[j].x;
+  const u32 o = poff[j];
+  for (u32 m = 0; m < s2.y; ++m) next[o + m] = make_uint2(g, reg_pend[s2.x + m]);
+}
+
+// The network's decision on every deferred pair: one warp per 32 pairs.
+__global__ void __launch_bounds__(kT)
+    k_ldecide(const uint2 *q, u64 nq, const WalkRec32 *walk32, const CellFeat *cfeat,
+              const float *gboxf, const float2 *gtol, const LearnedNet *net, const TreeRoot *root,
+              const double2 *mom, u8 *dec) {
+  __shared__ NetShared sn;
+  __shared__ uint4 rows[kT / 32][32];
+  load_net(net, sn);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u64 k = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  float thr = 0.f;
+  uint4 row = make_uint4(0u, 0u, 0u, 0u);
+  if (k < nq) {
+    const FeatScale fs = scale_of(root, mom);
+    const uint2 qk = q[k];
+    const u32 g = qk.x, p = qk.y;
+    const float4 b0 = reinterpret_cast<const float4 *>(gboxf)[2ull * g],
+                 b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
+    const WalkRec32 r = load_rec(walk32, p);
+    const float4 c0 = __ldg(reinterpret_cast<const float4 *>(cfeat + p));
+    const float4 c1 = __ldg(reinterpret_cast<const float4 *>(cfeat + p) + 1);
+    const float dx = fmaxf(fabsf(r.mx - b0.x) - b0.w, 0.f),
+                dy = fmaxf(fabsf(r.my - b0.y) - b1.x, 0.f),
+                dz = fmaxf(fabsf(r.mz - b0.z) - b1.y, 0.f);
+    const float f2 = distance_feature(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), fs);
+    const float2 gt = gtol[g];
+    const float e = prior_log2err(c0.z, f2) + net->y_mean;
+    thr = (gt.y - e) / net->y_std;
+    const float f[kFeat] = {gt.x, c0.w, f2, c1.x, c1.y, c1.z};
+    row = feature_row(f, sn);
+  }
+  rows[warp][lane] = row;
+  __syncwarp();
+  const float y = warp_mlp(rows[warp], sn.w1, sn.w2, sn.b2, sn.w3, net->b3, lane);
+  if (k < nq) dec[k] = y < thr ? 1 : 0;
+}
+
+struct RoundView {
+  const u64 *base;         // per round: global index of its first item
+  const u32 *gstart;       // per round r >= 1: [ng + 1] starts of the groups' items
+  u32 rounds, ntasks, ng;
+};
 
 // Per group: its items' cells and bodies summed, and the list counters.
 __global__ void __launch_bounds__(kT)
-    k_lsum(const uint4 *seg, const u32 *seg_bodies, u32 ng, u32 ntasks, const u32 *gbegin,
+    k_lsum(const uint4 *seg, const uint4 *seg2, RoundView rv, const u32 *gbegin,
            const u32 *gend, u64 *ncells, u64 *nbodies, Scalars *sc) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
+  if (g >= rv.ng) return;
   u64 nc = 0, nb = 0;
-  for (u32 t = 0; t < ntasks; ++t) {
-    const u64 k = static_cast<u64>(t) * ng + g;
+  for (u32 t = 0; t < rv.ntasks; ++t) {
+    const u64 k = static_cast<u64>(g) * rv.ntasks + t;
     nc += seg[k].y;
-    nb += seg_bodies[k];
+    nb += seg2[k].z;
+  }
+  for (u32 r = 1; r < rv.rounds; ++r) {
+    const u32 *st = rv.gstart + static_cast<u64>(r - 1) * (rv.ng + 1);
+    for (u32 j = st[g]; j < st[g + 1]; ++j) {
+      nc += seg[rv.base[r] + j].y;
+      nb += seg2[rv.base[r] + j].z;
+    }
   }
   ncells[g] = nc;
   nbodies[g] = nb;
@@ -445,47 +495,67 @@ __global__ void __launch_bounds__(kT)
   atomicMax(&sc->max_group, static_cast<u32>(tg));
 }
 
-// One warp per group: its items' lists in task order, into the group's
-// ranges of cell_list and body_list, and its GTGroup record.
+// Copies one item's cells and body runs (warp-cooperative) to the group's lists.
+__device__ __forceinline__ void copy_item(const uint4 &sg, const u32 *reg_cells,
+                                          const uint2 *reg_runs, u32 *cell_list, u32 *body_list,
+                                          u64 &oc, u64 &ob, int lane) {
+  for (u32 k = lane; k < sg.y; k += 32) cell_list[oc + k] = reg_cells[sg.x + k];
+  oc += sg.y;
+  for (u32 k0 = 0; k0 < sg.w; k0 += 32) {
+    const u32 k = k0 + lane;
+    const uint2 run = k < sg.w ? reg_runs[sg.z + k] : make_uint2(0u, 0u);
+    u32 incl = run.y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 v = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const u64 start = ob + incl - run.y;
+    for (u32 j = 0; j < run.y; ++j) body_list[start + j] = run.x + j;
+    ob += __shfl_sync(kFullMask, incl, 31);
+  }
+}
+
+// One warp per group: its items' lists in (round, item) order into the
+// group's ranges of cell_list and body_list, and its GTGroup record.
 constexpr int kGatherWarps = kT / 32;
 
 __global__ void __launch_bounds__(kT)
-    k_lgather(const uint4 *seg, u32 ng, u32 ntasks, const u32 *reg_cells, const uint2 *reg_runs,
+    k_lgather(const uint4 *seg, RoundView rv, const u32 *reg_cells, const uint2 *reg_runs,
               const u32 *gbegin, const u32 *gend, const u64 *cell_off, const u64 *body_off,
               u32 *cell_list, u32 *body_list, uint4 *groups) {
   const u32 g = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (g >= ng) return;
+  if (g >= rv.ng) return;
   u64 oc = cell_off[g], ob = body_off[g];
   if (lane == 0) {
     groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(oc),
                                   static_cast<u32>(cell_off[g + 1]));
     groups[2ull * g + 1] = make_uint4(static_cast<u32>(ob), static_cast<u32>(body_off[g + 1]), 0u, 0u);
   }
-  for (u32 t0 = 0; t0 < ntasks; t0 += 32) {
-    // the next (up to) 32 items of the group, one per lane
-    const u32 t = t0 + lane;
-    const uint4 sgm = t < ntasks ? seg[static_cast<u64>(t) * ng + g] : make_uint4(0u, 0u, 0u, 0u);
-    unsigned busy = __ballot_sync(kFullMask, sgm.y != 0 || sgm.w != 0);
-    while (busy) {
-      const int src = __ffs(busy) - 1;
-      busy &= busy - 1u;
-      const u32 c0 = __shfl_sync(kFullMask, sgm.x, src), nc = __shfl_sync(kFullMask, sgm.y, src);
-      const u32 r0 = __shfl_sync(kFullMask, sgm.z, src), nr = __shfl_sync(kFullMask, sgm.w, src);
-      for (u32 k = lane; k < nc; k += 32) cell_list[oc + k] = reg_cells[c0 + k];
-      oc += nc;
-      for (u32 k0 = 0; k0 < nr; k0 += 32) {
-        const u32 k = k0 + lane;
-        const uint2 run = k < nr ? reg_runs[r0 + k] : make_uint2(0u, 0u);
-        u32 incl = run.y;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const u32 v = __shfl_up_sync(kFullMask, incl, o);
-          if (lane >= o) incl += v;
-        }
-        const u64 start = ob + incl - run.y;
-        for (u32 j = 0; j < run.y; ++j) body_list[start + j] = run.x + j;
-        ob += __shfl_sync(kFullMask, incl, 31);
+  for (u32 r = 0; r < rv.rounds; ++r) {
+    u64 first, count;
+    if (r == 0) {
+      first = static_cast<u64>(g) * rv.ntasks;
+      count = rv.ntasks;
+    } else {
+      const u32 *st = rv.gstart + static_cast<u64>(r - 1) * (rv.ng + 1);
+      first = rv.base[r] + st[g];
+      count = st[g + 1] - st[g];
+    }
+    for (u64 j0 = 0; j0 < count; j0 += 32) {
+      // the next (up to) 32 items of the group, one per lane
+      const u64 j = j0 + lane;
+      const uint4 sg = j < count ? seg[first + j] : make_uint4(0u, 0u, 0u, 0u);
+      unsigned busy = __ballot_sync(kFullMask, sg.y != 0 || sg.w != 0);
+      while (busy) {
+        const int src = __ffs(busy) - 1;
+        busy &= busy - 1u;
+        const uint4 s = make_uint4(__shfl_sync(kFullMask, sg.x, src),
+                                   __shfl_sync(kFullMask, sg.y, src),
+                                   __shfl_sync(kFullMask, sg.z, src),
+                                   __shfl_sync(kFullMask, sg.w, src));
+        copy_item(s, reg_cells, reg_runs, cell_list, body_list, oc, ob, lane);
       }
     }
   }
@@ -499,9 +569,6 @@ __global__ void __launch_bounds__(kT)
   __shared__ uint4 rows[kT / 32][32];
   load_net(net, sn);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  u32 w1[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) w1[j] = net->w1[j * 32 + lane];
   __syncthreads();
   const u64 k = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
   float f[kFeat] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -509,7 +576,7 @@ __global__ void __launch_bounds__(kT)
     for (int j = 0; j < kFeat; ++j) f[j] = feat[k * kFeat + j];
   rows[warp][lane] = feature_row(f, sn);
   __syncwarp();
-  const float y = warp_mlp(rows[warp], w1, sn.w2, sn.b2, sn.w3, net->b3, lane);
+  const float y = warp_mlp(rows[warp], sn.w1, sn.w2, sn.b2, sn.w3, net->b3, lane);
   if (k < n) {
     const float prior = kPriorBase + f[3] + 3.f * f[1];
     pred[k] = prior_log2err(prior, f[2]) + net->y_mean + net->y_std * y;
@@ -557,18 +624,17 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   int dev = 0, sms = 0, per_sm = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const bool net = lw.band > 0.f;
-  if (net)
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lwalk<true>, kT, 0));
-  else
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lwalk<false>, kT, 0));
+  GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lwalk, kT, 0));
   const u32 blocks = static_cast<u32>(std::max(1, sms * std::max(1, per_sm)));
   const u64 lanes = static_cast<u64>(blocks) * kT;
-  const u64 nitems = static_cast<u64>(ng) * ntasks;
+  const u64 n0 = static_cast<u64>(ng) * ntasks;
+  LearnedScratch &ls = *lw.scratch;
   ws.gcells.ensure(static_cast<u64>(ng) * 8);
   ws.gbodies.ensure(static_cast<u64>(ng) * 8);
   ws.gcell_off.ensure((static_cast<u64>(ng) + 1) * 8);
   ws.gbody_off.ensure((static_cast<u64>(ng) + 1) * 8);
+  ls.gstart.ensure(static_cast<u64>(kMaxRounds) * (ng + 1) * sizeof(u32));
+  ls.lane_fill.ensure(lanes * 3 * sizeof(u32));
   LArgs a{};
   a.walk32 = ws.walk32.as<WalkRec32>();
   a.cfeat = lw.cfeat;
@@ -577,70 +643,145 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   a.gboxf = ws.gboxf.as<float>();
   a.gtol = lw.gtol->as<float2>();
   a.ng = ng;
-  a.nitems = nitems;
-  a.net = lw.net;
   a.root = ws.root.as<TreeRoot>();
   a.mom = ws.mom.as<double2>();
   a.inv_theta_guard = lw.inv_theta_guard;
   a.band = lw.band;
-  a.batch_min = lw.batch_min;
+  a.y_mean = lw.y_mean;
+  a.lane_fill = ls.lane_fill.as<u32>();
   a.sc = sc;
-  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  // each lane's region holds what its items append; if one outgrows it, the
-  // regions double and the walk runs again
-  u32 lane_cells = std::max<u32>(*lw.lane_cells, 256), lane_runs = std::max<u32>(*lw.lane_runs, 64);
+  std::vector<u64> base;
   for (int attempt = 0;; ++attempt) {
-    const u64 seg_bytes = nitems * (sizeof(uint4) + sizeof(u32));
-    const u64 reg_bytes = lanes * (static_cast<u64>(lane_cells) * 4 + static_cast<u64>(lane_runs) * 8);
-    lw.scratch->ensure(seg_bytes + reg_bytes);
-    char *base = lw.scratch->as<char>();
-    a.seg = reinterpret_cast<uint4 *>(base);
-    a.reg_runs = reinterpret_cast<uint2 *>(base + nitems * sizeof(uint4));
-    a.reg_cells = reinterpret_cast<u32 *>(base + nitems * sizeof(uint4) +
-                                          lanes * static_cast<u64>(lane_runs) * 8);
-    a.seg_bodies = reinterpret_cast<u32 *>(base + nitems * sizeof(uint4) + reg_bytes);
-    a.lane_cells = lane_cells;
-    a.lane_runs = lane_runs;
+    // lane regions (grown and walked again if one overflows)
+    const u64 reg_bytes = lanes * (static_cast<u64>(ls.lane_cells) * 4 +
+                                   static_cast<u64>(ls.lane_runs) * 8 +
+                                   static_cast<u64>(ls.lane_pend) * 4);
+    ls.regions.ensure(reg_bytes);
+    char *rb = ls.regions.as<char>();
+    a.reg_runs = reinterpret_cast<uint2 *>(rb);
+    a.reg_cells = reinterpret_cast<u32 *>(rb + lanes * static_cast<u64>(ls.lane_runs) * 8);
+    a.reg_pend = a.reg_cells + lanes * static_cast<u64>(ls.lane_cells);
+    a.lane_cells = ls.lane_cells;
+    a.lane_runs = ls.lane_runs;
+    a.lane_pend = ls.lane_pend;
+    GTC_CUDA(cudaMemsetAsync(a.lane_fill, 0, lanes * 3 * sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
-    GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 3 * sizeof(unsigned long long), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
-    if (net)
-      k_lwalk<true><<<blocks, kT, 0, s>>>(a);
-    else
-      k_lwalk<false><<<blocks, kT, 0, s>>>(a);
-    GTC_LAUNCH_CHECK();
-    k_lsum<<<ceil_div(ng, kT), kT, 0, s>>>(a.seg, a.seg_bodies, ng, ntasks, ws.gbegin.as<u32>(),
-                                           ws.gend.as<u32>(), ws.gcells.as<u64>(),
-                                           ws.gbodies.as<u64>(), sc);
-    GTC_LAUNCH_CHECK();
-    exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, ng, cell_off + ng, ws.scan_tmp, s);
-    exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, ng, body_off + ng, ws.scan_tmp, s);
-    GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + ng, 8, cudaMemcpyDeviceToDevice, s));
-    GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + ng, 8, cudaMemcpyDeviceToDevice, s));
-    GTC_CUDA(cudaMemcpyAsync(host, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-    GTC_CUDA(cudaStreamSynchronize(s));
-    if (host->error)
-      throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                         std::to_string(host->error) + ")");
-    if (!host->list_overflow) break;
-    if (attempt >= 4 || lanes * lane_cells * 2 > 0xffffffffull ||
-        lanes * lane_runs * 2 > 0xffffffffull)
+    base.assign(1, 0);
+    u64 nitems = n0, total_items = 0, rows = 0, batches = 0;
+    int qsel = 0;
+    bool overflow = false;
+    for (u32 round = 0;; ++round) {
+      if (round >= static_cast<u32>(kMaxRounds))
+        throw RuntimeError("learned walk: more rounds than the tree has levels");
+      const u64 need = base.back() + nitems;
+      if (need > ls.items_cap) {  // grow the item arrays, keeping what is there
+        const u64 cap = std::max<u64>(need + need / 2, n0 + 4ull * ng);
+        DeviceBuffer nseg;
+        nseg.ensure(cap * 2 * sizeof(uint4));
+        if (ls.items_cap && base.back())
+          for (int h = 0; h < 2; ++h)
+            GTC_CUDA(cudaMemcpyAsync(nseg.as<uint4>() + h * cap, ls.seg.as<uint4>() + h * ls.items_cap,
+                                     base.back() * sizeof(uint4), cudaMemcpyDeviceToDevice, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        ls.seg.release();
+        ls.seg = nseg;
+        ls.items_cap = cap;
+      }
+      a.seg = ls.seg.as<uint4>();
+      a.seg2 = a.seg + ls.items_cap;
+      ls.pcount.ensure((nitems + 1) * sizeof(u32));
+      ls.poff.ensure((nitems + 1) * sizeof(u32));
+      a.pcount = ls.pcount.as<u32>();
+      a.round = round;
+      a.nitems = nitems;
+      a.item_base = base.back();
+      a.qitems = round ? ls.q[qsel].as<uint2>() : nullptr;
+      a.qdec = round ? ls.dec[qsel].as<u8>() : nullptr;
+      GTC_CUDA(cudaMemsetAsync(&sc->walk_items, 0, sizeof(unsigned long long), s));
+      k_lwalk<<<blocks, kT, 0, s>>>(a);
+      GTC_LAUNCH_CHECK();
+      u32 *poff = ls.poff.as<u32>();
+      exclusive_scan_u32(a.pcount, poff, nitems, poff + nitems, ws.scan_tmp, s);
+      u32 *gst = ls.gstart.as<u32>() + static_cast<u64>(round) * (ng + 1);
+      k_lgstart<<<ceil_div(ng + 1, kT), kT, 0, s>>>(
+          round, ng, ntasks, poff, round ? gst - (ng + 1) : nullptr, gst);
+      GTC_LAUNCH_CHECK();
+      u32 deferred = 0, flags[2] = {0, 0};
+      GTC_CUDA(cudaMemcpyAsync(&deferred, poff + nitems, sizeof(u32), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(flags, &sc->list_overflow, sizeof(u32), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(flags + 1, &sc->error, sizeof(u32), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+      total_items = base.back() + nitems;
+      if (flags[1])
+        throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                           std::to_string(flags[1]) + ")");
+      if (flags[0]) {
+        overflow = true;
+        break;
+      }
+      if (deferred == 0) break;
+      // the deferred pairs become the next round's items, with the network's decisions
+      const int nq = qsel ^ 1;
+      ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
+      ls.dec[nq].ensure(deferred);
+      k_lcompact<<<ceil_div(nitems, kT), kT, 0, s>>>(round, nitems, base.back(), ntasks,
+                                                    a.qitems, a.seg2, poff, a.reg_pend,
+                                                    ls.q[nq].as<uint2>());
+      GTC_LAUNCH_CHECK();
+      k_ldecide<<<ceil_div(deferred, kT), kT, 0, s>>>(
+          ls.q[nq].as<uint2>(), deferred, a.walk32, a.cfeat, a.gboxf, a.gtol, lw.net, a.root,
+          a.mom, ls.dec[nq].as<u8>());
+      GTC_LAUNCH_CHECK();
+      rows += deferred;
+      batches += (deferred + 31) / 32;
+      qsel = nq;
+      base.push_back(total_items);
+      nitems = deferred;
+    }
+    if (!overflow) {
+      host->mlp_rows = rows;
+      host->mlp_batches = batches;
+      break;
+    }
+    if (attempt >= 4 || lanes * static_cast<u64>(ls.lane_cells) * 2 > 0xffffffffull ||
+        lanes * static_cast<u64>(ls.lane_runs) * 2 > 0xffffffffull ||
+        lanes * static_cast<u64>(ls.lane_pend) * 2 > 0xffffffffull)
       throw RuntimeError("learned walk: the lane regions keep overflowing");
-    lane_cells *= 2;
-    lane_runs *= 2;
+    ls.lane_cells *= 2;
+    ls.lane_runs *= 2;
+    ls.lane_pend *= 2;
   }
-  *lw.lane_cells = lane_cells;
-  *lw.lane_runs = lane_runs;
-  if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
+  const u32 rounds = static_cast<u32>(base.size());
+  ls.base.ensure(rounds * sizeof(u64));
+  GTC_CUDA(cudaMemcpyAsync(ls.base.ptr, base.data(), rounds * sizeof(u64), cudaMemcpyHostToDevice, s));
+  GTC_CUDA(cudaMemcpyAsync(&sc->mlp_rows, &host->mlp_rows, 2 * sizeof(unsigned long long),
+                           cudaMemcpyHostToDevice, s));
+  const RoundView rv{ls.base.as<u64>(), ls.gstart.as<u32>(), rounds, ntasks, ng};
+  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
+  k_lsum<<<ceil_div(ng, kT), kT, 0, s>>>(a.seg, a.seg2, rv, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
+                                         ws.gcells.as<u64>(), ws.gbodies.as<u64>(), sc);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, ng, cell_off + ng, ws.scan_tmp, s);
+  exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, ng, body_off + ng, ws.scan_tmp, s);
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + ng, 8, cudaMemcpyDeviceToDevice, s));
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + ng, 8, cudaMemcpyDeviceToDevice, s));
+  u64 totals[2] = {0, 0};
+  GTC_CUDA(cudaMemcpyAsync(totals, &sc->n_cell_list, sizeof(totals), cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  if (totals[0] > 0xffffffffull || totals[1] > 0xffffffffull)
     throw RuntimeError("interaction lists too long for 32 bit offsets");
-  ws.n_cell_list = host->n_cell_list;
-  ws.n_body_list = host->n_body_list;
+  ws.n_cell_list = totals[0];
+  ws.n_body_list = totals[1];
+  host->n_cell_list = totals[0];
+  host->n_body_list = totals[1];
   ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   k_lgather<<<ceil_div(ng, kGatherWarps), kT, 0, s>>>(
-      a.seg, ng, ntasks, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
-      cell_off, body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>());
+      a.seg, rv, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(), cell_off,
+      body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>());
   GTC_LAUNCH_CHECK();
 }
 

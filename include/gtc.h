@@ -215,11 +215,10 @@ gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
  *                        cell closer than 2 h / guard + delta (the theta
  *                        test with this angle guards the network).
  *   "learned_band"       >= 0 log2 units, or < 0 for the model's own band
- *                        (default): tests whose error prior lies further than
- *                        this from the tolerance skip the network.
- *   "learned_batch_min"  1..32 (default 16): waiting lanes of a warp that
- *                        trigger a network evaluation.
- *   "learned_split_depth" 0..3 (default 2): the learned walk runs each group
+ *                        (default): tests whose centred error prior lies
+ *                        further than this from the tolerance are decided by
+ *                        it; the rest go to the network (0: prior only).
+ *   "learned_split_depth" 0..3 (default 1): the learned walk runs each group
  *                        as independent tasks, one per subtree at this depth
  *                        (the nodes above it are opened for every group).
  * GTC_INVALID_ARGUMENT for an unknown name or a value out of range. */
@@ -246,8 +245,9 @@ gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops);
  * log2(alpha * a_g * L^2 / (G M_total)), a_g = max(min |a|, mean |a| / 2)
  * over the group's targets, |a| from the context's previous solve of the
  * same bodies (caller order). Cells inside the guard (learned_guard_theta) are always opened.
- * The walk runs the network in BF16 on the tensor cores (mma.sync), FP32
- * accumulation.
+ * The walk defers the pairs the prior cannot settle; the network decides
+ * them in dense batches in BF16 on the tensor cores (mma.sync), FP32
+ * accumulation, and the walk continues under the cells it opens.
  * Fallback: with no model, or no previous solve of the same n, the call runs
  * the theta walk (gtc_stats.criterion_used says which ran). Every solve of a
  * context with a model records |a| for the next.
@@ -283,7 +283,7 @@ gtc_status gtc_learned_clear_samples(gtc_context *ctx);
  * `steps` Adam steps (learning rate lr) on random minibatches of `batch`
  * samples, mean squared error of the correction in normalised units. With
  * init = 1 first sets the normalisation from the samples and draws new
- * weights from `seed`. Afterwards sets the band to the 0.999 quantile of
+ * weights from `seed`. Afterwards sets the band to the 0.99 quantile of
  * |y_std net| over the samples. *loss: the last minibatch's loss. */
 gtc_status gtc_learned_train(gtc_context *ctx, uint64_t steps, uint32_t batch, float lr,
                              uint64_t seed, int init, double *loss);

@@ -288,6 +288,6 @@ def test_invalid_learned_arguments(ctx, gtc):
     with pytest.raises(ValueError):
         ctx.learned_set_model(bad[:10])
     with pytest.raises(gtc.GtcInvalidArgument):
-        ctx.set_option("learned_batch_min", 0)
+        ctx.set_option("learned_band_size", 1)
     with pytest.raises(gtc.GtcInvalidArgument):
         ctx.set_option("learned_split_depth", 7)
