@@ -10,6 +10,7 @@
 
 #include "../../include/gtc.h"
 #include "context.cuh"
+#include "integrate.cuh"
 
 static_assert(sizeof(gtc_float4) == 16 && alignof(gtc_float4) == 16, "float4 layout");
 static_assert(sizeof(gtc_kernel_params) == 32, "GTParams layout");
@@ -25,6 +26,7 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 unsigned long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 [[noreturn]] void throw_cuda(cudaError_t e, const char *what, const char *file, int line) {
+  (void)cudaGetLastError();  // a failed call leaves its error for the next check to find
   std::string msg = std::string("CUDA error ") + cudaGetErrorName(e) + " (" +
                     cudaGetErrorString(e) + ") in " + what + " at " + file + ":" +
                     std::to_string(line);
@@ -220,6 +222,163 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   ctx->last = sp;
 }
 
+// The leapfrog with each step replayed from one CUDA graph: kick and drift,
+// the whole grouped solve (tree, groups, walk, evaluation, scatter) and the
+// closing kick, with no host synchronisation inside. An eager solve sizes
+// the buffers first; the graph is captured with headroom over those sizes,
+// and a replay that outgrows them aborts (its kernels return) and the step's
+// evaluation and closing kick are redone eagerly, after which the graph is
+// captured again for the new sizes. Returns the steps replayed.
+u64 leapfrog_graph(gtc_context *ctx, double *pos, double *vel, const double *mass, double *acc,
+                   double *pot, u64 n, const gtc::SolverParams &sp, double dt, u64 steps,
+                   bool prime) {
+  cudaStream_t s = ctx->stream;
+  gtc::Workspace &ws = ctx->ws;
+  const double h = 0.5 * dt;
+  if (prime) {
+    group_force(ctx, pos, mass, n, sp, acc, pot);
+  } else {  // only to size the workspace: the caller's forces stay as they are
+    ws.acc.ensure(n * 24);
+    ws.pot.ensure(n * 8);
+    group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+  }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  auto drop = [&] {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  };
+  gtc::Scalars *sc = ws.scalars.as<gtc::Scalars>();
+  auto capture = [&] {
+    gtc::GraphCaps caps{};
+    const gtc::Scalars &hs = *ctx->host_sc;
+    const double f = 1.0 + ctx->graph_headroom;
+    const u64 pad = ctx->graph_headroom > 0 ? 1024 : 0;
+    caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
+    caps.depth = std::min<int>(gtc::kMaxDepth, static_cast<int>(hs.depth) + (pad ? 2 : 0));
+    caps.cells = static_cast<u64>(ws.n_cell_list * f) + 4 * pad;
+    caps.bodies = static_cast<u64>(ws.n_body_list * f) + 4 * pad;
+    const u64 m = caps.nodes;
+    ws.geom.ensure(m * 2 * sizeof(double2));
+    ws.mom.ensure(m * 2 * sizeof(double2));
+    ws.quad.ensure(m * 3 * sizeof(double2));
+    ws.delta.ensure(m * 8);
+    ws.nbegin.ensure(m * 4);
+    ws.nend.ensure(m * 4);
+    ws.skip.ensure(m * 4);
+    ws.parent.ensure(m * 4);
+    ws.depth.ensure(m);
+    ws.nchild.ensure(m);
+    ws.isleaf.ensure(m);
+    ws.bucket.ensure(m * 4);
+    ws.walk32.ensure(m * sizeof(gtc::WalkRec32));
+    ws.walk64.ensure(m * sizeof(gtc::WalkRec64));
+    ws.cells.ensure(m * 3 * sizeof(float4));
+    ws.flags.ensure(std::max<u64>(n, m) * 4);
+    ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
+    ws.gcells.ensure(n * 8);
+    ws.gbodies.ensure(n * 8);
+    ws.gcell_off.ensure((n + 1) * 8);
+    ws.gbody_off.ensure((n + 1) * 8);
+    ws.groups.ensure(n * 32);
+    ws.cell_list.ensure(caps.cells * 4);
+    ws.body_list.ensure(caps.bodies * 4);
+    ws.out.ensure(n * sizeof(float4));
+    ctx->counter.ensure(sizeof(u32));
+    gtc::reserve_scans(ws.scan_tmp, std::max<u64>(n, m));
+    gtc::write_root_task(ws, s);
+    GTC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      gtc::kick_drift(pos, vel, acc, n, h, dt, s);
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal));
+      gtc::build_tree_graph(ws, pos, mass, n, sp, caps, s);
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal));
+      gtc::build_lists_graph(ws, sp, caps, s);
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal));
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal));
+      gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
+                                ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
+                                ws.groups.as<uint4>(), n, sc, static_cast<float>(sp.G),
+                                static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0,
+                                ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[5], s, cudaEventRecordExternal));
+      gtc::scatter_results_graph(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, sc, s);
+      if (ctx->have_model) {
+        ctx->prev_amag.ensure(n * sizeof(float));
+        gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
+                                 ctx->prev_amag.as<float>(), s);
+      }
+      gtc::kick(vel, acc, n, h, s, &sc->abort);
+      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal));
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      throw;
+    }
+    GTC_CUDA(cudaStreamEndCapture(s, &graph));
+    GTC_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  };
+  u64 replays = 0;
+  try {
+    for (u64 k = 0; k < steps; ++k) {
+      if (!exec) capture();
+      GTC_CUDA(cudaGraphLaunch(exec, s));
+      GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, sc, sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+      const gtc::Scalars &hs = *ctx->host_sc;
+      if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
+      if (hs.error)
+        throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                                std::to_string(hs.error) + ")");
+      if (hs.abort) {
+        // outgrown: this step's evaluation and closing kick, eagerly; then a
+        // new graph for the new sizes
+        group_force(ctx, pos, mass, n, sp, acc, pot);
+        gtc::kick(vel, acc, n, h, s);
+        GTC_CUDA(cudaStreamSynchronize(s));
+        drop();
+        continue;
+      }
+      ++replays;
+      ws.n_nodes = hs.n_nodes;
+      ws.n_groups = hs.n_groups;
+      ws.n_cell_list = hs.n_cell_list;
+      ws.n_body_list = hs.n_body_list;
+      gtc_stats &st = ctx->stats;
+      st = gtc_stats{};
+      st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
+      st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+      st.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+      st.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+      st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
+      st.cell_interactions = hs.cell_interactions;
+      st.body_interactions = hs.body_interactions;
+      st.max_list = hs.max_list;
+      st.max_group = hs.max_group;
+      st.depth = hs.depth;
+      st.walk_tests_fp64 = hs.fp64_tests;
+      st.n_cell_list = hs.n_cell_list;
+      st.n_body_list = hs.n_body_list;
+      st.n_nodes = hs.n_nodes;
+      st.n_groups = hs.n_groups;
+      st.criterion_used = GTC_CRITERION_THETA;
+      st.kernel_launches = 0;  // one graph launch (its kernels were counted at capture)
+      ctx->have_group = true;
+      ctx->last = sp;
+    }
+  } catch (...) {
+    drop();
+    throw;
+  }
+  drop();
+  ctx->stats.graph_steps = static_cast<u32>(std::min<u64>(replays, 0xffffffffu));
+  return replays;
+}
+
 void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
                   const gtc::SolverParams &sp, double *acc, double *pot) {
   if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the CUDA kernels");
@@ -326,6 +485,7 @@ void gtc_destroy(gtc_context *ctx) {
                                &ctx->train_scratch, &ctx->cfeat, &ctx->gtol, &ctx->prev_amag})
     b->release();
   ctx->lscratch.release();
+  ctx->diag.release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
@@ -532,6 +692,9 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
       ctx->guard_theta = value;
     } else if (key == "learned_band") {
       ctx->band_override = value;
+    } else if (key == "graph_headroom") {
+      if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
+      ctx->graph_headroom = value;
     } else if (key == "learned_split_depth") {
       if (value != std::floor(value) || value < 0 || value > 3)
         throw gtc::InvalidArgument("learned_split_depth must be 0..3");
@@ -546,6 +709,66 @@ gtc_status gtc_measure_fp32_peak(gtc_context *ctx, double *tflops) {
   return guarded(ctx, [&] {
     if (!tflops) throw gtc::InvalidArgument("tflops is required");
     *tflops = gtc::fp32_peak_tflops(ctx->stream);
+  });
+}
+
+// ---------------------------------------------------- time integration
+
+gtc_status gtc_leapfrog_device(gtc_context *ctx, double *pos, double *vel, const double *mass,
+                               double *acc, double *pot, uint64_t n,
+                               const gtc_gravity_params *gp, int solver, double dt,
+                               uint64_t steps, int prime, int graph) {
+  return guarded(ctx, [&] {
+    if (solver != GTC_SOLVER_GROUP && solver != GTC_SOLVER_DIRECT)
+      throw gtc::InvalidArgument("unknown solver");
+    const gtc::SolverParams sp = check_params(gp, solver == GTC_SOLVER_GROUP);
+    if (!std::isfinite(dt)) throw gtc::InvalidArgument("dt must be finite");
+    if (n == 0) return;
+    if (!pos || !vel || !mass || !acc || !pot)
+      throw gtc::InvalidArgument("pos, vel, mass, acc and pot are required");
+    cudaStream_t s = ctx->stream;
+    auto forces = [&] {
+      if (solver == GTC_SOLVER_GROUP) {
+        group_force(ctx, pos, mass, n, sp, acc, pot);
+      } else {
+        direct_force(ctx, pos, mass, n, sp, acc, pot);
+        gtc::k_unpack_direct<<<gtc::ceil_div(n, 256), 256, 0, s>>>(ctx->ws.out.as<float4>(),
+                                                                  static_cast<u32>(n), acc, pot);
+        GTC_LAUNCH_CHECK();
+      }
+    };
+    if (graph && solver == GTC_SOLVER_GROUP && sp.criterion == GTC_CRITERION_THETA) {
+      leapfrog_graph(ctx, pos, vel, mass, acc, pot, n, sp, dt, steps, prime != 0);
+      return;
+    }
+    if (prime) forces();
+    const double h = 0.5 * dt;
+    for (u64 k = 0; k < steps; ++k) {
+      gtc::kick_drift(pos, vel, acc, n, h, dt, s);
+      forces();
+      gtc::kick(vel, acc, n, h, s);
+    }
+    GTC_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+gtc_status gtc_diagnostics_device(gtc_context *ctx, const double *pos, const double *vel,
+                                  const double *mass, const double *pot, uint64_t n,
+                                  double time, gtc_diagnostics *out) {
+  return guarded(ctx, [&] {
+    if (!out) throw gtc::InvalidArgument("out is required");
+    if (n > 0 && (!pos || !vel || !mass || !pot))
+      throw gtc::InvalidArgument("pos, vel, mass and pot are required");
+    const size_t bytes = gtc::diagnostics_blocks() * gtc::kDiagTerms * sizeof(double);
+    ctx->diag.ensure(bytes);
+    std::vector<double> part(bytes / sizeof(double));
+    if (n > 0) {
+      gtc::diagnostics_launch(pos, vel, mass, pot, n, ctx->diag.as<double>(), ctx->stream);
+      GTC_CUDA(cudaMemcpyAsync(part.data(), ctx->diag.ptr, bytes, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+      GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    gtc::diagnostics_finish(part.data(), time, out);
   });
 }
 

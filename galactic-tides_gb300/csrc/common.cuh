@@ -68,6 +68,8 @@ void exclusive_scan_u32(const u32 *in, u32 *out, u64 n, u32 *total_dev, DeviceBu
                         cudaStream_t s);
 void exclusive_scan_u64(const u64 *in, u64 *out, u64 n, u64 *total_dev, DeviceBuffer &tmp,
                         cudaStream_t s);
+// Grows tmp to what scans of up to n elements need (none allocates after).
+void reserve_scans(DeviceBuffer &tmp, u64 n);
 
 // ---------------------------------------------------------- radix sort
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the

@@ -34,6 +34,8 @@ struct gtc_context {
   double guard_theta = 1.5;         // options of the learned walk
   double band_override = -1.0;      // < 0: the model's band
   int learned_split = 1;            // learned walk tasks: subtrees at this depth
+  gtc::DeviceBuffer diag;           // diagnostics partial sums
+  double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes
 };
 
 namespace gtc {

@@ -75,10 +75,14 @@ __global__ void __launch_bounds__(kT)
     k_eval(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
            const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
            const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
-           float4 *__restrict__ out, u32 *next_group) {
+           float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev = nullptr,
+           const u32 *abort = nullptr) {
   __shared__ Staged sc[kWarpsPerBlock][32];
   __shared__ float4 sb[kWarpsPerBlock][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // a graph replay: the group count from the device, nothing after an abort
+  if (abort && *abort) return;
+  if (ng_dev) ngroups = min(ngroups, *ng_dev);
   for (;;) {
     u32 g = 0;
     if (lane == 0) g = atomicAdd(next_group, 1u);
@@ -147,9 +151,10 @@ __global__ void __launch_bounds__(kT)
 
 // Tree order -> caller order, FP32 -> FP64 (gravity_backends.cpp:132-136).
 __global__ void __launch_bounds__(256)
-    k_scatter(const float4 *out, const u32 *order, u32 n, double *acc, double *pot) {
+    k_scatter(const float4 *out, const u32 *order, u32 n, double *acc, double *pot,
+              const u32 *abort = nullptr) {
   const u32 k = blockIdx.x * 256 + threadIdx.x;
-  if (k >= n) return;
+  if (k >= n || (abort && *abort)) return;
   const float4 o = out[k];
   const u64 i = order[k];
   acc[3 * i] = o.x;
@@ -161,7 +166,7 @@ __global__ void __launch_bounds__(256)
 template <bool kQuad, bool kSoft>
 void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                  const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                 float4 *out, u32 *counter, cudaStream_t s) {
+                 float4 *out, u32 *counter, cudaStream_t s, const Scalars *sc = nullptr) {
   int dev = 0, sms = 0, per_sm = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -169,7 +174,9 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
   const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
   k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
-                                           static_cast<u32>(n_groups), G, eps2, out, counter);
+                                           static_cast<u32>(n_groups), G, eps2, out, counter,
+                                           sc ? &sc->n_groups : nullptr,
+                                           sc ? &sc->abort : nullptr);
   GTC_LAUNCH_CHECK();
 }
 
@@ -189,6 +196,30 @@ void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_l
     launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
   else
     launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+}
+
+void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                          const u32 *body_list, const uint4 *groups, u64 max_groups,
+                          const Scalars *sc, float G, float eps2, bool quadrupole, float4 *out,
+                          u32 *counter, cudaStream_t s) {
+  if (max_groups == 0) return;
+  GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
+  const bool soft = eps2 > 0.0f;
+  if (quadrupole && soft)
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+  else if (quadrupole)
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+  else if (soft)
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+  else
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+}
+
+void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
+                           const Scalars *sc, cudaStream_t s) {
+  if (n == 0) return;
+  k_scatter<<<ceil_div(n, 256), 256, 0, s>>>(out, order, static_cast<u32>(n), acc, pot, &sc->abort);
+  GTC_LAUNCH_CHECK();
 }
 
 void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,

@@ -28,15 +28,23 @@ namespace {
 
 constexpr int kT = 256;
 
+// Graph replays pass the abort word of their Scalars and counts on the
+// device; eager calls pass null and their host-known sizes.
+__device__ __forceinline__ bool aborted(const u32 *abort) { return abort && *abort; }
+__device__ __forceinline__ u32 bounded(u32 cap, const u32 *dev) {
+  return dev ? min(cap, *dev) : cap;
+}
+
 struct NodeView {
   const u32 *nbegin, *nend, *skip;
   const u8 *isleaf;
 };
 
 __global__ void __launch_bounds__(kT)
-    k_group_marks(NodeView nv, u32 m, u32 n, u32 gs, int pack, u32 *mark) {
+    k_group_marks(NodeView nv, u32 m, u32 n, u32 gs, int pack, u32 *mark,
+                  const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p >= m) return;
+  if (aborted(abort) || p >= bounded(m, m_dev)) return;
   const u32 size = nv.nend[p] - nv.nbegin[p];
   if (p == 0 && (size <= gs || nv.isleaf[0])) {
     for (u32 c = 0; c < n; c += gs) mark[c] = 1;
@@ -72,16 +80,24 @@ __global__ void __launch_bounds__(kT)
 }
 
 __global__ void __launch_bounds__(kT)
-    k_group_ranges(const u32 *mark, const u32 *scan, u32 n, u32 *gbegin, u32 *gend) {
+    k_group_ranges(const u32 *mark, const u32 *scan, u32 n, u32 *gbegin, u32 *gend,
+                   const u32 *abort = nullptr) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
-  if (b >= n || !mark[b]) return;
+  if (b >= n || aborted(abort) || !mark[b]) return;
   const u32 g = scan[b];
   gbegin[g] = b;
   if (g > 0) gend[g - 1] = b;
 }
 
 __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
-  if (sc->n_groups > 0) gend[sc->n_groups - 1] = n;
+  if (sc->abort) return;
+  if (sc->n_groups > 0 && sc->n_groups <= n) gend[sc->n_groups - 1] = n;
+}
+
+// A graph replay's check before the lists are written: more list entries
+// than the captured buffers hold (bit 8).
+__global__ void k_check_lists_graph(Scalars *sc, u64 cells, u64 bodies) {
+  if (sc->n_cell_list > cells || sc->n_body_list > bodies) sc->abort |= 8u;
 }
 
 // Group bounding box (group_lists.cpp:125-131): centre and half-extent in
@@ -89,10 +105,11 @@ __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
 // centre (the frame of the FP32 walk records).
 __global__ void __launch_bounds__(kT)
     k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos,
-                const TreeRoot *root, double *gbox, float *gboxf) {
+                const TreeRoot *root, double *gbox, float *gboxf, const u32 *ng_dev = nullptr,
+                const u32 *abort = nullptr) {
   // gboxf per group: centre (3), half-extent (3), magnitude bound, pad
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
+  if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
   const u32 b0 = gbegin[g], b1 = gend[g];
   double lo[3], hi[3];
   for (int a = 0; a < 3; ++a) lo[a] = hi[a] = tpos[3ull * b0 + a];
@@ -232,9 +249,11 @@ __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk6
 template <bool kFill>
 __global__ void __launch_bounds__(kT)
     k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
-           const float *gboxf, u32 ng, const Task *tasks, u32 ntasks, WalkOut out,
-           Scalars *sc) {
+           const float *gboxf, u32 ng_cap, const Task *tasks, u32 ntasks, WalkOut out,
+           Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
   const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (aborted(abort)) return;
+  const u32 ng = bounded(ng_cap, ng_dev);
   if (tid >= static_cast<u64>(ng) * ntasks) return;
   // consecutive threads: consecutive groups on the same task (similar walks)
   const u32 t = static_cast<u32>(tid / ng), g = static_cast<u32>(tid % ng);
@@ -320,9 +339,10 @@ __global__ void __launch_bounds__(kT)
 // GTGroup records from the per-task offsets, and the list counters.
 __global__ void __launch_bounds__(kT)
     k_group_records(const u32 *gbegin, const u32 *gend, u32 ng, u32 ntasks, const u64 *cell_off,
-                    const u64 *body_off, uint4 *groups, Scalars *sc) {
+                    const u64 *body_off, uint4 *groups, Scalars *sc,
+                    const u32 *ng_dev = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
+  if (sc->abort || g >= bounded(ng, ng_dev)) return;
   const u64 c0 = cell_off[static_cast<u64>(g) * ntasks],
             c1 = cell_off[static_cast<u64>(g + 1) * ntasks];
   const u64 b0 = body_off[static_cast<u64>(g) * ntasks],
@@ -431,6 +451,65 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), ng,
                                  ws.tasks.as<Task>(), ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
+}
+
+void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &caps,
+                       cudaStream_t s) {
+  const u64 n = ws.n;
+  const u32 n32 = static_cast<u32>(n), mcap = caps.nodes;
+  const u32 gs = static_cast<u32>(sp.group_size);
+  Scalars *sc = ws.scalars.as<Scalars>();
+  u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
+  const u32 *abort = &sc->abort;
+  const u32 nb = ceil_div(n, kT), mb = ceil_div(mcap, kT);
+  // groups (the one walk task, the root, was written before capture)
+  GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
+  NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
+  k_group_marks<<<mb, kT, 0, s>>>(nv, mcap, n32, gs, sp.pack, mark, &sc->n_nodes, abort);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u32(mark, mscan, n, &sc->n_groups, ws.scan_tmp, s);
+  u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
+  k_group_ranges<<<nb, kT, 0, s>>>(mark, mscan, n32, gbegin, gend, abort);
+  GTC_LAUNCH_CHECK();
+  k_last_end<<<1, 1, 0, s>>>(sc, n32, gend);
+  GTC_LAUNCH_CHECK();
+  GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, 3 * sizeof(unsigned long long), s));
+  k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
+                                ws.gbox.as<double>(), ws.gboxf.as<float>(), &sc->n_groups, abort);
+  GTC_LAUNCH_CHECK();
+  // count pass over every possible group (the counts past the last are zero)
+  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
+  GTC_CUDA(cudaMemsetAsync(ws.gcells.ptr, 0, n * 8, s));
+  GTC_CUDA(cudaMemsetAsync(ws.gbodies.ptr, 0, n * 8, s));
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off,
+             ws.cell_list.as<u32>(), ws.body_list.as<u32>()};
+  const Task *tasks = ws.tasks.as<Task>();
+  k_walk<false><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
+                                  &sc->n_groups, abort);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, n, cell_off + n, ws.scan_tmp, s);
+  exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, n, body_off + n, ws.scan_tmp, s);
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + n, 8, cudaMemcpyDeviceToDevice, s));
+  GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + n, 8, cudaMemcpyDeviceToDevice, s));
+  k_group_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, 1, cell_off, body_off,
+                                    ws.groups.as<uint4>(), sc, &sc->n_groups);
+  GTC_LAUNCH_CHECK();
+  k_check_lists_graph<<<1, 1, 0, s>>>(sc, caps.cells, caps.bodies);
+  GTC_LAUNCH_CHECK();
+  k_walk<true><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
+                                 &sc->n_groups, abort);
+  GTC_LAUNCH_CHECK();
+}
+
+void write_root_task(Workspace &ws, cudaStream_t s) {
+  ws.tasks.ensure(sizeof(Task));
+  const Task t{0u, kNone, 0u, 0u};
+  GTC_CUDA(cudaMemcpyAsync(ws.tasks.ptr, &t, sizeof(Task), cudaMemcpyHostToDevice, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace gtc

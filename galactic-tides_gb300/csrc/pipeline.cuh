@@ -96,6 +96,7 @@ struct Scalars {
   unsigned long long mlp_batches; // learned walk: warp inferences
   unsigned long long walk_items; // learned walk: next item to take
   u32 list_overflow;      // learned walk: a lane's region overflowed
+  u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)
 };
 
@@ -122,6 +123,33 @@ void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_l
                     bool quadrupole, float4 *out, u32 *counter, cudaStream_t s);
 void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
                      cudaStream_t s);
+
+// Capacities of a solve replayed from a CUDA graph: the sizes of the
+// buffers the graph was captured with. A replay whose tree, depth or lists
+// outgrow them sets Scalars::abort, and every later kernel of the replay
+// returns at once (memory stays in bounds; the step is then redone eagerly).
+struct GraphCaps {
+  u32 nodes;        // node arrays
+  int depth;        // deepest node the per-depth moment launches cover
+  u64 cells, bodies;  // cell_list, body_list
+};
+// Both stages without a host synchronisation, for stream capture: grids
+// sized by the capacities, counts read on the device. One key word only (a
+// tree deeper than 21 levels aborts), one walk task per group.
+void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 n,
+                      const SolverParams &sp, const GraphCaps &caps, cudaStream_t s);
+void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &caps,
+                       cudaStream_t s);
+// The single walk task of a graph replay (the root), written before capture.
+void write_root_task(Workspace &ws, cudaStream_t s);
+// The evaluation of a replay: the group count from the device, nothing
+// after an abort.
+void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                          const u32 *body_list, const uint4 *groups, u64 max_groups,
+                          const Scalars *sc, float G, float eps2, bool quadrupole, float4 *out,
+                          u32 *counter, cudaStream_t s);
+void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
+                           const Scalars *sc, cudaStream_t s);
 
 // Direct summation kernels.
 void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, cudaStream_t s);

@@ -1,6 +1,8 @@
 // Device-wide exclusive prefix sums (reduce, scan of block totals, add back).
 // Used for node numbering, group offsets, list offsets and the radix sort.
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace gtc {
@@ -122,6 +124,10 @@ void exclusive_scan_u32(const u32 *in, u32 *out, u64 n, u32 *total_dev, DeviceBu
                         cudaStream_t s) {
   tmp.ensure(scratch_elems<u32>(n) * sizeof(u32));
   scan_impl<u32>(in, out, n, total_dev, tmp, 0, s);
+}
+
+void reserve_scans(DeviceBuffer &tmp, u64 n) {
+  tmp.ensure(std::max(scratch_elems<u32>(n) * sizeof(u32), scratch_elems<u64>(n) * sizeof(u64)));
 }
 
 void exclusive_scan_u64(const u64 *in, u64 *out, u64 n, u64 *total_dev, DeviceBuffer &tmp,

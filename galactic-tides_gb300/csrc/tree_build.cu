@@ -39,6 +39,13 @@ namespace gtc {
 namespace {
 
 constexpr int kT = 256;
+
+// Graph replays pass the abort word of their Scalars and the node count on
+// the device; eager calls pass null and their host-known sizes.
+__device__ __forceinline__ bool aborted(const u32 *abort) { return abort && *abort; }
+__device__ __forceinline__ u32 bounded(u32 cap, const u32 *dev) {
+  return dev ? min(cap, *dev) : cap;
+}
 constexpr u8 kNoTiny = 255;
 
 struct Dbl4 {
@@ -324,8 +331,10 @@ __global__ void __launch_bounds__(kT)
 // ------------------------------------------------------------------ nodes
 
 __global__ void __launch_bounds__(kT)
-    k_node_count(const signed char *lcp_next, const u8 *leafdepth, u32 n, u32 *count) {
+    k_node_count(const signed char *lcp_next, const u8 *leafdepth, u32 n, u32 *count,
+                 const u32 *abort = nullptr) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
+  if (aborted(abort)) return;
   if (b < n) count[b] = static_cast<u32>(max(0, static_cast<int>(leafdepth[b]) - lcp_next[b]));
 }
 
@@ -333,9 +342,10 @@ __global__ void __launch_bounds__(kT)
 __global__ void __launch_bounds__(kT)
     k_nodes(KeyView kv, const signed char *lcp_next, const u8 *leafdepth, const u32 *count,
             const u32 *count_scan, u32 n, const Scalars *sc, const TreeRoot *root, double2 *geom,
-            u32 *nbegin, u32 *nend, u32 *skip, u8 *depth, u8 *isleaf) {
+            u32 *nbegin, u32 *nend, u32 *skip, u8 *depth, u8 *isleaf,
+            const u32 *abort = nullptr) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
-  if (b >= n) return;
+  if (b >= n || aborted(abort)) return;
   const u32 c = count[b];
   if (c == 0) return;
   const u32 total = sc->n_nodes;
@@ -372,9 +382,10 @@ __device__ __forceinline__ int children_of(u32 p, const u32 *skip, u32 ch[8]) {
 }
 
 __global__ void __launch_bounds__(kT)
-    k_children(const u32 *skip, const u8 *isleaf, u32 m, u32 *parent, u8 *nchild) {
+    k_children(const u32 *skip, const u8 *isleaf, u32 m, u32 *parent, u8 *nchild,
+               const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p >= m) return;
+  if (aborted(abort) || p >= bounded(m, m_dev)) return;
   if (p == 0) parent[0] = 0xffffffffu;
   if (isleaf[p]) {
     nchild[p] = 0;
@@ -388,9 +399,10 @@ __global__ void __launch_bounds__(kT)
 
 // Input order inside each leaf (the reference never splits a leaf's range).
 __global__ void __launch_bounds__(kT)
-    k_leaf_order(const u8 *isleaf, const u32 *nbegin, const u32 *nend, u32 m, u32 *idx) {
+    k_leaf_order(const u8 *isleaf, const u32 *nbegin, const u32 *nend, u32 m, u32 *idx,
+                 const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p >= m || !isleaf[p]) return;
+  if (aborted(abort) || p >= bounded(m, m_dev) || !isleaf[p]) return;
   const u32 b0 = nbegin[p], b1 = nend[p];
   for (u32 i = b0 + 1; i < b1; ++i) {
     const u32 v = idx[i];
@@ -405,9 +417,9 @@ __global__ void __launch_bounds__(kT)
 
 __global__ void __launch_bounds__(kT)
     k_tree_order(const double *pos, const double *mass, const u32 *idx, u32 n, double *tpos,
-                 double *tmass) {
+                 double *tmass, const u32 *abort = nullptr) {
   const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k >= n) return;
+  if (k >= n || aborted(abort)) return;
   const u64 i = idx[k];
   tpos[3ull * k] = pos[3 * i];
   tpos[3ull * k + 1] = pos[3 * i + 1];
@@ -531,20 +543,26 @@ constexpr int kBuckets = kMaxDepth + 2;
 
 // Per-block histograms in shared memory, one global atomic per bucket.
 __global__ void __launch_bounds__(kT)
-    k_bucket_count(const u8 *depth, const u8 *isleaf, u32 m, u32 *count) {
+    k_bucket_count(const u8 *depth, const u8 *isleaf, u32 m, u32 *count,
+                   const u32 *m_dev = nullptr, u32 *abort = nullptr, int depth_cap = kMaxDepth) {
   __shared__ u32 h[kBuckets];
+  if (aborted(abort)) return;
   for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
   __syncthreads();
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p < m) atomicAdd(&h[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+  if (p < bounded(m, m_dev)) {
+    if (abort && !isleaf[p] && depth[p] > depth_cap) atomicOr(abort, 4u);
+    atomicAdd(&h[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+  }
   __syncthreads();
   for (int b = threadIdx.x; b < kBuckets; b += kT)
     if (h[b]) atomicAdd(&count[b], h[b]);
 }
 
 // offsets[b] = start of bucket b; also clears the fill counters.
-__global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill) {
-  if (threadIdx.x != 0) return;
+__global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill,
+                                 const u32 *abort = nullptr) {
+  if (threadIdx.x != 0 || aborted(abort)) return;
   u32 run = 0;
   for (int b = 0; b < kBuckets; ++b) {
     offset[b] = run;
@@ -556,14 +574,15 @@ __global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill) {
 // Each block reserves one range per bucket, then places its nodes in it.
 __global__ void __launch_bounds__(kT)
     k_bucket_fill(const u8 *depth, const u8 *isleaf, u32 m, const u32 *offset, u32 *fill,
-                  u32 *bucket) {
+                  u32 *bucket, const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   __shared__ u32 h[kBuckets], base[kBuckets];
+  if (aborted(abort)) return;
   for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
   __syncthreads();
   const u32 p = blockIdx.x * kT + threadIdx.x;
   int b = -1;
   u32 local = 0;
-  if (p < m) {
+  if (p < bounded(m, m_dev)) {
     b = isleaf[p] ? kLeafBucket : depth[p];
     local = atomicAdd(&h[b], 1u);
   }
@@ -586,6 +605,26 @@ __global__ void __launch_bounds__(kT)
   if (k < count) node_moments(a, bucket[k]);
 }
 
+// A graph replay's moments of bucket b: the count and offset from the
+// device (meta = count[kBuckets], offset[kBuckets]), grid-stride.
+__global__ void __launch_bounds__(kT)
+    k_moments_graph(MomentArrays a, const u32 *bucket, const u32 *meta, int b,
+                    const u32 *abort) {
+  if (*abort) return;
+  const u32 count = meta[b], off = meta[kBuckets + b];
+  for (u32 k = blockIdx.x * kT + threadIdx.x; k < count; k += gridDim.x * kT) {
+    if (b == kLeafBucket) leaf_moments(a, bucket[off + k]);
+    else node_moments(a, bucket[off + k]);
+  }
+}
+
+// A graph replay's checks after the node count: deeper keys needed (bit 1)
+// or more nodes than the node arrays hold (bit 2).
+__global__ void k_check_tree_graph(Scalars *sc, u32 cap) {
+  if (sc->deep > 0) sc->abort |= 1u;
+  if (sc->n_nodes > cap) sc->abort |= 2u;
+}
+
 // --------------------------------------------------------------- packing
 
 // Walk records (FP32 and FP64) and FP32 cell of every node
@@ -594,9 +633,10 @@ __global__ void __launch_bounds__(kT)
     k_pack_nodes(const double2 *geom, const double2 *mom, const double2 *quad,
                  const double *delta, const u32 *nbegin, const u32 *nend, const u32 *skip,
                  const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta,
-                 WalkRec32 *walk32, WalkRec64 *walk64, float4 *cells) {
+                 WalkRec32 *walk32, WalkRec64 *walk64, float4 *cells, const u32 *m_dev = nullptr,
+                 const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
-  if (p >= m) return;
+  if (aborted(abort) || p >= bounded(m, m_dev)) return;
   const Dbl4 g = load_pair(geom, p), c = load_pair(mom, p);
   const double crit = 2.0 * g.w * inv_theta + delta[p];
   WalkRec64 r;
@@ -638,9 +678,9 @@ __global__ void __launch_bounds__(kT)
 // FP32 bodies relative to `origin` (group_lists.cpp:46-50, gravity_backends.cpp:15-23).
 __global__ void __launch_bounds__(kT)
     k_pack_bodies(const double *tpos, const double *tmass, u32 n, const double *origin,
-                  float4 *bodies) {
+                  float4 *bodies, const u32 *abort = nullptr) {
   const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k >= n) return;
+  if (k >= n || aborted(abort)) return;
   bodies[k] = make_float4(static_cast<float>(tpos[3ull * k] - origin[0]),
                           static_cast<float>(tpos[3ull * k + 1] - origin[1]),
                           static_cast<float>(tpos[3ull * k + 2] - origin[2]),
@@ -866,6 +906,85 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_LAUNCH_CHECK();
   k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
                                   root_centre(root), ws.bodies.as<float4>());
+  GTC_LAUNCH_CHECK();
+}
+
+void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 n,
+                      const SolverParams &sp, const GraphCaps &caps, cudaStream_t s) {
+  ws.n = n;
+  ws.key_words = 1;
+  const u32 n32 = static_cast<u32>(n), mcap = caps.nodes;
+  const u32 nb = ceil_div(n, kT), mb = ceil_div(mcap, kT);
+  const int L = std::max(1, sp.leaf_size);
+  Scalars *sc = ws.scalars.as<Scalars>();
+  u32 *abort = &sc->abort;
+  GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
+  bbox_root(ws, pos, n, s);
+  const TreeRoot *root = ws.root.as<TreeRoot>();
+  u64 *key0 = ws.key0.as<u64>();
+  u32 *idx = ws.idx.as<u32>();
+  u8 *tiny = ws.tiny.as<u8>();
+  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny, &sc->error);
+  GTC_LAUNCH_CHECK();
+  radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
+  const KeyView kv{key0, nullptr, nullptr, 1};
+  signed char *lcp_next = ws.lcp.as<signed char>();
+  u8 *leafdepth = ws.leafdepth.as<u8>();
+  k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
+  GTC_LAUNCH_CHECK();
+  u32 *count = ws.count.as<u32>(), *cscan = ws.count_scan.as<u32>();
+  k_node_count<<<nb, kT, 0, s>>>(lcp_next, leafdepth, n32, count);
+  GTC_LAUNCH_CHECK();
+  exclusive_scan_u32(count, cscan, n, &sc->n_nodes, ws.scan_tmp, s);
+  k_check_tree_graph<<<1, 1, 0, s>>>(sc, mcap);
+  GTC_LAUNCH_CHECK();
+  const u32 *m_dev = &sc->n_nodes;
+  k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
+                            ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), abort);
+  GTC_LAUNCH_CHECK();
+  k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, ws.parent.as<u32>(),
+                               ws.nchild.as<u8>(), m_dev, abort);
+  GTC_LAUNCH_CHECK();
+  k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), mcap,
+                                 idx, m_dev, abort);
+  GTC_LAUNCH_CHECK();
+  k_tree_order<<<nb, kT, 0, s>>>(pos, mass, idx, n32, ws.tpos.as<double>(), ws.tmass.as<double>(),
+                                 abort);
+  GTC_LAUNCH_CHECK();
+  u32 *meta = ws.arrive.as<u32>();
+  u32 *bucket = ws.bucket.as<u32>();
+  GTC_CUDA(cudaMemsetAsync(meta, 0, kBuckets * sizeof(u32), s));
+  k_bucket_count<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), mcap, meta, m_dev, abort,
+                                   caps.depth);
+  GTC_LAUNCH_CHECK();
+  k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets, abort);
+  GTC_LAUNCH_CHECK();
+  k_bucket_fill<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), mcap, meta + kBuckets,
+                                  meta + 2 * kBuckets, bucket, m_dev, abort);
+  GTC_LAUNCH_CHECK();
+  MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                  ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
+                  ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
+                  ws.quad.as<double2>(), ws.delta.as<double>()};
+  int dev = 0, sms = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const u32 gb = std::min<u32>(mb, static_cast<u32>(std::max(1, 8 * sms)));
+  k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, kLeafBucket, abort);
+  GTC_LAUNCH_CHECK();
+  for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
+    k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, d, abort);
+    GTC_LAUNCH_CHECK();
+  }
+  k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
+                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, root,
+                                 1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
+                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), m_dev, abort);
+  GTC_LAUNCH_CHECK();
+  k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
+                                  root_centre(root), ws.bodies.as<float4>(), abort);
   GTC_LAUNCH_CHECK();
 }
 

@@ -38,6 +38,16 @@ class GravityParams(C.Structure):
                 ("alpha", C.c_double)]
 
 
+class Diagnostics(C.Structure):
+    _fields_ = [("time", C.c_double), ("kinetic", C.c_double), ("potential", C.c_double),
+                ("total", C.c_double), ("virial_ratio", C.c_double),
+                ("momentum", C.c_double * 3), ("angular_momentum", C.c_double * 3),
+                ("centre_of_mass", C.c_double * 3)]
+
+
+SOLVER_GROUP, SOLVER_DIRECT = 0, 1
+
+
 class KernelParams(C.Structure):
     _fields_ = [("n", C.c_uint32), ("n_groups", C.c_uint32), ("G", C.c_float),
                 ("eps2", C.c_float), ("quadrupole", C.c_uint32), ("pad", C.c_uint32 * 3)]
@@ -52,7 +62,7 @@ class Stats(C.Structure):
                 ("depth", C.c_uint32), ("eval_kernel_ms", C.c_double),
                 ("kernel_launches", C.c_uint64), ("walk_tests_fp64", C.c_uint64),
                 ("mlp_rows", C.c_uint64), ("mlp_batches", C.c_uint64),
-                ("criterion_used", C.c_uint32), ("pad", C.c_uint32)]
+                ("criterion_used", C.c_uint32), ("graph_steps", C.c_uint32)]
 
 
 NODE_DTYPE = np.dtype([
@@ -102,6 +112,9 @@ def _load():
         "gtc_learned_get_model": (I, [V, P]),
         "gtc_learned_predict": (I, [V, P, U64, P]),
         "gtc_direct_fp64_noalloc": (I, [P, P, U64, P, U64, D, D, P, P, V]),
+        "gtc_leapfrog_device": (I, [V, P, P, P, P, P, U64, C.POINTER(GravityParams), I, D, U64,
+                                    I, I]),
+        "gtc_diagnostics_device": (I, [V, P, P, P, P, U64, D, C.POINTER(Diagnostics)]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -256,6 +269,25 @@ class Context:
     def set_option(self, name, value):
         self._check(lib.gtc_set_option(self.h, name.encode(), float(value)))
 
+    # ---- time integration ------------------------------------------------------
+
+    def leapfrog_device(self, pos_ptr, vel_ptr, mass_ptr, acc_ptr, pot_ptr, n, dt, steps,
+                        prime=True, graph=False, solver=SOLVER_GROUP, **kw):
+        """LeapfrogKDK on device arrays: optional prime(), then `steps` KDK steps."""
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_leapfrog_device(self.h, pos_ptr, vel_ptr, mass_ptr, acc_ptr,
+                                            pot_ptr, n, C.byref(gp), solver, dt, steps,
+                                            int(prime), int(graph)))
+
+    def diagnostics_device(self, pos_ptr, vel_ptr, mass_ptr, pot_ptr, n, time=0.0):
+        d = Diagnostics()
+        self._check(lib.gtc_diagnostics_device(self.h, pos_ptr, vel_ptr, mass_ptr, pot_ptr, n,
+                                               time, C.byref(d)))
+        out = {k: getattr(d, k) for k, _ in Diagnostics._fields_}
+        for k in ("momentum", "angular_momentum", "centre_of_mass"):
+            out[k] = list(out[k])
+        return out
+
     # ---- learned opening criterion -------------------------------------------
 
     def learned_add_samples(self, pos, mass, theta_gen=0.5, theta_guard=1.5, max_new=1 << 20,
@@ -378,6 +410,13 @@ def _ics_lib():
         _ics.gtc_galaxy_default.argtypes = [C.POINTER(GalaxyModel), C.c_uint64, C.c_uint64]
         _ics.gtc_make_galaxy.restype = C.c_int
         _ics.gtc_make_galaxy.argtypes = [C.POINTER(GalaxyModel)] + [C.c_void_p] * 4
+        _ics.gtc_orient.restype = None
+        _ics.gtc_orient.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_double, C.c_double]
+        _ics.gtc_parabolic_orbit.restype = C.c_int
+        _ics.gtc_parabolic_orbit.argtypes = [C.c_double] * 5 + [C.c_void_p, C.c_void_p]
+        _ics.gtc_make_encounter.restype = C.c_int
+        _ics.gtc_make_encounter.argtypes = [C.POINTER(GalaxyModel)] + [C.c_double] * 6 + \
+            [C.c_void_p] * 4
         _ics.gtc_sample_indices.restype = None
         _ics.gtc_sample_indices.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
     return _ics
@@ -410,3 +449,31 @@ def sample_indices(n, m=4096, seed=1):
     out = np.empty(min(n, m), np.uint64)
     _ics_lib().gtc_sample_indices(n, m, seed, _ptr(out))
     return out
+
+
+def orient(pos, vel, incl_deg, omega_deg=0.0):
+    """Rotates (in place) by incl_deg about x, then omega_deg about z."""
+    assert pos.flags.c_contiguous and vel.flags.c_contiguous
+    _ics_lib().gtc_orient(_ptr(pos), _ptr(vel), pos.shape[0], incl_deg, omega_deg)
+
+
+def parabolic_orbit(G, m1, m2, rp, r0):
+    """-> (dx, dv): relative position and velocity of the parabolic orbit."""
+    dx, dv = np.empty(3), np.empty(3)
+    if _ics_lib().gtc_parabolic_orbit(G, m1, m2, rp, r0, _ptr(dx), _ptr(dv)):
+        raise ValueError("parabolic_orbit: start separation below pericentre")
+    return dx, dv
+
+
+def make_encounter(n_each, seed=1, incl1=30.0, incl2=60.0, rp=2.0, r0=15.0, omega1=0.0,
+                   omega2=0.0, **fields):
+    """Two galaxies of n_each particles (seeds seed, seed + 1) on a parabolic
+    orbit, centre of mass at rest: -> pos, vel, mass, type (2 n_each)."""
+    m = galaxy_model(n_each, seed, **fields)
+    tot = 2 * (m.disk_n + m.bulge_n + m.halo_n)
+    pos, vel = np.empty((tot, 3)), np.empty((tot, 3))
+    mass, typ = np.empty(tot), np.empty(tot, np.int32)
+    if _ics_lib().gtc_make_encounter(C.byref(m), incl1, omega1, incl2, omega2, rp, r0, _ptr(pos),
+                                     _ptr(vel), _ptr(mass), _ptr(typ)):
+        raise ValueError("invalid encounter")
+    return pos, vel, mass, typ

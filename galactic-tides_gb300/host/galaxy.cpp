@@ -283,6 +283,67 @@ int gtc_make_galaxy(const gtc_galaxy_model *mp, double *pos, double *vel, double
   return 0;
 }
 
+void gtc_orient(double *pos, double *vel, uint64_t n, double incl_deg, double omega_deg) {
+  const double i = incl_deg * M_PI / 180.0, w = omega_deg * M_PI / 180.0;
+  const double ci = std::cos(i), si = std::sin(i), cw = std::cos(w), sw = std::sin(w);
+  auto rot = [&](double *v) {
+    // about x, then about z
+    const double ax = v[0], ay = ci * v[1] - si * v[2], az = si * v[1] + ci * v[2];
+    v[0] = cw * ax - sw * ay;
+    v[1] = sw * ax + cw * ay;
+    v[2] = az;
+  };
+  for (uint64_t k = 0; k < n; ++k) {
+    rot(pos + 3 * k);
+    rot(vel + 3 * k);
+  }
+}
+
+int gtc_parabolic_orbit(double G, double m1, double m2, double rp, double r0, double dx[3],
+                        double dv[3]) {
+  if (!(r0 >= rp) || !(rp > 0)) return 1;
+  const double M = m1 + m2;
+  // true anomaly at r0 on the approaching branch: r = 2 rp / (1 + cos f)
+  const double f = -std::acos(std::clamp(2 * rp / r0 - 1, -1.0, 1.0));
+  const double hmom = std::sqrt(2 * G * M * rp);
+  const double vr = G * M / hmom * std::sin(f), vt = hmom / r0;
+  const double rh[3] = {std::cos(f), std::sin(f), 0.0}, fh[3] = {-std::sin(f), std::cos(f), 0.0};
+  for (int a = 0; a < 3; ++a) {
+    dx[a] = r0 * rh[a];
+    dv[a] = vr * rh[a] + vt * fh[a];
+  }
+  return 0;
+}
+
+int gtc_make_encounter(const gtc_galaxy_model *m, double incl1, double omega1, double incl2,
+                       double omega2, double rp, double r0, double *pos, double *vel,
+                       double *mass, int32_t *type) {
+  const uint64_t n = m->disk_n + m->bulge_n + m->halo_n;
+  gtc_galaxy_model m2 = *m;
+  m2.seed = m->seed + 1;
+  if (gtc_make_galaxy(m, pos, vel, mass, type)) return 1;
+  if (gtc_make_galaxy(&m2, pos + 3 * n, vel + 3 * n, mass + n, type + n)) return 1;
+  gtc_orient(pos, vel, n, incl1, omega1);
+  gtc_orient(pos + 3 * n, vel + 3 * n, n, incl2, omega2);
+  double m1 = 0, mm2 = 0;
+  for (uint64_t k = 0; k < n; ++k) {
+    m1 += mass[k];
+    mm2 += mass[n + k];
+  }
+  double dx[3], dv[3];
+  if (gtc_parabolic_orbit(m->G, m1, mm2, rp, r0, dx, dv)) return 1;
+  // centre of mass at rest at the origin
+  const double f1 = -mm2 / (m1 + mm2), f2 = m1 / (m1 + mm2);
+  for (uint64_t k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) {
+      pos[3 * k + a] += f1 * dx[a];
+      vel[3 * k + a] += f1 * dv[a];
+      pos[3 * (n + k) + a] += f2 * dx[a];
+      vel[3 * (n + k) + a] += f2 * dv[a];
+    }
+  return 0;
+}
+
 void gtc_sample_indices(uint64_t n, uint64_t m, uint64_t seed, uint64_t *out) {
   std::mt19937_64 rng(seed);
   std::vector<std::size_t> s(n);

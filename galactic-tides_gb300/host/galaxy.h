@@ -48,6 +48,26 @@ void gtc_galaxy_default(gtc_galaxy_model *m, uint64_t n, uint64_t seed);
 int gtc_make_galaxy(const gtc_galaxy_model *m, double *pos, double *vel, double *mass,
                     int32_t *type);
 
+/* Rotates positions and velocities of n bodies by incl_deg about x, then
+ * omega_deg about z (orient, src/hernquist_ics.cpp). */
+void gtc_orient(double *pos, double *vel, uint64_t n, double incl_deg, double omega_deg);
+
+/* Relative position dx and velocity dv of a parabolic two-point-mass orbit
+ * with pericentre rp, approaching from separation r0 in the x-y plane
+ * (parabolic_orbit, src/hernquist_ics.cpp). Returns 1 if r0 < rp. */
+int gtc_parabolic_orbit(double G, double m1, double m2, double rp, double r0, double dx[3],
+                        double dv[3]);
+
+/* A parabolic encounter of two galaxies of model m (seeds m.seed and
+ * m.seed + 1), inclined incl1 / incl2 degrees (omega1 / omega2 about z),
+ * pericentre rp, start separation r0, centre of mass at rest at the origin:
+ * the encounter mode of apps/galactic_tides_ics.cpp:78-97. Fills 2 n
+ * bodies (n = one galaxy), galaxy 1 first. Returns 0, or 1 on a bad model
+ * or orbit. */
+int gtc_make_encounter(const gtc_galaxy_model *m, double incl1, double omega1, double incl2,
+                       double omega2, double rp, double r0, double *pos, double *vel,
+                       double *mass, int32_t *type);
+
 /* The accuracy sample of the reference bench (apps/galactic_tides_bench.cpp:
  * 75-79): indices 0..n-1 shuffled by std::shuffle with std::mt19937_64(seed),
  * first m kept. */

@@ -122,7 +122,7 @@ typedef struct gtc_stats {
   uint64_t mlp_rows;          /* learned walk: opening tests the network decided */
   uint64_t mlp_batches;       /* learned walk: warp-wide network evaluations */
   uint32_t criterion_used;    /* GTC_CRITERION_* the walk actually used */
-  uint32_t pad;
+  uint32_t graph_steps;       /* leapfrog: steps of the last call replayed from a CUDA graph */
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
@@ -204,6 +204,37 @@ gtc_status gtc_direct_fp64_noalloc(const double *pos, const double *mass, uint64
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
 
+/* ---- time integration (src/integrator.cpp) ----------------------------- */
+
+/* Diagnostics (integrator.h:46-58): potential = 0.5 sum m phi, total =
+ * kinetic + potential, virial_ratio = -2 kinetic / potential. */
+typedef struct gtc_diagnostics {
+  double time, kinetic, potential, total, virial_ratio;
+  double momentum[3], angular_momentum[3], centre_of_mass[3];
+} gtc_diagnostics;
+
+#define GTC_SOLVER_GROUP 0  /* gtc_group_force_device (theta or learned criterion) */
+#define GTC_SOLVER_DIRECT 1 /* gtc_direct_force_device */
+
+/* LeapfrogKDK (integrator.h:31-40, integrator.cpp:5-17) on device arrays:
+ * with prime = 1 first computes the forces (prime()), then runs `steps`
+ * kick-drift-force-kick steps of dt, FP64 kicks and drifts, on the context's
+ * stream; the particles never leave the device. acc and pot hold the forces
+ * of the last evaluation. With graph = 1 the whole step (kick, drift,
+ * rebuild, evaluation, kick) is replayed as one CUDA graph once the sizes
+ * have settled (the group solver with the theta criterion); a step whose
+ * tree or lists outgrow the graph's buffers is redone eagerly. gtc_get_stats
+ * describes the last force evaluation. */
+gtc_status gtc_leapfrog_device(gtc_context *ctx, double *pos, double *vel, const double *mass,
+                               double *acc, double *pot, uint64_t n,
+                               const gtc_gravity_params *gp, int solver, double dt,
+                               uint64_t steps, int prime, int graph);
+
+/* compute_diagnostics (integrator.cpp:19-36) on device arrays, FP64 sums. */
+gtc_status gtc_diagnostics_device(gtc_context *ctx, const double *pos, const double *vel,
+                                  const double *mass, const double *pot, uint64_t n,
+                                  double time, gtc_diagnostics *out);
+
 /* ---- tuning and diagnostics (no reference counterpart) ------------------ */
 
 /* Sets an option of the context:
@@ -218,6 +249,10 @@ gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
  *                        (default): tests whose centred error prior lies
  *                        further than this from the tolerance are decided by
  *                        it; the rest go to the network (0: prior only).
+ *   "graph_headroom"     0..4 (default 0.25): a leapfrog graph is captured
+ *                        with buffers this fraction larger than the last
+ *                        solve's tree and lists (0: exactly those sizes, so
+ *                        most changes abort the replay and redo it eagerly).
  *   "learned_split_depth" 0..3 (default 1): the learned walk runs each group
  *                        as independent tasks, one per subtree at this depth
  *                        (the nodes above it are opened for every group).
