@@ -222,37 +222,24 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   ctx->last = sp;
 }
 
-// The leapfrog with each step replayed from one CUDA graph: kick and drift,
+// One system's leapfrog step inside a captured CUDA graph: kick and drift,
 // the whole grouped solve (tree, groups, walk, evaluation, scatter) and the
-// closing kick, with no host synchronisation inside. An eager solve sizes
-// the buffers first; the graph is captured with headroom over those sizes,
-// and a replay that outgrows them aborts (its kernels return) and the step's
-// evaluation and closing kick are redone eagerly, after which the graph is
-// captured again for the new sizes. Returns the steps replayed.
-u64 leapfrog_graph(gtc_context *ctx, double *pos, double *vel, const double *mass, double *acc,
-                   double *pot, u64 n, const gtc::SolverParams &sp, double dt, u64 steps,
-                   bool prime) {
-  cudaStream_t s = ctx->stream;
-  gtc::Workspace &ws = ctx->ws;
-  const double h = 0.5 * dt;
-  if (prime) {
-    group_force(ctx, pos, mass, n, sp, acc, pot);
-  } else {  // only to size the workspace: the caller's forces stay as they are
-    ws.acc.ensure(n * 24);
-    ws.pot.ensure(n * 8);
-    group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
-  }
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  auto drop = [&] {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-  };
-  gtc::Scalars *sc = ws.scalars.as<gtc::Scalars>();
-  auto capture = [&] {
-    gtc::GraphCaps caps{};
+// closing kick, with no host synchronisation inside. reserve() sizes the
+// buffers from the system's last eager solve with headroom; record() issues
+// the step on a capturing stream; finish() reads the replay's scalars: a
+// replay that outgrew its buffers aborted (its kernels returned), so the
+// step's evaluation and closing kick are redone eagerly and the graph must
+// be captured again for the new sizes.
+struct GraphStep {
+  gtc_context *ctx = nullptr;
+  double *pos = nullptr, *vel = nullptr, *acc = nullptr, *pot = nullptr;
+  const double *mass = nullptr;
+  u64 n = 0;
+  gtc::SolverParams sp{};
+  gtc::GraphCaps caps{};
+
+  void reserve() {
+    gtc::Workspace &ws = ctx->ws;
     const gtc::Scalars &hs = *ctx->host_sc;
     const double f = 1.0 + ctx->graph_headroom;
     const u64 pad = ctx->graph_headroom > 0 ? 1024 : 0;
@@ -287,96 +274,188 @@ u64 leapfrog_graph(gtc_context *ctx, double *pos, double *vel, const double *mas
     ws.body_list.ensure(caps.bodies * 4);
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
+    if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));
     gtc::reserve_scans(ws.scan_tmp, std::max<u64>(n, m));
-    gtc::write_root_task(ws, s);
-    GTC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    gtc::write_root_task(ws, ctx->stream);
+  }
+
+  // Events are recorded as external nodes so that their times can be read.
+  void mark(int k, cudaStream_t s) const {
+    GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[k], s, cudaEventRecordExternal));
+  }
+
+  void record(double dt, cudaStream_t s) const {
+    gtc::Workspace &ws = ctx->ws;
+    gtc::Scalars *sc = ws.scalars.as<gtc::Scalars>();
+    const double h = 0.5 * dt;
+    gtc::kick_drift(pos, vel, acc, n, h, dt, s);
+    mark(0, s);
+    gtc::build_tree_graph(ws, pos, mass, n, sp, caps, s);
+    mark(1, s);
+    gtc::build_lists_graph(ws, sp, caps, s);
+    mark(2, s);
+    mark(4, s);
+    gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
+                              ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
+                              ws.groups.as<uint4>(), n, sc, static_cast<float>(sp.G),
+                              static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0,
+                              ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+    mark(5, s);
+    gtc::scatter_results_graph(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, sc, s);
+    if (ctx->have_model)
+      gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
+                               ctx->prev_amag.as<float>(), s);
+    gtc::kick(vel, acc, n, h, s, &sc->abort);
+    mark(3, s);
+  }
+
+  // After the replay and the copy of its scalars into host_sc: true if the
+  // graph must be captured again (the step was redone eagerly).
+  bool finish(double dt) {
+    gtc::Workspace &ws = ctx->ws;
+    const gtc::Scalars &hs = *ctx->host_sc;
+    if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
+    if (hs.error)
+      throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                              std::to_string(hs.error) + ")");
+    if (hs.abort) {
+      group_force(ctx, pos, mass, n, sp, acc, pot);
+      gtc::kick(vel, acc, n, 0.5 * dt, ctx->stream);
+      GTC_CUDA(cudaStreamSynchronize(ctx->stream));
+      return true;
+    }
+    ws.n_nodes = hs.n_nodes;
+    ws.n_groups = hs.n_groups;
+    ws.n_cell_list = hs.n_cell_list;
+    ws.n_body_list = hs.n_body_list;
+    gtc_stats &st = ctx->stats;
+    const u32 replays = st.graph_steps;
+    st = gtc_stats{};
+    st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
+    st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
+    st.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
+    st.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
+    st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
+    st.cell_interactions = hs.cell_interactions;
+    st.body_interactions = hs.body_interactions;
+    st.max_list = hs.max_list;
+    st.max_group = hs.max_group;
+    st.depth = hs.depth;
+    st.walk_tests_fp64 = hs.fp64_tests;
+    st.n_cell_list = hs.n_cell_list;
+    st.n_body_list = hs.n_body_list;
+    st.n_nodes = hs.n_nodes;
+    st.n_groups = hs.n_groups;
+    st.criterion_used = GTC_CRITERION_THETA;
+    st.kernel_launches = 0;  // one graph launch (its kernels were counted at capture)
+    st.graph_steps = replays + 1;
+    ctx->have_group = true;
+    ctx->last = sp;
+    return false;
+  }
+};
+
+// A captured step graph of one or more systems.
+struct StepGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+  // Captures every system's step on `main`: each system on its own stream
+  // (forked from main and joined back), then the copies of their scalars.
+  void capture(std::vector<GraphStep> &steps, double dt, cudaStream_t main, cudaEvent_t fork,
+               std::vector<cudaEvent_t> &joins) {
+    for (GraphStep &g : steps) g.reserve();
+    GTC_CUDA(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
     try {
-      gtc::kick_drift(pos, vel, acc, n, h, dt, s);
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal));
-      gtc::build_tree_graph(ws, pos, mass, n, sp, caps, s);
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal));
-      gtc::build_lists_graph(ws, sp, caps, s);
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal));
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal));
-      gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
-                                ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
-                                ws.groups.as<uint4>(), n, sc, static_cast<float>(sp.G),
-                                static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0,
-                                ws.out.as<float4>(), ctx->counter.as<u32>(), s);
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[5], s, cudaEventRecordExternal));
-      gtc::scatter_results_graph(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, sc, s);
-      if (ctx->have_model) {
-        ctx->prev_amag.ensure(n * sizeof(float));
-        gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
-                                 ctx->prev_amag.as<float>(), s);
+      GTC_CUDA(cudaEventRecord(fork, main));
+      for (std::size_t k = 0; k < steps.size(); ++k) {
+        cudaStream_t s = steps[k].ctx->stream;
+        if (s != main) GTC_CUDA(cudaStreamWaitEvent(s, fork, 0));
+        steps[k].record(dt, s);
+        GTC_CUDA(cudaMemcpyAsync(steps[k].ctx->host_sc, steps[k].ctx->ws.scalars.ptr,
+                                 sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
+        if (s != main) {
+          GTC_CUDA(cudaEventRecord(joins[k], s));
+          GTC_CUDA(cudaStreamWaitEvent(main, joins[k], 0));
+        }
       }
-      gtc::kick(vel, acc, n, h, s, &sc->abort);
-      GTC_CUDA(cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal));
     } catch (...) {
       cudaGraph_t g = nullptr;
-      cudaStreamEndCapture(s, &g);
+      cudaStreamEndCapture(main, &g);
       if (g) cudaGraphDestroy(g);
       (void)cudaGetLastError();
       throw;
     }
-    GTC_CUDA(cudaStreamEndCapture(s, &graph));
+    GTC_CUDA(cudaStreamEndCapture(main, &graph));
     GTC_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  };
+  }
+};
+
+// The leapfrog of one or more systems with every step replayed from one
+// CUDA graph. An eager solve of each system sizes its buffers first (with
+// prime, it is the priming evaluation; without, it goes to scratch and the
+// caller's forces stay). Returns the steps replayed.
+u64 leapfrog_graph_systems(std::vector<GraphStep> &sys, double dt, u64 steps, bool prime,
+                           cudaStream_t main, cudaEvent_t fork, std::vector<cudaEvent_t> &joins) {
+  for (GraphStep &g : sys) {
+    gtc::Workspace &ws = g.ctx->ws;
+    if (prime) {
+      group_force(g.ctx, g.pos, g.mass, g.n, g.sp, g.acc, g.pot);
+    } else {
+      ws.acc.ensure(g.n * 24);
+      ws.pot.ensure(g.n * 8);
+      group_force(g.ctx, g.pos, g.mass, g.n, g.sp, ws.acc.as<double>(), ws.pot.as<double>());
+    }
+    g.ctx->stats.graph_steps = 0;
+  }
+  StepGraph graph;
   u64 replays = 0;
   try {
     for (u64 k = 0; k < steps; ++k) {
-      if (!exec) capture();
-      GTC_CUDA(cudaGraphLaunch(exec, s));
-      GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, sc, sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
-      GTC_CUDA(cudaStreamSynchronize(s));
-      const gtc::Scalars &hs = *ctx->host_sc;
-      if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
-      if (hs.error)
-        throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                                std::to_string(hs.error) + ")");
-      if (hs.abort) {
-        // outgrown: this step's evaluation and closing kick, eagerly; then a
-        // new graph for the new sizes
-        group_force(ctx, pos, mass, n, sp, acc, pot);
-        gtc::kick(vel, acc, n, h, s);
-        GTC_CUDA(cudaStreamSynchronize(s));
-        drop();
-        continue;
-      }
-      ++replays;
-      ws.n_nodes = hs.n_nodes;
-      ws.n_groups = hs.n_groups;
-      ws.n_cell_list = hs.n_cell_list;
-      ws.n_body_list = hs.n_body_list;
-      gtc_stats &st = ctx->stats;
-      st = gtc_stats{};
-      st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
-      st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
-      st.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
-      st.total_ms = elapsed(ctx->ev[0], ctx->ev[3]);
-      st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
-      st.cell_interactions = hs.cell_interactions;
-      st.body_interactions = hs.body_interactions;
-      st.max_list = hs.max_list;
-      st.max_group = hs.max_group;
-      st.depth = hs.depth;
-      st.walk_tests_fp64 = hs.fp64_tests;
-      st.n_cell_list = hs.n_cell_list;
-      st.n_body_list = hs.n_body_list;
-      st.n_nodes = hs.n_nodes;
-      st.n_groups = hs.n_groups;
-      st.criterion_used = GTC_CRITERION_THETA;
-      st.kernel_launches = 0;  // one graph launch (its kernels were counted at capture)
-      ctx->have_group = true;
-      ctx->last = sp;
+      if (!graph.exec) graph.capture(sys, dt, main, fork, joins);
+      GTC_CUDA(cudaGraphLaunch(graph.exec, main));
+      GTC_CUDA(cudaStreamSynchronize(main));
+      bool again = false;
+      for (GraphStep &g : sys) again |= g.finish(dt);
+      if (again) graph.drop();
+      else ++replays;
     }
   } catch (...) {
-    drop();
+    graph.drop();
     throw;
   }
-  drop();
-  ctx->stats.graph_steps = static_cast<u32>(std::min<u64>(replays, 0xffffffffu));
+  graph.drop();
   return replays;
+}
+
+u64 leapfrog_graph(gtc_context *ctx, double *pos, double *vel, const double *mass, double *acc,
+                   double *pot, u64 n, const gtc::SolverParams &sp, double dt, u64 steps,
+                   bool prime) {
+  std::vector<GraphStep> sys(1);
+  sys[0].ctx = ctx;
+  sys[0].pos = pos;
+  sys[0].vel = vel;
+  sys[0].mass = mass;
+  sys[0].acc = acc;
+  sys[0].pot = pot;
+  sys[0].n = n;
+  sys[0].sp = sp;
+  std::vector<cudaEvent_t> joins(1, nullptr);
+  cudaEvent_t fork = nullptr;
+  GTC_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  try {
+    const u64 r = leapfrog_graph_systems(sys, dt, steps, prime, ctx->stream, fork, joins);
+    cudaEventDestroy(fork);
+    return r;
+  } catch (...) {
+    cudaEventDestroy(fork);
+    throw;
+  }
 }
 
 void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
@@ -421,6 +500,41 @@ __global__ void k_unpack_direct(const float4 *out, u32 n, double *acc, double *p
   pot[i] = o.w;
 }
 }  // namespace gtc
+
+// Independent systems advanced together: one context (stream, workspace)
+// per system, every system's step in one captured graph.
+struct gtc_ensemble {
+  int device = 0;
+  cudaStream_t main = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  std::vector<gtc_context *> ctx;
+  std::vector<GraphStep> sys;
+  std::string error;
+};
+
+namespace {
+template <class F>
+gtc_status ensemble_guarded(gtc_ensemble *e, F &&f) {
+  if (!e) return GTC_INVALID_ARGUMENT;
+  try {
+    GTC_CUDA(cudaSetDevice(e->device));
+    f();
+    e->error.clear();
+    return GTC_OK;
+  } catch (const gtc::InvalidArgument &ex) {
+    e->error = ex.what();
+    return GTC_INVALID_ARGUMENT;
+  } catch (const gtc::OutOfMemory &ex) {
+    e->error = ex.what();
+    return GTC_OUT_OF_MEMORY;
+  } catch (const std::exception &ex) {
+    e->error = ex.what();
+    return GTC_RUNTIME_ERROR;
+  }
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -934,6 +1048,144 @@ gtc_status gtc_learned_predict(gtc_context *ctx, const float *feat, uint64_t n, 
     gtc::learned_predict(ctx->net.as<gtc::LearnedNet>(), f.as<float>(), n, p.as<float>(), s);
     GTC_CUDA(cudaMemcpyAsync(pred, p.ptr, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+// ---------------------------------------------------- ensembles and tuning
+
+void gtc_ensemble_destroy(gtc_ensemble *e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->main) cudaStreamSynchronize(e->main);
+  for (gtc_context *c : e->ctx) gtc_destroy(c);
+  for (cudaEvent_t ev : e->joins)
+    if (ev) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->main) cudaStreamDestroy(e->main);
+  delete e;
+}
+
+gtc_status gtc_ensemble_create(gtc_ensemble **out, int device, uint32_t systems) {
+  if (!out) return GTC_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (systems == 0 || systems > 4096) {
+    g_create_error = "an ensemble holds 1..4096 systems";
+    return GTC_INVALID_ARGUMENT;
+  }
+  gtc_ensemble *e = new (std::nothrow) gtc_ensemble;
+  if (!e) return GTC_OUT_OF_MEMORY;
+  e->device = device;
+  for (uint32_t k = 0; k < systems; ++k) {
+    gtc_context *c = nullptr;
+    const gtc_status st = gtc_create(&c, device);
+    if (st != GTC_OK) {
+      gtc_ensemble_destroy(e);
+      return st;
+    }
+    e->ctx.push_back(c);
+  }
+  try {
+    GTC_CUDA(cudaSetDevice(device));
+    GTC_CUDA(cudaStreamCreateWithFlags(&e->main, cudaStreamNonBlocking));
+    GTC_CUDA(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming));
+    e->joins.assign(systems, nullptr);
+    for (auto &ev : e->joins) GTC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  } catch (const std::exception &ex) {
+    g_create_error = ex.what();
+    gtc_ensemble_destroy(e);
+    return GTC_RUNTIME_ERROR;
+  }
+  e->sys.assign(systems, GraphStep{});
+  for (uint32_t k = 0; k < systems; ++k) e->sys[k].ctx = e->ctx[k];
+  *out = e;
+  return GTC_OK;
+}
+
+const char *gtc_ensemble_last_error(const gtc_ensemble *e) {
+  return e ? e->error.c_str() : g_create_error.c_str();
+}
+
+gtc_context *gtc_ensemble_context(gtc_ensemble *e, uint32_t i) {
+  return e && i < e->ctx.size() ? e->ctx[i] : nullptr;
+}
+
+gtc_status gtc_ensemble_set_system(gtc_ensemble *e, uint32_t i, double *pos, double *vel,
+                                   const double *mass, double *acc, double *pot, uint64_t n,
+                                   const gtc_gravity_params *gp) {
+  return ensemble_guarded(e, [&] {
+    if (i >= e->sys.size()) throw gtc::InvalidArgument("system index out of range");
+    const gtc::SolverParams sp = check_params(gp, true);
+    if (sp.criterion != GTC_CRITERION_THETA)
+      throw gtc::InvalidArgument("ensembles use the theta criterion");
+    if (n == 0 || !pos || !vel || !mass || !acc || !pot)
+      throw gtc::InvalidArgument("every system needs bodies and pos, vel, mass, acc, pot");
+    if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the 32 bit GPU indices");
+    GraphStep &g = e->sys[i];
+    g.pos = pos;
+    g.vel = vel;
+    g.mass = mass;
+    g.acc = acc;
+    g.pot = pot;
+    g.n = n;
+    g.sp = sp;
+  });
+}
+
+gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int prime,
+                                 int graph) {
+  return ensemble_guarded(e, [&] {
+    if (!std::isfinite(dt)) throw gtc::InvalidArgument("dt must be finite");
+    for (const GraphStep &g : e->sys)
+      if (g.n == 0) throw gtc::InvalidArgument("every system must be set before stepping");
+    if (graph) {
+      leapfrog_graph_systems(e->sys, dt, steps, prime != 0, e->main, e->fork, e->joins);
+      return;
+    }
+    for (GraphStep &g : e->sys)
+      if (prime) group_force(g.ctx, g.pos, g.mass, g.n, g.sp, g.acc, g.pot);
+    const double h = 0.5 * dt;
+    for (u64 k = 0; k < steps; ++k)
+      for (GraphStep &g : e->sys) {
+        gtc::kick_drift(g.pos, g.vel, g.acc, g.n, h, dt, g.ctx->stream);
+        group_force(g.ctx, g.pos, g.mass, g.n, g.sp, g.acc, g.pot);
+        gtc::kick(g.vel, g.acc, g.n, h, g.ctx->stream);
+      }
+    for (GraphStep &g : e->sys) GTC_CUDA(cudaStreamSynchronize(g.ctx->stream));
+  });
+}
+
+gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double *mass,
+                              uint64_t n, const gtc_gravity_params *base,
+                              gtc_gravity_params *best, double *best_ms) {
+  return guarded(ctx, [&] {
+    if (!base || !best) throw gtc::InvalidArgument("base and best parameters are required");
+    if (n == 0 || !pos || !mass) throw gtc::InvalidArgument("pos and mass are required");
+    check_params(base, true);
+    gtc::Workspace &ws = ctx->ws;
+    ws.acc.ensure(n * 24);
+    ws.pot.ensure(n * 8);
+    double best_t = 1e300;
+    gtc_gravity_params pick = *base;
+    for (int gs : {8, 16, 24, 32})
+      for (int pack : {0, 1}) {
+        gtc_gravity_params p = *base;
+        p.group_size = gs;
+        p.pack = pack;
+        p.criterion = GTC_CRITERION_THETA;
+        const gtc::SolverParams sp = check_params(&p, true);
+        double t = 0;
+        for (int rep = 0; rep < 4; ++rep) {
+          group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+          if (rep > 0) t += ctx->stats.total_ms;  // the first warms up
+        }
+        if (t / 3 < best_t) {
+          best_t = t / 3;
+          pick = p;
+        }
+      }
+    pick.criterion = base->criterion;
+    *best = pick;
+    if (best_ms) *best_ms = best_t;
   });
 }
 

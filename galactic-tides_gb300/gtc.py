@@ -115,6 +115,14 @@ def _load():
         "gtc_leapfrog_device": (I, [V, P, P, P, P, P, U64, C.POINTER(GravityParams), I, D, U64,
                                     I, I]),
         "gtc_diagnostics_device": (I, [V, P, P, P, P, U64, D, C.POINTER(Diagnostics)]),
+        "gtc_ensemble_create": (I, [C.POINTER(V), I, U32]),
+        "gtc_ensemble_destroy": (None, [V]),
+        "gtc_ensemble_last_error": (C.c_char_p, [V]),
+        "gtc_ensemble_set_system": (I, [V, U32, P, P, P, P, P, U64, C.POINTER(GravityParams)]),
+        "gtc_ensemble_leapfrog": (I, [V, D, U64, I, I]),
+        "gtc_ensemble_context": (V, [V, U32]),
+        "gtc_autotune_group": (I, [V, P, P, U64, C.POINTER(GravityParams),
+                                   C.POINTER(GravityParams), C.POINTER(C.c_double)]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -268,6 +276,17 @@ class Context:
 
     def set_option(self, name, value):
         self._check(lib.gtc_set_option(self.h, name.encode(), float(value)))
+
+    # ---- tuning ----------------------------------------------------------------
+
+    def autotune_group(self, pos_ptr, mass_ptr, n, **kw):
+        """gtc_autotune_group -> (group_size, pack, ms per evaluation)."""
+        base = gravity_params(**kw)
+        best = GravityParams()
+        ms = C.c_double()
+        self._check(lib.gtc_autotune_group(self.h, pos_ptr, mass_ptr, n, C.byref(base),
+                                           C.byref(best), C.byref(ms)))
+        return best.group_size, bool(best.pack), ms.value
 
     # ---- time integration ------------------------------------------------------
 
@@ -477,3 +496,59 @@ def make_encounter(n_each, seed=1, incl1=30.0, incl2=60.0, rp=2.0, r0=15.0, omeg
                                      _ptr(vel), _ptr(mass), _ptr(typ)):
         raise ValueError("invalid encounter")
     return pos, vel, mass, typ
+
+
+class _Borrowed(Context):
+    """A context owned by an ensemble (not destroyed by this object)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def close(self):
+        self.h = None
+
+
+class Ensemble:
+    """gtc_ensemble: independent systems advanced together (device arrays)."""
+
+    def __init__(self, systems, device=0):
+        h = C.c_void_p()
+        rc = lib.gtc_ensemble_create(C.byref(h), device, systems)
+        if rc != GTC_OK:
+            raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(
+                rc, lib.gtc_ensemble_last_error(None).decode())
+        self.h = h
+        self.systems = systems
+
+    def _check(self, rc):
+        if rc != GTC_OK:
+            msg = lib.gtc_ensemble_last_error(self.h).decode()
+            raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(rc, msg)
+
+    def set_system(self, i, pos_ptr, vel_ptr, mass_ptr, acc_ptr, pot_ptr, n, **kw):
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_ensemble_set_system(self.h, i, pos_ptr, vel_ptr, mass_ptr, acc_ptr,
+                                                pot_ptr, n, C.byref(gp)))
+
+    def leapfrog(self, dt, steps, prime=True, graph=True):
+        self._check(lib.gtc_ensemble_leapfrog(self.h, dt, steps, int(prime), int(graph)))
+
+    def context(self, i):
+        return _Borrowed(lib.gtc_ensemble_context(self.h, i))
+
+    def close(self):
+        if self.h:
+            lib.gtc_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

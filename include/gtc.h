@@ -235,6 +235,36 @@ gtc_status gtc_diagnostics_device(gtc_context *ctx, const double *pos, const dou
                                   const double *mass, const double *pot, uint64_t n,
                                   double time, gtc_diagnostics *out);
 
+/* ---- batched ensembles (no reference counterpart) ---------------------- */
+
+/* Independent systems (galaxies) advanced together: each has its own
+ * context (stream, workspace), and with graph = 1 one CUDA graph launch
+ * replays every system's whole step (kick, drift, rebuild, evaluation,
+ * kick), the systems' kernel chains running concurrently. */
+typedef struct gtc_ensemble gtc_ensemble;
+gtc_status gtc_ensemble_create(gtc_ensemble **e, int device, uint32_t systems);
+void gtc_ensemble_destroy(gtc_ensemble *e);
+/* Message of the last failed call on e (NULL: of gtc_ensemble_create). */
+const char *gtc_ensemble_last_error(const gtc_ensemble *e);
+/* System i's device arrays (n bodies; acc and pot receive its forces) and
+ * grouped-solver parameters (theta criterion). */
+gtc_status gtc_ensemble_set_system(gtc_ensemble *e, uint32_t i, double *pos, double *vel,
+                                   const double *mass, double *acc, double *pot, uint64_t n,
+                                   const gtc_gravity_params *gp);
+/* gtc_leapfrog_device for every system: prime, then `steps` steps of dt. */
+gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int prime,
+                                 int graph);
+/* System i's context (its stats, exports and options). */
+gtc_context *gtc_ensemble_context(gtc_ensemble *e, uint32_t i);
+
+/* The autotuner: times the grouped solver (theta criterion) on these bodies
+ * (device arrays) for group_size 8, 16, 24, 32 with sibling packing off and
+ * on, and returns in *best the base parameters with the fastest pair, and
+ * its mean time per evaluation in *best_ms. */
+gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double *mass,
+                              uint64_t n, const gtc_gravity_params *base,
+                              gtc_gravity_params *best, double *best_ms);
+
 /* ---- tuning and diagnostics (no reference counterpart) ------------------ */
 
 /* Sets an option of the context:

@@ -213,3 +213,44 @@ def test_encounter_energy_drift(gtc):
         assert c.stats()["graph_steps"] >= 90
     assert abs(d1["total"] / d0["total"] - 1) < 2e-3
     assert np.abs(d1["momentum"]).max() < 1e-3 * np.abs(mass).sum()
+
+
+@gpu
+def test_ensemble_step_graph_equals_each_system_alone(gtc):
+    """Three galaxies advanced together (one graph launch per step, tuned-like
+    parameters per system) give bitwise the trajectories each gives alone."""
+    import torch
+    specs = [(12_000, 1, 32, True), (30_000, 2, 16, False), (8_000, 3, 24, True)]
+    alone = []
+    with gtc.Context(0) as c:
+        for n, seed, gs, pack in specs:
+            pos, vel, mass, _ = gtc.make_galaxy(n, seed=seed)
+            alone.append(_run(c, pos, vel, mass, 0.01, 5, group_size=gs, pack=pack))
+    d = torch.device("cuda", 0)
+    bufs = []
+    with gtc.Ensemble(len(specs)) as ens:
+        for i, (n, seed, gs, pack) in enumerate(specs):
+            pos, vel, mass, _ = gtc.make_galaxy(n, seed=seed)
+            dpos, dvel, dmass = _dev(pos, vel, mass)
+            dacc = torch.zeros((n, 3), dtype=torch.float64, device=d)
+            dpot = torch.zeros(n, dtype=torch.float64, device=d)
+            bufs.append((dpos, dvel, dacc, dpot, dmass))
+            kw = dict(SOLVER, group_size=gs, pack=pack)
+            ens.set_system(i, dpos.data_ptr(), dvel.data_ptr(), dmass.data_ptr(), dacc.data_ptr(),
+                           dpot.data_ptr(), n, **kw)
+        ens.leapfrog(0.01, 5, prime=True, graph=True)
+        torch.cuda.synchronize()
+        for i in range(len(specs)):
+            assert ens.context(i).stats()["graph_steps"] == 5
+    for (dpos, dvel, dacc, dpot, _), want in zip(bufs, alone):
+        assert np.array_equal(dpos.cpu().numpy(), want[0])
+        assert np.array_equal(dvel.cpu().numpy(), want[1])
+        assert np.array_equal(dacc.cpu().numpy(), want[2])
+
+
+@gpu
+def test_autotuner_returns_a_timed_configuration(ctx, gtc):
+    pos, _, mass, _ = gtc.make_galaxy(60_000, seed=9)
+    dpos, dmass = _dev(pos, mass)
+    gs, pack, ms = ctx.autotune_group(dpos.data_ptr(), dmass.data_ptr(), len(mass), **SOLVER)
+    assert gs in (8, 16, 24, 32) and isinstance(pack, bool) and ms > 0
