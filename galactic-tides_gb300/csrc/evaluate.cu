@@ -11,8 +11,9 @@
 // load, then one 48-byte cell or 16-byte body), scales its mass and
 // quadrupole by G once, and stages it in shared memory; then every lane
 // reads the 32 staged entries back as broadcast loads (one shared-memory
-// transaction serves the whole warp) and accumulates. The body index of
-// each staged entry is passed round with __shfl_sync for the self test.
+// transaction serves the whole warp) and accumulates. A group of 16 or
+// fewer targets splits its lists into 2-4 slices worked by separate lane
+// sets (lanes that would otherwise idle), summed by shuffles at the end.
 // Groups are handed out to warps by an atomic counter, so a warp that drew
 // a long list does not hold back the others' next groups.
 
@@ -77,8 +78,12 @@ __global__ void __launch_bounds__(kT)
            const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
            float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev = nullptr,
            const u32 *abort = nullptr) {
-  __shared__ Staged sc[kWarpsPerBlock][32];
-  __shared__ float4 sb[kWarpsPerBlock][32];
+  // Staged entries, per warp: slice k's W entries start at float4 k (3W + 1)
+  // (cells) and k (W + 1) (bodies); the 16-byte gap puts the slices on
+  // different shared-memory banks, so their broadcast loads do not conflict.
+  __shared__ float4 sc[kWarpsPerBlock][3 * 32 + 4];
+  __shared__ float4 sb[kWarpsPerBlock][32 + 4];
+  __shared__ u32 sj[kWarpsPerBlock][kSoft ? 1 : 32 + 4];  // staged body indices (self test)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // a graph replay: the group count from the device, nothing after an abort
   if (abort && *abort) return;
@@ -89,63 +94,108 @@ __global__ void __launch_bounds__(kT)
     g = __shfl_sync(kFullMask, g, 0);
     if (g >= ngroups) return;
     const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
-    const u32 i = ga.x + lane;
-    const bool active = i < ga.y;
-    const float4 bi = active ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // A group of T <= 16 targets splits its lists into ns = min(4, 32 / T)
+    // slices: lane l takes target l % T of slice l / T, each slice stages
+    // W = 32 / ns entries per round, and the slices' sums are added up by
+    // shuffles at the end (larger groups: one slice, W = 32).
+    const u32 T = ga.y - ga.x;
+    const u32 ns = T == 0 ? 1u : min(4u, 32u / T);
+    const u32 W = 32u / ns;
+    const u32 slice = T ? static_cast<u32>(lane) / T : 0u;
+    const u32 t = T ? static_cast<u32>(lane) % T : 0u;
+    const bool computes = slice < ns;  // lanes past ns * T only stage
+    const u32 i = ga.x + t;
+    const float4 bi = computes ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const u32 stage_slice = static_cast<u32>(lane) / W, stage_pos = static_cast<u32>(lane) % W;
     float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
 
-    for (u32 base = ga.z; base < ga.w; base += 32) {
-      const u32 k = base + lane;
-      if (k < ga.w) {
-        const u64 c = cell_list[k];
-        const float4 c0 = __ldg(&cells[3 * c]);
-        Staged st;
-        st.cm = make_float4(c0.x, c0.y, c0.z, G * c0.w);
-        if (kQuad) {
-          const float4 c1 = __ldg(&cells[3 * c + 1]), c2 = __ldg(&cells[3 * c + 2]);
-          st.q0 = make_float4(G * c1.x, G * c1.y, G * c1.z, G * c1.w);
-          st.q1 = make_float4(G * c2.x, G * c2.y, 0.f, 0.f);
+    {
+      const u32 e = ga.w - ga.z;  // cells, slice k: [e k / ns, e (k + 1) / ns)
+      const u32 c0 = ga.z + e * stage_slice / ns, c1 = ga.z + e * (stage_slice + 1) / ns;
+      const u32 m0 = ga.z + e * slice / ns, m1 = ga.z + e * (slice + 1) / ns;
+      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
+      for (u32 r = 0; r < rounds; ++r) {
+        const u32 k = c0 + r * W + stage_pos;
+        if (stage_slice < ns && k < c1) {
+          const u64 c = cell_list[k];
+          const float4 q = __ldg(&cells[3 * c]);
+          float4 *dst = &sc[warp][stage_slice * (3 * W + 1) + 3 * stage_pos];
+          dst[0] = make_float4(q.x, q.y, q.z, G * q.w);
+          if (kQuad) {
+            const float4 c1v = __ldg(&cells[3 * c + 1]), c2v = __ldg(&cells[3 * c + 2]);
+            dst[1] = make_float4(G * c1v.x, G * c1v.y, G * c1v.z, G * c1v.w);
+            dst[2] = make_float4(G * c2v.x, G * c2v.y, 0.f, 0.f);
+          }
         }
-        sc[warp][lane] = st;
+        __syncwarp();
+        const u32 base = m0 + r * W;
+        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+        const float4 *mine = &sc[warp][slice * (3 * W + 1)];
+        for (u32 j = 0; j < cnt; ++j) {
+          Staged st;
+          st.cm = mine[3 * j];
+          if (kQuad) {
+            st.q0 = mine[3 * j + 1];
+            st.q1 = mine[3 * j + 2];
+          }
+          add_cell<kQuad>(bi.x, bi.y, bi.z, st, eps2, ax, ay, az, pot);
+        }
+        __syncwarp();
       }
-      __syncwarp();
-      const u32 cnt = min(32u, ga.w - base);
-      for (u32 t = 0; t < cnt; ++t) add_cell<kQuad>(bi.x, bi.y, bi.z, sc[warp][t], eps2, ax, ay, az, pot);
-      __syncwarp();
     }
 
-    for (u32 base = gb.x; base < gb.y; base += 32) {
-      const u32 k = base + lane;
-      u32 j = 0xffffffffu;
-      if (k < gb.y) {
-        j = body_list[k];
-        const float4 b = __ldg(&bodies[j]);
-        sb[warp][lane] = make_float4(b.x, b.y, b.z, G * b.w);
-      }
-      __syncwarp();
-      const u32 cnt = min(32u, gb.y - base);
-      for (u32 t = 0; t < cnt; ++t) {
-        const float4 b = sb[warp][t];
-        const float dx = bi.x - b.x, dy = bi.y - b.y, dz = bi.z - b.z;
-        float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-        float w = b.w;
-        if (!kSoft) {
-          const bool self = __shfl_sync(kFullMask, j, t) == i;
-          r2 = self ? 1.0f : r2;
-          w = self ? 0.0f : w;
+    {
+      const u32 e = gb.y - gb.x;
+      const u32 c0 = gb.x + e * stage_slice / ns, c1 = gb.x + e * (stage_slice + 1) / ns;
+      const u32 m0 = gb.x + e * slice / ns, m1 = gb.x + e * (slice + 1) / ns;
+      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
+      for (u32 r = 0; r < rounds; ++r) {
+        const u32 k = c0 + r * W + stage_pos;
+        if (stage_slice < ns && k < c1) {
+          const u32 j = body_list[k];
+          const float4 b = __ldg(&bodies[j]);
+          sb[warp][stage_slice * (W + 1) + stage_pos] = make_float4(b.x, b.y, b.z, G * b.w);
+          if (!kSoft) sj[warp][stage_slice * (W + 1) + stage_pos] = j;
         }
-        const float inv = rsqrtf(r2);
-        const float gm = w * inv;
-        const float gm3 = gm * inv * inv;
-        ax = fmaf(-gm3, dx, ax);
-        ay = fmaf(-gm3, dy, ay);
-        az = fmaf(-gm3, dz, az);
-        pot -= gm;
+        __syncwarp();
+        const u32 base = m0 + r * W;
+        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+        const float4 *mine = &sb[warp][slice * (W + 1)];
+        for (u32 q = 0; q < cnt; ++q) {
+          const float4 b = mine[q];
+          const float dx = bi.x - b.x, dy = bi.y - b.y, dz = bi.z - b.z;
+          float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+          float w = b.w;
+          if (!kSoft) {
+            const bool self = sj[warp][kSoft ? 0 : slice * (W + 1) + q] == i;
+            r2 = self ? 1.0f : r2;
+            w = self ? 0.0f : w;
+          }
+          const float inv = rsqrtf(r2);
+          const float gm = w * inv;
+          const float gm3 = gm * inv * inv;
+          ax = fmaf(-gm3, dx, ax);
+          ay = fmaf(-gm3, dy, ay);
+          az = fmaf(-gm3, dz, az);
+          pot -= gm;
+        }
+        __syncwarp();
       }
-      __syncwarp();
+    }
+    // the slices' partial sums onto slice 0
+    for (u32 k = 1; k < ns; ++k) {
+      const int src = min(lane + static_cast<int>(k * T), 31);
+      const float sx = __shfl_sync(kFullMask, ax, src), sy = __shfl_sync(kFullMask, ay, src),
+                  sz = __shfl_sync(kFullMask, az, src), sp = __shfl_sync(kFullMask, pot, src);
+      if (slice == 0) {
+        ax += sx;
+        ay += sy;
+        az += sz;
+        pot += sp;
+      }
     }
     if (kSoft) pot += G * bi.w * rsqrtf(eps2);  // the self term, added once above
-    if (active) out[i] = make_float4(ax, ay, az, pot);
+    if (slice == 0 && t < T) out[i] = make_float4(ax, ay, az, pot);
   }
 }
 

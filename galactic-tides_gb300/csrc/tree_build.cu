@@ -538,21 +538,40 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
 // children are complete when it is combined. Nodes are bucketed by depth
 // (bucket kLeafBucket holds the leaves); the order inside a bucket does not
 // matter, each node's sums run in the reference's order.
-constexpr int kLeafBucket = kMaxDepth + 1;
-constexpr int kBuckets = kMaxDepth + 2;
+// Buckets also split by size -- inner nodes by child count, leaves by body
+// count -- so that the nodes a warp combines loop the same number of times:
+// the FP64 pipe, the bound here, then issues full warps.
+constexpr int kSizeClasses = 8;                          // 1..8 children
+constexpr int kLeafClasses = 9;                          // 1..8 bodies, more
+constexpr int kLeafBucket = (kMaxDepth + 1) * kSizeClasses;  // first leaf bucket
+constexpr int kBuckets = kLeafBucket + kLeafClasses;
+
+struct BucketView {
+  const u8 *depth, *isleaf, *nchild;
+  const u32 *nbegin, *nend;
+};
+
+__device__ __forceinline__ int bucket_of(const BucketView &v, u32 p) {
+  if (v.isleaf[p]) {
+    const u32 nb = v.nend[p] - v.nbegin[p];
+    return kLeafBucket + static_cast<int>(nb < 1 ? 0u : min(nb, static_cast<u32>(kLeafClasses)) - 1);
+  }
+  const int c = v.nchild[p];
+  return v.depth[p] * kSizeClasses + (c < 1 ? 0 : min(c, kSizeClasses) - 1);
+}
 
 // Per-block histograms in shared memory, one global atomic per bucket.
 __global__ void __launch_bounds__(kT)
-    k_bucket_count(const u8 *depth, const u8 *isleaf, u32 m, u32 *count,
-                   const u32 *m_dev = nullptr, u32 *abort = nullptr, int depth_cap = kMaxDepth) {
+    k_bucket_count(BucketView v, u32 m, u32 *count, const u32 *m_dev = nullptr,
+                   u32 *abort = nullptr, int depth_cap = kMaxDepth) {
   __shared__ u32 h[kBuckets];
   if (aborted(abort)) return;
   for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
   __syncthreads();
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p < bounded(m, m_dev)) {
-    if (abort && !isleaf[p] && depth[p] > depth_cap) atomicOr(abort, 4u);
-    atomicAdd(&h[isleaf[p] ? kLeafBucket : depth[p]], 1u);
+    if (abort && !v.isleaf[p] && v.depth[p] > depth_cap) atomicOr(abort, 4u);
+    atomicAdd(&h[bucket_of(v, p)], 1u);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < kBuckets; b += kT)
@@ -573,8 +592,8 @@ __global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill,
 
 // Each block reserves one range per bucket, then places its nodes in it.
 __global__ void __launch_bounds__(kT)
-    k_bucket_fill(const u8 *depth, const u8 *isleaf, u32 m, const u32 *offset, u32 *fill,
-                  u32 *bucket, const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
+    k_bucket_fill(BucketView v, u32 m, const u32 *offset, u32 *fill, u32 *bucket,
+                  const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   __shared__ u32 h[kBuckets], base[kBuckets];
   if (aborted(abort)) return;
   for (int b = threadIdx.x; b < kBuckets; b += kT) h[b] = 0;
@@ -583,7 +602,7 @@ __global__ void __launch_bounds__(kT)
   int b = -1;
   u32 local = 0;
   if (p < bounded(m, m_dev)) {
-    b = isleaf[p] ? kLeafBucket : depth[p];
+    b = bucket_of(v, p);
     local = atomicAdd(&h[b], 1u);
   }
   __syncthreads();
@@ -605,15 +624,18 @@ __global__ void __launch_bounds__(kT)
   if (k < count) node_moments(a, bucket[k]);
 }
 
-// A graph replay's moments of bucket b: the count and offset from the
-// device (meta = count[kBuckets], offset[kBuckets]), grid-stride.
+// A graph replay's moments of the nb consecutive buckets from b0: the
+// counts and offset from the device (meta = count[kBuckets],
+// offset[kBuckets]), grid-stride.
 __global__ void __launch_bounds__(kT)
-    k_moments_graph(MomentArrays a, const u32 *bucket, const u32 *meta, int b,
+    k_moments_graph(MomentArrays a, const u32 *bucket, const u32 *meta, int b0, int nb,
                     const u32 *abort) {
   if (*abort) return;
-  const u32 count = meta[b], off = meta[kBuckets + b];
+  u32 count = 0;
+  for (int b = b0; b < b0 + nb; ++b) count += meta[b];
+  const u32 off = meta[kBuckets + b0];
   for (u32 k = blockIdx.x * kT + threadIdx.x; k < count; k += gridDim.x * kT) {
-    if (b == kLeafBucket) leaf_moments(a, bucket[off + k]);
+    if (b0 >= kLeafBucket) leaf_moments(a, bucket[off + k]);
     else node_moments(a, bucket[off + k]);
   }
 }
@@ -690,7 +712,7 @@ __global__ void __launch_bounds__(kT)
 // Pinned host words for small read-backs (kept in the workspace).
 u32 *host_meta(Workspace &ws) {
   if (!ws.host_words) {
-    GTC_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ws.host_words), 256 * sizeof(u32),
+    GTC_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ws.host_words), 2 * kBuckets * sizeof(u32),
                            cudaHostAllocDefault));
   }
   return ws.host_words;
@@ -871,12 +893,13 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   u32 *meta = ws.arrive.as<u32>();  // count[kBuckets], offset[kBuckets], fill[kBuckets]
   u32 *bucket = ws.bucket.as<u32>();
   GTC_CUDA(cudaMemsetAsync(meta, 0, kBuckets * sizeof(u32), s));
-  k_bucket_count<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, meta);
+  const BucketView bv{ws.depth.as<u8>(), ws.isleaf.as<u8>(), ws.nchild.as<u8>(),
+                      ws.nbegin.as<u32>(), ws.nend.as<u32>()};
+  k_bucket_count<<<mb, kT, 0, s>>>(bv, m, meta);
   GTC_LAUNCH_CHECK();
   k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets);
   GTC_LAUNCH_CHECK();
-  k_bucket_fill<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, meta + kBuckets,
-                                  meta + 2 * kBuckets, bucket);
+  k_bucket_fill<<<mb, kT, 0, s>>>(bv, m, meta + kBuckets, meta + 2 * kBuckets, bucket);
   GTC_LAUNCH_CHECK();
   u32 counts[2 * kBuckets];
   GTC_CUDA(cudaMemcpyAsync(host_meta(ws), meta, 2 * kBuckets * sizeof(u32),
@@ -887,13 +910,20 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
                   ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
                   ws.quad.as<double2>(), ws.delta.as<double>()};
+  auto range = [&](int b0, int nb, u32 &c, u32 &o) {
+    c = 0;
+    for (int b = b0; b < b0 + nb; ++b) c += counts[b];
+    o = counts[kBuckets + b0];
+  };
   {
-    const u32 c = counts[kLeafBucket], o = counts[kBuckets + kLeafBucket];
+    u32 c, o;
+    range(kLeafBucket, kLeafClasses, c, o);
     if (c) k_leaf_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
     GTC_LAUNCH_CHECK();
   }
   for (int d = kMaxDepth; d >= 0; --d) {
-    const u32 c = counts[d], o = counts[kBuckets + d];
+    u32 c, o;
+    range(d * kSizeClasses, kSizeClasses, c, o);
     if (!c) continue;
     k_node_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
     GTC_LAUNCH_CHECK();
@@ -955,13 +985,14 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   u32 *meta = ws.arrive.as<u32>();
   u32 *bucket = ws.bucket.as<u32>();
   GTC_CUDA(cudaMemsetAsync(meta, 0, kBuckets * sizeof(u32), s));
-  k_bucket_count<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), mcap, meta, m_dev, abort,
-                                   caps.depth);
+  const BucketView bv{ws.depth.as<u8>(), ws.isleaf.as<u8>(), ws.nchild.as<u8>(),
+                      ws.nbegin.as<u32>(), ws.nend.as<u32>()};
+  k_bucket_count<<<mb, kT, 0, s>>>(bv, mcap, meta, m_dev, abort, caps.depth);
   GTC_LAUNCH_CHECK();
   k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets, abort);
   GTC_LAUNCH_CHECK();
-  k_bucket_fill<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), mcap, meta + kBuckets,
-                                  meta + 2 * kBuckets, bucket, m_dev, abort);
+  k_bucket_fill<<<mb, kT, 0, s>>>(bv, mcap, meta + kBuckets, meta + 2 * kBuckets, bucket, m_dev,
+                                  abort);
   GTC_LAUNCH_CHECK();
   MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
@@ -971,10 +1002,10 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const u32 gb = std::min<u32>(mb, static_cast<u32>(std::max(1, 8 * sms)));
-  k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, kLeafBucket, abort);
+  k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
   GTC_LAUNCH_CHECK();
   for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
-    k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, d, abort);
+    k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses, abort);
     GTC_LAUNCH_CHECK();
   }
   k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
