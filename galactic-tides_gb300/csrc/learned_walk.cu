@@ -269,6 +269,7 @@ struct LArgs {
   uint4 *seg;              // per item: first cell, cells, first run, runs (region indices)
   uint4 *seg2;             // per item: first deferred, deferred, bodies, 0
   u32 *pcount;             // per item of the round (storage order): deferred
+  unsigned long long *gcells, *gbodies;  // per group: list entries of all its items
   Scalars *sc;
 };
 
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
   Scalars *sc = a.sc;
 
   u64 item = kNoItem, store = 0;
-  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0;
+  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0, grp = 0;
   int pre = -1;  // the network's decision on a deferred item's node
   bool exhausted = false;
   float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f}, tau = 0.f;
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
           exhausted = true;
         } else {
           item = k;
-          u32 g;
+          u32 &g = grp;
           if (a.round == 0) {
             const u32 t = static_cast<u32>(k / a.ng);
             g = static_cast<u32>(k % a.ng);
@@ -390,6 +391,8 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
                              static_cast<u32>(gtid * a.lane_runs + r0i), lr - r0i);
       a.seg2[gi] = make_uint4(static_cast<u32>(gtid * a.lane_pend + p0i), lp - p0i, nb, 0u);
       a.pcount[store] = lp - p0i;
+      if (lc > c0i) atomicAdd(&a.gcells[grp], static_cast<unsigned long long>(lc - c0i));
+      if (nb) atomicAdd(&a.gbodies[grp], static_cast<unsigned long long>(nb));
       item = kNoItem;
     }
   }
@@ -467,40 +470,12 @@ struct RoundView {
   u32 rounds, ntasks, ng;
 };
 
-// Per group: its items' cells and bodies summed, and the list counters.
-__global__ void __launch_bounds__(kT)
-    k_lsum(const uint4 *seg, const uint4 *seg2, RoundView rv, const u32 *gbegin,
-           const u32 *gend, u64 *ncells, u64 *nbodies, Scalars *sc) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= rv.ng) return;
-  u64 nc = 0, nb = 0;
-  for (u32 t = 0; t < rv.ntasks; ++t) {
-    const u64 k = static_cast<u64>(g) * rv.ntasks + t;
-    nc += seg[k].y;
-    nb += seg2[k].z;
-  }
-  for (u32 r = 1; r < rv.rounds; ++r) {
-    const u32 *st = rv.gstart + static_cast<u64>(r - 1) * (rv.ng + 1);
-    for (u32 j = st[g]; j < st[g + 1]; ++j) {
-      nc += seg[rv.base[r] + j].y;
-      nb += seg2[rv.base[r] + j].z;
-    }
-  }
-  ncells[g] = nc;
-  nbodies[g] = nb;
-  const u64 tg = gend[g] - gbegin[g];
-  atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(tg * nc));
-  atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(tg * nb - tg));
-  atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
-  atomicMax(&sc->max_group, static_cast<u32>(tg));
-}
-
-// Copies one item's cells and body runs (warp-cooperative) to the group's lists.
-__device__ __forceinline__ void copy_item(const uint4 &sg, const u32 *reg_cells,
-                                          const uint2 *reg_runs, u32 *cell_list, u32 *body_list,
-                                          u64 &oc, u64 &ob, int lane) {
+// Copies one item's cells and body runs to the group's lists at (oc, ob),
+// all lanes of the warp together.
+__device__ __forceinline__ void copy_item_warp(const uint4 &sg, const u32 *reg_cells,
+                                               const uint2 *reg_runs, u32 *cell_list,
+                                               u32 *body_list, u64 oc, u64 ob, int lane) {
   for (u32 k = lane; k < sg.y; k += 32) cell_list[oc + k] = reg_cells[sg.x + k];
-  oc += sg.y;
   for (u32 k0 = 0; k0 < sg.w; k0 += 32) {
     const u32 k = k0 + lane;
     const uint2 run = k < sg.w ? reg_runs[sg.z + k] : make_uint2(0u, 0u);
@@ -516,22 +491,42 @@ __device__ __forceinline__ void copy_item(const uint4 &sg, const u32 *reg_cells,
   }
 }
 
+__device__ __forceinline__ u32 warp_exclusive_scan(u32 v, int lane) {
+  u32 incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 x = __shfl_up_sync(kFullMask, incl, o);
+    if (lane >= o) incl += x;
+  }
+  return incl - v;
+}
+
+constexpr u32 kSmallItem = 8;  // items with at most this many cells and runs copy by lane
+
 // One warp per group: its items' lists in (round, item) order into the
-// group's ranges of cell_list and body_list, and its GTGroup record.
+// group's ranges of cell_list and body_list, its GTGroup record and the
+// list counters. Each batch of 32 items gets its output offsets from warp
+// scans; small items (most deferred ones: one cell, or a leaf's run) are
+// copied by their own lane, large ones by the whole warp.
 constexpr int kGatherWarps = kT / 32;
 
 __global__ void __launch_bounds__(kT)
-    k_lgather(const uint4 *seg, RoundView rv, const u32 *reg_cells, const uint2 *reg_runs,
-              const u32 *gbegin, const u32 *gend, const u64 *cell_off, const u64 *body_off,
-              u32 *cell_list, u32 *body_list, uint4 *groups) {
+    k_lgather(const uint4 *seg, const uint4 *seg2, RoundView rv, const u32 *reg_cells,
+              const uint2 *reg_runs, const u32 *gbegin, const u32 *gend, const u64 *cell_off,
+              const u64 *body_off, u32 *cell_list, u32 *body_list, uint4 *groups, Scalars *sc) {
   const u32 g = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (g >= rv.ng) return;
   u64 oc = cell_off[g], ob = body_off[g];
   if (lane == 0) {
+    const u64 nc = cell_off[g + 1] - oc, nb = body_off[g + 1] - ob, t = gend[g] - gbegin[g];
     groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(oc),
                                   static_cast<u32>(cell_off[g + 1]));
     groups[2ull * g + 1] = make_uint4(static_cast<u32>(ob), static_cast<u32>(body_off[g + 1]), 0u, 0u);
+    atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
+    atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
+    atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
+    atomicMax(&sc->max_group, static_cast<u32>(t));
   }
   for (u32 r = 0; r < rv.rounds; ++r) {
     u64 first, count;
@@ -544,23 +539,37 @@ __global__ void __launch_bounds__(kT)
       count = st[g + 1] - st[g];
     }
     for (u64 j0 = 0; j0 < count; j0 += 32) {
-      // the next (up to) 32 items of the group, one per lane
       const u64 j = j0 + lane;
-      const uint4 sg = j < count ? seg[first + j] : make_uint4(0u, 0u, 0u, 0u);
-      unsigned busy = __ballot_sync(kFullMask, sg.y != 0 || sg.w != 0);
-      while (busy) {
-        const int src = __ffs(busy) - 1;
-        busy &= busy - 1u;
-        const uint4 s = make_uint4(__shfl_sync(kFullMask, sg.x, src),
-                                   __shfl_sync(kFullMask, sg.y, src),
-                                   __shfl_sync(kFullMask, sg.z, src),
-                                   __shfl_sync(kFullMask, sg.w, src));
-        copy_item(s, reg_cells, reg_runs, cell_list, body_list, oc, ob, lane);
+      const bool have = j < count;
+      const uint4 sg = have ? seg[first + j] : make_uint4(0u, 0u, 0u, 0u);
+      const u32 nbj = have ? seg2[first + j].z : 0u;
+      const u32 cs = warp_exclusive_scan(sg.y, lane), bs = warp_exclusive_scan(nbj, lane);
+      const bool small = sg.y <= kSmallItem && sg.w <= kSmallItem;
+      if (small) {
+        for (u32 k = 0; k < sg.y; ++k) cell_list[oc + cs + k] = reg_cells[sg.x + k];
+        u64 o = ob + bs;
+        for (u32 k = 0; k < sg.w; ++k) {
+          const uint2 run = reg_runs[sg.z + k];
+          for (u32 q = 0; q < run.y; ++q) body_list[o + q] = run.x + q;
+          o += run.y;
+        }
       }
+      unsigned big = __ballot_sync(kFullMask, !small);
+      while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1u;
+        const uint4 s4 = make_uint4(__shfl_sync(kFullMask, sg.x, src),
+                                    __shfl_sync(kFullMask, sg.y, src),
+                                    __shfl_sync(kFullMask, sg.z, src),
+                                    __shfl_sync(kFullMask, sg.w, src));
+        const u32 c_at = __shfl_sync(kFullMask, cs, src), b_at = __shfl_sync(kFullMask, bs, src);
+        copy_item_warp(s4, reg_cells, reg_runs, cell_list, body_list, oc + c_at, ob + b_at, lane);
+      }
+      oc += __shfl_sync(kFullMask, cs + sg.y, 31);
+      ob += __shfl_sync(kFullMask, bs + nbj, 31);
     }
   }
 }
-
 
 // The walk's inference on given raw features (tests and diagnostics).
 __global__ void __launch_bounds__(kT)
@@ -649,6 +658,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   a.band = lw.band;
   a.y_mean = lw.y_mean;
   a.lane_fill = ls.lane_fill.as<u32>();
+  a.gcells = reinterpret_cast<unsigned long long *>(ws.gcells.as<u64>());
+  a.gbodies = reinterpret_cast<unsigned long long *>(ws.gbodies.as<u64>());
   a.sc = sc;
   std::vector<u64> base;
   for (int attempt = 0;; ++attempt) {
@@ -665,6 +676,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
     a.lane_runs = ls.lane_runs;
     a.lane_pend = ls.lane_pend;
     GTC_CUDA(cudaMemsetAsync(a.lane_fill, 0, lanes * 3 * sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(ws.gcells.ptr, 0, static_cast<u64>(ng) * 8, s));
+    GTC_CUDA(cudaMemsetAsync(ws.gbodies.ptr, 0, static_cast<u64>(ng) * 8, s));
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
@@ -761,9 +774,6 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
                            cudaMemcpyHostToDevice, s));
   const RoundView rv{ls.base.as<u64>(), ls.gstart.as<u32>(), rounds, ntasks, ng};
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  k_lsum<<<ceil_div(ng, kT), kT, 0, s>>>(a.seg, a.seg2, rv, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
-                                         ws.gcells.as<u64>(), ws.gbodies.as<u64>(), sc);
-  GTC_LAUNCH_CHECK();
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, ng, cell_off + ng, ws.scan_tmp, s);
   exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, ng, body_off + ng, ws.scan_tmp, s);
   GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + ng, 8, cudaMemcpyDeviceToDevice, s));
@@ -780,8 +790,9 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   k_lgather<<<ceil_div(ng, kGatherWarps), kT, 0, s>>>(
-      a.seg, rv, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(), cell_off,
-      body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>());
+      a.seg, a.seg2, rv, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
+      cell_off, body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>(),
+      sc);
   GTC_LAUNCH_CHECK();
 }
 
