@@ -199,6 +199,170 @@ __global__ void __launch_bounds__(kT)
   }
 }
 
+// The softened quadrupole evaluation (the benchmark configuration) with
+// Blackwell's packed FP32 instructions: each lane works two staged entries
+// at once, one in each half of a float2, so every FFMA2/FMUL2/FADD2 does two
+// interactions' arithmetic and the issue count per interaction halves.
+// Entries are staged as interleaved pairs (x_a, x_b, y_a, y_b, ...), with
+// coordinates and G m negated so that d = p + (-c) is one FADD2; a slot
+// past the list holds a dummy far away with zero mass and quadrupole, which
+// adds exactly zero (its r^2 overflows to inf and rsqrt(inf) = 0). The two
+// halves are summed at the end, so the sum runs over even and odd entries
+// separately before they are added.
+constexpr float kFar = 1.0e30f;
+constexpr int kPairCellF4 = 5;   // float4 per staged cell pair
+constexpr int kPairBodyF4 = 2;   // float4 per staged body pair
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__global__ void __launch_bounds__(kT)
+    k_eval_pairs(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
+                 const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
+                 const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
+                 float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev,
+                 const u32 *abort) {
+  // per warp: slice k's pairs start at float4 k * (pairs * per-pair + 1); the
+  // 16-byte gap puts the slices on different shared-memory banks
+  __shared__ float4 sc[kWarpsPerBlock][84];
+  __shared__ float4 sb[kWarpsPerBlock][36];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (abort && *abort) return;
+  if (ng_dev) ngroups = min(ngroups, *ng_dev);
+  const float2 e2 = f2(eps2, eps2), m25 = f2(-2.5f, -2.5f), mhalf = f2(-0.5f, -0.5f);
+  for (;;) {
+    u32 g = 0;
+    if (lane == 0) g = atomicAdd(next_group, 1u);
+    g = __shfl_sync(kFullMask, g, 0);
+    if (g >= ngroups) return;
+    const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
+    const u32 T = ga.y - ga.x;
+    const u32 ns = T == 0 ? 1u : min(4u, 32u / T);
+    const u32 W = 32u / ns;  // even for every ns
+    const u32 slice = T ? static_cast<u32>(lane) / T : 0u;
+    const u32 t = T ? static_cast<u32>(lane) % T : 0u;
+    const bool computes = slice < ns;
+    const u32 i = ga.x + t;
+    const float4 bi = computes ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 px = f2(bi.x, bi.x), py = f2(bi.y, bi.y), pz = f2(bi.z, bi.z);
+    const u32 stage_slice = static_cast<u32>(lane) / W, stage_pos = static_cast<u32>(lane) % W;
+    const u32 half = stage_pos & 1u, pair = stage_pos >> 1;
+    float2 ax = f2(0.f, 0.f), ay = ax, az = ax, pot = ax;
+
+    {  // cells
+      const u32 cstride = (W / 2) * kPairCellF4 + 1;
+      const u32 e = ga.w - ga.z;
+      const u32 c0 = ga.z + e * stage_slice / ns, c1 = ga.z + e * (stage_slice + 1) / ns;
+      const u32 m0 = ga.z + e * slice / ns, m1 = ga.z + e * (slice + 1) / ns;
+      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
+      for (u32 r = 0; r < rounds; ++r) {
+        if (stage_slice < ns) {
+          const u32 k = c0 + r * W + stage_pos;
+          float v[10];
+          if (k < c1) {
+            const u64 c = cell_list[k];
+            const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
+                         q = __ldg(&cells[3 * c + 2]);
+            v[0] = -a.x; v[1] = -a.y; v[2] = -a.z; v[3] = -G * a.w;
+            v[4] = G * b.x; v[5] = G * b.y; v[6] = G * b.z; v[7] = G * b.w;
+            v[8] = G * q.x; v[9] = G * q.y;
+          } else {
+            v[0] = v[1] = v[2] = -kFar;
+            v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = v[9] = 0.f;
+          }
+          float *f = reinterpret_cast<float *>(&sc[warp][stage_slice * cstride + pair * kPairCellF4]);
+#pragma unroll
+          for (int q = 0; q < 10; ++q) f[2 * q + half] = v[q];
+        }
+        __syncwarp();
+        const u32 base = m0 + r * W;
+        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+        const float4 *mine = &sc[warp][slice * cstride];
+        for (u32 j = 0; j < cnt; j += 2) {
+          const float4 s0 = mine[0], s1 = mine[1], s2 = mine[2], s3 = mine[3], s4 = mine[4];
+          mine += kPairCellF4;
+          // s0 = -cx, -cy  s1 = -cz, -Gm  s2 = Qxx, Qyy  s3 = Qzz, Qxy  s4 = Qxz, Qyz (pairs)
+          const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
+                       dz = __fadd2_rn(pz, f2(s1.x, s1.y));
+          const float2 ngm = f2(s1.z, s1.w);
+          const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+          const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+          const float2 inv2 = __fmul2_rn(inv, inv), inv3 = __fmul2_rn(inv, inv2);
+          const float2 qxx = f2(s2.x, s2.y), qyy = f2(s2.z, s2.w), qzz = f2(s3.x, s3.y),
+                       qxy = f2(s3.z, s3.w), qxz = f2(s4.x, s4.y), qyz = f2(s4.z, s4.w);
+          const float2 qx = __ffma2_rn(qxx, dx, __ffma2_rn(qxy, dy, __fmul2_rn(qxz, dz)));
+          const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
+          const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
+          const float2 rqr = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+          const float2 inv5 = __fmul2_rn(inv3, inv2), inv7 = __fmul2_rn(inv5, inv2);
+          const float2 along = __ffma2_rn(__fmul2_rn(m25, rqr), inv7, __fmul2_rn(ngm, inv3));
+          ax = __ffma2_rn(along, dx, __ffma2_rn(qx, inv5, ax));
+          ay = __ffma2_rn(along, dy, __ffma2_rn(qy, inv5, ay));
+          az = __ffma2_rn(along, dz, __ffma2_rn(qz, inv5, az));
+          pot = __ffma2_rn(ngm, inv, __ffma2_rn(__fmul2_rn(mhalf, rqr), inv5, pot));
+        }
+        __syncwarp();
+      }
+    }
+
+    {  // bodies
+      const u32 bstride = (W / 2) * kPairBodyF4 + 1;
+      const u32 e = gb.y - gb.x;
+      const u32 c0 = gb.x + e * stage_slice / ns, c1 = gb.x + e * (stage_slice + 1) / ns;
+      const u32 m0 = gb.x + e * slice / ns, m1 = gb.x + e * (slice + 1) / ns;
+      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
+      for (u32 r = 0; r < rounds; ++r) {
+        if (stage_slice < ns) {
+          const u32 k = c0 + r * W + stage_pos;
+          float v[4];
+          if (k < c1) {
+            const float4 b = __ldg(&bodies[body_list[k]]);
+            v[0] = -b.x; v[1] = -b.y; v[2] = -b.z; v[3] = -G * b.w;
+          } else {
+            v[0] = v[1] = v[2] = -kFar;
+            v[3] = 0.f;
+          }
+          float *f = reinterpret_cast<float *>(&sb[warp][stage_slice * bstride + pair * kPairBodyF4]);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) f[2 * q + half] = v[q];
+        }
+        __syncwarp();
+        const u32 base = m0 + r * W;
+        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+        const float4 *mine = &sb[warp][slice * bstride];
+        for (u32 j = 0; j < cnt; j += 2) {
+          const float4 s0 = mine[0], s1 = mine[1];
+          mine += kPairBodyF4;
+          const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
+                       dz = __fadd2_rn(pz, f2(s1.x, s1.y));
+          const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+          const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+          const float2 gm = __fmul2_rn(f2(s1.z, s1.w), inv);       // -G m / r
+          const float2 gm3 = __fmul2_rn(gm, __fmul2_rn(inv, inv));  // -G m / r^3
+          ax = __ffma2_rn(gm3, dx, ax);
+          ay = __ffma2_rn(gm3, dy, ay);
+          az = __ffma2_rn(gm3, dz, az);
+          pot = __fadd2_rn(pot, gm);
+        }
+        __syncwarp();
+      }
+    }
+    float sx = ax.x + ax.y, sy = ay.x + ay.y, sz = az.x + az.y, sp = pot.x + pot.y;
+    for (u32 k = 1; k < ns; ++k) {
+      const int src = min(lane + static_cast<int>(k * T), 31);
+      const float ox = __shfl_sync(kFullMask, sx, src), oy = __shfl_sync(kFullMask, sy, src),
+                  oz = __shfl_sync(kFullMask, sz, src), op = __shfl_sync(kFullMask, sp, src);
+      if (slice == 0) {
+        sx += ox;
+        sy += oy;
+        sz += oz;
+        sp += op;
+      }
+    }
+    sp += G * bi.w * rsqrtf(eps2);  // the self term (softened), taken back once
+    if (slice == 0 && t < T) out[i] = make_float4(sx, sy, sz, sp);
+  }
+}
+
 // Tree order -> caller order, FP32 -> FP64 (gravity_backends.cpp:132-136).
 __global__ void __launch_bounds__(256)
     k_scatter(const float4 *out, const u32 *order, u32 n, double *acc, double *pot,
@@ -222,11 +386,19 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<kQuad, kSoft>, kT, 0));
   const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
-  k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
-                                           static_cast<u32>(n_groups), G, eps2, out, counter,
-                                           sc ? &sc->n_groups : nullptr,
-                                           sc ? &sc->abort : nullptr);
+  if (kQuad && kSoft) {
+    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_pairs, kT, 0));
+    const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
+    k_eval_pairs<<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
+                                     static_cast<u32>(n_groups), G, eps2, out, counter,
+                                     sc ? &sc->n_groups : nullptr, sc ? &sc->abort : nullptr);
+  } else {
+    const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
+    k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
+                                             static_cast<u32>(n_groups), G, eps2, out, counter,
+                                             sc ? &sc->n_groups : nullptr,
+                                             sc ? &sc->abort : nullptr);
+  }
   GTC_LAUNCH_CHECK();
 }
 
