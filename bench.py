@@ -64,6 +64,8 @@ def parse():
                     help="skip the learned-criterion measurement")
     ap.add_argument("--only-steps", action="store_true",
                     help="warm-up and timed steps only (for profiler launch lists)")
+    ap.add_argument("--learned-steps", action="store_true",
+                    help="with --only-steps: the learned criterion's warm-up and timed steps")
     return ap.parse_args()
 
 
@@ -279,6 +281,15 @@ def main():
     def step():
         ctx.group_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
                                dpot.data_ptr(), pack=True, **SOLVER)
+
+    if args.only_steps and args.learned_steps:
+        info = json.loads(MODEL_INFO.read_text())
+        ctx.learned_set_model(np.fromfile(MODEL, dtype="<f4"))
+
+        def step():  # noqa: F811  (the learned solver on the same bodies)
+            ctx.group_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                                   dpot.data_ptr(), pack=True, criterion=gtc.CRITERION_LEARNED,
+                                   alpha=float(info["alpha"]), **SOLVER)
 
     for _ in range(max(3, args.warmup)):
         step()

@@ -810,8 +810,8 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;
     } else if (key == "learned_split_depth") {
-      if (value != std::floor(value) || value < 0 || value > 3)
-        throw gtc::InvalidArgument("learned_split_depth must be 0..3");
+      if (value != std::floor(value) || value < 0 || value > 8)
+        throw gtc::InvalidArgument("learned_split_depth must be 0..8");
       ctx->learned_split = static_cast<int>(value);
     } else {
       throw gtc::InvalidArgument("unknown option '" + key + "'");

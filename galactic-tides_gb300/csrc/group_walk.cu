@@ -378,13 +378,16 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
 
   // walk tasks (their count is read back with the group count)
   ws.tasks.ensure(m * sizeof(Task));
-  k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m,
-                                 lw ? lw->split_depth : ws.walk_split_depth, mark);
-  GTC_LAUNCH_CHECK();
-  exclusive_scan_u32(mark, mscan, m, &sc->aux, ws.scan_tmp, s);
-  k_task_fill<<<mb, kT, 0, s>>>(mark, mscan, ws.depth.as<u8>(), ws.parent.as<u32>(), m,
-                                ws.tasks.as<Task>());
-  GTC_LAUNCH_CHECK();
+  // (the learned walk splits each group's walk along its own path instead)
+  if (!lw) {
+    k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, ws.walk_split_depth,
+                                   mark);
+    GTC_LAUNCH_CHECK();
+    exclusive_scan_u32(mark, mscan, m, &sc->aux, ws.scan_tmp, s);
+    k_task_fill<<<mb, kT, 0, s>>>(mark, mscan, ws.depth.as<u8>(), ws.parent.as<u32>(), m,
+                                  ws.tasks.as<Task>());
+    GTC_LAUNCH_CHECK();
+  }
 
   // groups
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
@@ -414,7 +417,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_LAUNCH_CHECK();
   if (lw) {
     learned_group_tolerances(ws, *lw, ng, s);
-    learned_build_lists(ws, *lw, ng, ntasks, host, s);
+    learned_build_lists(ws, *lw, ng, host, s);
     return;
   }
 

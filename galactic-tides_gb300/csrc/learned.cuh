@@ -100,7 +100,7 @@ struct LearnedScratch {
   DeviceBuffer gstart, pcount, poff, base;
   DeviceBuffer q[2], dec[2];        // deferred pairs and the network's decisions
   u64 items_cap = 0;
-  u32 lane_cells = 1024, lane_runs = 256, lane_pend = 256;  // grown when outgrown
+  u32 lane_cells = 2048, lane_runs = 512, lane_pend = 512;  // grown when outgrown
   void release() {
     for (DeviceBuffer *b : {&seg, &regions, &lane_fill, &gstart, &pcount, &poff, &base, &q[0],
                             &q[1], &dec[0], &dec[1]})
@@ -115,7 +115,7 @@ struct LearnedWalk {
   const CellFeat *cfeat = nullptr;  // per node (device)
   DeviceBuffer *gtol = nullptr;     // per group (f0, tolerance), filled by build_lists
   LearnedScratch *scratch = nullptr;
-  int split_depth = 1;              // tasks: the subtrees at this depth
+  int split_depth = 2;              // round 0: each group's walk split along its path this deep
   const float *prev_amag = nullptr; // |a| per body in caller order (device)
   double alpha = 0.02, G = 1.0;
   float inv_theta_guard = 1.f / 1.5f;
@@ -127,11 +127,10 @@ struct LearnedWalk {
 void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s);
 // Per-group group feature and tolerance (inside build_lists, after the group boxes).
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s);
-// The learned walk over ntasks x ng items (ws.tasks holds the task roots),
-// then the gather: GTGroup records, cell_list, body_list and the interaction
+// The learned walk over the groups' path-split items in rounds, then the gather: GTGroup records, cell_list, body_list and the interaction
 // counters of the ng groups (inside build_lists).
-void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntasks,
-                         Scalars *host, cudaStream_t s);
+void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
+                         cudaStream_t s);
 // |a| per body, caller order, from the evaluator's tree-order output.
 void learned_record_amag(const float4 *out, const u32 *order, u64 n, float *amag,
                          cudaStream_t s);

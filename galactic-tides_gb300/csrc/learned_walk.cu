@@ -225,10 +225,14 @@ __device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
   return r;
 }
 
-// The learned walk runs in rounds. Round 0's items are (task, group) pairs:
-// a task is a subtree (the nodes at the split depth, and leaves above it, in
-// node order) and the nodes above the split depth are opened for every
-// group. A walk decides what the guard and the prior settle and defers the
+// The learned walk runs in rounds over items, (group, node) pairs: walk the
+// subtree under the node for the group. Round 0's items split each group's
+// walk along the group's own path from the root: for the path's first
+// `split` levels, every sibling of the path node is an item, and the node
+// the path reaches is the last (the group's near field, its longest walk;
+// it is stored first). Only nodes that hold the group are opened for it on
+// the way down, as the walk itself would, so the decisions are the unsplit
+// walk's. A walk decides what the guard and the prior settle and defers the
 // rest, the (group, cell) pairs whose centred prior lies within the band of
 // the group's tolerance, skipping their subtrees. A dense kernel then runs
 // the network on all deferred pairs at once, 32 rows per warp on the tensor
@@ -240,24 +244,22 @@ __device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
 // Each lane appends what its items produce to its own region: accepted
 // cells, runs of bodies (first, count) and deferred nodes. A gather pass
 // concatenates a group's items in (round, item) order into the group's
-// lists. Item storage is grouped by group: round 0 item (t, g) is stored at
-// g * ntasks + t, and the deferred pairs of a round keep that order.
+// lists. Items are stored grouped by group in every round (a round's
+// deferred pairs keep their items' order), with each group's range kept
+// per round.
 constexpr u64 kNoItem = ~0ull;
 constexpr int kMaxRounds = kMaxDepth + 4;
 
 struct LArgs {
   const WalkRec32 *walk32;
   const CellFeat *cfeat;
-  const uint4 *tasks;      // .x = the task's root node
-  u32 ntasks;
   const float *gboxf;
   const float2 *gtol;
   u32 ng;
-  u32 round;
   u64 nitems;              // items of this round
   u64 item_base;           // global index of the round's first item
-  const uint2 *qitems;     // rounds > 0: (group, node) of each item
-  const u8 *qdec;          // rounds > 0: the network's decision (1: accept)
+  const uint2 *qitems;     // (group, node) of each item
+  const u8 *qdec;          // rounds > 0: the network's decision on the node (1: accept)
   const TreeRoot *root;
   const double2 *mom;
   float inv_theta_guard, band, y_mean;
@@ -305,19 +307,11 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
         } else {
           item = k;
           u32 &g = grp;
-          if (a.round == 0) {
-            const u32 t = static_cast<u32>(k / a.ng);
-            g = static_cast<u32>(k % a.ng);
-            store = static_cast<u64>(g) * a.ntasks + t;
-            i = a.tasks[t].x;
-            pre = -1;
-          } else {
-            const uint2 q = a.qitems[k];
-            g = q.x;
-            i = q.y;
-            store = k;
-            pre = a.qdec[k];
-          }
+          const uint2 q = a.qitems[k];
+          g = q.x;
+          i = q.y;
+          store = k;
+          pre = a.qdec ? a.qdec[k] : -1;
           end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.walk32 + i) + 2).x);
           const float4 b0 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g],
                        b1 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g + 1];
@@ -402,26 +396,65 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
   if (lc > a.lane_cells || lr > a.lane_runs || lp > a.lane_pend) atomicOr(&sc->list_overflow, 1u);
 }
 
-// Start of every group's deferred pairs in the next round's item order
-// (round 0 items of group g start at g * ntasks; later rounds' at the
-// previous round's starts), from the exclusive scan of the deferred counts.
+// Round 0's items of each group (kFill = false: their count): the siblings
+// of the group's path nodes down `split` levels, after the node the path
+// reaches. A path stops early at a leaf or where the group's targets span
+// more than one child.
+constexpr int kMaxSplit = 8;
+
+template <bool kFill>
 __global__ void __launch_bounds__(kT)
-    k_lgstart(u32 round, u32 ng, u32 ntasks, const u32 *poff, const u32 *prev, u32 *out) {
+    k_path_items(const u32 *gbegin, const u32 *gend, u32 ng, const u32 *skip, const u32 *nbegin,
+                 const u32 *nend, const u8 *isleaf, int split, u32 *count, const u32 *offset,
+                 uint2 *items) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= ng) return;
+  const u32 b0 = gbegin[g], b1 = gend[g];
+  u32 path[kMaxSplit + 1];
+  int depth = 0;
+  u32 p = 0;
+  path[0] = 0;
+  while (depth < split && !isleaf[p]) {
+    u32 next = 0xffffffffu;
+    for (u32 c = p + 1; c < skip[p]; c = skip[c])
+      if (nbegin[c] <= b0 && b1 <= nend[c]) next = c;
+    if (next == 0xffffffffu) break;
+    p = next;
+    path[++depth] = p;
+  }
+  if (!kFill) {
+    u32 n = 1;
+    for (int d = 0; d < depth; ++d)
+      for (u32 c = path[d] + 1; c < skip[path[d]]; c = skip[c]) n += c != path[d + 1];
+    count[g] = n;
+    return;
+  }
+  u64 o = offset[g];
+  items[o++] = make_uint2(g, p);  // the near field first
+  for (int d = 0; d < depth; ++d)
+    for (u32 c = path[d] + 1; c < skip[path[d]]; c = skip[c])
+      if (c != path[d + 1]) items[o++] = make_uint2(g, c);
+}
+
+// Start of every group's deferred pairs in the next round's item order,
+// from the exclusive scan of the deferred counts and the starts of the
+// groups' items in this round.
+__global__ void __launch_bounds__(kT)
+    k_lgstart(u32 ng, const u32 *poff, const u32 *cur, u32 *next) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (g > ng) return;
-  const u64 first = round == 0 ? static_cast<u64>(g) * ntasks : prev[g];
-  out[g] = poff[first];
+  next[g] = poff[cur[g]];
 }
 
 // The deferred pairs of a round, in storage order, as the next round's items.
 __global__ void __launch_bounds__(kT)
-    k_lcompact(u32 round, u64 nitems, u64 item_base, u32 ntasks, const uint2 *qitems,
-               const uint4 *seg2, const u32 *poff, const u32 *reg_pend, uint2 *next) {
+    k_lcompact(u64 nitems, u64 item_base, const uint2 *qitems, const uint4 *seg2,
+               const u32 *poff, const u32 *reg_pend, uint2 *next) {
   const u64 j = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
   if (j >= nitems) return;
   const uint4 s2 = seg2[item_base + j];
   if (s2.y == 0) return;
-  const u32 g = round == 0 ? static_cast<u32>(j / ntasks) : qitems[j].x;
+  const u32 g = qitems[j].x;
   const u32 o = poff[j];
   for (u32 m = 0; m < s2.y; ++m) next[o + m] = make_uint2(g, reg_pend[s2.x + m]);
 }
@@ -466,8 +499,8 @@ __global__ void __launch_bounds__(kT)
 
 struct RoundView {
   const u64 *base;         // per round: global index of its first item
-  const u32 *gstart;       // per round r >= 1: [ng + 1] starts of the groups' items
-  u32 rounds, ntasks, ng;
+  const u32 *gstart;       // per round: [ng + 1] starts of the groups' items
+  u32 rounds, ng;
 };
 
 // Copies one item's cells and body runs to the group's lists at (oc, ob),
@@ -529,15 +562,8 @@ __global__ void __launch_bounds__(kT)
     atomicMax(&sc->max_group, static_cast<u32>(t));
   }
   for (u32 r = 0; r < rv.rounds; ++r) {
-    u64 first, count;
-    if (r == 0) {
-      first = static_cast<u64>(g) * rv.ntasks;
-      count = rv.ntasks;
-    } else {
-      const u32 *st = rv.gstart + static_cast<u64>(r - 1) * (rv.ng + 1);
-      first = rv.base[r] + st[g];
-      count = st[g + 1] - st[g];
-    }
+    const u32 *st = rv.gstart + static_cast<u64>(r) * (rv.ng + 1);
+    const u64 first = rv.base[r] + st[g], count = st[g + 1] - st[g];
     for (u64 j0 = 0; j0 < count; j0 += 32) {
       const u64 j = j0 + lane;
       const bool have = j < count;
@@ -626,8 +652,8 @@ void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cuda
   GTC_LAUNCH_CHECK();
 }
 
-void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntasks,
-                         Scalars *host, cudaStream_t s) {
+void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
+                         cudaStream_t s) {
   if (ng == 0) return;
   Scalars *sc = ws.scalars.as<Scalars>();
   int dev = 0, sms = 0, per_sm = 0;
@@ -636,19 +662,17 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lwalk, kT, 0));
   const u32 blocks = static_cast<u32>(std::max(1, sms * std::max(1, per_sm)));
   const u64 lanes = static_cast<u64>(blocks) * kT;
-  const u64 n0 = static_cast<u64>(ng) * ntasks;
   LearnedScratch &ls = *lw.scratch;
+  const int split = std::min(std::max(lw.split_depth, 0), kMaxSplit);
   ws.gcells.ensure(static_cast<u64>(ng) * 8);
   ws.gbodies.ensure(static_cast<u64>(ng) * 8);
   ws.gcell_off.ensure((static_cast<u64>(ng) + 1) * 8);
   ws.gbody_off.ensure((static_cast<u64>(ng) + 1) * 8);
-  ls.gstart.ensure(static_cast<u64>(kMaxRounds) * (ng + 1) * sizeof(u32));
+  ls.gstart.ensure(static_cast<u64>(kMaxRounds + 1) * (ng + 1) * sizeof(u32));
   ls.lane_fill.ensure(lanes * 3 * sizeof(u32));
   LArgs a{};
   a.walk32 = ws.walk32.as<WalkRec32>();
   a.cfeat = lw.cfeat;
-  a.tasks = ws.tasks.as<uint4>();
-  a.ntasks = ntasks;
   a.gboxf = ws.gboxf.as<float>();
   a.gtol = lw.gtol->as<float2>();
   a.ng = ng;
@@ -682,6 +706,22 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
+    // round 0's items: each group's path split
+    u32 *st0 = ls.gstart.as<u32>();
+    ls.pcount.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
+    k_path_items<false><<<ceil_div(ng, kT), kT, 0, s>>>(
+        ws.gbegin.as<u32>(), ws.gend.as<u32>(), ng, ws.skip.as<u32>(), ws.nbegin.as<u32>(),
+        ws.nend.as<u32>(), ws.isleaf.as<u8>(), split, ls.pcount.as<u32>(), nullptr, nullptr);
+    GTC_LAUNCH_CHECK();
+    exclusive_scan_u32(ls.pcount.as<u32>(), st0, ng, st0 + ng, ws.scan_tmp, s);
+    u32 n0 = 0;
+    GTC_CUDA(cudaMemcpyAsync(&n0, st0 + ng, sizeof(u32), cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    ls.q[0].ensure(static_cast<u64>(n0) * sizeof(uint2));
+    k_path_items<true><<<ceil_div(ng, kT), kT, 0, s>>>(
+        ws.gbegin.as<u32>(), ws.gend.as<u32>(), ng, ws.skip.as<u32>(), ws.nbegin.as<u32>(),
+        ws.nend.as<u32>(), ws.isleaf.as<u8>(), split, nullptr, st0, ls.q[0].as<uint2>());
+    GTC_LAUNCH_CHECK();
     base.assign(1, 0);
     u64 nitems = n0, total_items = 0, rows = 0, batches = 0;
     int qsel = 0;
@@ -691,7 +731,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
         throw RuntimeError("learned walk: more rounds than the tree has levels");
       const u64 need = base.back() + nitems;
       if (need > ls.items_cap) {  // grow the item arrays, keeping what is there
-        const u64 cap = std::max<u64>(need + need / 2, n0 + 4ull * ng);
+        const u64 cap = std::max<u64>(need + need / 2, static_cast<u64>(n0) + 4ull * ng);
         DeviceBuffer nseg;
         nseg.ensure(cap * 2 * sizeof(uint4));
         if (ls.items_cap && base.back())
@@ -708,19 +748,17 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
       ls.pcount.ensure((nitems + 1) * sizeof(u32));
       ls.poff.ensure((nitems + 1) * sizeof(u32));
       a.pcount = ls.pcount.as<u32>();
-      a.round = round;
       a.nitems = nitems;
       a.item_base = base.back();
-      a.qitems = round ? ls.q[qsel].as<uint2>() : nullptr;
+      a.qitems = ls.q[qsel].as<uint2>();
       a.qdec = round ? ls.dec[qsel].as<u8>() : nullptr;
       GTC_CUDA(cudaMemsetAsync(&sc->walk_items, 0, sizeof(unsigned long long), s));
       k_lwalk<<<blocks, kT, 0, s>>>(a);
       GTC_LAUNCH_CHECK();
       u32 *poff = ls.poff.as<u32>();
       exclusive_scan_u32(a.pcount, poff, nitems, poff + nitems, ws.scan_tmp, s);
-      u32 *gst = ls.gstart.as<u32>() + static_cast<u64>(round) * (ng + 1);
-      k_lgstart<<<ceil_div(ng + 1, kT), kT, 0, s>>>(
-          round, ng, ntasks, poff, round ? gst - (ng + 1) : nullptr, gst);
+      u32 *cur = ls.gstart.as<u32>() + static_cast<u64>(round) * (ng + 1);
+      k_lgstart<<<ceil_div(ng + 1, kT), kT, 0, s>>>(ng, poff, cur, cur + (ng + 1));
       GTC_LAUNCH_CHECK();
       u32 deferred = 0, flags[2] = {0, 0};
       GTC_CUDA(cudaMemcpyAsync(&deferred, poff + nitems, sizeof(u32), cudaMemcpyDeviceToHost, s));
@@ -740,9 +778,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
       const int nq = qsel ^ 1;
       ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
       ls.dec[nq].ensure(deferred);
-      k_lcompact<<<ceil_div(nitems, kT), kT, 0, s>>>(round, nitems, base.back(), ntasks,
-                                                    a.qitems, a.seg2, poff, a.reg_pend,
-                                                    ls.q[nq].as<uint2>());
+      k_lcompact<<<ceil_div(nitems, kT), kT, 0, s>>>(nitems, base.back(), a.qitems, a.seg2, poff,
+                                                    a.reg_pend, ls.q[nq].as<uint2>());
       GTC_LAUNCH_CHECK();
       k_ldecide<<<ceil_div(deferred, kT), kT, 0, s>>>(
           ls.q[nq].as<uint2>(), deferred, a.walk32, a.cfeat, a.gboxf, a.gtol, lw.net, a.root,
@@ -772,7 +809,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, u32 ntask
   GTC_CUDA(cudaMemcpyAsync(ls.base.ptr, base.data(), rounds * sizeof(u64), cudaMemcpyHostToDevice, s));
   GTC_CUDA(cudaMemcpyAsync(&sc->mlp_rows, &host->mlp_rows, 2 * sizeof(unsigned long long),
                            cudaMemcpyHostToDevice, s));
-  const RoundView rv{ls.base.as<u64>(), ls.gstart.as<u32>(), rounds, ntasks, ng};
+  const RoundView rv{ls.base.as<u64>(), ls.gstart.as<u32>(), rounds, ng};
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, ng, cell_off + ng, ws.scan_tmp, s);
   exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, ng, body_off + ng, ws.scan_tmp, s);
