@@ -3,8 +3,11 @@
 // Each pass: per-tile digit histograms (digit-major, so one exclusive scan
 // gives every tile's output offset per digit), then a scatter in which each
 // warp ranks its keys with __match_any_sync and a warp-private histogram,
-// which keeps equal digits in input order (stability). HBM-bound: one pass reads 8 B of key in
-// the histogram and reads + writes 12 B per pair in the scatter.
+// which keeps equal digits in input order (stability); the tile is put in
+// digit order in shared memory and written out in that order, so that
+// consecutive threads write consecutive places of a digit's run. HBM-bound:
+// one pass reads 8 B of key in the histogram and reads + writes 12 B per
+// pair in the scatter.
 
 #include <utility>
 
@@ -19,6 +22,7 @@ constexpr int kPerLane = 8;                  // keys per lane per tile
 constexpr u32 kTile = kThreads * kPerLane;   // 2048 keys per tile
 constexpr u32 kPerWarp = 32 * kPerLane;      // contiguous keys per warp
 constexpr int kBins = 256;
+static_assert(kThreads == kBins, "the scatter gives each thread one digit");
 
 __global__ void __launch_bounds__(kThreads)
     k_histogram(const u64 *keys, u32 n, int shift, u32 ntiles, u32 *counts) {
@@ -39,6 +43,10 @@ __global__ void __launch_bounds__(kThreads)
               u32 ntiles, const u32 *offsets) {
   __shared__ u32 wh[kWarps][kBins];     // per-warp running counts
   __shared__ u32 woff[kWarps][kBins];   // per-warp start within the tile's digit run
+  __shared__ u32 dstart[kBins];         // start of each digit's run inside the tile
+  __shared__ u32 gout[kBins];           // where each digit's run goes in the output
+  __shared__ u64 skey[kTile];           // the tile, sorted by digit
+  __shared__ u32 sval[kTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int b = lane; b < kBins; b += 32) wh[warp][b] = 0;
   __syncwarp();
@@ -64,7 +72,9 @@ __global__ void __launch_bounds__(kThreads)
     rank[c] = before + __popc(peers & lt);
   }
   __syncthreads();
-  // Start of each warp's run of every digit inside this tile.
+  // Start of each warp's run of every digit inside the digit's run, the
+  // digit runs' starts inside the tile (a block scan over the digits), and
+  // each digit's output position.
   {
     const int d = threadIdx.x;  // kThreads == kBins
     u32 run = 0;
@@ -73,16 +83,42 @@ __global__ void __launch_bounds__(kThreads)
       woff[w][d] = run;
       run += wh[w][d];
     }
+    // exclusive scan of run over the 256 digits: warp scans, then the warp totals
+    u32 incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 v = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += v;
+    }
+    __shared__ u32 wsum[kWarps];
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    u32 before = 0;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    dstart[d] = before + incl - run;
+    gout[d] = offsets[static_cast<u64>(d) * ntiles + blockIdx.x];
   }
   __syncthreads();
+  // the tile in digit order in shared memory
 #pragma unroll
   for (int c = 0; c < kPerLane; ++c) {
     const u64 i = base + static_cast<u64>(c) * 32 + lane;
     if (i >= n) continue;
     const u32 d = static_cast<u32>((key[c] >> shift) & 0xff);
-    const u32 dst = offsets[static_cast<u64>(d) * ntiles + blockIdx.x] + woff[warp][d] + rank[c];
-    keys_out[dst] = key[c];
-    vals_out[dst] = val[c];
+    const u32 local = dstart[d] + woff[warp][d] + rank[c];
+    skey[local] = key[c];
+    sval[local] = val[c];
+  }
+  __syncthreads();
+  // out in order: consecutive threads write consecutive places of a digit's run
+  const u64 tile0 = static_cast<u64>(blockIdx.x) * kTile;
+  const u32 count = static_cast<u32>(n - tile0 < kTile ? n - tile0 : kTile);
+  for (u32 j = threadIdx.x; j < count; j += kThreads) {
+    const u64 k = skey[j];
+    const u32 d = static_cast<u32>((k >> shift) & 0xff);
+    const u32 dst = gout[d] + (j - dstart[d]);
+    keys_out[dst] = k;
+    vals_out[dst] = sval[j];
   }
 }
 
