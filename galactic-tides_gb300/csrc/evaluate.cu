@@ -206,14 +206,40 @@ __global__ void __launch_bounds__(kT)
 // Entries are staged as interleaved pairs (x_a, x_b, y_a, y_b, ...), with
 // coordinates and G m negated so that d = p + (-c) is one FADD2; a slot
 // past the list holds a dummy far away with zero mass and quadrupole, which
-// adds exactly zero (its r^2 overflows to inf and rsqrt(inf) = 0). The two
-// halves are summed at the end, so the sum runs over even and odd entries
-// separately before they are added.
+// adds exactly zero (its r^2 overflows to inf and rsqrt(inf) = 0).
+//
+// Lane fill: a group of T targets splits both lists into ns slices and
+// numbers its (slice k, target t) slots v = k T + t; pass p gives slot
+// 32 p + l to lane l, so ceil(ns T / 32) passes keep nearly every lane busy
+// whatever T is (ns T / 32 lanes' worth of work per pass, against T of 32
+// with one slice). ns is picked per group from the list lengths. A pass
+// holds at most 4 slices (T >= 11: a 32-slot window spans at most
+// floor(31 / T) + 2 of them; T <= 10: one pass of min(4, 32 / T) slices),
+// each staged in its own shared-memory area. After a pass the lanes add
+// their partial sums (even plus odd entries) onto the target's running sum
+// in shared memory, slice by slice in increasing order, so the summation
+// order is fixed.
 constexpr float kFar = 1.0e30f;
 constexpr int kPairCellF4 = 5;   // float4 per staged cell pair
 constexpr int kPairBodyF4 = 2;   // float4 per staged body pair
+constexpr u32 kMaxSlices = 16;   // slices per group at most
+constexpr u32 kPassCost = 8;     // a pass's fixed cost, in staged entries per lane
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+__device__ __forceinline__ u32 even_up(u32 x) { return (x + 1u) & ~1u; }
+
+// Slices for a group of T targets with ec cells and eb bodies (warp-uniform):
+// the ns in 1..16 that minimises passes x (pair steps per pass + kPassCost).
+__device__ __forceinline__ u32 choose_slices(u32 T, u32 ec, u32 eb, int lane) {
+  if (T <= 10) return T == 0 ? 1u : min(4u, 32u / T);
+  const u32 ns = static_cast<u32>(lane) % kMaxSlices + 1u;
+  const u32 passes = (ns * T + 31u) / 32u;
+  const u64 cost = static_cast<u64>(passes) *
+                   (even_up((ec + ns - 1) / ns) + even_up((eb + ns - 1) / ns) + kPassCost);
+  const u32 key = static_cast<u32>(cost < (1ull << 27) ? cost : (1ull << 27) - 1) << 4 | (ns - 1u);
+  return (__reduce_min_sync(kFullMask, key) & 15u) + 1u;
+}
 
 __global__ void __launch_bounds__(kT)
     k_eval_pairs(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
@@ -221,10 +247,12 @@ __global__ void __launch_bounds__(kT)
                  const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
                  float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev,
                  const u32 *abort) {
-  // per warp: slice k's pairs start at float4 k * (pairs * per-pair + 1); the
-  // 16-byte gap puts the slices on different shared-memory banks
+  // per warp, staged pairs: area a starts at float4 a * (pairs * per-pair + 1)
+  // (at most 4 areas: 84 and 36 float4); the 16-byte gap puts the areas on
+  // different shared-memory banks
   __shared__ float4 sc[kWarpsPerBlock][84];
   __shared__ float4 sb[kWarpsPerBlock][36];
+  __shared__ float4 sacc[kWarpsPerBlock][32];  // per target: a and potential
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (abort && *abort) return;
   if (ng_dev) ngroups = min(ngroups, *ng_dev);
@@ -236,130 +264,147 @@ __global__ void __launch_bounds__(kT)
     if (g >= ngroups) return;
     const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
     const u32 T = ga.y - ga.x;
-    const u32 ns = T == 0 ? 1u : min(4u, 32u / T);
-    const u32 W = 32u / ns;  // even for every ns
-    const u32 slice = T ? static_cast<u32>(lane) / T : 0u;
-    const u32 t = T ? static_cast<u32>(lane) % T : 0u;
-    const bool computes = slice < ns;
-    const u32 i = ga.x + t;
-    const float4 bi = computes ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float2 px = f2(bi.x, bi.x), py = f2(bi.y, bi.y), pz = f2(bi.z, bi.z);
-    const u32 stage_slice = static_cast<u32>(lane) / W, stage_pos = static_cast<u32>(lane) % W;
-    const u32 half = stage_pos & 1u, pair = stage_pos >> 1;
-    float2 ax = f2(0.f, 0.f), ay = ax, az = ax, pot = ax;
+    if (T == 0) continue;
+    const u32 ec = ga.w - ga.z, eb = gb.y - gb.x;
+    const u32 ns = choose_slices(T, ec, eb, lane);
+    const u32 slots = ns * T;
+    const u32 passes = (slots + 31u) / 32u;
+    if (static_cast<u32>(lane) < T) sacc[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
 
-    {  // cells
-      const u32 cstride = (W / 2) * kPairCellF4 + 1;
-      const u32 e = ga.w - ga.z;
-      const u32 c0 = ga.z + e * stage_slice / ns, c1 = ga.z + e * (stage_slice + 1) / ns;
-      const u32 m0 = ga.z + e * slice / ns, m1 = ga.z + e * (slice + 1) / ns;
-      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
-      for (u32 r = 0; r < rounds; ++r) {
-        if (stage_slice < ns) {
-          const u32 k = c0 + r * W + stage_pos;
-          float v[10];
-          if (k < c1) {
-            const u64 c = cell_list[k];
-            const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
-                         q = __ldg(&cells[3 * c + 2]);
-            v[0] = -a.x; v[1] = -a.y; v[2] = -a.z; v[3] = -G * a.w;
-            v[4] = G * b.x; v[5] = G * b.y; v[6] = G * b.z; v[7] = G * b.w;
-            v[8] = G * q.x; v[9] = G * q.y;
-          } else {
-            v[0] = v[1] = v[2] = -kFar;
-            v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = v[9] = 0.f;
-          }
-          float *f = reinterpret_cast<float *>(&sc[warp][stage_slice * cstride + pair * kPairCellF4]);
-#pragma unroll
-          for (int q = 0; q < 10; ++q) f[2 * q + half] = v[q];
-        }
-        __syncwarp();
-        const u32 base = m0 + r * W;
-        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
-        const float4 *mine = &sc[warp][slice * cstride];
-        for (u32 j = 0; j < cnt; j += 2) {
-          const float4 s0 = mine[0], s1 = mine[1], s2 = mine[2], s3 = mine[3], s4 = mine[4];
-          mine += kPairCellF4;
-          // s0 = -cx, -cy  s1 = -cz, -Gm  s2 = Qxx, Qyy  s3 = Qzz, Qxy  s4 = Qxz, Qyz (pairs)
-          const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
-                       dz = __fadd2_rn(pz, f2(s1.x, s1.y));
-          const float2 ngm = f2(s1.z, s1.w);
-          const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-          const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
-          const float2 inv2 = __fmul2_rn(inv, inv), inv3 = __fmul2_rn(inv, inv2);
-          const float2 qxx = f2(s2.x, s2.y), qyy = f2(s2.z, s2.w), qzz = f2(s3.x, s3.y),
-                       qxy = f2(s3.z, s3.w), qxz = f2(s4.x, s4.y), qyz = f2(s4.z, s4.w);
-          const float2 qx = __ffma2_rn(qxx, dx, __ffma2_rn(qxy, dy, __fmul2_rn(qxz, dz)));
-          const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
-          const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
-          const float2 rqr = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
-          const float2 inv5 = __fmul2_rn(inv3, inv2), inv7 = __fmul2_rn(inv5, inv2);
-          const float2 along = __ffma2_rn(__fmul2_rn(m25, rqr), inv7, __fmul2_rn(ngm, inv3));
-          ax = __ffma2_rn(along, dx, __ffma2_rn(qx, inv5, ax));
-          ay = __ffma2_rn(along, dy, __ffma2_rn(qy, inv5, ay));
-          az = __ffma2_rn(along, dz, __ffma2_rn(qz, inv5, az));
-          pot = __ffma2_rn(ngm, inv, __ffma2_rn(__fmul2_rn(mhalf, rqr), inv5, pot));
-        }
-        __syncwarp();
-      }
-    }
+    for (u32 p = 0; p < passes; ++p) {
+      const u32 v = 32u * p + static_cast<u32>(lane);
+      const bool computes = v < slots;
+      const u32 slice = v / T, t = v % T;
+      const u32 k_lo = (32u * p) / T;
+      const u32 nsp = min(ns - 1u, (32u * p + 31u) / T) - k_lo + 1u;  // 1..4
+      const u32 W = nsp == 1u ? 32u : (nsp == 2u ? 16u : (nsp == 3u ? 10u : 8u));
+      const u32 area = slice - k_lo;
+      const u32 stage_area = static_cast<u32>(lane) / W, stage_pos = static_cast<u32>(lane) % W;
+      const u32 stage_slice = k_lo + stage_area;
+      const bool stages = stage_area < nsp;
+      const u32 half = stage_pos & 1u, pair = stage_pos >> 1;
+      const float4 bi = computes ? bodies[ga.x + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float2 px = f2(bi.x, bi.x), py = f2(bi.y, bi.y), pz = f2(bi.z, bi.z);
+      float2 ax = f2(0.f, 0.f), ay = ax, az = ax, pot = ax;
 
-    {  // bodies
-      const u32 bstride = (W / 2) * kPairBodyF4 + 1;
-      const u32 e = gb.y - gb.x;
-      const u32 c0 = gb.x + e * stage_slice / ns, c1 = gb.x + e * (stage_slice + 1) / ns;
-      const u32 m0 = gb.x + e * slice / ns, m1 = gb.x + e * (slice + 1) / ns;
-      const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
-      for (u32 r = 0; r < rounds; ++r) {
-        if (stage_slice < ns) {
-          const u32 k = c0 + r * W + stage_pos;
-          float v[4];
-          if (k < c1) {
-            const float4 b = __ldg(&bodies[body_list[k]]);
-            v[0] = -b.x; v[1] = -b.y; v[2] = -b.z; v[3] = -G * b.w;
-          } else {
-            v[0] = v[1] = v[2] = -kFar;
-            v[3] = 0.f;
-          }
-          float *f = reinterpret_cast<float *>(&sb[warp][stage_slice * bstride + pair * kPairBodyF4]);
+      {  // cells
+        const u32 cstride = (W / 2) * kPairCellF4 + 1;
+        const u32 c0 = ga.z + ec * stage_slice / ns, c1 = ga.z + ec * (stage_slice + 1) / ns;
+        const u32 m0 = ga.z + ec * slice / ns, m1 = ga.z + ec * (slice + 1) / ns;
+        const u32 rounds = ((ec + ns - 1) / ns + W - 1) / W;
+        for (u32 r = 0; r < rounds; ++r) {
+          if (stages) {
+            const u32 k = c0 + r * W + stage_pos;
+            float v[10];
+            if (k < c1) {
+              const u64 c = cell_list[k];
+              const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
+                           q = __ldg(&cells[3 * c + 2]);
+              v[0] = -a.x; v[1] = -a.y; v[2] = -a.z; v[3] = -G * a.w;
+              v[4] = G * b.x; v[5] = G * b.y; v[6] = G * b.z; v[7] = G * b.w;
+              v[8] = G * q.x; v[9] = G * q.y;
+            } else {
+              v[0] = v[1] = v[2] = -kFar;
+              v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = v[9] = 0.f;
+            }
+            float *f =
+                reinterpret_cast<float *>(&sc[warp][stage_area * cstride + pair * kPairCellF4]);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) f[2 * q + half] = v[q];
+            for (int q = 0; q < 10; ++q) f[2 * q + half] = v[q];
+          }
+          __syncwarp();
+          const u32 base = m0 + r * W;
+          const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+          const float4 *mine = &sc[warp][area * cstride];
+          for (u32 j = 0; j < cnt; j += 2) {
+            const float4 s0 = mine[0], s1 = mine[1], s2 = mine[2], s3 = mine[3], s4 = mine[4];
+            mine += kPairCellF4;
+            // s0 = -cx, -cy  s1 = -cz, -Gm  s2 = Qxx, Qyy  s3 = Qzz, Qxy  s4 = Qxz, Qyz (pairs)
+            const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
+                         dz = __fadd2_rn(pz, f2(s1.x, s1.y));
+            const float2 ngm = f2(s1.z, s1.w);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+            const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 inv2 = __fmul2_rn(inv, inv), inv3 = __fmul2_rn(inv, inv2);
+            const float2 qxx = f2(s2.x, s2.y), qyy = f2(s2.z, s2.w), qzz = f2(s3.x, s3.y),
+                         qxy = f2(s3.z, s3.w), qxz = f2(s4.x, s4.y), qyz = f2(s4.z, s4.w);
+            const float2 qx = __ffma2_rn(qxx, dx, __ffma2_rn(qxy, dy, __fmul2_rn(qxz, dz)));
+            const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
+            const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
+            const float2 rqr = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+            const float2 inv5 = __fmul2_rn(inv3, inv2), inv7 = __fmul2_rn(inv5, inv2);
+            const float2 along = __ffma2_rn(__fmul2_rn(m25, rqr), inv7, __fmul2_rn(ngm, inv3));
+            ax = __ffma2_rn(along, dx, __ffma2_rn(qx, inv5, ax));
+            ay = __ffma2_rn(along, dy, __ffma2_rn(qy, inv5, ay));
+            az = __ffma2_rn(along, dz, __ffma2_rn(qz, inv5, az));
+            pot = __ffma2_rn(ngm, inv, __ffma2_rn(__fmul2_rn(mhalf, rqr), inv5, pot));
+          }
+          __syncwarp();
         }
-        __syncwarp();
-        const u32 base = m0 + r * W;
-        const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
-        const float4 *mine = &sb[warp][slice * bstride];
-        for (u32 j = 0; j < cnt; j += 2) {
-          const float4 s0 = mine[0], s1 = mine[1];
-          mine += kPairBodyF4;
-          const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
-                       dz = __fadd2_rn(pz, f2(s1.x, s1.y));
-          const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-          const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
-          const float2 gm = __fmul2_rn(f2(s1.z, s1.w), inv);       // -G m / r
-          const float2 gm3 = __fmul2_rn(gm, __fmul2_rn(inv, inv));  // -G m / r^3
-          ax = __ffma2_rn(gm3, dx, ax);
-          ay = __ffma2_rn(gm3, dy, ay);
-          az = __ffma2_rn(gm3, dz, az);
-          pot = __fadd2_rn(pot, gm);
+      }
+
+      {  // bodies
+        const u32 bstride = (W / 2) * kPairBodyF4 + 1;
+        const u32 c0 = gb.x + eb * stage_slice / ns, c1 = gb.x + eb * (stage_slice + 1) / ns;
+        const u32 m0 = gb.x + eb * slice / ns, m1 = gb.x + eb * (slice + 1) / ns;
+        const u32 rounds = ((eb + ns - 1) / ns + W - 1) / W;
+        for (u32 r = 0; r < rounds; ++r) {
+          if (stages) {
+            const u32 k = c0 + r * W + stage_pos;
+            float v[4];
+            if (k < c1) {
+              const float4 b = __ldg(&bodies[body_list[k]]);
+              v[0] = -b.x; v[1] = -b.y; v[2] = -b.z; v[3] = -G * b.w;
+            } else {
+              v[0] = v[1] = v[2] = -kFar;
+              v[3] = 0.f;
+            }
+            float *f =
+                reinterpret_cast<float *>(&sb[warp][stage_area * bstride + pair * kPairBodyF4]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) f[2 * q + half] = v[q];
+          }
+          __syncwarp();
+          const u32 base = m0 + r * W;
+          const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+          const float4 *mine = &sb[warp][area * bstride];
+          for (u32 j = 0; j < cnt; j += 2) {
+            const float4 s0 = mine[0], s1 = mine[1];
+            mine += kPairBodyF4;
+            const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
+                         dz = __fadd2_rn(pz, f2(s1.x, s1.y));
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+            const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 gm = __fmul2_rn(f2(s1.z, s1.w), inv);       // -G m / r
+            const float2 gm3 = __fmul2_rn(gm, __fmul2_rn(inv, inv));  // -G m / r^3
+            ax = __ffma2_rn(gm3, dx, ax);
+            ay = __ffma2_rn(gm3, dy, ay);
+            az = __ffma2_rn(gm3, dz, az);
+            pot = __fadd2_rn(pot, gm);
+          }
+          __syncwarp();
+        }
+      }
+      // this pass's partial sums onto the targets', slice by slice
+      const float sx = ax.x + ax.y, sy = ay.x + ay.y, sz = az.x + az.y, sp = pot.x + pot.y;
+      for (u32 a = 0; a < nsp; ++a) {
+        if (computes && area == a) {
+          float4 &acc = sacc[warp][t];
+          acc.x += sx;
+          acc.y += sy;
+          acc.z += sz;
+          acc.w += sp;
         }
         __syncwarp();
       }
     }
-    float sx = ax.x + ax.y, sy = ay.x + ay.y, sz = az.x + az.y, sp = pot.x + pot.y;
-    for (u32 k = 1; k < ns; ++k) {
-      const int src = min(lane + static_cast<int>(k * T), 31);
-      const float ox = __shfl_sync(kFullMask, sx, src), oy = __shfl_sync(kFullMask, sy, src),
-                  oz = __shfl_sync(kFullMask, sz, src), op = __shfl_sync(kFullMask, sp, src);
-      if (slice == 0) {
-        sx += ox;
-        sy += oy;
-        sz += oz;
-        sp += op;
-      }
+    if (static_cast<u32>(lane) < T) {
+      const u32 i = ga.x + static_cast<u32>(lane);
+      float4 acc = sacc[warp][lane];
+      acc.w += G * bodies[i].w * rsqrtf(eps2);  // the self term (softened), taken back once
+      out[i] = acc;
     }
-    sp += G * bi.w * rsqrtf(eps2);  // the self term (softened), taken back once
-    if (slice == 0 && t < T) out[i] = make_float4(sx, sy, sz, sp);
   }
 }
 
