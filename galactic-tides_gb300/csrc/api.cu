@@ -328,6 +328,7 @@ struct GraphStep {
     ws.n_groups = hs.n_groups;
     ws.n_cell_list = hs.n_cell_list;
     ws.n_body_list = hs.n_body_list;
+    ws.gapped = false;
     gtc_stats &st = ctx->stats;
     const u32 replays = st.graph_steps;
     st = gtc_stats{};
@@ -690,6 +691,7 @@ gtc_status gtc_tree(gtc_context *ctx, const gtc_float4 *bodies, const gtc_cell *
     GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));
     ctx->have_group = false;
+    ws.gapped = false;
     ctx->stats = gtc_stats{};
     ctx->stats.evaluate_ms = elapsed(ctx->ev[2], ctx->ev[3]);
     ctx->stats.total_ms = ctx->stats.evaluate_ms;
@@ -1266,9 +1268,42 @@ gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
     }
     get(bodies, ws.bodies, n * 16);
     get(cells, ws.cells, m * 48);
-    get(groups, ws.groups, ws.n_groups * 32);
-    get(cell_list, ws.cell_list, ws.n_cell_list * 4);
-    get(body_list, ws.body_list, ws.n_body_list * 4);
+    if (ws.gapped && (groups || cell_list || body_list)) {
+      // one-pass lists sit in per-group slots: exported back to back
+      const u64 ng = ws.n_groups;
+      std::vector<uint4> rec(2 * ng);
+      get(rec.data(), ws.groups, ng * 32);
+      u64 cext = 0, bext = 0;
+      for (u64 g = 0; g < ng; ++g) {
+        cext = std::max<u64>(cext, rec[2 * g].w);
+        bext = std::max<u64>(bext, rec[2 * g + 1].y);
+      }
+      std::vector<u32> cl(cell_list ? cext : 0), bl(body_list ? bext : 0);
+      get(cl.data(), ws.cell_list, cl.size() * 4);
+      get(bl.data(), ws.body_list, bl.size() * 4);
+      u64 c = 0, b = 0;
+      for (u64 g = 0; g < ng; ++g) {
+        const uint4 ra = rec[2 * g], rb = rec[2 * g + 1];
+        if (cell_list) std::copy(cl.begin() + ra.z, cl.begin() + ra.w, cell_list + c);
+        if (body_list) std::copy(bl.begin() + rb.x, bl.begin() + rb.y, body_list + b);
+        if (groups) {
+          gtc_group &o = groups[g];
+          o.begin = ra.x;
+          o.end = ra.y;
+          o.cell_begin = static_cast<uint32_t>(c);
+          o.cell_end = static_cast<uint32_t>(c + (ra.w - ra.z));
+          o.body_begin = static_cast<uint32_t>(b);
+          o.body_end = static_cast<uint32_t>(b + (rb.y - rb.x));
+          o.pad0 = o.pad1 = 0;
+        }
+        c += ra.w - ra.z;
+        b += rb.y - rb.x;
+      }
+    } else {
+      get(groups, ws.groups, ws.n_groups * 32);
+      get(cell_list, ws.cell_list, ws.n_cell_list * 4);
+      get(body_list, ws.body_list, ws.n_body_list * 4);
+    }
     get(out, ws.out, n * 16);
   });
 }

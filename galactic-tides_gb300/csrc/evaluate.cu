@@ -247,11 +247,12 @@ __global__ void __launch_bounds__(kT)
                  const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
                  float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev,
                  const u32 *abort) {
-  // per warp, staged pairs: area a starts at float4 a * (pairs * per-pair + 1)
-  // (at most 4 areas: 84 and 36 float4); the 16-byte gap puts the areas on
-  // different shared-memory banks
-  __shared__ float4 sc[kWarpsPerBlock][84];
-  __shared__ float4 sb[kWarpsPerBlock][36];
+  // per warp, staged pairs: each lane stages two entries per round, so area
+  // a (2W entries) starts at float4 a * (W * per-pair + 1) (at most 4 areas:
+  // 164 and 68 float4); the 16-byte gap puts the areas on different
+  // shared-memory banks
+  __shared__ float4 sc[kWarpsPerBlock][164];
+  __shared__ float4 sb[kWarpsPerBlock][68];
   __shared__ float4 sacc[kWarpsPerBlock][32];  // per target: a and potential
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (abort && *abort) return;
@@ -289,33 +290,40 @@ __global__ void __launch_bounds__(kT)
       float2 ax = f2(0.f, 0.f), ay = ax, az = ax, pot = ax;
 
       {  // cells
-        const u32 cstride = (W / 2) * kPairCellF4 + 1;
+        const u32 cstride = W * kPairCellF4 + 1;
         const u32 c0 = ga.z + ec * stage_slice / ns, c1 = ga.z + ec * (stage_slice + 1) / ns;
         const u32 m0 = ga.z + ec * slice / ns, m1 = ga.z + ec * (slice + 1) / ns;
-        const u32 rounds = ((ec + ns - 1) / ns + W - 1) / W;
+        const u32 rounds = ((ec + ns - 1) / ns + 2 * W - 1) / (2 * W);
         for (u32 r = 0; r < rounds; ++r) {
           if (stages) {
-            const u32 k = c0 + r * W + stage_pos;
-            float v[10];
-            if (k < c1) {
-              const u64 c = cell_list[k];
-              const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
-                           q = __ldg(&cells[3 * c + 2]);
-              v[0] = -a.x; v[1] = -a.y; v[2] = -a.z; v[3] = -G * a.w;
-              v[4] = G * b.x; v[5] = G * b.y; v[6] = G * b.z; v[7] = G * b.w;
-              v[8] = G * q.x; v[9] = G * q.y;
-            } else {
-              v[0] = v[1] = v[2] = -kFar;
-              v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = v[9] = 0.f;
-            }
-            float *f =
-                reinterpret_cast<float *>(&sc[warp][stage_area * cstride + pair * kPairCellF4]);
+            // two entries per lane: positions stage_pos and stage_pos + W
+            float v[2][10];
 #pragma unroll
-            for (int q = 0; q < 10; ++q) f[2 * q + half] = v[q];
+            for (int h = 0; h < 2; ++h) {
+              const u32 k = c0 + 2 * r * W + h * W + stage_pos;
+              if (k < c1) {
+                const u64 c = cell_list[k];
+                const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
+                             q = __ldg(&cells[3 * c + 2]);
+                v[h][0] = -a.x; v[h][1] = -a.y; v[h][2] = -a.z; v[h][3] = -G * a.w;
+                v[h][4] = G * b.x; v[h][5] = G * b.y; v[h][6] = G * b.z; v[h][7] = G * b.w;
+                v[h][8] = G * q.x; v[h][9] = G * q.y;
+              } else {
+                v[h][0] = v[h][1] = v[h][2] = -kFar;
+                v[h][3] = v[h][4] = v[h][5] = v[h][6] = v[h][7] = v[h][8] = v[h][9] = 0.f;
+              }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              float *f = reinterpret_cast<float *>(
+                  &sc[warp][stage_area * cstride + (pair + h * (W / 2)) * kPairCellF4]);
+#pragma unroll
+              for (int q = 0; q < 10; ++q) f[2 * q + half] = v[h][q];
+            }
           }
           __syncwarp();
-          const u32 base = m0 + r * W;
-          const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+          const u32 base = m0 + 2 * r * W;
+          const u32 cnt = computes && base < m1 ? min(2 * W, m1 - base) : 0u;
           const float4 *mine = &sc[warp][area * cstride];
           for (u32 j = 0; j < cnt; j += 2) {
             const float4 s0 = mine[0], s1 = mine[1], s2 = mine[2], s3 = mine[3], s4 = mine[4];
@@ -345,29 +353,35 @@ __global__ void __launch_bounds__(kT)
       }
 
       {  // bodies
-        const u32 bstride = (W / 2) * kPairBodyF4 + 1;
+        const u32 bstride = W * kPairBodyF4 + 1;
         const u32 c0 = gb.x + eb * stage_slice / ns, c1 = gb.x + eb * (stage_slice + 1) / ns;
         const u32 m0 = gb.x + eb * slice / ns, m1 = gb.x + eb * (slice + 1) / ns;
-        const u32 rounds = ((eb + ns - 1) / ns + W - 1) / W;
+        const u32 rounds = ((eb + ns - 1) / ns + 2 * W - 1) / (2 * W);
         for (u32 r = 0; r < rounds; ++r) {
           if (stages) {
-            const u32 k = c0 + r * W + stage_pos;
-            float v[4];
-            if (k < c1) {
-              const float4 b = __ldg(&bodies[body_list[k]]);
-              v[0] = -b.x; v[1] = -b.y; v[2] = -b.z; v[3] = -G * b.w;
-            } else {
-              v[0] = v[1] = v[2] = -kFar;
-              v[3] = 0.f;
-            }
-            float *f =
-                reinterpret_cast<float *>(&sb[warp][stage_area * bstride + pair * kPairBodyF4]);
+            float v[2][4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) f[2 * q + half] = v[q];
+            for (int h = 0; h < 2; ++h) {
+              const u32 k = c0 + 2 * r * W + h * W + stage_pos;
+              if (k < c1) {
+                const float4 b = __ldg(&bodies[body_list[k]]);
+                v[h][0] = -b.x; v[h][1] = -b.y; v[h][2] = -b.z; v[h][3] = -G * b.w;
+              } else {
+                v[h][0] = v[h][1] = v[h][2] = -kFar;
+                v[h][3] = 0.f;
+              }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              float *f = reinterpret_cast<float *>(
+                  &sb[warp][stage_area * bstride + (pair + h * (W / 2)) * kPairBodyF4]);
+#pragma unroll
+              for (int q = 0; q < 4; ++q) f[2 * q + half] = v[h][q];
+            }
           }
           __syncwarp();
-          const u32 base = m0 + r * W;
-          const u32 cnt = computes && base < m1 ? min(W, m1 - base) : 0u;
+          const u32 base = m0 + 2 * r * W;
+          const u32 cnt = computes && base < m1 ? min(2 * W, m1 - base) : 0u;
           const float4 *mine = &sb[warp][area * bstride];
           for (u32 j = 0; j < cnt; j += 2) {
             const float4 s0 = mine[0], s1 = mine[1];

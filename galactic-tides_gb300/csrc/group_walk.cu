@@ -16,7 +16,10 @@
 // (the order the reference's stack pops them): accept -> record and jump to
 // the node's skip link, leaf -> record its bodies and jump, otherwise step
 // to the next node (its last child). A counting pass sizes the lists; after
-// the offsets are scanned a second pass writes them.
+// the offsets are scanned a second pass writes them. Once a walk has
+// measured the longest lists, later walks run once, writing each group's
+// lists into fixed per-group slots (a quarter larger), and fall back to the
+// two passes when a list outgrows its slot.
 
 #include <algorithm>
 
@@ -225,10 +228,16 @@ struct Task {
 constexpr u32 kNone = 0xffffffffu;
 
 struct WalkOut {
-  u64 *ncells, *nbodies;          // count pass, [group * ntasks + task]
+  u64 *ncells, *nbodies;          // count and one-pass walks, [group * ntasks + task]
   const u64 *cell_off, *body_off; // fill pass, same indexing
   u32 *cell_list, *body_list;
+  u32 slot_cells, slot_bodies;    // one-pass walk: each group's capacities
 };
+
+// Walk modes: count the lists; write them at scanned offsets; or both in
+// one pass into fixed per-group slots (one task per group), flagging a
+// list that outgrows its slot.
+constexpr int kCount = 0, kFill = 1, kSlots = 2;
 
 __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk64, u32 i,
                                       const float *gf, const float *hf, float gbound,
@@ -246,7 +255,7 @@ __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk6
   return verdict;
 }
 
-template <bool kFill>
+template <int kMode>
 __global__ void __launch_bounds__(kT)
     k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
            const float *gboxf, u32 ng_cap, const Task *tasks, u32 ntasks, WalkOut out,
@@ -263,20 +272,25 @@ __global__ void __launch_bounds__(kT)
   const float gf[3] = {b0.x, b0.y, b0.z}, hf[3] = {b0.w, b1.x, b1.y};
   const float gbound = b1.z;
   u32 *cl = nullptr, *bl = nullptr;
-  if (kFill) {
+  if (kMode == kFill) {
     cl = out.cell_list + out.cell_off[slot];
     bl = out.body_list + out.body_off[slot];
+  } else if (kMode == kSlots) {
+    cl = out.cell_list + static_cast<u64>(g) * out.slot_cells;
+    bl = out.body_list + static_cast<u64>(g) * out.slot_bodies;
   }
   u32 nc = 0, nb = 0, exact = 0;
   const Task task = tasks[t];
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
     if (verdict == 1 && nbody > kFewBodies) {
-      if (kFill) cl[nc] = i;
+      if (kMode == kFill || (kMode == kSlots && nc < out.slot_cells)) cl[nc] = i;
       ++nc;
     } else {
-      if (kFill)
+      if (kMode == kFill)
         for (u32 j = 0; j < nbody; ++j) bl[nb + j] = r.begin + j;
+      if (kMode == kSlots)
+        for (u32 j = 0; j < nbody && nb + j < out.slot_bodies; ++j) bl[nb + j] = r.begin + j;
       nb += nbody;
     }
   };
@@ -306,11 +320,13 @@ __global__ void __launch_bounds__(kT)
       }
     }
   }
-  if (!kFill) {
+  if (kMode != kFill) {
     out.ncells[slot] = nc;
     out.nbodies[slot] = nb;
     if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
   }
+  if (kMode == kSlots && (nc > out.slot_cells || nb > out.slot_bodies))
+    atomicOr(&sc->list_overflow, 1u);
 }
 
 // Walk tasks: nodes at depth `split` (0..2), and leaves above it, in node
@@ -337,6 +353,15 @@ __global__ void __launch_bounds__(kT)
 }
 
 // GTGroup records from the per-task offsets, and the list counters.
+__device__ __forceinline__ void group_stats(Scalars *sc, u64 t, u64 nc, u64 nb) {
+  atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
+  atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
+  atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
+  atomicMax(&sc->max_group, static_cast<u32>(t));
+  atomicMax(&sc->max_cells, static_cast<u32>(nc < 0xffffffffull ? nc : 0xffffffffull));
+  atomicMax(&sc->max_bodies, static_cast<u32>(nb < 0xffffffffull ? nb : 0xffffffffull));
+}
+
 __global__ void __launch_bounds__(kT)
     k_group_records(const u32 *gbegin, const u32 *gend, u32 ng, u32 ntasks, const u64 *cell_off,
                     const u64 *body_off, uint4 *groups, Scalars *sc,
@@ -349,11 +374,26 @@ __global__ void __launch_bounds__(kT)
             b1 = body_off[static_cast<u64>(g + 1) * ntasks];
   groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c1));
   groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b1), 0u, 0u);
-  const u64 t = gend[g] - gbegin[g], nc = c1 - c0, nb = b1 - b0;
-  atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
-  atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
-  atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
-  atomicMax(&sc->max_group, static_cast<u32>(t));
+  group_stats(sc, gend[g] - gbegin[g], c1 - c0, b1 - b0);
+}
+
+// Group records of a one-pass walk: group g's lists start at its slots.
+__global__ void __launch_bounds__(kT)
+    k_slot_records(const u32 *gbegin, const u32 *gend, u32 ng, const u64 *ncells,
+                   const u64 *nbodies, u32 slot_cells, u32 slot_bodies, uint4 *groups,
+                   Scalars *sc) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= ng) return;
+  const u64 nc = ncells[g], nb = nbodies[g];
+  const u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
+  const u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
+  groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c0 + kc));
+  groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + kb), 0u, 0u);
+  group_stats(sc, gend[g] - gbegin[g], nc, nb);
+  atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_cell_list),
+            static_cast<unsigned long long>(nc));
+  atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_body_list),
+            static_cast<unsigned long long>(nb));
 }
 
 void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
@@ -361,12 +401,25 @@ void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
   GTC_CUDA(cudaStreamSynchronize(s));
 }
 
+// Slots for the next one-pass walk: this walk's longest lists plus a
+// quarter and 32, in multiples of 32 entries (each slot starts on 128 bytes).
+void size_slots(Workspace &ws, const Scalars &h) {
+  auto slot = [](u64 longest) {
+    const u64 v = (longest + longest / 4 + 32 + 31) & ~31ull;
+    return static_cast<u32>(std::min<u64>(v, 0x7fffffe0ull));
+  };
+  ws.slot_cells = slot(h.max_cells);
+  ws.slot_bodies = slot(h.max_bodies);
+}
+
 }  // namespace
 
 void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host,
                  const LearnedWalk *lw) {
   const u64 n = ws.n;
+  const u64 prev_entries = ws.n_cell_list + ws.n_body_list;
   ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
+  ws.gapped = false;
   if (n == 0) return;
   const u32 n32 = static_cast<u32>(n), m = static_cast<u32>(ws.n_nodes);
   const u32 gs = static_cast<u32>(sp.group_size);
@@ -421,18 +474,58 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     return;
   }
 
-  // count pass, offsets, fill pass
+  const WalkRec32 *w32 = ws.walk32.as<WalkRec32>();
+  const WalkRec64 *w64 = ws.walk64.as<WalkRec64>();
+  const double *gbox = ws.gbox.as<double>();
+  const float *gboxf = ws.gboxf.as<float>();
+  const Task *tasks = ws.tasks.as<Task>();
   const u64 slots = static_cast<u64>(ng) * ntasks;
   ws.gcells.ensure(slots * 8);
   ws.gbodies.ensure(slots * 8);
+  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  const u32 tb = ceil_div(slots, kT);
+
+  // One pass into per-group slots when the last walk sized them and they
+  // fit 32-bit offsets and a few times the lists' own size.
+  const u64 slot_entries =
+      static_cast<u64>(ng) * (static_cast<u64>(ws.slot_cells) + ws.slot_bodies);
+  if (ws.slot_cells > 0 && ntasks == 1 &&
+      static_cast<u64>(ng) * ws.slot_cells <= 0xffffffffull &&
+      static_cast<u64>(ng) * ws.slot_bodies <= 0xffffffffull &&
+      slot_entries <= std::max<u64>(4 * prev_entries, 1ull << 26)) {
+    const u32 sl_c = ws.slot_cells, sl_b = ws.slot_bodies;
+    ws.cell_list.ensure(std::max<u64>(1, static_cast<u64>(ng) * sl_c) * 4);
+    ws.body_list.ensure(std::max<u64>(1, static_cast<u64>(ng) * sl_b) * 4);
+    GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
+    WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), sl_c, sl_b};
+    k_walk<kSlots><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
+    GTC_LAUNCH_CHECK();
+    k_slot_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
+                                     sl_c, sl_b, ws.groups.as<uint4>(), sc);
+    GTC_LAUNCH_CHECK();
+    read_scalars(ws, host, s);
+    size_slots(ws, *host);
+    if (!host->list_overflow) {
+      ws.n_cell_list = host->n_cell_list;
+      ws.n_body_list = host->n_body_list;
+      ws.gapped = true;
+      return;
+    }
+    // a list outgrew its slot: the counters start again for the two passes
+    GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  }
+
+  // count pass, offsets, fill pass
   ws.gcell_off.ensure((slots + 1) * 8);
   ws.gbody_off.ensure((slots + 1) * 8);
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr};
-  const u32 tb = ceil_div(slots, kT);
-  k_walk<false><<<tb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), ng,
-                                  ws.tasks.as<Task>(), ntasks, wo, sc);
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr, 0, 0};
+  k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
   exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, slots, body_off + slots, ws.scan_tmp, s);
@@ -444,15 +537,14 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   read_scalars(ws, host, s);
   if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
     throw RuntimeError("interaction lists too long for 32 bit offsets");
+  size_slots(ws, *host);
   ws.n_cell_list = host->n_cell_list;
   ws.n_body_list = host->n_body_list;
   ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   wo.cell_list = ws.cell_list.as<u32>();
   wo.body_list = ws.body_list.as<u32>();
-  k_walk<true><<<tb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), ng,
-                                 ws.tasks.as<Task>(), ntasks, wo, sc);
+  k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
 }
 
@@ -464,6 +556,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   Scalars *sc = ws.scalars.as<Scalars>();
   u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
   const u32 *abort = &sc->abort;
+  ws.gapped = false;  // replays write the lists back to back
   const u32 nb = ceil_div(n, kT), mb = ceil_div(mcap, kT);
   // groups (the one walk task, the root, was written before capture)
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
@@ -487,9 +580,9 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_CUDA(cudaMemsetAsync(ws.gcells.ptr, 0, n * 8, s));
   GTC_CUDA(cudaMemsetAsync(ws.gbodies.ptr, 0, n * 8, s));
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off,
-             ws.cell_list.as<u32>(), ws.body_list.as<u32>()};
+             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), 0, 0};
   const Task *tasks = ws.tasks.as<Task>();
-  k_walk<false><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+  k_walk<kCount><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
                                   ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
                                   &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
@@ -502,7 +595,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_LAUNCH_CHECK();
   k_check_lists_graph<<<1, 1, 0, s>>>(sc, caps.cells, caps.bodies);
   GTC_LAUNCH_CHECK();
-  k_walk<true><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+  k_walk<kFill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
                                  &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();

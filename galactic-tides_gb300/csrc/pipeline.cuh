@@ -78,6 +78,12 @@ struct Workspace {
   int key_words = 1;
   u32 *host_words = nullptr;  // pinned, for small read-backs
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
+  // One-pass walk: group g's lists start at g * slot_cells and g *
+  // slot_bodies (capacities sized from the previous walk's longest lists);
+  // 0 until a walk has measured them. `gapped`: the current lists use that
+  // layout (groups' ranges are not back to back).
+  u32 slot_cells = 0, slot_bodies = 0;
+  bool gapped = false;
   void release_all();
 };
 
@@ -98,6 +104,7 @@ struct Scalars {
   u32 list_overflow;      // learned walk: a lane's region overflowed
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)
+  u32 max_cells, max_bodies;  // longest cell and body list of a group
 };
 
 // Stage 1: octree on the device. pos (N x 3) and mass in caller order.

@@ -85,3 +85,49 @@ def test_repeat_calls_reuse_buffers(ctx, gtc):
     ctx.group_force(small, smass)
     a2, p2 = ctx.group_force(pos, mass)
     assert np.array_equal(a1, a2) and np.array_equal(p1, p2)
+
+
+def test_one_pass_walk_matches_two_passes(gtc):
+    """A repeated solve walks once, into per-group slots sized by the first
+    walk's longest lists; its lists (exported back to back) and forces are
+    the two-pass walk's, bit for bit."""
+    pos, _, mass, _ = gtc.make_galaxy(100_000, seed=3)
+    kw = dict(G=1.0, eps=0.025, quadrupole=True, theta=0.75, group_size=32, leaf_size=8,
+              pack=True)
+    c = gtc.Context(0)
+    try:
+        a1, p1 = c.group_force(pos, mass, **kw)
+        d1, s1 = c.export(), c.stats()
+        a2, p2 = c.group_force(pos, mass, **kw)
+        d2, s2 = c.export(), c.stats()
+    finally:
+        c.close()
+    assert s2["kernel_launches"] < s1["kernel_launches"]  # no count pass, no list scans
+    assert np.array_equal(a1, a2) and np.array_equal(p1, p2)
+    for k in ("groups", "cell_list", "body_list"):
+        assert np.array_equal(d1[k], d2[k]), k
+    for k in ("cell_interactions", "body_interactions", "max_list", "max_group",
+              "n_cell_list", "n_body_list", "walk_tests_fp64"):
+        assert s1[k] == s2[k], k
+
+
+def test_one_pass_walk_overflow_falls_back(ctx, gtc, oracle):
+    """Slots sized by a loose walk (theta 1.0) are outgrown by a tighter one
+    (theta 0.4): that solve falls back to counting first and still gives the
+    oracle's lists."""
+    pos, _, mass, _ = gtc.make_galaxy(60_000, seed=5)
+    c = gtc.Context(0)
+    try:
+        kw = dict(G=1.0, eps=0.025, quadrupole=True, group_size=32, leaf_size=8, pack=True)
+        c.group_force(pos, mass, theta=1.0, **kw)
+        c.group_force(pos, mass, theta=1.0, **kw)
+        n_short = c.stats()["max_list"]
+        acc, pot = c.group_force(pos, mass, theta=0.4, **kw)
+        d = c.export()
+        assert c.stats()["max_list"] > n_short
+        ref_acc, ref_pot = ctx.group_force(pos, mass, theta=0.4, **kw)
+    finally:
+        c.close()
+    nodes, order, lists = oracle.lists(pos, mass, theta=0.4, group_size=32, leaf_size=8, pack=True)
+    assert compare_lists(d, d["nodes"], lists, nodes) == []
+    assert np.array_equal(acc, ref_acc) and np.array_equal(pot, ref_pot)
