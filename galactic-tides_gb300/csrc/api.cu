@@ -245,8 +245,17 @@ struct GraphStep {
     const u64 pad = ctx->graph_headroom > 0 ? 1024 : 0;
     caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
     caps.depth = std::min<int>(gtc::kMaxDepth, static_cast<int>(hs.depth) + (pad ? 2 : 0));
-    caps.cells = static_cast<u64>(ws.n_cell_list * f) + 4 * pad;
-    caps.bodies = static_cast<u64>(ws.n_body_list * f) + 4 * pad;
+    // list slots: the last walk's group count and longest lists, with the
+    // headroom; offsets stay below 2^32 (a replay that needs more aborts)
+    caps.groups = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_groups * f) + pad, n));
+    caps.groups = std::max<u32>(caps.groups, 1);
+    auto slot = [&](u32 longest) {
+      const u64 v = (static_cast<u64>(longest * f) + (pad ? 32 : 0) + 31) & ~31ull;
+      const u64 most = (0xffffffffull / caps.groups) & ~31ull;
+      return static_cast<u32>(std::max<u64>(32, std::min(v, most)));
+    };
+    caps.slot_cells = slot(hs.max_cells);
+    caps.slot_bodies = slot(hs.max_bodies);
     const u64 m = caps.nodes;
     ws.geom.ensure(m * 2 * sizeof(double2));
     ws.mom.ensure(m * 2 * sizeof(double2));
@@ -270,8 +279,8 @@ struct GraphStep {
     ws.gcell_off.ensure((n + 1) * 8);
     ws.gbody_off.ensure((n + 1) * 8);
     ws.groups.ensure(n * 32);
-    ws.cell_list.ensure(caps.cells * 4);
-    ws.body_list.ensure(caps.bodies * 4);
+    ws.cell_list.ensure(static_cast<u64>(caps.groups) * caps.slot_cells * 4);
+    ws.body_list.ensure(static_cast<u64>(caps.groups) * caps.slot_bodies * 4);
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
     if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));
@@ -328,7 +337,7 @@ struct GraphStep {
     ws.n_groups = hs.n_groups;
     ws.n_cell_list = hs.n_cell_list;
     ws.n_body_list = hs.n_body_list;
-    ws.gapped = false;
+    ws.gapped = true;  // replays walk once into the captured slots
     gtc_stats &st = ctx->stats;
     const u32 replays = st.graph_steps;
     st = gtc_stats{};

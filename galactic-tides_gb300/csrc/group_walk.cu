@@ -97,10 +97,14 @@ __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
   if (sc->n_groups > 0 && sc->n_groups <= n) gend[sc->n_groups - 1] = n;
 }
 
-// A graph replay's check before the lists are written: more list entries
-// than the captured buffers hold (bit 8).
-__global__ void k_check_lists_graph(Scalars *sc, u64 cells, u64 bodies) {
-  if (sc->n_cell_list > cells || sc->n_body_list > bodies) sc->abort |= 8u;
+// A graph replay's checks around the one-pass walk (bit 8): more groups
+// than the captured slots cover (before), a list longer than its slot
+// (after).
+__global__ void k_check_groups_graph(Scalars *sc, u32 groups) {
+  if (sc->n_groups > groups) sc->abort |= 8u;
+}
+__global__ void k_check_slots_graph(Scalars *sc) {
+  if (sc->list_overflow) sc->abort |= 8u;
 }
 
 // Group bounding box (group_lists.cpp:125-131): centre and half-extent in
@@ -381,9 +385,9 @@ __global__ void __launch_bounds__(kT)
 __global__ void __launch_bounds__(kT)
     k_slot_records(const u32 *gbegin, const u32 *gend, u32 ng, const u64 *ncells,
                    const u64 *nbodies, u32 slot_cells, u32 slot_bodies, uint4 *groups,
-                   Scalars *sc) {
+                   Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
+  if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
   const u64 nc = ncells[g], nb = nbodies[g];
   const u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
   const u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
@@ -556,7 +560,6 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   Scalars *sc = ws.scalars.as<Scalars>();
   u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
   const u32 *abort = &sc->abort;
-  ws.gapped = false;  // replays write the lists back to back
   const u32 nb = ceil_div(n, kT), mb = ceil_div(mcap, kT);
   // groups (the one walk task, the root, was written before capture)
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
@@ -575,29 +578,24 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  // count pass over every possible group (the counts past the last are zero)
-  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  GTC_CUDA(cudaMemsetAsync(ws.gcells.ptr, 0, n * 8, s));
-  GTC_CUDA(cudaMemsetAsync(ws.gbodies.ptr, 0, n * 8, s));
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off,
-             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), 0, 0};
+  // one pass into the captured slots
+  k_check_groups_graph<<<1, 1, 0, s>>>(sc, caps.groups);
+  GTC_LAUNCH_CHECK();
+  GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), caps.slot_cells, caps.slot_bodies};
   const Task *tasks = ws.tasks.as<Task>();
-  k_walk<kCount><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                  ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
-                                  &sc->n_groups, abort);
+  k_walk<kSlots><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                   ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
+                                   sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, n, cell_off + n, ws.scan_tmp, s);
-  exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, n, body_off + n, ws.scan_tmp, s);
-  GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + n, 8, cudaMemcpyDeviceToDevice, s));
-  GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + n, 8, cudaMemcpyDeviceToDevice, s));
-  k_group_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, 1, cell_off, body_off,
-                                    ws.groups.as<uint4>(), sc, &sc->n_groups);
+  k_slot_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
+                                   caps.slot_cells, caps.slot_bodies, ws.groups.as<uint4>(), sc,
+                                   &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  k_check_lists_graph<<<1, 1, 0, s>>>(sc, caps.cells, caps.bodies);
-  GTC_LAUNCH_CHECK();
-  k_walk<kFill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo, sc,
-                                 &sc->n_groups, abort);
+  k_check_slots_graph<<<1, 1, 0, s>>>(sc);
   GTC_LAUNCH_CHECK();
 }
 

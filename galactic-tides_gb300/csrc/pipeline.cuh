@@ -138,11 +138,13 @@ void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, do
 struct GraphCaps {
   u32 nodes;        // node arrays
   int depth;        // deepest node the per-depth moment launches cover
-  u64 cells, bodies;  // cell_list, body_list
+  u32 groups;       // groups the list slots cover
+  u32 slot_cells, slot_bodies;  // each group's list slots (one-pass walk)
 };
 // Both stages without a host synchronisation, for stream capture: grids
 // sized by the capacities, counts read on the device. One key word only (a
-// tree deeper than 21 levels aborts), one walk task per group.
+// tree deeper than 21 levels aborts), one walk task per group, written in
+// one pass into per-group slots (more groups or a longer list aborts).
 void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 n,
                       const SolverParams &sp, const GraphCaps &caps, cudaStream_t s);
 void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &caps,
