@@ -357,28 +357,26 @@ __global__ void __launch_bounds__(kT)
 }
 
 // GTGroup records from the per-task offsets, and the list counters.
-__device__ __forceinline__ void group_stats(Scalars *sc, u64 t, u64 nc, u64 nb) {
-  atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
-  atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
-  atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
-  atomicMax(&sc->max_group, static_cast<u32>(t));
-  atomicMax(&sc->max_cells, static_cast<u32>(nc < 0xffffffffull ? nc : 0xffffffffull));
-  atomicMax(&sc->max_bodies, static_cast<u32>(nb < 0xffffffffull ? nb : 0xffffffffull));
-}
-
 __global__ void __launch_bounds__(kT)
     k_group_records(const u32 *gbegin, const u32 *gend, u32 ng, u32 ntasks, const u64 *cell_off,
                     const u64 *body_off, uint4 *groups, Scalars *sc,
                     const u32 *ng_dev = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (sc->abort || g >= bounded(ng, ng_dev)) return;
-  const u64 c0 = cell_off[static_cast<u64>(g) * ntasks],
-            c1 = cell_off[static_cast<u64>(g + 1) * ntasks];
-  const u64 b0 = body_off[static_cast<u64>(g) * ntasks],
-            b1 = body_off[static_cast<u64>(g + 1) * ntasks];
-  groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c1));
-  groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b1), 0u, 0u);
-  group_stats(sc, gend[g] - gbegin[g], c1 - c0, b1 - b0);
+  if (sc->abort) return;
+  const bool valid = g < bounded(ng, ng_dev);
+  u64 t = 0, nc = 0, nb = 0;
+  if (valid) {
+    const u64 c0 = cell_off[static_cast<u64>(g) * ntasks],
+              c1 = cell_off[static_cast<u64>(g + 1) * ntasks];
+    const u64 b0 = body_off[static_cast<u64>(g) * ntasks],
+              b1 = body_off[static_cast<u64>(g + 1) * ntasks];
+    groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c1));
+    groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b1), 0u, 0u);
+    t = gend[g] - gbegin[g];
+    nc = c1 - c0;
+    nb = b1 - b0;
+  }
+  group_stats_warp(sc, valid, t, nc, nb, false);
 }
 
 // Group records of a one-pass walk: group g's lists start at its slots.
@@ -387,17 +385,19 @@ __global__ void __launch_bounds__(kT)
                    const u64 *nbodies, u32 slot_cells, u32 slot_bodies, uint4 *groups,
                    Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
-  const u64 nc = ncells[g], nb = nbodies[g];
-  const u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
-  const u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
-  groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c0 + kc));
-  groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + kb), 0u, 0u);
-  group_stats(sc, gend[g] - gbegin[g], nc, nb);
-  atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_cell_list),
-            static_cast<unsigned long long>(nc));
-  atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_body_list),
-            static_cast<unsigned long long>(nb));
+  if (aborted(abort)) return;
+  const bool valid = g < bounded(ng, ng_dev);
+  u64 t = 0, nc = 0, nb = 0;
+  if (valid) {
+    nc = ncells[g];
+    nb = nbodies[g];
+    t = gend[g] - gbegin[g];
+    const u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
+    const u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
+    groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c0 + kc));
+    groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + kb), 0u, 0u);
+  }
+  group_stats_warp(sc, valid, t, nc, nb, true);
 }
 
 void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {

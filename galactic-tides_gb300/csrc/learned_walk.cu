@@ -552,14 +552,9 @@ __global__ void __launch_bounds__(kT)
   if (g >= rv.ng) return;
   u64 oc = cell_off[g], ob = body_off[g];
   if (lane == 0) {
-    const u64 nc = cell_off[g + 1] - oc, nb = body_off[g + 1] - ob, t = gend[g] - gbegin[g];
     groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(oc),
                                   static_cast<u32>(cell_off[g + 1]));
     groups[2ull * g + 1] = make_uint4(static_cast<u32>(ob), static_cast<u32>(body_off[g + 1]), 0u, 0u);
-    atomicAdd(&sc->cell_interactions, static_cast<unsigned long long>(t * nc));
-    atomicAdd(&sc->body_interactions, static_cast<unsigned long long>(t * nb - t));
-    atomicMax(&sc->max_list, static_cast<unsigned long long>(nc + nb));
-    atomicMax(&sc->max_group, static_cast<u32>(t));
   }
   for (u32 r = 0; r < rv.rounds; ++r) {
     const u32 *st = rv.gstart + static_cast<u64>(r) * (rv.ng + 1);
@@ -595,6 +590,21 @@ __global__ void __launch_bounds__(kT)
       ob += __shfl_sync(kFullMask, bs + nbj, 31);
     }
   }
+}
+
+// The groups' list statistics, one group per lane.
+__global__ void __launch_bounds__(kT)
+    k_list_stats(const u32 *gbegin, const u32 *gend, const u64 *cell_off, const u64 *body_off,
+                 u32 ng, Scalars *sc) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  const bool valid = g < ng;
+  u64 t = 0, nc = 0, nb = 0;
+  if (valid) {
+    t = gend[g] - gbegin[g];
+    nc = cell_off[g + 1] - cell_off[g];
+    nb = body_off[g + 1] - body_off[g];
+  }
+  group_stats_warp(sc, valid, t, nc, nb, false);
 }
 
 // The walk's inference on given raw features (tests and diagnostics).
@@ -830,6 +840,9 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       a.seg, a.seg2, rv, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
       cell_off, body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>(),
       sc);
+  GTC_LAUNCH_CHECK();
+  k_list_stats<<<ceil_div(ng, kT), kT, 0, s>>>(ws.gbegin.as<u32>(), ws.gend.as<u32>(), cell_off,
+                                               body_off, ng, sc);
   GTC_LAUNCH_CHECK();
 }
 

@@ -107,6 +107,42 @@ struct Scalars {
   u32 max_cells, max_bodies;  // longest cell and body list of a group
 };
 
+// The list statistics of one group per lane (valid lanes), summed and
+// maximised over the warp first so that each counter takes one atomic per
+// warp; every lane of the warp must call it. With `totals`, the list
+// lengths are added to the list sizes too.
+__device__ __forceinline__ void group_stats_warp(Scalars *sc, bool valid, u64 t, u64 nc, u64 nb,
+                                                 bool totals) {
+  unsigned long long ci = valid ? t * nc : 0, bi = valid ? t * nb - t : 0,
+                     ml = valid ? nc + nb : 0, tc = valid ? nc : 0, tb = valid ? nb : 0;
+  u32 mg = valid ? static_cast<u32>(t) : 0u;
+  u32 mc = valid ? static_cast<u32>(nc < 0xffffffffull ? nc : 0xffffffffull) : 0u;
+  u32 mb = valid ? static_cast<u32>(nb < 0xffffffffull ? nb : 0xffffffffull) : 0u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ci += __shfl_xor_sync(kFullMask, ci, o);
+    bi += __shfl_xor_sync(kFullMask, bi, o);
+    tc += __shfl_xor_sync(kFullMask, tc, o);
+    tb += __shfl_xor_sync(kFullMask, tb, o);
+    const unsigned long long m = __shfl_xor_sync(kFullMask, ml, o);
+    ml = m > ml ? m : ml;
+  }
+  mg = __reduce_max_sync(kFullMask, mg);
+  mc = __reduce_max_sync(kFullMask, mc);
+  mb = __reduce_max_sync(kFullMask, mb);
+  if ((threadIdx.x & 31) != 0 || __ballot_sync(kFullMask, valid) == 0) return;
+  atomicAdd(&sc->cell_interactions, ci);
+  atomicAdd(&sc->body_interactions, bi);
+  atomicMax(&sc->max_list, ml);
+  atomicMax(&sc->max_group, mg);
+  atomicMax(&sc->max_cells, mc);
+  atomicMax(&sc->max_bodies, mb);
+  if (totals) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_cell_list), tc);
+    atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_body_list), tb);
+  }
+}
+
 // Stage 1: octree on the device. pos (N x 3) and mass in caller order.
 // Fills geometry, moments, ranges, the tree-order permutation (idx), the
 // FP32 bodies and cells and the walk records. Returns the node count.
