@@ -63,7 +63,7 @@ void Workspace::release_all() {
                          &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
                          &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
-                         &groups, &cell_list, &body_list, &root, &bbox_part, &scalars, &scan_tmp,
+                         &groups, &cell_list, &body_list, &spill, &root, &bbox_part, &scalars, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (host_words) cudaFreeHost(host_words);
@@ -213,6 +213,8 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     st.mlp_batches = h.mlp_batches;
   }
   st.criterion_used = learned ? GTC_CRITERION_LEARNED : GTC_CRITERION_THETA;
+  st.list_passes = ws.list_passes;
+  st.spilled_groups = n > 0 ? ctx->host_sc->spilled : 0;
   ctx->prev_n = ctx->have_model ? n : 0;
   st.n_cell_list = ws.n_cell_list;
   st.n_body_list = ws.n_body_list;
@@ -245,17 +247,25 @@ struct GraphStep {
     const u64 pad = ctx->graph_headroom > 0 ? 1024 : 0;
     caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
     caps.depth = std::min<int>(gtc::kMaxDepth, static_cast<int>(hs.depth) + (pad ? 2 : 0));
-    // list slots: the last walk's group count and longest lists, with the
-    // headroom; offsets stay below 2^32 (a replay that needs more aborts)
+    // list slots: the last walk's group count, and its longest lists with
+    // twice the headroom (the longest of many lists moves more than the
+    // totals do); offsets stay below 2^32 (a replay that needs more aborts)
     caps.groups = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_groups * f) + pad, n));
     caps.groups = std::max<u32>(caps.groups, 1);
+    const double fs = 1.0 + 2.0 * ctx->graph_headroom;
     auto slot = [&](u32 longest) {
-      const u64 v = (static_cast<u64>(longest * f) + (pad ? 32 : 0) + 31) & ~31ull;
+      const u64 v = (static_cast<u64>(longest * fs) + (pad ? 64 : 0) + 31) & ~31ull;
       const u64 most = (0xffffffffull / caps.groups) & ~31ull;
       return static_cast<u32>(std::max<u64>(32, std::min(v, most)));
     };
     caps.slot_cells = slot(hs.max_cells);
     caps.slot_bodies = slot(hs.max_bodies);
+    auto pool = [&](u32 sl) {
+      const u64 room = 0xffffffffull - static_cast<u64>(caps.groups) * sl;
+      return std::min<u64>(gtc::Workspace::pool_for(caps.groups, sl), room);
+    };
+    caps.pool_cells = pool(caps.slot_cells);
+    caps.pool_bodies = pool(caps.slot_bodies);
     const u64 m = caps.nodes;
     ws.geom.ensure(m * 2 * sizeof(double2));
     ws.mom.ensure(m * 2 * sizeof(double2));
@@ -279,8 +289,9 @@ struct GraphStep {
     ws.gcell_off.ensure((n + 1) * 8);
     ws.gbody_off.ensure((n + 1) * 8);
     ws.groups.ensure(n * 32);
-    ws.cell_list.ensure(static_cast<u64>(caps.groups) * caps.slot_cells * 4);
-    ws.body_list.ensure(static_cast<u64>(caps.groups) * caps.slot_bodies * 4);
+    ws.cell_list.ensure((static_cast<u64>(caps.groups) * caps.slot_cells + caps.pool_cells) * 4);
+    ws.body_list.ensure((static_cast<u64>(caps.groups) * caps.slot_bodies + caps.pool_bodies) * 4);
+    ws.spill.ensure(2 * n * sizeof(u32));
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
     if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));
@@ -357,6 +368,8 @@ struct GraphStep {
     st.n_nodes = hs.n_nodes;
     st.n_groups = hs.n_groups;
     st.criterion_used = GTC_CRITERION_THETA;
+    st.list_passes = 1;
+    st.spilled_groups = hs.spilled;
     st.kernel_launches = 0;  // one graph launch (its kernels were counted at capture)
     st.graph_steps = replays + 1;
     ctx->have_group = true;

@@ -18,7 +18,7 @@
 // to the next node (its last child). A counting pass sizes the lists; after
 // the offsets are scanned a second pass writes them. Once a walk has
 // measured the longest lists, later walks run once, writing each group's
-// lists into fixed per-group slots (a quarter larger), and fall back to the
+// lists into fixed per-group slots (half as long again), and fall back to the
 // two passes when a list outgrows its slot.
 
 #include <algorithm>
@@ -98,8 +98,8 @@ __global__ void k_last_end(const Scalars *sc, u32 n, u32 *gend) {
 }
 
 // A graph replay's checks around the one-pass walk (bit 8): more groups
-// than the captured slots cover (before), a list longer than its slot
-// (after).
+// than the captured slots cover (before), overflow pools too small for the
+// lists that outgrew their slots (after).
 __global__ void k_check_groups_graph(Scalars *sc, u32 groups) {
   if (sc->n_groups > groups) sc->abort |= 8u;
 }
@@ -236,12 +236,19 @@ struct WalkOut {
   const u64 *cell_off, *body_off; // fill pass, same indexing
   u32 *cell_list, *body_list;
   u32 slot_cells, slot_bodies;    // one-pass walk: each group's capacities
+  u32 *spill_cells, *spill_bodies;  // where an outgrown group's lists go (kNoSpill: its slot)
+  u64 pool_cells_at, pool_cells;    // overflow pools: first entry and size
+  u64 pool_bodies_at, pool_bodies;
 };
 
-// Walk modes: count the lists; write them at scanned offsets; or both in
-// one pass into fixed per-group slots (one task per group), flagging a
-// list that outgrows its slot.
-constexpr int kCount = 0, kFill = 1, kSlots = 2;
+// Walk modes: count the lists; write them at scanned offsets; both in one
+// pass into fixed per-group slots (one task per group; an outgrown slot
+// keeps counting, and its group then takes a place in the overflow pools
+// for its whole lists, or flags the lists as overflowing when the pools are
+// too small); or write again, whole, the lists of the groups that outgrew
+// their slots, into their places in the pools.
+constexpr int kCount = 0, kFill = 1, kSlots = 2, kSpill = 3;
+constexpr u32 kNoSpill = 0xffffffffu;
 
 __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk64, u32 i,
                                       const float *gf, const float *hf, float gbound,
@@ -282,16 +289,20 @@ __global__ void __launch_bounds__(kT)
   } else if (kMode == kSlots) {
     cl = out.cell_list + static_cast<u64>(g) * out.slot_cells;
     bl = out.body_list + static_cast<u64>(g) * out.slot_bodies;
+  } else if (kMode == kSpill) {
+    if (out.spill_cells[g] == kNoSpill) return;
+    cl = out.cell_list + out.spill_cells[g];
+    bl = out.body_list + out.spill_bodies[g];
   }
   u32 nc = 0, nb = 0, exact = 0;
   const Task task = tasks[t];
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
     if (verdict == 1 && nbody > kFewBodies) {
-      if (kMode == kFill || (kMode == kSlots && nc < out.slot_cells)) cl[nc] = i;
+      if (kMode == kFill || kMode == kSpill || (kMode == kSlots && nc < out.slot_cells)) cl[nc] = i;
       ++nc;
     } else {
-      if (kMode == kFill)
+      if (kMode == kFill || kMode == kSpill)
         for (u32 j = 0; j < nbody; ++j) bl[nb + j] = r.begin + j;
       if (kMode == kSlots)
         for (u32 j = 0; j < nbody && nb + j < out.slot_bodies; ++j) bl[nb + j] = r.begin + j;
@@ -324,14 +335,29 @@ __global__ void __launch_bounds__(kT)
       }
     }
   }
-  if (kMode != kFill) {
+  if (kMode == kCount || kMode == kSlots) {
     out.ncells[slot] = nc;
     out.nbodies[slot] = nb;
     if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
   }
-  if (kMode == kSlots && (nc > out.slot_cells || nb > out.slot_bodies))
-    atomicOr(&sc->list_overflow, 1u);
+  if (kMode == kSlots) {
+    u32 oc = kNoSpill, ob = kNoSpill;
+    if (nc > out.slot_cells || nb > out.slot_bodies) {
+      const u64 c = atomicAdd(&sc->spill_used[0], static_cast<unsigned long long>(nc));
+      const u64 b = atomicAdd(&sc->spill_used[1], static_cast<unsigned long long>(nb));
+      if (c + nc <= out.pool_cells && b + nb <= out.pool_bodies) {
+        oc = static_cast<u32>(out.pool_cells_at + c);
+        ob = static_cast<u32>(out.pool_bodies_at + b);
+      } else {
+        atomicOr(&sc->list_overflow, 1u);
+      }
+      atomicAdd(&sc->spilled, 1u);
+    }
+    out.spill_cells[g] = oc;
+    out.spill_bodies[g] = ob;
+  }
 }
+
 
 // Walk tasks: nodes at depth `split` (0..2), and leaves above it, in node
 // order. The root is never accepted (every group lies inside it), so only a
@@ -382,8 +408,9 @@ __global__ void __launch_bounds__(kT)
 // Group records of a one-pass walk: group g's lists start at its slots.
 __global__ void __launch_bounds__(kT)
     k_slot_records(const u32 *gbegin, const u32 *gend, u32 ng, const u64 *ncells,
-                   const u64 *nbodies, u32 slot_cells, u32 slot_bodies, uint4 *groups,
-                   Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+                   const u64 *nbodies, u32 slot_cells, u32 slot_bodies, const u32 *spill_cells,
+                   const u32 *spill_bodies, uint4 *groups, Scalars *sc,
+                   const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort)) return;
   const bool valid = g < bounded(ng, ng_dev);
@@ -392,8 +419,14 @@ __global__ void __launch_bounds__(kT)
     nc = ncells[g];
     nb = nbodies[g];
     t = gend[g] - gbegin[g];
-    const u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
-    const u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
+    u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
+    u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
+    if (spill_cells[g] != kNoSpill) {  // the whole lists, in the pools
+      c0 = spill_cells[g];
+      b0 = spill_bodies[g];
+      kc = nc;
+      kb = nb;
+    }
     groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c0 + kc));
     groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + kb), 0u, 0u);
   }
@@ -405,11 +438,13 @@ void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
   GTC_CUDA(cudaStreamSynchronize(s));
 }
 
-// Slots for the next one-pass walk: this walk's longest lists plus a
-// quarter and 32, in multiples of 32 entries (each slot starts on 128 bytes).
+// Slots for the next one-pass walk: this walk's longest lists plus a half
+// and 64, in multiples of 32 entries (each slot starts on 128 bytes). The
+// longest of many groups' lists moves from one step to the next, so the
+// margin is wide; slots cost only memory.
 void size_slots(Workspace &ws, const Scalars &h) {
   auto slot = [](u64 longest) {
-    const u64 v = (longest + longest / 4 + 32 + 31) & ~31ull;
+    const u64 v = (longest + longest / 2 + 64 + 31) & ~31ull;
     return static_cast<u32>(std::min<u64>(v, 0x7fffffe0ull));
   };
   ws.slot_cells = slot(h.max_cells);
@@ -424,10 +459,12 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u64 prev_entries = ws.n_cell_list + ws.n_body_list;
   ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
   ws.gapped = false;
+  ws.list_passes = 0;
   if (n == 0) return;
   const u32 n32 = static_cast<u32>(n), m = static_cast<u32>(ws.n_nodes);
   const u32 gs = static_cast<u32>(sp.group_size);
   Scalars *sc = ws.scalars.as<Scalars>();
+  GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
   ws.flags.ensure(std::max<u64>(n, m) * 4);
   ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
   u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
@@ -490,24 +527,32 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u32 tb = ceil_div(slots, kT);
 
   // One pass into per-group slots when the last walk sized them and they
-  // fit 32-bit offsets and a few times the lists' own size.
-  const u64 slot_entries =
-      static_cast<u64>(ng) * (static_cast<u64>(ws.slot_cells) + ws.slot_bodies);
-  if (ws.slot_cells > 0 && ntasks == 1 &&
-      static_cast<u64>(ng) * ws.slot_cells <= 0xffffffffull &&
-      static_cast<u64>(ng) * ws.slot_bodies <= 0xffffffffull &&
-      slot_entries <= std::max<u64>(4 * prev_entries, 1ull << 26)) {
-    const u32 sl_c = ws.slot_cells, sl_b = ws.slot_bodies;
-    ws.cell_list.ensure(std::max<u64>(1, static_cast<u64>(ng) * sl_c) * 4);
-    ws.body_list.ensure(std::max<u64>(1, static_cast<u64>(ng) * sl_b) * 4);
+  // fit 32-bit offsets and eight times the lists' own size (the slots of
+  // the benchmark galaxy take about four times). Groups whose
+  // lists outgrow their slots are walked again into the overflow pools;
+  // pools too small fall back to the two passes below.
+  const u32 sl_c = ws.slot_cells, sl_b = ws.slot_bodies;
+  const u64 pool_c = Workspace::pool_for(ng, sl_c), pool_b = Workspace::pool_for(ng, sl_b);
+  const u64 ext_c = static_cast<u64>(ng) * sl_c + pool_c, ext_b = static_cast<u64>(ng) * sl_b + pool_b;
+  if (sl_c > 0 && ntasks == 1 && ext_c <= 0xffffffffull && ext_b <= 0xffffffffull &&
+      ext_c + ext_b <= std::max<u64>(8 * prev_entries, 1ull << 26)) {
+    ws.cell_list.ensure(ext_c * 4);
+    ws.body_list.ensure(ext_b * 4);
+    ws.spill.ensure(2ull * ng * sizeof(u32));
+    u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + ng;
     GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
     WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), sl_c, sl_b};
+               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), sl_c, sl_b, spill_c, spill_b,
+               static_cast<u64>(ng) * sl_c, pool_c, static_cast<u64>(ng) * sl_b, pool_b};
     k_walk<kSlots><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
     GTC_LAUNCH_CHECK();
+    k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
+    GTC_LAUNCH_CHECK();
     k_slot_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
-                                     sl_c, sl_b, ws.groups.as<uint4>(), sc);
+                                     sl_c, sl_b, spill_c, spill_b, ws.groups.as<uint4>(), sc);
     GTC_LAUNCH_CHECK();
     read_scalars(ws, host, s);
     size_slots(ws, *host);
@@ -515,9 +560,10 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
       ws.n_cell_list = host->n_cell_list;
       ws.n_body_list = host->n_body_list;
       ws.gapped = true;
+      ws.list_passes = 1;
       return;
     }
-    // a list outgrew its slot: the counters start again for the two passes
+    // the pools were too small: the counters start again for the two passes
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
@@ -528,7 +574,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gcell_off.ensure((slots + 1) * 8);
   ws.gbody_off.ensure((slots + 1) * 8);
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr, 0, 0};
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr,
+             0, 0, nullptr, nullptr, 0, 0, 0, 0};
   k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
@@ -550,6 +597,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   wo.body_list = ws.body_list.as<u32>();
   k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
+  ws.list_passes = 2;
 }
 
 void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &caps,
@@ -578,22 +626,31 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  // one pass into the captured slots
+  // one pass into the captured slots, outgrown groups again into the pools
   k_check_groups_graph<<<1, 1, 0, s>>>(sc, caps.groups);
   GTC_LAUNCH_CHECK();
   GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
   GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
+  u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + n;
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), caps.slot_cells, caps.slot_bodies};
+             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), caps.slot_cells, caps.slot_bodies,
+             spill_c, spill_b, static_cast<u64>(caps.groups) * caps.slot_cells, caps.pool_cells,
+             static_cast<u64>(caps.groups) * caps.slot_bodies, caps.pool_bodies};
   const Task *tasks = ws.tasks.as<Task>();
   k_walk<kSlots><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
                                    ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
                                    sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
+  k_walk<kSpill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                   ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
+                                   sc, &sc->n_groups, abort);
+  GTC_LAUNCH_CHECK();
   k_slot_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
-                                   caps.slot_cells, caps.slot_bodies, ws.groups.as<uint4>(), sc,
-                                   &sc->n_groups, abort);
+                                   caps.slot_cells, caps.slot_bodies, spill_c, spill_b,
+                                   ws.groups.as<uint4>(), sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
   k_check_slots_graph<<<1, 1, 0, s>>>(sc);
   GTC_LAUNCH_CHECK();

@@ -804,6 +804,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     if (!overflow) {
       host->mlp_rows = rows;
       host->mlp_batches = batches;
+      ws.list_passes = static_cast<u32>(base.size());
       break;
     }
     if (attempt >= 4 || lanes * static_cast<u64>(ls.lane_cells) * 2 > 0xffffffffull ||

@@ -67,7 +67,7 @@ struct Workspace {
       arrive, bucket, walk32, walk64, cells;
   // groups and lists
   DeviceBuffer tasks, gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
-      body_list;
+      body_list, spill;
   // scalars and reductions
   DeviceBuffer root, bbox_part, scalars;
   DeviceBuffer scan_tmp;
@@ -84,6 +84,10 @@ struct Workspace {
   // layout (groups' ranges are not back to back).
   u32 slot_cells = 0, slot_bodies = 0;
   bool gapped = false;
+  u32 list_passes = 0;  // walks of the last list build (1 one pass, 2 count + fill, rounds)
+  // Overflow pool behind n_groups slots of `slot` entries: a sixteenth of
+  // the slots plus four slots.
+  static u64 pool_for(u64 n_groups, u32 slot) { return n_groups * slot / 16 + 4ull * slot; }
   void release_all();
 };
 
@@ -105,6 +109,8 @@ struct Scalars {
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)
   u32 max_cells, max_bodies;  // longest cell and body list of a group
+  unsigned long long spill_used[2];  // one-pass walk: overflow pool entries taken (cells, bodies)
+  u32 spilled;            // one-pass walk: groups that outgrew their slots
 };
 
 // The list statistics of one group per lane (valid lanes), summed and
@@ -176,6 +182,7 @@ struct GraphCaps {
   int depth;        // deepest node the per-depth moment launches cover
   u32 groups;       // groups the list slots cover
   u32 slot_cells, slot_bodies;  // each group's list slots (one-pass walk)
+  u64 pool_cells, pool_bodies;  // overflow pools behind the slots
 };
 // Both stages without a host synchronisation, for stream capture: grids
 // sized by the capacities, counts read on the device. One key word only (a

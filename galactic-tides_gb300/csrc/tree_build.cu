@@ -233,19 +233,26 @@ __global__ void __launch_bounds__(kT)
     k_levels(KeyView kv, const u32 *idx, const u8 *tiny, u32 n, int L, signed char *lcp_next,
              u8 *leafdepth, Scalars *sc) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
-  if (b >= n) return;
-  lcp_next[b] = static_cast<signed char>(b + 1 < n ? lcp(kv, b, b + 1) : -1);
-  int w = -1;
-  if (n > static_cast<u32>(L)) {
-    const u32 lo = b >= static_cast<u32>(L) ? b - L : 0;
-    const u32 hi = min(b, n - 1 - L);
-    for (u32 i = lo; i <= hi; ++i) w = max(w, lcp(kv, i, i + L));
+  int ld = 0;
+  if (b < n) {
+    lcp_next[b] = static_cast<signed char>(b + 1 < n ? lcp(kv, b, b + 1) : -1);
+    int w = -1;
+    if (n > static_cast<u32>(L)) {
+      const u32 lo = b >= static_cast<u32>(L) ? b - L : 0;
+      const u32 hi = min(b, n - 1 - L);
+      for (u32 i = lo; i <= hi; ++i) w = max(w, lcp(kv, i, i + L));
+    }
+    ld = min(w + 1, kMaxDepth);
+    ld = min(ld, static_cast<int>(tiny[idx[b]]));
+    leafdepth[b] = static_cast<u8>(ld);
   }
-  int ld = min(w + 1, kMaxDepth);
-  ld = min(ld, static_cast<int>(tiny[idx[b]]));
-  leafdepth[b] = static_cast<u8>(ld);
-  if (ld > kLevelsPerWord * kv.words) atomicAdd(&sc->deep, 1u);
-  atomicMax(&sc->depth, static_cast<u32>(ld));
+  // one atomic per warp for each counter
+  const u32 deep = __popc(__ballot_sync(kFullMask, b < n && ld > kLevelsPerWord * kv.words));
+  const u32 dmax = __reduce_max_sync(kFullMask, static_cast<u32>(ld));
+  if ((threadIdx.x & 31) == 0) {
+    if (deep) atomicAdd(&sc->deep, deep);
+    atomicMax(&sc->depth, dmax);
+  }
 }
 
 // ------------------------------------------------------- deeper key words

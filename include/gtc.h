@@ -123,6 +123,10 @@ typedef struct gtc_stats {
   uint64_t mlp_batches;       /* learned walk: warp-wide network evaluations */
   uint32_t criterion_used;    /* GTC_CRITERION_* the walk actually used */
   uint32_t graph_steps;       /* leapfrog: steps of the last call replayed from a CUDA graph */
+  uint32_t list_passes;       /* walks over the tree for the lists: 1 one pass into per-group
+                                 slots, 2 count then fill, learned: the walk's rounds */
+  uint32_t spilled_groups;    /* one-pass walk: groups whose lists outgrew their slots and
+                                 were written again into the overflow pools */
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is

@@ -102,6 +102,7 @@ def test_one_pass_walk_matches_two_passes(gtc):
         d2, s2 = c.export(), c.stats()
     finally:
         c.close()
+    assert (s1["list_passes"], s2["list_passes"], s2["spilled_groups"]) == (2, 1, 0)
     assert s2["kernel_launches"] < s1["kernel_launches"]  # no count pass, no list scans
     assert np.array_equal(a1, a2) and np.array_equal(p1, p2)
     for k in ("groups", "cell_list", "body_list"):
@@ -129,5 +130,34 @@ def test_one_pass_walk_overflow_falls_back(ctx, gtc, oracle):
     finally:
         c.close()
     nodes, order, lists = oracle.lists(pos, mass, theta=0.4, group_size=32, leaf_size=8, pack=True)
+    assert compare_lists(d, d["nodes"], lists, nodes) == []
+    assert np.array_equal(acc, ref_acc) and np.array_equal(pot, ref_pot)
+
+
+def test_one_pass_walk_spills_outgrown_groups(gtc, oracle):
+    """Slots sized on a uniform cube are outgrown by a few groups once a
+    dense clump is added: those groups' lists are written again, whole,
+    into the overflow pools, the others stay in their slots, and lists and
+    forces are the two-pass walk's."""
+    rng = np.random.default_rng(2)
+    n = 20_000
+    pos = rng.uniform(-1, 1, (n, 3))
+    mass = np.full(n, 1.0 / n)
+    pos2 = np.vstack([pos, rng.normal(0, 0.01, (4000, 3)) + 0.3])
+    mass2 = np.full(len(pos2), 1.0 / len(pos2))
+    kw = dict(G=1.0, eps=0.01, quadrupole=True, theta=0.75, group_size=32, leaf_size=8, pack=True)
+    c, fresh = gtc.Context(0), gtc.Context(0)
+    try:
+        c.group_force(pos, mass, **kw)
+        acc, pot = c.group_force(pos2, mass2, **kw)
+        st, d = c.stats(), c.export()
+        ref_acc, ref_pot = fresh.group_force(pos2, mass2, **kw)
+        assert fresh.stats()["list_passes"] == 2
+    finally:
+        c.close()
+        fresh.close()
+    assert st["list_passes"] == 1 and 0 < st["spilled_groups"] < st["n_groups"] // 10
+    nodes, order, lists = oracle.lists(pos2, mass2, theta=0.75, group_size=32, leaf_size=8,
+                                       pack=True)
     assert compare_lists(d, d["nodes"], lists, nodes) == []
     assert np.array_equal(acc, ref_acc) and np.array_equal(pot, ref_pot)
