@@ -61,9 +61,9 @@ void Workspace::release_all() {
                          &key2, &tiny, &lcp, &leafdepth, &count, &count_scan, &flags,
                          &flags_scan, &tpos, &tmass, &bodies, &out, &dpos, &dkey, &dkey_alt,
                          &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
-                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &arrive, &bucket, &walk32, &walk64, &cells,
+                         &nend, &skip, &parent, &depth, &nchild, &isleaf, &kids, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
-                         &groups, &cell_list, &body_list, &spill, &root, &bbox_part, &scalars, &scan_tmp,
+                         &groups, &cell_list, &body_list, &spill, &root, &bbox_part, &scalars, &split, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (host_words) cudaFreeHost(host_words);
@@ -277,11 +277,13 @@ struct GraphStep {
     ws.parent.ensure(m * 4);
     ws.depth.ensure(m);
     ws.nchild.ensure(m);
+    ws.kids.ensure(m * 8 * sizeof(u32));
     ws.isleaf.ensure(m);
     ws.bucket.ensure(m * 4);
     ws.walk32.ensure(m * sizeof(gtc::WalkRec32));
     ws.walk64.ensure(m * sizeof(gtc::WalkRec64));
     ws.cells.ensure(m * 3 * sizeof(float4));
+    ws.split.ensure(3ull * gtc::kSplitSize * sizeof(double));
     ws.flags.ensure(std::max<u64>(n, m) * 4);
     ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
     ws.gcells.ensure(n * 8);

@@ -24,7 +24,7 @@
 namespace gtc {
 namespace {
 
-constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpsPerBlock = 8;
 constexpr int kT = 32 * kWarpsPerBlock;
 
 struct Staged {

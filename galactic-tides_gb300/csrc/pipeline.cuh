@@ -20,6 +20,10 @@ namespace gtc {
 
 constexpr int kMaxDepth = 60;     // depth cap of the reference octree (octree.cpp:18)
 constexpr int kLevelsPerWord = 21;
+// Levels of the per-axis split-value table of the key kernel, and its size
+// per axis (heap order, index 0 unused).
+constexpr int kSplitLevels = 17;
+constexpr u32 kSplitSize = 1u << kSplitLevels;
 constexpr u32 kFewBodies = 2;     // accepted cells this small go on the body list (group_lists.h:58)
 constexpr int kMaxGroupSize = 32;
 
@@ -63,13 +67,13 @@ struct Workspace {
   // deep rounds
   DeviceBuffer dpos, dkey, dkey_alt, drec, drec_alt, dseg, dtmp;
   // nodes
-  DeviceBuffer geom, mom, quad, delta, nbegin, nend, skip, parent, depth, nchild, isleaf,
+  DeviceBuffer geom, mom, quad, delta, nbegin, nend, skip, parent, depth, nchild, isleaf, kids,
       arrive, bucket, walk32, walk64, cells;
   // groups and lists
   DeviceBuffer tasks, gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
       body_list, spill;
   // scalars and reductions
-  DeviceBuffer root, bbox_part, scalars;
+  DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
   RadixScratch radix;
 

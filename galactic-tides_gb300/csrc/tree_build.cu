@@ -185,9 +185,58 @@ __device__ __forceinline__ u64 order_key(double v) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// Split values. Along one axis the centre a body's walk compares against at
+// level d depends only on the body's first d bits on that axis: the centres
+// of all levels form a binary tree per axis (heap order, node 1 the root
+// centre, the children of node k at level d the centre stepped down and up
+// by half_at[d + 1], with the reference's FP64 addition). A body's key bits
+// on an axis are then a binary search in that tree. The table holds levels
+// 0..kSplitLevels - 1 (2^kSplitLevels - 1 values per axis), built once per
+// tree instead of once per body; the levels below are stepped per body.
+constexpr int kSplitTop = 11;                    // levels one block per axis builds
+
+// Levels 0..kSplitTop - 1, one block per axis, level by level.
+__global__ void __launch_bounds__(1024) k_split_top(const TreeRoot *root, double *split) {
+  const int axis = blockIdx.x;
+  double *t = split + static_cast<u64>(axis) * kSplitSize;
+  if (threadIdx.x == 0) t[1] = root->center[axis];
+  __syncthreads();
+  for (int d = 1; d < kSplitTop; ++d) {
+    const double h = root->half_at[d];
+    for (u32 j = threadIdx.x; j < (1u << d); j += blockDim.x) {
+      const u32 k = (1u << d) + j;
+      const double c = t[k >> 1];
+      t[k] = c + ((k & 1u) ? h : -h);  // step_centre's operation
+    }
+    __syncthreads();
+  }
+}
+
+// Levels kSplitTop..kSplitLevels - 1: one thread per node of level
+// kSplitTop - 1 builds its subtree, level by level.
+__global__ void __launch_bounds__(256) k_split_rest(const TreeRoot *root, double *split) {
+  const u32 per_axis = 1u << (kSplitTop - 1);
+  const u32 tid = blockIdx.x * 256 + threadIdx.x;
+  if (tid >= 3 * per_axis) return;
+  const int axis = static_cast<int>(tid / per_axis);
+  double *t = split + static_cast<u64>(axis) * kSplitSize;
+  const u32 base = per_axis + tid % per_axis;  // heap index at level kSplitTop - 1
+  for (int d = kSplitTop; d < kSplitLevels; ++d) {
+    const double h = root->half_at[d];
+    const int below = d - (kSplitTop - 1);  // levels under the subtree's root
+    const u32 first = base << below;
+    for (u32 j = 0; j < (1u << below); ++j) {
+      const u32 k = first + j;
+      t[k] = t[k >> 1] + ((k & 1u) ? h : -h);
+    }
+  }
+}
+
 // First key word: levels 1..21 from the root; records the first depth whose
 // node is "tiny" (a leaf whatever its count). Digits below a tiny node are 0,
-// so bodies of such a leaf stay in input order through the sort.
+// so bodies of such a leaf stay in input order through the sort. The centres
+// of the first kSplitLevels levels come from the split table; the rest are
+// stepped as the reference does.
 //
 // A node holding body p has |centre|_1 <= |p|_1 + 3 half (plus rounding), so
 // it can only be tiny once half < 1e-12 (|p|_1 + 3 half + 1e-300), i.e. once
@@ -195,12 +244,10 @@ __device__ __forceinline__ u64 order_key(double v) {
 // twice that bound skip the exact FP64 test; the comparison of two positive
 // doubles is done on their bit patterns.
 __global__ void __launch_bounds__(kT)
-    k_keys(const double *pos, u32 n, const TreeRoot *root, u64 *key, u32 *idx, u8 *tiny,
-           u32 *error) {
+    k_keys(const double *pos, u32 n, const TreeRoot *root, const double *split, u64 *key,
+           u32 *idx, u8 *tiny, u32 *error) {
   __shared__ double half_at[kLevelsPerWord + 1];
-  __shared__ double c0[3];
   if (threadIdx.x <= kLevelsPerWord) half_at[threadIdx.x] = root->half_at[threadIdx.x];
-  if (threadIdx.x < 3) c0[threadIdx.x] = root->center[threadIdx.x];
   __syncthreads();
   const u32 i = blockIdx.x * kT + threadIdx.x;
   if (i >= n) return;
@@ -209,10 +256,17 @@ __global__ void __launch_bounds__(kT)
   const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
   const long long maybe_tiny =
       __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
-  double cx = c0[0], cy = c0[1], cz = c0[2];
+  const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
+  u32 ix = 1, iy = 1, iz = 1;
+  double cx = 0.0, cy = 0.0, cz = 0.0;
   u64 k = 0;
   int t = kNoTiny;
   for (int d = 0; d < kLevelsPerWord; ++d) {
+    if (d < kSplitLevels) {
+      cx = __ldg(tx + ix);
+      cy = __ldg(ty + iy);
+      cz = __ldg(tz + iz);
+    }
     if (t == kNoTiny && __double_as_longlong(half_at[d]) < maybe_tiny &&
         tiny_node(half_at[d], cx, cy, cz))
       t = d;
@@ -220,7 +274,13 @@ __global__ void __launch_bounds__(kT)
             (kz >= order_key(cz) ? 4 : 0);
     if (t != kNoTiny) o = 0;
     k = (k << 3) | static_cast<u64>(o);
-    step_centre(cx, cy, cz, o, half_at[d + 1]);
+    if (d + 1 < kSplitLevels) {
+      ix = 2 * ix + (o & 1);
+      iy = 2 * iy + ((o >> 1) & 1);
+      iz = 2 * iz + (o >> 2);
+    } else {
+      step_centre(cx, cy, cz, o, half_at[d + 1]);
+    }
   }
   if (t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz)) t = kLevelsPerWord;
   key[i] = k;
@@ -388,8 +448,11 @@ __device__ __forceinline__ int children_of(u32 p, const u32 *skip, u32 ch[8]) {
   return k;
 }
 
+// Parents, child counts and every inner node's children (8 slots, last
+// octant first), so that the moment kernels load a node's children at once
+// instead of following the skip chain.
 __global__ void __launch_bounds__(kT)
-    k_children(const u32 *skip, const u8 *isleaf, u32 m, u32 *parent, u8 *nchild,
+    k_children(const u32 *skip, const u8 *isleaf, u32 m, u32 *parent, u8 *nchild, uint4 *kids,
                const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || p >= bounded(m, m_dev)) return;
@@ -398,10 +461,12 @@ __global__ void __launch_bounds__(kT)
     nchild[p] = 0;
     return;
   }
-  u32 ch[8];
+  u32 ch[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
   const int k = children_of(p, skip, ch);
   nchild[p] = static_cast<u8>(k);
   for (int j = 0; j < k; ++j) parent[ch[j]] = p;
+  kids[2ull * p] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
+  kids[2ull * p + 1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
 }
 
 // Input order inside each leaf (the reference never splits a leaf's range).
@@ -440,6 +505,7 @@ struct MomentArrays {
   const double2 *geom;   // 2 per node: (cx, cy), (cz, half)
   const u32 *nbegin, *nend, *skip, *parent;
   const u8 *nchild;
+  const uint4 *kids;     // 2 per node: the children, last octant first
   const double *tpos, *tmass;
   double2 *mom;     // 2 per node: (mx, my), (mz, mass)
   double2 *quad;    // 3 x double2 per node: xx yy | zz xy | xz yz
@@ -500,8 +566,9 @@ __device__ void leaf_moments(const MomentArrays &a, u32 p) {  // octree.cpp:46-7
 
 __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-102
   const Dbl4 g = load_pair(a.geom, p);
-  u32 ch[8];
-  const int nc = children_of(p, a.skip, ch);  // last octant first
+  const uint4 k0 = a.kids[2ull * p], k1 = a.kids[2ull * p + 1];
+  const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};  // last octant first
+  const int nc = a.nchild[p];
   double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
   for (int j = nc - 1; j >= 0; --j) {
     const Dbl4 c = load_pair(a.mom, ch[j]);
@@ -625,23 +692,37 @@ __global__ void __launch_bounds__(kT)
   if (k < count) leaf_moments(a, bucket[k]);
 }
 
-__global__ void __launch_bounds__(kT)
-    k_node_moments(MomentArrays a, const u32 *bucket, u32 count) {
-  const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k < count) node_moments(a, bucket[k]);
+// Inner-node moments of one depth: one warp per block, `per` nodes to a
+// warp (lanes past it idle). A depth with few nodes spreads them over many
+// SMs: the sums are FP64-bound, and one SM's FP64 rate took ~40 us for a
+// block of 256 nodes whatever the depth.
+constexpr int kMomentWarps = 1216;  // warps a depth is spread over (8 per SM)
+
+__host__ __device__ __forceinline__ u32 nodes_per_warp(u32 count) {
+  const u32 per = (count + kMomentWarps - 1) / kMomentWarps;
+  return per < 1 ? 1u : (per > 32 ? 32u : per);
 }
 
-// A graph replay's moments of the nb consecutive buckets from b0: the
-// counts and offset from the device (meta = count[kBuckets],
-// offset[kBuckets]), grid-stride.
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(32)
+    k_node_moments(MomentArrays a, const u32 *bucket, u32 count, u32 per) {
+  const u32 lane = threadIdx.x;
+  const u64 k = static_cast<u64>(blockIdx.x) * per + lane;
+  if (lane < per && k < count) node_moments(a, bucket[k]);
+}
+
+// The same for a graph replay, over the device counts of buckets
+// [b0, b0 + nb) (leaves or one depth's inner nodes), grid-stride.
+__global__ void __launch_bounds__(32)
     k_moments_graph(MomentArrays a, const u32 *bucket, const u32 *meta, int b0, int nb,
                     const u32 *abort) {
   if (*abort) return;
   u32 count = 0;
   for (int b = b0; b < b0 + nb; ++b) count += meta[b];
   const u32 off = meta[kBuckets + b0];
-  for (u32 k = blockIdx.x * kT + threadIdx.x; k < count; k += gridDim.x * kT) {
+  const u32 per = nodes_per_warp(count);
+  if (threadIdx.x >= per) return;
+  for (u64 k = static_cast<u64>(blockIdx.x) * per + threadIdx.x; k < count;
+       k += static_cast<u64>(gridDim.x) * per) {
     if (b0 >= kLeafBucket) leaf_moments(a, bucket[off + k]);
     else node_moments(a, bucket[off + k]);
   }
@@ -788,7 +869,12 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny, &sc->error);
+  ws.split.ensure(3ull * kSplitSize * sizeof(double));
+  k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 256), 256, 0, s>>>(root, ws.split.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
   radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
 
@@ -888,8 +974,9 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                             ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                             ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>());
   GTC_LAUNCH_CHECK();
+  ws.kids.ensure(static_cast<u64>(m) * 8 * sizeof(u32));
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, ws.parent.as<u32>(),
-                               ws.nchild.as<u8>());
+                               ws.nchild.as<u8>(), ws.kids.as<uint4>());
   GTC_LAUNCH_CHECK();
   k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), m, idx);
   GTC_LAUNCH_CHECK();
@@ -915,7 +1002,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   std::memcpy(counts, host_meta(ws), sizeof counts);
   MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
-                  ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
+                  ws.kids.as<uint4>(), ws.tpos.as<double>(), ws.tmass.as<double>(),
+                  ws.mom.as<double2>(),
                   ws.quad.as<double2>(), ws.delta.as<double>()};
   auto range = [&](int b0, int nb, u32 &c, u32 &o) {
     c = 0;
@@ -932,7 +1020,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     u32 c, o;
     range(d * kSizeClasses, kSizeClasses, c, o);
     if (!c) continue;
-    k_node_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
+    const u32 per = nodes_per_warp(c);
+    k_node_moments<<<ceil_div(c, per), 32, 0, s>>>(ma, bucket + o, c, per);
     GTC_LAUNCH_CHECK();
   }
   k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
@@ -961,7 +1050,12 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, key0, idx, tiny, &sc->error);
+  ws.split.ensure(3ull * kSplitSize * sizeof(double));
+  k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 256), 256, 0, s>>>(root, ws.split.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
   radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
   const KeyView kv{key0, nullptr, nullptr, 1};
@@ -981,7 +1075,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
                             ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), abort);
   GTC_LAUNCH_CHECK();
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, ws.parent.as<u32>(),
-                               ws.nchild.as<u8>(), m_dev, abort);
+                               ws.nchild.as<u8>(), ws.kids.as<uint4>(), m_dev, abort);
   GTC_LAUNCH_CHECK();
   k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), mcap,
                                  idx, m_dev, abort);
@@ -1003,16 +1097,18 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
   MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
-                  ws.tpos.as<double>(), ws.tmass.as<double>(), ws.mom.as<double2>(),
+                  ws.kids.as<uint4>(), ws.tpos.as<double>(), ws.tmass.as<double>(),
+                  ws.mom.as<double2>(),
                   ws.quad.as<double2>(), ws.delta.as<double>()};
   int dev = 0, sms = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const u32 gb = std::min<u32>(mb, static_cast<u32>(std::max(1, 8 * sms)));
-  k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
+  k_moments_graph<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
   GTC_LAUNCH_CHECK();
   for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
-    k_moments_graph<<<gb, kT, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses, abort);
+    k_moments_graph<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses,
+                                                abort);
     GTC_LAUNCH_CHECK();
   }
   k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
