@@ -256,20 +256,24 @@ __global__ void __launch_bounds__(kT)
   const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
   const long long maybe_tiny =
       __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
+  // the first level whose node could be tiny for this body (half_at falls
+  // with depth): the levels above it need no tiny test at all
+  int dt = 0;
+  while (dt <= kLevelsPerWord && __double_as_longlong(half_at[dt]) >= maybe_tiny) ++dt;
   const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
   u32 ix = 1, iy = 1, iz = 1;
   double cx = 0.0, cy = 0.0, cz = 0.0;
   u64 k = 0;
   int t = kNoTiny;
-  for (int d = 0; d < kLevelsPerWord; ++d) {
+  // level d: its centre (table, or stepped below the table), the tiny test
+  // where it can apply, the digit, and the next level's index or centre
+  auto level = [&](int d, bool test) {
     if (d < kSplitLevels) {
       cx = __ldg(tx + ix);
       cy = __ldg(ty + iy);
       cz = __ldg(tz + iz);
     }
-    if (t == kNoTiny && __double_as_longlong(half_at[d]) < maybe_tiny &&
-        tiny_node(half_at[d], cx, cy, cz))
-      t = d;
+    if (test && t == kNoTiny && tiny_node(half_at[d], cx, cy, cz)) t = d;
     int o = (kx >= order_key(cx) ? 1 : 0) | (ky >= order_key(cy) ? 2 : 0) |
             (kz >= order_key(cz) ? 4 : 0);
     if (t != kNoTiny) o = 0;
@@ -281,8 +285,12 @@ __global__ void __launch_bounds__(kT)
     } else {
       step_centre(cx, cy, cz, o, half_at[d + 1]);
     }
-  }
-  if (t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz)) t = kLevelsPerWord;
+  };
+  int d = 0;
+  for (; d < kLevelsPerWord && d < dt; ++d) level(d, false);
+  for (; d < kLevelsPerWord; ++d) level(d, true);
+  if (dt <= kLevelsPerWord && t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz))
+    t = kLevelsPerWord;
   key[i] = k;
   idx[i] = i;
   tiny[i] = static_cast<u8>(t);
@@ -408,9 +416,9 @@ __global__ void __launch_bounds__(kT)
 // Writes the nodes ending at sorted position b, shallowest first.
 __global__ void __launch_bounds__(kT)
     k_nodes(KeyView kv, const signed char *lcp_next, const u8 *leafdepth, const u32 *count,
-            const u32 *count_scan, u32 n, const Scalars *sc, const TreeRoot *root, double2 *geom,
-            u32 *nbegin, u32 *nend, u32 *skip, u8 *depth, u8 *isleaf,
-            const u32 *abort = nullptr) {
+            const u32 *count_scan, u32 n, const Scalars *sc, const TreeRoot *root,
+            const double *split, double2 *geom, u32 *nbegin, u32 *nend, u32 *skip, u8 *depth,
+            u8 *isleaf, const u32 *abort = nullptr) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
   if (b >= n || aborted(abort)) return;
   const u32 c = count[b];
@@ -418,10 +426,32 @@ __global__ void __launch_bounds__(kT)
   const u32 total = sc->n_nodes;
   const u32 first = total - count_scan[b] - c;  // nodes ending after b come first
   const int d0 = lcp_next[b] + 1, ld = leafdepth[b];
-  double cx = root->center[0], cy = root->center[1], cz = root->center[2];
+  // centres from the split table down to its last level, stepped below it
+  const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
+  u32 ix = 1, iy = 1, iz = 1;
+  double cx = 0.0, cy = 0.0, cz = 0.0;
   for (int d = 0; d <= ld; ++d) {
-    if (d > 0) step_centre(cx, cy, cz, digit(kv, b, d), root->half_at[d]);
+    if (d > 0) {
+      const int o = digit(kv, b, d);
+      if (d < kSplitLevels) {
+        ix = 2 * ix + (o & 1);
+        iy = 2 * iy + ((o >> 1) & 1);
+        iz = 2 * iz + (o >> 2);
+      } else {
+        if (d == kSplitLevels) {  // the table's deepest centre on this path
+          cx = __ldg(tx + ix);
+          cy = __ldg(ty + iy);
+          cz = __ldg(tz + iz);
+        }
+        step_centre(cx, cy, cz, o, root->half_at[d]);
+      }
+    }
     if (d < d0) continue;
+    if (d < kSplitLevels) {
+      cx = __ldg(tx + ix);
+      cy = __ldg(ty + iy);
+      cz = __ldg(tz + iz);
+    }
     const u32 p = first + static_cast<u32>(d - d0);
     // first body of the node: smallest b0 sharing d levels with b
     u32 lo = 0, hi = b;
@@ -971,7 +1001,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   const u32 mb = ceil_div(m, kT);
 
   k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
-                            ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                            ws.split.as<double>(), ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                             ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>());
   GTC_LAUNCH_CHECK();
   ws.kids.ensure(static_cast<u64>(m) * 8 * sizeof(u32));
@@ -1071,7 +1101,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
   const u32 *m_dev = &sc->n_nodes;
   k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
-                            ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                            ws.split.as<double>(), ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                             ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), abort);
   GTC_LAUNCH_CHECK();
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, ws.parent.as<u32>(),
