@@ -249,7 +249,8 @@ def measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, r
             "network_rows": st["mlp_rows"], "network_batches": st["mlp_batches"],
             "alpha": alpha, "band": float(model[-1]),
             "model": "galactic-tides_gb300/criterion_model.f32 (6-64-64-1, BF16 inference)",
-            "alpha_source": "largest alpha with p99 <= plain theta=0.75 on a 2M galaxy of seed 7",
+            "alpha_source": ("band and alpha calibrated on a 2M galaxy of seed 7: per band the "
+                             "largest alpha with p99 <= plain theta=0.75, then the fastest pair"),
             "gpu_launches": sum(s["kernel_launches"] for s in stats)}
 
 

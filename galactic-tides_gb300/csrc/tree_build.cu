@@ -214,9 +214,10 @@ __global__ void __launch_bounds__(1024) k_split_top(const TreeRoot *root, double
 
 // Levels kSplitTop..kSplitLevels - 1: one thread per node of level
 // kSplitTop - 1 builds its subtree, level by level.
-__global__ void __launch_bounds__(256) k_split_rest(const TreeRoot *root, double *split) {
+// (One warp per block: the subtrees spread over the SMs' FP64 units.)
+__global__ void __launch_bounds__(32) k_split_rest(const TreeRoot *root, double *split) {
   const u32 per_axis = 1u << (kSplitTop - 1);
-  const u32 tid = blockIdx.x * 256 + threadIdx.x;
+  const u32 tid = blockIdx.x * 32 + threadIdx.x;
   if (tid >= 3 * per_axis) return;
   const int axis = static_cast<int>(tid / per_axis);
   double *t = split + static_cast<u64>(axis) * kSplitSize;
@@ -902,7 +903,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   ws.split.ensure(3ull * kSplitSize * sizeof(double));
   k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
   GTC_LAUNCH_CHECK();
-  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 256), 256, 0, s>>>(root, ws.split.as<double>());
+  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 32), 32, 0, s>>>(root, ws.split.as<double>());
   GTC_LAUNCH_CHECK();
   k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
@@ -1083,7 +1084,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   ws.split.ensure(3ull * kSplitSize * sizeof(double));
   k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
   GTC_LAUNCH_CHECK();
-  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 256), 256, 0, s>>>(root, ws.split.as<double>());
+  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 32), 32, 0, s>>>(root, ws.split.as<double>());
   GTC_LAUNCH_CHECK();
   k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();

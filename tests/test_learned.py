@@ -226,6 +226,9 @@ def test_fallback_then_learned_lists_are_valid(gtc):
 
 @gpu
 def test_band_only_skips_the_network_where_it_cannot_change_the_decision(gtc):
+    """The training band (the 0.99 quantile of the network's correction)
+    leaves to the prior only tests the network would decide the same way."""
+    train_band = json.loads(MODEL_INFO.read_text())["training_band"]
     pos, _, mass, _ = gtc.make_galaxy(100_000, seed=6)
     kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
     with _learned_ctx(gtc) as c:
@@ -233,13 +236,38 @@ def test_band_only_skips_the_network_where_it_cannot_change_the_decision(gtc):
         c.set_option("learned_band", 1e6)  # the network decides every guarded test
         full, _ = c.group_force(pos, mass, **kw)
         s_full = c.stats()
-        c.set_option("learned_band", -1)  # the model's band
+        c.set_option("learned_band", train_band)
         band, _ = c.group_force(pos, mass, **kw)
         s_band = c.stats()
     assert s_band["mlp_rows"] < s_full["mlp_rows"]
     tot = lambda s: s["cell_interactions"] + s["body_interactions"]
     assert abs(tot(s_band) / tot(s_full) - 1) < 0.01
     assert np.median(rel_errors(band, full)) < 1e-6
+
+
+@gpu
+def test_model_band_is_the_calibrated_one(gtc):
+    """The committed model carries the band its calibration chose (a
+    narrower one than the training band: the network decides fewer tests,
+    the prior more), and the model's own band is the default."""
+    info = json.loads(MODEL_INFO.read_text())
+    model = np.fromfile(MODEL, dtype="<f4")
+    assert model[-1] == np.float32(info["band_calibration"]["chosen"]["band"])
+    assert info["alpha"] == info["band_calibration"]["chosen"]["alpha"]
+    assert model[-1] <= info["training_band"]
+    pos, _, mass, _ = gtc.make_galaxy(100_000, seed=6)
+    kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
+    runs = {}
+    for name, band in (("default", None), ("model", float(model[-1])),
+                       ("training", info["training_band"])):
+        with _learned_ctx(gtc) as c:  # the same call history in each context
+            if band is not None:
+                c.set_option("learned_band", band)
+            c.group_force(pos, mass, **kw)
+            acc, _ = c.group_force(pos, mass, **kw)
+            runs[name] = (acc, c.stats())
+    assert np.array_equal(runs["default"][0], runs["model"][0])
+    assert runs["default"][1]["mlp_rows"] <= runs["training"][1]["mlp_rows"]
 
 
 @gpu
