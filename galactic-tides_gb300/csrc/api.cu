@@ -162,6 +162,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.G = sp.G;
     lw.inv_theta_guard = static_cast<float>(1.0 / ctx->guard_theta);
     lw.band = ctx->band_override >= 0 ? static_cast<float>(ctx->band_override) : ctx->model_band;
+    gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, s);
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
     gtc::build_lists(ws, sp, s, ctx->host_sc);
@@ -215,6 +216,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   st.criterion_used = learned ? GTC_CRITERION_LEARNED : GTC_CRITERION_THETA;
   st.list_passes = ws.list_passes;
   st.spilled_groups = n > 0 ? ctx->host_sc->spilled : 0;
+  st.walk_nodes = n > 0 ? ctx->host_sc->walk_nodes : 0;
   ctx->prev_n = ctx->have_model ? n : 0;
   st.n_cell_list = ws.n_cell_list;
   st.n_body_list = ws.n_body_list;
@@ -372,6 +374,7 @@ struct GraphStep {
     st.criterion_used = GTC_CRITERION_THETA;
     st.list_passes = 1;
     st.spilled_groups = hs.spilled;
+    st.walk_nodes = hs.walk_nodes;
     st.kernel_launches = 0;  // one graph launch (its kernels were counted at capture)
     st.graph_steps = replays + 1;
     ctx->have_group = true;

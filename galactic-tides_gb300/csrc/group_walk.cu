@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(kT)
     cl = out.cell_list + out.spill_cells[g];
     bl = out.body_list + out.spill_bodies[g];
   }
-  u32 nc = 0, nb = 0, exact = 0;
+  u32 nc = 0, nb = 0, exact = 0, visits = 0;
   const Task task = tasks[t];
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(kT)
   };
   bool enter = true;
   if (task.anc != kNone) {
+    ++visits;
     const WalkRec32 a = load32(walk32, task.anc);
     if (decide(a, walk64, task.anc, gf, hf, gbound, gbox, g, exact) == 1) {
       if (task.first) take(a, task.anc, 1);
@@ -322,6 +323,7 @@ __global__ void __launch_bounds__(kT)
     const u32 end = load32(walk32, task.root).skip;
     while (i < end) {
       const WalkRec32 r = load32(walk32, i);
+      ++visits;
       const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
       if (verdict == 1 || (r.nbody_leaf >> 31)) {
         take(r, i, verdict);
@@ -339,6 +341,11 @@ __global__ void __launch_bounds__(kT)
     out.ncells[slot] = nc;
     out.nbodies[slot] = nb;
     if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
+    // visited nodes: one atomic per set of converged lanes
+    const unsigned mask = __activemask();
+    const u32 sum = __reduce_add_sync(mask, visits);
+    if ((threadIdx.x & 31) == static_cast<unsigned>(__ffs(mask) - 1))
+      atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(sum));
   }
   if (kMode == kSlots) {
     u32 oc = kNoSpill, ob = kNoSpill;
@@ -465,6 +472,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u32 gs = static_cast<u32>(sp.group_size);
   Scalars *sc = ws.scalars.as<Scalars>();
   GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
   ws.flags.ensure(std::max<u64>(n, m) * 4);
   ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
   u32 *mark = ws.flags.as<u32>(), *mscan = ws.flags_scan.as<u32>();
@@ -564,6 +572,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
       return;
     }
     // the pools were too small: the counters start again for the two passes
+    GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
@@ -634,6 +643,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
   u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + n;
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
              ws.cell_list.as<u32>(), ws.body_list.as<u32>(), caps.slot_cells, caps.slot_bodies,

@@ -74,6 +74,27 @@ __device__ __forceinline__ float prior_log2err(float node_prior, float f2) {
   return node_prior - 5.f * f2;
 }
 
+// The learned walk's node record, 48 bytes (one record, one array per
+// visited node): the overlap test's centre and slack and the centre of mass
+// (the walk records' FP32 values), the guard's (2 h / theta_guard + delta)^2,
+// the links and the node's part of the centred prior as a distance scale.
+//
+// The centred prior of a (group, cell) pair is
+//   e = prior + y_mean - 5 f2,  f2 = log2(d / L),
+// so the walk's tests e < tau - band (accept) and e > tau + band (open) are
+// tests on d^2 alone:
+//   accept  d^2 > pscale * 2^(0.4 (band - tau)) L^2,
+//   open    d^2 < pscale * 2^(0.4 (-band - tau)) L^2,
+// with pscale = 2^(0.4 (prior + y_mean)) per node and the rest per group:
+// no square root or logarithm per visited node.
+struct alignas(16) LWalkRec {
+  float cx, cy, cz, slack;
+  float mx, my, mz, guard2;
+  u32 skip, nbody_leaf, begin;
+  float pscale;
+};
+static_assert(sizeof(LWalkRec) == 48, "three float4 loads");
+
 // Training set held by the context.
 struct LearnedSet {
   DeviceBuffer feat;    // kFeat floats per sample
@@ -99,10 +120,11 @@ struct LearnedScratch {
   DeviceBuffer regions, lane_fill;  // the lanes' list regions and how full they are
   DeviceBuffer gstart, pcount, poff, base;
   DeviceBuffer q[2], dec[2];        // deferred pairs and the network's decisions
+  DeviceBuffer lrec;                // per node: the walk's record (LWalkRec)
   u64 items_cap = 0;
   u32 lane_cells = 2048, lane_runs = 512, lane_pend = 512;  // grown when outgrown
   void release() {
-    for (DeviceBuffer *b : {&seg, &regions, &lane_fill, &gstart, &pcount, &poff, &base, &q[0],
+    for (DeviceBuffer *b : {&seg, &regions, &lane_fill, &gstart, &pcount, &poff, &base, &lrec, &q[0],
                             &q[1], &dec[0], &dec[1]})
       b->release();
     items_cap = 0;
@@ -125,6 +147,10 @@ struct LearnedWalk {
 
 // Per-node features (after build_tree).
 void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s);
+// The walk's per-node records (LWalkRec) from the walk records and the node
+// features, for the guard angle 1 / inv_theta_guard and the model's y_mean.
+void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lrec,
+                          float inv_theta_guard, float y_mean, cudaStream_t s);
 // Per-group group feature and tolerance (inside build_lists, after the group boxes).
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s);
 // The learned walk over the groups' path-split items in rounds, then the gather: GTGroup records, cell_list, body_list and the interaction

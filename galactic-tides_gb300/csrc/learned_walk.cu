@@ -172,6 +172,30 @@ __global__ void __launch_bounds__(kT)
                          static_cast<float>(qn), static_cast<float>(delta[p]), fs);
 }
 
+__global__ void __launch_bounds__(kT)
+    k_lwalk_rec(const WalkRec32 *walk32, const CellFeat *cfeat, u32 m, float inv_theta_guard,
+                float y_mean, LWalkRec *out) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  const WalkRec32 w = walk32[p];
+  const float4 c0 = reinterpret_cast<const float4 *>(cfeat + p)[0];
+  const float crit = fmaf(2.f * c0.x, inv_theta_guard, c0.y);
+  LWalkRec r;
+  r.cx = w.cx;
+  r.cy = w.cy;
+  r.cz = w.cz;
+  r.slack = w.slack;
+  r.mx = w.mx;
+  r.my = w.my;
+  r.mz = w.mz;
+  r.guard2 = crit * crit;
+  r.skip = w.skip;
+  r.nbody_leaf = w.nbody_leaf;
+  r.begin = w.begin;
+  r.pscale = exp2f(0.4f * (c0.z + y_mean));
+  out[p] = r;
+}
+
 // Per group: the group feature f0 and the tolerance
 // tau = log2(alpha * a_g * L^2 / (G M_tot)), with the group's force scale
 // a_g = max(min |a_prev|, mean |a_prev| / 2) over its targets. The floor
@@ -253,6 +277,7 @@ constexpr int kMaxRounds = kMaxDepth + 4;
 struct LArgs {
   const WalkRec32 *walk32;
   const CellFeat *cfeat;
+  const LWalkRec *lrec;
   const float *gboxf;
   const float2 *gtol;
   u32 ng;
@@ -286,10 +311,12 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
   Scalars *sc = a.sc;
 
   u64 item = kNoItem, store = 0;
-  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0, grp = 0;
+  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0, grp = 0, visits = 0;
   int pre = -1;  // the network's decision on a deferred item's node
   bool exhausted = false;
-  float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f}, tau = 0.f;
+  float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f};
+  float acc_d2 = 0.f, open_d2 = 0.f;  // the item's group: d^2 scales of the accept and open tests
+  const float l2 = 1.f / (fs.inv_l * fs.inv_l);
   while (true) {
     // idle lanes take the next items (one atomic per warp)
     const bool want = item == kNoItem && !exhausted;
@@ -312,7 +339,7 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
           i = q.y;
           store = k;
           pre = a.qdec ? a.qdec[k] : -1;
-          end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.walk32 + i) + 2).x);
+          end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.lrec + i) + 2).x);
           const float4 b0 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g],
                        b1 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g + 1];
           gf[0] = b0.x;
@@ -321,7 +348,9 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
           hf[0] = b0.w;
           hf[1] = b1.x;
           hf[2] = b1.y;
-          tau = a.gtol[g].y;
+          const float tau = a.gtol[g].y;
+          acc_d2 = exp2f(0.4f * (a.band - tau)) * l2;
+          open_d2 = exp2f(0.4f * (-a.band - tau)) * l2;
           c0i = lc;
           r0i = lr;
           p0i = lp;
@@ -332,14 +361,28 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
     if (__ballot_sync(kFullMask, item != kNoItem) == 0) break;
     if (item == kNoItem) continue;  // the lanes meet again at the next ballot
 
-    const WalkRec32 r = load_rec(a.walk32, i);
+    const float4 *rp = reinterpret_cast<const float4 *>(a.lrec + i);
+    const float4 ra = __ldg(rp), rb = __ldg(rp + 1), rc = __ldg(rp + 2);
+    LWalkRec r;
+    r.cx = ra.x;
+    r.cy = ra.y;
+    r.cz = ra.z;
+    r.slack = ra.w;
+    r.mx = rb.x;
+    r.my = rb.y;
+    r.mz = rb.z;
+    r.guard2 = rb.w;
+    r.skip = __float_as_uint(rc.x);
+    r.nbody_leaf = __float_as_uint(rc.y);
+    r.begin = __float_as_uint(rc.z);
+    r.pscale = rc.w;
+    ++visits;
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
     int verdict;  // 0 open, 1 accept, 2 defer
     if (pre >= 0) {
       verdict = pre;
       pre = -1;
     } else {
-      const float4 c0 = __ldg(reinterpret_cast<const float4 *>(a.cfeat + i));
       // the reference's overlap test (group_lists.cpp:147), in FP32
       const bool overlap = fabsf(r.cx - gf[0]) <= r.slack + hf[0] &&
                            fabsf(r.cy - gf[1]) <= r.slack + hf[1] &&
@@ -348,14 +391,12 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
                   dy = fmaxf(fabsf(r.my - gf[1]) - hf[1], 0.f),
                   dz = fmaxf(fabsf(r.mz - gf[2]) - hf[2], 0.f);
       const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      const float crit = fmaf(2.f * c0.x, a.inv_theta_guard, c0.y);
-      if (overlap || !(d2 > crit * crit)) {
+      if (overlap || !(d2 > r.guard2)) {
         verdict = 0;
       } else if (nbody <= kFewBodies) {
         verdict = 1;
       } else {
-        const float e = prior_log2err(c0.z, distance_feature(d2, fs)) + a.y_mean;
-        verdict = e < tau - a.band ? 1 : e > tau + a.band ? 0 : 2;
+        verdict = d2 > r.pscale * acc_d2 ? 1 : d2 < r.pscale * open_d2 ? 0 : 2;
       }
     }
     if (verdict == 2) {
@@ -390,6 +431,7 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
       item = kNoItem;
     }
   }
+  warp_add(&sc->walk_nodes, visits);  // the lanes leave the loop together
   a.lane_fill[3 * gtid] = lc;
   a.lane_fill[3 * gtid + 1] = lr;
   a.lane_fill[3 * gtid + 2] = lp;
@@ -652,6 +694,16 @@ void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s) {
   GTC_LAUNCH_CHECK();
 }
 
+void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lrec,
+                          float inv_theta_guard, float y_mean, cudaStream_t s) {
+  const u32 m = static_cast<u32>(ws.n_nodes);
+  if (m == 0) return;
+  lrec.ensure(static_cast<u64>(m) * sizeof(LWalkRec));
+  k_lwalk_rec<<<ceil_div(m, kT), kT, 0, s>>>(ws.walk32.as<WalkRec32>(), cfeat, m, inv_theta_guard,
+                                             y_mean, lrec.as<LWalkRec>());
+  GTC_LAUNCH_CHECK();
+}
+
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s) {
   if (ng == 0) return;
   lw.gtol->ensure(static_cast<u64>(ng) * sizeof(float2));
@@ -683,6 +735,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   LArgs a{};
   a.walk32 = ws.walk32.as<WalkRec32>();
   a.cfeat = lw.cfeat;
+  a.lrec = ls.lrec.as<LWalkRec>();
   a.gboxf = ws.gboxf.as<float>();
   a.gtol = lw.gtol->as<float2>();
   a.ng = ng;

@@ -115,6 +115,7 @@ struct Scalars {
   u32 max_cells, max_bodies;  // longest cell and body list of a group
   unsigned long long spill_used[2];  // one-pass walk: overflow pool entries taken (cells, bodies)
   u32 spilled;            // one-pass walk: groups that outgrew their slots
+  unsigned long long walk_nodes;  // node records the walk tested
 };
 
 // The list statistics of one group per lane (valid lanes), summed and
@@ -151,6 +152,14 @@ __device__ __forceinline__ void group_stats_warp(Scalars *sc, bool valid, u64 t,
     atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_cell_list), tc);
     atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_body_list), tb);
   }
+}
+
+// Adds each lane's count to *total with one atomic per warp (every lane of
+// the warp must call it).
+__device__ __forceinline__ void warp_add(unsigned long long *total, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFullMask, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(total, v);
 }
 
 // Stage 1: octree on the device. pos (N x 3) and mass in caller order.

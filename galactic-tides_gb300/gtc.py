@@ -63,7 +63,8 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_uint64), ("walk_tests_fp64", C.c_uint64),
                 ("mlp_rows", C.c_uint64), ("mlp_batches", C.c_uint64),
                 ("criterion_used", C.c_uint32), ("graph_steps", C.c_uint32),
-                ("list_passes", C.c_uint32), ("spilled_groups", C.c_uint32)]
+                ("list_passes", C.c_uint32), ("spilled_groups", C.c_uint32),
+                ("walk_nodes", C.c_uint64)]
 
 
 NODE_DTYPE = np.dtype([
@@ -72,7 +73,7 @@ NODE_DTYPE = np.dtype([
     ("parent", "<u4"), ("depth", "<i4"), ("n_children", "<i4")])
 assert NODE_DTYPE.itemsize == 144
 
-assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 144
+assert C.sizeof(GravityParams) == 56 and C.sizeof(KernelParams) == 32 and C.sizeof(Stats) == 152
 
 # Learned criterion model: W1[6][64], b1[64], W2[64][64], b2[64], W3[64], b3,
 # then feature mean[6], std[6], y_mean, y_std, band (include/gtc.h).

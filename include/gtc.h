@@ -127,6 +127,7 @@ typedef struct gtc_stats {
                                  slots, 2 count then fill, learned: the walk's rounds */
   uint32_t spilled_groups;    /* one-pass walk: groups whose lists outgrew their slots and
                                  were written again into the overflow pools */
+  uint64_t walk_nodes;        /* node records the walk tested (every round of the learned walk) */
 } gtc_stats;
 
 /* Creates a context on CUDA device `device` (GTC_NO_DEVICE if there is
