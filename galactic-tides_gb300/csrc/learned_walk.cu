@@ -272,6 +272,7 @@ __device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
 // deferred pairs keep their items' order), with each group's range kept
 // per round.
 constexpr u64 kNoItem = ~0ull;
+constexpr int kGrabLanes = 8;
 constexpr int kMaxRounds = kMaxDepth + 4;
 
 struct LArgs {
@@ -318,10 +319,13 @@ __global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
   float acc_d2 = 0.f, open_d2 = 0.f;  // the item's group: d^2 scales of the accept and open tests
   const float l2 = 1.f / (fs.inv_l * fs.inv_l);
   while (true) {
-    // idle lanes take the next items (one atomic per warp)
+    // idle lanes take the next items (one atomic per warp), once at least
+    // kGrabLanes of them wait or no lane has work: the grab runs with its
+    // lanes together instead of for one or two lanes every step
     const bool want = item == kNoItem && !exhausted;
     const unsigned wantm = __ballot_sync(kFullMask, want);
-    if (wantm) {
+    const unsigned busym = __ballot_sync(kFullMask, item != kNoItem);
+    if (wantm && (__popc(wantm) >= kGrabLanes || busym == 0)) {
       const int leader = __ffs(wantm) - 1;
       unsigned long long base = 0;
       if (lane == leader)
