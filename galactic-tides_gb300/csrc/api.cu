@@ -292,7 +292,7 @@ struct GraphStep {
     ws.gbodies.ensure(n * 8);
     ws.gcell_off.ensure((n + 1) * 8);
     ws.gbody_off.ensure((n + 1) * 8);
-    ws.groups.ensure(n * 32);
+    ws.groups.ensure(n * gtc::kGroupRecWords * 4);
     ws.cell_list.ensure((static_cast<u64>(caps.groups) * caps.slot_cells + caps.pool_cells) * 4);
     ws.body_list.ensure((static_cast<u64>(caps.groups) * caps.slot_bodies + caps.pool_bodies) * 4);
     ws.spill.ensure(2 * n * sizeof(u32));
@@ -700,14 +700,22 @@ gtc_status gtc_tree(gtc_context *ctx, const gtc_float4 *bodies, const gtc_cell *
     ws.cells.ensure(std::max<u64>(1, n_cells) * 48);
     ws.cell_list.ensure(std::max<u64>(1, n_cell_list) * 4);
     ws.body_list.ensure(std::max<u64>(1, n_body_list) * 4);
-    ws.groups.ensure(ng * 32);
+    ws.groups.ensure(ng * gtc::kGroupRecWords * 4);
     GTC_CUDA(cudaMemcpyAsync(ws.bodies.ptr, bodies, n * 16, cudaMemcpyHostToDevice, s));
     if (n_cells) GTC_CUDA(cudaMemcpyAsync(ws.cells.ptr, cells, n_cells * 48ull, cudaMemcpyHostToDevice, s));
     if (n_cell_list)
       GTC_CUDA(cudaMemcpyAsync(ws.cell_list.ptr, cell_list, n_cell_list * 4, cudaMemcpyHostToDevice, s));
     if (n_body_list)
       GTC_CUDA(cudaMemcpyAsync(ws.body_list.ptr, body_list, n_body_list * 4, cudaMemcpyHostToDevice, s));
-    GTC_CUDA(cudaMemcpyAsync(ws.groups.ptr, groups, ng * 32, cudaMemcpyHostToDevice, s));
+    std::vector<uint4> rec(4 * ng);
+    for (u64 g = 0; g < ng; ++g) {
+      const gtc_group &G = groups[g];
+      gtc::store_group_rec(rec.data(), g, G.begin, G.end,
+                           gtc::one_segment(G.cell_begin, G.cell_end - G.cell_begin),
+                           gtc::one_segment(G.body_begin, G.body_end - G.body_begin));
+    }
+    GTC_CUDA(cudaMemcpyAsync(ws.groups.ptr, rec.data(), ng * 64, cudaMemcpyHostToDevice, s));
+    GTC_CUDA(cudaStreamSynchronize(s));  // rec is released at the end of scope
     GTC_CUDA(cudaMemsetAsync(ws.out.ptr, 0, n * 16, s));
     ctx->counter.ensure(sizeof(u32));
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
@@ -1295,41 +1303,46 @@ gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
     }
     get(bodies, ws.bodies, n * 16);
     get(cells, ws.cells, m * 48);
-    if (ws.gapped && (groups || cell_list || body_list)) {
-      // one-pass lists sit in per-group slots: exported back to back
+    if (groups || cell_list || body_list) {
+      // the lists as the reference lays them out: each group's segments
+      // concatenated, the groups back to back
       const u64 ng = ws.n_groups;
-      std::vector<uint4> rec(2 * ng);
-      get(rec.data(), ws.groups, ng * 32);
+      std::vector<uint4> rec(4 * ng);
+      get(rec.data(), ws.groups, ng * 64);
       u64 cext = 0, bext = 0;
       for (u64 g = 0; g < ng; ++g) {
-        cext = std::max<u64>(cext, rec[2 * g].w);
-        bext = std::max<u64>(bext, rec[2 * g + 1].y);
+        const gtc::SegView c = gtc::cell_segs(rec[4 * g + 1], rec[4 * g + 2]);
+        const gtc::SegView b = gtc::body_segs(rec[4 * g + 2], rec[4 * g + 3]);
+        const uint4 q3 = rec[4 * g + 3];
+        cext = std::max<u64>({cext, u64{c.s0} + c.n0, u64{c.s1} + c.n1,
+                              u64{c.s2} + rec[4 * g + 2].y});
+        bext = std::max<u64>({bext, u64{b.s0} + b.n0, u64{b.s1} + b.n1, u64{b.s2} + q3.w});
       }
       std::vector<u32> cl(cell_list ? cext : 0), bl(body_list ? bext : 0);
       get(cl.data(), ws.cell_list, cl.size() * 4);
       get(bl.data(), ws.body_list, bl.size() * 4);
       u64 c = 0, b = 0;
       for (u64 g = 0; g < ng; ++g) {
-        const uint4 ra = rec[2 * g], rb = rec[2 * g + 1];
-        if (cell_list) std::copy(cl.begin() + ra.z, cl.begin() + ra.w, cell_list + c);
-        if (body_list) std::copy(bl.begin() + rb.x, bl.begin() + rb.y, body_list + b);
+        const uint4 q0 = rec[4 * g];
+        const gtc::SegView cs = gtc::cell_segs(rec[4 * g + 1], rec[4 * g + 2]);
+        const gtc::SegView bs = gtc::body_segs(rec[4 * g + 2], rec[4 * g + 3]);
+        if (cell_list)
+          for (u32 e = 0; e < q0.z; ++e) cell_list[c + e] = cl[cs.at(e)];
+        if (body_list)
+          for (u32 e = 0; e < q0.w; ++e) body_list[b + e] = bl[bs.at(e)];
         if (groups) {
           gtc_group &o = groups[g];
-          o.begin = ra.x;
-          o.end = ra.y;
+          o.begin = q0.x;
+          o.end = q0.y;
           o.cell_begin = static_cast<uint32_t>(c);
-          o.cell_end = static_cast<uint32_t>(c + (ra.w - ra.z));
+          o.cell_end = static_cast<uint32_t>(c + q0.z);
           o.body_begin = static_cast<uint32_t>(b);
-          o.body_end = static_cast<uint32_t>(b + (rb.y - rb.x));
+          o.body_end = static_cast<uint32_t>(b + q0.w);
           o.pad0 = o.pad1 = 0;
         }
-        c += ra.w - ra.z;
-        b += rb.y - rb.x;
+        c += q0.z;
+        b += q0.w;
       }
-    } else {
-      get(groups, ws.groups, ws.n_groups * 32);
-      get(cell_list, ws.cell_list, ws.n_cell_list * 4);
-      get(body_list, ws.body_list, ws.n_body_list * 4);
     }
     get(out, ws.out, n * 16);
   });

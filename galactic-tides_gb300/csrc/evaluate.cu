@@ -93,31 +93,33 @@ __global__ void __launch_bounds__(kT)
     if (lane == 0) g = atomicAdd(next_group, 1u);
     g = __shfl_sync(kFullMask, g, 0);
     if (g >= ngroups) return;
-    const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
+    const uint4 q0 = groups[4ull * g], q1 = groups[4ull * g + 1], q2 = groups[4ull * g + 2],
+                q3 = groups[4ull * g + 3];
+    const SegView cs = cell_segs(q1, q2), bs = body_segs(q2, q3);  // list entry -> index
     // A group of T <= 16 targets splits its lists into ns = min(4, 32 / T)
     // slices: lane l takes target l % T of slice l / T, each slice stages
     // W = 32 / ns entries per round, and the slices' sums are added up by
     // shuffles at the end (larger groups: one slice, W = 32).
-    const u32 T = ga.y - ga.x;
+    const u32 T = q0.y - q0.x;
     const u32 ns = T == 0 ? 1u : min(4u, 32u / T);
     const u32 W = 32u / ns;
     const u32 slice = T ? static_cast<u32>(lane) / T : 0u;
     const u32 t = T ? static_cast<u32>(lane) % T : 0u;
     const bool computes = slice < ns;  // lanes past ns * T only stage
-    const u32 i = ga.x + t;
+    const u32 i = q0.x + t;
     const float4 bi = computes ? bodies[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const u32 stage_slice = static_cast<u32>(lane) / W, stage_pos = static_cast<u32>(lane) % W;
     float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
 
     {
-      const u32 e = ga.w - ga.z;  // cells, slice k: [e k / ns, e (k + 1) / ns)
-      const u32 c0 = ga.z + e * stage_slice / ns, c1 = ga.z + e * (stage_slice + 1) / ns;
-      const u32 m0 = ga.z + e * slice / ns, m1 = ga.z + e * (slice + 1) / ns;
+      const u32 e = q0.z;  // cells, slice k: entries [e k / ns, e (k + 1) / ns)
+      const u32 c0 = e * stage_slice / ns, c1 = e * (stage_slice + 1) / ns;
+      const u32 m0 = e * slice / ns, m1 = e * (slice + 1) / ns;
       const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
       for (u32 r = 0; r < rounds; ++r) {
         const u32 k = c0 + r * W + stage_pos;
         if (stage_slice < ns && k < c1) {
-          const u64 c = cell_list[k];
+          const u64 c = cell_list[cs.at(k)];
           const float4 q = __ldg(&cells[3 * c]);
           float4 *dst = &sc[warp][stage_slice * (3 * W + 1) + 3 * stage_pos];
           dst[0] = make_float4(q.x, q.y, q.z, G * q.w);
@@ -145,14 +147,14 @@ __global__ void __launch_bounds__(kT)
     }
 
     {
-      const u32 e = gb.y - gb.x;
-      const u32 c0 = gb.x + e * stage_slice / ns, c1 = gb.x + e * (stage_slice + 1) / ns;
-      const u32 m0 = gb.x + e * slice / ns, m1 = gb.x + e * (slice + 1) / ns;
+      const u32 e = q0.w;
+      const u32 c0 = e * stage_slice / ns, c1 = e * (stage_slice + 1) / ns;
+      const u32 m0 = e * slice / ns, m1 = e * (slice + 1) / ns;
       const u32 rounds = (((e + ns - 1) / ns) + W - 1) / W;
       for (u32 r = 0; r < rounds; ++r) {
         const u32 k = c0 + r * W + stage_pos;
         if (stage_slice < ns && k < c1) {
-          const u32 j = body_list[k];
+          const u32 j = body_list[bs.at(k)];
           const float4 b = __ldg(&bodies[j]);
           sb[warp][stage_slice * (W + 1) + stage_pos] = make_float4(b.x, b.y, b.z, G * b.w);
           if (!kSoft) sj[warp][stage_slice * (W + 1) + stage_pos] = j;
@@ -263,10 +265,12 @@ __global__ void __launch_bounds__(kT)
     if (lane == 0) g = atomicAdd(next_group, 1u);
     g = __shfl_sync(kFullMask, g, 0);
     if (g >= ngroups) return;
-    const uint4 ga = groups[2ull * g], gb = groups[2ull * g + 1];
-    const u32 T = ga.y - ga.x;
+    const uint4 q0 = groups[4ull * g], q1 = groups[4ull * g + 1], q2 = groups[4ull * g + 2],
+                q3 = groups[4ull * g + 3];
+    const SegView cs = cell_segs(q1, q2), bs = body_segs(q2, q3);  // list entry -> index
+    const u32 T = q0.y - q0.x;
     if (T == 0) continue;
-    const u32 ec = ga.w - ga.z, eb = gb.y - gb.x;
+    const u32 ec = q0.z, eb = q0.w;
     const u32 ns = choose_slices(T, ec, eb, lane);
     const u32 slots = ns * T;
     const u32 passes = (slots + 31u) / 32u;
@@ -285,14 +289,14 @@ __global__ void __launch_bounds__(kT)
       const u32 stage_slice = k_lo + stage_area;
       const bool stages = stage_area < nsp;
       const u32 half = stage_pos & 1u, pair = stage_pos >> 1;
-      const float4 bi = computes ? bodies[ga.x + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 bi = computes ? bodies[q0.x + t] : make_float4(0.f, 0.f, 0.f, 0.f);
       const float2 px = f2(bi.x, bi.x), py = f2(bi.y, bi.y), pz = f2(bi.z, bi.z);
       float2 ax = f2(0.f, 0.f), ay = ax, az = ax, pot = ax;
 
       {  // cells
         const u32 cstride = W * kPairCellF4 + 1;
-        const u32 c0 = ga.z + ec * stage_slice / ns, c1 = ga.z + ec * (stage_slice + 1) / ns;
-        const u32 m0 = ga.z + ec * slice / ns, m1 = ga.z + ec * (slice + 1) / ns;
+        const u32 c0 = ec * stage_slice / ns, c1 = ec * (stage_slice + 1) / ns;
+        const u32 m0 = ec * slice / ns, m1 = ec * (slice + 1) / ns;
         const u32 rounds = ((ec + ns - 1) / ns + 2 * W - 1) / (2 * W);
         for (u32 r = 0; r < rounds; ++r) {
           if (stages) {
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(kT)
             for (int h = 0; h < 2; ++h) {
               const u32 k = c0 + 2 * r * W + h * W + stage_pos;
               if (k < c1) {
-                const u64 c = cell_list[k];
+                const u64 c = cell_list[cs.at(k)];
                 const float4 a = __ldg(&cells[3 * c]), b = __ldg(&cells[3 * c + 1]),
                              q = __ldg(&cells[3 * c + 2]);
                 v[h][0] = -a.x; v[h][1] = -a.y; v[h][2] = -a.z; v[h][3] = -G * a.w;
@@ -354,8 +358,8 @@ __global__ void __launch_bounds__(kT)
 
       {  // bodies
         const u32 bstride = W * kPairBodyF4 + 1;
-        const u32 c0 = gb.x + eb * stage_slice / ns, c1 = gb.x + eb * (stage_slice + 1) / ns;
-        const u32 m0 = gb.x + eb * slice / ns, m1 = gb.x + eb * (slice + 1) / ns;
+        const u32 c0 = eb * stage_slice / ns, c1 = eb * (stage_slice + 1) / ns;
+        const u32 m0 = eb * slice / ns, m1 = eb * (slice + 1) / ns;
         const u32 rounds = ((eb + ns - 1) / ns + 2 * W - 1) / (2 * W);
         for (u32 r = 0; r < rounds; ++r) {
           if (stages) {
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(kT)
             for (int h = 0; h < 2; ++h) {
               const u32 k = c0 + 2 * r * W + h * W + stage_pos;
               if (k < c1) {
-                const float4 b = __ldg(&bodies[body_list[k]]);
+                const float4 b = __ldg(&bodies[body_list[bs.at(k)]]);
                 v[h][0] = -b.x; v[h][1] = -b.y; v[h][2] = -b.z; v[h][3] = -G * b.w;
               } else {
                 v[h][0] = v[h][1] = v[h][2] = -kFar;
@@ -414,7 +418,7 @@ __global__ void __launch_bounds__(kT)
       }
     }
     if (static_cast<u32>(lane) < T) {
-      const u32 i = ga.x + static_cast<u32>(lane);
+      const u32 i = q0.x + static_cast<u32>(lane);
       float4 acc = sacc[warp][lane];
       acc.w += G * bodies[i].w * rsqrtf(eps2);  // the self term (softened), taken back once
       out[i] = acc;

@@ -403,8 +403,8 @@ __global__ void __launch_bounds__(kT)
               c1 = cell_off[static_cast<u64>(g + 1) * ntasks];
     const u64 b0 = body_off[static_cast<u64>(g) * ntasks],
               b1 = body_off[static_cast<u64>(g + 1) * ntasks];
-    groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c1));
-    groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b1), 0u, 0u);
+    store_group_rec(groups, g, gbegin[g], gend[g], one_segment(c0, c1 - c0),
+                    one_segment(b0, b1 - b0));
     t = gend[g] - gbegin[g];
     nc = c1 - c0;
     nb = b1 - b0;
@@ -434,8 +434,7 @@ __global__ void __launch_bounds__(kT)
       kc = nc;
       kb = nb;
     }
-    groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(c0), static_cast<u32>(c0 + kc));
-    groups[2ull * g + 1] = make_uint4(static_cast<u32>(b0), static_cast<u32>(b0 + kb), 0u, 0u);
+    store_group_rec(groups, g, gbegin[g], gend[g], one_segment(c0, kc), one_segment(b0, kb));
   }
   group_stats_warp(sc, valid, t, nc, nb, true);
 }
@@ -501,7 +500,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gend.ensure(n * 4);
   ws.gbox.ensure(n * 48);
   ws.gboxf.ensure(n * 32);
-  ws.groups.ensure(n * 32);
+  ws.groups.ensure(n * kGroupRecWords * 4);
   u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
   k_group_ranges<<<ceil_div(n, kT), kT, 0, s>>>(mark, mscan, n32, gbegin, gend);
   GTC_LAUNCH_CHECK();

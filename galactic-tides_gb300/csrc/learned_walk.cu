@@ -598,9 +598,8 @@ __global__ void __launch_bounds__(kT)
   if (g >= rv.ng) return;
   u64 oc = cell_off[g], ob = body_off[g];
   if (lane == 0) {
-    groups[2ull * g] = make_uint4(gbegin[g], gend[g], static_cast<u32>(oc),
-                                  static_cast<u32>(cell_off[g + 1]));
-    groups[2ull * g + 1] = make_uint4(static_cast<u32>(ob), static_cast<u32>(body_off[g + 1]), 0u, 0u);
+    store_group_rec(groups, g, gbegin[g], gend[g], one_segment(oc, cell_off[g + 1] - oc),
+                    one_segment(ob, body_off[g + 1] - ob));
   }
   for (u32 r = 0; r < rv.rounds; ++r) {
     const u32 *st = rv.gstart + static_cast<u64>(r) * (rv.ng + 1);

@@ -154,6 +154,50 @@ __device__ __forceinline__ void group_stats_warp(Scalars *sc, bool valid, u64 t,
   }
 }
 
+// The evaluator's group record, 64 bytes (four uint4): targets [begin, end),
+// the list lengths, and the cell and body lists as up to kListSegments
+// segments each (start, count), concatenated in list order; empty segments
+// are skipped. uint4 0: begin, end, cells, bodies; 1: cell segments 0 and 1;
+// 2: cell segment 2, body segment 0; 3: body segments 1 and 2.
+constexpr int kListSegments = 3;
+constexpr int kGroupRecWords = 16;
+
+struct ListSegs {
+  u32 start[kListSegments], count[kListSegments];
+};
+
+__host__ __device__ inline ListSegs one_segment(u64 start, u64 count) {
+  ListSegs s{};
+  s.start[0] = static_cast<u32>(start);
+  s.count[0] = static_cast<u32>(count);
+  return s;
+}
+
+__host__ __device__ inline void store_group_rec(uint4 *groups, u64 g, u32 begin, u32 end,
+                                                const ListSegs &c, const ListSegs &b) {
+  const u32 nc = c.count[0] + c.count[1] + c.count[2];
+  const u32 nb = b.count[0] + b.count[1] + b.count[2];
+  groups[4 * g] = make_uint4(begin, end, nc, nb);
+  groups[4 * g + 1] = make_uint4(c.start[0], c.count[0], c.start[1], c.count[1]);
+  groups[4 * g + 2] = make_uint4(c.start[2], c.count[2], b.start[0], b.count[0]);
+  groups[4 * g + 3] = make_uint4(b.start[1], b.count[1], b.start[2], b.count[2]);
+}
+
+// A group's lists as the evaluator reads them: entry e of the concatenated
+// segments is at at(e).
+struct SegView {
+  u32 s0, n0, s1, n1, s2;
+  __host__ __device__ __forceinline__ u32 at(u32 e) const {
+    return e < n0 ? s0 + e : (e - n0 < n1 ? s1 + (e - n0) : s2 + (e - n0 - n1));
+  }
+};
+__host__ __device__ __forceinline__ SegView cell_segs(const uint4 &q1, const uint4 &q2) {
+  return SegView{q1.x, q1.y, q1.z, q1.w, q2.x};
+}
+__host__ __device__ __forceinline__ SegView body_segs(const uint4 &q2, const uint4 &q3) {
+  return SegView{q2.z, q2.w, q3.x, q3.y, q3.z};
+}
+
 // Adds each lane's count to *total with one atomic per warp (every lane of
 // the warp must call it).
 __device__ __forceinline__ void warp_add(unsigned long long *total, unsigned long long v) {
