@@ -63,7 +63,7 @@ void Workspace::release_all() {
                          &drec, &drec_alt, &dseg, &dtmp, &geom, &mom, &quad, &delta, &nbegin,
                          &nend, &skip, &parent, &depth, &nchild, &isleaf, &kids, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
-                         &groups, &cell_list, &body_list, &spill, &root, &bbox_part, &scalars, &split, &scan_tmp,
+                         &groups, &cell_list, &body_list, &spill, &splitpt, &root, &bbox_part, &scalars, &split, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (host_words) cudaFreeHost(host_words);
@@ -155,7 +155,6 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
     lw.gtol = &ctx->gtol;
     lw.scratch = &ctx->lscratch;
-    lw.split_depth = ctx->learned_split;
     lw.y_mean = ctx->model_ymean;
     lw.prev_amag = ctx->prev_amag.as<float>();
     lw.alpha = sp.alpha;
@@ -257,17 +256,22 @@ struct GraphStep {
     const double fs = 1.0 + 2.0 * ctx->graph_headroom;
     auto slot = [&](u32 longest) {
       const u64 v = (static_cast<u64>(longest * fs) + (pad ? 64 : 0) + 31) & ~31ull;
-      const u64 most = (0xffffffffull / caps.groups) & ~31ull;
+      const u64 most = (0xffffffffull / caps.groups / 2) & ~31ull;  // two slot arrays
       return static_cast<u32>(std::max<u64>(32, std::min(v, most)));
     };
+    // (the last walk split: rest and near field; the two passes: whole lists)
+    const bool split = ws.list_passes == 1;
     caps.slot_cells = slot(hs.max_cells);
     caps.slot_bodies = slot(hs.max_bodies);
-    auto pool = [&](u32 sl) {
-      const u64 room = 0xffffffffull - static_cast<u64>(caps.groups) * sl;
-      return std::min<u64>(gtc::Workspace::pool_for(caps.groups, sl), room);
+    caps.slot_near_cells = slot(split ? hs.max_near_cells : hs.max_cells);
+    caps.slot_near_bodies = slot(split ? hs.max_near_bodies : hs.max_bodies);
+    auto pool = [&](u32 rest, u32 near) {
+      const u64 used = static_cast<u64>(caps.groups) * (static_cast<u64>(rest) + near);
+      const u64 room = used < 0xffffffffull ? 0xffffffffull - used : 0;
+      return std::min<u64>(gtc::Workspace::pool_for(caps.groups, rest + near), room);
     };
-    caps.pool_cells = pool(caps.slot_cells);
-    caps.pool_bodies = pool(caps.slot_bodies);
+    caps.pool_cells = pool(caps.slot_cells, caps.slot_near_cells);
+    caps.pool_bodies = pool(caps.slot_bodies, caps.slot_near_bodies);
     const u64 m = caps.nodes;
     ws.geom.ensure(m * 2 * sizeof(double2));
     ws.mom.ensure(m * 2 * sizeof(double2));
@@ -288,14 +292,17 @@ struct GraphStep {
     ws.split.ensure(3ull * gtc::kSplitSize * sizeof(double));
     ws.flags.ensure(std::max<u64>(n, m) * 4);
     ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
-    ws.gcells.ensure(n * 8);
-    ws.gbodies.ensure(n * 8);
+    ws.gcells.ensure(2 * n * 8);
+    ws.gbodies.ensure(2 * n * 8);
     ws.gcell_off.ensure((n + 1) * 8);
     ws.gbody_off.ensure((n + 1) * 8);
     ws.groups.ensure(n * gtc::kGroupRecWords * 4);
-    ws.cell_list.ensure((static_cast<u64>(caps.groups) * caps.slot_cells + caps.pool_cells) * 4);
-    ws.body_list.ensure((static_cast<u64>(caps.groups) * caps.slot_bodies + caps.pool_bodies) * 4);
+    ws.cell_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_cells + caps.slot_near_cells) +
+                         caps.pool_cells) * 4);
+    ws.body_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_bodies + caps.slot_near_bodies) +
+                         caps.pool_bodies) * 4);
     ws.spill.ensure(2 * n * sizeof(u32));
+    ws.splitpt.ensure(2 * n * sizeof(u32));
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
     if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));
@@ -846,10 +853,6 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
     } else if (key == "graph_headroom") {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;
-    } else if (key == "learned_split_depth") {
-      if (value != std::floor(value) || value < 0 || value > 8)
-        throw gtc::InvalidArgument("learned_split_depth must be 0..8");
-      ctx->learned_split = static_cast<int>(value);
     } else {
       throw gtc::InvalidArgument("unknown option '" + key + "'");
     }

@@ -33,7 +33,6 @@ struct gtc_context {
   gtc::u64 prev_n = 0;              // bodies in prev_amag (0: none)
   double guard_theta = 1.5;         // options of the learned walk
   double band_override = -1.0;      // < 0: the model's band
-  int learned_split = 2;            // learned walk: path split depth of round 0
   gtc::DeviceBuffer diag;           // diagnostics partial sums
   double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes
 };

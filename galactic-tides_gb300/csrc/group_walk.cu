@@ -232,22 +232,16 @@ struct Task {
 constexpr u32 kNone = 0xffffffffu;
 
 struct WalkOut {
-  u64 *ncells, *nbodies;          // count and one-pass walks, [group * ntasks + task]
+  u64 *ncells, *nbodies;          // count pass, [group * ntasks + task]
   const u64 *cell_off, *body_off; // fill pass, same indexing
   u32 *cell_list, *body_list;
-  u32 slot_cells, slot_bodies;    // one-pass walk: each group's capacities
-  u32 *spill_cells, *spill_bodies;  // where an outgrown group's lists go (kNoSpill: its slot)
-  u64 pool_cells_at, pool_cells;    // overflow pools: first entry and size
-  u64 pool_bodies_at, pool_bodies;
+  const u32 *spill_cells, *spill_bodies;  // spill walk: where an outgrown group's lists go
 };
 
-// Walk modes: count the lists; write them at scanned offsets; both in one
-// pass into fixed per-group slots (one task per group; an outgrown slot
-// keeps counting, and its group then takes a place in the overflow pools
-// for its whole lists, or flags the lists as overflowing when the pools are
-// too small); or write again, whole, the lists of the groups that outgrew
-// their slots, into their places in the pools.
-constexpr int kCount = 0, kFill = 1, kSlots = 2, kSpill = 3;
+// Walk modes: count the lists; write them at scanned offsets; or write
+// again, whole, the lists of the groups whose one-pass walk (k_walk_split)
+// outgrew their slots, into their places in the overflow pools.
+constexpr int kCount = 0, kFill = 1, kSpill = 3;
 constexpr u32 kNoSpill = 0xffffffffu;
 
 __device__ __forceinline__ int decide(const WalkRec32 &r, const WalkRec64 *walk64, u32 i,
@@ -286,9 +280,6 @@ __global__ void __launch_bounds__(kT)
   if (kMode == kFill) {
     cl = out.cell_list + out.cell_off[slot];
     bl = out.body_list + out.body_off[slot];
-  } else if (kMode == kSlots) {
-    cl = out.cell_list + static_cast<u64>(g) * out.slot_cells;
-    bl = out.body_list + static_cast<u64>(g) * out.slot_bodies;
   } else if (kMode == kSpill) {
     if (out.spill_cells[g] == kNoSpill) return;
     cl = out.cell_list + out.spill_cells[g];
@@ -299,13 +290,11 @@ __global__ void __launch_bounds__(kT)
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
     if (verdict == 1 && nbody > kFewBodies) {
-      if (kMode == kFill || kMode == kSpill || (kMode == kSlots && nc < out.slot_cells)) cl[nc] = i;
+      if (kMode == kFill || kMode == kSpill) cl[nc] = i;
       ++nc;
     } else {
       if (kMode == kFill || kMode == kSpill)
         for (u32 j = 0; j < nbody; ++j) bl[nb + j] = r.begin + j;
-      if (kMode == kSlots)
-        for (u32 j = 0; j < nbody && nb + j < out.slot_bodies; ++j) bl[nb + j] = r.begin + j;
       nb += nbody;
     }
   };
@@ -337,7 +326,7 @@ __global__ void __launch_bounds__(kT)
       }
     }
   }
-  if (kMode == kCount || kMode == kSlots) {
+  if (kMode == kCount) {
     out.ncells[slot] = nc;
     out.nbodies[slot] = nb;
     if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
@@ -347,24 +336,194 @@ __global__ void __launch_bounds__(kT)
     if ((threadIdx.x & 31) == static_cast<unsigned>(__ffs(mask) - 1))
       atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(sum));
   }
-  if (kMode == kSlots) {
-    u32 oc = kNoSpill, ob = kNoSpill;
-    if (nc > out.slot_cells || nb > out.slot_bodies) {
-      const u64 c = atomicAdd(&sc->spill_used[0], static_cast<unsigned long long>(nc));
-      const u64 b = atomicAdd(&sc->spill_used[1], static_cast<unsigned long long>(nb));
-      if (c + nc <= out.pool_cells && b + nb <= out.pool_bodies) {
-        oc = static_cast<u32>(out.pool_cells_at + c);
-        ob = static_cast<u32>(out.pool_bodies_at + b);
-      } else {
-        atomicOr(&sc->list_overflow, 1u);
-      }
-      atomicAdd(&sc->spilled, 1u);
-    }
-    out.spill_cells[g] = oc;
-    out.spill_bodies[g] = ob;
-  }
 }
 
+
+// The one-pass walk, split in two per group. A long walk spends about half
+// its nodes inside the root child that holds the group (its near field),
+// and one thread per group leaves the others idle while the longest walks
+// finish. So thread `rest` walks from the root but jumps over that child,
+// noting how much it had written when it did, and thread `near` walks the
+// child. The group's lists are then [rest before | near | rest after]: the
+// reference's order. Each part writes into its own slots; a group whose
+// part outgrows its slot is walked again whole into the overflow pools.
+struct SplitOut {
+  u64 *ncells, *nbodies;   // [part * cap + group]: part 0 the rest, 1 the near field
+  u32 *split;              // per group: the rest's cells and bodies before the near field
+  u32 *cell_list, *body_list;
+  u64 near_cells_at, near_bodies_at;  // the near parts' slots start here (the rest's at 0)
+  u32 slot_cells, slot_bodies, slot_near_cells, slot_near_bodies;
+  u32 cap;                 // groups the count arrays hold per part
+};
+
+// The root child that holds targets [b0, b1), or kNone.
+__device__ __forceinline__ u32 near_child(u32 b0, u32 b1, const uint4 *kids, const u8 *nchild,
+                                          const u32 *nbegin, const u32 *nend) {
+  const int k = nchild[0];
+  const uint4 k0 = kids[0], k1 = kids[1];
+  const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+  for (int j = 0; j < k && j < 8; ++j)
+    if (nbegin[ch[j]] <= b0 && b1 <= nend[ch[j]]) return ch[j];
+  return kNone;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_walk_split(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
+                 const float *gboxf, const u32 *gbegin, const u32 *gend, const uint4 *kids,
+                 const u8 *nchild, const u32 *nbegin, const u32 *nend, u32 ng_cap, SplitOut out,
+                 Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (aborted(abort)) return;
+  const u32 ng = bounded(ng_cap, ng_dev);
+  if (tid >= 2ull * ng) return;
+  const u32 part = tid >= ng ? 1u : 0u;
+  const u32 g = static_cast<u32>(part ? tid - ng : tid);
+  const float4 b0 = reinterpret_cast<const float4 *>(gboxf)[2ull * g],
+               b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
+  const float gf[3] = {b0.x, b0.y, b0.z}, hf[3] = {b0.w, b1.x, b1.y};
+  const float gbound = b1.z;
+  const u32 near = near_child(gbegin[g], gend[g], kids, nchild, nbegin, nend);
+  const u32 near_end = near == kNone ? 0u : load32(walk32, near).skip;
+  const u32 cap_c = part ? out.slot_near_cells : out.slot_cells;
+  const u32 cap_b = part ? out.slot_near_bodies : out.slot_bodies;
+  u32 *cl = out.cell_list + (part ? out.near_cells_at : 0ull) + static_cast<u64>(g) * cap_c;
+  u32 *bl = out.body_list + (part ? out.near_bodies_at : 0ull) + static_cast<u64>(g) * cap_b;
+  u32 nc = 0, nb = 0, exact = 0, visits = 0, split_c = 0, split_b = 0;
+  bool jumped = false;
+  u32 i = 0, end = 0;
+  if (part == 0) {
+    end = load32(walk32, 0).skip;
+  } else if (near != kNone) {
+    i = near;
+    end = near_end;
+  }
+  while (i < end) {
+    if (part == 0 && i == near) {  // the near field is the other thread's
+      split_c = nc;
+      split_b = nb;
+      jumped = true;
+      i = near_end;
+      continue;
+    }
+    const WalkRec32 r = load32(walk32, i);
+    ++visits;
+    const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
+    if (verdict == 1 || (r.nbody_leaf >> 31)) {
+      const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+      if (verdict == 1 && nbody > kFewBodies) {
+        if (nc < cap_c) cl[nc] = i;
+        ++nc;
+      } else {
+        for (u32 j = 0; j < nbody && nb + j < cap_b; ++j) bl[nb + j] = r.begin + j;
+        nb += nbody;
+      }
+      if (r.skip <= i) {  // malformed tree: never loop
+        atomicOr(&sc->error, 1u);
+        break;
+      }
+      i = r.skip;
+    } else {
+      ++i;
+    }
+  }
+  if (part == 0 && !jumped) {
+    split_c = nc;
+    split_b = nb;
+  }
+  out.ncells[static_cast<u64>(part) * out.cap + g] = nc;
+  out.nbodies[static_cast<u64>(part) * out.cap + g] = nb;
+  if (part == 0) {
+    out.split[2ull * g] = split_c;
+    out.split[2ull * g + 1] = split_b;
+  }
+  if (exact) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(exact));
+  const unsigned mask = __activemask();
+  const u32 sum = __reduce_add_sync(mask, visits);
+  if ((threadIdx.x & 31) == static_cast<unsigned>(__ffs(mask) - 1))
+    atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(sum));
+}
+
+// Places in the overflow pools for the groups one of whose parts outgrew its
+// slot (their whole lists, walked again by one thread); pools too small flag
+// the lists as overflowing.
+__global__ void __launch_bounds__(kT)
+    k_split_spill(const SplitOut out, u32 ng, u64 pool_cells_at, u64 pool_cells,
+                  u64 pool_bodies_at, u64 pool_bodies, u32 *spill_cells, u32 *spill_bodies,
+                  Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
+  const u64 rc = out.ncells[g], rb = out.nbodies[g];
+  const u64 nc = out.ncells[static_cast<u64>(out.cap) + g], nb = out.nbodies[static_cast<u64>(out.cap) + g];
+  u32 oc = kNoSpill, ob = kNoSpill;
+  if (rc > out.slot_cells || rb > out.slot_bodies || nc > out.slot_near_cells ||
+      nb > out.slot_near_bodies) {
+    const u64 tc = rc + nc, tb = rb + nb;
+    const u64 c = atomicAdd(&sc->spill_used[0], static_cast<unsigned long long>(tc));
+    const u64 b = atomicAdd(&sc->spill_used[1], static_cast<unsigned long long>(tb));
+    if (c + tc <= pool_cells && b + tb <= pool_bodies) {
+      oc = static_cast<u32>(pool_cells_at + c);
+      ob = static_cast<u32>(pool_bodies_at + b);
+    } else {
+      atomicOr(&sc->list_overflow, 1u);
+    }
+    atomicAdd(&sc->spilled, 1u);
+  }
+  spill_cells[g] = oc;
+  spill_bodies[g] = ob;
+}
+
+// Group records of a split one-pass walk: three segments per list (one, in
+// the pools, for a spilled group), the statistics, and the longest lists of
+// either part.
+__global__ void __launch_bounds__(kT)
+    k_split_records(const u32 *gbegin, const u32 *gend, u32 ng, const SplitOut out,
+                    const u32 *spill_cells, const u32 *spill_bodies, uint4 *groups, Scalars *sc,
+                    const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (aborted(abort)) return;
+  const bool valid = g < bounded(ng, ng_dev);
+  u64 t = 0, rc = 0, rb = 0, nc = 0, nb = 0;
+  if (valid) {
+    rc = out.ncells[g];
+    rb = out.nbodies[g];
+    nc = out.ncells[static_cast<u64>(out.cap) + g];
+    nb = out.nbodies[static_cast<u64>(out.cap) + g];
+    t = gend[g] - gbegin[g];
+    ListSegs cs, bs;
+    if (spill_cells[g] != kNoSpill) {
+      cs = one_segment(spill_cells[g], rc + nc);
+      bs = one_segment(spill_bodies[g], rb + nb);
+    } else {
+      const u32 sc_ = out.split[2ull * g], sb_ = out.split[2ull * g + 1];
+      const u64 r0 = static_cast<u64>(g) * out.slot_cells, q0 = static_cast<u64>(g) * out.slot_bodies;
+      const u64 n0 = out.near_cells_at + static_cast<u64>(g) * out.slot_near_cells;
+      const u64 m0 = out.near_bodies_at + static_cast<u64>(g) * out.slot_near_bodies;
+      cs.start[0] = static_cast<u32>(r0);
+      cs.count[0] = sc_;
+      cs.start[1] = static_cast<u32>(n0);
+      cs.count[1] = static_cast<u32>(nc);
+      cs.start[2] = static_cast<u32>(r0 + sc_);
+      cs.count[2] = static_cast<u32>(rc - sc_);
+      bs.start[0] = static_cast<u32>(q0);
+      bs.count[0] = sb_;
+      bs.start[1] = static_cast<u32>(m0);
+      bs.count[1] = static_cast<u32>(nb);
+      bs.start[2] = static_cast<u32>(q0 + sb_);
+      bs.count[2] = static_cast<u32>(rb - sb_);
+    }
+    store_group_rec(groups, g, gbegin[g], gend[g], cs, bs);
+  }
+  group_stats_warp(sc, valid, t, rc + nc, rb + nb, true, false);
+  auto clamp = [](u64 v) { return static_cast<u32>(v < 0xffffffffull ? v : 0xffffffffull); };
+  const u32 m_rc = __reduce_max_sync(kFullMask, clamp(rc)), m_rb = __reduce_max_sync(kFullMask, clamp(rb));
+  const u32 m_nc = __reduce_max_sync(kFullMask, clamp(nc)), m_nb = __reduce_max_sync(kFullMask, clamp(nb));
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&sc->max_cells, m_rc);
+    atomicMax(&sc->max_bodies, m_rb);
+    atomicMax(&sc->max_near_cells, m_nc);
+    atomicMax(&sc->max_near_bodies, m_nb);
+  }
+}
 
 // Walk tasks: nodes at depth `split` (0..2), and leaves above it, in node
 // order. The root is never accepted (every group lies inside it), so only a
@@ -412,32 +571,6 @@ __global__ void __launch_bounds__(kT)
   group_stats_warp(sc, valid, t, nc, nb, false);
 }
 
-// Group records of a one-pass walk: group g's lists start at its slots.
-__global__ void __launch_bounds__(kT)
-    k_slot_records(const u32 *gbegin, const u32 *gend, u32 ng, const u64 *ncells,
-                   const u64 *nbodies, u32 slot_cells, u32 slot_bodies, const u32 *spill_cells,
-                   const u32 *spill_bodies, uint4 *groups, Scalars *sc,
-                   const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (aborted(abort)) return;
-  const bool valid = g < bounded(ng, ng_dev);
-  u64 t = 0, nc = 0, nb = 0;
-  if (valid) {
-    nc = ncells[g];
-    nb = nbodies[g];
-    t = gend[g] - gbegin[g];
-    u64 c0 = static_cast<u64>(g) * slot_cells, b0 = static_cast<u64>(g) * slot_bodies;
-    u64 kc = nc < slot_cells ? nc : slot_cells, kb = nb < slot_bodies ? nb : slot_bodies;
-    if (spill_cells[g] != kNoSpill) {  // the whole lists, in the pools
-      c0 = spill_cells[g];
-      b0 = spill_bodies[g];
-      kc = nc;
-      kb = nb;
-    }
-    store_group_rec(groups, g, gbegin[g], gend[g], one_segment(c0, kc), one_segment(b0, kb));
-  }
-  group_stats_warp(sc, valid, t, nc, nb, true);
-}
 
 void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
   GTC_CUDA(cudaMemcpyAsync(host, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
@@ -448,13 +581,18 @@ void read_scalars(Workspace &ws, Scalars *host, cudaStream_t s) {
 // and 64, in multiples of 32 entries (each slot starts on 128 bytes). The
 // longest of many groups' lists moves from one step to the next, so the
 // margin is wide; slots cost only memory.
-void size_slots(Workspace &ws, const Scalars &h) {
+// After a split walk max_cells / max_bodies are the rest's longest lists and
+// max_near_* the near field's; after the two passes they are whole lists,
+// which size both parts' slots.
+void size_slots(Workspace &ws, const Scalars &h, bool split) {
   auto slot = [](u64 longest) {
     const u64 v = (longest + longest / 2 + 64 + 31) & ~31ull;
     return static_cast<u32>(std::min<u64>(v, 0x7fffffe0ull));
   };
   ws.slot_cells = slot(h.max_cells);
   ws.slot_bodies = slot(h.max_bodies);
+  ws.slot_near_cells = slot(split ? h.max_near_cells : h.max_cells);
+  ws.slot_near_bodies = slot(split ? h.max_near_bodies : h.max_bodies);
 }
 
 }  // namespace
@@ -530,39 +668,56 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u64 slots = static_cast<u64>(ng) * ntasks;
   ws.gcells.ensure(slots * 8);
   ws.gbodies.ensure(slots * 8);
-  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
   const u32 tb = ceil_div(slots, kT);
 
   // One pass into per-group slots when the last walk sized them and they
-  // fit 32-bit offsets and eight times the lists' own size (the slots of
-  // the benchmark galaxy take about four times). Groups whose
-  // lists outgrow their slots are walked again into the overflow pools;
-  // pools too small fall back to the two passes below.
+  // fit 32-bit offsets and sixteen times the lists' own size (slots sized
+  // by a two-pass walk's whole lists take about eight times for the
+  // benchmark galaxy, those of a split walk about four): two threads per group, the
+  // near field and the rest. Groups whose lists outgrow their slots are
+  // walked again into the overflow pools; pools too small fall back to the
+  // two passes below.
   const u32 sl_c = ws.slot_cells, sl_b = ws.slot_bodies;
-  const u64 pool_c = Workspace::pool_for(ng, sl_c), pool_b = Workspace::pool_for(ng, sl_b);
-  const u64 ext_c = static_cast<u64>(ng) * sl_c + pool_c, ext_b = static_cast<u64>(ng) * sl_b + pool_b;
+  const u32 sn_c = ws.slot_near_cells, sn_b = ws.slot_near_bodies;
+  const u64 near_c = static_cast<u64>(ng) * sl_c, near_b = static_cast<u64>(ng) * sl_b;
+  const u64 pool_at_c = near_c + static_cast<u64>(ng) * sn_c;
+  const u64 pool_at_b = near_b + static_cast<u64>(ng) * sn_b;
+  const u64 pool_c = Workspace::pool_for(ng, sl_c + sn_c), pool_b = Workspace::pool_for(ng, sl_b + sn_b);
+  const u64 ext_c = pool_at_c + pool_c, ext_b = pool_at_b + pool_b;
   if (sl_c > 0 && ntasks == 1 && ext_c <= 0xffffffffull && ext_b <= 0xffffffffull &&
-      ext_c + ext_b <= std::max<u64>(8 * prev_entries, 1ull << 26)) {
+      ext_c + ext_b <= std::max<u64>(16 * prev_entries, 1ull << 26)) {
     ws.cell_list.ensure(ext_c * 4);
     ws.body_list.ensure(ext_b * 4);
     ws.spill.ensure(2ull * ng * sizeof(u32));
+    ws.splitpt.ensure(2ull * ng * sizeof(u32));
+    ws.gcells.ensure(2ull * ng * 8);
+    ws.gbodies.ensure(2ull * ng * 8);
     u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + ng;
     GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
-    WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), sl_c, sl_b, spill_c, spill_b,
-               static_cast<u64>(ng) * sl_c, pool_c, static_cast<u64>(ng) * sl_b, pool_b};
-    k_walk<kSlots><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
+    GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
+    const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
+                      ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
+                      sl_c, sl_b, sn_c, sn_b, ng};
+    k_walk_split<<<ceil_div(2ull * ng, kT), kT, 0, s>>>(
+        w32, w64, gbox, gboxf, gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
+        ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc);
     GTC_LAUNCH_CHECK();
+    k_split_spill<<<gb, kT, 0, s>>>(so, ng, pool_at_c, pool_c, pool_at_b, pool_b, spill_c, spill_b,
+                                    sc);
+    GTC_LAUNCH_CHECK();
+    WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
     k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
     GTC_LAUNCH_CHECK();
-    k_slot_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
-                                     sl_c, sl_b, spill_c, spill_b, ws.groups.as<uint4>(), sc);
+    k_split_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, so, spill_c, spill_b,
+                                      ws.groups.as<uint4>(), sc);
     GTC_LAUNCH_CHECK();
     read_scalars(ws, host, s);
-    size_slots(ws, *host);
+    size_slots(ws, *host, true);
     if (!host->list_overflow) {
       ws.n_cell_list = host->n_cell_list;
       ws.n_body_list = host->n_body_list;
@@ -575,7 +730,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
-    GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
   }
 
   // count pass, offsets, fill pass
@@ -583,7 +738,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gbody_off.ensure((slots + 1) * 8);
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr,
-             0, 0, nullptr, nullptr, 0, 0, 0, 0};
+             nullptr, nullptr};
   k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
@@ -596,7 +751,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   read_scalars(ws, host, s);
   if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
     throw RuntimeError("interaction lists too long for 32 bit offsets");
-  size_slots(ws, *host);
+  size_slots(ws, *host, false);
   ws.n_cell_list = host->n_cell_list;
   ws.n_body_list = host->n_body_list;
   ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
@@ -634,32 +789,42 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>(), &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  // one pass into the captured slots, outgrown groups again into the pools
+  // one pass into the captured slots (near field and rest), outgrown groups
+  // again into the pools
   k_check_groups_graph<<<1, 1, 0, s>>>(sc, caps.groups);
   GTC_LAUNCH_CHECK();
   GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
   GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
-  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 2 * sizeof(u32), s));
+  GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
   u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + n;
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), caps.slot_cells, caps.slot_bodies,
-             spill_c, spill_b, static_cast<u64>(caps.groups) * caps.slot_cells, caps.pool_cells,
-             static_cast<u64>(caps.groups) * caps.slot_bodies, caps.pool_bodies};
-  const Task *tasks = ws.tasks.as<Task>();
-  k_walk<kSlots><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                   ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
-                                   sc, &sc->n_groups, abort);
+  const u64 near_c = static_cast<u64>(caps.groups) * caps.slot_cells;
+  const u64 near_b = static_cast<u64>(caps.groups) * caps.slot_bodies;
+  const u64 pool_at_c = near_c + static_cast<u64>(caps.groups) * caps.slot_near_cells;
+  const u64 pool_at_b = near_b + static_cast<u64>(caps.groups) * caps.slot_near_bodies;
+  const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
+                    ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
+                    caps.slot_cells, caps.slot_bodies, caps.slot_near_cells,
+                    caps.slot_near_bodies, n32};
+  k_walk_split<<<ceil_div(2ull * n, kT), kT, 0, s>>>(
+      ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
+      ws.gboxf.as<float>(), gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
+      ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
+  k_split_spill<<<nb, kT, 0, s>>>(so, n32, pool_at_c, caps.pool_cells, pool_at_b,
+                                  caps.pool_bodies, spill_c, spill_b, sc, &sc->n_groups, abort);
+  GTC_LAUNCH_CHECK();
+  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
+  const Task *tasks = ws.tasks.as<Task>();
   k_walk<kSpill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
                                    ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
                                    sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  k_slot_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.gcells.as<u64>(), ws.gbodies.as<u64>(),
-                                   caps.slot_cells, caps.slot_bodies, spill_c, spill_b,
-                                   ws.groups.as<uint4>(), sc, &sc->n_groups, abort);
+  k_split_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, so, spill_c, spill_b,
+                                    ws.groups.as<uint4>(), sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
   k_check_slots_graph<<<1, 1, 0, s>>>(sc);
   GTC_LAUNCH_CHECK();

@@ -116,18 +116,18 @@ struct alignas(16) LearnedNet {
 
 // Device memory of the learned walk, kept between calls.
 struct LearnedScratch {
-  DeviceBuffer seg;                 // per item: two uint4 records (items_cap each)
-  DeviceBuffer regions, lane_fill;  // the lanes' list regions and how full they are
-  DeviceBuffer gstart, pcount, poff, base;
-  DeviceBuffer q[2], dec[2];        // deferred pairs and the network's decisions
   DeviceBuffer lrec;                // per node: the walk's record (LWalkRec)
-  u64 items_cap = 0;
-  u32 lane_cells = 2048, lane_runs = 512, lane_pend = 512;  // grown when outgrown
+  DeviceBuffer pend, pcount;        // per part and group: the pairs a round deferred, how many
+  DeviceBuffer roff, ptotal;        // per group: its first deferred row, its count
+  DeviceBuffer q[2], dec[2];        // deferred (group, node) rows and the network's decisions
+  // per-group slots of the three parts of round 0 (0: not sized yet) and
+  // of deferred pairs
+  u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
   void release() {
-    for (DeviceBuffer *b : {&seg, &regions, &lane_fill, &gstart, &pcount, &poff, &base, &lrec, &q[0],
-                            &q[1], &dec[0], &dec[1]})
+    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &ptotal, &q[0], &q[1], &dec[0], &dec[1]})
       b->release();
-    items_cap = 0;
+    for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
+    slot_pend = 0;
   }
 };
 
@@ -137,7 +137,6 @@ struct LearnedWalk {
   const CellFeat *cfeat = nullptr;  // per node (device)
   DeviceBuffer *gtol = nullptr;     // per group (f0, tolerance), filled by build_lists
   LearnedScratch *scratch = nullptr;
-  int split_depth = 2;              // round 0: each group's walk split along its path this deep
   const float *prev_amag = nullptr; // |a| per body in caller order (device)
   double alpha = 0.02, G = 1.0;
   float inv_theta_guard = 1.f / 1.5f;
@@ -153,8 +152,10 @@ void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lr
                           float inv_theta_guard, float y_mean, cudaStream_t s);
 // Per-group group feature and tolerance (inside build_lists, after the group boxes).
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s);
-// The learned walk over the groups' path-split items in rounds, then the gather: GTGroup records, cell_list, body_list and the interaction
-// counters of the ng groups (inside build_lists).
+// The learned walk in rounds (round 0 three threads per group, later rounds
+// one), each group writing into its own slots: group records, cell_list,
+// body_list and the interaction counters of the ng groups (inside
+// build_lists).
 void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
                          cudaStream_t s);
 // |a| per body, caller order, from the evaluator's tree-order output.

@@ -249,260 +249,244 @@ __device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
   return r;
 }
 
-// The learned walk runs in rounds over items, (group, node) pairs: walk the
-// subtree under the node for the group. Round 0's items split each group's
-// walk along the group's own path from the root: for the path's first
-// `split` levels, every sibling of the path node is an item, and the node
-// the path reaches is the last (the group's near field, its longest walk;
-// it is stored first). Only nodes that hold the group are opened for it on
-// the way down, as the walk itself would, so the decisions are the unsplit
-// walk's. A walk decides what the guard and the prior settle and defers the
-// rest, the (group, cell) pairs whose centred prior lies within the band of
-// the group's tolerance, skipping their subtrees. A dense kernel then runs
-// the network on all deferred pairs at once, 32 rows per warp on the tensor
-// cores, and the next round's items are those pairs with the network's
-// decision: accept the cell, or walk its children (deferring again). The
-// walk kernel itself carries no network and few registers, so many warps
-// hide its memory latency, and the network's latency is off its path.
-//
-// Each lane appends what its items produce to its own region: accepted
-// cells, runs of bodies (first, count) and deferred nodes. A gather pass
-// concatenates a group's items in (round, item) order into the group's
-// lists. Items are stored grouped by group in every round (a round's
-// deferred pairs keep their items' order), with each group's range kept
-// per round.
-constexpr u64 kNoItem = ~0ull;
-constexpr int kGrabLanes = 8;
 constexpr int kMaxRounds = kMaxDepth + 4;
 
-struct LArgs {
-  const WalkRec32 *walk32;
-  const CellFeat *cfeat;
+// Round 0 runs as kParts threads per group, each walking a range of the
+// root's children (3, 3 and 2 of 8, in walk order) into its own slots: the
+// groups with the longest lists, at the centre where |a| is small, set the
+// round's time, and their walks spread over all the root's children. The
+// parts' lists follow each other in walk order, so a group's lists are its
+// parts' lists in turn; later rounds append to the last part's slot.
+constexpr int kParts = 3;
+
+struct GArgs {
   const LWalkRec *lrec;
   const float *gboxf;
   const float2 *gtol;
   u32 ng;
-  u64 nitems;              // items of this round
-  u64 item_base;           // global index of the round's first item
-  const uint2 *qitems;     // (group, node) of each item
-  const u8 *qdec;          // rounds > 0: the network's decision on the node (1: accept)
-  const TreeRoot *root;
+  const TreeRoot *root;     // with mom: L, the d unit of the prior tests
   const double2 *mom;
-  float inv_theta_guard, band, y_mean;
-  u32 lane_cells, lane_runs, lane_pend;  // capacity of each lane's regions
-  u32 *reg_cells;
-  uint2 *reg_runs;
-  u32 *reg_pend;
-  u32 *lane_fill;          // per lane: cells, runs, deferred used so far
-  uint4 *seg;              // per item: first cell, cells, first run, runs (region indices)
-  uint4 *seg2;             // per item: first deferred, deferred, bodies, 0
-  u32 *pcount;             // per item of the round (storage order): deferred
-  unsigned long long *gcells, *gbodies;  // per group: list entries of all its items
+  float band;
+  u32 slot_cells[kParts], slot_bodies[kParts], slot_pend;
+  u64 cells_at[kParts], bodies_at[kParts];  // part k's slots: at + g * slot
+  u32 *cells, *bodies, *pend;  // deferred pairs: part k's at (k * ng + g) * slot_pend
+  u64 *ncells, *nbodies;    // [part * ng + group]
+  u32 *pcount;              // [part * ng + group]: pairs deferred this round
+  const uint4 *kids;        // the root's children (last octant first: walk order)
+  const u8 *nchild;
+  const uint2 *rows;        // later rounds: the last round's deferred (group, node) pairs,
+  const u8 *dec;            // the network's decisions (1 accept)
+  const u32 *roff;          // and each group's first row (ng + 1)
   Scalars *sc;
 };
 
-__global__ void __launch_bounds__(kT, 5) k_lwalk(LArgs a) {
-  const int lane = threadIdx.x & 31;
-  const FeatScale fs = scale_of(a.root, a.mom);
-  const u64 gtid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
-  u32 lc = a.lane_fill[3 * gtid], lr = a.lane_fill[3 * gtid + 1], lp = a.lane_fill[3 * gtid + 2];
-  u32 *reg_c = a.reg_cells + gtid * a.lane_cells;
-  uint2 *reg_r = a.reg_runs + gtid * a.lane_runs;
-  u32 *reg_p = a.reg_pend + gtid * a.lane_pend;
-  Scalars *sc = a.sc;
+// The walk of subtrees [i, end) for one group, the first node's verdict
+// given when pre >= 0; cells, bodies and deferred pairs to cl, bl, pl
+// (capacities capc, capb, capp; counting goes on past them).
+struct LWalkState {
+  u64 nc, nb;
+  u32 np, visits;
+};
 
-  u64 item = kNoItem, store = 0;
-  u32 i = 0, end = 0, c0i = 0, r0i = 0, p0i = 0, nb = 0, grp = 0, visits = 0;
-  int pre = -1;  // the network's decision on a deferred item's node
-  bool exhausted = false;
-  float gf[3] = {0.f, 0.f, 0.f}, hf[3] = {0.f, 0.f, 0.f};
-  float acc_d2 = 0.f, open_d2 = 0.f;  // the item's group: d^2 scales of the accept and open tests
-  const float l2 = 1.f / (fs.inv_l * fs.inv_l);
-  while (true) {
-    // idle lanes take the next items (one atomic per warp), once at least
-    // kGrabLanes of them wait or no lane has work: the grab runs with its
-    // lanes together instead of for one or two lanes every step
-    const bool want = item == kNoItem && !exhausted;
-    const unsigned wantm = __ballot_sync(kFullMask, want);
-    const unsigned busym = __ballot_sync(kFullMask, item != kNoItem);
-    if (wantm && (__popc(wantm) >= kGrabLanes || busym == 0)) {
-      const int leader = __ffs(wantm) - 1;
-      unsigned long long base = 0;
-      if (lane == leader)
-        base = atomicAdd(&sc->walk_items, static_cast<unsigned long long>(__popc(wantm)));
-      base = __shfl_sync(kFullMask, base, leader);
-      if (want) {
-        const u64 k = base + __popc(wantm & ((1u << lane) - 1u));
-        if (k >= a.nitems) {
-          exhausted = true;
-        } else {
-          item = k;
-          u32 &g = grp;
-          const uint2 q = a.qitems[k];
-          g = q.x;
-          i = q.y;
-          store = k;
-          pre = a.qdec ? a.qdec[k] : -1;
-          end = __float_as_uint(__ldg(reinterpret_cast<const float4 *>(a.lrec + i) + 2).x);
-          const float4 b0 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g],
-                       b1 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g + 1];
-          gf[0] = b0.x;
-          gf[1] = b0.y;
-          gf[2] = b0.z;
-          hf[0] = b0.w;
-          hf[1] = b1.x;
-          hf[2] = b1.y;
-          const float tau = a.gtol[g].y;
-          acc_d2 = exp2f(0.4f * (a.band - tau)) * l2;
-          open_d2 = exp2f(0.4f * (-a.band - tau)) * l2;
-          c0i = lc;
-          r0i = lr;
-          p0i = lp;
-          nb = 0;
-        }
-      }
-    }
-    if (__ballot_sync(kFullMask, item != kNoItem) == 0) break;
-    if (item == kNoItem) continue;  // the lanes meet again at the next ballot
-
+__device__ __forceinline__ void lwalk_range(const GArgs &a, const float *gf, const float *hf,
+                                            float acc_d2, float open_d2, u32 i, u32 end, int pre,
+                                            u32 *cl, u32 *bl, u32 *pl, u32 capc, u32 capb,
+                                            u32 capp, LWalkState &w) {
+  while (i < end) {
     const float4 *rp = reinterpret_cast<const float4 *>(a.lrec + i);
     const float4 ra = __ldg(rp), rb = __ldg(rp + 1), rc = __ldg(rp + 2);
-    LWalkRec r;
-    r.cx = ra.x;
-    r.cy = ra.y;
-    r.cz = ra.z;
-    r.slack = ra.w;
-    r.mx = rb.x;
-    r.my = rb.y;
-    r.mz = rb.z;
-    r.guard2 = rb.w;
-    r.skip = __float_as_uint(rc.x);
-    r.nbody_leaf = __float_as_uint(rc.y);
-    r.begin = __float_as_uint(rc.z);
-    r.pscale = rc.w;
-    ++visits;
-    const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+    ++w.visits;
+    const u32 skip = __float_as_uint(rc.x), nbody_leaf = __float_as_uint(rc.y);
+    const u32 nbody = nbody_leaf & 0x7fffffffu;
     int verdict;  // 0 open, 1 accept, 2 defer
     if (pre >= 0) {
       verdict = pre;
       pre = -1;
     } else {
       // the reference's overlap test (group_lists.cpp:147), in FP32
-      const bool overlap = fabsf(r.cx - gf[0]) <= r.slack + hf[0] &&
-                           fabsf(r.cy - gf[1]) <= r.slack + hf[1] &&
-                           fabsf(r.cz - gf[2]) <= r.slack + hf[2];
-      const float dx = fmaxf(fabsf(r.mx - gf[0]) - hf[0], 0.f),
-                  dy = fmaxf(fabsf(r.my - gf[1]) - hf[1], 0.f),
-                  dz = fmaxf(fabsf(r.mz - gf[2]) - hf[2], 0.f);
+      const bool overlap = fabsf(ra.x - gf[0]) <= ra.w + hf[0] &&
+                           fabsf(ra.y - gf[1]) <= ra.w + hf[1] &&
+                           fabsf(ra.z - gf[2]) <= ra.w + hf[2];
+      const float dx = fmaxf(fabsf(rb.x - gf[0]) - hf[0], 0.f),
+                  dy = fmaxf(fabsf(rb.y - gf[1]) - hf[1], 0.f),
+                  dz = fmaxf(fabsf(rb.z - gf[2]) - hf[2], 0.f);
       const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (overlap || !(d2 > r.guard2)) {
+      if (overlap || !(d2 > rb.w)) {
         verdict = 0;
       } else if (nbody <= kFewBodies) {
         verdict = 1;
       } else {
-        verdict = d2 > r.pscale * acc_d2 ? 1 : d2 < r.pscale * open_d2 ? 0 : 2;
+        verdict = d2 > rc.w * acc_d2 ? 1 : d2 < rc.w * open_d2 ? 0 : 2;
       }
     }
     if (verdict == 2) {
-      if (lp < a.lane_pend) reg_p[lp] = i;
-      ++lp;
+      if (w.np < capp) pl[w.np] = i;
+      ++w.np;
     } else if (verdict == 1 && nbody > kFewBodies) {
-      if (lc < a.lane_cells) reg_c[lc] = i;
-      ++lc;
-    } else if (verdict == 1 || (r.nbody_leaf >> 31)) {
-      if (lr < a.lane_runs) reg_r[lr] = make_uint2(r.begin, nbody);
-      ++lr;
-      nb += nbody;
+      if (w.nc < capc) cl[w.nc] = i;
+      ++w.nc;
+    } else if (verdict == 1 || (nbody_leaf >> 31)) {
+      const u32 first = __float_as_uint(rc.z);
+      for (u32 j = 0; j < nbody && w.nb + j < capb; ++j) bl[w.nb + j] = first + j;
+      w.nb += nbody;
     }
-    if (verdict != 0 || (r.nbody_leaf >> 31)) {
-      if (r.skip <= i) {  // malformed tree: never loop
-        atomicOr(&sc->error, 1u);
-        i = end;
-      } else {
-        i = r.skip;
+    if (verdict != 0 || (nbody_leaf >> 31)) {
+      if (skip <= i) {  // malformed tree: never loop
+        atomicOr(&a.sc->error, 1u);
+        return;
       }
+      i = skip;
     } else {
       ++i;
     }
-    if (i >= end) {  // the item is done
-      const u64 gi = a.item_base + store;
-      a.seg[gi] = make_uint4(static_cast<u32>(gtid * a.lane_cells + c0i), lc - c0i,
-                             static_cast<u32>(gtid * a.lane_runs + r0i), lr - r0i);
-      a.seg2[gi] = make_uint4(static_cast<u32>(gtid * a.lane_pend + p0i), lp - p0i, nb, 0u);
-      a.pcount[store] = lp - p0i;
-      if (lc > c0i) atomicAdd(&a.gcells[grp], static_cast<unsigned long long>(lc - c0i));
-      if (nb) atomicAdd(&a.gbodies[grp], static_cast<unsigned long long>(nb));
-      item = kNoItem;
+  }
+}
+
+__device__ __forceinline__ u32 lskip(const LWalkRec *lrec, u32 i) {
+  return __float_as_uint(__ldg(reinterpret_cast<const float4 *>(lrec + i) + 2).x);
+}
+
+__device__ __forceinline__ void group_scales(const GArgs &a, u32 g, float *gf, float *hf,
+                                             float &acc_d2, float &open_d2) {
+  const float4 b0 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g],
+               b1 = reinterpret_cast<const float4 *>(a.gboxf)[2ull * g + 1];
+  gf[0] = b0.x;
+  gf[1] = b0.y;
+  gf[2] = b0.z;
+  hf[0] = b0.w;
+  hf[1] = b1.x;
+  hf[2] = b1.y;
+  const float tau = a.gtol[g].y;
+  const FeatScale fs = scale_of(a.root, a.mom);
+  const float l2 = 1.f / (fs.inv_l * fs.inv_l);
+  acc_d2 = exp2f(0.4f * (a.band - tau)) * l2;
+  open_d2 = exp2f(0.4f * (-a.band - tau)) * l2;
+}
+
+// A part's maxima and the visits: one atomic per set of converged lanes of
+// the same part (a warp can hold lanes of two parts).
+__device__ __forceinline__ void lround_stats(Scalars *sc, int part, u64 nc, u64 nb, u32 np,
+                                             u32 visits) {
+  auto clamp = [](u64 v) { return static_cast<u32>(v < 0xffffffffull ? v : 0xffffffffull); };
+  const unsigned mask = __match_any_sync(__activemask(), part);
+  const u32 mc = __reduce_max_sync(mask, clamp(nc)), mb = __reduce_max_sync(mask, clamp(nb));
+  const u32 mp = __reduce_max_sync(mask, np), sv = __reduce_add_sync(mask, visits);
+  if ((threadIdx.x & 31) == static_cast<unsigned>(__ffs(mask) - 1)) {
+    atomicMax(&sc->lmax_cells[part], mc);
+    atomicMax(&sc->lmax_bodies[part], mb);
+    atomicMax(&sc->max_pend, mp);
+    atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(sv));
+  }
+}
+
+// Round 0: thread (part, group) walks the part's range of the root's
+// children (the root itself, when it is a leaf, in part 0).
+__global__ void __launch_bounds__(kT) k_lround0(GArgs a) {
+  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (tid >= static_cast<u64>(kParts) * a.ng) return;
+  const int part = static_cast<int>(tid / a.ng);
+  const u32 g = static_cast<u32>(tid % a.ng);
+  float gf[3], hf[3], acc_d2, open_d2;
+  group_scales(a, g, gf, hf, acc_d2, open_d2);
+  const int nc = a.nchild[0];
+  u32 i = 0, end = 0;
+  if (nc == 0) {
+    if (part == 0) end = lskip(a.lrec, 0);
+  } else {
+    const uint4 k0 = a.kids[0], k1 = a.kids[1];
+    const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+    const int j0 = (part * nc + kParts - 1) / kParts, j1 = ((part + 1) * nc + kParts - 1) / kParts;
+    if (j0 < j1) {
+      i = ch[j0];
+      end = lskip(a.lrec, ch[j1 - 1]);
     }
   }
-  warp_add(&sc->walk_nodes, visits);  // the lanes leave the loop together
-  a.lane_fill[3 * gtid] = lc;
-  a.lane_fill[3 * gtid + 1] = lr;
-  a.lane_fill[3 * gtid + 2] = lp;
-  if (lc > a.lane_cells || lr > a.lane_runs || lp > a.lane_pend) atomicOr(&sc->list_overflow, 1u);
+  const u32 capc = a.slot_cells[part], capb = a.slot_bodies[part];
+  u32 *cl = a.cells + a.cells_at[part] + static_cast<u64>(g) * capc;
+  u32 *bl = a.bodies + a.bodies_at[part] + static_cast<u64>(g) * capb;
+  u32 *pl = a.pend + (static_cast<u64>(part) * a.ng + g) * a.slot_pend;
+  LWalkState w{0, 0, 0, 0};
+  lwalk_range(a, gf, hf, acc_d2, open_d2, i, end, -1, cl, bl, pl, capc, capb, a.slot_pend, w);
+  a.ncells[static_cast<u64>(part) * a.ng + g] = w.nc;
+  a.nbodies[static_cast<u64>(part) * a.ng + g] = w.nb;
+  a.pcount[static_cast<u64>(part) * a.ng + g] = w.np;
+  if (w.nc > capc || w.nb > capb || w.np > a.slot_pend) atomicOr(&a.sc->list_overflow, 1u);
+  lround_stats(a.sc, part, w.nc, w.nb, w.np, w.visits);
 }
 
-// Round 0's items of each group (kFill = false: their count): the siblings
-// of the group's path nodes down `split` levels, after the node the path
-// reaches. A path stops early at a leaf or where the group's targets span
-// more than one child.
-constexpr int kMaxSplit = 8;
-
-template <bool kFill>
-__global__ void __launch_bounds__(kT)
-    k_path_items(const u32 *gbegin, const u32 *gend, u32 ng, const u32 *skip, const u32 *nbegin,
-                 const u32 *nend, const u8 *isleaf, int split, u32 *count, const u32 *offset,
-                 uint2 *items) {
+// A later round, one thread per group: the group's deferred pairs of the
+// last round in order, appended to its last part's slot; new deferred pairs
+// to that part's pend slot (the other parts' counts are set to zero).
+__global__ void __launch_bounds__(kT) k_lround(GArgs a) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= ng) return;
-  const u32 b0 = gbegin[g], b1 = gend[g];
-  u32 path[kMaxSplit + 1];
-  int depth = 0;
-  u32 p = 0;
-  path[0] = 0;
-  while (depth < split && !isleaf[p]) {
-    u32 next = 0xffffffffu;
-    for (u32 c = p + 1; c < skip[p]; c = skip[c])
-      if (nbegin[c] <= b0 && b1 <= nend[c]) next = c;
-    if (next == 0xffffffffu) break;
-    p = next;
-    path[++depth] = p;
+  if (g >= a.ng) return;
+  float gf[3], hf[3], acc_d2, open_d2;
+  group_scales(a, g, gf, hf, acc_d2, open_d2);
+  constexpr int last = kParts - 1;
+  const u64 at = static_cast<u64>(last) * a.ng + g;
+  const u32 capc = a.slot_cells[last], capb = a.slot_bodies[last];
+  u32 *cl = a.cells + a.cells_at[last] + static_cast<u64>(g) * capc;
+  u32 *bl = a.bodies + a.bodies_at[last] + static_cast<u64>(g) * capb;
+  u32 *pl = a.pend + at * a.slot_pend;
+  LWalkState w{a.ncells[at], a.nbodies[at], 0, 0};
+  for (u32 k = a.roff[g], k1 = a.roff[g + 1]; k < k1; ++k) {
+    const u32 i = a.rows[k].y;
+    lwalk_range(a, gf, hf, acc_d2, open_d2, i, lskip(a.lrec, i), a.dec[k], cl, bl, pl, capc, capb,
+                a.slot_pend, w);
   }
-  if (!kFill) {
-    u32 n = 1;
-    for (int d = 0; d < depth; ++d)
-      for (u32 c = path[d] + 1; c < skip[path[d]]; c = skip[c]) n += c != path[d + 1];
-    count[g] = n;
-    return;
-  }
-  u64 o = offset[g];
-  items[o++] = make_uint2(g, p);  // the near field first
-  for (int d = 0; d < depth; ++d)
-    for (u32 c = path[d] + 1; c < skip[path[d]]; c = skip[c])
-      if (c != path[d + 1]) items[o++] = make_uint2(g, c);
+  a.ncells[at] = w.nc;
+  a.nbodies[at] = w.nb;
+  for (int k = 0; k < last; ++k) a.pcount[static_cast<u64>(k) * a.ng + g] = 0;
+  a.pcount[at] = w.np;
+  if (w.nc > capc || w.nb > capb || w.np > a.slot_pend) atomicOr(&a.sc->list_overflow, 1u);
+  lround_stats(a.sc, last, w.nc, w.nb, w.np, w.visits);
 }
 
-// Start of every group's deferred pairs in the next round's item order,
-// from the exclusive scan of the deferred counts and the starts of the
-// groups' items in this round.
-__global__ void __launch_bounds__(kT)
-    k_lgstart(u32 ng, const u32 *poff, const u32 *cur, u32 *next) {
+// Each group's deferred pairs of a round, over the parts.
+__global__ void __launch_bounds__(kT) k_lpend_total(const GArgs a, u32 *total) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g > ng) return;
-  next[g] = poff[cur[g]];
+  if (g >= a.ng) return;
+  u32 t = 0;
+  for (int k = 0; k < kParts; ++k) t += a.pcount[static_cast<u64>(k) * a.ng + g];
+  total[g] = t;
 }
 
-// The deferred pairs of a round, in storage order, as the next round's items.
-__global__ void __launch_bounds__(kT)
-    k_lcompact(u64 nitems, u64 item_base, const uint2 *qitems, const uint4 *seg2,
-               const u32 *poff, const u32 *reg_pend, uint2 *next) {
-  const u64 j = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
-  if (j >= nitems) return;
-  const uint4 s2 = seg2[item_base + j];
-  if (s2.y == 0) return;
-  const u32 g = qitems[j].x;
-  const u32 o = poff[j];
-  for (u32 m = 0; m < s2.y; ++m) next[o + m] = make_uint2(g, reg_pend[s2.x + m]);
+// A round's deferred pairs as dense rows, each group's in its order (part
+// by part).
+__global__ void __launch_bounds__(kT) k_lrows(const GArgs a, const u32 *roff, uint2 *rows) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (g >= a.ng) return;
+  u32 o = roff[g];
+  for (int k = 0; k < kParts; ++k) {
+    const u64 at = static_cast<u64>(k) * a.ng + g;
+    const u32 n = a.pcount[at];
+    const u32 *pl = a.pend + at * a.slot_pend;
+    for (u32 j = 0; j < n; ++j) rows[o++] = make_uint2(g, pl[j]);
+  }
+}
+
+// Group records of the learned walk (the parts' slots, one segment each) and
+// the list statistics.
+__global__ void __launch_bounds__(kT) k_lgroup_records(const GArgs a, const u32 *gbegin,
+                                                       const u32 *gend, uint4 *groups) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  const bool valid = g < a.ng;
+  u64 t = 0, nc = 0, nb = 0;
+  if (valid) {
+    ListSegs cs, bs;
+    for (int k = 0; k < kParts; ++k) {
+      const u64 at = static_cast<u64>(k) * a.ng + g;
+      cs.start[k] = static_cast<u32>(a.cells_at[k] + static_cast<u64>(g) * a.slot_cells[k]);
+      cs.count[k] = static_cast<u32>(a.ncells[at]);
+      bs.start[k] = static_cast<u32>(a.bodies_at[k] + static_cast<u64>(g) * a.slot_bodies[k]);
+      bs.count[k] = static_cast<u32>(a.nbodies[at]);
+      nc += a.ncells[at];
+      nb += a.nbodies[at];
+    }
+    store_group_rec(groups, g, gbegin[g], gend[g], cs, bs);
+    t = gend[g] - gbegin[g];
+  }
+  group_stats_warp(a.sc, valid, t, nc, nb, true, false);
 }
 
 // The network's decision on every deferred pair: one warp per 32 pairs.
@@ -541,115 +525,6 @@ __global__ void __launch_bounds__(kT)
   __syncwarp();
   const float y = warp_mlp(rows[warp], sn.w1, sn.w2, sn.b2, sn.w3, net->b3, lane);
   if (k < nq) dec[k] = y < thr ? 1 : 0;
-}
-
-struct RoundView {
-  const u64 *base;         // per round: global index of its first item
-  const u32 *gstart;       // per round: [ng + 1] starts of the groups' items
-  u32 rounds, ng;
-};
-
-// Copies one item's cells and body runs to the group's lists at (oc, ob),
-// all lanes of the warp together.
-__device__ __forceinline__ void copy_item_warp(const uint4 &sg, const u32 *reg_cells,
-                                               const uint2 *reg_runs, u32 *cell_list,
-                                               u32 *body_list, u64 oc, u64 ob, int lane) {
-  for (u32 k = lane; k < sg.y; k += 32) cell_list[oc + k] = reg_cells[sg.x + k];
-  for (u32 k0 = 0; k0 < sg.w; k0 += 32) {
-    const u32 k = k0 + lane;
-    const uint2 run = k < sg.w ? reg_runs[sg.z + k] : make_uint2(0u, 0u);
-    u32 incl = run.y;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const u32 v = __shfl_up_sync(kFullMask, incl, o);
-      if (lane >= o) incl += v;
-    }
-    const u64 start = ob + incl - run.y;
-    for (u32 j = 0; j < run.y; ++j) body_list[start + j] = run.x + j;
-    ob += __shfl_sync(kFullMask, incl, 31);
-  }
-}
-
-__device__ __forceinline__ u32 warp_exclusive_scan(u32 v, int lane) {
-  u32 incl = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const u32 x = __shfl_up_sync(kFullMask, incl, o);
-    if (lane >= o) incl += x;
-  }
-  return incl - v;
-}
-
-constexpr u32 kSmallItem = 8;  // items with at most this many cells and runs copy by lane
-
-// One warp per group: its items' lists in (round, item) order into the
-// group's ranges of cell_list and body_list, its GTGroup record and the
-// list counters. Each batch of 32 items gets its output offsets from warp
-// scans; small items (most deferred ones: one cell, or a leaf's run) are
-// copied by their own lane, large ones by the whole warp.
-constexpr int kGatherWarps = kT / 32;
-
-__global__ void __launch_bounds__(kT)
-    k_lgather(const uint4 *seg, const uint4 *seg2, RoundView rv, const u32 *reg_cells,
-              const uint2 *reg_runs, const u32 *gbegin, const u32 *gend, const u64 *cell_off,
-              const u64 *body_off, u32 *cell_list, u32 *body_list, uint4 *groups, Scalars *sc) {
-  const u32 g = blockIdx.x * kGatherWarps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (g >= rv.ng) return;
-  u64 oc = cell_off[g], ob = body_off[g];
-  if (lane == 0) {
-    store_group_rec(groups, g, gbegin[g], gend[g], one_segment(oc, cell_off[g + 1] - oc),
-                    one_segment(ob, body_off[g + 1] - ob));
-  }
-  for (u32 r = 0; r < rv.rounds; ++r) {
-    const u32 *st = rv.gstart + static_cast<u64>(r) * (rv.ng + 1);
-    const u64 first = rv.base[r] + st[g], count = st[g + 1] - st[g];
-    for (u64 j0 = 0; j0 < count; j0 += 32) {
-      const u64 j = j0 + lane;
-      const bool have = j < count;
-      const uint4 sg = have ? seg[first + j] : make_uint4(0u, 0u, 0u, 0u);
-      const u32 nbj = have ? seg2[first + j].z : 0u;
-      const u32 cs = warp_exclusive_scan(sg.y, lane), bs = warp_exclusive_scan(nbj, lane);
-      const bool small = sg.y <= kSmallItem && sg.w <= kSmallItem;
-      if (small) {
-        for (u32 k = 0; k < sg.y; ++k) cell_list[oc + cs + k] = reg_cells[sg.x + k];
-        u64 o = ob + bs;
-        for (u32 k = 0; k < sg.w; ++k) {
-          const uint2 run = reg_runs[sg.z + k];
-          for (u32 q = 0; q < run.y; ++q) body_list[o + q] = run.x + q;
-          o += run.y;
-        }
-      }
-      unsigned big = __ballot_sync(kFullMask, !small);
-      while (big) {
-        const int src = __ffs(big) - 1;
-        big &= big - 1u;
-        const uint4 s4 = make_uint4(__shfl_sync(kFullMask, sg.x, src),
-                                    __shfl_sync(kFullMask, sg.y, src),
-                                    __shfl_sync(kFullMask, sg.z, src),
-                                    __shfl_sync(kFullMask, sg.w, src));
-        const u32 c_at = __shfl_sync(kFullMask, cs, src), b_at = __shfl_sync(kFullMask, bs, src);
-        copy_item_warp(s4, reg_cells, reg_runs, cell_list, body_list, oc + c_at, ob + b_at, lane);
-      }
-      oc += __shfl_sync(kFullMask, cs + sg.y, 31);
-      ob += __shfl_sync(kFullMask, bs + nbj, 31);
-    }
-  }
-}
-
-// The groups' list statistics, one group per lane.
-__global__ void __launch_bounds__(kT)
-    k_list_stats(const u32 *gbegin, const u32 *gend, const u64 *cell_off, const u64 *body_off,
-                 u32 ng, Scalars *sc) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  const bool valid = g < ng;
-  u64 t = 0, nc = 0, nb = 0;
-  if (valid) {
-    t = gend[g] - gbegin[g];
-    nc = cell_off[g + 1] - cell_off[g];
-    nb = body_off[g + 1] - body_off[g];
-  }
-  group_stats_warp(sc, valid, t, nc, nb, false);
 }
 
 // The walk's inference on given raw features (tests and diagnostics).
@@ -717,121 +592,98 @@ void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cuda
   GTC_LAUNCH_CHECK();
 }
 
+namespace {
+// Slots for the next learned walk: the longest lists plus a half and 64, in
+// multiples of 32 entries.
+u32 learned_slot(u64 longest) {
+  const u64 v = (longest + longest / 2 + 64 + 31) & ~31ull;
+  return static_cast<u32>(std::min<u64>(v, 0x7fffffe0ull));
+}
+}  // namespace
+
 void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
                          cudaStream_t s) {
+  static_assert(kParts == kListSegments, "one list segment per part");
   if (ng == 0) return;
   Scalars *sc = ws.scalars.as<Scalars>();
-  int dev = 0, sms = 0, per_sm = 0;
-  GTC_CUDA(cudaGetDevice(&dev));
-  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lwalk, kT, 0));
-  const u32 blocks = static_cast<u32>(std::max(1, sms * std::max(1, per_sm)));
-  const u64 lanes = static_cast<u64>(blocks) * kT;
   LearnedScratch &ls = *lw.scratch;
-  const int split = std::min(std::max(lw.split_depth, 0), kMaxSplit);
-  ws.gcells.ensure(static_cast<u64>(ng) * 8);
-  ws.gbodies.ensure(static_cast<u64>(ng) * 8);
-  ws.gcell_off.ensure((static_cast<u64>(ng) + 1) * 8);
-  ws.gbody_off.ensure((static_cast<u64>(ng) + 1) * 8);
-  ls.gstart.ensure(static_cast<u64>(kMaxRounds + 1) * (ng + 1) * sizeof(u32));
-  ls.lane_fill.ensure(lanes * 3 * sizeof(u32));
-  LArgs a{};
-  a.walk32 = ws.walk32.as<WalkRec32>();
-  a.cfeat = lw.cfeat;
+  if (ls.slot_cells[0] == 0) {  // the first learned walk: the theta walk's slots to start with
+    for (int k = 0; k < kParts; ++k) {
+      ls.slot_cells[k] = std::max<u32>(ws.slot_cells / 2, 256);
+      ls.slot_bodies[k] = std::max<u32>(ws.slot_bodies / 2, 256);
+    }
+    ls.slot_pend = 256;
+  }
+  ws.gcells.ensure(static_cast<u64>(kParts) * ng * 8);
+  ws.gbodies.ensure(static_cast<u64>(kParts) * ng * 8);
+  ls.pcount.ensure(static_cast<u64>(kParts) * ng * sizeof(u32));
+  ls.ptotal.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
+  ls.roff.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
+  GArgs a{};
   a.lrec = ls.lrec.as<LWalkRec>();
   a.gboxf = ws.gboxf.as<float>();
   a.gtol = lw.gtol->as<float2>();
   a.ng = ng;
   a.root = ws.root.as<TreeRoot>();
   a.mom = ws.mom.as<double2>();
-  a.inv_theta_guard = lw.inv_theta_guard;
   a.band = lw.band;
-  a.y_mean = lw.y_mean;
-  a.lane_fill = ls.lane_fill.as<u32>();
-  a.gcells = reinterpret_cast<unsigned long long *>(ws.gcells.as<u64>());
-  a.gbodies = reinterpret_cast<unsigned long long *>(ws.gbodies.as<u64>());
+  a.ncells = ws.gcells.as<u64>();
+  a.nbodies = ws.gbodies.as<u64>();
+  a.pcount = ls.pcount.as<u32>();
+  a.kids = ws.kids.as<uint4>();
+  a.nchild = ws.nchild.as<u8>();
+  a.roff = ls.roff.as<u32>();
   a.sc = sc;
-  std::vector<u64> base;
+  const u32 gb = ceil_div(ng, kT);
+  u64 rows = 0, batches = 0;
+  u32 rounds = 0;
   for (int attempt = 0;; ++attempt) {
-    // lane regions (grown and walked again if one overflows)
-    const u64 reg_bytes = lanes * (static_cast<u64>(ls.lane_cells) * 4 +
-                                   static_cast<u64>(ls.lane_runs) * 8 +
-                                   static_cast<u64>(ls.lane_pend) * 4);
-    ls.regions.ensure(reg_bytes);
-    char *rb = ls.regions.as<char>();
-    a.reg_runs = reinterpret_cast<uint2 *>(rb);
-    a.reg_cells = reinterpret_cast<u32 *>(rb + lanes * static_cast<u64>(ls.lane_runs) * 8);
-    a.reg_pend = a.reg_cells + lanes * static_cast<u64>(ls.lane_cells);
-    a.lane_cells = ls.lane_cells;
-    a.lane_runs = ls.lane_runs;
-    a.lane_pend = ls.lane_pend;
-    GTC_CUDA(cudaMemsetAsync(a.lane_fill, 0, lanes * 3 * sizeof(u32), s));
-    GTC_CUDA(cudaMemsetAsync(ws.gcells.ptr, 0, static_cast<u64>(ng) * 8, s));
-    GTC_CUDA(cudaMemsetAsync(ws.gbodies.ptr, 0, static_cast<u64>(ng) * 8, s));
+    u64 c_at = 0, b_at = 0;
+    for (int k = 0; k < kParts; ++k) {
+      a.slot_cells[k] = ls.slot_cells[k];
+      a.slot_bodies[k] = ls.slot_bodies[k];
+      a.cells_at[k] = c_at;
+      a.bodies_at[k] = b_at;
+      c_at += static_cast<u64>(ng) * ls.slot_cells[k];
+      b_at += static_cast<u64>(ng) * ls.slot_bodies[k];
+    }
+    if (c_at > 0xffffffffull || b_at > 0xffffffffull)
+      throw RuntimeError("interaction lists too long for 32 bit offsets");
+    ws.cell_list.ensure(std::max<u64>(1, c_at) * 4);
+    ws.body_list.ensure(std::max<u64>(1, b_at) * 4);
+    ls.pend.ensure(std::max<u64>(1, static_cast<u64>(kParts) * ng * ls.slot_pend) * 4);
+    a.slot_pend = ls.slot_pend;
+    a.cells = ws.cell_list.as<u32>();
+    a.bodies = ws.body_list.as<u32>();
+    a.pend = ls.pend.as<u32>();
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
-    GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
-    // round 0's items: each group's path split
-    u32 *st0 = ls.gstart.as<u32>();
-    ls.pcount.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
-    k_path_items<false><<<ceil_div(ng, kT), kT, 0, s>>>(
-        ws.gbegin.as<u32>(), ws.gend.as<u32>(), ng, ws.skip.as<u32>(), ws.nbegin.as<u32>(),
-        ws.nend.as<u32>(), ws.isleaf.as<u8>(), split, ls.pcount.as<u32>(), nullptr, nullptr);
-    GTC_LAUNCH_CHECK();
-    exclusive_scan_u32(ls.pcount.as<u32>(), st0, ng, st0 + ng, ws.scan_tmp, s);
-    u32 n0 = 0;
-    GTC_CUDA(cudaMemcpyAsync(&n0, st0 + ng, sizeof(u32), cudaMemcpyDeviceToHost, s));
-    GTC_CUDA(cudaStreamSynchronize(s));
-    ls.q[0].ensure(static_cast<u64>(n0) * sizeof(uint2));
-    k_path_items<true><<<ceil_div(ng, kT), kT, 0, s>>>(
-        ws.gbegin.as<u32>(), ws.gend.as<u32>(), ng, ws.skip.as<u32>(), ws.nbegin.as<u32>(),
-        ws.nend.as<u32>(), ws.isleaf.as<u8>(), split, nullptr, st0, ls.q[0].as<uint2>());
-    GTC_LAUNCH_CHECK();
-    base.assign(1, 0);
-    u64 nitems = n0, total_items = 0, rows = 0, batches = 0;
-    int qsel = 0;
+    GTC_CUDA(cudaMemsetAsync(sc->lmax_cells, 0, (2 * kParts + 1) * sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
+    rows = batches = 0;
     bool overflow = false;
-    for (u32 round = 0;; ++round) {
-      if (round >= static_cast<u32>(kMaxRounds))
+    int qsel = 0;
+    for (rounds = 0;; ++rounds) {
+      if (rounds >= static_cast<u32>(kMaxRounds))
         throw RuntimeError("learned walk: more rounds than the tree has levels");
-      const u64 need = base.back() + nitems;
-      if (need > ls.items_cap) {  // grow the item arrays, keeping what is there
-        const u64 cap = std::max<u64>(need + need / 2, static_cast<u64>(n0) + 4ull * ng);
-        DeviceBuffer nseg;
-        nseg.ensure(cap * 2 * sizeof(uint4));
-        if (ls.items_cap && base.back())
-          for (int h = 0; h < 2; ++h)
-            GTC_CUDA(cudaMemcpyAsync(nseg.as<uint4>() + h * cap, ls.seg.as<uint4>() + h * ls.items_cap,
-                                     base.back() * sizeof(uint4), cudaMemcpyDeviceToDevice, s));
-        GTC_CUDA(cudaStreamSynchronize(s));
-        ls.seg.release();
-        ls.seg = nseg;
-        ls.items_cap = cap;
+      if (rounds == 0) {
+        k_lround0<<<ceil_div(static_cast<u64>(kParts) * ng, kT), kT, 0, s>>>(a);
+      } else {
+        a.rows = ls.q[qsel].as<uint2>();
+        a.dec = ls.dec[qsel].as<u8>();
+        k_lround<<<gb, kT, 0, s>>>(a);
       }
-      a.seg = ls.seg.as<uint4>();
-      a.seg2 = a.seg + ls.items_cap;
-      ls.pcount.ensure((nitems + 1) * sizeof(u32));
-      ls.poff.ensure((nitems + 1) * sizeof(u32));
-      a.pcount = ls.pcount.as<u32>();
-      a.nitems = nitems;
-      a.item_base = base.back();
-      a.qitems = ls.q[qsel].as<uint2>();
-      a.qdec = round ? ls.dec[qsel].as<u8>() : nullptr;
-      GTC_CUDA(cudaMemsetAsync(&sc->walk_items, 0, sizeof(unsigned long long), s));
-      k_lwalk<<<blocks, kT, 0, s>>>(a);
       GTC_LAUNCH_CHECK();
-      u32 *poff = ls.poff.as<u32>();
-      exclusive_scan_u32(a.pcount, poff, nitems, poff + nitems, ws.scan_tmp, s);
-      u32 *cur = ls.gstart.as<u32>() + static_cast<u64>(round) * (ng + 1);
-      k_lgstart<<<ceil_div(ng + 1, kT), kT, 0, s>>>(ng, poff, cur, cur + (ng + 1));
+      u32 *roff = ls.roff.as<u32>(), *ptot = ls.ptotal.as<u32>();
+      k_lpend_total<<<gb, kT, 0, s>>>(a, ptot);
       GTC_LAUNCH_CHECK();
+      exclusive_scan_u32(ptot, roff, ng, roff + ng, ws.scan_tmp, s);
       u32 deferred = 0, flags[2] = {0, 0};
-      GTC_CUDA(cudaMemcpyAsync(&deferred, poff + nitems, sizeof(u32), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(&deferred, roff + ng, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags, &sc->list_overflow, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags + 1, &sc->error, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaStreamSynchronize(s));
-      total_items = base.back() + nitems;
       if (flags[1])
         throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
                            std::to_string(flags[1]) + ")");
@@ -840,69 +692,63 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
         break;
       }
       if (deferred == 0) break;
-      // the deferred pairs become the next round's items, with the network's decisions
+      // the deferred pairs as dense rows, with the network's decisions
       const int nq = qsel ^ 1;
       ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
       ls.dec[nq].ensure(deferred);
-      k_lcompact<<<ceil_div(nitems, kT), kT, 0, s>>>(nitems, base.back(), a.qitems, a.seg2, poff,
-                                                    a.reg_pend, ls.q[nq].as<uint2>());
+      k_lrows<<<gb, kT, 0, s>>>(a, roff, ls.q[nq].as<uint2>());
       GTC_LAUNCH_CHECK();
       k_ldecide<<<ceil_div(deferred, kT), kT, 0, s>>>(
-          ls.q[nq].as<uint2>(), deferred, a.walk32, a.cfeat, a.gboxf, a.gtol, lw.net, a.root,
-          a.mom, ls.dec[nq].as<u8>());
+          ls.q[nq].as<uint2>(), deferred, ws.walk32.as<WalkRec32>(), lw.cfeat, a.gboxf, a.gtol,
+          lw.net, ws.root.as<TreeRoot>(), ws.mom.as<double2>(), ls.dec[nq].as<u8>());
       GTC_LAUNCH_CHECK();
       rows += deferred;
       batches += (deferred + 31) / 32;
       qsel = nq;
-      base.push_back(total_items);
-      nitems = deferred;
     }
-    if (!overflow) {
-      host->mlp_rows = rows;
-      host->mlp_batches = batches;
-      ws.list_passes = static_cast<u32>(base.size());
-      break;
+    if (!overflow) break;
+    // a slot was outgrown: the counts went on, so slots of their size fit
+    // that round at least; walk again from the start
+    Scalars h{};
+    GTC_CUDA(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    GTC_CUDA(cudaStreamSynchronize(s));
+    if (attempt >= 4) {
+      std::string m = "learned walk: the list slots keep overflowing (round " +
+                      std::to_string(rounds) + "; slot / longest:";
+      for (int k = 0; k < kParts; ++k)
+        m += " " + std::to_string(ls.slot_cells[k]) + "/" + std::to_string(h.lmax_cells[k]) + " " +
+             std::to_string(ls.slot_bodies[k]) + "/" + std::to_string(h.lmax_bodies[k]);
+      m += " pend " + std::to_string(ls.slot_pend) + "/" + std::to_string(h.max_pend) + ")";
+      throw RuntimeError(m);
     }
-    if (attempt >= 4 || lanes * static_cast<u64>(ls.lane_cells) * 2 > 0xffffffffull ||
-        lanes * static_cast<u64>(ls.lane_runs) * 2 > 0xffffffffull ||
-        lanes * static_cast<u64>(ls.lane_pend) * 2 > 0xffffffffull)
-      throw RuntimeError("learned walk: the lane regions keep overflowing");
-    ls.lane_cells *= 2;
-    ls.lane_runs *= 2;
-    ls.lane_pend *= 2;
+    for (int k = 0; k < kParts; ++k) {
+      ls.slot_cells[k] = std::max<u32>(ls.slot_cells[k], learned_slot(h.lmax_cells[k]));
+      ls.slot_bodies[k] = std::max<u32>(ls.slot_bodies[k], learned_slot(h.lmax_bodies[k]));
+    }
+    ls.slot_pend = std::max<u32>(ls.slot_pend, learned_slot(h.max_pend));
   }
-  const u32 rounds = static_cast<u32>(base.size());
-  ls.base.ensure(rounds * sizeof(u64));
-  GTC_CUDA(cudaMemcpyAsync(ls.base.ptr, base.data(), rounds * sizeof(u64), cudaMemcpyHostToDevice, s));
+  // group records and statistics
+  GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
+  host->mlp_rows = rows;
+  host->mlp_batches = batches;
   GTC_CUDA(cudaMemcpyAsync(&sc->mlp_rows, &host->mlp_rows, 2 * sizeof(unsigned long long),
                            cudaMemcpyHostToDevice, s));
-  const RoundView rv{ls.base.as<u64>(), ls.gstart.as<u32>(), rounds, ng};
-  u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
-  exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, ng, cell_off + ng, ws.scan_tmp, s);
-  exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, ng, body_off + ng, ws.scan_tmp, s);
-  GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + ng, 8, cudaMemcpyDeviceToDevice, s));
-  GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + ng, 8, cudaMemcpyDeviceToDevice, s));
-  u64 totals[2] = {0, 0};
-  GTC_CUDA(cudaMemcpyAsync(totals, &sc->n_cell_list, sizeof(totals), cudaMemcpyDeviceToHost, s));
+  k_lgroup_records<<<gb, kT, 0, s>>>(a, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
+                                     ws.groups.as<uint4>());
+  GTC_LAUNCH_CHECK();
+  GTC_CUDA(cudaMemcpyAsync(host, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
-  if (totals[0] > 0xffffffffull || totals[1] > 0xffffffffull)
-    throw RuntimeError("interaction lists too long for 32 bit offsets");
-  ws.n_cell_list = totals[0];
-  ws.n_body_list = totals[1];
-  host->n_cell_list = totals[0];
-  host->n_body_list = totals[1];
-  ws.cell_list.ensure(std::max<u64>(1, ws.n_cell_list) * 4);
-  ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
-  k_lgather<<<ceil_div(ng, kGatherWarps), kT, 0, s>>>(
-      a.seg, a.seg2, rv, a.reg_cells, a.reg_runs, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
-      cell_off, body_off, ws.cell_list.as<u32>(), ws.body_list.as<u32>(), ws.groups.as<uint4>(),
-      sc);
-  GTC_LAUNCH_CHECK();
-  k_list_stats<<<ceil_div(ng, kT), kT, 0, s>>>(ws.gbegin.as<u32>(), ws.gend.as<u32>(), cell_off,
-                                               body_off, ng, sc);
-  GTC_LAUNCH_CHECK();
+  ws.n_cell_list = host->n_cell_list;
+  ws.n_body_list = host->n_body_list;
+  ws.gapped = true;
+  ws.list_passes = rounds + 1;
+  // slots for the next learned walk, from this one's longest lists
+  for (int k = 0; k < kParts; ++k) {
+    ls.slot_cells[k] = learned_slot(host->lmax_cells[k]);
+    ls.slot_bodies[k] = learned_slot(host->lmax_bodies[k]);
+  }
+  ls.slot_pend = learned_slot(host->max_pend);
 }
-
 
 void learned_record_amag(const float4 *out, const u32 *order, u64 n, float *amag,
                          cudaStream_t s) {

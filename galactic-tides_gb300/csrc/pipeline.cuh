@@ -71,7 +71,7 @@ struct Workspace {
       arrive, bucket, walk32, walk64, cells;
   // groups and lists
   DeviceBuffer tasks, gbegin, gend, gbox, gboxf, gcells, gbodies, gcell_off, gbody_off, groups, cell_list,
-      body_list, spill;
+      body_list, spill, splitpt;
   // scalars and reductions
   DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
@@ -86,7 +86,7 @@ struct Workspace {
   // slot_bodies (capacities sized from the previous walk's longest lists);
   // 0 until a walk has measured them. `gapped`: the current lists use that
   // layout (groups' ranges are not back to back).
-  u32 slot_cells = 0, slot_bodies = 0;
+  u32 slot_cells = 0, slot_bodies = 0, slot_near_cells = 0, slot_near_bodies = 0;
   bool gapped = false;
   u32 list_passes = 0;  // walks of the last list build (1 one pass, 2 count + fill, rounds)
   // Overflow pool behind n_groups slots of `slot` entries: a sixteenth of
@@ -112,7 +112,12 @@ struct Scalars {
   u32 list_overflow;      // learned walk: a lane's region overflowed
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)
-  u32 max_cells, max_bodies;  // longest cell and body list of a group
+  u32 max_cells, max_bodies;  // longest cell and body list of a group (one-pass walk: its rest)
+  u32 max_near_cells, max_near_bodies;  // one-pass walk: longest lists of a near-field walk
+  // learned walk: longest lists of each part of round 0 (cells, then
+  // bodies; the last part also holds the later rounds), most pairs a group
+  // deferred in a round
+  u32 lmax_cells[3], lmax_bodies[3], max_pend;
   unsigned long long spill_used[2];  // one-pass walk: overflow pool entries taken (cells, bodies)
   u32 spilled;            // one-pass walk: groups that outgrew their slots
   unsigned long long walk_nodes;  // node records the walk tested
@@ -123,7 +128,7 @@ struct Scalars {
 // warp; every lane of the warp must call it. With `totals`, the list
 // lengths are added to the list sizes too.
 __device__ __forceinline__ void group_stats_warp(Scalars *sc, bool valid, u64 t, u64 nc, u64 nb,
-                                                 bool totals) {
+                                                 bool totals, bool maxima = true) {
   unsigned long long ci = valid ? t * nc : 0, bi = valid ? t * nb - t : 0,
                      ml = valid ? nc + nb : 0, tc = valid ? nc : 0, tb = valid ? nb : 0;
   u32 mg = valid ? static_cast<u32>(t) : 0u;
@@ -141,13 +146,16 @@ __device__ __forceinline__ void group_stats_warp(Scalars *sc, bool valid, u64 t,
   mg = __reduce_max_sync(kFullMask, mg);
   mc = __reduce_max_sync(kFullMask, mc);
   mb = __reduce_max_sync(kFullMask, mb);
-  if ((threadIdx.x & 31) != 0 || __ballot_sync(kFullMask, valid) == 0) return;
+  const unsigned any = __ballot_sync(kFullMask, valid);  // every lane, before lane 0 alone goes on
+  if ((threadIdx.x & 31) != 0 || any == 0) return;
   atomicAdd(&sc->cell_interactions, ci);
   atomicAdd(&sc->body_interactions, bi);
   atomicMax(&sc->max_list, ml);
   atomicMax(&sc->max_group, mg);
-  atomicMax(&sc->max_cells, mc);
-  atomicMax(&sc->max_bodies, mb);
+  if (maxima) {
+    atomicMax(&sc->max_cells, mc);
+    atomicMax(&sc->max_bodies, mb);
+  }
   if (totals) {
     atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_cell_list), tc);
     atomicAdd(reinterpret_cast<unsigned long long *>(&sc->n_body_list), tb);
@@ -238,7 +246,8 @@ struct GraphCaps {
   u32 nodes;        // node arrays
   int depth;        // deepest node the per-depth moment launches cover
   u32 groups;       // groups the list slots cover
-  u32 slot_cells, slot_bodies;  // each group's list slots (one-pass walk)
+  u32 slot_cells, slot_bodies;  // each group's list slots (one-pass walk, its rest)
+  u32 slot_near_cells, slot_near_bodies;  // ... and its near-field walk
   u64 pool_cells, pool_bodies;  // overflow pools behind the slots
 };
 // Both stages without a host synchronisation, for stream capture: grids

@@ -288,11 +288,6 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
  *                        with buffers this fraction larger than the last
  *                        solve's tree and lists (0: exactly those sizes, so
  *                        most changes abort the replay and redo it eagerly).
- *   "learned_split_depth" 0..8 (default 2): the learned walk splits each
- *                        group's walk into independent items along the
- *                        group's own path this many levels down (every
- *                        sibling subtree of the path one item). The
- *                        accept/open decisions do not depend on it.
  * GTC_INVALID_ARGUMENT for an unknown name or a value out of range. */
 gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value);
 

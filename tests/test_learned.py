@@ -318,4 +318,4 @@ def test_invalid_learned_arguments(ctx, gtc):
     with pytest.raises(gtc.GtcInvalidArgument):
         ctx.set_option("learned_band_size", 1)
     with pytest.raises(gtc.GtcInvalidArgument):
-        ctx.set_option("learned_split_depth", 9)
+        ctx.set_option("graph_headroom", 5)
