@@ -117,14 +117,14 @@ struct alignas(16) LearnedNet {
 // Device memory of the learned walk, kept between calls.
 struct LearnedScratch {
   DeviceBuffer lrec;                // per node: the walk's record (LWalkRec)
-  DeviceBuffer pend, pcount;        // per part and group: the pairs a round deferred, how many
-  DeviceBuffer roff, ptotal;        // per group: its first deferred row, its count
+  DeviceBuffer pend, pcount, roff;  // per (part, group): the pairs a round deferred, how many,
+                                    // the first of their rows
   DeviceBuffer q[2], dec[2];        // deferred (group, node) rows and the network's decisions
   // per-group slots of the three parts of round 0 (0: not sized yet) and
   // of deferred pairs
   u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
   void release() {
-    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &ptotal, &q[0], &q[1], &dec[0], &dec[1]})
+    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1]})
       b->release();
     for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
     slot_pend = 0;

@@ -276,7 +276,7 @@ struct GArgs {
   const u8 *nchild;
   const uint2 *rows;        // later rounds: the last round's deferred (group, node) pairs,
   const u8 *dec;            // the network's decisions (1 accept)
-  const u32 *roff;          // and each group's first row (ng + 1)
+  const u32 *roff;          // and each (part, group)'s first row (kParts ng + 1)
   Scalars *sc;
 };
 
@@ -414,55 +414,49 @@ __global__ void __launch_bounds__(kT) k_lround0(GArgs a) {
   lround_stats(a.sc, part, w.nc, w.nb, w.np, w.visits);
 }
 
-// A later round, one thread per group: the group's deferred pairs of the
-// last round in order, appended to its last part's slot; new deferred pairs
-// to that part's pend slot (the other parts' counts are set to zero).
+// A later round, kParts threads per group: thread (part, group) takes the
+// pairs its part deferred in the last round, in order, with the network's
+// decisions, appends to the part's slot and defers into the part's pend
+// slot, so a part's lists are its round-0 walk followed by each later
+// round's.
 __global__ void __launch_bounds__(kT) k_lround(GArgs a) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= a.ng) return;
+  const u64 pg = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (pg >= static_cast<u64>(kParts) * a.ng) return;
+  const int part = static_cast<int>(pg / a.ng);
+  const u32 g = static_cast<u32>(pg % a.ng);
+  const u32 k0 = a.roff[pg], k1 = a.roff[pg + 1];
+  if (k0 == k1) {
+    a.pcount[pg] = 0;
+    return;
+  }
   float gf[3], hf[3], acc_d2, open_d2;
   group_scales(a, g, gf, hf, acc_d2, open_d2);
-  constexpr int last = kParts - 1;
-  const u64 at = static_cast<u64>(last) * a.ng + g;
-  const u32 capc = a.slot_cells[last], capb = a.slot_bodies[last];
-  u32 *cl = a.cells + a.cells_at[last] + static_cast<u64>(g) * capc;
-  u32 *bl = a.bodies + a.bodies_at[last] + static_cast<u64>(g) * capb;
-  u32 *pl = a.pend + at * a.slot_pend;
-  LWalkState w{a.ncells[at], a.nbodies[at], 0, 0};
-  for (u32 k = a.roff[g], k1 = a.roff[g + 1]; k < k1; ++k) {
+  const u32 capc = a.slot_cells[part], capb = a.slot_bodies[part];
+  u32 *cl = a.cells + a.cells_at[part] + static_cast<u64>(g) * capc;
+  u32 *bl = a.bodies + a.bodies_at[part] + static_cast<u64>(g) * capb;
+  u32 *pl = a.pend + pg * a.slot_pend;
+  LWalkState w{a.ncells[pg], a.nbodies[pg], 0, 0};
+  for (u32 k = k0; k < k1; ++k) {
     const u32 i = a.rows[k].y;
     lwalk_range(a, gf, hf, acc_d2, open_d2, i, lskip(a.lrec, i), a.dec[k], cl, bl, pl, capc, capb,
                 a.slot_pend, w);
   }
-  a.ncells[at] = w.nc;
-  a.nbodies[at] = w.nb;
-  for (int k = 0; k < last; ++k) a.pcount[static_cast<u64>(k) * a.ng + g] = 0;
-  a.pcount[at] = w.np;
+  a.ncells[pg] = w.nc;
+  a.nbodies[pg] = w.nb;
+  a.pcount[pg] = w.np;
   if (w.nc > capc || w.nb > capb || w.np > a.slot_pend) atomicOr(&a.sc->list_overflow, 1u);
-  lround_stats(a.sc, last, w.nc, w.nb, w.np, w.visits);
+  lround_stats(a.sc, part, w.nc, w.nb, w.np, w.visits);
 }
 
-// Each group's deferred pairs of a round, over the parts.
-__global__ void __launch_bounds__(kT) k_lpend_total(const GArgs a, u32 *total) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= a.ng) return;
-  u32 t = 0;
-  for (int k = 0; k < kParts; ++k) t += a.pcount[static_cast<u64>(k) * a.ng + g];
-  total[g] = t;
-}
-
-// A round's deferred pairs as dense rows, each group's in its order (part
-// by part).
-__global__ void __launch_bounds__(kT) k_lrows(const GArgs a, const u32 *roff, uint2 *rows) {
-  const u32 g = blockIdx.x * kT + threadIdx.x;
-  if (g >= a.ng) return;
-  u32 o = roff[g];
-  for (int k = 0; k < kParts; ++k) {
-    const u64 at = static_cast<u64>(k) * a.ng + g;
-    const u32 n = a.pcount[at];
-    const u32 *pl = a.pend + at * a.slot_pend;
-    for (u32 j = 0; j < n; ++j) rows[o++] = make_uint2(g, pl[j]);
-  }
+// A round's deferred pairs as dense rows, ordered by (part, group) and, for
+// each, in the order they were deferred.
+__global__ void __launch_bounds__(kT) k_lrows(const GArgs a, uint2 *rows) {
+  const u64 pg = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (pg >= static_cast<u64>(kParts) * a.ng) return;
+  const u32 g = static_cast<u32>(pg % a.ng);
+  const u32 n = a.pcount[pg], o = a.roff[pg];
+  const u32 *pl = a.pend + pg * a.slot_pend;
+  for (u32 j = 0; j < n; ++j) rows[o + j] = make_uint2(g, pl[j]);
 }
 
 // Group records of the learned walk (the parts' slots, one segment each) and
@@ -616,9 +610,9 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   }
   ws.gcells.ensure(static_cast<u64>(kParts) * ng * 8);
   ws.gbodies.ensure(static_cast<u64>(kParts) * ng * 8);
-  ls.pcount.ensure(static_cast<u64>(kParts) * ng * sizeof(u32));
-  ls.ptotal.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
-  ls.roff.ensure((static_cast<u64>(ng) + 1) * sizeof(u32));
+  const u64 nparts = static_cast<u64>(kParts) * ng;  // (part, group) pairs
+  ls.pcount.ensure(nparts * sizeof(u32));
+  ls.roff.ensure((nparts + 1) * sizeof(u32));
   GArgs a{};
   a.lrec = ls.lrec.as<LWalkRec>();
   a.gboxf = ws.gboxf.as<float>();
@@ -634,7 +628,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   a.nchild = ws.nchild.as<u8>();
   a.roff = ls.roff.as<u32>();
   a.sc = sc;
-  const u32 gb = ceil_div(ng, kT);
+  const u32 gb = ceil_div(ng, kT), pb = static_cast<u32>(ceil_div(nparts, kT));
   u64 rows = 0, batches = 0;
   u32 rounds = 0;
   for (int attempt = 0;; ++attempt) {
@@ -668,19 +662,17 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       if (rounds >= static_cast<u32>(kMaxRounds))
         throw RuntimeError("learned walk: more rounds than the tree has levels");
       if (rounds == 0) {
-        k_lround0<<<ceil_div(static_cast<u64>(kParts) * ng, kT), kT, 0, s>>>(a);
+        k_lround0<<<pb, kT, 0, s>>>(a);
       } else {
         a.rows = ls.q[qsel].as<uint2>();
         a.dec = ls.dec[qsel].as<u8>();
-        k_lround<<<gb, kT, 0, s>>>(a);
+        k_lround<<<pb, kT, 0, s>>>(a);
       }
       GTC_LAUNCH_CHECK();
-      u32 *roff = ls.roff.as<u32>(), *ptot = ls.ptotal.as<u32>();
-      k_lpend_total<<<gb, kT, 0, s>>>(a, ptot);
-      GTC_LAUNCH_CHECK();
-      exclusive_scan_u32(ptot, roff, ng, roff + ng, ws.scan_tmp, s);
+      u32 *roff = ls.roff.as<u32>();
+      exclusive_scan_u32(a.pcount, roff, nparts, roff + nparts, ws.scan_tmp, s);
       u32 deferred = 0, flags[2] = {0, 0};
-      GTC_CUDA(cudaMemcpyAsync(&deferred, roff + ng, sizeof(u32), cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(&deferred, roff + nparts, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags, &sc->list_overflow, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags + 1, &sc->error, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaStreamSynchronize(s));
@@ -696,7 +688,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       const int nq = qsel ^ 1;
       ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
       ls.dec[nq].ensure(deferred);
-      k_lrows<<<gb, kT, 0, s>>>(a, roff, ls.q[nq].as<uint2>());
+      k_lrows<<<pb, kT, 0, s>>>(a, ls.q[nq].as<uint2>());
       GTC_LAUNCH_CHECK();
       k_ldecide<<<ceil_div(deferred, kT), kT, 0, s>>>(
           ls.q[nq].as<uint2>(), deferred, ws.walk32.as<WalkRec32>(), lw.cfeat, a.gboxf, a.gtol,
