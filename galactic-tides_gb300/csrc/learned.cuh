@@ -152,10 +152,10 @@ void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lr
                           float inv_theta_guard, float y_mean, cudaStream_t s);
 // Per-group group feature and tolerance (inside build_lists, after the group boxes).
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s);
-// The learned walk in rounds (round 0 three threads per group, later rounds
-// one), each group writing into its own slots: group records, cell_list,
-// body_list and the interaction counters of the ng groups (inside
-// build_lists).
+// The learned walk in rounds, three threads per group (one per part of the
+// root's children, later rounds each taking its own part's deferred pairs),
+// each writing into its own slots: group records, cell_list, body_list and
+// the interaction counters of the ng groups (inside build_lists).
 void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
                          cudaStream_t s);
 // |a| per body, caller order, from the evaluator's tree-order output.
