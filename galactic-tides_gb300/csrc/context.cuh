@@ -33,6 +33,8 @@ struct gtc_context {
   gtc::u64 prev_n = 0;              // bodies in prev_amag (0: none)
   double guard_theta = 1.5;         // options of the learned walk
   double band_override = -1.0;      // < 0: the model's band
+  gtc::u32 walk_budget = gtc::kLearnedWalkBudget;  // learned walk: nodes a thread tests before
+  gtc::u32 pair_budget = gtc::kLearnedPairBudget;  // a warp takes over, round 0 / later (0: all)
   gtc::DeviceBuffer diag;           // diagnostics partial sums
   double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes
 };

@@ -31,6 +31,10 @@ constexpr int kOffMean = kParams, kOffStd = kOffMean + kFeat, kOffYMean = kOffSt
               kOffYStd = kOffYMean + 1, kOffBand = kOffYStd + 1;
 constexpr int kModelFloats = kOffBand + 1;  // 4688
 constexpr float kPriorBase = 3.3773f;       // log2(2 * 3^1.5)
+// Node records one thread of the learned walk tests before the rest of its
+// walk goes to a warp: in round 0, and in later rounds (where each deferred
+// pair costs a few dependent loads more than a node).
+constexpr u32 kLearnedWalkBudget = 640, kLearnedPairBudget = 32;
 
 // Raw features of a (group, cell) pair, all from FP32 quantities so that
 // training and inference see the same numbers:
@@ -120,11 +124,12 @@ struct LearnedScratch {
   DeviceBuffer pend, pcount, roff;  // per (part, group): the pairs a round deferred, how many,
                                     // the first of their rows
   DeviceBuffer q[2], dec[2];        // deferred (group, node) rows and the network's decisions
+  DeviceBuffer cont;                // round-0 walks handed on to warps
   // per-group slots of the three parts of round 0 (0: not sized yet) and
   // of deferred pairs
   u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
   void release() {
-    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1]})
+    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1], &cont})
       b->release();
     for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
     slot_pend = 0;
@@ -142,6 +147,8 @@ struct LearnedWalk {
   float inv_theta_guard = 1.f / 1.5f;
   float band = 3.f;                 // log2 units; 0: prior only; huge: the MLP decides all
   float y_mean = 0.f;               // the model's mean correction (centres the prior)
+  u32 walk_budget = kLearnedWalkBudget;  // round 0: nodes a thread tests before a warp takes over
+  u32 pair_budget = kLearnedPairBudget;  // later rounds: the same
 };
 
 // Per-node features (after build_tree).

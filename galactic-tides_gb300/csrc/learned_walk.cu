@@ -256,7 +256,14 @@ constexpr int kMaxRounds = kMaxDepth + 4;
 // groups with the longest lists, at the centre where |a| is small, set the
 // round's time, and their walks spread over all the root's children. The
 // parts' lists follow each other in walk order, so a group's lists are its
-// parts' lists in turn; later rounds append to the last part's slot.
+// parts' lists in turn; later rounds append to each part's own slot.
+//
+// A round-0 walk stops after a budget of node records (kLearnedWalkBudget
+// by default). What is left of it
+// (the nodes from where it stopped to the end of its range) goes to a
+// continuation that a whole warp walks (k_lcont): the few longest walks,
+// thousands of dependent record loads each, would otherwise set the round's
+// time alone.
 constexpr int kParts = 3;
 
 struct GArgs {
@@ -277,48 +284,54 @@ struct GArgs {
   const uint2 *rows;        // later rounds: the last round's deferred (group, node) pairs,
   const u8 *dec;            // the network's decisions (1 accept)
   const u32 *roff;          // and each (part, group)'s first row (kParts ng + 1)
+  uint4 *cont;              // round-0 walks handed on: (part * ng + group, next node, end)
+  u32 budget;               // nodes a thread tests before handing on (this round)
   Scalars *sc;
 };
 
+// The walk's test of node record (ra, rb, rc) for one group: 0 open,
+// 1 accept, 2 defer to the network.
+__device__ __forceinline__ int lverdict(const float4 &ra, const float4 &rb, const float4 &rc,
+                                        const float *gf, const float *hf, float acc_d2,
+                                        float open_d2) {
+  // the reference's overlap test (group_lists.cpp:147), in FP32
+  const bool overlap = fabsf(ra.x - gf[0]) <= ra.w + hf[0] && fabsf(ra.y - gf[1]) <= ra.w + hf[1] &&
+                       fabsf(ra.z - gf[2]) <= ra.w + hf[2];
+  const float dx = fmaxf(fabsf(rb.x - gf[0]) - hf[0], 0.f),
+              dy = fmaxf(fabsf(rb.y - gf[1]) - hf[1], 0.f),
+              dz = fmaxf(fabsf(rb.z - gf[2]) - hf[2], 0.f);
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  if (overlap || !(d2 > rb.w)) return 0;
+  if ((__float_as_uint(rc.y) & 0x7fffffffu) <= kFewBodies) return 1;
+  return d2 > rc.w * acc_d2 ? 1 : d2 < rc.w * open_d2 ? 0 : 2;
+}
+
 // The walk of subtrees [i, end) for one group, the first node's verdict
 // given when pre >= 0; cells, bodies and deferred pairs to cl, bl, pl
-// (capacities capc, capb, capp; counting goes on past them).
+// (capacities capc, capb, capp; counting goes on past them). It stops
+// before the next node once it has tested `budget` nodes in all and
+// returns where it stopped (end when done).
 struct LWalkState {
   u64 nc, nb;
   u32 np, visits;
 };
 
-__device__ __forceinline__ void lwalk_range(const GArgs &a, const float *gf, const float *hf,
-                                            float acc_d2, float open_d2, u32 i, u32 end, int pre,
-                                            u32 *cl, u32 *bl, u32 *pl, u32 capc, u32 capb,
-                                            u32 capp, LWalkState &w) {
+__device__ __forceinline__ u32 lwalk_range(const GArgs &a, const float *gf, const float *hf,
+                                           float acc_d2, float open_d2, u32 i, u32 end, int pre,
+                                           u32 *cl, u32 *bl, u32 *pl, u32 capc, u32 capb,
+                                           u32 capp, u32 budget, LWalkState &w) {
   while (i < end) {
+    if (w.visits >= budget) return i;
     const float4 *rp = reinterpret_cast<const float4 *>(a.lrec + i);
     const float4 ra = __ldg(rp), rb = __ldg(rp + 1), rc = __ldg(rp + 2);
     ++w.visits;
     const u32 skip = __float_as_uint(rc.x), nbody_leaf = __float_as_uint(rc.y);
     const u32 nbody = nbody_leaf & 0x7fffffffu;
-    int verdict;  // 0 open, 1 accept, 2 defer
-    if (pre >= 0) {
-      verdict = pre;
+    int verdict = pre;
+    if (pre >= 0)
       pre = -1;
-    } else {
-      // the reference's overlap test (group_lists.cpp:147), in FP32
-      const bool overlap = fabsf(ra.x - gf[0]) <= ra.w + hf[0] &&
-                           fabsf(ra.y - gf[1]) <= ra.w + hf[1] &&
-                           fabsf(ra.z - gf[2]) <= ra.w + hf[2];
-      const float dx = fmaxf(fabsf(rb.x - gf[0]) - hf[0], 0.f),
-                  dy = fmaxf(fabsf(rb.y - gf[1]) - hf[1], 0.f),
-                  dz = fmaxf(fabsf(rb.z - gf[2]) - hf[2], 0.f);
-      const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      if (overlap || !(d2 > rb.w)) {
-        verdict = 0;
-      } else if (nbody <= kFewBodies) {
-        verdict = 1;
-      } else {
-        verdict = d2 > rc.w * acc_d2 ? 1 : d2 < rc.w * open_d2 ? 0 : 2;
-      }
-    }
+    else
+      verdict = lverdict(ra, rb, rc, gf, hf, acc_d2, open_d2);
     if (verdict == 2) {
       if (w.np < capp) pl[w.np] = i;
       ++w.np;
@@ -333,13 +346,14 @@ __device__ __forceinline__ void lwalk_range(const GArgs &a, const float *gf, con
     if (verdict != 0 || (nbody_leaf >> 31)) {
       if (skip <= i) {  // malformed tree: never loop
         atomicOr(&a.sc->error, 1u);
-        return;
+        return end;
       }
       i = skip;
     } else {
       ++i;
     }
   }
+  return end;
 }
 
 __device__ __forceinline__ u32 lskip(const LWalkRec *lrec, u32 i) {
@@ -406,12 +420,188 @@ __global__ void __launch_bounds__(kT) k_lround0(GArgs a) {
   u32 *bl = a.bodies + a.bodies_at[part] + static_cast<u64>(g) * capb;
   u32 *pl = a.pend + (static_cast<u64>(part) * a.ng + g) * a.slot_pend;
   LWalkState w{0, 0, 0, 0};
-  lwalk_range(a, gf, hf, acc_d2, open_d2, i, end, -1, cl, bl, pl, capc, capb, a.slot_pend, w);
+  const u32 stop = lwalk_range(a, gf, hf, acc_d2, open_d2, i, end, -1, cl, bl, pl, capc, capb,
+                               a.slot_pend, a.budget, w);
+  if (stop < end) {  // at most one per (part, group): the array holds kParts ng
+    const u32 c = atomicAdd(&a.sc->lcont, 1u);
+    a.cont[c] = make_uint4(static_cast<u32>(tid), stop, end, 0u);
+  }
   a.ncells[static_cast<u64>(part) * a.ng + g] = w.nc;
   a.nbodies[static_cast<u64>(part) * a.ng + g] = w.nb;
   a.pcount[static_cast<u64>(part) * a.ng + g] = w.np;
   if (w.nc > capc || w.nb > capb || w.np > a.slot_pend) atomicOr(&a.sc->list_overflow, 1u);
   lround_stats(a.sc, part, w.nc, w.nb, w.np, w.visits);
+}
+
+// The rest of the walks that ran out of budget, one warp each. The warp
+// keeps the walk's remaining nodes as a stack of index ranges, each a run of
+// whole subtrees whose parents the walk opened. Each step the lanes take the
+// 32 ranges on top, test each range's first node and push back its children
+// (when opened) and the rest of its range, so the lanes test exactly the
+// nodes the thread would have, 32 at a time. In later rounds the thread's
+// remaining deferred pairs go on the stack too, as a node with the network's
+// decision in place of the range's end (kPairOpen, kPairAccept), 64 at a
+// time whenever fewer than 32 ranges are left. Entries are appended to the
+// part's slots in step order, lane order within a step: a fixed order for
+// given inputs.
+constexpr int kContWarps = 4;
+constexpr int kContStack = 1024;  // ranges per warp
+constexpr u32 kPairOpen = 0xfffffffeu, kPairAccept = 0xffffffffu;  // node counts stay below
+
+__global__ void __launch_bounds__(kContWarps * 32) k_lcont(GArgs a, bool later) {
+  __shared__ uint2 stack_all[kContWarps][kContStack];
+  const int lane = threadIdx.x & 31;
+  uint2 *stk = stack_all[threadIdx.x >> 5];
+  const unsigned below = (1u << lane) - 1u;
+  const u32 ncont = a.sc->lcont;
+  for (;;) {
+    u32 c = 0;
+    if (lane == 0) c = atomicAdd(&a.sc->lcont_taken, 1u);
+    c = __shfl_sync(kFullMask, c, 0);
+    if (c >= ncont) return;
+    const uint4 ct = a.cont[c];
+    const u32 pg = ct.x;
+    const int part = static_cast<int>(pg / a.ng);
+    const u32 g = pg % a.ng;
+    float gf[3], hf[3], acc_d2, open_d2;
+    group_scales(a, g, gf, hf, acc_d2, open_d2);
+    const u32 capc = a.slot_cells[part], capb = a.slot_bodies[part], capp = a.slot_pend;
+    u32 *cl = a.cells + a.cells_at[part] + static_cast<u64>(g) * capc;
+    u32 *bl = a.bodies + a.bodies_at[part] + static_cast<u64>(g) * capb;
+    u32 *pl = a.pend + static_cast<u64>(pg) * capp;
+    u64 nc = a.ncells[pg], nb = a.nbodies[pg];
+    u32 np = a.pcount[pg], visits = 0;
+    u32 kp = later ? ct.w : 0u;  // the next deferred pair, up to k1
+    const u32 k1 = later ? a.roff[pg + 1] : 0u;
+    int size = 0;
+    if (ct.y < ct.z) {
+      if (lane == 0) stk[0] = make_uint2(ct.y, ct.z);
+      size = 1;
+    }
+    bool bad = false;
+    __syncwarp();
+    while ((size > 0 || kp < k1) && !bad) {
+      if (size < 32 && kp < k1) {  // room: 32 + 64 ranges stay below kContStack - 32
+        const u32 cnt = k1 - kp < 64u ? k1 - kp : 64u;
+        for (u32 j = lane; j < cnt; j += 32)
+          stk[size + cnt - 1 - j] = make_uint2(a.rows[kp + j].y, a.dec[kp + j] ? kPairAccept : kPairOpen);
+        kp += cnt;
+        size += static_cast<int>(cnt);
+        __syncwarp();
+      }
+      if (size > kContStack - 32) {
+        // nearly full (a step adds at most one range per lane): lane 0
+        // walks the range on top alone
+        if (lane == 0) {
+          const uint2 r = stk[size - 1];
+          const bool pair = r.y >= kPairOpen;
+          LWalkState w{nc, nb, np, 0};
+          lwalk_range(a, gf, hf, acc_d2, open_d2, r.x, pair ? lskip(a.lrec, r.x) : r.y,
+                      pair ? static_cast<int>(r.y - kPairOpen) : -1, cl, bl, pl, capc, capb, capp,
+                      ~0u, w);
+          nc = w.nc;
+          nb = w.nb;
+          np = w.np;
+          visits += w.visits;
+        }
+        nc = __shfl_sync(kFullMask, nc, 0);
+        nb = __shfl_sync(kFullMask, nb, 0);
+        np = __shfl_sync(kFullMask, np, 0);
+        --size;
+        __syncwarp();
+        continue;
+      }
+      const int k = size < 32 ? size : 32;
+      const bool act = lane < k;
+      uint2 r = make_uint2(0u, 0u);
+      if (act) r = stk[size - 1 - lane];
+      __syncwarp();
+      size -= k;
+      int verdict = 0;
+      u32 skip = 0, nbody_leaf = 0, first = 0, rend = r.y;
+      if (act) {
+        const float4 *rp = reinterpret_cast<const float4 *>(a.lrec + r.x);
+        const float4 ra = __ldg(rp), rb = __ldg(rp + 1), rc = __ldg(rp + 2);
+        ++visits;
+        skip = __float_as_uint(rc.x);
+        nbody_leaf = __float_as_uint(rc.y);
+        first = __float_as_uint(rc.z);
+        if (r.y >= kPairOpen) {  // a deferred pair: the network's decision, its subtree
+          verdict = static_cast<int>(r.y - kPairOpen);
+          rend = skip;
+        } else {
+          verdict = lverdict(ra, rb, rc, gf, hf, acc_d2, open_d2);
+        }
+      }
+      const u32 nbody = nbody_leaf & 0x7fffffffu;
+      const bool leaf = (nbody_leaf >> 31) != 0;
+      const bool is_cell = act && verdict == 1 && nbody > kFewBodies;
+      const bool is_pend = act && verdict == 2;
+      const u32 nbo = act && ((verdict == 1 && nbody <= kFewBodies) || (verdict == 0 && leaf))
+                          ? nbody : 0u;
+      const unsigned bc = __ballot_sync(kFullMask, is_cell), bp = __ballot_sync(kFullMask, is_pend);
+      if (is_cell) {
+        const u64 at = nc + __popc(bc & below);
+        if (at < capc) cl[at] = r.x;
+      }
+      if (is_pend) {
+        const u64 at = np + __popc(bp & below);
+        if (at < capp) pl[at] = r.x;
+      }
+      u32 incl = nbo;  // bodies: inclusive scan over the lanes
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += t;
+      }
+      for (u32 j = 0; j < nbo; ++j) {
+        const u64 at = nb + (incl - nbo) + j;
+        if (at < capb) bl[at] = first + j;
+      }
+      nc += __popc(bc);
+      np += __popc(bp);
+      nb += __shfl_sync(kFullMask, incl, 31);
+      // the next ranges: the opened node's children [r.x + 1, skip) above
+      // the rest of its range [skip, r.y)
+      bool has_rest = false, has_kids = false;
+      const u32 kids_end = skip < rend ? skip : rend;
+      if (act) {
+        if (skip <= r.x) {  // malformed tree: never loop
+          bad = true;
+        } else {
+          has_rest = skip < rend;
+          has_kids = verdict == 0 && !leaf && r.x + 1 < kids_end;
+        }
+      }
+      const u32 npush = (has_rest ? 1u : 0u) + (has_kids ? 1u : 0u);
+      u32 from = npush;  // pushes of this lane and the lanes above it
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 t = __shfl_down_sync(kFullMask, from, o);
+        if (lane + o < 32) from += t;
+      }
+      const u32 base = static_cast<u32>(size) + from - npush;
+      if (has_rest) stk[base] = make_uint2(skip, rend);
+      if (has_kids) stk[base + (has_rest ? 1u : 0u)] = make_uint2(r.x + 1, kids_end);
+      size += static_cast<int>(__shfl_sync(kFullMask, from, 0));
+      bad = __any_sync(kFullMask, bad);
+      __syncwarp();
+    }
+    const u32 sv = __reduce_add_sync(kFullMask, visits);
+    if (lane == 0) {
+      if (bad) atomicOr(&a.sc->error, 1u);
+      a.ncells[pg] = nc;
+      a.nbodies[pg] = nb;
+      a.pcount[pg] = np;
+      if (nc > capc || nb > capb || np > capp) atomicOr(&a.sc->list_overflow, 1u);
+      auto clamp = [](u64 v) { return static_cast<u32>(v < 0xffffffffull ? v : 0xffffffffull); };
+      atomicMax(&a.sc->lmax_cells[part], clamp(nc));
+      atomicMax(&a.sc->lmax_bodies[part], clamp(nb));
+      atomicMax(&a.sc->max_pend, np);
+      atomicAdd(&a.sc->walk_nodes, static_cast<unsigned long long>(sv));
+    }
+    __syncwarp();
+  }
 }
 
 // A later round, kParts threads per group: thread (part, group) takes the
@@ -437,9 +627,19 @@ __global__ void __launch_bounds__(kT) k_lround(GArgs a) {
   u32 *pl = a.pend + pg * a.slot_pend;
   LWalkState w{a.ncells[pg], a.nbodies[pg], 0, 0};
   for (u32 k = k0; k < k1; ++k) {
-    const u32 i = a.rows[k].y;
-    lwalk_range(a, gf, hf, acc_d2, open_d2, i, lskip(a.lrec, i), a.dec[k], cl, bl, pl, capc, capb,
-                a.slot_pend, w);
+    if (w.visits >= a.budget) {  // the pairs from k on go to a warp
+      const u32 c = atomicAdd(&a.sc->lcont, 1u);
+      a.cont[c] = make_uint4(static_cast<u32>(pg), 0u, 0u, k);
+      break;
+    }
+    const u32 i = a.rows[k].y, end = lskip(a.lrec, i);
+    const u32 stop = lwalk_range(a, gf, hf, acc_d2, open_d2, i, end, a.dec[k], cl, bl, pl, capc,
+                                 capb, a.slot_pend, a.budget, w);
+    if (stop < end) {  // the rest of this pair's subtree and the later pairs
+      const u32 c = atomicAdd(&a.sc->lcont, 1u);
+      a.cont[c] = make_uint4(static_cast<u32>(pg), stop, end, k + 1);
+      break;
+    }
   }
   a.ncells[pg] = w.nc;
   a.nbodies[pg] = w.nb;
@@ -599,6 +799,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
                          cudaStream_t s) {
   static_assert(kParts == kListSegments, "one list segment per part");
   if (ng == 0) return;
+  if (ws.n_nodes >= kPairOpen)
+    throw RuntimeError("learned walk: too many tree nodes for 32 bit node ranges");
   Scalars *sc = ws.scalars.as<Scalars>();
   LearnedScratch &ls = *lw.scratch;
   if (ls.slot_cells[0] == 0) {  // the first learned walk: the theta walk's slots to start with
@@ -627,8 +829,15 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   a.kids = ws.kids.as<uint4>();
   a.nchild = ws.nchild.as<u8>();
   a.roff = ls.roff.as<u32>();
+  ls.cont.ensure(nparts * sizeof(uint4));
+  a.cont = ls.cont.as<uint4>();
   a.sc = sc;
   const u32 gb = ceil_div(ng, kT), pb = static_cast<u32>(ceil_div(nparts, kT));
+  int dev = 0, sms = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // warps that take the handed-on walks in turn: a few per SM
+  const u32 cont_blocks = static_cast<u32>(std::max(1, sms) * 4);
   u64 rows = 0, batches = 0;
   u32 rounds = 0;
   for (int attempt = 0;; ++attempt) {
@@ -661,6 +870,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     for (rounds = 0;; ++rounds) {
       if (rounds >= static_cast<u32>(kMaxRounds))
         throw RuntimeError("learned walk: more rounds than the tree has levels");
+      GTC_CUDA(cudaMemsetAsync(&sc->lcont, 0, 2 * sizeof(u32), s));
+      a.budget = rounds == 0 ? lw.walk_budget : lw.pair_budget;
       if (rounds == 0) {
         k_lround0<<<pb, kT, 0, s>>>(a);
       } else {
@@ -668,6 +879,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
         a.dec = ls.dec[qsel].as<u8>();
         k_lround<<<pb, kT, 0, s>>>(a);
       }
+      GTC_LAUNCH_CHECK();
+      k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, rounds > 0);
       GTC_LAUNCH_CHECK();
       u32 *roff = ls.roff.as<u32>();
       exclusive_scan_u32(a.pcount, roff, nparts, roff + nparts, ws.scan_tmp, s);

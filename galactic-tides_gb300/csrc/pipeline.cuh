@@ -108,7 +108,7 @@ struct Scalars {
   unsigned long long fp64_tests;  // opening tests the FP32 bounds left undecided
   unsigned long long mlp_rows;    // learned walk: rows the MLP decided
   unsigned long long mlp_batches; // learned walk: warp inferences
-  unsigned long long walk_items; // learned walk: next item to take
+  u32 lcont, lcont_taken; // learned walk: walks handed on to warps, and taken so far
   u32 list_overflow;      // learned walk: a lane's region overflowed
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)

@@ -224,6 +224,55 @@ def test_fallback_then_learned_lists_are_valid(gtc):
         assert c.stats()["criterion_used"] == gtc.CRITERION_THETA
 
 
+def _sorted_per_group(values, starts, ends):
+    """Each group's entries sorted, groups in turn."""
+    counts = (ends - starts).astype(np.int64)
+    gid = np.repeat(np.arange(len(counts)), counts)
+    take = np.concatenate([np.arange(s, e) for s, e in zip(starts, ends)]) if len(counts) else []
+    v = values[np.asarray(take, np.int64)]
+    return v[np.lexsort((v, gid))]
+
+
+@gpu
+def test_walk_budget_only_reorders_the_lists(gtc):
+    """Walks handed on to warps (budget 3 in round 0 and 1 in later rounds:
+    nearly every walk; 64 and 8: the long ones) give each group the same
+    cells, bodies and network rows as threads that walk to the end, so
+    forces differ by summation order only."""
+    pos, _, mass, _ = gtc.make_galaxy(60_000, seed=4)
+    kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
+    runs = {}
+    for budget in (0, 3, 64):
+        with _learned_ctx(gtc) as c:
+            c.set_option("learned_walk_budget", budget)
+            c.set_option("learned_pair_budget", (budget + 7) // 8)
+            c.group_force(pos, mass, **kw)
+            acc, _ = c.group_force(pos, mass, **kw)
+            runs[budget] = (acc, c.stats(), c.export())
+            assert runs[budget][1]["criterion_used"] == gtc.CRITERION_LEARNED
+    acc0, st0, dev0 = runs[0]
+    g0 = dev0["groups"].astype(np.int64)
+    want_c = _sorted_per_group(dev0["cell_list"], g0[:, 2], g0[:, 3])
+    want_b = _sorted_per_group(dev0["body_list"], g0[:, 4], g0[:, 5])
+    for budget in (3, 64):
+        acc, st, dev = runs[budget]
+        for key in ("cell_interactions", "body_interactions", "mlp_rows", "walk_nodes"):
+            assert st[key] == st0[key], (budget, key)
+        g = dev["groups"].astype(np.int64)
+        assert np.array_equal(g[:, :2], g0[:, :2])
+        assert np.array_equal(_sorted_per_group(dev["cell_list"], g[:, 2], g[:, 3]), want_c)
+        assert np.array_equal(_sorted_per_group(dev["body_list"], g[:, 4], g[:, 5]), want_b)
+        _check_list_invariants(dev, len(mass))
+        err = rel_errors(acc, acc0)
+        assert np.median(err) < 1e-6 and np.max(err) < 1e-4, budget
+    with _learned_ctx(gtc) as c:  # the same budget twice: bitwise the same forces
+        c.set_option("learned_walk_budget", 3)
+        c.set_option("learned_pair_budget", 1)
+        c.group_force(pos, mass, **kw)
+        again, _ = c.group_force(pos, mass, **kw)
+    assert np.array_equal(again, runs[3][0])
+
+
 @gpu
 def test_band_only_skips_the_network_where_it_cannot_change_the_decision(gtc):
     """The training band (the 0.99 quantile of the network's correction)
@@ -319,3 +368,9 @@ def test_invalid_learned_arguments(ctx, gtc):
         ctx.set_option("learned_band_size", 1)
     with pytest.raises(gtc.GtcInvalidArgument):
         ctx.set_option("graph_headroom", 5)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_walk_budget", 2.5)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_walk_budget", -1)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_pair_budget", 0.5)
