@@ -72,14 +72,14 @@ void exclusive_scan_u64(const u64 *in, u64 *out, u64 n, u64 *total_dev, DeviceBu
 void reserve_scans(DeviceBuffer &tmp, u64 n);
 
 // ---------------------------------------------------------- radix sort
-// Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the
-// key. The sorted pairs end up back in keys/vals; alt_* are scratch of n
-// elements each.
+// Stable LSD radix sort of (key, value) pairs on `bits` bits of the key from
+// bit `low_bit` up, 8 bits a pass. The sorted pairs end up back in
+// keys/vals; alt_* are scratch of n elements each.
 struct RadixScratch {
   DeviceBuffer counts, scan_tmp;
 };
 void radix_sort_pairs(u64 *keys, u32 *vals, u64 *alt_keys, u32 *alt_vals, u32 n, int bits,
-                      RadixScratch &scratch, cudaStream_t s);
+                      RadixScratch &scratch, cudaStream_t s, int low_bit = 0);
 
 // ------------------------------------------------------- warp helpers
 constexpr unsigned kFullMask = 0xffffffffu;

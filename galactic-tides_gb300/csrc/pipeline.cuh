@@ -80,6 +80,7 @@ struct Workspace {
   // host-side view of the last build
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
+  int sort_levels = 0;        // key levels the next eager build sorts first (0: all 21)
   u32 *host_words = nullptr;  // pinned, for small read-backs
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
   // One-pass walk: group g's lists start at g * slot_cells and g *
@@ -109,14 +110,13 @@ struct Scalars {
   unsigned long long mlp_rows;    // learned walk: rows the MLP decided
   unsigned long long mlp_batches; // learned walk: warp inferences
   u32 lcont, lcont_taken; // learned walk: walks handed on to warps, and taken so far
-  u32 list_overflow;      // learned walk: a lane's region overflowed
+  u32 list_overflow;      // learned walk: a list slot overflowed
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)
   u32 max_cells, max_bodies;  // longest cell and body list of a group (one-pass walk: its rest)
   u32 max_near_cells, max_near_bodies;  // one-pass walk: longest lists of a near-field walk
-  // learned walk: longest lists of each part of round 0 (cells, then
-  // bodies; the last part also holds the later rounds), most pairs a group
-  // deferred in a round
+  // learned walk: longest lists of each part (cells, then bodies; all
+  // rounds), most pairs a part deferred in a round
   u32 lmax_cells[3], lmax_bodies[3], max_pend;
   unsigned long long spill_used[2];  // one-pass walk: overflow pool entries taken (cells, bodies)
   u32 spilled;            // one-pass walk: groups that outgrew their slots

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kThreads)
 }  // namespace
 
 void radix_sort_pairs(u64 *keys, u32 *vals, u64 *alt_keys, u32 *alt_vals, u32 n, int bits,
-                      RadixScratch &scratch, cudaStream_t s) {
+                      RadixScratch &scratch, cudaStream_t s, int low_bit) {
   if (n <= 1 || bits <= 0) return;
   const u32 ntiles = ceil_div(n, kTile);
   const u64 ncounts = static_cast<u64>(kBins) * ntiles;
@@ -139,7 +139,7 @@ void radix_sort_pairs(u64 *keys, u32 *vals, u64 *alt_keys, u32 *alt_vals, u32 n,
   u64 *src_k = keys, *dst_k = alt_keys;
   u32 *src_v = vals, *dst_v = alt_vals;
   for (int p = 0; p < passes; ++p) {
-    const int shift = 8 * p;
+    const int shift = low_bit + 8 * p;
     k_histogram<<<ntiles, kThreads, 0, s>>>(src_k, n, shift, ntiles, counts);
     GTC_LAUNCH_CHECK();
     exclusive_scan_u32(counts, offsets, ncounts, nullptr, scratch.scan_tmp, s);

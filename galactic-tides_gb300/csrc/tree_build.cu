@@ -759,10 +759,11 @@ __global__ void __launch_bounds__(32)
   }
 }
 
-// A graph replay's checks after the node count: deeper keys needed (bit 1)
-// or more nodes than the node arrays hold (bit 2).
-__global__ void k_check_tree_graph(Scalars *sc, u32 cap) {
-  if (sc->deep > 0) sc->abort |= 1u;
+// A graph replay's checks after the node count: deeper keys needed, or a
+// leaf below the sorted levels (bit 1), or more nodes than the node arrays
+// hold (bit 2).
+__global__ void k_check_tree_graph(Scalars *sc, u32 cap, int sorted_levels) {
+  if (sc->deep > 0 || static_cast<int>(sc->depth) > sorted_levels) sc->abort |= 1u;
   if (sc->n_nodes > cap) sc->abort |= 2u;
 }
 
@@ -869,6 +870,21 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
 }
 
+namespace {
+// Sorts the (key, body) pairs on the first `levels` levels of the first key
+// word, rounded up to whole 8-bit passes (21 or more: the whole word), and
+// returns the levels the order is exact for. Bodies that share those levels
+// keep their input order, which is all the tree needs while no leaf lies
+// deeper.
+int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s) {
+  const int passes = levels >= kLevelsPerWord ? 8 : (3 * std::max(levels, 1) + 7) / 8;
+  const int low = std::max(0, 3 * kLevelsPerWord - 8 * passes);
+  radix_sort_pairs(ws.key0.as<u64>(), ws.idx.as<u32>(), ws.key0_alt.as<u64>(),
+                   ws.idx_alt.as<u32>(), n, 3 * kLevelsPerWord - low, ws.radix, s, low);
+  return low == 0 ? kLevelsPerWord : (3 * kLevelsPerWord - low) / 3;
+}
+}  // namespace
+
 void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                 const SolverParams &sp, cudaStream_t s, Scalars *host) {
   ws.n = n;
@@ -907,7 +923,9 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_LAUNCH_CHECK();
   k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
-  radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
+  // the levels the last tree needed first; all of them when a leaf lies
+  // deeper (sorting the partly sorted pairs again gives the full order)
+  const int sorted = sort_top_levels(ws, n32, ws.sort_levels > 0 ? ws.sort_levels : kLevelsPerWord, s);
 
   KeyView kv{key0, nullptr, nullptr, 1};
   signed char *lcp_next = ws.lcp.as<signed char>();
@@ -916,6 +934,14 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_LAUNCH_CHECK();
   read_scalars(ws, host, s);
   if (host->error & 4u) throw InvalidArgument("cuda: positions must be finite");
+  if (sorted < kLevelsPerWord && static_cast<int>(host->depth) > sorted) {
+    sort_top_levels(ws, n32, kLevelsPerWord, s);
+    GTC_CUDA(cudaMemsetAsync(&sc->deep, 0, sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->depth, 0, sizeof(u32), s));
+    k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
+    GTC_LAUNCH_CHECK();
+    read_scalars(ws, host, s);
+  }
 
   // Deeper key words for bodies whose leaves lie below the words so far.
   while (host->deep > 0 && kv.words < 3) {
@@ -974,6 +1000,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   }
   if (host->deep > 0) throw RuntimeError("octree deeper than the depth cap");
   ws.key_words = kv.words;
+  ws.sort_levels = kv.words == 1 ? static_cast<int>(host->depth) + 1 : 0;
 
   // Node numbering: count the nodes ending at each sorted position.
   u32 *count = ws.count.as<u32>(), *cscan = ws.count_scan.as<u32>();
@@ -1088,7 +1115,8 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
   k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
   GTC_LAUNCH_CHECK();
-  radix_sort_pairs(key0, idx, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n32, 63, ws.radix, s);
+  // the levels the captured depth allows: a deeper tree aborts the replay
+  const int sorted = sort_top_levels(ws, n32, caps.depth + 1, s);
   const KeyView kv{key0, nullptr, nullptr, 1};
   signed char *lcp_next = ws.lcp.as<signed char>();
   u8 *leafdepth = ws.leafdepth.as<u8>();
@@ -1098,7 +1126,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   k_node_count<<<nb, kT, 0, s>>>(lcp_next, leafdepth, n32, count);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(count, cscan, n, &sc->n_nodes, ws.scan_tmp, s);
-  k_check_tree_graph<<<1, 1, 0, s>>>(sc, mcap);
+  k_check_tree_graph<<<1, 1, 0, s>>>(sc, mcap, sorted);
   GTC_LAUNCH_CHECK();
   const u32 *m_dev = &sc->n_nodes;
   k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
