@@ -454,21 +454,39 @@ __global__ void __launch_bounds__(kT)
       cz = __ldg(tz + iz);
     }
     const u32 p = first + static_cast<u32>(d - d0);
-    // first body of the node: smallest b0 sharing d levels with b
-    u32 lo = 0, hi = b;
-    if (d > 0)
-      while (lo < hi) {
+    geom[2 * p] = make_double2(cx, cy);
+    geom[2 * p + 1] = make_double2(cz, root->half_at[d]);
+    nend[p] = b + 1;
+    depth[p] = static_cast<u8>(d);
+    isleaf[p] = d == ld ? 1 : 0;
+  }
+  // First body of each node: the smallest position sharing d levels with b.
+  // Deepest node first; each shallower node starts at or before the deeper
+  // one, so the search gallops back from there (a few probes for the small
+  // nodes that most are) and then halves the last interval.
+  u32 start = b;  // shares at least d levels with b for every d here
+  for (int d = ld; d >= d0; --d) {
+    u32 lo = 0, hi = start;
+    if (d > 0) {
+      for (u64 step = 1;; step *= 2) {  // 64-bit: never wraps to 0
+        if (step > hi) break;  // lo stays 0
+        const u32 cand = hi - static_cast<u32>(step);
+        if (lcp(kv, cand, b) < d) {
+          lo = cand + 1;
+          break;
+        }
+        hi = cand;
+      }
+      while (lo < hi) {  // lcp(lo - 1, b) < d (or lo = 0), lcp(hi, b) >= d
         const u32 mid = lo + (hi - lo) / 2;
         if (lcp(kv, mid, b) >= d) hi = mid;
         else lo = mid + 1;
       }
-    geom[2 * p] = make_double2(cx, cy);
-    geom[2 * p + 1] = make_double2(cz, root->half_at[d]);
+    }
+    const u32 p = first + static_cast<u32>(d - d0);
     nbegin[p] = lo;
-    nend[p] = b + 1;
     skip[p] = total - count_scan[lo];
-    depth[p] = static_cast<u8>(d);
-    isleaf[p] = d == ld ? 1 : 0;
+    start = lo;
   }
 }
 
