@@ -367,12 +367,16 @@ __device__ __forceinline__ u32 near_child(u32 b0, u32 b1, const uint4 *kids, con
   return kNone;
 }
 
-__global__ void __launch_bounds__(kT)
+// Small blocks for the one-pass walk: its blocks run for very different
+// times (the central groups walk longest), and small ones even out the SMs.
+constexpr u32 kWalkThreads = 128;
+
+__global__ void __launch_bounds__(kWalkThreads)
     k_walk_split(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
                  const float *gboxf, const u32 *gbegin, const u32 *gend, const uint4 *kids,
                  const u8 *nchild, const u32 *nbegin, const u32 *nend, u32 ng_cap, SplitOut out,
                  Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
-  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  const u64 tid = static_cast<u64>(blockIdx.x) * kWalkThreads + threadIdx.x;
   if (aborted(abort)) return;
   const u32 ng = bounded(ng_cap, ng_dev);
   if (tid >= 2ull * ng) return;
@@ -702,7 +706,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
                       ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
                       sl_c, sl_b, sn_c, sn_b, ng};
-    k_walk_split<<<ceil_div(2ull * ng, kT), kT, 0, s>>>(
+    k_walk_split<<<ceil_div(2ull * ng, kWalkThreads), kWalkThreads, 0, s>>>(
         w32, w64, gbox, gboxf, gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
         ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc);
     GTC_LAUNCH_CHECK();
@@ -808,7 +812,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
                     ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
                     caps.slot_cells, caps.slot_bodies, caps.slot_near_cells,
                     caps.slot_near_bodies, n32};
-  k_walk_split<<<ceil_div(2ull * n, kT), kT, 0, s>>>(
+  k_walk_split<<<ceil_div(2ull * n, kWalkThreads), kWalkThreads, 0, s>>>(
       ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
       ws.gboxf.as<float>(), gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
       ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort);

@@ -265,6 +265,9 @@ constexpr int kMaxRounds = kMaxDepth + 4;
 // thousands of dependent record loads each, would otherwise set the round's
 // time alone.
 constexpr int kParts = 3;
+// Small blocks for the walk rounds: their threads run for very different
+// times, and small blocks even out the SMs.
+constexpr u32 kRoundThreads = 128;
 
 struct GArgs {
   const LWalkRec *lrec;
@@ -395,8 +398,8 @@ __device__ __forceinline__ void lround_stats(Scalars *sc, int part, u64 nc, u64 
 
 // Round 0: thread (part, group) walks the part's range of the root's
 // children (the root itself, when it is a leaf, in part 0).
-__global__ void __launch_bounds__(kT) k_lround0(GArgs a) {
-  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+__global__ void __launch_bounds__(kRoundThreads) k_lround0(GArgs a) {
+  const u64 tid = static_cast<u64>(blockIdx.x) * kRoundThreads + threadIdx.x;
   if (tid >= static_cast<u64>(kParts) * a.ng) return;
   const int part = static_cast<int>(tid / a.ng);
   const u32 g = static_cast<u32>(tid % a.ng);
@@ -609,8 +612,8 @@ __global__ void __launch_bounds__(kContWarps * 32) k_lcont(GArgs a, bool later) 
 // decisions, appends to the part's slot and defers into the part's pend
 // slot, so a part's lists are its round-0 walk followed by each later
 // round's.
-__global__ void __launch_bounds__(kT) k_lround(GArgs a) {
-  const u64 pg = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+__global__ void __launch_bounds__(kRoundThreads) k_lround(GArgs a) {
+  const u64 pg = static_cast<u64>(blockIdx.x) * kRoundThreads + threadIdx.x;
   if (pg >= static_cast<u64>(kParts) * a.ng) return;
   const int part = static_cast<int>(pg / a.ng);
   const u32 g = static_cast<u32>(pg % a.ng);
@@ -833,6 +836,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   a.cont = ls.cont.as<uint4>();
   a.sc = sc;
   const u32 gb = ceil_div(ng, kT), pb = static_cast<u32>(ceil_div(nparts, kT));
+  const u32 rb = static_cast<u32>(ceil_div(nparts, kRoundThreads));
   int dev = 0, sms = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -873,11 +877,11 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       GTC_CUDA(cudaMemsetAsync(&sc->lcont, 0, 2 * sizeof(u32), s));
       a.budget = rounds == 0 ? lw.walk_budget : lw.pair_budget;
       if (rounds == 0) {
-        k_lround0<<<pb, kT, 0, s>>>(a);
+        k_lround0<<<rb, kRoundThreads, 0, s>>>(a);
       } else {
         a.rows = ls.q[qsel].as<uint2>();
         a.dec = ls.dec[qsel].as<u8>();
-        k_lround<<<pb, kT, 0, s>>>(a);
+        k_lround<<<rb, kRoundThreads, 0, s>>>(a);
       }
       GTC_LAUNCH_CHECK();
       k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, rounds > 0);
