@@ -96,24 +96,55 @@ __device__ __forceinline__ void step_centre(double &cx, double &cy, double &cz, 
 
 // ------------------------------------------------------------ bounding box
 
+// Order-preserving image of a double for integer comparison: a >= b exactly
+// when key(a) >= key(b), for finite a, b (-0.0 is taken as +0.0).
+__device__ __forceinline__ u64 order_key(double v) {
+  u64 b = static_cast<u64>(__double_as_longlong(v));
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_order_key(u64 k) {
+  return __longlong_as_double(static_cast<long long>((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// Per-block boxes. Min and max are taken on the order-preserving integer
+// images (exact, and off the FP64 pipe); with 16-byte aligned positions a
+// thread loads two bodies as three 16-byte words.
 __global__ void __launch_bounds__(kT) k_bbox_partial(const double *pos, u64 n, double *part) {
-  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (u64 i = blockIdx.x * static_cast<u64>(kT) + threadIdx.x; i < n;
-       i += static_cast<u64>(gridDim.x) * kT) {
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const double v = pos[3 * i + a];
-      lo[a] = fmin(lo[a], v);
-      hi[a] = fmax(hi[a], v);
+  const u64 inf_lo = order_key(INFINITY), inf_hi = order_key(-INFINITY);
+  u64 lo[3] = {inf_lo, inf_lo, inf_lo}, hi[3] = {inf_hi, inf_hi, inf_hi};
+  auto take = [&](int a, double v) {
+    const u64 k = order_key(v);
+    lo[a] = k < lo[a] ? k : lo[a];
+    hi[a] = k > hi[a] ? k : hi[a];
+  };
+  const u64 first = blockIdx.x * static_cast<u64>(kT) + threadIdx.x,
+            stride = static_cast<u64>(gridDim.x) * kT;
+  if ((reinterpret_cast<uintptr_t>(pos) & 15) == 0) {
+    const double2 *p2 = reinterpret_cast<const double2 *>(pos);
+    for (u64 q = first; q < n / 2; q += stride) {
+      const double2 u = __ldg(p2 + 3 * q), v = __ldg(p2 + 3 * q + 1), w = __ldg(p2 + 3 * q + 2);
+      take(0, u.x);
+      take(1, u.y);
+      take(2, v.x);
+      take(0, v.y);
+      take(1, w.x);
+      take(2, w.y);
     }
+    if ((n & 1) && first == 0)
+      for (int a = 0; a < 3; ++a) take(a, pos[3 * (n - 1) + a]);
+  } else {
+    for (u64 i = first; i < n; i += stride)
+      for (int a = 0; a < 3; ++a) take(a, pos[3 * i + a]);
   }
 #pragma unroll
   for (int a = 0; a < 3; ++a)
     for (int o = 16; o > 0; o >>= 1) {
-      lo[a] = fmin(lo[a], __shfl_xor_sync(kFullMask, lo[a], o));
-      hi[a] = fmax(hi[a], __shfl_xor_sync(kFullMask, hi[a], o));
+      const u64 l = __shfl_xor_sync(kFullMask, lo[a], o), h = __shfl_xor_sync(kFullMask, hi[a], o);
+      lo[a] = l < lo[a] ? l : lo[a];
+      hi[a] = h > hi[a] ? h : hi[a];
     }
-  __shared__ double s[kT / 32][6];
+  __shared__ u64 s[kT / 32][6];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
     for (int a = 0; a < 3; ++a) {
@@ -122,10 +153,12 @@ __global__ void __launch_bounds__(kT) k_bbox_partial(const double *pos, u64 n, d
     }
   __syncthreads();
   if (threadIdx.x < 6) {
-    double v = s[0][threadIdx.x];
-    for (int w = 1; w < kT / 32; ++w)
-      v = threadIdx.x < 3 ? fmin(v, s[w][threadIdx.x]) : fmax(v, s[w][threadIdx.x]);
-    part[6 * blockIdx.x + threadIdx.x] = v;
+    u64 v = s[0][threadIdx.x];
+    for (int w = 1; w < kT / 32; ++w) {
+      const u64 x = s[w][threadIdx.x];
+      v = threadIdx.x < 3 ? (x < v ? x : v) : (x > v ? x : v);
+    }
+    part[6 * blockIdx.x + threadIdx.x] = from_order_key(v);
   }
 }
 
@@ -177,13 +210,6 @@ __global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, Tre
 
 // ------------------------------------------------------------------- keys
 
-// Order-preserving image of a double for integer comparison: a >= b exactly
-// when key(a) >= key(b), for finite a, b (-0.0 is taken as +0.0).
-__device__ __forceinline__ u64 order_key(double v) {
-  u64 b = static_cast<u64>(__double_as_longlong(v));
-  if (b == 0x8000000000000000ull) b = 0;
-  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
 
 // Split values. Along one axis the centre a body's walk compares against at
 // level d depends only on the body's first d bits on that axis: the centres
@@ -301,7 +327,20 @@ __global__ void __launch_bounds__(kT)
 __global__ void __launch_bounds__(kT)
     k_levels(KeyView kv, const u32 *idx, const u8 *tiny, u32 n, int L, signed char *lcp_next,
              u8 *leafdepth, Scalars *sc) {
-  const u32 b = blockIdx.x * kT + threadIdx.x;
+  // win[i] = lcp(i, i + L) for the block's positions and the L before them,
+  // each computed once; a body's w is the largest over its windows
+  constexpr int kMaxWin = 64;
+  __shared__ signed char win[kT + kMaxWin];
+  const u32 base = blockIdx.x * kT, b = base + threadIdx.x;
+  const bool shared_win = L <= kMaxWin;
+  if (shared_win) {
+    for (int k = threadIdx.x; k < kT + L; k += kT) {
+      const long long i = static_cast<long long>(base) + k - L;
+      win[k] = static_cast<signed char>(
+          i >= 0 && i + L < static_cast<long long>(n) ? lcp(kv, static_cast<u32>(i), static_cast<u32>(i + L)) : -1);
+    }
+    __syncthreads();
+  }
   int ld = 0;
   if (b < n) {
     lcp_next[b] = static_cast<signed char>(b + 1 < n ? lcp(kv, b, b + 1) : -1);
@@ -309,7 +348,8 @@ __global__ void __launch_bounds__(kT)
     if (n > static_cast<u32>(L)) {
       const u32 lo = b >= static_cast<u32>(L) ? b - L : 0;
       const u32 hi = min(b, n - 1 - L);
-      for (u32 i = lo; i <= hi; ++i) w = max(w, lcp(kv, i, i + L));
+      for (u32 i = lo; i <= hi; ++i)
+        w = max(w, shared_win ? static_cast<int>(win[i - base + L]) : lcp(kv, i, i + L));
     }
     ld = min(w + 1, kMaxDepth);
     ld = min(ld, static_cast<int>(tiny[idx[b]]));
@@ -702,14 +742,36 @@ __global__ void __launch_bounds__(kT)
 }
 
 // offsets[b] = start of bucket b; also clears the fill counters.
-__global__ void k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill,
-                                 const u32 *abort = nullptr) {
-  if (threadIdx.x != 0 || aborted(abort)) return;
-  u32 run = 0;
-  for (int b = 0; b < kBuckets; ++b) {
-    offset[b] = run;
-    run += count[b];
-    fill[b] = 0;
+constexpr int kBucketThreads = 512;  // one bucket per thread
+static_assert(kBuckets <= kBucketThreads, "bucket scan covers every bucket");
+__global__ void __launch_bounds__(kBucketThreads)
+    k_bucket_offsets(const u32 *count, u32 *offset, u32 *fill, const u32 *abort = nullptr) {
+  __shared__ u32 part[kBucketThreads / 32];
+  if (aborted(abort)) return;  // the same flag for every thread
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const u32 c = t < kBuckets ? count[t] : 0u;
+  u32 incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 v = __shfl_up_sync(kFullMask, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) part[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const u32 v = lane < kBucketThreads / 32 ? part[lane] : 0u;
+    u32 pi = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 x = __shfl_up_sync(kFullMask, pi, o);
+      if (lane >= o) pi += x;
+    }
+    if (lane < kBucketThreads / 32) part[lane] = pi - v;
+  }
+  __syncthreads();
+  if (t < kBuckets) {
+    offset[t] = part[w] + incl - c;
+    fill[t] = 0;
   }
 }
 
@@ -1067,7 +1129,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                       ws.nbegin.as<u32>(), ws.nend.as<u32>()};
   k_bucket_count<<<mb, kT, 0, s>>>(bv, m, meta);
   GTC_LAUNCH_CHECK();
-  k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets);
+  k_bucket_offsets<<<1, kBucketThreads, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets);
   GTC_LAUNCH_CHECK();
   k_bucket_fill<<<mb, kT, 0, s>>>(bv, m, meta + kBuckets, meta + 2 * kBuckets, bucket);
   GTC_LAUNCH_CHECK();
@@ -1167,7 +1229,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
                       ws.nbegin.as<u32>(), ws.nend.as<u32>()};
   k_bucket_count<<<mb, kT, 0, s>>>(bv, mcap, meta, m_dev, abort, caps.depth);
   GTC_LAUNCH_CHECK();
-  k_bucket_offsets<<<1, 32, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets, abort);
+  k_bucket_offsets<<<1, kBucketThreads, 0, s>>>(meta, meta + kBuckets, meta + 2 * kBuckets, abort);
   GTC_LAUNCH_CHECK();
   k_bucket_fill<<<mb, kT, 0, s>>>(bv, mcap, meta + kBuckets, meta + 2 * kBuckets, bucket, m_dev,
                                   abort);
