@@ -20,9 +20,9 @@ namespace gtc {
 
 constexpr int kMaxDepth = 60;     // depth cap of the reference octree (octree.cpp:18)
 constexpr int kLevelsPerWord = 21;
-// Levels of the per-axis split-value table of the key kernel, and its size
-// per axis (heap order, index 0 unused).
-constexpr int kSplitLevels = 17;
+// Levels of the per-axis split-value table of the key kernel (all of the
+// first key word's), and its size per axis (heap order, index 0 unused).
+constexpr int kSplitLevels = kLevelsPerWord;
 constexpr u32 kSplitSize = 1u << kSplitLevels;
 constexpr u32 kFewBodies = 2;     // accepted cells this small go on the body list (group_lists.h:58)
 constexpr int kMaxGroupSize = 32;
@@ -33,6 +33,9 @@ struct TreeRoot {
   double lo[3], hi[3];
   double center[3];
   double half_at[kMaxDepth + 1];
+  // first level whose node may be "tiny" for some body (from the box: no
+  // body's own bound is larger), kMaxDepth + 1 when none is
+  int tiny_from;
 };
 
 // What the grouped walk reads per node. The FP32 record decides almost every
@@ -121,6 +124,7 @@ struct Scalars {
   unsigned long long spill_used[2];  // one-pass walk: overflow pool entries taken (cells, bodies)
   u32 spilled;            // one-pass walk: groups that outgrew their slots
   unsigned long long walk_nodes;  // node records the walk tested
+  u32 split_unsorted;     // the split table's in-order values decrease somewhere (keys step by level)
 };
 
 // The list statistics of one group per lane (valid lanes), summed and

@@ -206,6 +206,14 @@ __global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, Tre
   half = half * (1.0 + 1e-9) + 1e-300;
   root->half_at[0] = half;
   for (int d = 0; d < kMaxDepth; ++d) root->half_at[d + 1] = 0.5 * root->half_at[d];
+  // every body's |x| + |y| + |z| is at most this sum (rounding is monotone),
+  // so no body's tiny bound in k_keys exceeds this one
+  double m1 = 0.0;
+  for (int a = 0; a < 3; ++a) m1 = m1 + fmax(fabs(lo[a]), fabs(hi[a]));
+  const long long bound = __double_as_longlong(2e-12 * (m1 + 1e-300));
+  int d = 0;
+  while (d <= kMaxDepth && __double_as_longlong(root->half_at[d]) >= bound) ++d;
+  root->tiny_from = d;
 }
 
 // ------------------------------------------------------------------- keys
@@ -238,25 +246,89 @@ __global__ void __launch_bounds__(1024) k_split_top(const TreeRoot *root, double
   }
 }
 
-// Levels kSplitTop..kSplitLevels - 1: one thread per node of level
-// kSplitTop - 1 builds its subtree, level by level.
-// (One warp per block: the subtrees spread over the SMs' FP64 units.)
-__global__ void __launch_bounds__(32) k_split_rest(const TreeRoot *root, double *split) {
-  const u32 per_axis = 1u << (kSplitTop - 1);
-  const u32 tid = blockIdx.x * 32 + threadIdx.x;
+// `Levels` levels below level `from`: one thread per node of level `from`
+// builds its subtree in registers, level by level, and stores it.
+template <int Levels>
+__global__ void __launch_bounds__(kT) k_split_sub(const TreeRoot *root, double *split, int from) {
+  const u32 per_axis = 1u << from;
+  const u32 tid = blockIdx.x * kT + threadIdx.x;
   if (tid >= 3 * per_axis) return;
-  const int axis = static_cast<int>(tid / per_axis);
-  double *t = split + static_cast<u64>(axis) * kSplitSize;
-  const u32 base = per_axis + tid % per_axis;  // heap index at level kSplitTop - 1
-  for (int d = kSplitTop; d < kSplitLevels; ++d) {
-    const double h = root->half_at[d];
-    const int below = d - (kSplitTop - 1);  // levels under the subtree's root
-    const u32 first = base << below;
-    for (u32 j = 0; j < (1u << below); ++j) {
-      const u32 k = first + j;
-      t[k] = t[k >> 1] + ((k & 1u) ? h : -h);
+  double *t = split + static_cast<u64>(tid / per_axis) * kSplitSize;
+  const u32 base = per_axis + tid % per_axis;  // heap index at level `from`
+  double v[2 << Levels];                        // v[1] the subtree's root, heap order below
+  v[1] = t[base];
+#pragma unroll
+  for (int l = 1; l <= Levels; ++l) {
+    const double h = root->half_at[from + l];
+#pragma unroll
+    for (int j = 0; j < (1 << l); ++j) {
+      const int k = (1 << l) + j;
+      v[k] = v[k >> 1] + ((k & 1) ? h : -h);
+      t[(static_cast<u64>(base) << l) + j] = v[k];
     }
   }
+}
+
+// The table in order. Along an axis, the split values in in-order (heap
+// node 2^d + m of level d at in-order position (2m + 1) 2^(kSplitLevels - 1
+// - d) - 1). When they never decrease, a body's path through the table is
+// the rank of its coordinate among them: the number of values <= x, whose
+// kSplitLevels bits are the path's level-0.. bits (up iff x >= the centre),
+// the path's deepest centre being the value at the rank with its last bit
+// cleared.
+constexpr u32 kSplitValues = kSplitSize - 1;  // per axis: heap nodes 1..kSplitSize - 1
+
+// Heap index of in-order position p.
+__device__ __forceinline__ u32 split_heap(u32 p) {
+  const u32 q = p + 1;
+  const int tz = __ffs(q) - 1;
+  return (1u << (kSplitLevels - 1 - tz)) + (q >> (tz + 1));
+}
+
+// In-order neighbours come in (leaf, inner node) pairs, leaves at the even
+// positions: each leaf against the values on either side of it.
+__global__ void __launch_bounds__(kT) k_split_check(const double *split, u32 *unsorted) {
+  constexpr u32 kLeaves = 1u << (kSplitLevels - 1);
+  const u32 t = blockIdx.x * kT + threadIdx.x;
+  if (t >= 3 * kLeaves) return;
+  const double *s = split + static_cast<u64>(t / kLeaves) * kSplitSize;
+  const u32 j = t % kLeaves, p = 2 * j;
+  const u64 v = order_key(s[kLeaves + j]);
+  bool bad = false;
+  if (j > 0) bad |= order_key(s[split_heap(p - 1)]) > v;
+  if (p + 1 < kSplitValues) bad |= v > order_key(s[split_heap(p + 1)]);
+  if (bad) atomicOr(unsorted, 1u);
+}
+
+// Bits b of v at bit 3b (v < 2^21).
+__device__ __forceinline__ u64 spread3(u64 v) {
+  v &= 0x1fffffull;
+  v = (v | v << 32) & 0x1f00000000ffffull;
+  v = (v | v << 16) & 0x1f0000ff0000ffull;
+  v = (v | v << 8) & 0x100f00f00f00f00full;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+  v = (v | v << 2) & 0x1249249249249249ull;
+  return v;
+}
+
+// Rank of kx among an axis's in-order values: a guess from the grid the
+// values lie on (1 / inv_w apart), then moved until the values on either
+// side bracket kx. False if that takes more than a few steps.
+__device__ __forceinline__ bool split_rank(const double *table, u64 kx, double x,
+                                           double lo_edge, float inv_w, u32 &r) {
+  const float g = static_cast<float>(x - lo_edge) * inv_w;
+  int v = g > 0.f ? static_cast<int>(fminf(g, static_cast<float>(kSplitValues))) : 0;
+  for (int it = 0; it < 4; ++it) {
+    if (v > 0 && kx < order_key(__ldg(table + split_heap(v - 1)))) {
+      --v;
+    } else if (v < static_cast<int>(kSplitValues) && kx >= order_key(__ldg(table + split_heap(v)))) {
+      ++v;
+    } else {
+      r = static_cast<u32>(v);
+      return true;
+    }
+  }
+  return false;
 }
 
 // First key word: levels 1..21 from the root; records the first depth whose
@@ -271,22 +343,28 @@ __global__ void __launch_bounds__(32) k_split_rest(const TreeRoot *root, double 
 // twice that bound skip the exact FP64 test; the comparison of two positive
 // doubles is done on their bit patterns.
 __global__ void __launch_bounds__(kT)
-    k_keys(const double *pos, u32 n, const TreeRoot *root, const double *split, u64 *key,
-           u32 *idx, u8 *tiny, u32 *error) {
+    k_keys(const double *pos, u32 n, const TreeRoot *root, const double *split,
+           const u32 *unsorted, u64 *key, u32 *idx, u8 *tiny, u32 *error) {
   __shared__ double half_at[kLevelsPerWord + 1];
+  __shared__ float inv_spacing;  // 1 / the spacing of the table's deepest values
   if (threadIdx.x <= kLevelsPerWord) half_at[threadIdx.x] = root->half_at[threadIdx.x];
+  if (threadIdx.x == 0) inv_spacing = static_cast<float>(1.0 / root->half_at[kSplitLevels - 1]);
   __syncthreads();
+  const bool by_rank = *unsorted == 0;
   const u32 i = blockIdx.x * kT + threadIdx.x;
   if (i >= n) return;
   const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
   if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicOr(error, 4u);
   const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
-  const long long maybe_tiny =
-      __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
   // the first level whose node could be tiny for this body (half_at falls
   // with depth): the levels above it need no tiny test at all
-  int dt = 0;
-  while (dt <= kLevelsPerWord && __double_as_longlong(half_at[dt]) >= maybe_tiny) ++dt;
+  int dt = root->tiny_from;
+  if (dt <= kLevelsPerWord) {
+    const long long maybe_tiny =
+        __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
+    dt = 0;
+    while (dt <= kLevelsPerWord && __double_as_longlong(half_at[dt]) >= maybe_tiny) ++dt;
+  }
   const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
   u32 ix = 1, iy = 1, iz = 1;
   double cx = 0.0, cy = 0.0, cz = 0.0;
@@ -314,6 +392,25 @@ __global__ void __launch_bounds__(kT)
     }
   };
   int d = 0;
+  if (by_rank && dt >= kSplitLevels) {
+    // no tiny test within the table's levels: its levels by rank
+    const float inv_w = inv_spacing;
+    u32 rx, ry, rz;
+    if (split_rank(tx, kx, x, root->center[0] - half_at[0], inv_w, rx) &&
+        split_rank(ty, ky, y, root->center[1] - half_at[0], inv_w, ry) &&
+        split_rank(tz, kz, z, root->center[2] - half_at[0], inv_w, rz)) {
+      k = spread3(rx) | (spread3(ry) << 1) | (spread3(rz) << 2);
+      if (dt <= kLevelsPerWord) {  // the centre below the table, for the last tiny test
+        constexpr u32 kLeaves = 1u << (kSplitLevels - 1);
+        cx = __ldg(tx + kLeaves + (rx >> 1));
+        cy = __ldg(ty + kLeaves + (ry >> 1));
+        cz = __ldg(tz + kLeaves + (rz >> 1));
+        const int o = static_cast<int>((rx & 1u) | ((ry & 1u) << 1) | ((rz & 1u) << 2));
+        step_centre(cx, cy, cz, o, half_at[kSplitLevels]);
+      }
+      d = kSplitLevels;
+    }
+  }
   for (; d < kLevelsPerWord && d < dt; ++d) level(d, false);
   for (; d < kLevelsPerWord; ++d) level(d, true);
   if (dt <= kLevelsPerWord && t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz))
@@ -951,6 +1048,33 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
 }
 
 namespace {
+// The split table, its in-order copy and check, and the first key word of
+// every body.
+void make_keys(Workspace &ws, const double *pos, u32 n, cudaStream_t s) {
+  const TreeRoot *root = ws.root.as<TreeRoot>();
+  Scalars *sc = ws.scalars.as<Scalars>();
+  ws.split.ensure(3ull * kSplitSize * sizeof(double));
+  k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
+  GTC_LAUNCH_CHECK();
+  // levels kSplitTop..20: subtrees of 4, 4 and 2 levels
+  static_assert(kSplitTop - 1 + 4 + 4 + 2 == kSplitLevels - 1, "split table levels");
+  double *split = ws.split.as<double>();
+  k_split_sub<4><<<ceil_div(3u << (kSplitTop - 1), kT), kT, 0, s>>>(root, split, kSplitTop - 1);
+  GTC_LAUNCH_CHECK();
+  k_split_sub<4><<<ceil_div(3u << (kSplitTop + 3), kT), kT, 0, s>>>(root, split, kSplitTop + 3);
+  GTC_LAUNCH_CHECK();
+  k_split_sub<2><<<ceil_div(3u << (kSplitTop + 7), kT), kT, 0, s>>>(root, split, kSplitTop + 7);
+  GTC_LAUNCH_CHECK();
+  k_split_check<<<ceil_div(3u << (kSplitLevels - 1), kT), kT, 0, s>>>(split, &sc->split_unsorted);
+  GTC_LAUNCH_CHECK();
+  k_keys<<<ceil_div(n, kT), kT, 0, s>>>(pos, n, root, split, &sc->split_unsorted,
+                                        ws.key0.as<u64>(), ws.idx.as<u32>(), ws.tiny.as<u8>(),
+                                        &sc->error);
+  GTC_LAUNCH_CHECK();
+}
+}  // namespace
+
+namespace {
 // Sorts the (key, body) pairs on the first `levels` levels of the first key
 // word, rounded up to whole 8-bit passes (21 or more: the whole word), and
 // returns the levels the order is exact for. Bodies that share those levels
@@ -996,13 +1120,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  ws.split.ensure(3ull * kSplitSize * sizeof(double));
-  k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
-  GTC_LAUNCH_CHECK();
-  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 32), 32, 0, s>>>(root, ws.split.as<double>());
-  GTC_LAUNCH_CHECK();
-  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
-  GTC_LAUNCH_CHECK();
+  make_keys(ws, pos, n32, s);
   // the levels the last tree needed first; all of them when a leaf lies
   // deeper (sorting the partly sorted pairs again gives the full order)
   const int sorted = sort_top_levels(ws, n32, ws.sort_levels > 0 ? ws.sort_levels : kLevelsPerWord, s);
@@ -1188,13 +1306,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  ws.split.ensure(3ull * kSplitSize * sizeof(double));
-  k_split_top<<<3, 1024, 0, s>>>(root, ws.split.as<double>());
-  GTC_LAUNCH_CHECK();
-  k_split_rest<<<ceil_div(3u << (kSplitTop - 1), 32), 32, 0, s>>>(root, ws.split.as<double>());
-  GTC_LAUNCH_CHECK();
-  k_keys<<<nb, kT, 0, s>>>(pos, n32, root, ws.split.as<double>(), key0, idx, tiny, &sc->error);
-  GTC_LAUNCH_CHECK();
+  make_keys(ws, pos, n32, s);
   // the levels the captured depth allows: a deeper tree aborts the replay
   const int sorted = sort_top_levels(ws, n32, caps.depth + 1, s);
   const KeyView kv{key0, nullptr, nullptr, 1};
