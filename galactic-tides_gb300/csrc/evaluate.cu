@@ -345,12 +345,13 @@ __global__ void __launch_bounds__(kT)
             const float2 qy = __ffma2_rn(qxy, dx, __ffma2_rn(qyy, dy, __fmul2_rn(qyz, dz)));
             const float2 qz = __ffma2_rn(qxz, dx, __ffma2_rn(qyz, dy, __fmul2_rn(qzz, dz)));
             const float2 rqr = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
-            const float2 inv5 = __fmul2_rn(inv3, inv2), inv7 = __fmul2_rn(inv5, inv2);
-            const float2 along = __ffma2_rn(__fmul2_rn(m25, rqr), inv7, __fmul2_rn(ngm, inv3));
+            // r.Q.r / r^5 once, for both the acceleration along d and the potential
+            const float2 inv5 = __fmul2_rn(inv3, inv2), rqr5 = __fmul2_rn(rqr, inv5);
+            const float2 along = __ffma2_rn(__fmul2_rn(m25, rqr5), inv2, __fmul2_rn(ngm, inv3));
             ax = __ffma2_rn(along, dx, __ffma2_rn(qx, inv5, ax));
             ay = __ffma2_rn(along, dy, __ffma2_rn(qy, inv5, ay));
             az = __ffma2_rn(along, dz, __ffma2_rn(qz, inv5, az));
-            pot = __ffma2_rn(ngm, inv, __ffma2_rn(__fmul2_rn(mhalf, rqr), inv5, pot));
+            pot = __ffma2_rn(mhalf, rqr5, __ffma2_rn(ngm, inv, pot));
           }
           __syncwarp();
         }
