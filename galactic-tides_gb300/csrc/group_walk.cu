@@ -110,6 +110,14 @@ __global__ void k_check_slots_graph(Scalars *sc) {
 // Group bounding box (group_lists.cpp:125-131): centre and half-extent in
 // FP64, and the same in FP32 with the centre taken relative to the root
 // centre (the frame of the FP32 walk records).
+// Order-preserving image of a finite double with +0 and -0 equal: a < b as
+// doubles exactly when key(a) < key(b).
+__device__ __forceinline__ u64 zero_equal_key(double v) {
+  u64 b = static_cast<u64>(__double_as_longlong(v));
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 __global__ void __launch_bounds__(kT)
     k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos,
                 const TreeRoot *root, double *gbox, float *gboxf, const u32 *ng_dev = nullptr,
@@ -118,13 +126,27 @@ __global__ void __launch_bounds__(kT)
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
   const u32 b0 = gbegin[g], b1 = gend[g];
+  // the reference's running min and max (v < lo, hi < v: the first of equal
+  // values stays), compared on integer images of the doubles (+0 and -0
+  // equal) instead of on the FP64 pipe
   double lo[3], hi[3];
-  for (int a = 0; a < 3; ++a) lo[a] = hi[a] = tpos[3ull * b0 + a];
+  u64 klo[3], khi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = hi[a] = tpos[3ull * b0 + a];
+    klo[a] = khi[a] = zero_equal_key(lo[a]);
+  }
   for (u32 k = b0; k < b1; ++k)
     for (int a = 0; a < 3; ++a) {
       const double v = tpos[3ull * k + a];
-      lo[a] = v < lo[a] ? v : lo[a];
-      hi[a] = hi[a] < v ? v : hi[a];
+      const u64 kv = zero_equal_key(v);
+      if (kv < klo[a]) {
+        klo[a] = kv;
+        lo[a] = v;
+      }
+      if (khi[a] < kv) {
+        khi[a] = kv;
+        hi[a] = v;
+      }
     }
   float gmax = 0.f, hmax = 0.f;
   for (int a = 0; a < 3; ++a) {
