@@ -163,6 +163,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.band = ctx->band_override >= 0 ? static_cast<float>(ctx->band_override) : ctx->model_band;
     lw.walk_budget = ctx->walk_budget == 0 ? ~0u : ctx->walk_budget;
     lw.pair_budget = ctx->pair_budget == 0 ? ~0u : ctx->pair_budget;
+    lw.plan_rounds = !ctx->read_every_round;
     gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, s);
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
@@ -857,6 +858,10 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
         throw gtc::InvalidArgument(key + " must be a whole number of nodes >= 0");
       (key == "learned_walk_budget" ? ctx->walk_budget : ctx->pair_budget) =
           static_cast<gtc::u32>(value);
+    } else if (key == "learned_read_every_round") {
+      if (value != 0 && value != 1)
+        throw gtc::InvalidArgument("learned_read_every_round must be 0 or 1");
+      ctx->read_every_round = value != 0;
     } else if (key == "graph_headroom") {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;

@@ -128,11 +128,16 @@ struct LearnedScratch {
   // per-group slots of the three parts of round 0 (0: not sized yet) and
   // of deferred pairs
   u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
+  // rounds the last walk ran and the row capacity for its largest round:
+  // the next walk runs that many rounds before it reads anything back (0:
+  // one read per round)
+  u32 rounds = 0, row_cap = 0;
   void release() {
     for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1], &cont})
       b->release();
     for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
     slot_pend = 0;
+    rounds = row_cap = 0;
   }
 };
 
@@ -149,6 +154,7 @@ struct LearnedWalk {
   float y_mean = 0.f;               // the model's mean correction (centres the prior)
   u32 walk_budget = kLearnedWalkBudget;  // round 0: nodes a thread tests before a warp takes over
   u32 pair_budget = kLearnedPairBudget;  // later rounds: the same
+  bool plan_rounds = true;  // walk the last call's rounds before reading anything back
 };
 
 // Per-node features (after build_tree).

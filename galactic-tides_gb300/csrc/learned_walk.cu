@@ -457,6 +457,7 @@ __global__ void __launch_bounds__(kContWarps * 32) k_lcont(GArgs a, bool later) 
   uint2 *stk = stack_all[threadIdx.x >> 5];
   const unsigned below = (1u << lane) - 1u;
   const u32 ncont = a.sc->lcont;
+  if (a.sc->list_overflow) return;  // a buffer was outgrown: the walk is redone
   for (;;) {
     u32 c = 0;
     if (lane == 0) c = atomicAdd(&a.sc->lcont_taken, 1u);
@@ -615,6 +616,7 @@ __global__ void __launch_bounds__(kContWarps * 32) k_lcont(GArgs a, bool later) 
 __global__ void __launch_bounds__(kRoundThreads) k_lround(GArgs a) {
   const u64 pg = static_cast<u64>(blockIdx.x) * kRoundThreads + threadIdx.x;
   if (pg >= static_cast<u64>(kParts) * a.ng) return;
+  if (a.sc->list_overflow) return;  // an earlier round outgrew a buffer: redone
   const int part = static_cast<int>(pg / a.ng);
   const u32 g = static_cast<u32>(pg % a.ng);
   const u32 k0 = a.roff[pg], k1 = a.roff[pg + 1];
@@ -652,10 +654,20 @@ __global__ void __launch_bounds__(kRoundThreads) k_lround(GArgs a) {
 }
 
 // A round's deferred pairs as dense rows, ordered by (part, group) and, for
-// each, in the order they were deferred.
-__global__ void __launch_bounds__(kT) k_lrows(const GArgs a, uint2 *rows) {
+// each, in the order they were deferred, if the row buffer holds `cap`
+// rows (else the overflow flag); also the round's rows in the statistics.
+__global__ void __launch_bounds__(kT) k_lrows(const GArgs a, uint2 *rows, u64 cap) {
   const u64 pg = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
-  if (pg >= static_cast<u64>(kParts) * a.ng) return;
+  const u64 nparts = static_cast<u64>(kParts) * a.ng;
+  const u32 total = a.roff[nparts];
+  if (a.sc->list_overflow & 1u) return;  // a slot was outgrown: the walk is redone
+  if (pg == 0) {
+    atomicMax(&a.sc->max_rows, total);
+    atomicAdd(&a.sc->mlp_rows, static_cast<unsigned long long>(total));
+    atomicAdd(&a.sc->mlp_batches, static_cast<unsigned long long>((total + 31u) / 32u));
+    if (total > cap) atomicOr(&a.sc->list_overflow, 2u);
+  }
+  if (pg >= nparts || total > cap) return;
   const u32 g = static_cast<u32>(pg % a.ng);
   const u32 n = a.pcount[pg], o = a.roff[pg];
   const u32 *pl = a.pend + pg * a.slot_pend;
@@ -690,9 +702,14 @@ __global__ void __launch_bounds__(kT) k_lgroup_records(const GArgs a, const u32 
 __global__ void __launch_bounds__(kT)
     k_ldecide(const uint2 *q, u64 nq, const WalkRec32 *walk32, const CellFeat *cfeat,
               const float *gboxf, const float2 *gtol, const LearnedNet *net, const TreeRoot *root,
-              const double2 *mom, u8 *dec) {
+              const double2 *mom, u8 *dec, const u32 *nq_dev = nullptr,
+              const u32 *overflow = nullptr) {
   __shared__ NetShared sn;
   __shared__ uint4 rows[kT / 32][32];
+  // rows counted on the device; none written when a buffer was outgrown
+  if (nq_dev && *nq_dev < nq) nq = *nq_dev;
+  if (overflow && *overflow) nq = 0;
+  if (static_cast<u64>(blockIdx.x) * kT >= nq) return;  // the whole block
   load_net(net, sn);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -842,8 +859,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   // warps that take the handed-on walks in turn: a few per SM
   const u32 cont_blocks = static_cast<u32>(std::max(1, sms) * 4);
-  u64 rows = 0, batches = 0;
-  u32 rounds = 0;
+  u32 rounds = 0;  // rounds walked
   for (int attempt = 0;; ++attempt) {
     u64 c_at = 0, b_at = 0;
     for (int k = 0; k < kParts; ++k) {
@@ -868,15 +884,18 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(sc->lmax_cells, 0, (2 * kParts + 1) * sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
-    rows = batches = 0;
-    bool overflow = false;
+    GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
+    GTC_CUDA(cudaMemsetAsync(&sc->max_rows, 0, sizeof(u32), s));
+    u32 *roff = ls.roff.as<u32>();
     int qsel = 0;
-    for (rounds = 0;; ++rounds) {
-      if (rounds >= static_cast<u32>(kMaxRounds))
+    // one round: its walk, the warps' continuations, and the scan of the
+    // pairs it deferred (their total at roff[nparts])
+    auto walk_round = [&](u32 r) {
+      if (r >= static_cast<u32>(kMaxRounds))
         throw RuntimeError("learned walk: more rounds than the tree has levels");
       GTC_CUDA(cudaMemsetAsync(&sc->lcont, 0, 2 * sizeof(u32), s));
-      a.budget = rounds == 0 ? lw.walk_budget : lw.pair_budget;
-      if (rounds == 0) {
+      a.budget = r == 0 ? lw.walk_budget : lw.pair_budget;
+      if (r == 0) {
         k_lround0<<<rb, kRoundThreads, 0, s>>>(a);
       } else {
         a.rows = ls.q[qsel].as<uint2>();
@@ -884,11 +903,30 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
         k_lround<<<rb, kRoundThreads, 0, s>>>(a);
       }
       GTC_LAUNCH_CHECK();
-      k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, rounds > 0);
+      k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, r > 0);
       GTC_LAUNCH_CHECK();
-      u32 *roff = ls.roff.as<u32>();
       exclusive_scan_u32(a.pcount, roff, nparts, roff + nparts, ws.scan_tmp, s);
-      u32 deferred = 0, flags[2] = {0, 0};
+    };
+    // the round's deferred pairs as rows, and the network's decisions on
+    // them: `launch_rows` rows' worth of blocks, the count read on the device
+    auto decide = [&](u64 launch_rows) {
+      const int nq = qsel ^ 1;
+      const u64 cap = std::min<u64>(ls.q[nq].bytes / sizeof(uint2), ls.dec[nq].bytes);  // rows held
+      k_lrows<<<pb, kT, 0, s>>>(a, ls.q[nq].as<uint2>(), cap);
+      GTC_LAUNCH_CHECK();
+      if (launch_rows > 0) {
+        k_ldecide<<<ceil_div(launch_rows, kT), kT, 0, s>>>(
+            ls.q[nq].as<uint2>(), launch_rows, ws.walk32.as<WalkRec32>(), lw.cfeat, a.gboxf,
+            a.gtol, lw.net, ws.root.as<TreeRoot>(), ws.mom.as<double2>(), ls.dec[nq].as<u8>(),
+            roff + nparts, &sc->list_overflow);
+        GTC_LAUNCH_CHECK();
+      }
+      qsel = nq;
+    };
+    // the last round's deferred pairs and the flags; true on overflow
+    u32 deferred = 0;
+    auto read_back = [&]() {
+      u32 flags[2] = {0, 0};
       GTC_CUDA(cudaMemcpyAsync(&deferred, roff + nparts, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags, &sc->list_overflow, sizeof(u32), cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(flags + 1, &sc->error, sizeof(u32), cudaMemcpyDeviceToHost, s));
@@ -896,28 +934,40 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       if (flags[1])
         throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
                            std::to_string(flags[1]) + ")");
-      if (flags[0]) {
-        overflow = true;
-        break;
+      return flags[0] != 0;
+    };
+    bool overflow = false;
+    rounds = 0;
+    if (lw.plan_rounds && ls.rounds > 0 && ls.row_cap > 0) {
+      // as many rounds as the last walk, with buffers for its largest one,
+      // and one read back at the end
+      for (int k = 0; k < 2; ++k) {
+        ls.q[k].ensure(static_cast<u64>(ls.row_cap) * sizeof(uint2));
+        ls.dec[k].ensure(ls.row_cap);
       }
-      if (deferred == 0) break;
-      // the deferred pairs as dense rows, with the network's decisions
-      const int nq = qsel ^ 1;
-      ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
-      ls.dec[nq].ensure(deferred);
-      k_lrows<<<pb, kT, 0, s>>>(a, ls.q[nq].as<uint2>());
-      GTC_LAUNCH_CHECK();
-      k_ldecide<<<ceil_div(deferred, kT), kT, 0, s>>>(
-          ls.q[nq].as<uint2>(), deferred, ws.walk32.as<WalkRec32>(), lw.cfeat, a.gboxf, a.gtol,
-          lw.net, ws.root.as<TreeRoot>(), ws.mom.as<double2>(), ls.dec[nq].as<u8>());
-      GTC_LAUNCH_CHECK();
-      rows += deferred;
-      batches += (deferred + 31) / 32;
-      qsel = nq;
+      for (; rounds < ls.rounds; ++rounds) {
+        walk_round(rounds);
+        decide(ls.row_cap);
+      }
+      overflow = read_back();
+    }
+    // then one read back per round until a round defers nothing (the last
+    // planned round's pairs are decided already)
+    if (!overflow && (rounds == 0 || deferred > 0)) {
+      for (;;) {
+        walk_round(rounds);
+        ++rounds;
+        overflow = read_back();
+        if (overflow || deferred == 0) break;
+        const int nq = qsel ^ 1;
+        ls.q[nq].ensure(static_cast<u64>(deferred) * sizeof(uint2));
+        ls.dec[nq].ensure(deferred);
+        decide(deferred);
+      }
     }
     if (!overflow) break;
-    // a slot was outgrown: the counts went on, so slots of their size fit
-    // that round at least; walk again from the start
+    // a slot or the rows outgrew their buffers: the counts went on, so
+    // buffers of their size fit; walk again from the start
     Scalars h{};
     GTC_CUDA(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));
@@ -927,7 +977,8 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       for (int k = 0; k < kParts; ++k)
         m += " " + std::to_string(ls.slot_cells[k]) + "/" + std::to_string(h.lmax_cells[k]) + " " +
              std::to_string(ls.slot_bodies[k]) + "/" + std::to_string(h.lmax_bodies[k]);
-      m += " pend " + std::to_string(ls.slot_pend) + "/" + std::to_string(h.max_pend) + ")";
+      m += " pend " + std::to_string(ls.slot_pend) + "/" + std::to_string(h.max_pend) +
+           "; rows " + std::to_string(ls.row_cap) + "/" + std::to_string(h.max_rows) + ")";
       throw RuntimeError(m);
     }
     for (int k = 0; k < kParts; ++k) {
@@ -935,13 +986,10 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       ls.slot_bodies[k] = std::max<u32>(ls.slot_bodies[k], learned_slot(h.lmax_bodies[k]));
     }
     ls.slot_pend = std::max<u32>(ls.slot_pend, learned_slot(h.max_pend));
+    if (h.list_overflow & 2u) ls.row_cap = std::max<u32>(ls.row_cap, learned_slot(h.max_rows));
   }
   // group records and statistics
   GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
-  host->mlp_rows = rows;
-  host->mlp_batches = batches;
-  GTC_CUDA(cudaMemcpyAsync(&sc->mlp_rows, &host->mlp_rows, 2 * sizeof(unsigned long long),
-                           cudaMemcpyHostToDevice, s));
   k_lgroup_records<<<gb, kT, 0, s>>>(a, ws.gbegin.as<u32>(), ws.gend.as<u32>(),
                                      ws.groups.as<uint4>());
   GTC_LAUNCH_CHECK();
@@ -950,13 +998,15 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   ws.n_cell_list = host->n_cell_list;
   ws.n_body_list = host->n_body_list;
   ws.gapped = true;
-  ws.list_passes = rounds + 1;
+  ws.list_passes = rounds;
   // slots for the next learned walk, from this one's longest lists
   for (int k = 0; k < kParts; ++k) {
     ls.slot_cells[k] = learned_slot(host->lmax_cells[k]);
     ls.slot_bodies[k] = learned_slot(host->lmax_bodies[k]);
   }
   ls.slot_pend = learned_slot(host->max_pend);
+  ls.rounds = rounds;
+  ls.row_cap = learned_slot(host->max_rows);
 }
 
 void learned_record_amag(const float4 *out, const u32 *order, u64 n, float *amag,

@@ -113,6 +113,7 @@ struct Scalars {
   unsigned long long mlp_rows;    // learned walk: rows the MLP decided
   unsigned long long mlp_batches; // learned walk: warp inferences
   u32 lcont, lcont_taken; // learned walk: walks handed on to warps, and taken so far
+  u32 max_rows;           // learned walk: most pairs one round deferred (all parts and groups)
   u32 list_overflow;      // learned walk: a list slot overflowed
   u32 abort;              // graph replay: the step outgrew the captured sizes (bits)
   u32 error;              // device-detected failure code (0 = none)

@@ -291,6 +291,11 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
  *                        hold the same entries; only their order depends on it.
  *   "learned_pair_budget" the same for the later rounds (default 32), which
  *                        walk the subtrees of the pairs the network opened.
+ *   "learned_read_every_round" 0 (default) or 1: the learned walk first runs
+ *                        as many rounds as its last call needed, then reads
+ *                        back how many pairs the last one deferred (more
+ *                        rounds follow one read back each); 1 reads back
+ *                        after every round. Results do not depend on it.
  *   "graph_headroom"     0..4 (default 0.25): a leapfrog graph is captured
  *                        with buffers this fraction larger than the last
  *                        solve's tree and lists (0: exactly those sizes, so

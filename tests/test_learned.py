@@ -274,6 +274,36 @@ def test_walk_budget_only_reorders_the_lists(gtc):
 
 
 @gpu
+def test_rounds_before_the_first_read_back(gtc):
+    """The learned walk runs as many rounds as its last call needed before it
+    reads anything back, with row buffers sized by that call's largest
+    round. After a prior-only call (no network rows, one round) the network
+    deciding every guarded test needs more rounds and more rows: the walk
+    grows its buffers, walks again and goes on round by round, with the same
+    forces as a walk that reads back after every round."""
+    pos, _, mass, _ = gtc.make_galaxy(60_000, seed=8)
+    kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
+    runs = []
+    for every in (0, 1):
+        with _learned_ctx(gtc) as c:
+            c.set_option("learned_read_every_round", every)
+            c.group_force(pos, mass, **kw)  # theta: no previous |a|
+            c.set_option("learned_band", 0.0)
+            c.group_force(pos, mass, **kw)
+            assert c.stats()["mlp_rows"] < 100  # ties at the threshold only
+            c.set_option("learned_band", 1e6)
+            acc, _ = c.group_force(pos, mass, **kw)
+            st = c.stats()
+            again, _ = c.group_force(pos, mass, **kw)  # now the plan fits
+            runs.append((acc, st, again, c.stats()))
+    (acc0, st0, again0, st0b), (acc1, st1, again1, st1b) = runs
+    assert st0["list_passes"] >= 2 and st0["mlp_rows"] > 0
+    for key in ("list_passes", "mlp_rows", "mlp_batches", "cell_interactions", "body_interactions"):
+        assert st0[key] == st1[key] and st0b[key] == st1b[key], key
+    assert np.array_equal(acc0, acc1) and np.array_equal(again0, again1)
+
+
+@gpu
 def test_band_only_skips_the_network_where_it_cannot_change_the_decision(gtc):
     """The training band (the 0.99 quantile of the network's correction)
     leaves to the prior only tests the network would decide the same way."""
@@ -374,3 +404,5 @@ def test_invalid_learned_arguments(ctx, gtc):
         ctx.set_option("learned_walk_budget", -1)
     with pytest.raises(gtc.GtcInvalidArgument):
         ctx.set_option("learned_pair_budget", 0.5)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        ctx.set_option("learned_read_every_round", 2)
