@@ -159,17 +159,18 @@ __global__ void __launch_bounds__(kT)
 }
 
 __global__ void __launch_bounds__(kT)
-    k_cell_feat(const double2 *geom, const double2 *mom, const double2 *quad, const double *delta,
+    k_cell_feat(const double2 *geom, const double2 *mom, const float4 *cells, const double *delta,
                 const TreeRoot *root, u32 m, CellFeat *out) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p >= m) return;
   const FeatScale fs = scale_of(root, mom);
-  const double2 qa = quad[3 * p], qb = quad[3 * p + 1], qc = quad[3 * p + 2];
+  // mass and quadrupole from the FP32 cell (as the evaluator sees them)
+  const float4 cm = cells[3 * p], qa = cells[3 * p + 1], qb = cells[3 * p + 2];
   // Frobenius norm of the symmetric tensor (off-diagonal terms twice)
-  const double qn = sqrt(qa.x * qa.x + qa.y * qa.y + qb.x * qb.x +
-                         2.0 * (qb.y * qb.y + qc.x * qc.x + qc.y * qc.y));
-  out[p] = cell_features(static_cast<float>(geom[2 * p + 1].y), static_cast<float>(mom[2 * p + 1].y),
-                         static_cast<float>(qn), static_cast<float>(delta[p]), fs);
+  const float qn = sqrtf(qa.x * qa.x + qa.y * qa.y + qa.z * qa.z +
+                         2.f * (qa.w * qa.w + qb.x * qb.x + qb.y * qb.y));
+  out[p] = cell_features(static_cast<float>(geom[2 * p + 1].y), cm.w, qn,
+                         static_cast<float>(delta[p]), fs);
 }
 
 __global__ void __launch_bounds__(kT)
@@ -781,7 +782,7 @@ void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s) {
   if (m == 0) return;
   cfeat.ensure(static_cast<u64>(m) * sizeof(CellFeat));
   k_cell_feat<<<ceil_div(m, kT), kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(),
-                                             ws.quad.as<double2>(), ws.delta.as<double>(),
+                                             ws.cells.as<float4>(), ws.delta.as<double>(),
                                              ws.root.as<TreeRoot>(), m, cfeat.as<CellFeat>());
   GTC_LAUNCH_CHECK();
 }
