@@ -225,7 +225,7 @@ constexpr float kFar = 1.0e30f;
 constexpr int kPairCellF4 = 5;   // float4 per staged cell pair
 constexpr int kPairBodyF4 = 2;   // float4 per staged body pair
 constexpr u32 kMaxSlices = 16;   // slices per group at most
-constexpr u32 kPassCost = 8;     // a pass's fixed cost, in staged entries per lane
+constexpr u32 kPassCost = 24;    // a pass's fixed cost, in staged entries per lane
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
