@@ -68,6 +68,15 @@ void Workspace::release_all() {
   for (DeviceBuffer *b : all) b->release();
   if (host_words) cudaFreeHost(host_words);
   host_words = nullptr;
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+    cudaEventDestroy(side_fork);
+    cudaEventDestroy(side_done);
+  }
+  side = nullptr;
+  side_fork = side_done = nullptr;
+  side_pending = false;
 }
 
 }  // namespace gtc
@@ -146,10 +155,13 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   const bool learned = sp.criterion == GTC_CRITERION_LEARNED && ctx->have_model &&
                        ctx->prev_n == n;
   GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
+  const gtc::SideJoin side_join{ws, s};
   gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
   GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
   if (learned) {
-    gtc::learned_node_features(ws, ctx->cfeat, s);
+    // the node features and walk records after the moments, on their stream
+    const cudaStream_t ns = ws.side_pending ? ws.side : s;
+    gtc::learned_node_features(ws, ctx->cfeat, ns);
     gtc::LearnedWalk lw;
     lw.net = ctx->net.as<gtc::LearnedNet>();
     lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
@@ -164,7 +176,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.walk_budget = ctx->walk_budget == 0 ? ~0u : ctx->walk_budget;
     lw.pair_budget = ctx->pair_budget == 0 ? ~0u : ctx->pair_budget;
     lw.plan_rounds = !ctx->read_every_round;
-    gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, s);
+    gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, ns);
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
     gtc::build_lists(ws, sp, s, ctx->host_sc);

@@ -680,6 +680,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
+  join_side(ws, s);  // the walk reads the node records (and the tolerances the root's mass)
   if (lw) {
     learned_group_tolerances(ws, *lw, ng, s);
     learned_build_lists(ws, *lw, ng, host, s);

@@ -405,6 +405,7 @@ void learned_add_samples(gtc_context *ctx, const double *pos, const double *mass
   if (n == 0 || max_new == 0) return;
   cudaStream_t s = ctx->stream;
   Workspace &ws = ctx->ws;
+  const SideJoin side_join{ws, s};
   build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
   build_lists(ws, sp, s, ctx->host_sc);
   const u32 m = static_cast<u32>(ws.n_nodes), ng = static_cast<u32>(ws.n_groups);

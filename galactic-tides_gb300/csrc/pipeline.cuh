@@ -93,6 +93,12 @@ struct Workspace {
   u32 slot_cells = 0, slot_bodies = 0, slot_near_cells = 0, slot_near_bodies = 0;
   bool gapped = false;
   u32 list_passes = 0;  // walks of the last list build (1 one pass, 2 count + fill, rounds)
+  // The tree's moments and node records run on a side stream once the
+  // topology is known, beside the group choice on the main stream; whoever
+  // reads them first makes the main stream wait for `side_done`.
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_fork = nullptr, side_done = nullptr;
+  bool side_pending = false;
   // Overflow pool behind n_groups slots of `slot` entries: a sixteenth of
   // the slots plus four slots.
   static u64 pool_for(u64 n_groups, u32 slot) { return n_groups * slot / 16 + 4ull * slot; }
@@ -223,6 +229,17 @@ __device__ __forceinline__ void warp_add(unsigned long long *total, unsigned lon
 // Fills geometry, moments, ranges, the tree-order permutation (idx), the
 // FP32 bodies and cells and the walk records. Returns the node count.
 // `host` is pinned memory the device scalars are read back into.
+// The side stream, started after the work queued on s so far.
+cudaStream_t fork_side(Workspace &ws, cudaStream_t s);
+// Work queued on the side stream so far ends before what s runs next.
+void join_side(Workspace &ws, cudaStream_t s);
+// Joins the side stream when it leaves scope (every exit of a solve).
+struct SideJoin {
+  Workspace &ws;
+  cudaStream_t s;
+  ~SideJoin() { join_side(ws, s); }
+};
+
 void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                 const SolverParams &sp, cudaStream_t s, Scalars *host);
 

@@ -1047,6 +1047,25 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
 }
 
+cudaStream_t fork_side(Workspace &ws, cudaStream_t s) {
+  if (!ws.side) {
+    GTC_CUDA(cudaStreamCreateWithFlags(&ws.side, cudaStreamNonBlocking));
+    GTC_CUDA(cudaEventCreateWithFlags(&ws.side_fork, cudaEventDisableTiming));
+    GTC_CUDA(cudaEventCreateWithFlags(&ws.side_done, cudaEventDisableTiming));
+  }
+  GTC_CUDA(cudaEventRecord(ws.side_fork, s));
+  GTC_CUDA(cudaStreamWaitEvent(ws.side, ws.side_fork, 0));
+  ws.side_pending = true;
+  return ws.side;
+}
+
+void join_side(Workspace &ws, cudaStream_t s) {
+  if (!ws.side_pending) return;
+  ws.side_pending = false;
+  if (cudaEventRecord(ws.side_done, ws.side) == cudaSuccess)
+    cudaStreamWaitEvent(s, ws.side_done, 0);
+}
+
 namespace {
 // The split table, its in-order copy and check, and the first key word of
 // every body.
@@ -1112,6 +1131,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   ws.tmass.ensure(n * 8);
   ws.bodies.ensure(n * sizeof(float4));
   ws.scalars.ensure(sizeof(Scalars));
+  join_side(ws, s);  // nothing of an earlier call may still write the buffers
   Scalars *sc = ws.scalars.as<Scalars>();
   GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
 
@@ -1266,10 +1286,13 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     for (int b = b0; b < b0 + nb; ++b) c += counts[b];
     o = counts[kBuckets + b0];
   };
+  // the moments and node records on the side stream: the FP64 moments'
+  // small depths leave most SMs idle, and the group choice needs none of it
+  cudaStream_t ms = fork_side(ws, s);
   {
     u32 c, o;
     range(kLeafBucket, kLeafClasses, c, o);
-    if (c) k_leaf_moments<<<ceil_div(c, kT), kT, 0, s>>>(ma, bucket + o, c);
+    if (c) k_leaf_moments<<<ceil_div(c, kT), kT, 0, ms>>>(ma, bucket + o, c);
     GTC_LAUNCH_CHECK();
   }
   for (int d = kMaxDepth; d >= 0; --d) {
@@ -1277,14 +1300,14 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     range(d * kSizeClasses, kSizeClasses, c, o);
     if (!c) continue;
     const u32 per = nodes_per_warp(c);
-    k_node_moments<<<ceil_div(c, per), 32, 0, s>>>(ma, bucket + o, c, per);
+    k_node_moments<<<ceil_div(c, per), 32, 0, ms>>>(ma, bucket + o, c, per);
     GTC_LAUNCH_CHECK();
   }
-  k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
-                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
-                                 1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
-                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>());
+  k_pack_nodes<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
+                                  ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                  ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
+                                  1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
+                                  ws.walk64.as<WalkRec64>(), ws.cells.as<float4>());
   GTC_LAUNCH_CHECK();
   k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
                                   root_centre(root), ws.bodies.as<float4>());
