@@ -103,6 +103,28 @@ def test_deep_clump(ctx, oracle):
     assert ctx.stats()["depth"] > 21
 
 
+def test_trees_deeper_and_shallower_than_the_last(gtc, oracle):
+    """The sort orders only the key levels the context's last tree needed,
+    plus one: a deeper tree is sorted again on all 21 levels (and with a
+    second key word where needed), then shallower ones follow; each is the
+    oracle's tree."""
+    rng = np.random.default_rng(12)
+    wide = rng.normal(size=(3000, 3)) * 10.0
+
+    def clump(scale):
+        return np.concatenate([wide, 1.0 + rng.normal(size=(300, 3)) * scale])
+
+    cases = [wide, clump(1e-3), clump(1e-7), wide, clump(1e-3)]
+    depths = []
+    with gtc.Context(0) as c:
+        for pos in cases:
+            mass = np.full(len(pos), 1.0 / len(pos))
+            solve_and_compare(c, oracle, pos, mass, theta=0.75, gs=32, pack=True)
+            depths.append(c.stats()["depth"])
+    assert depths[0] < depths[1] <= 21 < depths[2], depths
+    assert depths[3] == depths[0] and depths[4] == depths[1], depths
+
+
 def test_tiny_inputs(ctx, oracle):
     for n in (1, 2, 3, 8, 9, 33):
         pos, mass = lopsided_sphere(n, n)
