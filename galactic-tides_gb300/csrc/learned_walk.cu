@@ -1,6 +1,7 @@
 // The learned criterion inside the grouped walk: per-node features, per-group
-// tolerances, the walk with warp-level BF16 tensor-core inference, and the
-// tensor-core layout of the model.
+// tolerances, the walk in rounds (threads per group, warps for the long
+// walks), the warp-level BF16 tensor-core inference on the pairs a round
+// defers, and the tensor-core layout of the model.
 //
 // Inference runs on the legacy warp-synchronous tensor path (mma.sync
 // m16n8k16, BF16 operands, FP32 accumulators): one warp evaluates 32 rows

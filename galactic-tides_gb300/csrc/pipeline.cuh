@@ -5,10 +5,14 @@
 //              words of octant digits), tree-order permutation, tree-order
 //              FP64 positions/masses, FP32 bodies (float4), FP32 output.
 //   per node   geometry (centre, half), FP64 moments (com, mass, quadrupole,
-//              delta), range [begin, end), skip, parent, depth, and the packed
-//              FP32 cell (48 B) and FP64 walk record (80 B) the kernels read.
-//   per group  target range, FP64 bounding box, list offsets, GTGroup.
-//   lists      cell_list / body_list, uint32 node / body indices.
+//              delta), range [begin, end), skip, parent, depth, children, and
+//              the packed FP32 cell (48 B), FP32 walk record (48 B) and FP64
+//              walk record (64 B) the kernels read.
+//   per axis   the split table: the centres of key levels 0..20, heap order.
+//   per group  target range, FP64 and FP32 boxes, and the 64 B group record
+//              (counts and up to three segments of each list).
+//   lists      cell_list / body_list, uint32 node / body indices: back to
+//              back, or in per-group slots (one segment per walk part).
 // Nodes are numbered in the reference walk's visiting order (root, then the
 // children's subtrees last octant first), which makes the grouped walk a
 // stackless forward scan with skip links.
