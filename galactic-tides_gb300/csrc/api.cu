@@ -66,8 +66,6 @@ void Workspace::release_all() {
                          &groups, &cell_list, &body_list, &spill, &splitpt, &root, &bbox_part, &scalars, &split, &scan_tmp,
                          &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
-  if (host_words) cudaFreeHost(host_words);
-  host_words = nullptr;
   if (side) {
     cudaStreamSynchronize(side);
     cudaStreamDestroy(side);

@@ -88,7 +88,6 @@ struct Workspace {
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
   int sort_levels = 0;        // key levels the next eager build sorts first (0: all 21)
-  u32 *host_words = nullptr;  // pinned, for small read-backs
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
   // One-pass walk: group g's lists start at g * slot_cells and g *
   // slot_bodies (capacities sized from the previous walk's longest lists);

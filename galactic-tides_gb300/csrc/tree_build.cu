@@ -895,9 +895,12 @@ __global__ void __launch_bounds__(kT)
 }
 
 __global__ void __launch_bounds__(kT)
-    k_leaf_moments(MomentArrays a, const u32 *bucket, u32 count) {
+    k_leaf_moments(MomentArrays a, const u32 *bucket, const u32 *meta) {
+  // the leaf buckets' count and first place, from the bucket scan
+  u32 count = 0;
+  for (int b = kLeafBucket; b < kLeafBucket + kLeafClasses; ++b) count += meta[b];
   const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k < count) leaf_moments(a, bucket[k]);
+  if (k < count) leaf_moments(a, bucket[meta[kBuckets + kLeafBucket] + k]);
 }
 
 // Inner-node moments of one depth: one warp per block, `per` nodes to a
@@ -911,18 +914,12 @@ __host__ __device__ __forceinline__ u32 nodes_per_warp(u32 count) {
   return per < 1 ? 1u : (per > 32 ? 32u : per);
 }
 
+// Over the device counts of buckets [b0, b0 + nb) (leaves or one depth's
+// inner nodes), grid-stride over kMomentWarps warps: no count is read back,
+// so the launches of every depth queue at once (eager and graph replays).
 __global__ void __launch_bounds__(32)
-    k_node_moments(MomentArrays a, const u32 *bucket, u32 count, u32 per) {
-  const u32 lane = threadIdx.x;
-  const u64 k = static_cast<u64>(blockIdx.x) * per + lane;
-  if (lane < per && k < count) node_moments(a, bucket[k]);
-}
-
-// The same for a graph replay, over the device counts of buckets
-// [b0, b0 + nb) (leaves or one depth's inner nodes), grid-stride.
-__global__ void __launch_bounds__(32)
-    k_moments_graph(MomentArrays a, const u32 *bucket, const u32 *meta, int b0, int nb,
-                    const u32 *abort) {
+    k_node_moments(MomentArrays a, const u32 *bucket, const u32 *meta, int b0, int nb,
+                   const u32 *abort) {
   if (*abort) return;
   u32 count = 0;
   for (int b = b0; b < b0 + nb; ++b) count += meta[b];
@@ -1004,15 +1001,6 @@ __global__ void __launch_bounds__(kT)
                           static_cast<float>(tpos[3ull * k + 1] - origin[1]),
                           static_cast<float>(tpos[3ull * k + 2] - origin[2]),
                           static_cast<float>(tmass[k]));
-}
-
-// Pinned host words for small read-backs (kept in the workspace).
-u32 *host_meta(Workspace &ws) {
-  if (!ws.host_words) {
-    GTC_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ws.host_words), 2 * kBuckets * sizeof(u32),
-                           cudaHostAllocDefault));
-  }
-  return ws.host_words;
 }
 
 const double *root_centre(const TreeRoot *root) {
@@ -1148,8 +1136,17 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   KeyView kv{key0, nullptr, nullptr, 1};
   signed char *lcp_next = ws.lcp.as<signed char>();
   u8 *leafdepth = ws.leafdepth.as<u8>();
+  // Node numbering: count the nodes ending at each sorted position (with
+  // the levels, so that one read back serves both).
+  u32 *count = ws.count.as<u32>(), *cscan = ws.count_scan.as<u32>();
+  auto count_nodes = [&] {
+    k_node_count<<<nb, kT, 0, s>>>(lcp_next, leafdepth, n32, count);
+    GTC_LAUNCH_CHECK();
+    exclusive_scan_u32(count, cscan, n, &sc->n_nodes, ws.scan_tmp, s);
+  };
   k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
   GTC_LAUNCH_CHECK();
+  count_nodes();
   read_scalars(ws, host, s);
   if (host->error & 4u) throw InvalidArgument("cuda: positions must be finite");
   if (sorted < kLevelsPerWord && static_cast<int>(host->depth) > sorted) {
@@ -1158,8 +1155,10 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     GTC_CUDA(cudaMemsetAsync(&sc->depth, 0, sizeof(u32), s));
     k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
     GTC_LAUNCH_CHECK();
+    count_nodes();
     read_scalars(ws, host, s);
   }
+  const bool had_deep = host->deep > 0;
 
   // Deeper key words for bodies whose leaves lie below the words so far.
   while (host->deep > 0 && kv.words < 3) {
@@ -1219,13 +1218,10 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   if (host->deep > 0) throw RuntimeError("octree deeper than the depth cap");
   ws.key_words = kv.words;
   ws.sort_levels = kv.words == 1 ? static_cast<int>(host->depth) + 1 : 0;
-
-  // Node numbering: count the nodes ending at each sorted position.
-  u32 *count = ws.count.as<u32>(), *cscan = ws.count_scan.as<u32>();
-  k_node_count<<<nb, kT, 0, s>>>(lcp_next, leafdepth, n32, count);
-  GTC_LAUNCH_CHECK();
-  exclusive_scan_u32(count, cscan, n, &sc->n_nodes, ws.scan_tmp, s);
-  read_scalars(ws, host, s);
+  if (had_deep) {  // new key words: count again
+    count_nodes();
+    read_scalars(ws, host, s);
+  }
   const u32 m = host->n_nodes;
   ws.n_nodes = m;
   ws.geom.ensure(m * 2 * sizeof(double2));
@@ -1271,36 +1267,21 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_LAUNCH_CHECK();
   k_bucket_fill<<<mb, kT, 0, s>>>(bv, m, meta + kBuckets, meta + 2 * kBuckets, bucket);
   GTC_LAUNCH_CHECK();
-  u32 counts[2 * kBuckets];
-  GTC_CUDA(cudaMemcpyAsync(host_meta(ws), meta, 2 * kBuckets * sizeof(u32),
-                           cudaMemcpyDeviceToHost, s));
-  GTC_CUDA(cudaStreamSynchronize(s));
-  std::memcpy(counts, host_meta(ws), sizeof counts);
   MomentArrays ma{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                   ws.skip.as<u32>(), ws.parent.as<u32>(), ws.nchild.as<u8>(),
                   ws.kids.as<uint4>(), ws.tpos.as<double>(), ws.tmass.as<double>(),
                   ws.mom.as<double2>(),
                   ws.quad.as<double2>(), ws.delta.as<double>()};
-  auto range = [&](int b0, int nb, u32 &c, u32 &o) {
-    c = 0;
-    for (int b = b0; b < b0 + nb; ++b) c += counts[b];
-    o = counts[kBuckets + b0];
-  };
   // the moments and node records on the side stream: the FP64 moments'
-  // small depths leave most SMs idle, and the group choice needs none of it
+  // small depths leave most SMs idle, and the group choice needs none of
+  // it. Bucket sizes are read on the device: leaves (at most m), then each
+  // depth's inner nodes from the deepest possible one up.
   cudaStream_t ms = fork_side(ws, s);
-  {
-    u32 c, o;
-    range(kLeafBucket, kLeafClasses, c, o);
-    if (c) k_leaf_moments<<<ceil_div(c, kT), kT, 0, ms>>>(ma, bucket + o, c);
-    GTC_LAUNCH_CHECK();
-  }
-  for (int d = kMaxDepth; d >= 0; --d) {
-    u32 c, o;
-    range(d * kSizeClasses, kSizeClasses, c, o);
-    if (!c) continue;
-    const u32 per = nodes_per_warp(c);
-    k_node_moments<<<ceil_div(c, per), 32, 0, ms>>>(ma, bucket + o, c, per);
+  k_leaf_moments<<<mb, kT, 0, ms>>>(ma, bucket, meta);
+  GTC_LAUNCH_CHECK();
+  for (int d = static_cast<int>(host->depth) - 1; d >= 0; --d) {
+    k_node_moments<<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, d * kSizeClasses,
+                                                 kSizeClasses, &sc->abort);
     GTC_LAUNCH_CHECK();
   }
   k_pack_nodes<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
@@ -1378,10 +1359,10 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const u32 gb = std::min<u32>(mb, static_cast<u32>(std::max(1, 8 * sms)));
-  k_moments_graph<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
+  k_node_moments<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
   GTC_LAUNCH_CHECK();
   for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
-    k_moments_graph<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses,
+    k_node_moments<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses,
                                                 abort);
     GTC_LAUNCH_CHECK();
   }
