@@ -77,6 +77,10 @@ class Context {
     check(gtc_get_stats(ctx_, &s), ctx_);
     return s;
   }
+  // A tuning option by name (gtc_set_option; the names are listed in gtc.h).
+  void set_option(const char *name, double value) {
+    check(gtc_set_option(ctx_, name, value), ctx_);
+  }
   gtc_context *handle() { return ctx_; }
 
  private:
