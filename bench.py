@@ -129,11 +129,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def galaxy(n):
-    import __graft_entry__
-    gtc = __graft_entry__.load_package().gtc
-    pos, vel, mass, _ = gtc.make_galaxy(n, seed=1)
+def galaxy(n, seed=1):
+    """The benchmark galaxy, from the pure-numpy generator loaded by its path
+    (the package itself, and with it libgtc.so, stays unloaded: the reference
+    arm uses this too)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "gtc_bench_galaxy", ROOT / "galactic-tides_gb300" / "galaxy.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    pos, vel, mass, _ = mod.make_galaxy(n, seed=seed)
     return pos, vel, mass
+
+
+def warmup_steps(args):
+    return max(3, args.warmup)
+
+
+def bench_config(n):
+    """The workload, identical in both arms."""
+    return {"workload": WORKLOAD, "n": n,
+            "l2": ("inputs and working set larger than L2 (2M bodies: 64 MB in, about 3.5 GB "
+                   "on the device); the GPU arm also writes 256 MiB before every timed step")}
 
 
 def cpu_group_ms(pos, mass, use_ref):
@@ -163,6 +180,9 @@ def cpu_tree_ms(pos, mass):
 
 
 def run_reference(args):
+    """The reference's CPU group solver on the host cores: its own sources
+    built by oracle/Makefile.ref where they are present, else the oracle's
+    restatement of it (pinned to that build bit for bit)."""
     rank, _, world = dist_info()
     if rank != 0:
         return
@@ -171,7 +191,8 @@ def run_reference(args):
     use_ref = native.have_ref()
     impl = native.Ref() if use_ref else native.Oracle()
     pos, _, mass = galaxy(args.n)
-    for _ in range(min(args.warmup, 1)):
+    warm = warmup_steps(args)
+    for _ in range(warm):
         impl.group_force(pos, mass, pack=False, **SOLVER)
     times, budget, t_start = [], 150.0, time.perf_counter()
     for k in range(args.steps):
@@ -183,15 +204,14 @@ def run_reference(args):
     ms = statistics.mean(times)
     cores = os.cpu_count()
     kind = "reference" if use_ref else "port"
-    sample = (f"{len(times)} full force evaluations at N={args.n} "
-              f"(warm-up {min(args.warmup, 1)}), group solver unpacked (the reference's CPU "
-              f"default), OpenMP over {cores} threads")
+    sample = (f"{len(times)} full force evaluations at N={args.n} after {warm} warm-up, group "
+              f"solver unpacked (the reference's CPU default), OpenMP over {cores} threads")
     line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms",
-            "n_gpus": world, "steps": len(times), "warmup": min(args.warmup, 1),
+            "n_gpus": world, "steps": len(times), "warmup": warm,
             "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 tree+lists, f32 evaluation",
+            "vs_baseline": None, "dtype": "f64 tree+walk, f32 evaluation",
             "data": "synthetic (Hernquist galaxy, seed 1)",
-            "config": {"workload": WORKLOAD, "n": args.n, "parallelism": "openmp host"},
+            "config": bench_config(args.n), "parallelism": "openmp host",
             "breakdown_ms": {"tree": tm["tree"] * 1e3, "lists": tm["lists"] * 1e3,
                              "evaluate": tm["evaluate"] * 1e3},
             "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": cores, "kind": kind,
@@ -292,7 +312,7 @@ def main():
                                    dpot.data_ptr(), pack=True, criterion=gtc.CRITERION_LEARNED,
                                    alpha=float(info["alpha"]), **SOLVER)
 
-    for _ in range(max(3, args.warmup)):
+    for _ in range(warmup_steps(args)):
         step()
     if world > 1:
         torch.distributed.barrier()
@@ -404,11 +424,10 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": "ms", "n_gpus": world,
-            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 4),
+            "steps": args.steps, "warmup": warmup_steps(args), "ms_per_step": round(ms, 4),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 tree+walk, f32 evaluation", "data": "synthetic (Hernquist galaxy, seed 1)",
-            "config": {"workload": WORKLOAD, "n": n, "parallelism": "replicas" if world > 1 else "1 gpu",
-                       "l2": "256 MiB flush before every timed step; working set > L2"},
+            "config": bench_config(n), "parallelism": "replicas" if world > 1 else "1 gpu",
             "breakdown_ms": {"tree": round(mean("tree_ms"), 4), "lists": round(mean("lists_ms"), 4),
                              "evaluate": round(mean("evaluate_ms"), 4),
                              "evaluate_kernel": round(kernel_ms, 4)},

@@ -5,6 +5,8 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <numeric>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -585,6 +587,14 @@ gtc_status ensemble_guarded(gtc_ensemble *e, F &&f) {
 }  // namespace
 
 extern "C" {
+
+void gtc_sample_indices(uint64_t n, uint64_t m, uint64_t seed, uint64_t *out) {
+  std::vector<std::size_t> s(n);
+  std::iota(s.begin(), s.end(), std::size_t{0});
+  std::mt19937_64 engine(seed);
+  std::shuffle(s.begin(), s.end(), engine);
+  for (uint64_t k = 0; k < std::min(m, n); ++k) out[k] = s[k];
+}
 
 const char *gtc_status_name(gtc_status s) {
   switch (s) {

@@ -15,7 +15,6 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 LIB_PATH = HERE / "libgtc.so"
-ICS_PATH = HERE / "libgtc_ics.so"
 
 GTC_OK, GTC_INVALID_ARGUMENT, GTC_RUNTIME_ERROR, GTC_NO_DEVICE, GTC_OUT_OF_MEMORY = range(5)
 CRITERION_THETA, CRITERION_LEARNED = 0, 1
@@ -101,6 +100,7 @@ def _load():
         "gtc_direct_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
+        "gtc_sample_indices": (None, [U64, U64, U64, P]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
         "gtc_set_option": (I, [V, C.c_char_p, D]),
         "gtc_learned_add_samples": (I, [V, P, P, U64, C.POINTER(GravityParams), D, D, U64, U32,
@@ -406,98 +406,18 @@ class Context:
                     cell_list=cl, body_list=bl, out=out)
 
 
-# ---- synthetic galaxies (host/galaxy.h, libgtc_ics.so) ----------------------
+# ---- inputs ------------------------------------------------------------------
 
-class GalaxyModel(C.Structure):
-    _fields_ = [("G", C.c_double), ("disk_n", C.c_uint64), ("bulge_n", C.c_uint64),
-                ("halo_n", C.c_uint64), ("disk_mass", C.c_double), ("disk_h", C.c_double),
-                ("disk_z0", C.c_double), ("disk_rmax", C.c_double), ("disk_Q", C.c_double),
-                ("disk_Q_radius", C.c_double), ("bulge_mass", C.c_double),
-                ("bulge_a", C.c_double), ("bulge_rmax", C.c_double), ("halo_mass", C.c_double),
-                ("halo_core", C.c_double), ("halo_cutoff", C.c_double),
-                ("halo_rmax", C.c_double), ("vesc_fraction", C.c_double), ("seed", C.c_uint64)]
-
-
-_ics = None
-
-
-def _ics_lib():
-    global _ics
-    if _ics is None:
-        if not ICS_PATH.exists():
-            raise ImportError(f"{ICS_PATH} is not built (make -C galactic-tides_gb300)")
-        _ics = C.CDLL(str(ICS_PATH))
-        _ics.gtc_galaxy_default.restype = None
-        _ics.gtc_galaxy_default.argtypes = [C.POINTER(GalaxyModel), C.c_uint64, C.c_uint64]
-        _ics.gtc_make_galaxy.restype = C.c_int
-        _ics.gtc_make_galaxy.argtypes = [C.POINTER(GalaxyModel)] + [C.c_void_p] * 4
-        _ics.gtc_orient.restype = None
-        _ics.gtc_orient.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_double, C.c_double]
-        _ics.gtc_parabolic_orbit.restype = C.c_int
-        _ics.gtc_parabolic_orbit.argtypes = [C.c_double] * 5 + [C.c_void_p, C.c_void_p]
-        _ics.gtc_make_encounter.restype = C.c_int
-        _ics.gtc_make_encounter.argtypes = [C.POINTER(GalaxyModel)] + [C.c_double] * 6 + \
-            [C.c_void_p] * 4
-        _ics.gtc_sample_indices.restype = None
-        _ics.gtc_sample_indices.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p]
-    return _ics
-
-
-def galaxy_model(n, seed=1, **fields):
-    """The benchmark galaxy model for n particles; keyword fields override."""
-    m = GalaxyModel()
-    _ics_lib().gtc_galaxy_default(C.byref(m), n, seed)
-    for k, v in fields.items():
-        setattr(m, k, v)
-    return m
-
-
-def make_galaxy(n=None, seed=1, model=None, **fields):
-    """-> pos (n,3), vel (n,3), mass (n,), type (n,) of a Hernquist galaxy."""
-    m = model if model is not None else galaxy_model(n, seed, **fields)
-    tot = m.disk_n + m.bulge_n + m.halo_n
-    pos = np.empty((tot, 3))
-    vel = np.empty((tot, 3))
-    mass = np.empty(tot)
-    typ = np.empty(tot, np.int32)
-    if _ics_lib().gtc_make_galaxy(C.byref(m), _ptr(pos), _ptr(vel), _ptr(mass), _ptr(typ)):
-        raise ValueError("invalid galaxy model")
-    return pos, vel, mass, typ
+# the synthetic galaxies live in galaxy.py (pure numpy); re-exported here
+from .galaxy import (GalaxyModel, galaxy_model, make_encounter, make_galaxy,  # noqa: E402,F401
+                     orient, parabolic_orbit)
 
 
 def sample_indices(n, m=4096, seed=1):
     """The reference bench's accuracy sample: mt19937_64(seed) shuffle, first m."""
     out = np.empty(min(n, m), np.uint64)
-    _ics_lib().gtc_sample_indices(n, m, seed, _ptr(out))
+    lib.gtc_sample_indices(n, m, seed, _ptr(out))
     return out
-
-
-def orient(pos, vel, incl_deg, omega_deg=0.0):
-    """Rotates (in place) by incl_deg about x, then omega_deg about z."""
-    assert pos.flags.c_contiguous and vel.flags.c_contiguous
-    _ics_lib().gtc_orient(_ptr(pos), _ptr(vel), pos.shape[0], incl_deg, omega_deg)
-
-
-def parabolic_orbit(G, m1, m2, rp, r0):
-    """-> (dx, dv): relative position and velocity of the parabolic orbit."""
-    dx, dv = np.empty(3), np.empty(3)
-    if _ics_lib().gtc_parabolic_orbit(G, m1, m2, rp, r0, _ptr(dx), _ptr(dv)):
-        raise ValueError("parabolic_orbit: start separation below pericentre")
-    return dx, dv
-
-
-def make_encounter(n_each, seed=1, incl1=30.0, incl2=60.0, rp=2.0, r0=15.0, omega1=0.0,
-                   omega2=0.0, **fields):
-    """Two galaxies of n_each particles (seeds seed, seed + 1) on a parabolic
-    orbit, centre of mass at rest: -> pos, vel, mass, type (2 n_each)."""
-    m = galaxy_model(n_each, seed, **fields)
-    tot = 2 * (m.disk_n + m.bulge_n + m.halo_n)
-    pos, vel = np.empty((tot, 3)), np.empty((tot, 3))
-    mass, typ = np.empty(tot), np.empty(tot, np.int32)
-    if _ics_lib().gtc_make_encounter(C.byref(m), incl1, omega1, incl2, omega2, rp, r0, _ptr(pos),
-                                     _ptr(vel), _ptr(mass), _ptr(typ)):
-        raise ValueError("invalid encounter")
-    return pos, vel, mass, typ
 
 
 class _Borrowed(Context):

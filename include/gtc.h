@@ -209,6 +209,12 @@ gtc_status gtc_direct_fp64_noalloc(const double *pos, const double *mass, uint64
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
 
+/* The accuracy sample of the reference bench (apps/galactic_tides_bench.cpp:
+ * 75-79): the indices 0..n-1 in the order std::shuffle leaves them with a
+ * std::mt19937_64(seed) engine, the first min(m, n) copied to out. Host only,
+ * needs no device. */
+void gtc_sample_indices(uint64_t n, uint64_t m, uint64_t seed, uint64_t *out);
+
 /* ---- time integration (src/integrator.cpp) ----------------------------- */
 
 /* Diagnostics (integrator.h:46-58): potential = 0.5 sum m phi, total =

@@ -44,11 +44,6 @@ def gtc():
 
 
 @pytest.fixture(scope="session")
-def gtc_ics(gtc):
-    return gtc
-
-
-@pytest.fixture(scope="session")
 def ctx(gtc):
     c = gtc.Context(0)
     yield c
