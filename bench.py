@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-criterion measurement")
+    ap.add_argument("--no-200k", action="store_true",
+                    help="skip the N = 200k group and direct lines")
     ap.add_argument("--only-steps", action="store_true",
                     help="warm-up and timed steps only (for profiler launch lists)")
     ap.add_argument("--learned-steps", action="store_true",
@@ -219,6 +221,166 @@ def run_reference(args):
             "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# Algorithmic bytes of the build's stages: what each must read and write once
+# (B per body, B per node); the sort's come from its pass count.
+KEYS_B_BODY = 24 + 24 + 13          # box: pos; keys: pos in, key + index + tiny flag out
+SORT_B_BODY_PASS = 24               # key and index in and out per 8-bit pass
+TOPO_B_BODY, TOPO_B_NODE = 118, 88  # levels, node count + scan, nodes, leaf and tree order
+MOM_B_BODY, MOM_B_NODE = 32, 417    # leaf bodies in; moments out, node records packed
+PACK_B_BODY = 48                    # FP32 bodies from the tree-order copies
+
+
+def timed_events(step, flush, stream, reps):
+    """Mean CUDA-event time of step() over reps calls on `stream`, L2
+    flushed before each."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / reps
+
+
+def measure_stages(ctx, step, flush, stream, n, hbm_gbs, reps=5):
+    """Per-stage device times of the plain solver (CUDA events at the stage
+    boundaries, context option stage_events) and their HBM rates: algorithmic
+    bytes / time, against the measured copy bandwidth."""
+    import torch
+    ctx.set_option("stage_events", 1)
+    acc = []
+    with torch.cuda.stream(stream):
+        for _ in range(reps):
+            flush.zero_()
+            step()
+            acc.append((ctx.stage_times(), ctx.stats()))
+    ctx.set_option("stage_events", 0)
+    tm = {k: statistics.mean(a[k] for a, _ in acc) for k in acc[0][0] if k != "sort_passes"}
+    passes = acc[-1][0]["sort_passes"]
+    st = acc[-1][1]
+    m, g = st["n_nodes"], st["n_groups"]
+    entries = st["n_cell_list"] + st["n_body_list"]
+    b_keys = KEYS_B_BODY * n
+    b_sort = SORT_B_BODY_PASS * passes * n
+    b_topo = TOPO_B_BODY * n + TOPO_B_NODE * m
+    b_mom = MOM_B_BODY * n + MOM_B_NODE * m
+    b_build = b_keys + b_sort + b_topo + b_mom + PACK_B_BODY * n
+    # the walk: node records read once, group boxes and ranges read, lists and
+    # group records written; `requested` counts every record test's 48 B
+    b_walk = 48 * m + 40 * g + 4 * entries + 64 * g
+
+    def rate(b, ms):
+        if ms is None or ms <= 0:
+            return None
+        gbs = b / (ms * 1e-3) / 1e9
+        return {"bytes": int(b), "ms": round(ms, 4), "gbs": round(gbs, 1),
+                "frac": round(gbs / hbm_gbs, 4)}
+
+    return {"note": ("algorithmic bytes (each stage's inputs read and outputs written once) / "
+                     "CUDA-event stage time, against the measured copy bandwidth; mean of "
+                     f"{reps} solves after the timed steps, L2 flushed before each"),
+            "hbm_peak_gbs": hbm_gbs, "sort_passes": passes,
+            "keys": rate(b_keys, tm["keys_ms"]), "radix_sort": rate(b_sort, tm["sort_ms"]),
+            "topology": rate(b_topo, tm["topology_ms"]), "moments": rate(b_mom, tm["moments_ms"]),
+            "tree_build": rate(b_build, tm["build_ms"]), "walk": rate(b_walk, tm["walk_ms"]),
+            "walk_record_bytes_requested": 48 * st["walk_nodes"],
+            "walk_requested_gbs": (round(48 * st["walk_nodes"] / (tm["walk_ms"] * 1e-3) / 1e9, 1)
+                                   if tm["walk_ms"] > 0 else None)}
+
+
+def sm_count(device):
+    import torch
+    return torch.cuda.get_device_properties(device).multi_processor_count
+
+
+def measure_200k(gtc, device, flush, sample, peak_fp32, sm_mhz, steps=10):
+    """The same galaxy model at N = 200k (the size of the reference's only
+    published GPU figures): the plain group solver (ms, breakdown, p99
+    against FP64 direct on the bench sample) and the tiled FP32 direct
+    kernel (ms, FP32 rate against this GPU's measured FMA peak and against
+    the spec bound SMs x 128 FMA/clk x the sampled SM clock)."""
+    import torch
+    n = 200_000
+    pos, _, mass = galaxy(n)
+    dev = torch.device("cuda", device)
+    dpos = torch.from_numpy(pos).to(dev)
+    dmass = torch.from_numpy(mass).to(dev)
+    dacc = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    dpot = torch.empty(n, dtype=torch.float64, device=dev)
+    c = gtc.Context(device)
+    stream = torch.cuda.ExternalStream(c.stream, device=dev)
+    torch.cuda.synchronize()
+
+    def group():
+        c.group_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                             dpot.data_ptr(), pack=True, **SOLVER)
+
+    for _ in range(3):
+        group()
+    torch.cuda.synchronize()
+    stats = []
+
+    def group_stats():
+        group()
+        stats.append(c.stats())
+
+    g_ms = timed_events(group_stats, flush, stream, steps)
+    mean = lambda key: statistics.mean(s[key] for s in stats)
+    st = stats[-1]
+    idx = gtc.sample_indices(n, sample, 1)
+    didx = torch.from_numpy(idx.astype(np.int64)).to(dev)
+    racc = torch.empty((len(idx), 3), dtype=torch.float64, device=dev)
+    rpot = torch.empty(len(idx), dtype=torch.float64, device=dev)
+    c.direct_fp64_device(dpos.data_ptr(), dmass.data_ptr(), n, didx.data_ptr(), len(idx),
+                         racc.data_ptr(), rpot.data_ptr(), G=SOLVER["G"], eps=SOLVER["eps"])
+    torch.cuda.synchronize()
+    ref = racc.cpu().numpy()
+    got = dacc.cpu().numpy()[idx.astype(np.int64)]
+    err = np.sort(np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1))
+    group_line = {"ms": round(g_ms, 4),
+                  "breakdown_ms": {"tree": round(mean("tree_ms"), 4),
+                                   "lists": round(mean("lists_ms"), 4),
+                                   "evaluate": round(mean("evaluate_ms"), 4)},
+                  "interactions_per_particle": (st["cell_interactions"]
+                                                + st["body_interactions"]) / n,
+                  "p99": float(err[len(err) * 99 // 100]), "sample": len(idx),
+                  "reference_published": {"group_ms": 16.0, "split_ms": [3.7, 5.6, 6.6],
+                                          "hardware": "Apple M4 Max (Metal), README.md:65-70",
+                                          "note": "unavailable on this box; context only"}}
+
+    def direct():
+        c.direct_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                              dpot.data_ptr(), **SOLVER)
+
+    direct()
+    torch.cuda.synchronize()
+    dstats = []
+
+    def direct_stats():
+        direct()
+        dstats.append(c.stats())
+
+    d_ms = timed_events(direct_stats, flush, stream, 5)
+    k_ms = statistics.mean(s["eval_kernel_ms"] for s in dstats)
+    flops = FLOPS_BODY * n * (n - 1)
+    tflops = flops / (k_ms * 1e-3) / 1e12
+    spec = (sm_count(device) * 256 * sm_mhz * 1e6 / 1e12) if sm_mhz else None
+    c.close()
+    direct_line = {"ms": round(d_ms, 4), "kernel_ms": round(k_ms, 4),
+                   "flops_per_launch": flops, "achieved_tflops": round(tflops, 2),
+                   "frac_of_measured_fp32": round(tflops / peak_fp32, 4),
+                   "spec_fp32_tflops": round(spec, 2) if spec else None,
+                   "frac_of_spec": round(tflops / spec, 4) if spec else None,
+                   "reference_published": {"direct_ms": 122.0,
+                                           "hardware": "Apple M4 Max (Metal), README.md:66",
+                                           "note": "unavailable on this box; context only"}}
+    return group_line, direct_line
 
 
 def measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, ref, plain_ms,
@@ -393,6 +555,12 @@ def main():
         learned = measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, ref,
                                   ms, local_rank)
     peak_fp32 = ctx.fp32_peak_tflops()
+    peaks, peak_src = read_peaks()
+    stages = measure_stages(ctx, step, flush, stream, n, peaks.get("hbm_gbs", 6800.0))
+    n200k = direct200k = None
+    if not args.no_200k:
+        n200k, direct200k = measure_200k(gtc, local_rank, flush, args.sample, peak_fp32,
+                                         clocks.get("sm_mhz"))
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     traffic = None
     tf = ROOT / "profiles" / "evaluate_traffic.json"
@@ -402,7 +570,6 @@ def main():
             traffic = float(t["dram_bytes_per_launch"]) * n / float(t["n"])
         except Exception:
             traffic = None
-    peaks, peak_src = read_peaks()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -448,7 +615,14 @@ def main():
                                         "kernel on every SM (no FP32 figure in MEASURED_PEAKS.json)",
                          "flops_per_launch": flops},
             "peaks": {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
-                      "source": peak_src},
+                      "source": peak_src, "fp32_measured_tflops": round(peak_fp32, 3),
+                      "fp32_spec_tflops": (round(sm_count(local_rank) * 256 * clocks["sm_mhz"]
+                                                 * 1e6 / 1e12, 2) if clocks.get("sm_mhz") else None),
+                      "fp32_spec_note": "SMs x 128 FMA/clk x 2 flops x the median SM clock sampled "
+                                        "during the timed steps"},
+            "stages": stages,
+            "n200k_group": n200k,
+            "n200k_direct": direct200k,
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,

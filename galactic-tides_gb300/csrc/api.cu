@@ -77,6 +77,17 @@ void Workspace::release_all() {
   side = nullptr;
   side_fork = side_done = nullptr;
   side_pending = false;
+  for (cudaEvent_t &e : stage_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+}
+
+void Workspace::stage(int k, cudaStream_t s) {
+  if (!stage_on) return;
+  if (!stage_ev[k]) GTC_CUDA(cudaEventCreate(&stage_ev[k]));
+  GTC_CUDA(cudaEventRecord(stage_ev[k], s));
+  stage_hit[k] = true;
 }
 
 }  // namespace gtc
@@ -154,6 +165,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   // bodies; otherwise the theta walk runs (the fallback).
   const bool learned = sp.criterion == GTC_CRITERION_LEARNED && ctx->have_model &&
                        ctx->prev_n == n;
+  for (bool &h : ws.stage_hit) h = false;
   GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
   const gtc::SideJoin side_join{ws, s};
   gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
@@ -885,6 +897,9 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
     } else if (key == "graph_headroom") {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;
+    } else if (key == "stage_events") {
+      if (value != 0 && value != 1) throw gtc::InvalidArgument("stage_events must be 0 or 1");
+      ctx->ws.stage_on = value != 0;
     } else {
       throw gtc::InvalidArgument("unknown option '" + key + "'");
     }
@@ -1265,6 +1280,26 @@ gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out) {
   if (!ctx || !out) return GTC_INVALID_ARGUMENT;
   *out = ctx->stats;
   return GTC_OK;
+}
+
+gtc_status gtc_get_stage_times(gtc_context *ctx, gtc_stage_times *out) {
+  return guarded(ctx, [&] {
+    if (!out) throw gtc::InvalidArgument("out is required");
+    const gtc::Workspace &ws = ctx->ws;
+    auto span = [&](int a, int b) -> double {
+      if (!ws.stage_hit[a] || !ws.stage_hit[b]) return -1.0;
+      return elapsed(ws.stage_ev[a], ws.stage_ev[b]);
+    };
+    using W = gtc::Workspace;
+    *out = gtc_stage_times{};
+    out->build_ms = span(W::kStBuild, W::kStMom1);
+    out->keys_ms = span(W::kStBuild, W::kStSort0);
+    out->sort_ms = span(W::kStSort0, W::kStSort1);
+    out->topology_ms = span(W::kStSort1, W::kStTopo);
+    out->moments_ms = span(W::kStMom0, W::kStMom1);
+    out->walk_ms = span(W::kStWalk0, W::kStWalk1);
+    out->sort_passes = static_cast<uint32_t>(ws.sort_passes);
+  });
 }
 
 gtc_status gtc_group_sizes(const gtc_context *ctx, uint64_t *n_bodies, uint64_t *n_nodes,

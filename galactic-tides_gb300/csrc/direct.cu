@@ -157,6 +157,26 @@ void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, 
   GTC_LAUNCH_CHECK();
 }
 
+Fp64SamplePlan plan_fp64_sample(u64 n, u64 m, int sms, u64 max_pairs) {
+  const u64 tb = (m + kST - 1) / kST;
+  u64 slices = std::max<u64>(1, (8ull * static_cast<u64>(sms) + tb - 1) / tb);
+  slices = std::min<u64>(slices, std::max<u64>(1, n / kST));
+  slices = std::min<u64>(slices, std::max<u64>(1, max_pairs / std::max<u64>(1, m)));
+  const u64 slice = std::max<u64>(1, (n + slices - 1) / slices);
+  return {std::max<u64>(1, (n + slice - 1) / slice), slice};
+}
+
+void launch_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
+                        double G, double eps, const Fp64SamplePlan &plan, double2 *part,
+                        double *acc, double *pot, cudaStream_t s) {
+  dim3 grid(ceil_div(m, kST), static_cast<u32>(plan.slices));
+  k_direct64<<<grid, kST, 0, s>>>(pos, mass, n, idx, m, plan.slice, G, eps * eps, part);
+  GTC_LAUNCH_CHECK();
+  k_direct64_sum<<<ceil_div(m, 256), 256, 0, s>>>(part, m, static_cast<u32>(plan.slices), acc,
+                                                  pot);
+  GTC_LAUNCH_CHECK();
+}
+
 void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
                         double G, double eps, double *acc, double *pot, DeviceBuffer &scratch,
                         cudaStream_t s) {
@@ -164,20 +184,9 @@ void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 
   int dev = 0, sms = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const u32 tb = ceil_div(m, kST);
-  // enough source slices for ~8 blocks per SM, each slice at least one tile
-  u64 slices = std::max<u64>(1, (8ull * sms + tb - 1) / tb);
-  slices = std::min<u64>(slices, std::max<u64>(1, n / kST));
-  const u64 slice = (n + slices - 1) / slices;
-  slices = (n + slice - 1) / slice;
-  scratch.ensure(slices * m * 2 * sizeof(double2));
-  dim3 grid(tb, static_cast<u32>(slices));
-  k_direct64<<<grid, kST, 0, s>>>(pos, mass, n, idx, m, slice, G, eps * eps,
-                                  scratch.as<double2>());
-  GTC_LAUNCH_CHECK();
-  k_direct64_sum<<<ceil_div(m, 256), 256, 0, s>>>(scratch.as<double2>(), m,
-                                                  static_cast<u32>(slices), acc, pot);
-  GTC_LAUNCH_CHECK();
+  const Fp64SamplePlan plan = plan_fp64_sample(n, m, sms, ~0ull);
+  scratch.ensure(plan.slices * m * 2 * sizeof(double2));
+  launch_fp64_sample(pos, mass, n, idx, m, G, eps, plan, scratch.as<double2>(), acc, pot, s);
 }
 
 }  // namespace gtc

@@ -681,9 +681,11 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
   join_side(ws, s);  // the walk reads the node records (and the tolerances the root's mass)
+  ws.stage(Workspace::kStWalk0, s);
   if (lw) {
     learned_group_tolerances(ws, *lw, ng, s);
     learned_build_lists(ws, *lw, ng, host, s);
+    ws.stage(Workspace::kStWalk1, s);
     return;
   }
 
@@ -743,6 +745,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     k_split_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, so, spill_c, spill_b,
                                       ws.groups.as<uint4>(), sc);
     GTC_LAUNCH_CHECK();
+    ws.stage(Workspace::kStWalk1, s);
     read_scalars(ws, host, s);
     size_slots(ws, *host, true);
     if (!host->list_overflow) {
@@ -787,6 +790,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   wo.body_list = ws.body_list.as<u32>();
   k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
   GTC_LAUNCH_CHECK();
+  ws.stage(Workspace::kStWalk1, s);
   ws.list_passes = 2;
 }
 

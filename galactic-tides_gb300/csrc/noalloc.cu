@@ -10,20 +10,30 @@
 //     device and stall the caller's pipeline.
 // For them, this file keeps the partial sums in one fixed device array,
 // g_partials (8 MiB, held by every GPU that loads libgtc.so until the
-// process exits), and takes the caller's stream. It allocates nothing.
+// process exits), and takes the caller's stream. It allocates nothing. The
+// kernels are the context path's own (launch_fp64_sample, direct.cu); only
+// where the partial sums live differs, and how many source slices fit.
 //
-// Set-up: the first call on a device looks up the array's device address
-// with cudaGetSymbolAddress, once per device, with that device current.
-// (In host code the array's name is only a host-side stand-in, not a device
-// address.) Make that first call before any stream capture.
+// Set-up: in host code the array's name is only a host-side stand-in, not a
+// device address. The first call in a CUDA context (normally a device's
+// primary context) looks its device address up with cudaGetSymbolAddress,
+// with that context current, and keeps it under the context's unique id
+// (cuCtxGetId). A new context -- after cudaDeviceReset, or a driver-API
+// context the caller made current -- has a new id and gets its own look-up,
+// so a stale address is never used. Make the first call in a context before
+// any stream capture.
 //
 // Every call shares the one array and it keeps the last call's contents.
 // Nothing needs clearing: each call writes every slot before reading it.
 // Calls that overlap on the GPU (for example on two streams) race on the
 // array and must be ordered by the caller.
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "../../include/gtc.h"
 #include "pipeline.cuh"
@@ -31,100 +41,60 @@
 namespace gtc {
 namespace {
 
-constexpr u64 kPartialBytes = 8ull << 20;                  // 8 MiB
-constexpr u64 kMaxSlots = kPartialBytes / (2 * sizeof(double2));  // (slice, target) pairs
-constexpr int kMaxDevices = 64;
-constexpr int kST = 128;                                   // sample targets per block
+constexpr u64 kPartialBytes = 8ull << 20;                          // 8 MiB
+constexpr u64 kMaxPairs = kPartialBytes / (2 * sizeof(double2));  // (slice, target) pairs
 
-static __device__ __align__(256) double2 g_partials[kMaxSlots * 2];
+static __device__ __align__(256) double2 g_partials[kMaxPairs * 2];
 
 std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
+std::unordered_map<unsigned long long, void *> g_addr;  // context id -> address
+PFN_cuCtxGetCurrent_v4000 g_get_current = nullptr;
+PFN_cuCtxGetId_v12000 g_get_id = nullptr;
 
-struct Body64 {
-  double x, y, z, m;
-};
-
-__device__ __forceinline__ u64 min_u64(u64 a, u64 b) { return a < b ? a : b; }
-
-// Partial sums of targets idx[blockIdx.x*kST + t] over source slice
-// blockIdx.y, written to part[slice][target] (two double2 per slot).
-__global__ void __launch_bounds__(kST)
-    k_sample_partials(const double *__restrict__ pos, const double *__restrict__ mass, u64 n,
-                      const u64 *__restrict__ idx, u64 m, u64 slice, double G, double eps2,
-                      double2 *part) {
-  __shared__ Body64 tile[kST];
-  const u64 s = static_cast<u64>(blockIdx.x) * kST + threadIdx.x;
-  const bool active = s < m;
-  const u64 i = active ? idx[s] : ~0ull;
-  double px = 0, py = 0, pz = 0;
-  if (active) {
-    px = pos[3 * i];
-    py = pos[3 * i + 1];
-    pz = pos[3 * i + 2];
+// Unique id of the CUDA context current on this thread; false when none is.
+bool current_context_id(unsigned long long *id) {
+  if (!g_get_current || !g_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    GTC_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault,
+                                              &q1));
+    GTC_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      throw RuntimeError("cuda: the driver offers no cuCtxGetCurrent / cuCtxGetId");
+    g_get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f1);
+    g_get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f2);
   }
-  double ax = 0, ay = 0, az = 0, phi = 0;
-  const u64 j0 = static_cast<u64>(blockIdx.y) * slice;
-  const u64 j1 = min_u64(n, j0 + slice);
-  for (u64 base = j0; base < j1; base += kST) {
-    const u64 j = base + threadIdx.x;
-    tile[threadIdx.x] = j < j1 ? Body64{pos[3 * j], pos[3 * j + 1], pos[3 * j + 2], mass[j]}
-                               : Body64{0, 0, 0, 0};
-    __syncthreads();
-    const u64 cnt = min_u64(kST, j1 - base);
-    for (u64 k = 0; k < cnt; ++k) {
-      if (base + k == i) continue;
-      const Body64 b = tile[k];
-      const double dx = px - b.x, dy = py - b.y, dz = pz - b.z;
-      const double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
-      const double gm = G * b.m * inv;
-      const double gm3 = gm * inv * inv;
-      ax -= gm3 * dx;
-      ay -= gm3 * dy;
-      az -= gm3 * dz;
-      phi -= gm;
-    }
-    __syncthreads();
-  }
-  if (active) {
-    double2 *o = part + 2 * (static_cast<u64>(blockIdx.y) * m + s);
-    o[0] = make_double2(ax, ay);
-    o[1] = make_double2(az, phi);
-  }
+  CUcontext c = nullptr;
+  if (g_get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return g_get_id(c, id) == CUDA_SUCCESS;
 }
 
-// Sums the slices of every target in slice order (deterministic).
-__global__ void k_sample_sum(const double2 *part, u64 m, u32 slices, double *acc, double *pot) {
-  const u64 s = static_cast<u64>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (s >= m) return;
-  double ax = 0, ay = 0, az = 0, phi = 0;
-  for (u32 k = 0; k < slices; ++k) {
-    const double2 *v = part + 2 * (static_cast<u64>(k) * m + s);
-    ax += v[0].x;
-    ay += v[0].y;
-    az += v[1].x;
-    phi += v[1].y;
+void *lookup_partials() {
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_partials);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw RuntimeError(std::string("cuda: cannot locate the fixed scratch array: ") +
+                       cudaGetErrorString(e));
   }
-  acc[3 * s] = ax;
-  acc[3 * s + 1] = ay;
-  acc[3 * s + 2] = az;
-  pot[s] = phi;
+  return p;
 }
 
-// Device address of g_partials on the current device, looked up once.
-void *partials_address(int dev) {
+// Device address of g_partials in the current context, looked up once per
+// context. On a thread with no context current yet, the look-up itself
+// makes the device's primary context current.
+double2 *partials_address() {
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_partials);
-    if (e != cudaSuccess) {
-      (void)cudaGetLastError();
-      throw RuntimeError(std::string("cuda: cannot locate the fixed scratch array: ") +
-                         cudaGetErrorString(e));
-    }
-    g_addr[dev] = p;
+  unsigned long long id = 0;
+  if (!current_context_id(&id)) {
+    void *p = lookup_partials();
+    if (!current_context_id(&id)) throw RuntimeError("cuda: no current context");
+    g_addr[id] = p;
+    return static_cast<double2 *>(p);
   }
-  return g_addr[dev];
+  auto it = g_addr.find(id);
+  if (it == g_addr.end()) it = g_addr.emplace(id, lookup_partials()).first;
+  return static_cast<double2 *>(it->second);
 }
 
 }  // namespace
@@ -141,30 +111,23 @@ gtc_status gtc_direct_fp64_noalloc(const double *pos, const double *mass, uint64
     if (!pos || !mass || !idx || !acc || !pot)
       throw InvalidArgument("pos, mass, idx, acc and pot are required");
     if (n == 0) throw InvalidArgument("no bodies to sum over (n = 0)");
-    if (m > kMaxSlots)
-      throw InvalidArgument("gtc_direct_fp64_noalloc: at most " + std::to_string(kMaxSlots) +
+    if (m > kMaxPairs)
+      throw InvalidArgument("gtc_direct_fp64_noalloc: at most " + std::to_string(kMaxPairs) +
                             " sample targets (fixed 8 MiB scratch), got " + std::to_string(m));
+    // An error left by the caller's own earlier work stays where it is, for
+    // the caller to find: this call neither reports it as its own nor
+    // clears it.
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+      throw RuntimeError(std::string("cuda: an earlier CUDA error is pending (left in place): ") +
+                         cudaGetErrorName(pending));
     int dev = 0, sms = 0;
     GTC_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) throw InvalidArgument("device index out of range");
     GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    double2 *part = static_cast<double2 *>(partials_address(dev));
-    const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const u32 tb = ceil_div(m, kST);
-    // source slices: ~8 blocks per SM, at least one tile each, and all the
-    // (slice, target) partial sums inside the fixed array
-    u64 slices = (8ull * sms + tb - 1) / tb;
-    if (slices < 1) slices = 1;
-    if (slices > n / kST) slices = n / kST > 0 ? n / kST : 1;
-    if (slices > kMaxSlots / m) slices = kMaxSlots / m;
-    const u64 slice = (n + slices - 1) / slices;
-    slices = n > 0 ? (n + slice - 1) / slice : 1;
-    dim3 grid(tb, static_cast<u32>(slices));
-    k_sample_partials<<<grid, kST, 0, s>>>(pos, mass, n, idx, m, slice > 0 ? slice : 1, G,
-                                           eps * eps, part);
-    GTC_LAUNCH_CHECK();
-    k_sample_sum<<<ceil_div(m, 256), 256, 0, s>>>(part, m, static_cast<u32>(slices), acc, pot);
-    GTC_LAUNCH_CHECK();
+    double2 *part = partials_address();
+    const Fp64SamplePlan plan = plan_fp64_sample(n, m, sms, kMaxPairs);
+    launch_fp64_sample(pos, mass, n, idx, m, G, eps, plan, part, acc, pot,
+                       static_cast<cudaStream_t>(stream));
     return GTC_OK;
   } catch (const InvalidArgument &e) {
     set_contextless_error(e.what());

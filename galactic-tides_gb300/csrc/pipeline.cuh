@@ -102,6 +102,16 @@ struct Workspace {
   cudaStream_t side = nullptr;
   cudaEvent_t side_fork = nullptr, side_done = nullptr;
   bool side_pending = false;
+  // Optional stage events (context option "stage_events"): CUDA events at
+  // the boundaries of the eager build's and walk's stages, for per-stage
+  // device times. Off by default.
+  enum Stage { kStBuild, kStSort0, kStSort1, kStTopo, kStMom0, kStMom1, kStWalk0, kStWalk1,
+               kStages };
+  bool stage_on = false;
+  cudaEvent_t stage_ev[kStages] = {};
+  bool stage_hit[kStages] = {};
+  int sort_passes = 0;  // 8-bit passes of the last build's first sort
+  void stage(int k, cudaStream_t s);
   // Overflow pool behind n_groups slots of `slot` entries: a sixteenth of
   // the slots plus four slots.
   static u64 pool_for(u64 n_groups, u32 slot) { return n_groups * slot / 16 + 4ull * slot; }
@@ -299,6 +309,18 @@ void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, 
 void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
                         double G, double eps, double *acc, double *pot, DeviceBuffer &scratch,
                         cudaStream_t s);
+// The FP64 sample sums in two launches: per-(source slice, target) partial
+// sums into `part` (2 double2 per pair), then each target's slices added in
+// slice order. The plan cuts the n sources into `slices` slices of `slice`
+// bodies: about 8 blocks per SM, at least one tile of bodies per slice, and
+// at most max_pairs (slice, target) pairs.
+struct Fp64SamplePlan {
+  u64 slices, slice;
+};
+Fp64SamplePlan plan_fp64_sample(u64 n, u64 m, int sms, u64 max_pairs);
+void launch_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
+                        double G, double eps, const Fp64SamplePlan &plan, double2 *part,
+                        double *acc, double *pot, cudaStream_t s);
 // float4 bodies relative to the bounding-box centre (gravity_backends.cpp:15-23, :62).
 void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 n,
                       cudaStream_t s);

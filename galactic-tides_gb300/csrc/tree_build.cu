@@ -1090,6 +1090,7 @@ namespace {
 int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s) {
   const int passes = levels >= kLevelsPerWord ? 8 : (3 * std::max(levels, 1) + 7) / 8;
   const int low = std::max(0, 3 * kLevelsPerWord - 8 * passes);
+  ws.sort_passes = passes;
   radix_sort_pairs(ws.key0.as<u64>(), ws.idx.as<u32>(), ws.key0_alt.as<u64>(),
                    ws.idx_alt.as<u32>(), n, 3 * kLevelsPerWord - low, ws.radix, s, low);
   return low == 0 ? kLevelsPerWord : (3 * kLevelsPerWord - low) / 3;
@@ -1123,6 +1124,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   Scalars *sc = ws.scalars.as<Scalars>();
   GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
 
+  ws.stage(Workspace::kStBuild, s);
   bbox_root(ws, pos, n, s);
   const TreeRoot *root = ws.root.as<TreeRoot>();
   u64 *key0 = ws.key0.as<u64>();
@@ -1131,7 +1133,9 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   make_keys(ws, pos, n32, s);
   // the levels the last tree needed first; all of them when a leaf lies
   // deeper (sorting the partly sorted pairs again gives the full order)
+  ws.stage(Workspace::kStSort0, s);
   const int sorted = sort_top_levels(ws, n32, ws.sort_levels > 0 ? ws.sort_levels : kLevelsPerWord, s);
+  ws.stage(Workspace::kStSort1, s);
 
   KeyView kv{key0, nullptr, nullptr, 1};
   signed char *lcp_next = ws.lcp.as<signed char>();
@@ -1254,6 +1258,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_LAUNCH_CHECK();
   k_tree_order<<<nb, kT, 0, s>>>(pos, mass, idx, n32, ws.tpos.as<double>(), ws.tmass.as<double>());
   GTC_LAUNCH_CHECK();
+  ws.stage(Workspace::kStTopo, s);
 
   // moments, one depth at a time from the leaves up
   u32 *meta = ws.arrive.as<u32>();  // count[kBuckets], offset[kBuckets], fill[kBuckets]
@@ -1277,6 +1282,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   // it. Bucket sizes are read on the device: leaves (at most m), then each
   // depth's inner nodes from the deepest possible one up.
   cudaStream_t ms = fork_side(ws, s);
+  ws.stage(Workspace::kStMom0, ms);
   k_leaf_moments<<<mb, kT, 0, ms>>>(ma, bucket, meta);
   GTC_LAUNCH_CHECK();
   for (int d = static_cast<int>(host->depth) - 1; d >= 0; --d) {
@@ -1290,6 +1296,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                                   1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
                                   ws.walk64.as<WalkRec64>(), ws.cells.as<float4>());
   GTC_LAUNCH_CHECK();
+  ws.stage(Workspace::kStMom1, ms);
   k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
                                   root_centre(root), ws.bodies.as<float4>());
   GTC_LAUNCH_CHECK();

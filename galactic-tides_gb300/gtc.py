@@ -66,6 +66,12 @@ class Stats(C.Structure):
                 ("walk_nodes", C.c_uint64)]
 
 
+class StageTimes(C.Structure):
+    _fields_ = [("build_ms", C.c_double), ("keys_ms", C.c_double), ("sort_ms", C.c_double),
+                ("topology_ms", C.c_double), ("moments_ms", C.c_double),
+                ("walk_ms", C.c_double), ("sort_passes", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 NODE_DTYPE = np.dtype([
     ("center", "<f8", 3), ("half", "<f8"), ("com", "<f8", 3), ("mass", "<f8"),
     ("quad", "<f8", 6), ("delta", "<f8"), ("begin", "<u4"), ("end", "<u4"), ("skip", "<u4"),
@@ -101,6 +107,7 @@ def _load():
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_sample_indices": (None, [U64, U64, U64, P]),
+        "gtc_get_stage_times": (I, [V, C.POINTER(StageTimes)]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
         "gtc_set_option": (I, [V, C.c_char_p, D]),
         "gtc_learned_add_samples": (I, [V, P, P, U64, C.POINTER(GravityParams), D, D, U64, U32,
@@ -380,6 +387,13 @@ class Context:
         v = C.c_double()
         self._check(lib.gtc_measure_fp32_peak(self.h, C.byref(v)))
         return v.value
+
+    def stage_times(self):
+        """Per-stage device times of the last eager group solve (option
+        stage_events = 1), ms; -1 where a stage was not timed."""
+        st = StageTimes()
+        self._check(lib.gtc_get_stage_times(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in StageTimes._fields_ if k != "reserved"}
 
     def stats(self):
         st = Stats()

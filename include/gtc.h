@@ -198,16 +198,36 @@ gtc_status gtc_direct_fp64_device(gtc_context *ctx, const double *pos, const dou
  * 262144 sample targets (m); larger m is refused (GTC_INVALID_ARGUMENT).
  * idx values must be < n. Enqueued on `stream` (a cudaStream_t, NULL for the
  * legacy default stream) without waiting; the results are ready when the
- * stream reaches that point. The first call on a device looks up the array's
- * address (once per device, on the current device): make it before any
- * stream capture. All calls share the array and it keeps the last call's
- * contents (each call writes every slot it reads, nothing needs clearing);
- * calls that overlap on the GPU race on it. Errors: gtc_last_error(NULL). */
+ * stream reaches that point. The first call in a CUDA context (a device's
+ * primary context, normally) looks up the array's address in that context
+ * and keeps it under the context's unique id, so a reset device or another
+ * context gets a fresh look-up: make that first call before any stream
+ * capture. All calls share the array and it keeps the last call's contents
+ * (each call writes every slot it reads, nothing needs clearing); calls that
+ * overlap on the GPU race on it. A CUDA error already pending from the
+ * caller's own work is left in place and the call fails without launching.
+ * Errors: gtc_last_error(NULL). */
 gtc_status gtc_direct_fp64_noalloc(const double *pos, const double *mass, uint64_t n,
                                    const uint64_t *idx, uint64_t m, double G, double eps,
                                    double *acc, double *pot, void *stream);
 
 gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
+
+/* Device times of the last eager gtc_group_force* call's stages, from CUDA
+ * events recorded when the context option "stage_events" is 1 (-1 for a
+ * stage the call did not time). No reference counterpart: the reference's
+ * Timings (gravity_backends.h:54-58) stop at tree / lists / evaluate. */
+typedef struct gtc_stage_times {
+  double build_ms;     /* tree build start to the end of the moments (side stream) */
+  double keys_ms;      /* bounding box, split table and keys */
+  double sort_ms;      /* the radix sort of the first key word */
+  double topology_ms;  /* levels, node count, nodes, children, leaf and tree order */
+  double moments_ms;   /* FP64 moments and node records (beside the group choice) */
+  double walk_ms;      /* the grouped walk, after the group choice */
+  uint32_t sort_passes; /* 8-bit passes of that sort */
+  uint32_t reserved;
+} gtc_stage_times;
+gtc_status gtc_get_stage_times(gtc_context *ctx, gtc_stage_times *out);
 
 /* The accuracy sample of the reference bench (apps/galactic_tides_bench.cpp:
  * 75-79): the indices 0..n-1 in the order std::shuffle leaves them with a
@@ -302,6 +322,8 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
  *                        back how many pairs the last one deferred (more
  *                        rounds follow one read back each); 1 reads back
  *                        after every round. Results do not depend on it.
+ *   "stage_events"       0 (default) or 1: record CUDA events at the stage
+ *                        boundaries of eager group solves (gtc_get_stage_times).
  *   "graph_headroom"     0..4 (default 0.25): a leapfrog graph is captured
  *                        with buffers this fraction larger than the last
  *                        solve's tree and lists (0: exactly those sizes, so

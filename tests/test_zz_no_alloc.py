@@ -30,11 +30,15 @@ def _system(n, seed):
     return pos, rng.random(n) / n + 0.5 / n
 
 
-def test_noalloc_matches_context_entry_point(gtc):
+@pytest.mark.parametrize("m", [1500, 262144])
+def test_noalloc_matches_context_entry_point(gtc, m):
+    """m = 262144 fills the fixed array with one source slice per target
+    (the most targets it takes); sample indices repeat there."""
     import torch
-    n, m = 20011, 1500
+    n = 20011
     pos, mass = _system(n, 17)
-    idx = np.random.default_rng(5).permutation(n)[:m].astype(np.int64)
+    rng = np.random.default_rng(5)
+    idx = (rng.permutation(n)[:m] if m <= n else rng.integers(0, n, m)).astype(np.int64)
     dev = torch.device("cuda", 0)
     dpos = torch.tensor(pos, device=dev)
     dmass = torch.tensor(mass, device=dev)
