@@ -66,7 +66,7 @@ void Workspace::release_all() {
                          &nend, &skip, &parent, &depth, &nchild, &isleaf, &kids, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
                          &groups, &cell_list, &body_list, &spill, &splitpt, &root, &bbox_part, &scalars, &split, &scan_tmp,
-                         &radix.counts, &radix.scan_tmp};
+                         &direct_part, &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (side) {
     cudaStreamSynchronize(side);
@@ -533,7 +533,7 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
     ws.out.ensure(n * sizeof(float4));
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
     gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), static_cast<float>(sp.G),
-                     static_cast<float>(sp.eps * sp.eps), ws.out.as<float4>(), s);
+                     static_cast<float>(sp.eps * sp.eps), ws.out.as<float4>(), ws.direct_part, s);
   } else {
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
   }
@@ -697,7 +697,7 @@ gtc_status gtc_direct(gtc_context *ctx, const gtc_float4 *bodies, const gtc_kern
     GTC_CUDA(cudaMemcpyAsync(ws.bodies.ptr, bodies, n * 16, cudaMemcpyHostToDevice, s));
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
     gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), p->G, p->eps2,
-                     ws.out.as<float4>(), s);
+                     ws.out.as<float4>(), ws.direct_part, s);
     GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
     GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));

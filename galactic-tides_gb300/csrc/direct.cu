@@ -13,67 +13,119 @@ namespace {
 
 // ------------------------------------------------------------------ FP32
 
-constexpr int kDT = 256;   // threads per block = bodies per shared tile
-constexpr int kDR = 2;     // targets per thread
+constexpr int kDT = 128;          // threads per block = sources per shared tile
+constexpr int kDR = 4;            // targets per thread
+constexpr int kDTB = kDT * kDR;   // targets per block
+constexpr float kFar = 1e15f;     // padding source: far away, zero mass, adds exactly 0
 
-// One softened body-body term, G folded into b.w.
-__device__ __forceinline__ void add_body(const float4 &p, const float4 &b, float eps2, float &ax,
-                                         float &ay, float &az, float &pot) {
-  const float dx = p.x - b.x, dy = p.y - b.y, dz = p.z - b.z;
-  const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
-  const float gm = b.w * inv;
-  const float gm3 = gm * inv * inv;
-  ax = fmaf(-gm3, dx, ax);
-  ay = fmaf(-gm3, dy, ay);
-  az = fmaf(-gm3, dz, az);
-  pot -= gm;
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// Two sources (one in each half of a float2) against one target: FFMA2 /
+// FMUL2 / FADD2 do both at once, the two rsqrts go to the SFU. The source
+// pair is (x0, x1, y0, y1), (z0, z1, Gm0, Gm1); the target's coordinates are
+// negated and doubled (-x, -x). With kMask, `skip` zeroes the half whose
+// source is the target itself (the reference skips j == i), before its
+// singular 1/r can reach the sums.
+template <bool kMask>
+__device__ __forceinline__ void add_pair(const float4 s0, const float4 s1, const float2 nx,
+                                         const float2 ny, const float2 nz, const float2 e2,
+                                         float2 &ax, float2 &ay, float2 &az, float2 &pt,
+                                         bool skip0 = false, bool skip1 = false) {
+  const float2 dx = __fadd2_rn(f2(s0.x, s0.y), nx);  // source - target
+  const float2 dy = __fadd2_rn(f2(s0.z, s0.w), ny);
+  const float2 dz = __fadd2_rn(f2(s1.x, s1.y), nz);
+  const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+  float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+  if (kMask) {
+    inv.x = skip0 ? 0.f : inv.x;
+    inv.y = skip1 ? 0.f : inv.y;
+  }
+  const float2 gm = __fmul2_rn(f2(s1.z, s1.w), inv);
+  const float2 gm3 = __fmul2_rn(gm, __fmul2_rn(inv, inv));
+  ax = __ffma2_rn(gm3, dx, ax);
+  ay = __ffma2_rn(gm3, dy, ay);
+  az = __ffma2_rn(gm3, dz, az);
+  pt = __fadd2_rn(pt, gm);
 }
 
-// Block b owns targets [b*kDT*kDR, (b+1)*kDT*kDR): thread t the targets
-// base + t and base + kDT + t. Bodies stream through shared memory in
-// tiles of kDT, in index order (the reference's summation order); only the
-// tiles holding the block's own targets test j == i.
+// Block (bx, by) owns targets [bx kDTB, (bx + 1) kDTB) -- thread t the
+// targets bx kDTB + r kDT + t -- and sums the sources of slice by,
+// [by len, (by + 1) len), streamed through shared memory in index order,
+// kDT at a time. Even and odd sources go to the two halves of each sum.
+// Only the tiles holding the block's own targets test j == i. With one
+// slice the sums go straight to `out`, otherwise to part[by][target],
+// added up in slice order by k_direct_sum (deterministic).
 __global__ void __launch_bounds__(kDT)
-    k_direct(const float4 *__restrict__ bodies, u32 n, float G, float eps2, float4 *out) {
-  __shared__ float4 tile[kDT];
-  const u32 t0 = blockIdx.x * (kDT * kDR);
+    k_direct(const float4 *__restrict__ bodies, u32 n, u32 len, float G, float eps2,
+             float4 *__restrict__ out) {
+  __shared__ float4 tile[kDT];  // kDT / 2 source pairs, two float4 each
+  const u32 t0 = blockIdx.x * kDTB;
+  const u32 j0 = blockIdx.y * len, j1 = min(n, j0 + len);
+  const float2 e2 = f2(eps2, eps2);
   u32 ti[kDR];
-  float4 p[kDR];
-  float ax[kDR], ay[kDR], az[kDR], pot[kDR];
+  float2 nx[kDR], ny[kDR], nz[kDR], ax[kDR], ay[kDR], az[kDR], pt[kDR];
 #pragma unroll
   for (int r = 0; r < kDR; ++r) {
     ti[r] = t0 + r * kDT + threadIdx.x;
-    p[r] = ti[r] < n ? bodies[ti[r]] : make_float4(0.f, 0.f, 0.f, 0.f);
-    ax[r] = ay[r] = az[r] = pot[r] = 0.f;
+    const float4 p = ti[r] < n ? bodies[ti[r]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    nx[r] = f2(-p.x, -p.x);
+    ny[r] = f2(-p.y, -p.y);
+    nz[r] = f2(-p.z, -p.z);
+    ax[r] = ay[r] = az[r] = pt[r] = f2(0.f, 0.f);
   }
-  for (u32 base = 0; base < n; base += kDT) {
+  float *tf = reinterpret_cast<float *>(tile);
+  const u32 pair = threadIdx.x >> 1, half = threadIdx.x & 1;
+  for (u32 base = j0; base < j1; base += kDT) {
     const u32 j = base + threadIdx.x;
-    float4 b = j < n ? bodies[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-    b.w *= G;
-    tile[threadIdx.x] = b;
+    const float4 b = j < j1 ? bodies[j] : make_float4(kFar, kFar, kFar, 0.f);
+    tf[8 * pair + half] = b.x;
+    tf[8 * pair + 2 + half] = b.y;
+    tf[8 * pair + 4 + half] = b.z;
+    tf[8 * pair + 6 + half] = G * b.w;
     __syncthreads();
-    const u32 cnt = min(static_cast<u32>(kDT), n - base);
-    const bool own = base + kDT > t0 && base < t0 + kDT * kDR;
-    if (!own && cnt == kDT) {
-#pragma unroll 8
-      for (int k = 0; k < kDT; ++k) {
-        const float4 bj = tile[k];
-#pragma unroll
-        for (int r = 0; r < kDR; ++r) add_body(p[r], bj, eps2, ax[r], ay[r], az[r], pot[r]);
-      }
-    } else {
-      for (u32 k = 0; k < cnt; ++k) {
-        const float4 bj = tile[k];
+    const bool own = base < t0 + kDTB && base + kDT > t0;
+    if (!own) {
+#pragma unroll 4
+      for (int q = 0; q < kDT / 2; ++q) {
+        const float4 s0 = tile[2 * q], s1 = tile[2 * q + 1];
 #pragma unroll
         for (int r = 0; r < kDR; ++r)
-          if (base + k != ti[r]) add_body(p[r], bj, eps2, ax[r], ay[r], az[r], pot[r]);
+          add_pair<false>(s0, s1, nx[r], ny[r], nz[r], e2, ax[r], ay[r], az[r], pt[r]);
+      }
+    } else {
+      for (int q = 0; q < kDT / 2; ++q) {
+        const float4 s0 = tile[2 * q], s1 = tile[2 * q + 1];
+        const u32 js = base + 2 * q;
+#pragma unroll
+        for (int r = 0; r < kDR; ++r)
+          add_pair<true>(s0, s1, nx[r], ny[r], nz[r], e2, ax[r], ay[r], az[r], pt[r],
+                         ti[r] == js, ti[r] == js + 1);
       }
     }
     __syncthreads();
   }
+  float4 *dst = out + static_cast<u64>(blockIdx.y) * n;
 #pragma unroll
   for (int r = 0; r < kDR; ++r)
-    if (ti[r] < n) out[ti[r]] = make_float4(ax[r], ay[r], az[r], pot[r]);
+    if (ti[r] < n)
+      dst[ti[r]] = make_float4(ax[r].x + ax[r].y, ay[r].x + ay[r].y, az[r].x + az[r].y,
+                               -(pt[r].x + pt[r].y));
+}
+
+// out[i] = the sum of the slices' partial sums of target i, in slice order.
+__global__ void k_direct_sum(const float4 *__restrict__ part, u32 n, u32 slices,
+                             float4 *__restrict__ out) {
+  const u32 i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  float4 a = part[i];
+  for (u32 k = 1; k < slices; ++k) {
+    const float4 v = part[static_cast<u64>(k) * n + i];
+    a.x += v.x;
+    a.y += v.y;
+    a.z += v.z;
+    a.w += v.w;
+  }
+  out[i] = a;
 }
 
 // ------------------------------------------------------------------ FP64
@@ -151,10 +203,30 @@ __global__ void k_direct64_sum(const double2 *part, u64 m, u32 slices, double *a
 
 }  // namespace
 
-void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, cudaStream_t s) {
+void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
+                 DeviceBuffer &scratch, cudaStream_t s) {
   if (n == 0) return;
-  k_direct<<<ceil_div(n, kDT * kDR), kDT, 0, s>>>(bodies, n, G, eps2, out);
+  int dev = 0, sms = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // Enough (target block, source slice) units for about 16 per SM, so that
+  // blocks of equal work end close together; each slice at least 8 tiles.
+  const u32 tiles = ceil_div(n, kDTB);
+  u32 slices = std::max<u32>(1, ceil_div(16u * static_cast<u32>(sms), tiles));
+  slices = std::min<u32>(slices, std::max<u32>(1, n / (8 * kDT)));
+  const u32 len = ceil_div(ceil_div(n, slices), kDT) * kDT;
+  slices = ceil_div(n, len);
+  float4 *dst = out;
+  if (slices > 1) {
+    scratch.ensure(static_cast<u64>(slices) * n * sizeof(float4));
+    dst = scratch.as<float4>();
+  }
+  k_direct<<<dim3(tiles, slices), kDT, 0, s>>>(bodies, n, len, G, eps2, dst);
   GTC_LAUNCH_CHECK();
+  if (slices > 1) {
+    k_direct_sum<<<ceil_div(n, 256), 256, 0, s>>>(dst, n, slices, out);
+    GTC_LAUNCH_CHECK();
+  }
 }
 
 Fp64SamplePlan plan_fp64_sample(u64 n, u64 m, int sms, u64 max_pairs) {

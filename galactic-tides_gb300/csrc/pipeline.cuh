@@ -82,6 +82,7 @@ struct Workspace {
   // scalars and reductions
   DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
+  DeviceBuffer direct_part;               // direct sum: per-slice partial sums
   RadixScratch radix;
 
   // host-side view of the last build
@@ -305,7 +306,9 @@ void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *a
                            const Scalars *sc, cudaStream_t s);
 
 // Direct summation kernels.
-void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out, cudaStream_t s);
+// The tiled FP32 direct sum; `scratch` holds per-source-slice partial sums.
+void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
+                 DeviceBuffer &scratch, cudaStream_t s);
 void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
                         double G, double eps, double *acc, double *pot, DeviceBuffer &scratch,
                         cudaStream_t s);

@@ -1,20 +1,33 @@
 #!/usr/bin/env python
-"""A batched ensemble of independent galaxies on one GPU.
+"""A batched ensemble of independent galaxies, on one GPU or sharded over
+several (one process per GPU).
 
   python galactic-tides_gb300/ensemble.py [--galaxies 64] [--steps 10]
+  torchrun --nproc-per-node N galactic-tides_gb300/ensemble.py ...
 
 Galaxies: N log-uniform in [10k, 500k], disk mass 0.5-2, bulge-to-disk
 mass 0-0.5, halo mass 3-10 (the benchmark model's other fields), one seed
-each. Each galaxy's group_size and sibling packing come from the autotuner
-(gtc_autotune_group); all galaxies then advance together, every step one
-CUDA graph launch (gtc_ensemble_leapfrog). Reported: the aggregate
-interactions/s of the ensemble, the same galaxies stepped one after another
-with the default parameters, and each galaxy's p99 force error against FP64
-direct sums on a sample. Prints one JSON object.
+each; every rank draws the same list. Galaxies are independent, so the
+ensemble shards by galaxy: `partition_by_cost` gives each rank a set of
+galaxies of about equal N log N cost (largest first, each to the least
+loaded rank), each rank advances its own set on its own GPU, and the
+per-galaxy results (interactions, p99 error, time) are gathered to rank 0 on
+the host. There is no exchange in the data path.
+
+On each GPU: each galaxy's group_size and sibling packing come from the
+autotuner (gtc_autotune_group); the rank's galaxies then advance together,
+every step one CUDA graph launch (gtc_ensemble_leapfrog). Reported: the
+aggregate interactions/s of the whole job (all ranks' interactions over the
+slowest rank's time), the same galaxies stepped one after another with the
+default parameters, and each galaxy's p99 force error against FP64 direct
+sums on a sample. Rank 0 prints one JSON object.
 """
 
 import argparse
+import importlib.util
 import json
+import math
+import os
 import pathlib
 import sys
 import time
@@ -28,7 +41,16 @@ SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, group_size=32, leaf
               pack=True)
 
 
-def draw_models(gtc, k, seed):
+def _galaxy_module():
+    spec = importlib.util.spec_from_file_location("gtc_ensemble_galaxy", HERE / "galaxy.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def draw_models(k, seed):
+    """The ensemble's k galaxy models (the same on every rank)."""
+    galaxy = _galaxy_module()
     rng = np.random.default_rng(seed)
     models = []
     for i in range(k):
@@ -36,48 +58,99 @@ def draw_models(gtc, k, seed):
         disk = rng.uniform(0.5, 2.0)
         bulge = max(rng.uniform(0.0, 0.5), 0.005) * disk
         halo = rng.uniform(3.0, 10.0)
-        m = gtc.galaxy_model(n, 1000 + i, disk_mass=disk, bulge_mass=bulge, halo_mass=halo)
-        models.append(m)
+        models.append(galaxy.galaxy_model(n, 1000 + i, disk_mass=disk, bulge_mass=bulge,
+                                          halo_mass=halo))
     return models
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--galaxies", type=int, default=64)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--dt", type=float, default=0.01)
-    ap.add_argument("--seed", type=int, default=4)
-    ap.add_argument("--sample", type=int, default=1024)
-    args = ap.parse_args()
+def galaxy_cost(n):
+    """Estimated cost of one step of a galaxy of n bodies: N log N."""
+    return n * math.log2(max(n, 2))
+
+
+def partition_by_cost(sizes, ranks):
+    """Galaxy indices per rank, about equal total cost: largest galaxy first,
+    each to the rank with the least cost so far (ties: the lowest rank).
+    Each rank's list is in galaxy order."""
+    if ranks < 1:
+        raise ValueError("need at least one rank")
+    load = [0.0] * ranks
+    parts = [[] for _ in range(ranks)]
+    for i in sorted(range(len(sizes)), key=lambda i: (-galaxy_cost(sizes[i]), i)):
+        r = min(range(ranks), key=lambda r: (load[r], r))
+        parts[r].append(i)
+        load[r] += galaxy_cost(sizes[i])
+    return [sorted(p) for p in parts]
+
+
+def gather_shards(shard, rank, world):
+    """Every rank's shard result on rank 0 (a list in rank order), None on
+    the others; the host-side gather of per-galaxy statistics."""
+    if world == 1:
+        return [shard]
+    import torch.distributed as dist
+    out = [None] * world if rank == 0 else None
+    dist.gather_object(shard, out, dst=0)
+    return out
+
+
+def combine(shards, steps):
+    """The job's figures from the ranks' shard results: per-galaxy rows in
+    galaxy order, interactions/s of all ranks over the slowest rank's time."""
+    rows = sorted((g for s in shards for g in s["galaxies"]), key=lambda g: g["galaxy"])
+    t_job = max(s["ensemble_seconds"] for s in shards)
+    inter = sum(g["interactions"] for g in rows)
+    p99 = [g["p99"] for g in rows]
+    return {
+        "ranks": len(shards), "galaxies": len(rows), "particles": sum(g["n"] for g in rows),
+        "steps": steps,
+        "ensemble_ms_per_step": round(1e3 * t_job / steps, 4),
+        "ensemble_interactions_per_s": inter / (t_job / steps) if t_job > 0 else None,
+        "per_rank": [{"rank": s["rank"], "galaxies": len(s["galaxies"]),
+                      "particles": sum(g["n"] for g in s["galaxies"]),
+                      "cost": sum(galaxy_cost(g["n"]) for g in s["galaxies"]),
+                      "ms_per_step": round(1e3 * s["ensemble_seconds"] / steps, 4)}
+                     for s in shards],
+        "p99": {"max": max(p99), "median": float(np.median(p99)), "per_galaxy": p99},
+        "tuned": [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "tuned_ms")}
+                  for g in rows],
+    }
+
+
+def run_shard(models, mine, args, device):
+    """Advances galaxies `mine` on GPU `device`: autotune, one eager pass as
+    the unbatched baseline, then the ensemble; the p99 error of each
+    galaxy's last forces. Returns the shard's result."""
     import torch
     import __graft_entry__
     gtc = __graft_entry__.load_package().gtc
-    dev = torch.device("cuda", 0)
-    models = draw_models(gtc, args.galaxies, args.seed)
+    galaxy = _galaxy_module()
+    dev = torch.device("cuda", device)
     gal = []
-    for m in models:
-        pos, vel, mass, _ = gtc.make_galaxy(model=m)
+    for i in mine:
+        pos, vel, mass, _ = galaxy.make_galaxy(model=models[i])
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
         n = len(mass)
-        gal.append(dict(n=n, pos0=pos, vel0=vel, pos=t(pos), vel=t(vel), mass=t(mass),
+        gal.append(dict(galaxy=i, n=n, pos=t(pos), vel=t(vel), mass=t(mass),
                         acc=torch.zeros((n, 3), dtype=torch.float64, device=dev),
                         pot=torch.zeros(n, dtype=torch.float64, device=dev)))
-    total_n = sum(g["n"] for g in gal)
+    shard = {"rank": args.rank, "galaxies": [], "ensemble_seconds": 0.0}
+    if not gal:
+        return shard
 
-    # the autotuner, per galaxy
-    tuner = gtc.Context(0)
+    tuner = gtc.Context(device)
     t0 = time.perf_counter()
     for g in gal:
         gs, pack, ms = tuner.autotune_group(g["pos"].data_ptr(), g["mass"].data_ptr(), g["n"],
                                             **SOLVER)
         g.update(group_size=gs, pack=pack, tuned_ms=ms)
-    t_tune = time.perf_counter() - t0
+    shard["autotune_seconds"] = time.perf_counter() - t0
 
     # one after another, default parameters, eager: the unbatched baseline
     for g in gal:
         tuner.group_force_device(g["pos"].data_ptr(), g["mass"].data_ptr(), g["n"],
                                  g["acc"].data_ptr(), g["pot"].data_ptr(), **SOLVER)
-    torch.cuda.synchronize()
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     seq_inter = 0
     for g in gal:
@@ -85,32 +158,30 @@ def main():
                                  g["acc"].data_ptr(), g["pot"].data_ptr(), **SOLVER)
         st = tuner.stats()
         seq_inter += st["cell_interactions"] + st["body_interactions"]
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
+    torch.cuda.synchronize(dev)
+    shard["sequential_seconds"] = time.perf_counter() - t0
+    shard["sequential_interactions"] = seq_inter
     tuner.close()
 
     # the ensemble: tuned parameters, one graph launch per step
-    ens = gtc.Ensemble(len(gal))
-    for i, g in enumerate(gal):
+    ens = gtc.Ensemble(len(gal), device)
+    for k, g in enumerate(gal):
         kw = dict(SOLVER, group_size=g["group_size"], pack=g["pack"])
-        ens.set_system(i, g["pos"].data_ptr(), g["vel"].data_ptr(), g["mass"].data_ptr(),
+        ens.set_system(k, g["pos"].data_ptr(), g["vel"].data_ptr(), g["mass"].data_ptr(),
                        g["acc"].data_ptr(), g["pot"].data_ptr(), g["n"], **kw)
     ens.leapfrog(args.dt, 2, prime=True, graph=True)  # capture and warm up
-    torch.cuda.synchronize()
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     ens.leapfrog(args.dt, args.steps, prime=False, graph=True)
-    torch.cuda.synchronize()
-    t_ens = time.perf_counter() - t0
-    inter = 0
-    replays = []
-    for i in range(len(gal)):
-        st = ens.context(i).stats()
-        inter += st["cell_interactions"] + st["body_interactions"]
-        replays.append(st["graph_steps"])
+    torch.cuda.synchronize(dev)
+    shard["ensemble_seconds"] = time.perf_counter() - t0
+    for k, g in enumerate(gal):
+        st = ens.context(k).stats()
+        g["interactions"] = st["cell_interactions"] + st["body_interactions"]
+        g["graph_steps"] = st["graph_steps"]
 
     # accuracy of each galaxy's last forces against FP64 direct sums
-    chk = gtc.Context(0)
-    p99 = []
+    chk = gtc.Context(device)
     for g in gal:
         n = g["n"]
         idx = gtc.sample_indices(n, args.sample, 1).astype(np.int64)
@@ -122,24 +193,46 @@ def main():
         ref = racc.cpu().numpy()
         got = g["acc"].cpu().numpy()[idx]
         e = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
-        p99.append(float(np.percentile(e, 99)))
+        g["p99"] = float(np.percentile(e, 99))
     chk.close()
     ens.close()
-    out = {
-        "galaxies": len(gal), "particles": total_n, "steps": args.steps, "dt": args.dt,
-        "ensemble_ms_per_step": round(1e3 * t_ens / args.steps, 4),
-        "ensemble_interactions_per_s": inter / (t_ens / args.steps),
-        "graph_replays_per_galaxy": [min(replays), max(replays)],
-        "sequential_force_eval_ms": round(1e3 * t_seq, 4),
-        "sequential_interactions_per_s": seq_inter / t_seq,
-        "note": ("ensemble steps include kicks and drifts; the sequential baseline is one force "
-                 "evaluation per galaxy with default group_size 32, packing on"),
-        "autotune_seconds": round(t_tune, 2),
-        "tuned": [dict(n=g["n"], group_size=g["group_size"], pack=g["pack"],
-                       ms=round(g["tuned_ms"], 4)) for g in gal],
-        "p99": {"max": max(p99), "median": float(np.median(p99)), "per_galaxy": p99},
-    }
-    print(json.dumps(out), flush=True)
+    shard["galaxies"] = [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "tuned_ms",
+                                             "interactions", "graph_steps", "p99")}
+                         for g in gal]
+    return shard
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--galaxies", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--dt", type=float, default=0.01)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--sample", type=int, default=1024)
+    args = ap.parse_args()
+    args.rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")  # host-side gather of statistics only
+    models = draw_models(args.galaxies, args.seed)
+    parts = partition_by_cost([m.n for m in models], world)
+    shard = run_shard(models, parts[args.rank], args, device)
+    shards = gather_shards(shard, args.rank, world)
+    if args.rank == 0:
+        out = combine(shards, args.steps)
+        seq_t = sum(s.get("sequential_seconds", 0.0) for s in shards)
+        out["sequential_interactions_per_s"] = (
+            sum(s.get("sequential_interactions", 0) for s in shards) / seq_t if seq_t else None)
+        out["autotune_seconds"] = round(max(s.get("autotune_seconds", 0.0) for s in shards), 2)
+        out["note"] = ("ensemble steps include kicks and drifts; the sequential baseline is one "
+                       "force evaluation per galaxy with default group_size 32, packing on")
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

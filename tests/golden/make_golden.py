@@ -3,7 +3,7 @@
 Run where the reference sources are present (they are built into
 oracle/_ref/libgtref.so by oracle/Makefile.ref):
 
-    make -f oracle/Makefile.ref REF=/root/reference
+    make -f oracle/Makefile.ref REF=<the reference tree>
     python tests/golden/make_golden.py
 
 Each fixture holds seeded inputs and the reference's outputs for them:
