@@ -168,3 +168,184 @@ def quad_norm(q):
     """Frobenius norm of the symmetric tensor (xx, yy, zz, xy, xz, yz)."""
     xx, yy, zz, xy, xz, yz = q
     return np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
+
+
+# ---- the learned walk's decisions -------------------------------------------
+#
+# A restatement of galactic-tides_gb300/csrc/learned_walk.cu's walk on a given
+# tree: the node and group records in FP32 as the device packs them, the
+# verdict of every (group, node) test the walk makes -- the reference's
+# overlap test (group_lists.cpp:147) and the guard open; cells of at most two
+# bodies accepted; the centred prior decides when it clears the tolerance by
+# more than the band; the network (BF16 emulation) decides the rest -- and
+# the cells and bodies each group ends with. The walk visits a node when its
+# parent was visited and opened (the root is always opened when it has
+# children). Rounds, parts and hand-offs to warps only order the device's
+# lists, so multisets are compared. Each test's distance from its threshold
+# is returned too: device and oracle may differ where the two FP32 pipelines
+# (FMA contraction, the fast log2 and exp2) or the BF16 emulation round a
+# test to the other side.
+
+KIND_GEOM, KIND_PRIOR, KIND_NET = 0, 1, 2
+
+
+def _f32(v):
+    return np.asarray(v, dtype=np.float32)
+
+
+def _log2f(v):
+    return _f32(np.log2(np.asarray(v, np.float64)))
+
+
+def _fmaf(a, b, c):
+    return _f32(np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64))
+
+
+def node_records(nodes, cells, theta_guard, y_mean):
+    """Per node, the FP32 record the learned walk reads (centre, slack,
+    centre of mass relative to the root centre; guard^2; the prior's node
+    part) and the cell-only features."""
+    origin = nodes["center"][0]
+    L, mt = float(nodes["half"][0]), float(nodes["mass"][0])
+    inv_l, inv_mt = _f32(1.0 / L), _f32(1.0 / mt)
+    rec = {
+        "c": _f32(nodes["center"] - origin), "slack": _f32(nodes["half"] * 1.0001),
+        "m": _f32(nodes["com"] - origin),
+        "nbody": (nodes["end"].astype(np.int64) - nodes["begin"]),
+        "leaf": nodes["n_children"] == 0,
+    }
+    half = _f32(nodes["half"])
+    delta = _f32(nodes["delta"])
+    mass = _f32(cells[:, 3])
+    qa, qb = _f32(cells[:, 4:8]), _f32(cells[:, 8:12])
+    qn = _f32(np.sqrt(qa[:, 0] ** 2 + qa[:, 1] ** 2 + qa[:, 2] ** 2
+                      + 2.0 * (qa[:, 3] ** 2 + qb[:, 0] ** 2 + qb[:, 1] ** 2)))
+    f1 = _log2f(np.maximum(half * inv_l, 1e-30))
+    f3 = _log2f(np.maximum(mass * inv_mt, 1e-30))
+    f4 = _log2f(np.maximum(qn / np.maximum(mass, _f32(1e-30)) * inv_l * inv_l + _f32(1e-12),
+                           1e-30))
+    f5 = _f32(delta / np.maximum(half, _f32(1e-30)))
+    prior = _f32(_f32(PRIOR_BASE) + f3 + _f32(3.0) * f1)
+    crit = _fmaf(_f32(2.0) * half, _f32(1.0 / theta_guard), delta)
+    rec.update(guard2=_f32(crit * crit), f1=f1, f3=f3, f4=f4, f5=f5, prior=prior,
+               pscale=_f32(np.exp2(np.float64(0.4) * (prior.astype(np.float64) + y_mean))),
+               inv_l=inv_l, inv_mt=inv_mt, L=L, mt=mt, origin=origin)
+    return rec
+
+
+def group_records(tpos, ranges, amag, rec, alpha, G):
+    """Per group: the FP32 box (centre relative to the root centre,
+    half-extent), the group feature f0 and the tolerance tau."""
+    ng = len(ranges)
+    gc = np.zeros((ng, 3), np.float32)
+    gh = np.zeros((ng, 3), np.float32)
+    tau = np.zeros(ng, np.float32)
+    for g, (b, e) in enumerate(ranges):
+        p = tpos[b:e]
+        lo_, hi_ = p.min(0), p.max(0)
+        gc[g] = _f32((lo_ + hi_) * 0.5 - rec["origin"])
+        gh[g] = _f32((hi_ - lo_) * 0.5)
+        a = _f32(amag[b:e])
+        asum = np.float32(0.0)
+        for v in a:  # in target order, FP32
+            asum = np.float32(asum + v)
+        ag = max(a.min(), np.float32(np.float32(0.5) * asum / np.float32(max(e - b, 1))))
+        v = alpha * float(ag) * rec["L"] * rec["L"] / (G * rec["mt"])
+        tau[g] = np.float32(np.log2(v)) if v > 0 else np.float32(-1e30)
+    f0 = _log2f(np.maximum(gh.max(1) * rec["inv_l"], _f32(1e-9)))
+    return gc, gh, f0, tau
+
+
+def walk_lists(nodes, cells, tpos, ranges, amag, model, alpha, G=1.0, theta_guard=1.5,
+               band=None):
+    """The learned walk on a tree whose every node comes after its parent
+    (nodes['parent']; the device's walk order and the reference's layout
+    both qualify), amag the previous |a| of each body in tree order. Returns, per group, the accepted cells
+    (node indices) and the bodies (tree positions, with repeats), and per
+    group the margins of its tests: a list of (node, kind, margin), margin
+    relative to the threshold for FP32 tests (KIND_GEOM, KIND_PRIOR) and in
+    log2 units for the network (KIND_NET)."""
+    p = unpack(model)
+    band = float(p["band"]) if band is None or band < 0 else float(band)
+    rec = node_records(nodes, cells, theta_guard, float(p["ymean"]))
+    gc, gh, f0, tau = group_records(tpos, ranges, amag, rec, alpha, G)
+    ng, m = len(ranges), len(nodes)
+    l2 = _f32(_f32(1.0) / (rec["inv_l"] * rec["inv_l"]))
+    acc_d2 = _f32(_f32(np.exp2(np.float64(0.4) * (band - tau.astype(np.float64)))) * l2)
+    open_d2 = _f32(_f32(np.exp2(np.float64(0.4) * (-band - tau.astype(np.float64)))) * l2)
+    parent = nodes["parent"].astype(np.int64)
+    visited = np.zeros((ng, m), bool)
+    final = np.zeros((ng, m), np.int8)  # 0 open, 1 accept
+    margins = [[] for _ in range(ng)]
+    root_opened = not rec["leaf"][0]
+    for i in range(m):
+        if i == 0:
+            vis = np.full(ng, not root_opened)
+            if root_opened:
+                visited[:, 0] = False
+                final[:, 0] = 0
+                continue
+        else:
+            q = parent[i]
+            vis = (visited[:, q] | ((q == 0) & root_opened)) & (final[:, q] == 0) & \
+                ~rec["leaf"][q]
+        visited[:, i] = vis
+        if not vis.any():
+            continue
+        gsel = np.nonzero(vis)[0]
+        c, s, mm = rec["c"][i], rec["slack"][i], rec["m"][i]
+        # overlap: every axis |c - gc| <= slack + gh
+        lhs = np.abs(c - gc[gsel])
+        rhs = _f32(s + gh[gsel])
+        overlap = np.all(lhs <= rhs, axis=1)
+        axis_margin = np.abs(lhs - rhs) / np.maximum(np.abs(rhs), _f32(1e-30))
+        d = np.maximum(np.abs(mm - gc[gsel]) - gh[gsel], _f32(0.0))
+        d2 = _fmaf(d[:, 0], d[:, 0], _fmaf(d[:, 1], d[:, 1], _f32(d[:, 2] * d[:, 2])))
+        guard = rec["guard2"][i]
+        verdict = np.full(len(gsel), 2, np.int8)
+        opened = overlap | ~(d2 > guard)
+        verdict[opened] = 0
+        few = ~opened & (rec["nbody"][i] <= FEW_BODIES)
+        verdict[few] = 1
+        rest = ~opened & ~few
+        acc_t = _f32(rec["pscale"][i] * acc_d2[gsel])
+        open_t = _f32(rec["pscale"][i] * open_d2[gsel])
+        verdict[rest & (d2 > acc_t)] = 1
+        verdict[rest & ~(d2 > acc_t) & (d2 < open_t)] = 0
+        gm = np.minimum(axis_margin.min(1),
+                        np.abs(d2 - guard) / np.maximum(guard, _f32(1e-30)))
+        pm = np.minimum(np.abs(d2 - acc_t) / np.maximum(acc_t, _f32(1e-30)),
+                        np.abs(d2 - open_t) / np.maximum(open_t, _f32(1e-30)))
+        for k, g in enumerate(gsel):
+            margins[g].append((i, KIND_GEOM, float(gm[k])))
+            if rest[k]:
+                margins[g].append((i, KIND_PRIOR, float(pm[k])))
+        final[gsel, i] = np.where(verdict == 1, 1, 0)
+        # the network decides the deferred pairs of this node (before any of
+        # its children is visited)
+        dsel = verdict == 2
+        if dsel.any():
+            gs_, d2s = gsel[dsel], d2[dsel]
+            f2 = _log2f(np.maximum(np.sqrt(d2s.astype(np.float64)).astype(np.float32)
+                                   * rec["inv_l"], _f32(1e-9)))
+            feat = np.stack([f0[gs_], np.full(len(gs_), rec["f1"][i]), f2,
+                             np.full(len(gs_), rec["f3"][i]), np.full(len(gs_), rec["f4"][i]),
+                             np.full(len(gs_), rec["f5"][i])], axis=1)
+            pred = predict_bf16(model, feat)
+            acc = pred < tau[gs_]
+            final[gs_, i] = np.where(acc, 1, 0)
+            for g, mg in zip(gs_, np.abs(pred - tau[gs_])):
+                margins[g].append((i, KIND_NET, float(mg)))
+    cells_out, bodies_out = [], []
+    nb, leaf = rec["nbody"], rec["leaf"]
+    begin = nodes["begin"].astype(np.int64)
+    for g in range(ng):
+        vis = np.nonzero(visited[g])[0]
+        fin = final[g, vis]
+        acc = vis[(fin == 1) & (nb[vis] > FEW_BODIES)]
+        src = vis[((fin == 1) & (nb[vis] <= FEW_BODIES)) | ((fin == 0) & leaf[vis])]
+        cells_out.append(np.sort(acc))
+        bodies_out.append(np.sort(np.concatenate(
+            [np.arange(begin[j], begin[j] + nb[j]) for j in src]) if len(src) else
+            np.zeros(0, np.int64)))
+    return cells_out, bodies_out, margins

@@ -406,3 +406,111 @@ def test_invalid_learned_arguments(ctx, gtc):
         ctx.set_option("learned_pair_budget", 0.5)
     with pytest.raises(gtc.GtcInvalidArgument):
         ctx.set_option("learned_read_every_round", 2)
+
+
+# ---------------------------------------------------- the walk's decisions
+
+def ref_tree_with_parents(nodes):
+    """The oracle's (reference-layout) nodes with a parent field."""
+    import numpy.lib.recfunctions as rfn
+    parent = np.zeros(len(nodes), np.int64)
+    for i in range(len(nodes)):
+        c0, nc = int(nodes["first_child"][i]), int(nodes["n_children"][i])
+        if nc > 0:
+            parent[c0:c0 + nc] = i
+    return rfn.append_fields(nodes, "parent", parent, usemask=False)
+
+
+def walk_margin_sets(nodes, margins, tol_fp32=2e-5, tol_net=0.06):
+    """Per group: the nodes whose subtree holds a test within rounding of
+    its threshold (FP32 tests relative, network tests in log2 units)."""
+    out = []
+    for ms in margins:
+        out.append({i for i, kind, m in ms
+                    if m < (tol_net if kind == lo.KIND_NET else tol_fp32)})
+    return out
+
+
+def test_walk_oracle_covers_every_body_once():
+    """The CPU restatement of the learned walk on the oracle's own tree and
+    groups (committed model): the reference's list invariants hold -- every
+    body covered exactly once per group, no accepted cell holding one of the
+    group's targets -- and fewer interactions than the theta walk."""
+    from native import Oracle
+    from checks import check_lists
+    orc = Oracle()
+    pos, mass = __import__("native").lopsided_sphere(6000, 21)
+    nodes, order, lists = orc.lists(pos, mass, theta=0.75, group_size=32, leaf_size=8, pack=True)
+    out = orc.eval_lists(lists, G=1.0, eps=0.025, quadrupole=True)
+    amag = np.sqrt((out[:, :3].astype(np.float64) ** 2).sum(1)).astype(np.float32)
+    model = np.fromfile(MODEL, dtype="<f4")
+    alpha = json.loads(MODEL_INFO.read_text())["alpha"]
+    tree = ref_tree_with_parents(nodes)
+    ranges = lists.groups[:, :2].astype(np.int64)
+    cells, bodies, margins = lo.walk_lists(tree, lists.cells, pos[order.astype(np.int64)], ranges,
+                                           amag, model, alpha)
+    cl = np.concatenate(cells).astype(np.uint32)
+    bl = np.concatenate(bodies).astype(np.uint32)
+    nc = np.cumsum([0] + [len(c) for c in cells])
+    nb = np.cumsum([0] + [len(b) for b in bodies])
+    groups = np.stack([ranges[:, 0], ranges[:, 1], nc[:-1], nc[1:], nb[:-1], nb[1:]], axis=1)
+    assert check_lists(nodes["begin"], nodes["end"], groups, cl, bl, len(mass), 32) == 0
+    t = ranges[:, 1] - ranges[:, 0]
+    inter = int((t * (nc[1:] - nc[:-1] + nb[1:] - nb[:-1])).sum())
+    assert inter < lists.stats.cell_interactions + lists.stats.body_interactions + len(mass)
+    assert any(k == lo.KIND_NET for ms in margins for _, k, _ in ms)  # the network decided some
+
+
+@gpu
+def test_walk_decisions_match_oracle(gtc):
+    """The device's learned lists against the oracle's restatement of the
+    walk (committed model and alpha, 20k-body galaxy, the device's own tree,
+    groups and previous |a|): each group holds the same multiset of
+    accepted cells and of bodies, except under a test that lies within
+    rounding of its threshold (2e-5 relative for the FP32 tests, 0.06 log2
+    units for the network against its BF16 emulation)."""
+    model = np.fromfile(MODEL, dtype="<f4")
+    alpha = json.loads(MODEL_INFO.read_text())["alpha"]
+    pos, _, mass, _ = gtc.make_galaxy(20_000, seed=3)
+    c = gtc.Context(0)
+    try:
+        c.learned_set_model(model)
+        c.group_force(pos, mass, criterion=gtc.CRITERION_LEARNED, alpha=alpha, **SOLVER)
+        first = c.export()  # the theta fallback: its forces are the walk's |a|
+        c.group_force(pos, mass, criterion=gtc.CRITERION_LEARNED, alpha=alpha, **SOLVER)
+        assert c.stats()["criterion_used"] == gtc.CRITERION_LEARNED
+        d = c.export()
+    finally:
+        c.close()
+    order = d["order"].astype(np.int64)
+    assert np.array_equal(order, first["order"])
+    amag = np.sqrt((first["out"][:, :3].astype(np.float64) ** 2).sum(1)).astype(np.float32)
+    nodes, g = d["nodes"], d["groups"].astype(np.int64)
+    cells, bodies, margins = lo.walk_lists(nodes, d["cells"], pos[order], g[:, :2], amag, model,
+                                           alpha)
+    near = walk_margin_sets(nodes, margins)
+    skip = nodes["skip"].astype(np.int64)
+    nbegin, nend = nodes["begin"].astype(np.int64), nodes["end"].astype(np.int64)
+    differ = unexplained = 0
+    for k in range(len(g)):
+        dc = np.sort(d["cell_list"][g[k, 2]:g[k, 3]].astype(np.int64))
+        db = np.sort(d["body_list"][g[k, 4]:g[k, 5]].astype(np.int64))
+        if np.array_equal(dc, cells[k]) and np.array_equal(db, bodies[k]):
+            continue
+        differ += 1
+        sub = np.zeros(len(nodes), bool)   # nodes under a near-threshold test
+        cov = np.zeros(len(mass) + 1, np.int64)
+        for j in near[k]:
+            sub[j:skip[j]] = True
+            cov[nbegin[j]] += 1
+            cov[nend[j]] -= 1
+        cov = np.cumsum(cov)[:len(mass)] > 0
+        dcells = np.setxor1d(dc, cells[k])
+        dbod = np.setdiff1d(np.union1d(db, bodies[k]), np.intersect1d(db, bodies[k]))
+        if len(db) != len(bodies[k]) and len(dbod) == 0:  # a repeated body
+            dbod = np.union1d(db, bodies[k])
+        unexplained += int((~sub[dcells]).sum() + (~cov[dbod]).sum())
+    print(f"\n[learned walk vs oracle] groups {len(g)}, differing {differ}, "
+          f"entries not explained by a near-threshold test {unexplained}")
+    assert unexplained == 0
+    assert differ <= max(3, len(g) // 50)
