@@ -66,7 +66,7 @@ void Workspace::release_all() {
                          &nend, &skip, &parent, &depth, &nchild, &isleaf, &kids, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
                          &groups, &cell_list, &body_list, &spill, &splitpt, &root, &bbox_part, &scalars, &split, &scan_tmp,
-                         &direct_part, &radix.counts, &radix.scan_tmp};
+                         &direct_part, &walk_next, &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (side) {
     cudaStreamSynchronize(side);
@@ -387,6 +387,7 @@ struct GraphStep {
     ws.n_cell_list = hs.n_cell_list;
     ws.n_body_list = hs.n_body_list;
     ws.gapped = true;  // replays walk once into the captured slots
+    ws.lists_unordered = ws.walk_warps;
     gtc_stats &st = ctx->stats;
     const u32 replays = st.graph_steps;
     st = gtc_stats{};
@@ -897,6 +898,10 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
     } else if (key == "graph_headroom") {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;
+    } else if (key == "walk_warps") {
+      if (value != 0 && value != 1) throw gtc::InvalidArgument("walk_warps must be 0 or 1");
+      ctx->ws.walk_warps = value != 0;
+      ctx->ws.slot_cells = 0;  // slots sized by the other walk would not fit: count first
     } else if (key == "stage_events") {
       if (value != 0 && value != 1) throw gtc::InvalidArgument("stage_events must be 0 or 1");
       ctx->ws.stage_on = value != 0;
@@ -1396,10 +1401,16 @@ gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
         const uint4 q0 = rec[4 * g];
         const gtc::SegView cs = gtc::cell_segs(rec[4 * g + 1], rec[4 * g + 2]);
         const gtc::SegView bs = gtc::body_segs(rec[4 * g + 2], rec[4 * g + 3]);
-        if (cell_list)
+        if (cell_list) {
           for (u32 e = 0; e < q0.z; ++e) cell_list[c + e] = cl[cs.at(e)];
-        if (body_list)
+          // the reference visits nodes in increasing index (node numbering)
+          if (ws.lists_unordered) std::sort(cell_list + c, cell_list + c + q0.z);
+        }
+        if (body_list) {
           for (u32 e = 0; e < q0.w; ++e) body_list[b + e] = bl[bs.at(e)];
+          // and so reaches bodies in increasing tree position
+          if (ws.lists_unordered) std::sort(body_list + b, body_list + b + q0.w);
+        }
         if (groups) {
           gtc_group &o = groups[g];
           o.begin = q0.x;

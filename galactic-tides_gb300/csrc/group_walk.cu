@@ -469,6 +469,192 @@ __global__ void __launch_bounds__(kWalkThreads)
     atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(sum));
 }
 
+// The walk by warps: one warp per group, 32 node tests per step. The
+// warp keeps the nodes still to visit as a stack of index ranges in shared
+// memory, each a run of whole subtrees [i, end) (i, skip[i], ... before
+// end). Each step the lanes take the ranges on top, test each range's first
+// node, and push back the rest of its range and, when the node is opened,
+// its children's range (children on top: depth first). The same nodes are
+// tested, with the same verdicts, as by the reference's walk; only the order
+// the entries reach the lists differs (step order, lane order within a
+// step; fixed for given inputs). Exports put each group's lists back in the
+// reference's order (increasing node and body index, which is its visiting
+// order). Modes: count the lists (kCount); write them at scanned offsets
+// (kFill); write them into per-group slots, counting past a slot that
+// overflows (kSlots, the one-pass walk, whose counts and records then go
+// through the split walk's spill and record kernels as one part); write the
+// lists of the groups that outgrew their slots again, whole, into their
+// places in the overflow pools (kSpill).
+constexpr int kSlots = 2;
+constexpr int kWarpWalkWarps = 4;
+constexpr int kWarpStack = 1024;  // ranges per warp
+constexpr u32 kWarpWalkThreads = kWarpWalkWarps * 32;
+
+struct WarpWalkOut {
+  u64 *ncells, *nbodies;          // kCount: per group; kSlots: SplitOut's part 0 (cap: its stride)
+  const u64 *cell_off, *body_off; // kFill
+  u32 *cell_list, *body_list;
+  const u32 *spill_cells, *spill_bodies;  // kSpill
+  u32 *split;                     // kSlots: the split walk's split points (all lists: part 0)
+  u32 slot_cells, slot_bodies, cap;
+};
+
+__device__ __forceinline__ u32 warp_excl_scan(u32 v, int lane, u32 &total) {
+  u32 s = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const u32 y = __shfl_up_sync(kFullMask, s, o);
+    if (lane >= o) s += y;
+  }
+  total = __shfl_sync(kFullMask, s, 31);
+  return s - v;
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(kWarpWalkThreads)
+    k_walk_warp(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
+                const float *gboxf, u32 ng_cap, WarpWalkOut out, u32 *next_group, Scalars *sc,
+                const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+  __shared__ uint2 stack_all[kWarpWalkWarps][kWarpStack];
+  if (aborted(abort)) return;
+  const u32 ng = bounded(ng_cap, ng_dev);
+  const int lane = threadIdx.x & 31;
+  uint2 *stk = stack_all[threadIdx.x >> 5];
+  const unsigned below = (1u << lane) - 1u;
+  const u32 root_end = load32(walk32, 0).skip;
+  const bool root_leaf = (load32(walk32, 0).nbody_leaf >> 31) != 0;
+  u32 exact = 0, visits = 0;
+  for (;;) {
+    u32 g = 0;
+    if (lane == 0) g = atomicAdd(next_group, 1u);
+    g = __shfl_sync(kFullMask, g, 0);
+    if (g >= ng) break;
+    u32 *cl = nullptr, *bl = nullptr;
+    u64 cap_c = ~0ull, cap_b = ~0ull;
+    if (kMode == kFill) {
+      cl = out.cell_list + out.cell_off[g];
+      bl = out.body_list + out.body_off[g];
+    } else if (kMode == kSlots) {
+      cap_c = out.slot_cells;
+      cap_b = out.slot_bodies;
+      cl = out.cell_list + static_cast<u64>(g) * cap_c;
+      bl = out.body_list + static_cast<u64>(g) * cap_b;
+    } else if (kMode == kSpill) {
+      if (out.spill_cells[g] == kNoSpill) continue;
+      cl = out.cell_list + out.spill_cells[g];
+      bl = out.body_list + out.spill_bodies[g];
+    }
+    const float4 b0 = reinterpret_cast<const float4 *>(gboxf)[2ull * g],
+                 b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
+    const float gf[3] = {b0.x, b0.y, b0.z}, hf[3] = {b0.w, b1.x, b1.y};
+    const float gbound = b1.z;
+    u64 nc = 0, nb = 0;  // warp-uniform
+    // the root contains every group and is opened, unless it is a leaf
+    if (lane == 0) stk[0] = root_leaf ? make_uint2(0u, root_end) : make_uint2(1u, root_end);
+    u32 top = 1;
+    __syncwarp();
+    while (top > 0) {
+      if (top > kWarpStack - 2 * 32) {
+        // nearly full: lane 0 walks the top range alone, without a stack
+        const uint2 e = stk[top - 1];
+        --top;
+        __syncwarp();
+        if (lane == 0) {
+          u32 i = e.x;
+          while (i < e.y) {
+            const WalkRec32 r = load32(walk32, i);
+            ++visits;
+            const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
+            const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+            const bool leaf = (r.nbody_leaf >> 31) != 0;
+            if (verdict == 1 && nbody > kFewBodies) {
+              if (kMode != kCount && nc < cap_c) cl[nc] = i;
+              ++nc;
+            } else if (verdict == 1 || leaf) {
+              for (u32 j = 0; j < nbody; ++j)
+                if (kMode != kCount && nb + j < cap_b) bl[nb + j] = r.begin + j;
+              nb += nbody;
+            }
+            if (verdict == 1 || leaf) {
+              if (r.skip <= i) {  // malformed tree: never loop
+                atomicOr(&sc->error, 1u);
+                break;
+              }
+              i = r.skip;
+            } else {
+              ++i;
+            }
+          }
+        }
+        nc = __shfl_sync(kFullMask, nc, 0);
+        nb = __shfl_sync(kFullMask, nb, 0);
+        continue;
+      }
+      const u32 take = min(32u, top);
+      const bool has = static_cast<u32>(lane) < take;
+      const uint2 e = has ? stk[top - 1 - lane] : make_uint2(0u, 0u);
+      top -= take;
+      __syncwarp();
+      WalkRec32 r{};
+      int verdict = 0;
+      if (has) {
+        r = load32(walk32, e.x);
+        ++visits;
+        verdict = decide(r, walk64, e.x, gf, hf, gbound, gbox, g, exact);
+      }
+      const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+      const bool leaf = (r.nbody_leaf >> 31) != 0;
+      const bool bad = has && r.skip <= e.x;  // malformed tree: never loop
+      if (bad) atomicOr(&sc->error, 1u);
+      const bool cell = has && verdict == 1 && nbody > kFewBodies;
+      const bool bod = has && !cell && (verdict == 1 || leaf);
+      const bool kids = has && !bad && verdict == 0 && !leaf;
+      const bool rest = has && !bad && r.skip < e.y;
+      // cells: one slot per accepting lane, in lane order
+      const unsigned mc = __ballot_sync(kFullMask, cell);
+      if (kMode != kCount && cell) {
+        const u64 pos = nc + __popc(mc & below);
+        if (pos < cap_c) cl[pos] = e.x;
+      }
+      nc += __popc(mc);
+      // bodies: each lane's run after the runs of the lanes before it
+      u32 bt = 0;
+      const u32 boff = warp_excl_scan(bod ? nbody : 0u, lane, bt);
+      if (kMode != kCount && bod)
+        for (u32 j = 0; j < nbody; ++j)
+          if (nb + boff + j < cap_b) bl[nb + boff + j] = r.begin + j;
+      nb += bt;
+      // pushes: each lane its rest, then its children's range (on top)
+      u32 pt = 0;
+      const u32 poff = warp_excl_scan(static_cast<u32>(rest) + static_cast<u32>(kids), lane, pt);
+      if (rest) stk[top + poff] = make_uint2(r.skip, e.y);
+      if (kids) stk[top + poff + (rest ? 1u : 0u)] = make_uint2(e.x + 1, r.skip);
+      top += pt;
+      __syncwarp();
+    }
+    if (lane == 0) {
+      if (kMode == kCount) {
+        out.ncells[g] = nc;
+        out.nbodies[g] = nb;
+      } else if (kMode == kSlots) {
+        out.ncells[g] = nc;
+        out.nbodies[g] = nb;
+        out.ncells[static_cast<u64>(out.cap) + g] = 0;
+        out.nbodies[static_cast<u64>(out.cap) + g] = 0;
+        out.split[2ull * g] = static_cast<u32>(nc < 0xffffffffull ? nc : 0xffffffffull);
+        out.split[2ull * g + 1] = static_cast<u32>(nb < 0xffffffffull ? nb : 0xffffffffull);
+      }
+    }
+  }
+  if (kMode == kCount || kMode == kSlots) {
+    const u32 ex = __reduce_add_sync(kFullMask, exact), vs = __reduce_add_sync(kFullMask, visits);
+    if (lane == 0) {
+      if (ex) atomicAdd(&sc->fp64_tests, static_cast<unsigned long long>(ex));
+      atomicAdd(&sc->walk_nodes, static_cast<unsigned long long>(vs));
+    }
+  }
+}
+
 // Places in the overflow pools for the groups one of whose parts outgrew its
 // slot (their whole lists, walked again by one thread); pools too small flag
 // the lists as overflowing.
@@ -617,8 +803,27 @@ void size_slots(Workspace &ws, const Scalars &h, bool split) {
   };
   ws.slot_cells = slot(h.max_cells);
   ws.slot_bodies = slot(h.max_bodies);
-  ws.slot_near_cells = slot(split ? h.max_near_cells : h.max_cells);
-  ws.slot_near_bodies = slot(split ? h.max_near_bodies : h.max_bodies);
+  // the warp walk writes a group's whole lists into the first slots
+  ws.slot_near_cells = slot(ws.walk_warps ? 0 : split ? h.max_near_cells : h.max_cells);
+  ws.slot_near_bodies = slot(ws.walk_warps ? 0 : split ? h.max_near_bodies : h.max_bodies);
+}
+
+// The warp walk over ng groups: enough warps to fill the GPU, groups taken
+// from a counter.
+template <int kMode>
+void launch_warp_walk(Workspace &ws, const WarpWalkOut &out, u32 ng_cap, Scalars *sc,
+                      cudaStream_t s, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+  int dev = 0, sms = 0;
+  GTC_CUDA(cudaGetDevice(&dev));
+  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  ws.walk_next.ensure(sizeof(u32));
+  GTC_CUDA(cudaMemsetAsync(ws.walk_next.ptr, 0, sizeof(u32), s));
+  const u32 blocks = static_cast<u32>(std::max<u64>(
+      1, std::min<u64>(ceil_div(ng_cap, kWarpWalkWarps), 8ull * static_cast<u64>(sms))));
+  k_walk_warp<kMode><<<blocks, kWarpWalkThreads, 0, s>>>(
+      ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
+      ws.gboxf.as<float>(), ng_cap, out, ws.walk_next.as<u32>(), sc, ng_dev, abort);
+  GTC_LAUNCH_CHECK();
 }
 
 }  // namespace
@@ -629,11 +834,13 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u64 prev_entries = ws.n_cell_list + ws.n_body_list;
   ws.n_groups = ws.n_cell_list = ws.n_body_list = 0;
   ws.gapped = false;
+  ws.lists_unordered = false;
   ws.list_passes = 0;
   if (n == 0) return;
   const u32 n32 = static_cast<u32>(n), m = static_cast<u32>(ws.n_nodes);
   const u32 gs = static_cast<u32>(sp.group_size);
   Scalars *sc = ws.scalars.as<Scalars>();
+  ws.walk_next.ensure(sizeof(u32));  // before any graph capture reuses the walk
   GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
   ws.flags.ensure(std::max<u64>(n, m) * 4);
@@ -731,17 +938,27 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
                       ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
                       sl_c, sl_b, sn_c, sn_b, ng};
-    k_walk_split<<<ceil_div(2ull * ng, kWalkThreads), kWalkThreads, 0, s>>>(
-        w32, w64, gbox, gboxf, gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
-        ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc);
-    GTC_LAUNCH_CHECK();
+    const WarpWalkOut wwo{so.ncells, so.nbodies, nullptr, nullptr, ws.cell_list.as<u32>(),
+                          ws.body_list.as<u32>(), spill_c, spill_b, so.split, sl_c, sl_b, ng};
+    if (ws.walk_warps) {
+      launch_warp_walk<kSlots>(ws, wwo, ng, sc, s);
+    } else {
+      k_walk_split<<<ceil_div(2ull * ng, kWalkThreads), kWalkThreads, 0, s>>>(
+          w32, w64, gbox, gboxf, gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
+          ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc);
+      GTC_LAUNCH_CHECK();
+    }
     k_split_spill<<<gb, kT, 0, s>>>(so, ng, pool_at_c, pool_c, pool_at_b, pool_b, spill_c, spill_b,
                                     sc);
     GTC_LAUNCH_CHECK();
-    WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
-    k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
-    GTC_LAUNCH_CHECK();
+    if (ws.walk_warps) {
+      launch_warp_walk<kSpill>(ws, wwo, ng, sc, s);
+    } else {
+      WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+                 ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
+      k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
+      GTC_LAUNCH_CHECK();
+    }
     k_split_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, so, spill_c, spill_b,
                                       ws.groups.as<uint4>(), sc);
     GTC_LAUNCH_CHECK();
@@ -752,6 +969,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
       ws.n_cell_list = host->n_cell_list;
       ws.n_body_list = host->n_body_list;
       ws.gapped = true;
+      ws.lists_unordered = ws.walk_warps;
       ws.list_passes = 1;
       return;
     }
@@ -769,8 +987,15 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   u64 *cell_off = ws.gcell_off.as<u64>(), *body_off = ws.gbody_off.as<u64>();
   WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr,
              nullptr, nullptr};
-  k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
-  GTC_LAUNCH_CHECK();
+  const bool warps = ws.walk_warps && ntasks == 1;
+  WarpWalkOut wwo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), cell_off, body_off, nullptr, nullptr,
+                  nullptr, nullptr, nullptr, 0u, 0u, ng};
+  if (warps) {
+    launch_warp_walk<kCount>(ws, wwo, ng, sc, s);
+  } else {
+    k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
+    GTC_LAUNCH_CHECK();
+  }
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
   exclusive_scan_u64(ws.gbodies.as<u64>(), body_off, slots, body_off + slots, ws.scan_tmp, s);
   GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + slots, 8, cudaMemcpyDeviceToDevice, s));
@@ -788,9 +1013,16 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.body_list.ensure(std::max<u64>(1, ws.n_body_list) * 4);
   wo.cell_list = ws.cell_list.as<u32>();
   wo.body_list = ws.body_list.as<u32>();
-  k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
-  GTC_LAUNCH_CHECK();
+  if (warps) {
+    wwo.cell_list = wo.cell_list;
+    wwo.body_list = wo.body_list;
+    launch_warp_walk<kFill>(ws, wwo, ng, sc, s);
+  } else {
+    k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
+    GTC_LAUNCH_CHECK();
+  }
   ws.stage(Workspace::kStWalk1, s);
+  ws.lists_unordered = warps;
   ws.list_passes = 2;
 }
 
@@ -839,21 +1071,32 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
                     ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
                     caps.slot_cells, caps.slot_bodies, caps.slot_near_cells,
                     caps.slot_near_bodies, n32};
-  k_walk_split<<<ceil_div(2ull * n, kWalkThreads), kWalkThreads, 0, s>>>(
-      ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
-      ws.gboxf.as<float>(), gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
-      ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort);
-  GTC_LAUNCH_CHECK();
+  const WarpWalkOut wwo{so.ncells, so.nbodies, nullptr, nullptr, ws.cell_list.as<u32>(),
+                        ws.body_list.as<u32>(), spill_c, spill_b, so.split, caps.slot_cells,
+                        caps.slot_bodies, n32};
+  if (ws.walk_warps) {
+    launch_warp_walk<kSlots>(ws, wwo, n32, sc, s, &sc->n_groups, abort);
+  } else {
+    k_walk_split<<<ceil_div(2ull * n, kWalkThreads), kWalkThreads, 0, s>>>(
+        ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
+        ws.gboxf.as<float>(), gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
+        ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort);
+    GTC_LAUNCH_CHECK();
+  }
   k_split_spill<<<nb, kT, 0, s>>>(so, n32, pool_at_c, caps.pool_cells, pool_at_b,
                                   caps.pool_bodies, spill_c, spill_b, sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();
-  WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
-             ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
-  const Task *tasks = ws.tasks.as<Task>();
-  k_walk<kSpill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
-                                   ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1, wo,
-                                   sc, &sc->n_groups, abort);
-  GTC_LAUNCH_CHECK();
+  if (ws.walk_warps) {
+    launch_warp_walk<kSpill>(ws, wwo, n32, sc, s, &sc->n_groups, abort);
+  } else {
+    WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
+               ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
+    const Task *tasks = ws.tasks.as<Task>();
+    k_walk<kSpill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
+                                     ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1,
+                                     wo, sc, &sc->n_groups, abort);
+    GTC_LAUNCH_CHECK();
+  }
   k_split_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, so, spill_c, spill_b,
                                     ws.groups.as<uint4>(), sc, &sc->n_groups, abort);
   GTC_LAUNCH_CHECK();

@@ -90,6 +90,13 @@ struct Workspace {
   int key_words = 1;
   int sort_levels = 0;        // key levels the next eager build sorts first (0: all 21)
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
+  // The plain walk by warps (one warp per group, 32 node tests per step);
+  // false: by threads (two per group in the one pass, one in count + fill).
+  bool walk_warps = true;
+  // The current lists hold each group's entries in walk-step order rather
+  // than the reference's visiting order (exports sort them back).
+  bool lists_unordered = false;
+  DeviceBuffer walk_next;     // the warp walk's group counter
   // One-pass walk: group g's lists start at g * slot_cells and g *
   // slot_bodies (capacities sized from the previous walk's longest lists);
   // 0 until a walk has measured them. `gapped`: the current lists use that

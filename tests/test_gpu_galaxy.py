@@ -219,3 +219,35 @@ def test_one_pass_walk_spills_outgrown_groups(gtc, oracle):
                                        pack=True)
     assert compare_lists(d, d["nodes"], lists, nodes) == []
     assert np.array_equal(acc, ref_acc) and np.array_equal(pot, ref_pot)
+
+
+def test_warp_walk_matches_thread_walk(gtc, oracle):
+    """The walk by warps (the default) and by threads (option walk_warps 0)
+    test the same nodes: the exported lists are identical and in the
+    reference's order, so are the counters, and the forces differ by
+    summation order only. Two solves each: count + fill, then one pass."""
+    pos, _, mass, _ = gtc.make_galaxy(100_000, seed=4)
+    kw = dict(G=1.0, eps=0.025, quadrupole=True, theta=0.75, group_size=32, leaf_size=8,
+              pack=True)
+    res = {}
+    for warps in (1, 0):
+        c = gtc.Context(0)
+        try:
+            c.set_option("walk_warps", warps)
+            for _ in range(2):
+                acc, pot = c.group_force(pos, mass, **kw)
+                res[(warps, c.stats()["list_passes"])] = (acc, pot, c.export(), c.stats())
+        finally:
+            c.close()
+    nodes, order, lists = oracle.lists(pos, mass, theta=0.75, group_size=32, leaf_size=8, pack=True)
+    for passes in (2, 1):
+        (aw, pw, dw, sw), (at, pt, dt, st) = res[(1, passes)], res[(0, passes)]
+        for k in ("groups", "cell_list", "body_list"):
+            assert np.array_equal(dw[k], dt[k]), (passes, k)
+        assert compare_lists(dw, dw["nodes"], lists, nodes) == []
+        for k in ("cell_interactions", "body_interactions", "max_list", "walk_tests_fp64",
+                  "walk_nodes"):
+            assert sw[k] == st[k], (passes, k)
+        err = rel_errors(aw, at)
+        assert np.median(err) < 1e-6 and err.max() < 1e-4
+        assert np.abs(pw / pt - 1).max() < 1e-5
