@@ -64,6 +64,8 @@ def parse():
                     help="skip the learned-criterion measurement")
     ap.add_argument("--no-200k", action="store_true",
                     help="skip the N = 200k group and direct lines")
+    ap.add_argument("--only-direct", action="store_true",
+                    help="the tiled FP32 direct kernel on --n bodies only (for profiler runs)")
     ap.add_argument("--only-steps", action="store_true",
                     help="warm-up and timed steps only (for profiler launch lists)")
     ap.add_argument("--learned-steps", action="store_true",
@@ -436,10 +438,39 @@ def measure_learned(gtc, n, dpos, dmass, dacc, dpot, flush, stream, args, idx, r
             "gpu_launches": sum(s["kernel_launches"] for s in stats)}
 
 
+def run_direct_only(args):
+    """The direct kernel alone on the galaxy of --n bodies: warm-up and timed
+    launches through gtc_direct_force_device, one JSON line."""
+    import torch
+    import __graft_entry__
+    gtc = __graft_entry__.load_package().gtc
+    n = args.n
+    pos, _, mass = galaxy(n)
+    dev = torch.device("cuda", 0)
+    dpos, dmass = torch.from_numpy(pos).to(dev), torch.from_numpy(mass).to(dev)
+    dacc = torch.empty((n, 3), dtype=torch.float64, device=dev)
+    dpot = torch.empty(n, dtype=torch.float64, device=dev)
+    with gtc.Context(0) as c:
+        for _ in range(warmup_steps(args)):
+            c.direct_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                                  dpot.data_ptr(), **SOLVER)
+        ms = []
+        for _ in range(args.steps):
+            c.direct_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
+                                  dpot.data_ptr(), **SOLVER)
+            ms.append(c.stats()["eval_kernel_ms"])
+    k = statistics.mean(ms)
+    print(json.dumps({"direct_n": n, "kernel_ms": round(k, 4), "steps": args.steps,
+                      "tflops": round(FLOPS_BODY * n * (n - 1) / (k * 1e-3) / 1e12, 2)}),
+          flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_direct:
+        return run_direct_only(args)
     import torch
     rank, local_rank, world = dist_info()
     torch.cuda.set_device(local_rank)

@@ -36,6 +36,7 @@ struct gtc_context {
   gtc::u32 walk_budget = gtc::kLearnedWalkBudget;  // learned walk: nodes a thread tests before
   gtc::u32 pair_budget = gtc::kLearnedPairBudget;  // a warp takes over, round 0 / later (0: all)
   bool read_every_round = false;    // learned walk: no rounds walked before the first read back
+  bool learned_warps = true;        // learned walk: rounds by warps (else threads per part)
   gtc::DeviceBuffer diag;           // diagnostics partial sums
   double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes
 };

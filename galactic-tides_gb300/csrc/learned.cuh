@@ -125,6 +125,7 @@ struct LearnedScratch {
                                     // the first of their rows
   DeviceBuffer q[2], dec[2];        // deferred (group, node) rows and the network's decisions
   DeviceBuffer cont;                // round-0 walks handed on to warps
+  DeviceBuffer next;                // the warp rounds' group counter
   // per-group slots of the three parts of round 0 (0: not sized yet) and
   // of deferred pairs
   u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
@@ -133,7 +134,8 @@ struct LearnedScratch {
   // one read per round)
   u32 rounds = 0, row_cap = 0;
   void release() {
-    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1], &cont})
+    for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1], &cont,
+                            &next})
       b->release();
     for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
     slot_pend = 0;
@@ -155,6 +157,7 @@ struct LearnedWalk {
   u32 walk_budget = kLearnedWalkBudget;  // round 0: nodes a thread tests before a warp takes over
   u32 pair_budget = kLearnedPairBudget;  // later rounds: the same
   bool plan_rounds = true;  // walk the last call's rounds before reading anything back
+  bool warps = true;        // each round by warps, one per group (else threads per part)
 };
 
 // Per-node features (after build_tree).

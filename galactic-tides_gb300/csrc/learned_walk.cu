@@ -291,6 +291,7 @@ struct GArgs {
   const u32 *roff;          // and each (part, group)'s first row (kParts ng + 1)
   uint4 *cont;              // round-0 walks handed on: (part * ng + group, next node, end)
   u32 budget;               // nodes a thread tests before handing on (this round)
+  u32 *next;                // the warp rounds' group counter
   Scalars *sc;
 };
 
@@ -610,6 +611,186 @@ __global__ void __launch_bounds__(kContWarps * 32) k_lcont(GArgs a, bool later) 
   }
 }
 
+// A round by warps: one warp per group, the group's whole walk in part 0's
+// slots (parts 1 and 2 stay empty). The warp keeps the nodes still to visit
+// as a stack of index ranges (as k_lcont does): round 0 starts from the
+// root's children; a later round from the pairs the group deferred in the
+// last round, each with the network's decision in place of the range's end
+// (accepted: the cell; opened: its subtree). Each step the lanes test the
+// first node of the 32 ranges on top; entries reach the lists in step order,
+// lane order within a step (fixed for given inputs), and the pairs deferred
+// now go to the group's pend slot for the next round.
+constexpr int kLWarps = 4;
+constexpr int kLStack = 1024;  // ranges per warp
+
+__global__ void __launch_bounds__(kLWarps * 32) k_lwarp(GArgs a, u32 round) {
+  __shared__ uint2 stack_all[kLWarps][kLStack];
+  const int lane = threadIdx.x & 31;
+  uint2 *stk = stack_all[threadIdx.x >> 5];
+  const unsigned below = (1u << lane) - 1u;
+  if (a.sc->list_overflow) return;  // a buffer was outgrown: the walk is redone
+  const u32 root_end = lskip(a.lrec, 0);
+  const bool root_leaf = a.nchild[0] == 0;
+  u32 visits = 0;
+  u32 mc_max = 0, mb_max = 0, mp_max = 0;
+  bool bad = false;
+  for (;;) {
+    u32 g = 0;
+    if (lane == 0) g = atomicAdd(a.next, 1u);
+    g = __shfl_sync(kFullMask, g, 0);
+    if (g >= a.ng) break;
+    float gf[3], hf[3], acc_d2, open_d2;
+    group_scales(a, g, gf, hf, acc_d2, open_d2);
+    const u32 capc = a.slot_cells[0], capb = a.slot_bodies[0], capp = a.slot_pend;
+    u32 *cl = a.cells + a.cells_at[0] + static_cast<u64>(g) * capc;
+    u32 *bl = a.bodies + a.bodies_at[0] + static_cast<u64>(g) * capb;
+    u32 *pl = a.pend + static_cast<u64>(g) * capp;  // part 0's pend slots come first
+    u64 nc = round ? a.ncells[g] : 0, nb = round ? a.nbodies[g] : 0;
+    u32 np = 0;
+    u32 kp = round ? a.roff[g] : 0u, k1 = round ? a.roff[g + 1] : 0u;
+    int size = 0;
+    if (round == 0) {
+      if (lane == 0) stk[0] = root_leaf ? make_uint2(0u, root_end) : make_uint2(1u, root_end);
+      size = 1;
+    }
+    __syncwarp();
+    while ((size > 0 || kp < k1) && !bad) {
+      if (size < 32 && kp < k1) {  // room: 32 + 64 ranges stay below kLStack - 32
+        const u32 cnt = k1 - kp < 64u ? k1 - kp : 64u;
+        for (u32 j = lane; j < cnt; j += 32)
+          stk[size + cnt - 1 - j] =
+              make_uint2(a.rows[kp + j].y, a.dec[kp + j] ? kPairAccept : kPairOpen);
+        kp += cnt;
+        size += static_cast<int>(cnt);
+        __syncwarp();
+      }
+      if (size > kLStack - 32) {
+        // nearly full (a step adds at most one range per lane): lane 0
+        // walks the range on top alone
+        if (lane == 0) {
+          const uint2 r = stk[size - 1];
+          const bool pair = r.y >= kPairOpen;
+          LWalkState w{nc, nb, np, 0};
+          lwalk_range(a, gf, hf, acc_d2, open_d2, r.x, pair ? lskip(a.lrec, r.x) : r.y,
+                      pair ? static_cast<int>(r.y - kPairOpen) : -1, cl, bl, pl, capc, capb, capp,
+                      ~0u, w);
+          nc = w.nc;
+          nb = w.nb;
+          np = w.np;
+          visits += w.visits;
+        }
+        nc = __shfl_sync(kFullMask, nc, 0);
+        nb = __shfl_sync(kFullMask, nb, 0);
+        np = __shfl_sync(kFullMask, np, 0);
+        --size;
+        __syncwarp();
+        continue;
+      }
+      const int k = size < 32 ? size : 32;
+      const bool act = lane < k;
+      uint2 r = make_uint2(0u, 0u);
+      if (act) r = stk[size - 1 - lane];
+      __syncwarp();
+      size -= k;
+      int verdict = 0;
+      u32 skip = 0, nbody_leaf = 0, first = 0, rend = r.y;
+      if (act) {
+        const float4 *rp = reinterpret_cast<const float4 *>(a.lrec + r.x);
+        const float4 ra = __ldg(rp), rb = __ldg(rp + 1), rc = __ldg(rp + 2);
+        ++visits;
+        skip = __float_as_uint(rc.x);
+        nbody_leaf = __float_as_uint(rc.y);
+        first = __float_as_uint(rc.z);
+        if (r.y >= kPairOpen) {  // a deferred pair: the network's decision, its subtree
+          verdict = static_cast<int>(r.y - kPairOpen);
+          rend = skip;
+        } else {
+          verdict = lverdict(ra, rb, rc, gf, hf, acc_d2, open_d2);
+        }
+      }
+      const u32 nbody = nbody_leaf & 0x7fffffffu;
+      const bool leaf = (nbody_leaf >> 31) != 0;
+      const bool is_cell = act && verdict == 1 && nbody > kFewBodies;
+      const bool is_pend = act && verdict == 2;
+      const u32 nbo = act && ((verdict == 1 && nbody <= kFewBodies) || (verdict == 0 && leaf))
+                          ? nbody : 0u;
+      const unsigned bc = __ballot_sync(kFullMask, is_cell), bp = __ballot_sync(kFullMask, is_pend);
+      if (is_cell) {
+        const u64 at = nc + __popc(bc & below);
+        if (at < capc) cl[at] = r.x;
+      }
+      if (is_pend) {
+        const u64 at = np + __popc(bp & below);
+        if (at < capp) pl[at] = r.x;
+      }
+      u32 incl = nbo;  // bodies: inclusive scan over the lanes
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 tt = __shfl_up_sync(kFullMask, incl, o);
+        if (lane >= o) incl += tt;
+      }
+      for (u32 j = 0; j < nbo; ++j) {
+        const u64 at = nb + (incl - nbo) + j;
+        if (at < capb) bl[at] = first + j;
+      }
+      nc += __popc(bc);
+      np += __popc(bp);
+      nb += __shfl_sync(kFullMask, incl, 31);
+      // the next ranges: the opened node's children [r.x + 1, skip) above
+      // the rest of its range [skip, r.y)
+      bool has_rest = false, has_kids = false;
+      const u32 kids_end = skip < rend ? skip : rend;
+      if (act) {
+        if (skip <= r.x) {  // malformed tree: never loop
+          bad = true;
+        } else {
+          has_rest = skip < rend;
+          has_kids = verdict == 0 && !leaf && r.x + 1 < kids_end;
+        }
+      }
+      const u32 npush = (has_rest ? 1u : 0u) + (has_kids ? 1u : 0u);
+      u32 from = npush;  // pushes of this lane and the lanes above it
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const u32 tt = __shfl_down_sync(kFullMask, from, o);
+        if (lane + o < 32) from += tt;
+      }
+      const u32 base = static_cast<u32>(size) + from - npush;
+      if (has_rest) stk[base] = make_uint2(skip, rend);
+      if (has_kids) stk[base + (has_rest ? 1u : 0u)] = make_uint2(r.x + 1, kids_end);
+      size += static_cast<int>(__shfl_sync(kFullMask, from, 0));
+      bad = __any_sync(kFullMask, bad);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      a.ncells[g] = nc;
+      a.nbodies[g] = nb;
+      a.pcount[g] = np;
+      if (round == 0) {  // parts 1 and 2 hold nothing
+        for (int part = 1; part < kParts; ++part) {
+          a.ncells[static_cast<u64>(part) * a.ng + g] = 0;
+          a.nbodies[static_cast<u64>(part) * a.ng + g] = 0;
+        }
+      }
+      for (int part = 1; part < kParts; ++part) a.pcount[static_cast<u64>(part) * a.ng + g] = 0;
+      if (nc > capc || nb > capb || np > capp) atomicOr(&a.sc->list_overflow, 1u);
+    }
+    auto clamp = [](u64 v) { return static_cast<u32>(v < 0xffffffffull ? v : 0xffffffffull); };
+    mc_max = max(mc_max, clamp(nc));
+    mb_max = max(mb_max, clamp(nb));
+    mp_max = max(mp_max, np);
+    __syncwarp();
+  }
+  const u32 sv = __reduce_add_sync(kFullMask, visits);
+  if (lane == 0) {
+    if (bad) atomicOr(&a.sc->error, 1u);
+    atomicMax(&a.sc->lmax_cells[0], mc_max);
+    atomicMax(&a.sc->lmax_bodies[0], mb_max);
+    atomicMax(&a.sc->max_pend, mp_max);
+    atomicAdd(&a.sc->walk_nodes, static_cast<unsigned long long>(sv));
+  }
+}
+
 // A later round, kParts threads per group: thread (part, group) takes the
 // pairs its part deferred in the last round, in order, with the network's
 // decisions, appends to the part's slot and defers into the part's pend
@@ -827,8 +1008,12 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   LearnedScratch &ls = *lw.scratch;
   if (ls.slot_cells[0] == 0) {  // the first learned walk: the theta walk's slots to start with
     for (int k = 0; k < kParts; ++k) {
-      ls.slot_cells[k] = std::max<u32>(ws.slot_cells / 2, 256);
-      ls.slot_bodies[k] = std::max<u32>(ws.slot_bodies / 2, 256);
+      // the warp rounds write a group's whole lists into part 0
+      const bool used = !lw.warps || k == 0;
+      ls.slot_cells[k] = used ? std::max<u32>(lw.warps ? ws.slot_cells : ws.slot_cells / 2, 256)
+                              : learned_slot(0);
+      ls.slot_bodies[k] = used ? std::max<u32>(lw.warps ? ws.slot_bodies : ws.slot_bodies / 2, 256)
+                               : learned_slot(0);
     }
     ls.slot_pend = 256;
   }
@@ -861,6 +1046,11 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   // warps that take the handed-on walks in turn: a few per SM
   const u32 cont_blocks = static_cast<u32>(std::max(1, sms) * 4);
+  // the warp rounds: enough warps to fill the GPU, groups from a counter
+  const u32 warp_blocks = static_cast<u32>(
+      std::max<u64>(1, std::min<u64>(ceil_div(ng, kLWarps), 8ull * std::max(1, sms))));
+  ls.next.ensure(sizeof(u32));
+  a.next = ls.next.as<u32>();
   u32 rounds = 0;  // rounds walked
   for (int attempt = 0;; ++attempt) {
     u64 c_at = 0, b_at = 0;
@@ -895,18 +1085,25 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     auto walk_round = [&](u32 r) {
       if (r >= static_cast<u32>(kMaxRounds))
         throw RuntimeError("learned walk: more rounds than the tree has levels");
-      GTC_CUDA(cudaMemsetAsync(&sc->lcont, 0, 2 * sizeof(u32), s));
-      a.budget = r == 0 ? lw.walk_budget : lw.pair_budget;
-      if (r == 0) {
-        k_lround0<<<rb, kRoundThreads, 0, s>>>(a);
-      } else {
+      if (r > 0) {
         a.rows = ls.q[qsel].as<uint2>();
         a.dec = ls.dec[qsel].as<u8>();
-        k_lround<<<rb, kRoundThreads, 0, s>>>(a);
       }
-      GTC_LAUNCH_CHECK();
-      k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, r > 0);
-      GTC_LAUNCH_CHECK();
+      if (lw.warps) {
+        GTC_CUDA(cudaMemsetAsync(a.next, 0, sizeof(u32), s));
+        k_lwarp<<<warp_blocks, kLWarps * 32, 0, s>>>(a, r);
+        GTC_LAUNCH_CHECK();
+      } else {
+        GTC_CUDA(cudaMemsetAsync(&sc->lcont, 0, 2 * sizeof(u32), s));
+        a.budget = r == 0 ? lw.walk_budget : lw.pair_budget;
+        if (r == 0)
+          k_lround0<<<rb, kRoundThreads, 0, s>>>(a);
+        else
+          k_lround<<<rb, kRoundThreads, 0, s>>>(a);
+        GTC_LAUNCH_CHECK();
+        k_lcont<<<cont_blocks, kContWarps * 32, 0, s>>>(a, r > 0);
+        GTC_LAUNCH_CHECK();
+      }
       exclusive_scan_u32(a.pcount, roff, nparts, roff + nparts, ws.scan_tmp, s);
     };
     // the round's deferred pairs as rows, and the network's decisions on

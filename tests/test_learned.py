@@ -234,43 +234,48 @@ def _sorted_per_group(values, starts, ends):
 
 
 @gpu
-def test_walk_budget_only_reorders_the_lists(gtc):
-    """Walks handed on to warps (budget 3 in round 0 and 1 in later rounds:
-    nearly every walk; 64 and 8: the long ones) give each group the same
-    cells, bodies and network rows as threads that walk to the end, so
-    forces differ by summation order only."""
+def test_walk_budget_and_warps_only_reorder_the_lists(gtc):
+    """The rounds by threads per part (learned_warps 0) with walks handed on
+    to warps (budget 3 in round 0 and 1 in later rounds: nearly every walk;
+    64 and 8: the long ones), and the rounds by warps (the default), give
+    each group the same cells, bodies and network rows as threads that walk
+    to the end, so forces differ by summation order only."""
     pos, _, mass, _ = gtc.make_galaxy(60_000, seed=4)
     kw = dict(SOLVER, criterion=gtc.CRITERION_LEARNED, alpha=0.0015)
     runs = {}
-    for budget in (0, 3, 64):
+    for warps, budget in ((0, 0), (0, 3), (0, 64), (1, 0)):
         with _learned_ctx(gtc) as c:
+            c.set_option("learned_warps", warps)
             c.set_option("learned_walk_budget", budget)
             c.set_option("learned_pair_budget", (budget + 7) // 8)
             c.group_force(pos, mass, **kw)
             acc, _ = c.group_force(pos, mass, **kw)
-            runs[budget] = (acc, c.stats(), c.export())
-            assert runs[budget][1]["criterion_used"] == gtc.CRITERION_LEARNED
-    acc0, st0, dev0 = runs[0]
+            runs[(warps, budget)] = (acc, c.stats(), c.export())
+            assert runs[(warps, budget)][1]["criterion_used"] == gtc.CRITERION_LEARNED
+    acc0, st0, dev0 = runs[(0, 0)]
     g0 = dev0["groups"].astype(np.int64)
     want_c = _sorted_per_group(dev0["cell_list"], g0[:, 2], g0[:, 3])
     want_b = _sorted_per_group(dev0["body_list"], g0[:, 4], g0[:, 5])
-    for budget in (3, 64):
-        acc, st, dev = runs[budget]
-        for key in ("cell_interactions", "body_interactions", "mlp_rows", "walk_nodes"):
-            assert st[key] == st0[key], (budget, key)
+    for key in ((0, 3), (0, 64), (1, 0)):
+        acc, st, dev = runs[key]
+        for k in ("cell_interactions", "body_interactions", "mlp_rows", "walk_nodes",
+                  "list_passes"):
+            assert st[k] == st0[k], (key, k)
         g = dev["groups"].astype(np.int64)
         assert np.array_equal(g[:, :2], g0[:, :2])
         assert np.array_equal(_sorted_per_group(dev["cell_list"], g[:, 2], g[:, 3]), want_c)
         assert np.array_equal(_sorted_per_group(dev["body_list"], g[:, 4], g[:, 5]), want_b)
         _check_list_invariants(dev, len(mass))
         err = rel_errors(acc, acc0)
-        assert np.median(err) < 1e-6 and np.max(err) < 1e-4, budget
-    with _learned_ctx(gtc) as c:  # the same budget twice: bitwise the same forces
-        c.set_option("learned_walk_budget", 3)
-        c.set_option("learned_pair_budget", 1)
-        c.group_force(pos, mass, **kw)
-        again, _ = c.group_force(pos, mass, **kw)
-    assert np.array_equal(again, runs[3][0])
+        assert np.median(err) < 1e-6 and np.max(err) < 1e-4, key
+    for warps, budget in ((0, 3), (1, 0)):  # the same settings twice: bitwise the same forces
+        with _learned_ctx(gtc) as c:
+            c.set_option("learned_warps", warps)
+            c.set_option("learned_walk_budget", budget)
+            c.set_option("learned_pair_budget", (budget + 7) // 8)
+            c.group_force(pos, mass, **kw)
+            again, _ = c.group_force(pos, mass, **kw)
+        assert np.array_equal(again, runs[(warps, budget)][0])
 
 
 @gpu
