@@ -108,6 +108,10 @@ def _load():
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_sample_indices": (None, [U64, U64, U64, P]),
         "gtc_get_stage_times": (I, [V, C.POINTER(StageTimes)]),
+        "gtc_write_snapshot": (I, [C.c_char_p, U64, P, P, P, P, P, P, D, C.c_char_p]),
+        "gtc_snapshot_info": (I, [C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_double), P,
+                                  C.POINTER(C.c_uint64)]),
+        "gtc_read_snapshot": (I, [C.c_char_p, U64, P, P, P, P, P, P, P]),
         "gtc_measure_fp32_peak": (I, [V, C.POINTER(C.c_double)]),
         "gtc_set_option": (I, [V, C.c_char_p, D]),
         "gtc_learned_add_samples": (I, [V, P, P, U64, C.POINTER(GravityParams), D, D, U64, U32,
@@ -425,6 +429,49 @@ class Context:
 # the synthetic galaxies live in galaxy.py (pure numpy); re-exported here
 from .galaxy import (GalaxyModel, galaxy_model, make_encounter, make_galaxy,  # noqa: E402,F401
                      orient, parabolic_orbit)
+
+
+# ---- snapshots (raw binary; the reference's GADGET HDF5 content) -------------
+
+def _check_free(rc):
+    if rc != GTC_OK:
+        msg = lib.gtc_last_error(None).decode()
+        raise (GtcInvalidArgument if rc == GTC_INVALID_ARGUMENT else GtcError)(rc, msg)
+
+
+def write_snapshot(path, pos, vel, mass, ids=None, types=None, pot=None, time=0.0,
+                   metadata=None):
+    """Writes a snapshot (gtc_write_snapshot); metadata: a dict of strings."""
+    pos = np.ascontiguousarray(pos, np.float64)
+    vel = np.ascontiguousarray(vel, np.float64)
+    mass = np.ascontiguousarray(mass, np.float64)
+    n = mass.shape[0]
+    ids = None if ids is None else np.ascontiguousarray(ids, np.uint64)
+    types = None if types is None else np.ascontiguousarray(types, np.uint8)
+    pot = None if pot is None else np.ascontiguousarray(pot, np.float64)
+    meta = "".join(f"{k}={v}\n" for k, v in (metadata or {}).items()).encode()
+    p = lambda a: None if a is None else _ptr(a)
+    _check_free(lib.gtc_write_snapshot(str(path).encode(), n, _ptr(pos), _ptr(vel), _ptr(mass),
+                                       p(ids), p(types), p(pot), float(time), meta))
+
+
+def read_snapshot(path):
+    """-> dict(pos, vel, mass, ids, types, pot, time, count_by_type, metadata)."""
+    n, t, mb = C.c_uint64(), C.c_double(), C.c_uint64()
+    counts = np.zeros(6, np.uint64)
+    path = str(path).encode()
+    _check_free(lib.gtc_snapshot_info(path, C.byref(n), C.byref(t), _ptr(counts), C.byref(mb)))
+    n = n.value
+    out = dict(pos=np.empty((n, 3)), vel=np.empty((n, 3)), mass=np.empty(n),
+               ids=np.empty(n, np.uint64), types=np.empty(n, np.uint8), pot=np.empty(n))
+    meta = C.create_string_buffer(max(1, mb.value))
+    _check_free(lib.gtc_read_snapshot(path, n, _ptr(out["pos"]), _ptr(out["vel"]),
+                                      _ptr(out["mass"]), _ptr(out["ids"]), _ptr(out["types"]),
+                                      _ptr(out["pot"]), meta))
+    text = meta.raw[:mb.value].decode()
+    out.update(time=t.value, count_by_type=counts,
+               metadata=dict(line.split("=", 1) for line in text.splitlines() if "=" in line))
+    return out
 
 
 def sample_indices(n, m=4096, seed=1):

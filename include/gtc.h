@@ -235,6 +235,30 @@ gtc_status gtc_get_stage_times(gtc_context *ctx, gtc_stage_times *out);
  * needs no device. */
 void gtc_sample_indices(uint64_t n, uint64_t m, uint64_t seed, uint64_t *out);
 
+/* ---- snapshots (src/snapshot_io.cpp) ------------------------------------
+ *
+ * The reference writes GADGET-style HDF5 snapshots (write_snapshot /
+ * read_snapshot, include/galactic_tides/snapshot_io.h:17-23); HDF5 is not
+ * available here, so these keep the same content in a raw binary file
+ * (layout in galactic-tides_gb300/host/snapshot.cpp): positions, velocities,
+ * masses, IDs, GADGET types (0..5), potentials, the time, the count of each
+ * type and free-form "key=value" metadata lines. Host arrays. Particles are
+ * written grouped by type in ascending type order (stable within a type), as
+ * the reference's reader returns them. id NULL: IDs 0..n-1 in the caller's
+ * order; type NULL: all halo (1); pot NULL: zeros. Errors:
+ * gtc_last_error(NULL). */
+gtc_status gtc_write_snapshot(const char *path, uint64_t n, const double *pos, const double *vel,
+                              const double *mass, const uint64_t *id, const uint8_t *type,
+                              const double *pot, double time, const char *metadata);
+/* The header of a snapshot: particle count, time, count of each type,
+ * metadata length in bytes (NULL to skip any). */
+gtc_status gtc_snapshot_info(const char *path, uint64_t *n, double *time,
+                             uint64_t count_by_type[6], uint64_t *metadata_bytes);
+/* Reads a snapshot of n particles (n must match the file; NULL skips an
+ * array); metadata receives metadata_bytes bytes, not terminated. */
+gtc_status gtc_read_snapshot(const char *path, uint64_t n, double *pos, double *vel, double *mass,
+                             uint64_t *id, uint8_t *type, double *pot, char *metadata);
+
 /* ---- time integration (src/integrator.cpp) ----------------------------- */
 
 /* Diagnostics (integrator.h:46-58): potential = 0.5 sum m phi, total =
