@@ -548,6 +548,49 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
   ctx->stats.kernel_launches = gtc::launches_so_far() - launches0;
 }
 
+// compute_gravity_tree (src/gravity.cpp:7-26) on device arrays: the tree,
+// then every body's own walk (Octree::accel_pot).
+void tree_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
+                const gtc::SolverParams &sp, double *acc, double *pot) {
+  if (n > 0xffffffffull) throw gtc::RuntimeError("too many particles for the 32 bit GPU indices");
+  cudaStream_t s = ctx->stream;
+  gtc::Workspace &ws = ctx->ws;
+  ctx->have_group = false;
+  ctx->stats = gtc_stats{};
+  const unsigned long long launches0 = gtc::launches_so_far();
+  if (n == 0) return;
+  GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
+  {
+    const gtc::SideJoin side_join{ws, s};
+    gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
+    gtc::join_side(ws, s);  // the walk reads the moments
+  }
+  GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
+  ctx->tree_counts.ensure(2 * sizeof(unsigned long long));
+  GTC_CUDA(cudaMemsetAsync(ctx->tree_counts.ptr, 0, 2 * sizeof(unsigned long long), s));
+  GTC_CUDA(cudaEventRecord(ctx->ev[4], s));
+  gtc::tree_walk_forces(ws, sp, acc, pot, ctx->tree_counts.as<unsigned long long>(), s);
+  GTC_CUDA(cudaEventRecord(ctx->ev[5], s));
+  unsigned long long counts[2] = {0, 0};
+  GTC_CUDA(cudaMemcpyAsync(counts, ctx->tree_counts.ptr, sizeof counts, cudaMemcpyDeviceToHost,
+                           s));
+  GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
+                           cudaMemcpyDeviceToHost, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  if (ctx->host_sc->error != 0)
+    throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                            std::to_string(ctx->host_sc->error) + ")");
+  gtc_stats &st = ctx->stats;
+  st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
+  st.evaluate_ms = st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
+  st.total_ms = elapsed(ctx->ev[0], ctx->ev[5]);
+  st.cell_interactions = counts[0];
+  st.body_interactions = counts[1];
+  st.depth = ctx->host_sc->depth;
+  st.n_nodes = static_cast<u32>(ws.n_nodes);
+  st.kernel_launches = gtc::launches_so_far() - launches0;
+}
+
 }  // namespace
 
 namespace gtc {
@@ -855,6 +898,46 @@ gtc_status gtc_direct_force(gtc_context *ctx, const double *pos, const double *m
       gtc::k_unpack_direct<<<gtc::ceil_div(n, 256), 256, 0, s>>>(
           ws.out.as<float4>(), static_cast<u32>(n), ws.acc.as<double>(), ws.pot.as<double>());
       GTC_LAUNCH_CHECK();
+      GTC_CUDA(cudaMemcpyAsync(acc, ws.acc.ptr, n * 24, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaMemcpyAsync(pot, ws.pot.ptr, n * 8, cudaMemcpyDeviceToHost, s));
+      GTC_CUDA(cudaStreamSynchronize(s));
+    }
+  });
+}
+
+gtc_status gtc_tree_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                 uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                 double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, false);
+    if (!(sp.theta > 0)) throw gtc::InvalidArgument("theta must be positive");
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    tree_force(ctx, pos, mass, n, sp, acc, pot);
+  });
+}
+
+gtc_status gtc_tree_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                          const gtc_gravity_params *gp, double *acc, double *pot) {
+  return guarded(ctx, [&] {
+    const gtc::SolverParams sp = check_params(gp, false);
+    if (!(sp.theta > 0)) throw gtc::InvalidArgument("theta must be positive");
+    if (n > 0 && (!pos || !mass || !acc || !pot))
+      throw gtc::InvalidArgument("pos, mass, acc and pot are required");
+    gtc::Workspace &ws = ctx->ws;
+    cudaStream_t s = ctx->stream;
+    const u64 nn = std::max<u64>(n, 1);
+    ws.pos.ensure(nn * 24);
+    ws.mass.ensure(nn * 8);
+    ws.acc.ensure(nn * 24);
+    ws.pot.ensure(nn * 8);
+    if (n) {
+      GTC_CUDA(cudaMemcpyAsync(ws.pos.ptr, pos, n * 24, cudaMemcpyHostToDevice, s));
+      GTC_CUDA(cudaMemcpyAsync(ws.mass.ptr, mass, n * 8, cudaMemcpyHostToDevice, s));
+    }
+    tree_force(ctx, ws.pos.as<double>(), ws.mass.as<double>(), n, sp, ws.acc.as<double>(),
+               ws.pot.as<double>());
+    if (n) {
       GTC_CUDA(cudaMemcpyAsync(acc, ws.acc.ptr, n * 24, cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaMemcpyAsync(pot, ws.pot.ptr, n * 8, cudaMemcpyDeviceToHost, s));
       GTC_CUDA(cudaStreamSynchronize(s));

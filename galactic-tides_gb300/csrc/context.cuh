@@ -38,6 +38,7 @@ struct gtc_context {
   bool read_every_round = false;    // learned walk: no rounds walked before the first read back
   bool learned_warps = true;        // learned walk: rounds by warps (else threads per part)
   gtc::DeviceBuffer diag;           // diagnostics partial sums
+  gtc::DeviceBuffer tree_counts;    // per-particle walk: cell and particle interactions
   double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes
 };
 

@@ -313,6 +313,11 @@ void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *a
                            const Scalars *sc, cudaStream_t s);
 
 // Direct summation kernels.
+// Octree::accel_pot for every body on the built tree (FP64, the reference's
+// per-particle walk): acc (n x 3) and pot in caller order; counts[0..1] +=
+// cell and particle interactions.
+void tree_walk_forces(Workspace &ws, const SolverParams &sp, double *acc, double *pot,
+                      unsigned long long *counts, cudaStream_t s);
 // The tiled FP32 direct sum; `scratch` holds per-source-slice partial sums.
 void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
                  DeviceBuffer &scratch, cudaStream_t s);

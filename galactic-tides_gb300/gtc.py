@@ -105,6 +105,8 @@ def _load():
         "gtc_direct_force": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
         "gtc_direct_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
         "gtc_direct_fp64_device": (I, [V, P, P, U64, P, U64, D, D, P, P]),
+        "gtc_tree_force": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
+        "gtc_tree_force_device": (I, [V, P, P, U64, C.POINTER(GravityParams), P, P]),
         "gtc_get_stats": (I, [V, C.POINTER(Stats)]),
         "gtc_sample_indices": (None, [U64, U64, U64, P]),
         "gtc_get_stage_times": (I, [V, C.POINTER(StageTimes)]),
@@ -240,6 +242,19 @@ class Context:
         gp = gravity_params(**kw)
         self._check(lib.gtc_direct_force(self.h, _ptr(pos), _ptr(mass), n, C.byref(gp),
                                          _ptr(acc), _ptr(pot)))
+        return acc, pot
+
+    def tree_force(self, pos, mass, **kw):
+        """compute_gravity_tree on the device (Octree::accel_pot per body,
+        FP64), host arrays."""
+        pos = _f64(pos, (-1, 3))
+        mass = _f64(mass)
+        n = mass.shape[0]
+        acc = np.empty((n, 3))
+        pot = np.empty(n)
+        gp = gravity_params(**kw)
+        self._check(lib.gtc_tree_force(self.h, _ptr(pos), _ptr(mass), n, C.byref(gp), _ptr(acc),
+                                       _ptr(pot)))
         return acc, pot
 
     def direct(self, bodies, G=1.0, eps2=0.0):

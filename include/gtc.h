@@ -180,6 +180,21 @@ gtc_status gtc_direct_force_device(gtc_context *ctx, const double *pos, const do
                                    uint64_t n, const gtc_gravity_params *gp, double *acc,
                                    double *pot);
 
+/* compute_gravity_tree (src/gravity.cpp:7-26), the `gravity = tree`
+ * solver, on the device: the octree, then every body's own walk,
+ * Octree::accel_pot (src/octree.cpp:275-344) -- the Barnes (1994) offset
+ * criterion with gp->theta, quadrupoles if gp->quadrupole, bodies of opened
+ * leaves except the body itself -- in FP64 with the reference's operand
+ * order, so the forces are the reference's bit for bit. gp->group_size is
+ * not used. gtc_get_stats gives the interactions (cell_interactions,
+ * body_interactions = particle interactions). Host pointers (copies are
+ * part of the call) or device pointers on the context's stream. */
+gtc_status gtc_tree_force(gtc_context *ctx, const double *pos, const double *mass, uint64_t n,
+                          const gtc_gravity_params *gp, double *acc, double *pot);
+gtc_status gtc_tree_force_device(gtc_context *ctx, const double *pos, const double *mass,
+                                 uint64_t n, const gtc_gravity_params *gp, double *acc,
+                                 double *pot);
+
 /* FP64 direct summation for the m targets idx[0..m) against all n bodies:
  * compute_gravity_direct (src/gravity.cpp:28-45) on a sample, as the
  * reference bench's accuracy judge (apps/galactic_tides_bench.cpp:74-95).
