@@ -535,7 +535,8 @@ void direct_force(gtc_context *ctx, const double *pos, const double *mass, u64 n
     ws.out.ensure(n * sizeof(float4));
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
     gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), static_cast<float>(sp.G),
-                     static_cast<float>(sp.eps * sp.eps), ws.out.as<float4>(), ws.direct_part, s);
+                     static_cast<float>(sp.eps * sp.eps), ws.out.as<float4>(), ws.direct_part, s,
+                     ws.direct_targets);
   } else {
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
   }
@@ -742,7 +743,7 @@ gtc_status gtc_direct(gtc_context *ctx, const gtc_float4 *bodies, const gtc_kern
     GTC_CUDA(cudaMemcpyAsync(ws.bodies.ptr, bodies, n * 16, cudaMemcpyHostToDevice, s));
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
     gtc::direct_fp32(ws.bodies.as<float4>(), static_cast<u32>(n), p->G, p->eps2,
-                     ws.out.as<float4>(), ws.direct_part, s);
+                     ws.out.as<float4>(), ws.direct_part, s, ws.direct_targets);
     GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
     GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));
@@ -987,9 +988,13 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
       ctx->learned_warps = value != 0;
       ctx->lscratch.release();  // slots sized for the other layout
     } else if (key == "walk_warps") {
-      if (value != 0 && value != 1) throw gtc::InvalidArgument("walk_warps must be 0 or 1");
-      ctx->ws.walk_warps = value != 0;
+      if (value != 0 && value != 1 && value != -1)
+        throw gtc::InvalidArgument("walk_warps must be -1, 0 or 1");
+      ctx->ws.walk_mode = static_cast<int>(value);
       ctx->ws.slot_cells = 0;  // slots sized by the other walk would not fit: count first
+    } else if (key == "direct_targets") {
+      if (value != 2 && value != 4) throw gtc::InvalidArgument("direct_targets must be 2 or 4");
+      ctx->ws.direct_targets = static_cast<int>(value);
     } else if (key == "stage_events") {
       if (value != 0 && value != 1) throw gtc::InvalidArgument("stage_events must be 0 or 1");
       ctx->ws.stage_on = value != 0;
@@ -1336,7 +1341,7 @@ gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int
 
 gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double *mass,
                               uint64_t n, const gtc_gravity_params *base,
-                              gtc_gravity_params *best, double *best_ms) {
+                              gtc_gravity_params *best, double *best_ms, int *walk_warps) {
   return guarded(ctx, [&] {
     if (!base || !best) throw gtc::InvalidArgument("base and best parameters are required");
     if (n == 0 || !pos || !mass) throw gtc::InvalidArgument("pos and mass are required");
@@ -1346,25 +1351,63 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
     ws.pot.ensure(n * 8);
     double best_t = 1e300;
     gtc_gravity_params pick = *base;
+    int pick_walk = ws.walk_mode;
+    const int mode0 = ws.walk_mode;
     for (int gs : {8, 16, 24, 32})
-      for (int pack : {0, 1}) {
-        gtc_gravity_params p = *base;
-        p.group_size = gs;
-        p.pack = pack;
-        p.criterion = GTC_CRITERION_THETA;
-        const gtc::SolverParams sp = check_params(&p, true);
-        double t = 0;
-        for (int rep = 0; rep < 4; ++rep) {
-          group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
-          if (rep > 0) t += ctx->stats.total_ms;  // the first warms up
+      for (int pack : {0, gs / 2, (3 * gs) / 4, 1})  // off, thresholds, a group's worth
+        for (int walk : {0, 1}) {
+          gtc_gravity_params p = *base;
+          p.group_size = gs;
+          p.pack = pack;
+          p.criterion = GTC_CRITERION_THETA;
+          const gtc::SolverParams sp = check_params(&p, true);
+          ws.walk_mode = walk;
+          ws.slot_cells = 0;  // slots of another walk or layout: count first
+          double t = 0;
+          for (int rep = 0; rep < 3; ++rep) {
+            group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+            if (rep > 0) t += ctx->stats.total_ms;  // the first warms up
+          }
+          if (t / 2 < best_t) {
+            best_t = t / 2;
+            pick = p;
+            pick_walk = walk;
+          }
         }
-        if (t / 3 < best_t) {
-          best_t = t / 3;
-          pick = p;
-        }
-      }
+    ws.walk_mode = mode0;
+    ws.slot_cells = 0;
     pick.criterion = base->criterion;
     *best = pick;
+    if (best_ms) *best_ms = best_t;
+    if (walk_warps) *walk_warps = pick_walk;
+  });
+}
+
+gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double *mass,
+                               uint64_t n, const gtc_gravity_params *gp, int *targets,
+                               double *best_ms) {
+  return guarded(ctx, [&] {
+    if (n == 0 || !pos || !mass || !gp) throw gtc::InvalidArgument("pos, mass and gp are required");
+    const gtc::SolverParams sp = check_params(gp, false);
+    gtc::Workspace &ws = ctx->ws;
+    ws.acc.ensure(n * 24);
+    ws.pot.ensure(n * 8);
+    double best_t = 1e300;
+    int pick = ws.direct_targets;
+    for (int k : {2, 4}) {
+      ws.direct_targets = k;
+      double t = 0;
+      for (int rep = 0; rep < 3; ++rep) {
+        direct_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+        if (rep > 0) t += ctx->stats.eval_kernel_ms;
+      }
+      if (t / 2 < best_t) {
+        best_t = t / 2;
+        pick = k;
+      }
+    }
+    ws.direct_targets = pick;  // the context keeps the winner
+    if (targets) *targets = pick;
     if (best_ms) *best_ms = best_t;
   });
 }
@@ -1496,7 +1539,7 @@ gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
         }
         if (body_list) {
           for (u32 e = 0; e < q0.w; ++e) body_list[b + e] = bl[bs.at(e)];
-          // and so reaches bodies in increasing tree position
+          // the walk by warps reaches bodies in its own order: canonical
           if (ws.lists_unordered) std::sort(body_list + b, body_list + b + q0.w);
         }
         if (groups) {

@@ -14,8 +14,6 @@ namespace {
 // ------------------------------------------------------------------ FP32
 
 constexpr int kDT = 128;          // threads per block = sources per shared tile
-constexpr int kDR = 4;            // targets per thread
-constexpr int kDTB = kDT * kDR;   // targets per block
 constexpr float kFar = 1e15f;     // padding source: far away, zero mass, adds exactly 0
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
@@ -48,16 +46,20 @@ __device__ __forceinline__ void add_pair(const float4 s0, const float4 s1, const
   pt = __fadd2_rn(pt, gm);
 }
 
-// Block (bx, by) owns targets [bx kDTB, (bx + 1) kDTB) -- thread t the
-// targets bx kDTB + r kDT + t -- and sums the sources of slice by,
+// Block (bx, by) owns targets [bx kR kDT, (bx + 1) kR kDT) -- thread t the
+// targets bx kR kDT + r kDT + t, r < kR (the tile shape: more targets per
+// thread reuse each staged source more, fewer leave registers for more
+// warps) -- and sums the sources of slice by,
 // [by len, (by + 1) len), streamed through shared memory in index order,
 // kDT at a time. Even and odd sources go to the two halves of each sum.
 // Only the tiles holding the block's own targets test j == i. With one
 // slice the sums go straight to `out`, otherwise to part[by][target],
 // added up in slice order by k_direct_sum (deterministic).
+template <int kDR>
 __global__ void __launch_bounds__(kDT)
     k_direct(const float4 *__restrict__ bodies, u32 n, u32 len, float G, float eps2,
              float4 *__restrict__ out) {
+  constexpr u32 kDTB = kDT * kDR;  // targets per block
   __shared__ float4 tile[kDT];  // kDT / 2 source pairs, two float4 each
   const u32 t0 = blockIdx.x * kDTB;
   const u32 j0 = blockIdx.y * len, j1 = min(n, j0 + len);
@@ -204,14 +206,15 @@ __global__ void k_direct64_sum(const double2 *part, u64 m, u32 slices, double *a
 }  // namespace
 
 void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
-                 DeviceBuffer &scratch, cudaStream_t s) {
+                 DeviceBuffer &scratch, cudaStream_t s, int targets) {
   if (n == 0) return;
+  if (targets != 2 && targets != 4) throw InvalidArgument("direct_targets must be 2 or 4");
   int dev = 0, sms = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   // Enough (target block, source slice) units for about 16 per SM, so that
   // blocks of equal work end close together; each slice at least 8 tiles.
-  const u32 tiles = ceil_div(n, kDTB);
+  const u32 tiles = ceil_div(n, kDT * static_cast<u32>(targets));
   u32 slices = std::max<u32>(1, ceil_div(16u * static_cast<u32>(sms), tiles));
   slices = std::min<u32>(slices, std::max<u32>(1, n / (8 * kDT)));
   const u32 len = ceil_div(ceil_div(n, slices), kDT) * kDT;
@@ -221,7 +224,10 @@ void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
     scratch.ensure(static_cast<u64>(slices) * n * sizeof(float4));
     dst = scratch.as<float4>();
   }
-  k_direct<<<dim3(tiles, slices), kDT, 0, s>>>(bodies, n, len, G, eps2, dst);
+  if (targets == 4)
+    k_direct<4><<<dim3(tiles, slices), kDT, 0, s>>>(bodies, n, len, G, eps2, dst);
+  else
+    k_direct<2><<<dim3(tiles, slices), kDT, 0, s>>>(bodies, n, len, G, eps2, dst);
   GTC_LAUNCH_CHECK();
   if (slices > 1) {
     k_direct_sum<<<ceil_div(n, 256), 256, 0, s>>>(dst, n, slices, out);

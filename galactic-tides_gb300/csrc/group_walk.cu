@@ -58,13 +58,16 @@ __global__ void __launch_bounds__(kT)
   u32 ch[8];
   int nc = 0;
   for (u32 c = p + 1; c < nv.skip[p] && nc < 8; c = nv.skip[c]) ch[nc++] = c;
+  // the packing threshold: runs of small siblings hold at most `limit`
+  // bodies (pack 1: a group's worth, the reference's rule)
+  const u32 limit = pack <= 1 ? gs : min(static_cast<u32>(pack), gs);
   bool open = false;
   u32 run_begin = 0, run_end = 0;
   for (int j = nc - 1; j >= 0; --j) {
     const u32 c = ch[j];
     const u32 cb = nv.nbegin[c], ce = nv.nend[c], cc = ce - cb;
     if (cc <= gs) {
-      if (pack && open && (run_end - run_begin) + cc <= gs) {
+      if (pack && open && (run_end - run_begin) + cc <= limit) {
         run_end = ce;
       } else {
         if (open) mark[run_begin] = 1;
@@ -883,6 +886,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   read_scalars(ws, host, s);
   const u32 ng = host->n_groups, ntasks = host->aux;
   ws.n_groups = ng;
+  ws.walk_warps = ws.warps_for(ng);
   const u32 gb = ceil_div(ng, kT);
   k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
@@ -1063,6 +1067,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
   u32 *spill_c = ws.spill.as<u32>(), *spill_b = spill_c + n;
+  ws.walk_warps = ws.warps_for(caps.groups);  // the replays' walk, chosen at capture
   const u64 near_c = static_cast<u64>(caps.groups) * caps.slot_cells;
   const u64 near_b = static_cast<u64>(caps.groups) * caps.slot_bodies;
   const u64 pool_at_c = near_c + static_cast<u64>(caps.groups) * caps.slot_near_cells;

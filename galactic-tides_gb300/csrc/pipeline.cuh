@@ -83,6 +83,7 @@ struct Workspace {
   DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
   DeviceBuffer direct_part;               // direct sum: per-slice partial sums
+  int direct_targets = 4;                 // direct sum: targets per thread (2 or 4)
   RadixScratch radix;
 
   // host-side view of the last build
@@ -90,9 +91,18 @@ struct Workspace {
   int key_words = 1;
   int sort_levels = 0;        // key levels the next eager build sorts first (0: all 21)
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
-  // The plain walk by warps (one warp per group, 32 node tests per step);
-  // false: by threads (two per group in the one pass, one in count + fill).
+  // The plain walk by warps (one warp per group, 32 node tests per step) or
+  // by threads (two per group in the one pass, one in count + fill). Mode
+  // -1 (default) picks warps below kWarpWalkGroups groups: with fewer, the
+  // thread walk leaves most of the GPU idle; with more, its neighbouring
+  // groups walking the same nodes together make it the faster. walk_warps:
+  // the choice of the current lists.
+  int walk_mode = -1;
   bool walk_warps = true;
+  static constexpr u64 kWarpWalkGroups = 40000;
+  bool warps_for(u64 groups) const {
+    return walk_mode > 0 || (walk_mode < 0 && groups < kWarpWalkGroups);
+  }
   // The current lists hold each group's entries in walk-step order rather
   // than the reference's visiting order (exports sort them back).
   bool lists_unordered = false;
@@ -318,9 +328,10 @@ void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *a
 // cell and particle interactions.
 void tree_walk_forces(Workspace &ws, const SolverParams &sp, double *acc, double *pot,
                       unsigned long long *counts, cudaStream_t s);
-// The tiled FP32 direct sum; `scratch` holds per-source-slice partial sums.
+// The tiled FP32 direct sum; `scratch` holds per-source-slice partial sums;
+// `targets` (2 or 4) per thread, the kernel's tile shape.
 void direct_fp32(const float4 *bodies, u32 n, float G, float eps2, float4 *out,
-                 DeviceBuffer &scratch, cudaStream_t s);
+                 DeviceBuffer &scratch, cudaStream_t s, int targets);
 void direct_fp64_sample(const double *pos, const double *mass, u64 n, const u64 *idx, u64 m,
                         double G, double eps, double *acc, double *pot, DeviceBuffer &scratch,
                         cudaStream_t s);

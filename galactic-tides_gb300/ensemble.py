@@ -14,8 +14,8 @@ loaded rank), each rank advances its own set on its own GPU, and the
 per-galaxy results (interactions, p99 error, time) are gathered to rank 0 on
 the host. There is no exchange in the data path.
 
-On each GPU: each galaxy's group_size and sibling packing come from the
-autotuner (gtc_autotune_group); the rank's galaxies then advance together,
+On each GPU: each galaxy's group_size, packing threshold and walk (threads or
+warps) come from the autotuner (gtc_autotune_group); the rank's galaxies then advance together,
 every step one CUDA graph launch (gtc_ensemble_leapfrog). Reported: the
 aggregate interactions/s of the whole job (all ranks' interactions over the
 slowest rank's time), the same galaxies stepped one after another with the
@@ -112,8 +112,8 @@ def combine(shards, steps):
                       "ms_per_step": round(1e3 * s["ensemble_seconds"] / steps, 4)}
                      for s in shards],
         "p99": {"max": max(p99), "median": float(np.median(p99)), "per_galaxy": p99},
-        "tuned": [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "tuned_ms")}
-                  for g in rows],
+        "tuned": [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "walk_warps",
+                                     "tuned_ms") if k in g} for g in rows],
     }
 
 
@@ -141,9 +141,9 @@ def run_shard(models, mine, args, device):
     tuner = gtc.Context(device)
     t0 = time.perf_counter()
     for g in gal:
-        gs, pack, ms = tuner.autotune_group(g["pos"].data_ptr(), g["mass"].data_ptr(), g["n"],
-                                            **SOLVER)
-        g.update(group_size=gs, pack=pack, tuned_ms=ms)
+        gs, pack, ms, walk = tuner.autotune_group(g["pos"].data_ptr(), g["mass"].data_ptr(),
+                                                  g["n"], **SOLVER)
+        g.update(group_size=gs, pack=pack, tuned_ms=ms, walk_warps=walk)
     shard["autotune_seconds"] = time.perf_counter() - t0
 
     # one after another, default parameters, eager: the unbatched baseline
@@ -169,6 +169,7 @@ def run_shard(models, mine, args, device):
         kw = dict(SOLVER, group_size=g["group_size"], pack=g["pack"])
         ens.set_system(k, g["pos"].data_ptr(), g["vel"].data_ptr(), g["mass"].data_ptr(),
                        g["acc"].data_ptr(), g["pot"].data_ptr(), g["n"], **kw)
+        ens.context(k).set_option("walk_warps", g["walk_warps"])
     ens.leapfrog(args.dt, 2, prime=True, graph=True)  # capture and warm up
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -196,8 +197,8 @@ def run_shard(models, mine, args, device):
         g["p99"] = float(np.percentile(e, 99))
     chk.close()
     ens.close()
-    shard["galaxies"] = [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "tuned_ms",
-                                             "interactions", "graph_steps", "p99")}
+    shard["galaxies"] = [{k: g[k] for k in ("galaxy", "n", "group_size", "pack", "walk_warps",
+                                             "tuned_ms", "interactions", "graph_steps", "p99")}
                          for g in gal]
     return shard
 

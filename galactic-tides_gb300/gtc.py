@@ -137,7 +137,10 @@ def _load():
         "gtc_ensemble_leapfrog": (I, [V, D, U64, I, I]),
         "gtc_ensemble_context": (V, [V, U32]),
         "gtc_autotune_group": (I, [V, P, P, U64, C.POINTER(GravityParams),
-                                   C.POINTER(GravityParams), C.POINTER(C.c_double)]),
+                                   C.POINTER(GravityParams), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_int)]),
+        "gtc_autotune_direct": (I, [V, P, P, U64, C.POINTER(GravityParams), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_double)]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -308,13 +311,24 @@ class Context:
     # ---- tuning ----------------------------------------------------------------
 
     def autotune_group(self, pos_ptr, mass_ptr, n, **kw):
-        """gtc_autotune_group -> (group_size, pack, ms per evaluation)."""
+        """gtc_autotune_group -> (group_size, pack (0 off, 1 a group's worth,
+        k >= 2 the packing threshold), ms per evaluation, walk_warps)."""
         base = gravity_params(**kw)
         best = GravityParams()
         ms = C.c_double()
+        walk = C.c_int()
         self._check(lib.gtc_autotune_group(self.h, pos_ptr, mass_ptr, n, C.byref(base),
-                                           C.byref(best), C.byref(ms)))
-        return best.group_size, bool(best.pack), ms.value
+                                           C.byref(best), C.byref(ms), C.byref(walk)))
+        return best.group_size, best.pack, ms.value, walk.value
+
+    def autotune_direct(self, pos_ptr, mass_ptr, n, **kw):
+        """gtc_autotune_direct -> (targets per thread, kernel ms); the context
+        keeps the winner."""
+        gp = gravity_params(**kw)
+        k, ms = C.c_int(), C.c_double()
+        self._check(lib.gtc_autotune_direct(self.h, pos_ptr, mass_ptr, n, C.byref(gp),
+                                            C.byref(k), C.byref(ms)))
+        return k.value, ms.value
 
     # ---- time integration ------------------------------------------------------
 

@@ -96,7 +96,9 @@ typedef struct gtc_gravity_params {
   int32_t quadrupole; /* 1: accepted cells carry quadrupoles */
   int32_t group_size; /* 1..32 on the device (GT_SIMD_WIDTH, gravity_backends.cpp:94-96) */
   int32_t leaf_size;  /* bucket size of the octree (default 8) */
-  int32_t pack;       /* 1: merge small sibling groups (the device default), 0: do not */
+  int32_t pack;       /* 1: merge small sibling groups while the run fits a group (the
+                         reference's rule, the device default), 0: do not; k >= 2: the
+                         packing threshold, runs of at most min(k, group_size) bodies */
   int32_t criterion;  /* GTC_CRITERION_* */
   int32_t reserved;
   double alpha;       /* learned criterion: per-cell error tolerance relative to the
@@ -328,12 +330,23 @@ gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int
 gtc_context *gtc_ensemble_context(gtc_ensemble *e, uint32_t i);
 
 /* The autotuner: times the grouped solver (theta criterion) on these bodies
- * (device arrays) for group_size 8, 16, 24, 32 with sibling packing off and
- * on, and returns in *best the base parameters with the fastest pair, and
- * its mean time per evaluation in *best_ms. */
+ * (device arrays) for group_size 8, 16, 24, 32, each with sibling packing
+ * off, packing thresholds group_size / 2 and 3 group_size / 4 and a group's
+ * worth (pack 1), each with the walk by threads and by warps, and returns
+ * in *best the base parameters with the fastest group_size and pack, in
+ * *walk_warps the fastest walk (for option "walk_warps"; NULL to skip) and
+ * in *best_ms its mean time per evaluation. The context's own options are
+ * left as they were. */
 gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double *mass,
                               uint64_t n, const gtc_gravity_params *base,
-                              gtc_gravity_params *best, double *best_ms);
+                              gtc_gravity_params *best, double *best_ms, int *walk_warps);
+/* The direct kernel's tile shape: times gtc_direct_force_device on these
+ * bodies (device arrays) with 2 and 4 targets per thread, keeps the faster
+ * in the context (option "direct_targets") and returns it in *targets, its
+ * kernel time in *best_ms. */
+gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double *mass,
+                               uint64_t n, const gtc_gravity_params *gp, int *targets,
+                               double *best_ms);
 
 /* ---- tuning and diagnostics (no reference counterpart) ------------------ */
 
@@ -361,6 +374,19 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
  *                        back how many pairs the last one deferred (more
  *                        rounds follow one read back each); 1 reads back
  *                        after every round. Results do not depend on it.
+ *   "walk_warps"         -1 (default), 0 or 1: the plain walk by warps, one
+ *                        per group, 32 node tests per step (1), or by
+ *                        threads, two per group in the one-pass walk (0),
+ *                        whose lists keep the reference's order; -1 takes
+ *                        warps below 40000 groups (the thread walk leaves
+ *                        the GPU idle there) and threads above (neighbouring
+ *                        groups share their record loads). Lists hold the
+ *                        same entries.
+ *   "learned_warps"      1 (default) or 0: the learned walk's rounds by warps,
+ *                        one per group; 0: three threads per group with the
+ *                        long walks handed to warps (the budgets below).
+ *   "direct_targets"     2 or 4 (default): targets per thread of the direct
+ *                        kernel (its tile shape; gtc_autotune_direct picks it).
  *   "stage_events"       0 (default) or 1: record CUDA events at the stage
  *                        boundaries of eager group solves (gtc_get_stage_times).
  *   "graph_headroom"     0..4 (default 0.25): a leapfrog graph is captured
@@ -471,7 +497,12 @@ gtc_status gtc_group_sizes(const gtc_context *ctx, uint64_t *n_bodies, uint64_t 
                            uint64_t *n_groups, uint64_t *n_cell_list, uint64_t *n_body_list);
 /* Copies the tree (NULL to skip any array): nodes, order (tree position ->
  * caller index), the FP32 bodies and cells the evaluator read, the groups
- * and both lists, the tree-order evaluator output. */
+ * and both lists, the tree-order evaluator output. The lists are laid out
+ * as the reference's GroupLists (group_lists.h:37-55): groups back to back,
+ * each group's cells in the reference's order. Each group's bodies are the
+ * reference's; the walk by warps (the default, option walk_warps) writes
+ * them in the order its steps reach them and the export gives them in
+ * ascending order, the walk by threads in the reference's order. */
 gtc_status gtc_group_export(gtc_context *ctx, gtc_node *nodes, uint64_t *order,
                             gtc_float4 *bodies, gtc_cell *cells, gtc_group *groups,
                             uint32_t *cell_list, uint32_t *body_list, gtc_float4 *out);

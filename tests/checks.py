@@ -48,8 +48,22 @@ def compare_trees(dev_nodes, ref_nodes):
     return bad
 
 
-def compare_lists(dev, dev_nodes, ref_lists, ref_nodes):
-    """Groups, and every group's cell and body list in order."""
+def sorted_per_group(values, starts, ends):
+    """Each group's entries sorted, groups in turn (a group's multiset)."""
+    counts = (np.asarray(ends, np.int64) - np.asarray(starts, np.int64))
+    gid = np.repeat(np.arange(len(counts)), counts)
+    v = np.asarray(values)[np.concatenate([np.arange(s, e) for s, e in zip(starts, ends)])
+                           if len(counts) else np.zeros(0, np.int64)]
+    return v[np.lexsort((v, gid))]
+
+
+def compare_lists(dev, dev_nodes, ref_lists, ref_nodes, body_order=False):
+    """Groups, every group's cell list in order, and every group's bodies:
+    as a multiset, or in order with body_order. The device's walk by warps
+    writes a group's bodies in the order its steps reach them (its exports
+    give them sorted); the reference's order -- siblings last octant first,
+    the bodies of a node in tree order -- is pinned through the walk by
+    threads (option walk_warps 0), which keeps it."""
     bad = []
     g_d, g_r = dev["groups"], ref_lists.groups
     if g_d.shape != g_r.shape:
@@ -57,7 +71,13 @@ def compare_lists(dev, dev_nodes, ref_lists, ref_nodes):
     if not np.array_equal(g_d[:, :6], g_r[:, :6]):
         k = np.nonzero(np.any(g_d[:, :6] != g_r[:, :6], axis=1))[0]
         bad.append(f"{len(k)} group records differ, first {k[0]}: {g_d[k[0]]} vs {g_r[k[0]]}")
-    if not np.array_equal(dev["body_list"], ref_lists.body_list):
+        return bad
+    if body_order:
+        same = np.array_equal(dev["body_list"], ref_lists.body_list)
+    else:
+        same = np.array_equal(sorted_per_group(dev["body_list"], g_d[:, 4], g_d[:, 5]),
+                              sorted_per_group(ref_lists.body_list, g_r[:, 4], g_r[:, 5]))
+    if not same:
         bad.append("body lists differ")
     dkey = node_keys(dev_nodes["begin"], dev_nodes["depth"])
     rkey = node_keys(ref_nodes["begin"], ref_depths(ref_nodes))

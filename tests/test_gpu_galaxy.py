@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from checks import (check_lists, check_packing, compare_lists, compare_trees, dev_children,
-                    rel_errors, scatter)
+                    rel_errors, scatter, sorted_per_group)
 from native import lopsided_sphere
 
 pytestmark = pytest.mark.gpu
@@ -85,13 +85,18 @@ def test_direct_200k_matches_oracle(ctx, oracle, gtc):
     racc, rpot = oracle.direct_fp64(pos, mass, G=1.0, eps=0.025, idx=idx)
     e_dev = np.sort(rel_errors(got[idx, :3].astype(np.float64), racc))
     e_cpu = np.sort(rel_errors(want[:, :3].astype(np.float64), racc))
+    p64 = np.abs(got[idx, 3].astype(np.float64) / rpot - 1)
     print(f"\n[direct 200k] vs FP32 oracle: median {np.median(e32):.3e} max {e32.max():.3e} "
           f"pot max {p32.max():.3e}; vs FP64: device median {e_dev[len(e_dev) // 2]:.3e} "
-          f"max {e_dev[-1]:.3e}, cpu FP32 median {e_cpu[len(e_cpu) // 2]:.3e} max {e_cpu[-1]:.3e}")
-    assert np.median(e32) < 1e-5 and e32.max() < 1e-3 and p32.max() < 1e-4
-    # no further from FP64 than the FP32 CPU kernel, beyond rounding
-    assert e_dev[len(e_dev) // 2] < 1.5 * e_cpu[len(e_cpu) // 2] + 1e-6
-    assert e_dev[-1] < 1e-3
+          f"max {e_dev[-1]:.3e} pot max {p64.max():.3e}, cpu FP32 median "
+          f"{e_cpu[len(e_cpu) // 2]:.3e} max {e_cpu[-1]:.3e}")
+    # the reference's bounds against FP64 (tests/test_gpu_kernels.cpp:232-234)
+    assert e_dev[len(e_dev) // 2] < 1e-5 and e_dev[-1] < 1e-3 and p64.max() < 1e-5
+    # no further from FP64 than the FP32 CPU kernel (the device sums each
+    # source slice and the even and odd sources apart: shorter sums)
+    assert e_dev[len(e_dev) // 2] <= 1.05 * e_cpu[len(e_cpu) // 2] + 1e-7
+    # and the FP32 kernels agree to their own summation error
+    assert np.median(e32) < 1e-5 and e32.max() < 1e-3 and p32.max() < 1e-3
 
 
 @pytest.mark.parametrize("pack", [False, True])
@@ -223,9 +228,11 @@ def test_one_pass_walk_spills_outgrown_groups(gtc, oracle):
 
 def test_warp_walk_matches_thread_walk(gtc, oracle):
     """The walk by warps (the default) and by threads (option walk_warps 0)
-    test the same nodes: the exported lists are identical and in the
-    reference's order, so are the counters, and the forces differ by
-    summation order only. Two solves each: count + fill, then one pass."""
+    test the same nodes: the exported cell lists are identical and in the
+    reference's order, each group's bodies are the same multiset (the thread
+    walk's in the reference's order too), the counters are equal, and the
+    forces differ by summation order only. Two solves each: count + fill,
+    then one pass."""
     pos, _, mass, _ = gtc.make_galaxy(100_000, seed=4)
     kw = dict(G=1.0, eps=0.025, quadrupole=True, theta=0.75, group_size=32, leaf_size=8,
               pack=True)
@@ -242,8 +249,13 @@ def test_warp_walk_matches_thread_walk(gtc, oracle):
     nodes, order, lists = oracle.lists(pos, mass, theta=0.75, group_size=32, leaf_size=8, pack=True)
     for passes in (2, 1):
         (aw, pw, dw, sw), (at, pt, dt, st) = res[(1, passes)], res[(0, passes)]
-        for k in ("groups", "cell_list", "body_list"):
+        for k in ("groups", "cell_list"):
             assert np.array_equal(dw[k], dt[k]), (passes, k)
+        g = dw["groups"]
+        assert np.array_equal(sorted_per_group(dw["body_list"], g[:, 4], g[:, 5]),
+                              sorted_per_group(dt["body_list"], g[:, 4], g[:, 5]))
+        # the walk by threads keeps the reference's order of every list
+        assert compare_lists(dt, dt["nodes"], lists, nodes, body_order=True) == []
         assert compare_lists(dw, dw["nodes"], lists, nodes) == []
         for k in ("cell_interactions", "body_interactions", "max_list", "walk_tests_fp64",
                   "walk_nodes"):

@@ -250,7 +250,49 @@ def test_ensemble_step_graph_equals_each_system_alone(gtc):
 
 @gpu
 def test_autotuner_returns_a_timed_configuration(ctx, gtc):
+    """group_size, packing (off, a threshold, a group's worth) and the walk;
+    the context's own options stay as they were; the direct kernel's tile
+    shape is kept in the context."""
     pos, _, mass, _ = gtc.make_galaxy(60_000, seed=9)
     dpos, dmass = _dev(pos, mass)
-    gs, pack, ms = ctx.autotune_group(dpos.data_ptr(), dmass.data_ptr(), len(mass), **SOLVER)
-    assert gs in (8, 16, 24, 32) and isinstance(pack, bool) and ms > 0
+    gs, pack, ms, walk = ctx.autotune_group(dpos.data_ptr(), dmass.data_ptr(), len(mass),
+                                            **SOLVER)
+    assert gs in (8, 16, 24, 32) and pack in (0, 1, gs // 2, 3 * gs // 4) and ms > 0
+    assert walk in (0, 1)
+    k, kms = ctx.autotune_direct(dpos.data_ptr(), dmass.data_ptr(), len(mass), **SOLVER)
+    assert k in (2, 4) and kms > 0
+    # the tuned parameters solve, with the chosen walk, to the same lists
+    c = gtc.Context(0)
+    try:
+        kw = dict(SOLVER, group_size=gs, pack=pack)
+        c.set_option("walk_warps", walk)
+        acc, _ = c.group_force(pos, mass, **kw)
+        d = c.export()
+        c.set_option("walk_warps", 1 - walk)
+        acc2, _ = c.group_force(pos, mass, **kw)
+        d2 = c.export()
+    finally:
+        c.close()
+    assert np.array_equal(d["cell_list"], d2["cell_list"])
+    assert np.abs(acc - acc2).max() <= 1e-4 * np.abs(acc).max()
+
+
+@gpu
+def test_packing_threshold_keeps_sibling_runs(ctx):
+    """pack = k >= 2 merges small siblings while the run holds at most k
+    bodies: groups are still whole nodes, leaf chunks or sibling runs, the
+    lists cover every body once, and merged runs stay within k."""
+    from checks import check_lists, check_packing, dev_children
+    from native import lopsided_sphere
+    pos, mass = lopsided_sphere(6000, 21)
+    counts = {}
+    for pack in (0, 12, 24, 1):
+        ctx.group_force(pos, mass, theta=0.7, eps=0.01, group_size=32, pack=pack)
+        d = ctx.export()
+        nd = d["nodes"]
+        assert check_lists(nd["begin"], nd["end"], d["groups"], d["cell_list"], d["body_list"],
+                           len(mass), 32) == 0
+        assert check_packing(nd["begin"], nd["end"], dev_children(nd), d["groups"]) == 0
+        counts[pack] = len(d["groups"])
+    assert counts[0] >= counts[12] >= counts[24] >= counts[1]
+    assert counts[0] > counts[1]
