@@ -66,6 +66,10 @@ def parse():
                     help="skip the N = 200k group and direct lines")
     ap.add_argument("--only-direct", action="store_true",
                     help="the tiled FP32 direct kernel on --n bodies only (for profiler runs)")
+    ap.add_argument("--walk-warps", type=int, default=-1, choices=[-1, 0, 1],
+                    help="the plain walk: -1 the solver's choice, 0 threads, 1 warps")
+    ap.add_argument("--direct-targets", type=int, default=0, choices=[0, 2, 4],
+                    help="the direct kernel's targets per thread (0: the default)")
     ap.add_argument("--only-steps", action="store_true",
                     help="warm-up and timed steps only (for profiler launch lists)")
     ap.add_argument("--learned-steps", action="store_true",
@@ -451,6 +455,8 @@ def run_direct_only(args):
     dacc = torch.empty((n, 3), dtype=torch.float64, device=dev)
     dpot = torch.empty(n, dtype=torch.float64, device=dev)
     with gtc.Context(0) as c:
+        if args.direct_targets:
+            c.set_option("direct_targets", args.direct_targets)
         for _ in range(warmup_steps(args)):
             c.direct_force_device(dpos.data_ptr(), dmass.data_ptr(), n, dacc.data_ptr(),
                                   dpot.data_ptr(), **SOLVER)
@@ -480,6 +486,7 @@ def main():
     import __graft_entry__
     gtc = __graft_entry__.load_package().gtc
     ctx = gtc.Context(local_rank)
+    ctx.set_option("walk_warps", args.walk_warps)
     n = args.n
     pos, _, mass = galaxy(n)
 
