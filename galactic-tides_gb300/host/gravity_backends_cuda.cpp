@@ -44,6 +44,25 @@ class CudaDirectGravity : public ForceModel {
   WalkStats stats_;
 };
 
+// gravity = tree, device = cuda: every body's own walk, FP64, the reference's
+// forces bit for bit.
+class CudaTreeGravity : public ForceModel {
+ public:
+  CudaTreeGravity(const GravityParams &gp, int leaf_size)
+      : grav_(gp.G, gp.theta, gp.eps, gp.quadrupole, leaf_size) {}
+  void compute(Particles &p) override { grav_.compute(p); }
+  WalkStats stats() const override {
+    const gtc_stats s = grav_.stats();
+    WalkStats w;
+    w.cell_interactions = s.cell_interactions;
+    w.particle_interactions = s.body_interactions;
+    return w;
+  }
+
+ private:
+  gtc::TreeGravity<Particles> grav_;
+};
+
 // Called from make_gravity when device == "cuda".
 std::unique_ptr<ForceModel> make_cuda_gravity(const Params &params, const GravityParams &gp,
                                               std::string *summary) {
@@ -60,7 +79,12 @@ std::unique_ptr<ForceModel> make_cuda_gravity(const Params &params, const Gravit
     if (summary) *summary = "direct summation, single precision, on cuda";
     return std::make_unique<CudaDirectGravity>(gp);
   }
-  throw std::runtime_error("gravity = " + kind + " has no cuda backend; use group or direct");
+  if (kind == "tree") {
+    const int leaf = static_cast<int>(params.get_int("leaf_size", 8));
+    if (summary) *summary = "tree (per-particle walk, double precision), built and walked on cuda";
+    return std::make_unique<CudaTreeGravity>(gp, leaf);
+  }
+  throw std::runtime_error("gravity = " + kind + " has no cuda backend");
 }
 
 }  // namespace galactic_tides

@@ -71,6 +71,10 @@ class Context {
                     const gtc_gravity_params &gp, double *acc, double *pot) {
     check(gtc_direct_force(ctx_, pos, mass, n, &gp, acc, pot), ctx_);
   }
+  void tree_force(const double *pos, const double *mass, uint64_t n,
+                  const gtc_gravity_params &gp, double *acc, double *pot) {
+    check(gtc_tree_force(ctx_, pos, mass, n, &gp, acc, pot), ctx_);
+  }
 
   gtc_stats stats() const {
     gtc_stats s{};
@@ -146,6 +150,29 @@ class DirectGravity {
     ctx_.direct_force(n ? &p.pos[0].x : nullptr, p.mass.data(), n, gp_,
                       n ? &p.acc[0].x : nullptr, p.pot.data());
   }
+
+ private:
+  Context ctx_;
+  gtc_gravity_params gp_;
+};
+
+// TreeGravity with the device (gravity = tree): the per-particle walk
+// (Octree::accel_pot, octree.cpp:275-344) for every body, FP64, the
+// reference's forces bit for bit.
+template <class Particles>
+class TreeGravity {
+ public:
+  TreeGravity(double G, double theta, double eps, bool quadrupole, int leaf_size = 8,
+              int device = 0)
+      : ctx_(device), gp_(gravity_params(G, theta, eps, quadrupole, 32, leaf_size)) {}
+  void compute(Particles &p) {
+    const std::size_t n = p.size();
+    p.acc.resize(n);
+    p.pot.resize(n);
+    ctx_.tree_force(n ? &p.pos[0].x : nullptr, p.mass.data(), n, gp_,
+                    n ? &p.acc[0].x : nullptr, p.pot.data());
+  }
+  const gtc_stats stats() const { return ctx_.stats(); }
 
  private:
   Context ctx_;
