@@ -188,7 +188,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.walk_budget = ctx->walk_budget == 0 ? ~0u : ctx->walk_budget;
     lw.pair_budget = ctx->pair_budget == 0 ? ~0u : ctx->pair_budget;
     lw.plan_rounds = !ctx->read_every_round;
-    lw.warps = ctx->learned_warps;
+    lw.warps_mode = ctx->learned_warps;
     gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, ns);
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
@@ -984,8 +984,9 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
       if (!(value >= 0) || value > 4) throw gtc::InvalidArgument("graph_headroom must be 0..4");
       ctx->graph_headroom = value;
     } else if (key == "learned_warps") {
-      if (value != 0 && value != 1) throw gtc::InvalidArgument("learned_warps must be 0 or 1");
-      ctx->learned_warps = value != 0;
+      if (value != 0 && value != 1 && value != -1)
+        throw gtc::InvalidArgument("learned_warps must be -1, 0 or 1");
+      ctx->learned_warps = static_cast<int>(value);
       ctx->lscratch.release();  // slots sized for the other layout
     } else if (key == "walk_warps") {
       if (value != 0 && value != 1 && value != -1)

@@ -36,7 +36,8 @@ struct gtc_context {
   gtc::u32 walk_budget = gtc::kLearnedWalkBudget;  // learned walk: nodes a thread tests before
   gtc::u32 pair_budget = gtc::kLearnedPairBudget;  // a warp takes over, round 0 / later (0: all)
   bool read_every_round = false;    // learned walk: no rounds walked before the first read back
-  bool learned_warps = true;        // learned walk: rounds by warps (else threads per part)
+  int learned_warps = -1;           // learned walk: rounds by warps (1), threads per part (0),
+                                    // or warps below the walk's group threshold (-1)
   gtc::DeviceBuffer diag;           // diagnostics partial sums
   gtc::DeviceBuffer tree_counts;    // per-particle walk: cell and particle interactions
   double graph_headroom = 0.25;     // leapfrog graphs: buffer headroom over the last sizes

@@ -157,7 +157,9 @@ struct LearnedWalk {
   u32 walk_budget = kLearnedWalkBudget;  // round 0: nodes a thread tests before a warp takes over
   u32 pair_budget = kLearnedPairBudget;  // later rounds: the same
   bool plan_rounds = true;  // walk the last call's rounds before reading anything back
-  bool warps = true;        // each round by warps, one per group (else threads per part)
+  // each round by warps, one per group (1), by threads per part (0), or by
+  // warps below Workspace::kWarpWalkGroups groups (-1), as the plain walk
+  int warps_mode = -1;
 };
 
 // Per-node features (after build_tree).

@@ -1006,13 +1006,14 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     throw RuntimeError("learned walk: too many tree nodes for 32 bit node ranges");
   Scalars *sc = ws.scalars.as<Scalars>();
   LearnedScratch &ls = *lw.scratch;
+  const bool warps = lw.warps_mode > 0 || (lw.warps_mode < 0 && ng < Workspace::kWarpWalkGroups);
   if (ls.slot_cells[0] == 0) {  // the first learned walk: the theta walk's slots to start with
     for (int k = 0; k < kParts; ++k) {
       // the warp rounds write a group's whole lists into part 0
-      const bool used = !lw.warps || k == 0;
-      ls.slot_cells[k] = used ? std::max<u32>(lw.warps ? ws.slot_cells : ws.slot_cells / 2, 256)
+      const bool used = !warps || k == 0;
+      ls.slot_cells[k] = used ? std::max<u32>(warps ? ws.slot_cells : ws.slot_cells / 2, 256)
                               : learned_slot(0);
-      ls.slot_bodies[k] = used ? std::max<u32>(lw.warps ? ws.slot_bodies : ws.slot_bodies / 2, 256)
+      ls.slot_bodies[k] = used ? std::max<u32>(warps ? ws.slot_bodies : ws.slot_bodies / 2, 256)
                                : learned_slot(0);
     }
     ls.slot_pend = 256;
@@ -1089,7 +1090,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
         a.rows = ls.q[qsel].as<uint2>();
         a.dec = ls.dec[qsel].as<u8>();
       }
-      if (lw.warps) {
+      if (warps) {
         GTC_CUDA(cudaMemsetAsync(a.next, 0, sizeof(u32), s));
         k_lwarp<<<warp_blocks, kLWarps * 32, 0, s>>>(a, r);
         GTC_LAUNCH_CHECK();

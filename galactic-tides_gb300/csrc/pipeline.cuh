@@ -83,7 +83,7 @@ struct Workspace {
   DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
   DeviceBuffer direct_part;               // direct sum: per-slice partial sums
-  int direct_targets = 4;                 // direct sum: targets per thread (2 or 4)
+  int direct_targets = 2;                 // direct sum: targets per thread (2 or 4)
   RadixScratch radix;
 
   // host-side view of the last build

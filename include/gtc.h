@@ -382,10 +382,11 @@ gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double
  *                        the GPU idle there) and threads above (neighbouring
  *                        groups share their record loads). Lists hold the
  *                        same entries.
- *   "learned_warps"      1 (default) or 0: the learned walk's rounds by warps,
- *                        one per group; 0: three threads per group with the
- *                        long walks handed to warps (the budgets below).
- *   "direct_targets"     2 or 4 (default): targets per thread of the direct
+ *   "learned_warps"      -1 (default), 0 or 1: the learned walk's rounds by
+ *                        warps, one per group (1), or by three threads per
+ *                        group with the long walks handed to warps (0, the
+ *                        budgets below); -1 picks as "walk_warps" does.
+ *   "direct_targets"     2 (default) or 4: targets per thread of the direct
  *                        kernel (its tile shape; gtc_autotune_direct picks it).
  *   "stage_events"       0 (default) or 1: record CUDA events at the stage
  *                        boundaries of eager group solves (gtc_get_stage_times).
