@@ -171,9 +171,11 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
   GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
   if (learned) {
-    // the node features and walk records after the moments, on their stream
-    const cudaStream_t ns = ws.side_pending ? ws.side : s;
-    gtc::learned_node_features(ws, ctx->cfeat, ns);
+    // the walk's inputs from FP32 moment estimates on the main stream: the
+    // walk runs while the side stream accumulates the FP64 moments the
+    // evaluation reads
+    gtc::learned_walk_inputs(ws, ctx->lscratch, ctx->cfeat,
+                             static_cast<float>(1.0 / ctx->guard_theta), ctx->model_ymean, s);
     gtc::LearnedWalk lw;
     lw.net = ctx->net.as<gtc::LearnedNet>();
     lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
@@ -189,7 +191,6 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     lw.pair_budget = ctx->pair_budget == 0 ? ~0u : ctx->pair_budget;
     lw.plan_rounds = !ctx->read_every_round;
     lw.warps_mode = ctx->learned_warps;
-    gtc::learned_walk_records(ws, lw.cfeat, ctx->lscratch.lrec, lw.inv_theta_guard, lw.y_mean, ns);
     gtc::build_lists(ws, sp, s, ctx->host_sc, &lw);
   } else {
     gtc::build_lists(ws, sp, s, ctx->host_sc);

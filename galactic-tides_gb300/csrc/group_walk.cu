@@ -891,14 +891,18 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
                                 ws.gbox.as<double>(), ws.gboxf.as<float>());
   GTC_LAUNCH_CHECK();
-  join_side(ws, s);  // the walk reads the node records (and the tolerances the root's mass)
-  ws.stage(Workspace::kStWalk0, s);
   if (lw) {
+    // the learned walk decides from FP32 moment estimates: the FP64 moments
+    // go on on the side stream, and are joined for the evaluation after it
+    ws.stage(Workspace::kStWalk0, s);
     learned_group_tolerances(ws, *lw, ng, s);
     learned_build_lists(ws, *lw, ng, host, s);
     ws.stage(Workspace::kStWalk1, s);
+    join_side(ws, s);
     return;
   }
+  join_side(ws, s);  // the walk reads the node records
+  ws.stage(Workspace::kStWalk0, s);
 
   const WalkRec32 *w32 = ws.walk32.as<WalkRec32>();
   const WalkRec64 *w64 = ws.walk64.as<WalkRec64>();

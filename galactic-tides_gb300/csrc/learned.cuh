@@ -126,6 +126,9 @@ struct LearnedScratch {
   DeviceBuffer q[2], dec[2];        // deferred (group, node) rows and the network's decisions
   DeviceBuffer cont;                // round-0 walks handed on to warps
   DeviceBuffer next;                // the warp rounds' group counter
+  // FP32 estimates of the moments the walk decides from (cells in GTCell
+  // layout, delta), and the root's mass as rootmom[1].y
+  DeviceBuffer cells32, delta32, rootmom;
   // per-group slots of the three parts of round 0 (0: not sized yet) and
   // of deferred pairs
   u32 slot_cells[3] = {0, 0, 0}, slot_bodies[3] = {0, 0, 0}, slot_pend = 0;
@@ -135,7 +138,7 @@ struct LearnedScratch {
   u32 rounds = 0, row_cap = 0;
   void release() {
     for (DeviceBuffer *b : {&lrec, &pend, &pcount, &roff, &q[0], &q[1], &dec[0], &dec[1], &cont,
-                            &next})
+                            &next, &cells32, &delta32, &rootmom})
       b->release();
     for (int k = 0; k < 3; ++k) slot_cells[k] = slot_bodies[k] = 0;
     slot_pend = 0;
@@ -162,12 +165,16 @@ struct LearnedWalk {
   int warps_mode = -1;
 };
 
-// Per-node features (after build_tree).
+// Per-node features (after build_tree and the FP64 moments: the training
+// samples' features).
 void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s);
-// The walk's per-node records (LWalkRec) from the walk records and the node
-// features, for the guard angle 1 / inv_theta_guard and the model's y_mean.
-void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lrec,
-                          float inv_theta_guard, float y_mean, cudaStream_t s);
+// The learned walk's inputs from FP32 moment estimates (moments32), on the
+// main stream while the FP64 moments may still run: scratch.cells32,
+// delta32 and rootmom, the per-node features and the walk's per-node
+// records (LWalkRec) for the guard angle 1 / inv_theta_guard and the model's
+// y_mean.
+void learned_walk_inputs(Workspace &ws, LearnedScratch &scratch, DeviceBuffer &cfeat,
+                         float inv_theta_guard, float y_mean, cudaStream_t s);
 // Per-group group feature and tolerance (inside build_lists, after the group boxes).
 void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cudaStream_t s);
 // The learned walk in rounds, three threads per group (one per part of the

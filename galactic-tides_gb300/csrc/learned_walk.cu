@@ -174,26 +174,44 @@ __global__ void __launch_bounds__(kT)
                          static_cast<float>(delta[p]), fs);
 }
 
+// The same features and records from the FP32 moment estimates (cells32,
+// delta32) and the tree's topology, so that they need nothing of the FP64
+// moments.
 __global__ void __launch_bounds__(kT)
-    k_lwalk_rec(const WalkRec32 *walk32, const CellFeat *cfeat, u32 m, float inv_theta_guard,
-                float y_mean, LWalkRec *out) {
+    k_cell_feat32(const double2 *geom, const double2 *rootmom, const float4 *cells32,
+                  const float *delta32, const TreeRoot *root, u32 m, CellFeat *out) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (p >= m) return;
-  const WalkRec32 w = walk32[p];
+  const FeatScale fs = scale_of(root, rootmom);
+  const float4 cm = cells32[3 * p], qa = cells32[3 * p + 1], qb = cells32[3 * p + 2];
+  const float qn = sqrtf(qa.x * qa.x + qa.y * qa.y + qa.z * qa.z +
+                         2.f * (qa.w * qa.w + qb.x * qb.x + qb.y * qb.y));
+  out[p] = cell_features(static_cast<float>(geom[2 * p + 1].y), cm.w, qn, delta32[p], fs);
+}
+
+__global__ void __launch_bounds__(kT)
+    k_lwalk_rec32(const double2 *geom, const float4 *cells32, const CellFeat *cfeat,
+                  const u32 *nbegin, const u32 *nend, const u32 *skip, const u8 *isleaf,
+                  const TreeRoot *root, u32 m, float inv_theta_guard, float y_mean,
+                  LWalkRec *out) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (p >= m) return;
+  const double2 g0 = geom[2 * p], g1 = geom[2 * p + 1];
+  const float4 cm = cells32[3 * p];
   const float4 c0 = reinterpret_cast<const float4 *>(cfeat + p)[0];
   const float crit = fmaf(2.f * c0.x, inv_theta_guard, c0.y);
   LWalkRec r;
-  r.cx = w.cx;
-  r.cy = w.cy;
-  r.cz = w.cz;
-  r.slack = w.slack;
-  r.mx = w.mx;
-  r.my = w.my;
-  r.mz = w.mz;
+  r.cx = static_cast<float>(g0.x - root->center[0]);
+  r.cy = static_cast<float>(g0.y - root->center[1]);
+  r.cz = static_cast<float>(g1.x - root->center[2]);
+  r.slack = static_cast<float>(g1.y * 1.0001);
+  r.mx = cm.x;
+  r.my = cm.y;
+  r.mz = cm.z;
   r.guard2 = crit * crit;
-  r.skip = w.skip;
-  r.nbody_leaf = w.nbody_leaf;
-  r.begin = w.begin;
+  r.skip = skip[p];
+  r.nbody_leaf = (nend[p] - nbegin[p]) | (isleaf[p] ? 0x80000000u : 0u);
+  r.begin = nbegin[p];
   r.pscale = exp2f(0.4f * (c0.z + y_mean));
   out[p] = r;
 }
@@ -230,25 +248,6 @@ __global__ void __launch_bounds__(kT)
   if (t >= n) return;
   const float4 o = out[t];
   amag[order[t]] = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-}
-
-__device__ __forceinline__ WalkRec32 load_rec(const WalkRec32 *w, u32 i) {
-  const float4 *p = reinterpret_cast<const float4 *>(w + i);
-  const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-  WalkRec32 r;
-  r.cx = a.x;
-  r.cy = a.y;
-  r.cz = a.z;
-  r.slack = a.w;
-  r.mx = b.x;
-  r.my = b.y;
-  r.mz = b.z;
-  r.crit2 = b.w;
-  r.skip = __float_as_uint(c.x);
-  r.nbody_leaf = __float_as_uint(c.y);
-  r.begin = __float_as_uint(c.z);
-  r.bound = c.w;
-  return r;
 }
 
 constexpr int kMaxRounds = kMaxDepth + 4;
@@ -883,7 +882,7 @@ __global__ void __launch_bounds__(kT) k_lgroup_records(const GArgs a, const u32 
 
 // The network's decision on every deferred pair: one warp per 32 pairs.
 __global__ void __launch_bounds__(kT)
-    k_ldecide(const uint2 *q, u64 nq, const WalkRec32 *walk32, const CellFeat *cfeat,
+    k_ldecide(const uint2 *q, u64 nq, const LWalkRec *lrec, const CellFeat *cfeat,
               const float *gboxf, const float2 *gtol, const LearnedNet *net, const TreeRoot *root,
               const double2 *mom, u8 *dec, const u32 *nq_dev = nullptr,
               const u32 *overflow = nullptr) {
@@ -905,12 +904,12 @@ __global__ void __launch_bounds__(kT)
     const u32 g = qk.x, p = qk.y;
     const float4 b0 = reinterpret_cast<const float4 *>(gboxf)[2ull * g],
                  b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
-    const WalkRec32 r = load_rec(walk32, p);
+    const float4 rm = __ldg(reinterpret_cast<const float4 *>(lrec + p) + 1);  // com, guard
     const float4 c0 = __ldg(reinterpret_cast<const float4 *>(cfeat + p));
     const float4 c1 = __ldg(reinterpret_cast<const float4 *>(cfeat + p) + 1);
-    const float dx = fmaxf(fabsf(r.mx - b0.x) - b0.w, 0.f),
-                dy = fmaxf(fabsf(r.my - b0.y) - b1.x, 0.f),
-                dz = fmaxf(fabsf(r.mz - b0.z) - b1.y, 0.f);
+    const float dx = fmaxf(fabsf(rm.x - b0.x) - b0.w, 0.f),
+                dy = fmaxf(fabsf(rm.y - b0.y) - b1.x, 0.f),
+                dz = fmaxf(fabsf(rm.z - b0.z) - b1.y, 0.f);
     const float f2 = distance_feature(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), fs);
     const float2 gt = gtol[g];
     const float e = prior_log2err(c0.z, f2) + net->y_mean;
@@ -969,13 +968,24 @@ void learned_node_features(Workspace &ws, DeviceBuffer &cfeat, cudaStream_t s) {
   GTC_LAUNCH_CHECK();
 }
 
-void learned_walk_records(Workspace &ws, const CellFeat *cfeat, DeviceBuffer &lrec,
-                          float inv_theta_guard, float y_mean, cudaStream_t s) {
+void learned_walk_inputs(Workspace &ws, LearnedScratch &ls, DeviceBuffer &cfeat,
+                         float inv_theta_guard, float y_mean, cudaStream_t s) {
   const u32 m = static_cast<u32>(ws.n_nodes);
   if (m == 0) return;
-  lrec.ensure(static_cast<u64>(m) * sizeof(LWalkRec));
-  k_lwalk_rec<<<ceil_div(m, kT), kT, 0, s>>>(ws.walk32.as<WalkRec32>(), cfeat, m, inv_theta_guard,
-                                             y_mean, lrec.as<LWalkRec>());
+  ls.cells32.ensure(static_cast<u64>(m) * 3 * sizeof(float4));
+  ls.delta32.ensure(static_cast<u64>(m) * sizeof(float));
+  ls.rootmom.ensure(2 * sizeof(double2));
+  moments32(ws, ls.cells32.as<float4>(), ls.delta32.as<float>(), ls.rootmom.as<double2>(), s);
+  cfeat.ensure(static_cast<u64>(m) * sizeof(CellFeat));
+  k_cell_feat32<<<ceil_div(m, kT), kT, 0, s>>>(ws.geom.as<double2>(), ls.rootmom.as<double2>(),
+                                               ls.cells32.as<float4>(), ls.delta32.as<float>(),
+                                               ws.root.as<TreeRoot>(), m, cfeat.as<CellFeat>());
+  GTC_LAUNCH_CHECK();
+  ls.lrec.ensure(static_cast<u64>(m) * sizeof(LWalkRec));
+  k_lwalk_rec32<<<ceil_div(m, kT), kT, 0, s>>>(
+      ws.geom.as<double2>(), ls.cells32.as<float4>(), cfeat.as<CellFeat>(), ws.nbegin.as<u32>(),
+      ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>(), ws.root.as<TreeRoot>(), m,
+      inv_theta_guard, y_mean, ls.lrec.as<LWalkRec>());
   GTC_LAUNCH_CHECK();
 }
 
@@ -984,8 +994,8 @@ void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cuda
   lw.gtol->ensure(static_cast<u64>(ng) * sizeof(float2));
   k_group_tol<<<ceil_div(ng, kT), kT, 0, s>>>(
       ws.gbegin.as<u32>(), ws.gend.as<u32>(), ng, ws.idx.as<u32>(), lw.prev_amag,
-      ws.gboxf.as<float>(), ws.root.as<TreeRoot>(), ws.mom.as<double2>(), lw.alpha, lw.G,
-      lw.gtol->as<float2>());
+      ws.gboxf.as<float>(), ws.root.as<TreeRoot>(), lw.scratch->rootmom.as<double2>(), lw.alpha,
+      lw.G, lw.gtol->as<float2>());
   GTC_LAUNCH_CHECK();
 }
 
@@ -1029,7 +1039,7 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   a.gtol = lw.gtol->as<float2>();
   a.ng = ng;
   a.root = ws.root.as<TreeRoot>();
-  a.mom = ws.mom.as<double2>();
+  a.mom = ls.rootmom.as<double2>();  // the root's mass, from the FP32 estimates
   a.band = lw.band;
   a.ncells = ws.gcells.as<u64>();
   a.nbodies = ws.gbodies.as<u64>();
@@ -1116,9 +1126,9 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
       GTC_LAUNCH_CHECK();
       if (launch_rows > 0) {
         k_ldecide<<<ceil_div(launch_rows, kT), kT, 0, s>>>(
-            ls.q[nq].as<uint2>(), launch_rows, ws.walk32.as<WalkRec32>(), lw.cfeat, a.gboxf,
-            a.gtol, lw.net, ws.root.as<TreeRoot>(), ws.mom.as<double2>(), ls.dec[nq].as<u8>(),
-            roff + nparts, &sc->list_overflow);
+            ls.q[nq].as<uint2>(), launch_rows, a.lrec, lw.cfeat, a.gboxf, a.gtol, lw.net,
+            ws.root.as<TreeRoot>(), a.mom, ls.dec[nq].as<u8>(), roff + nparts,
+            &sc->list_overflow);
         GTC_LAUNCH_CHECK();
       }
       qsel = nq;

@@ -90,6 +90,7 @@ struct Workspace {
   u64 n = 0, n_nodes = 0, n_groups = 0, n_cell_list = 0, n_body_list = 0;
   int key_words = 1;
   int sort_levels = 0;        // key levels the next eager build sorts first (0: all 21)
+  int tree_depth = 0;         // the last eager build's deepest leaf
   int walk_split_depth = 0;   // tuning: subtree depth of the walk tasks (0..2)
   // The plain walk by warps (one warp per group, 32 node tests per step) or
   // by threads (two per group in the one pass, one in count + fill). Mode
@@ -323,6 +324,12 @@ void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *a
                            const Scalars *sc, cudaStream_t s);
 
 // Direct summation kernels.
+// FP32 estimates of every node's moments (GTCell layout in cells32, delta in
+// delta32) from the FP32 bodies, and the root's mass as rootmom[1].y, for
+// the learned walk's decisions (after an eager build_tree, on the main
+// stream; the FP64 moments may still be running on the side stream).
+void moments32(Workspace &ws, float4 *cells32, float *delta32, double2 *rootmom,
+               cudaStream_t s);
 // Octree::accel_pot for every body on the built tree (FP64, the reference's
 // per-particle walk): acc (n x 3) and pot in caller order; counts[0..1] +=
 // cell and particle interactions.

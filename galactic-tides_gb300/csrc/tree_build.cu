@@ -793,6 +793,115 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
   a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
 }
 
+// FP32 estimates of the moments, for the learned walk's decisions only: the
+// same sums as leaf_moments / node_moments, in FP32 on the FP32 bodies
+// (relative to the root centre), written as GTCell-layout cells plus delta.
+// They take a few tens of microseconds where the FP64 moments take most of a
+// millisecond, so the learned walk starts while the FP64 moments -- which
+// the evaluation reads -- are still being accumulated.
+struct Moment32Arrays {
+  const double2 *geom;
+  const u32 *nbegin, *nend;
+  const u8 *nchild;
+  const uint4 *kids;
+  const float4 *bodies;  // tree order, relative to the root centre
+  const TreeRoot *root;
+  float4 *cells;         // 3 per node: (com, mass), (xx, yy, zz, xy), (xz, yz, 0, 0)
+  float *delta;
+};
+
+__device__ __forceinline__ void finish_moments32(const Moment32Arrays &a, u32 p, float m, float cx,
+                                                 float cy, float cz, const float *q) {
+  const Dbl4 g = load_pair(a.geom, p);
+  const float gx = static_cast<float>(g.x - a.root->center[0]),
+              gy = static_cast<float>(g.y - a.root->center[1]),
+              gz = static_cast<float>(g.z - a.root->center[2]);
+  a.cells[3 * p] = make_float4(cx, cy, cz, m);
+  a.cells[3 * p + 1] = make_float4(q[0], q[1], q[2], q[3]);
+  a.cells[3 * p + 2] = make_float4(q[4], q[5], 0.f, 0.f);
+  const float ex = cx - gx, ey = cy - gy, ez = cz - gz;
+  a.delta[p] = sqrtf(ex * ex + ey * ey + ez * ez);
+}
+
+__device__ __forceinline__ float3 centre32(const Moment32Arrays &a, u32 p) {
+  const Dbl4 g = load_pair(a.geom, p);
+  return make_float3(static_cast<float>(g.x - a.root->center[0]),
+                     static_cast<float>(g.y - a.root->center[1]),
+                     static_cast<float>(g.z - a.root->center[2]));
+}
+
+__device__ void leaf_moments32(const Moment32Arrays &a, u32 p) {
+  const u32 b0 = a.nbegin[p], b1 = a.nend[p];
+  float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  for (u32 k = b0; k < b1; ++k) {
+    const float4 b = a.bodies[k];
+    m += b.w;
+    cx += b.w * b.x;
+    cy += b.w * b.y;
+    cz += b.w * b.z;
+  }
+  if (m > 0) {
+    cx /= m;
+    cy /= m;
+    cz /= m;
+  } else {
+    const float3 c = centre32(a, p);
+    cx = c.x;
+    cy = c.y;
+    cz = c.z;
+  }
+  float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (u32 k = b0; k < b1; ++k) {
+    const float4 b = a.bodies[k];
+    const float dx = b.x - cx, dy = b.y - cy, dz = b.z - cz;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    q[0] += b.w * (3.f * dx * dx - r2);
+    q[1] += b.w * (3.f * dy * dy - r2);
+    q[2] += b.w * (3.f * dz * dz - r2);
+    q[3] += b.w * 3.f * dx * dy;
+    q[4] += b.w * 3.f * dx * dz;
+    q[5] += b.w * 3.f * dy * dz;
+  }
+  finish_moments32(a, p, m, cx, cy, cz, q);
+}
+
+__device__ void node_moments32(const Moment32Arrays &a, u32 p) {
+  const uint4 k0 = a.kids[2ull * p], k1 = a.kids[2ull * p + 1];
+  const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+  const int nc = a.nchild[p];
+  float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  for (int j = nc - 1; j >= 0; --j) {
+    const float4 c = a.cells[3 * ch[j]];
+    m += c.w;
+    cx += c.w * c.x;
+    cy += c.w * c.y;
+    cz += c.w * c.z;
+  }
+  if (m > 0) {
+    cx /= m;
+    cy /= m;
+    cz /= m;
+  } else {
+    const float3 c = centre32(a, p);
+    cx = c.x;
+    cy = c.y;
+    cz = c.z;
+  }
+  float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int j = nc - 1; j >= 0; --j) {
+    const float4 c = a.cells[3 * ch[j]], qa = a.cells[3 * ch[j] + 1], qb = a.cells[3 * ch[j] + 2];
+    const float dx = c.x - cx, dy = c.y - cy, dz = c.z - cz;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    q[0] += qa.x + c.w * (3.f * dx * dx - r2);
+    q[1] += qa.y + c.w * (3.f * dy * dy - r2);
+    q[2] += qa.z + c.w * (3.f * dz * dz - r2);
+    q[3] += qa.w + c.w * 3.f * dx * dy;
+    q[4] += qb.x + c.w * 3.f * dx * dz;
+    q[5] += qb.y + c.w * 3.f * dy * dz;
+  }
+  finish_moments32(a, p, m, cx, cy, cz, q);
+}
+
 // Moments bottom-up, one launch per depth: leaves first (any depth), then
 // the inner nodes of each depth from the deepest up, so every node's
 // children are complete when it is combined. Nodes are bucketed by depth
@@ -931,6 +1040,29 @@ __global__ void __launch_bounds__(32)
     if (b0 >= kLeafBucket) leaf_moments(a, bucket[off + k]);
     else node_moments(a, bucket[off + k]);
   }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_leaf_moments32(Moment32Arrays a, const u32 *bucket, const u32 *meta) {
+  u32 count = 0;
+  for (int b = kLeafBucket; b < kLeafBucket + kLeafClasses; ++b) count += meta[b];
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k < count) leaf_moments32(a, bucket[meta[kBuckets + kLeafBucket] + k]);
+}
+
+// One depth's inner nodes, one thread each (FP32: no need to spread them).
+__global__ void __launch_bounds__(kT)
+    k_node_moments32(Moment32Arrays a, const u32 *bucket, const u32 *meta, int b0, int nb) {
+  u32 count = 0;
+  for (int b = b0; b < b0 + nb; ++b) count += meta[b];
+  const u32 off = meta[kBuckets + b0];
+  for (u32 k = blockIdx.x * kT + threadIdx.x; k < count; k += gridDim.x * kT)
+    node_moments32(a, bucket[off + k]);
+}
+
+__global__ void k_root_mass(const float4 *cells32, double2 *rootmom) {
+  rootmom[0] = make_double2(0.0, 0.0);
+  rootmom[1] = make_double2(0.0, static_cast<double>(cells32[0].w));
 }
 
 // A graph replay's checks after the node count: deeper keys needed, or a
@@ -1228,6 +1360,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   }
   const u32 m = host->n_nodes;
   ws.n_nodes = m;
+  ws.tree_depth = static_cast<int>(host->depth);
   ws.geom.ensure(m * 2 * sizeof(double2));
   ws.mom.ensure(m * 2 * sizeof(double2));
   ws.quad.ensure(m * 3 * sizeof(double2));
@@ -1299,6 +1432,25 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   ws.stage(Workspace::kStMom1, ms);
   k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
                                   root_centre(root), ws.bodies.as<float4>());
+  GTC_LAUNCH_CHECK();
+}
+
+void moments32(Workspace &ws, float4 *cells32, float *delta32, double2 *rootmom,
+               cudaStream_t s) {
+  const u32 m = static_cast<u32>(ws.n_nodes);
+  if (m == 0) return;
+  const Moment32Arrays a{ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                         ws.nchild.as<u8>(),   ws.kids.as<uint4>(), ws.bodies.as<float4>(),
+                         ws.root.as<TreeRoot>(), cells32, delta32};
+  const u32 *meta = ws.arrive.as<u32>(), *bucket = ws.bucket.as<u32>();
+  k_leaf_moments32<<<ceil_div(m, kT), kT, 0, s>>>(a, bucket, meta);
+  GTC_LAUNCH_CHECK();
+  for (int d = ws.tree_depth - 1; d >= 0; --d) {
+    k_node_moments32<<<ceil_div(std::max<u32>(1, m / 4), kT), kT, 0, s>>>(
+        a, bucket, meta, d * kSizeClasses, kSizeClasses);
+    GTC_LAUNCH_CHECK();
+  }
+  k_root_mass<<<1, 1, 0, s>>>(cells32, rootmom);
   GTC_LAUNCH_CHECK();
 }
 

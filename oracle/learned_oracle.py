@@ -201,23 +201,102 @@ def _fmaf(a, b, c):
     return _f32(np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64))
 
 
-def node_records(nodes, cells, theta_guard, y_mean):
-    """Per node, the FP32 record the learned walk reads (centre, slack,
-    centre of mass relative to the root centre; guard^2; the prior's node
-    part) and the cell-only features."""
+def children_of(nodes):
+    """Each node's children in octant order (every child after its parent)."""
+    parent = np.asarray(nodes["parent"], np.int64)
+    kids = [[] for _ in range(len(nodes))]
+    for i in range(1, len(nodes)):
+        kids[parent[i]].append(i)
+    # the device numbers siblings last octant first, the reference first
+    # octant first: order them by their first body, which follows the octants
+    begin = np.asarray(nodes["begin"], np.int64)
+    return [sorted(k, key=lambda c: begin[c]) for k in kids]
+
+
+def moments32(nodes, bodies):
+    """The FP32 moment estimates the learned walk decides from
+    (tree_build.cu: leaf_moments32 / node_moments32): the reference's sums
+    (octree.cpp:46-102) in FP32, each product and sum rounded on its own, on
+    the FP32 bodies relative to the root centre. -> cells (m, 12) in GTCell
+    layout and delta (m,)."""
+    f = np.float32
     origin = nodes["center"][0]
-    L, mt = float(nodes["half"][0]), float(nodes["mass"][0])
+    cen = (nodes["center"] - origin).astype(np.float32)
+    m_nodes = len(nodes)
+    cells = np.zeros((m_nodes, 12), np.float32)
+    delta = np.zeros(m_nodes, np.float32)
+    kids = children_of(nodes)
+    b = np.asarray(bodies, np.float32)
+    three = f(3.0)
+
+    def finish(p, m, cx, cy, cz, q):
+        cells[p, :4] = (cx, cy, cz, m)
+        cells[p, 4:8] = q[:4]
+        cells[p, 8:10] = q[4:]
+        ex, ey, ez = f(cx - cen[p, 0]), f(cy - cen[p, 1]), f(cz - cen[p, 2])
+        delta[p] = f(np.sqrt(f(f(f(ex * ex) + f(ey * ey)) + f(ez * ez))))
+
+    def com(p, m, cx, cy, cz):
+        if m > 0:
+            return f(cx / m), f(cy / m), f(cz / m)
+        return cen[p, 0], cen[p, 1], cen[p, 2]
+
+    def quad(terms):
+        q = [f(0.0)] * 6
+        for w, dx, dy, dz, qa in terms:
+            r2 = f(f(f(dx * dx) + f(dy * dy)) + f(dz * dz))
+            adds = (f(w * f(f(f(three * dx) * dx) - r2)), f(w * f(f(f(three * dy) * dy) - r2)),
+                    f(w * f(f(f(three * dz) * dz) - r2)), f(f(f(w * three) * dx) * dy),
+                    f(f(f(w * three) * dx) * dz), f(f(f(w * three) * dy) * dz))
+            for k in range(6):
+                q[k] = f(q[k] + (f(qa[k] + adds[k]) if qa is not None else adds[k]))
+        return q
+
+    depth = np.zeros(m_nodes, np.int64)
+    for i in range(1, m_nodes):
+        depth[i] = depth[int(nodes["parent"][i])] + 1
+    for p in sorted(range(m_nodes), key=lambda i: -depth[i]):  # children before parents
+        if not kids[p]:
+            rows = b[int(nodes["begin"][p]):int(nodes["end"][p])]
+            m, cx, cy, cz = f(0.0), f(0.0), f(0.0), f(0.0)
+            for x, y, z, w in rows:
+                m, cx, cy, cz = f(m + w), f(cx + f(w * x)), f(cy + f(w * y)), f(cz + f(w * z))
+            cx, cy, cz = com(p, m, cx, cy, cz)
+            q = quad([(w, f(x - cx), f(y - cy), f(z - cz), None) for x, y, z, w in rows])
+        else:
+            m, cx, cy, cz = f(0.0), f(0.0), f(0.0), f(0.0)
+            for c in kids[p]:
+                w = cells[c, 3]
+                m = f(m + w)
+                cx, cy, cz = (f(cx + f(w * cells[c, 0])), f(cy + f(w * cells[c, 1])),
+                              f(cz + f(w * cells[c, 2])))
+            cx, cy, cz = com(p, m, cx, cy, cz)
+            q = quad([(cells[c, 3], f(cells[c, 0] - cx), f(cells[c, 1] - cy),
+                       f(cells[c, 2] - cz), (cells[c, 4], cells[c, 5], cells[c, 6], cells[c, 7],
+                                             cells[c, 8], cells[c, 9])) for c in kids[p]])
+        finish(p, m, cx, cy, cz, q)
+    return cells, delta
+
+
+def node_records(nodes, bodies, theta_guard, y_mean):
+    """Per node, the FP32 record the learned walk reads -- centre and slack
+    relative to the root centre from the FP64 geometry, the centre of mass,
+    guard^2 and the prior's node part from the FP32 moment estimates -- and
+    the cell-only features."""
+    origin = nodes["center"][0]
+    L = float(nodes["half"][0])
+    cells, delta = moments32(nodes, bodies)
+    mt = float(cells[0, 3])  # the root's mass, as the walk takes it
     inv_l, inv_mt = _f32(1.0 / L), _f32(1.0 / mt)
     rec = {
         "c": _f32(nodes["center"] - origin), "slack": _f32(nodes["half"] * 1.0001),
-        "m": _f32(nodes["com"] - origin),
+        "m": cells[:, :3].copy(),
         "nbody": (nodes["end"].astype(np.int64) - nodes["begin"]),
         "leaf": nodes["n_children"] == 0,
     }
     half = _f32(nodes["half"])
-    delta = _f32(nodes["delta"])
-    mass = _f32(cells[:, 3])
-    qa, qb = _f32(cells[:, 4:8]), _f32(cells[:, 8:12])
+    mass = cells[:, 3]
+    qa, qb = cells[:, 4:8], cells[:, 8:12]
     qn = _f32(np.sqrt(qa[:, 0] ** 2 + qa[:, 1] ** 2 + qa[:, 2] ** 2
                       + 2.0 * (qa[:, 3] ** 2 + qb[:, 0] ** 2 + qb[:, 1] ** 2)))
     f1 = _log2f(np.maximum(half * inv_l, 1e-30))
@@ -256,18 +335,19 @@ def group_records(tpos, ranges, amag, rec, alpha, G):
     return gc, gh, f0, tau
 
 
-def walk_lists(nodes, cells, tpos, ranges, amag, model, alpha, G=1.0, theta_guard=1.5,
+def walk_lists(nodes, bodies, tpos, ranges, amag, model, alpha, G=1.0, theta_guard=1.5,
                band=None):
     """The learned walk on a tree whose every node comes after its parent
     (nodes['parent']; the device's walk order and the reference's layout
-    both qualify), amag the previous |a| of each body in tree order. Returns, per group, the accepted cells
+    both qualify), bodies the FP32 bodies relative to the root centre (tree
+    order), amag the previous |a| of each body in tree order. Returns, per group, the accepted cells
     (node indices) and the bodies (tree positions, with repeats), and per
     group the margins of its tests: a list of (node, kind, margin), margin
     relative to the threshold for FP32 tests (KIND_GEOM, KIND_PRIOR) and in
     log2 units for the network (KIND_NET)."""
     p = unpack(model)
     band = float(p["band"]) if band is None or band < 0 else float(band)
-    rec = node_records(nodes, cells, theta_guard, float(p["ymean"]))
+    rec = node_records(nodes, bodies, theta_guard, float(p["ymean"]))
     gc, gh, f0, tau = group_records(tpos, ranges, amag, rec, alpha, G)
     ng, m = len(ranges), len(nodes)
     l2 = _f32(_f32(1.0) / (rec["inv_l"] * rec["inv_l"]))

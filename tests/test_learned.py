@@ -452,8 +452,8 @@ def test_walk_oracle_covers_every_body_once():
     alpha = json.loads(MODEL_INFO.read_text())["alpha"]
     tree = ref_tree_with_parents(nodes)
     ranges = lists.groups[:, :2].astype(np.int64)
-    cells, bodies, margins = lo.walk_lists(tree, lists.cells, pos[order.astype(np.int64)], ranges,
-                                           amag, model, alpha)
+    cells, bodies, margins = lo.walk_lists(tree, lists.bodies, pos[order.astype(np.int64)],
+                                           ranges, amag, model, alpha)
     cl = np.concatenate(cells).astype(np.uint32)
     bl = np.concatenate(bodies).astype(np.uint32)
     nc = np.cumsum([0] + [len(c) for c in cells])
@@ -470,7 +470,8 @@ def test_walk_oracle_covers_every_body_once():
 def test_walk_decisions_match_oracle(gtc):
     """The device's learned lists against the oracle's restatement of the
     walk (committed model and alpha, 20k-body galaxy, the device's own tree,
-    groups and previous |a|): each group holds the same multiset of
+    FP32 bodies, groups and previous |a|; the FP32 moment estimates the walk
+    decides from restated too): each group holds the same multiset of
     accepted cells and of bodies, except under a test that lies within
     rounding of its threshold (2e-5 relative for the FP32 tests, 0.06 log2
     units for the network against its BF16 emulation)."""
@@ -491,7 +492,7 @@ def test_walk_decisions_match_oracle(gtc):
     assert np.array_equal(order, first["order"])
     amag = np.sqrt((first["out"][:, :3].astype(np.float64) ** 2).sum(1)).astype(np.float32)
     nodes, g = d["nodes"], d["groups"].astype(np.int64)
-    cells, bodies, margins = lo.walk_lists(nodes, d["cells"], pos[order], g[:, :2], amag, model,
+    cells, bodies, margins = lo.walk_lists(nodes, d["bodies"], pos[order], g[:, :2], amag, model,
                                            alpha)
     near = walk_margin_sets(nodes, margins)
     skip = nodes["skip"].astype(np.int64)
