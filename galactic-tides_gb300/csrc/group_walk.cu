@@ -916,7 +916,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u32 tb = ceil_div(slots, kT);
 
   // One pass into per-group slots when the last walk sized them and they
-  // fit 32-bit offsets and sixteen times the lists' own size (slots sized
+  // fit 32-bit offsets and sixteen times the lists' own size or 2^28
+  // entries, whichever is more (slots sized
   // by a two-pass walk's whole lists take about eight times for the
   // benchmark galaxy, those of a split walk about four): two threads per group, the
   // near field and the rest. Groups whose lists outgrow their slots are
@@ -930,7 +931,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   const u64 pool_c = Workspace::pool_for(ng, sl_c + sn_c), pool_b = Workspace::pool_for(ng, sl_b + sn_b);
   const u64 ext_c = pool_at_c + pool_c, ext_b = pool_at_b + pool_b;
   if (sl_c > 0 && ntasks == 1 && ext_c <= 0xffffffffull && ext_b <= 0xffffffffull &&
-      ext_c + ext_b <= std::max<u64>(16 * prev_entries, 1ull << 26)) {
+      ext_c + ext_b <= std::max<u64>(16 * prev_entries, 1ull << 28)) {
     ws.cell_list.ensure(ext_c * 4);
     ws.body_list.ensure(ext_b * 4);
     ws.spill.ensure(2ull * ng * sizeof(u32));
