@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -12,6 +13,7 @@
 
 #include "../../include/gtc.h"
 #include "context.cuh"
+#include "forest.cuh"
 #include "integrate.cuh"
 
 static_assert(sizeof(gtc_float4) == 16 && alignof(gtc_float4) == 16, "float4 layout");
@@ -610,8 +612,10 @@ __global__ void k_unpack_direct(const float4 *out, u32 n, double *acc, double *p
 }
 }  // namespace gtc
 
-// Independent systems advanced together: one context (stream, workspace)
-// per system, every system's step in one captured graph.
+// Independent systems advanced together. As one forest (every stage one
+// launch for all systems, forest.cu) when their shared parameters agree, or
+// with one context (stream, workspace) per system and every system's step
+// in one captured graph.
 struct gtc_ensemble {
   int device = 0;
   cudaStream_t main = nullptr;
@@ -620,6 +624,9 @@ struct gtc_ensemble {
   std::vector<gtc_context *> ctx;
   std::vector<GraphStep> sys;
   std::string error;
+  int forest_mode = -1;  // option "forest": 1 always, 0 never, -1 when eligible
+  int forest_walk = -1;  // option "walk_warps" of the forest's walk
+  std::unique_ptr<gtc::ForestRun> forest;
 };
 
 namespace {
@@ -640,6 +647,33 @@ gtc_status ensemble_guarded(gtc_ensemble *e, F &&f) {
   } catch (const std::exception &ex) {
     e->error = ex.what();
     return GTC_RUNTIME_ERROR;
+  }
+}
+
+// The ensemble's leapfrog as one forest; afterwards each system's context
+// holds its interaction counts of the last step's lists.
+void leapfrog_forest(gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs, double dt,
+                     u64 steps, bool prime, bool graph) {
+  (void)graph;
+  if (!e->forest) e->forest = std::make_unique<gtc::ForestRun>();
+  gtc::ForestRun &f = *e->forest;
+  cudaStream_t s = e->main;
+  f.setup(fs, s);
+  f.ws.walk_mode = e->forest_walk;
+  if (prime) f.solve(0, 0.0, s);
+  for (u64 k = 0; k < steps; ++k) f.step(dt, s);
+  const std::vector<gtc::ForestSystemStats> st = f.system_stats(s);
+  for (std::size_t k = 0; k < e->ctx.size(); ++k) {
+    gtc_stats &c = e->ctx[k]->stats;
+    c = gtc_stats{};
+    c.cell_interactions = st[k].cell_interactions;
+    c.body_interactions = st[k].body_interactions;
+    c.n_groups = static_cast<u32>(st[k].groups);
+    c.max_list = st[k].max_list;
+    c.criterion_used = GTC_CRITERION_THETA;
+    c.list_passes = f.ws.list_passes;
+    c.graph_steps = 0;
+    e->ctx[k]->have_group = false;  // the lists are the forest's
   }
 }
 
@@ -1318,12 +1352,49 @@ gtc_status gtc_ensemble_set_system(gtc_ensemble *e, uint32_t i, double *pos, dou
   });
 }
 
+gtc_status gtc_ensemble_set_option(gtc_ensemble *e, const char *name, double value) {
+  return ensemble_guarded(e, [&] {
+    if (!name) throw gtc::InvalidArgument("option name is required");
+    const std::string opt(name);
+    if (opt == "forest") {
+      if (value != -1 && value != 0 && value != 1)
+        throw gtc::InvalidArgument("forest is -1 (when eligible), 0 or 1");
+      e->forest_mode = static_cast<int>(value);
+    } else if (opt == "walk_warps") {
+      if (value != -1 && value != 0 && value != 1)
+        throw gtc::InvalidArgument("walk_warps is -1 (by group count), 0 or 1");
+      e->forest_walk = static_cast<int>(value);
+    } else {
+      throw gtc::InvalidArgument("unknown ensemble option: " + opt);
+    }
+  });
+}
+
 gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int prime,
                                  int graph) {
   return ensemble_guarded(e, [&] {
     if (!std::isfinite(dt)) throw gtc::InvalidArgument("dt must be finite");
     for (const GraphStep &g : e->sys)
       if (g.n == 0) throw gtc::InvalidArgument("every system must be set before stepping");
+    std::vector<gtc::ForestSystem> fs;
+    for (const GraphStep &g : e->sys) {
+      gtc::ForestSystem f;
+      f.pos = g.pos;
+      f.vel = g.vel;
+      f.acc = g.acc;
+      f.pot = g.pot;
+      f.mass = g.mass;
+      f.n = g.n;
+      f.sp = g.sp;
+      fs.push_back(f);
+    }
+    std::string why;
+    const bool can = gtc::ForestRun::eligible(fs, &why);
+    if (e->forest_mode == 1 && !can) throw gtc::InvalidArgument("forest: " + why);
+    if (e->forest_mode != 0 && can) {
+      leapfrog_forest(e, fs, dt, steps, prime != 0, graph != 0);
+      return;
+    }
     if (graph) {
       leapfrog_graph_systems(e->sys, dt, steps, prime != 0, e->main, e->fork, e->joins);
       return;

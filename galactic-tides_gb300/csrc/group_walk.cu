@@ -41,16 +41,29 @@ __device__ __forceinline__ u32 bounded(u32 cap, const u32 *dev) {
 struct NodeView {
   const u32 *nbegin, *nend, *skip;
   const u8 *isleaf;
+  // a forest: node depths (its roots are at depth 0), the system of each
+  // body, and each system's group size and packing
+  const u8 *depth = nullptr;
+  const u16 *sys = nullptr;
+  const u8 *gsize = nullptr, *gpack = nullptr;
 };
 
 __global__ void __launch_bounds__(kT)
-    k_group_marks(NodeView nv, u32 m, u32 n, u32 gs, int pack, u32 *mark,
+    k_group_marks(NodeView nv, u32 m, u32 gs, int pack, u32 *mark,
                   const u32 *m_dev = nullptr, const u32 *abort = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || p >= bounded(m, m_dev)) return;
-  const u32 size = nv.nend[p] - nv.nbegin[p];
-  if (p == 0 && (size <= gs || nv.isleaf[0])) {
-    for (u32 c = 0; c < n; c += gs) mark[c] = 1;
+  const u32 b0 = nv.nbegin[p], b1 = nv.nend[p];
+  bool root = p == 0;
+  if (nv.sys) {
+    const u16 k = nv.sys[b0];
+    gs = nv.gsize[k];
+    pack = nv.gpack[k];
+    root = nv.depth[p] == 0;
+  }
+  const u32 size = b1 - b0;
+  if (root && (size <= gs || nv.isleaf[p])) {
+    for (u32 c = b0; c < b1; c += gs) mark[c] = 1;
     return;
   }
   if (nv.isleaf[p] || size <= gs) return;
@@ -123,12 +136,17 @@ __device__ __forceinline__ u64 zero_equal_key(double v) {
 
 __global__ void __launch_bounds__(kT)
     k_group_box(const u32 *gbegin, const u32 *gend, u32 ng, const double *tpos,
-                const TreeRoot *root, double *gbox, float *gboxf, const u32 *ng_dev = nullptr,
-                const u32 *abort = nullptr) {
+                const TreeRoot *root, double *gbox, float *gboxf, const u32 *ng_dev,
+                const u32 *abort, ForestView fv) {
   // gboxf per group: centre (3), half-extent (3), magnitude bound, pad
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || g >= bounded(ng, ng_dev)) return;
   const u32 b0 = gbegin[g], b1 = gend[g];
+  if (fv.sys) {  // a forest: the group's system's root
+    const u16 k = fv.sys[b0];
+    root += k;
+    fv.group_root[g] = fv.root_node[k];
+  }
   // the reference's running min and max (v < lo, hi < v: the first of equal
   // values stays), compared on integer images of the doubles (+0 and -0
   // equal) instead of on the FP64 pipe
@@ -289,7 +307,7 @@ template <int kMode>
 __global__ void __launch_bounds__(kT)
     k_walk(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
            const float *gboxf, u32 ng_cap, const Task *tasks, u32 ntasks, WalkOut out,
-           Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+           Scalars *sc, const u32 *ng_dev, const u32 *abort, const u32 *group_root) {
   const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
   if (aborted(abort)) return;
   const u32 ng = bounded(ng_cap, ng_dev);
@@ -311,7 +329,8 @@ __global__ void __launch_bounds__(kT)
     bl = out.body_list + out.spill_bodies[g];
   }
   u32 nc = 0, nb = 0, exact = 0, visits = 0;
-  const Task task = tasks[t];
+  // (a forest has one task, its group's own root)
+  const Task task = group_root ? Task{group_root[g], kNone, 0u, 0u} : tasks[t];
   auto take = [&](const WalkRec32 &r, u32 i, int verdict) {
     const u32 nbody = r.nbody_leaf & 0x7fffffffu;
     if (verdict == 1 && nbody > kFewBodies) {
@@ -381,11 +400,11 @@ struct SplitOut {
   u32 cap;                 // groups the count arrays hold per part
 };
 
-// The root child that holds targets [b0, b1), or kNone.
-__device__ __forceinline__ u32 near_child(u32 b0, u32 b1, const uint4 *kids, const u8 *nchild,
-                                          const u32 *nbegin, const u32 *nend) {
-  const int k = nchild[0];
-  const uint4 k0 = kids[0], k1 = kids[1];
+// The child of `root` that holds targets [b0, b1), or kNone.
+__device__ __forceinline__ u32 near_child(u32 root, u32 b0, u32 b1, const uint4 *kids,
+                                          const u8 *nchild, const u32 *nbegin, const u32 *nend) {
+  const int k = nchild[root];
+  const uint4 k0 = kids[2ull * root], k1 = kids[2ull * root + 1];
   const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
   for (int j = 0; j < k && j < 8; ++j)
     if (nbegin[ch[j]] <= b0 && b1 <= nend[ch[j]]) return ch[j];
@@ -400,7 +419,7 @@ __global__ void __launch_bounds__(kWalkThreads)
     k_walk_split(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
                  const float *gboxf, const u32 *gbegin, const u32 *gend, const uint4 *kids,
                  const u8 *nchild, const u32 *nbegin, const u32 *nend, u32 ng_cap, SplitOut out,
-                 Scalars *sc, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+                 Scalars *sc, const u32 *ng_dev, const u32 *abort, const u32 *group_root) {
   const u64 tid = static_cast<u64>(blockIdx.x) * kWalkThreads + threadIdx.x;
   if (aborted(abort)) return;
   const u32 ng = bounded(ng_cap, ng_dev);
@@ -411,7 +430,9 @@ __global__ void __launch_bounds__(kWalkThreads)
                b1 = reinterpret_cast<const float4 *>(gboxf)[2ull * g + 1];
   const float gf[3] = {b0.x, b0.y, b0.z}, hf[3] = {b0.w, b1.x, b1.y};
   const float gbound = b1.z;
-  const u32 near = near_child(gbegin[g], gend[g], kids, nchild, nbegin, nend);
+  const u32 root = group_root ? group_root[g] : 0u;
+  // (a leaf root has no children: nchild 0)
+  const u32 near = near_child(root, gbegin[g], gend[g], kids, nchild, nbegin, nend);
   const u32 near_end = near == kNone ? 0u : load32(walk32, near).skip;
   const u32 cap_c = part ? out.slot_near_cells : out.slot_cells;
   const u32 cap_b = part ? out.slot_near_bodies : out.slot_bodies;
@@ -421,7 +442,8 @@ __global__ void __launch_bounds__(kWalkThreads)
   bool jumped = false;
   u32 i = 0, end = 0;
   if (part == 0) {
-    end = load32(walk32, 0).skip;
+    i = root;
+    end = load32(walk32, root).skip;
   } else if (near != kNone) {
     i = near;
     end = near_end;
@@ -517,15 +539,13 @@ template <int kMode>
 __global__ void __launch_bounds__(kWarpWalkThreads)
     k_walk_warp(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
                 const float *gboxf, u32 ng_cap, WarpWalkOut out, u32 *next_group, Scalars *sc,
-                const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
+                const u32 *ng_dev, const u32 *abort, const u32 *group_root) {
   __shared__ uint2 stack_all[kWarpWalkWarps][kWarpStack];
   if (aborted(abort)) return;
   const u32 ng = bounded(ng_cap, ng_dev);
   const int lane = threadIdx.x & 31;
   uint2 *stk = stack_all[threadIdx.x >> 5];
   const unsigned below = (1u << lane) - 1u;
-  const u32 root_end = load32(walk32, 0).skip;
-  const bool root_leaf = (load32(walk32, 0).nbody_leaf >> 31) != 0;
   u32 exact = 0, visits = 0;
   for (;;) {
     u32 g = 0;
@@ -553,7 +573,10 @@ __global__ void __launch_bounds__(kWarpWalkThreads)
     const float gbound = b1.z;
     u64 nc = 0, nb = 0;  // warp-uniform
     // the root contains every group and is opened, unless it is a leaf
-    if (lane == 0) stk[0] = root_leaf ? make_uint2(0u, root_end) : make_uint2(1u, root_end);
+    const u32 root = group_root ? group_root[g] : 0u;
+    const WalkRec32 rr = load32(walk32, root);
+    const bool root_leaf = (rr.nbody_leaf >> 31) != 0;
+    if (lane == 0) stk[0] = make_uint2(root_leaf ? root : root + 1, rr.skip);
     u32 top = 1;
     __syncwarp();
     while (top > 0) {
@@ -825,8 +848,21 @@ void launch_warp_walk(Workspace &ws, const WarpWalkOut &out, u32 ng_cap, Scalars
       1, std::min<u64>(ceil_div(ng_cap, kWarpWalkWarps), 8ull * static_cast<u64>(sms))));
   k_walk_warp<kMode><<<blocks, kWarpWalkThreads, 0, s>>>(
       ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
-      ws.gboxf.as<float>(), ng_cap, out, ws.walk_next.as<u32>(), sc, ng_dev, abort);
+      ws.gboxf.as<float>(), ng_cap, out, ws.walk_next.as<u32>(), sc, ng_dev, abort,
+      ws.forest.group_root);
   GTC_LAUNCH_CHECK();
+}
+
+// The node arrays the group choice reads (a forest's per-system fields too).
+NodeView node_view(const Workspace &ws) {
+  NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
+  if (ws.forest) {
+    nv.depth = ws.depth.as<u8>();
+    nv.sys = ws.forest.sys;
+    nv.gsize = ws.forest.group_size;
+    nv.gpack = ws.forest.pack;
+  }
+  return nv;
 }
 
 }  // namespace
@@ -853,8 +889,10 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
 
   // walk tasks (their count is read back with the group count)
   ws.tasks.ensure(m * sizeof(Task));
-  // (the learned walk splits each group's walk along its own path instead)
-  if (!lw) {
+  // (the learned walk splits each group's walk along its own path instead;
+  // a forest's groups walk their own system's tree whole, one task each)
+  const ForestView &fv = ws.forest;
+  if (!lw && !fv) {
     k_task_flags<<<mb, kT, 0, s>>>(ws.depth.as<u8>(), ws.isleaf.as<u8>(), m, ws.walk_split_depth,
                                    mark);
     GTC_LAUNCH_CHECK();
@@ -866,8 +904,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
 
   // groups
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
-  NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
-  k_group_marks<<<mb, kT, 0, s>>>(nv, m, n32, gs, sp.pack, mark);
+  const NodeView nv = node_view(ws);
+  k_group_marks<<<mb, kT, 0, s>>>(nv, m, gs, sp.pack, mark);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(mark, mscan, n, &sc->n_groups, ws.scan_tmp, s);
   ws.gbegin.ensure(n * 4);
@@ -884,12 +922,13 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, 3 * sizeof(unsigned long long), s));
   read_scalars(ws, host, s);
-  const u32 ng = host->n_groups, ntasks = host->aux;
+  const u32 ng = host->n_groups, ntasks = fv ? 1u : host->aux;
   ws.n_groups = ng;
   ws.walk_warps = ws.warps_for(ng);
   const u32 gb = ceil_div(ng, kT);
-  k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
-                                ws.gbox.as<double>(), ws.gboxf.as<float>());
+  k_group_box<<<gb, kT, 0, s>>>(gbegin, gend, ng, ws.tpos.as<double>(),
+                                fv ? fv.roots : ws.root.as<TreeRoot>(), ws.gbox.as<double>(),
+                                ws.gboxf.as<float>(), nullptr, nullptr, fv);
   GTC_LAUNCH_CHECK();
   if (lw) {
     // the learned walk decides from FP32 moment estimates: the FP64 moments
@@ -954,7 +993,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     } else {
       k_walk_split<<<ceil_div(2ull * ng, kWalkThreads), kWalkThreads, 0, s>>>(
           w32, w64, gbox, gboxf, gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
-          ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc);
+          ws.nbegin.as<u32>(), ws.nend.as<u32>(), ng, so, sc, nullptr, nullptr, fv.group_root);
       GTC_LAUNCH_CHECK();
     }
     k_split_spill<<<gb, kT, 0, s>>>(so, ng, pool_at_c, pool_c, pool_at_b, pool_b, spill_c, spill_b,
@@ -965,7 +1004,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     } else {
       WalkOut wo{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), nullptr, nullptr,
                  ws.cell_list.as<u32>(), ws.body_list.as<u32>(), spill_c, spill_b};
-      k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc);
+      k_walk<kSpill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, 1, wo, sc, nullptr,
+                                       nullptr, fv.group_root);
       GTC_LAUNCH_CHECK();
     }
     k_split_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, so, spill_c, spill_b,
@@ -1002,7 +1042,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   if (warps) {
     launch_warp_walk<kCount>(ws, wwo, ng, sc, s);
   } else {
-    k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
+    k_walk<kCount><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc, nullptr,
+                                     nullptr, fv.group_root);
     GTC_LAUNCH_CHECK();
   }
   exclusive_scan_u64(ws.gcells.as<u64>(), cell_off, slots, cell_off + slots, ws.scan_tmp, s);
@@ -1027,7 +1068,8 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     wwo.body_list = wo.body_list;
     launch_warp_walk<kFill>(ws, wwo, ng, sc, s);
   } else {
-    k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc);
+    k_walk<kFill><<<tb, kT, 0, s>>>(w32, w64, gbox, gboxf, ng, tasks, ntasks, wo, sc, nullptr,
+                                    nullptr, fv.group_root);
     GTC_LAUNCH_CHECK();
   }
   ws.stage(Workspace::kStWalk1, s);
@@ -1046,8 +1088,9 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   const u32 nb = ceil_div(n, kT), mb = ceil_div(mcap, kT);
   // groups (the one walk task, the root, was written before capture)
   GTC_CUDA(cudaMemsetAsync(mark, 0, n * 4, s));
-  NodeView nv{ws.nbegin.as<u32>(), ws.nend.as<u32>(), ws.skip.as<u32>(), ws.isleaf.as<u8>()};
-  k_group_marks<<<mb, kT, 0, s>>>(nv, mcap, n32, gs, sp.pack, mark, &sc->n_nodes, abort);
+  const ForestView &fv = ws.forest;
+  const NodeView nv = node_view(ws);
+  k_group_marks<<<mb, kT, 0, s>>>(nv, mcap, gs, sp.pack, mark, &sc->n_nodes, abort);
   GTC_LAUNCH_CHECK();
   exclusive_scan_u32(mark, mscan, n, &sc->n_groups, ws.scan_tmp, s);
   u32 *gbegin = ws.gbegin.as<u32>(), *gend = ws.gend.as<u32>();
@@ -1058,8 +1101,9 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, 3 * sizeof(unsigned long long), s));
-  k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(), ws.root.as<TreeRoot>(),
-                                ws.gbox.as<double>(), ws.gboxf.as<float>(), &sc->n_groups, abort);
+  k_group_box<<<nb, kT, 0, s>>>(gbegin, gend, n32, ws.tpos.as<double>(),
+                                fv ? fv.roots : ws.root.as<TreeRoot>(), ws.gbox.as<double>(),
+                                ws.gboxf.as<float>(), &sc->n_groups, abort, fv);
   GTC_LAUNCH_CHECK();
   // one pass into the captured slots (near field and rest), outgrown groups
   // again into the pools
@@ -1090,7 +1134,8 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
     k_walk_split<<<ceil_div(2ull * n, kWalkThreads), kWalkThreads, 0, s>>>(
         ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), ws.gbox.as<double>(),
         ws.gboxf.as<float>(), gbegin, gend, ws.kids.as<uint4>(), ws.nchild.as<u8>(),
-        ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort);
+        ws.nbegin.as<u32>(), ws.nend.as<u32>(), n32, so, sc, &sc->n_groups, abort,
+        fv.group_root);
     GTC_LAUNCH_CHECK();
   }
   k_split_spill<<<nb, kT, 0, s>>>(so, n32, pool_at_c, caps.pool_cells, pool_at_b,
@@ -1104,7 +1149,7 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
     const Task *tasks = ws.tasks.as<Task>();
     k_walk<kSpill><<<nb, kT, 0, s>>>(ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(),
                                      ws.gbox.as<double>(), ws.gboxf.as<float>(), n32, tasks, 1,
-                                     wo, sc, &sc->n_groups, abort);
+                                     wo, sc, &sc->n_groups, abort, fv.group_root);
     GTC_LAUNCH_CHECK();
   }
   k_split_records<<<nb, kT, 0, s>>>(gbegin, gend, n32, so, spill_c, spill_b,

@@ -64,7 +64,30 @@ struct SolverParams {
   double alpha;  // learned criterion's tolerance
 };
 
+// A forest: the bodies of several independent systems back to back (system
+// k at [start[k], start[k + 1])), each with its own root cube and tree, built
+// and walked by the same launches as one system. Sorted by (system, key),
+// system k keeps the same positions in tree order, so `sys` serves both
+// orders. Nodes are numbered as for one tree over all bodies: every
+// system's nodes form one contiguous range (the last system's first), its
+// root first. Null (systems == 0) for one system.
+struct ForestView {
+  u32 systems = 0;
+  const u16 *sys = nullptr;        // system of every body
+  const u32 *start = nullptr;      // systems + 1 body offsets
+  TreeRoot *roots = nullptr;       // per system: root cube
+  u32 *root_node = nullptr;        // per system: its root's node index
+  const u8 *group_size = nullptr;  // per system: group size
+  const u8 *pack = nullptr;        // per system: packing (0 off, 1 a group's worth, k >= 2 threshold)
+  u32 *group_root = nullptr;       // per group: its system's root node
+  const uint4 *bbox_blocks = nullptr;  // bounding-box blocks: (system, rank, blocks, 0)
+  const uint2 *sys_blocks = nullptr;   // per system: (first bounding-box block, blocks)
+  u32 bbox_nblocks = 0;
+  explicit operator bool() const { return systems > 0; }
+};
+
 struct Workspace {
+  ForestView forest;
   // bodies
   DeviceBuffer pos, mass;                 // staged caller input (host calls)
   DeviceBuffer acc, pot;                  // staged caller output (host calls)

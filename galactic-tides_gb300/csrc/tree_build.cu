@@ -58,6 +58,7 @@ __device__ __forceinline__ Dbl4 make_dbl4(double x, double y, double z, double w
 struct KeyView {
   const u64 *w0, *w1, *w2;
   int words;
+  const u16 *sys = nullptr;  // a forest: the system of each sorted position
 };
 
 __device__ __forceinline__ int word_lcp(u64 a, u64 b, int levels) {
@@ -69,6 +70,7 @@ __device__ __forceinline__ int word_lcp(u64 a, u64 b, int levels) {
 
 // Levels shared by the bodies at sorted positions a and b.
 __device__ __forceinline__ int lcp(const KeyView &kv, u32 a, u32 b) {
+  if (kv.sys && kv.sys[a] != kv.sys[b]) return -1;  // two systems share no node
   int l = word_lcp(kv.w0[a], kv.w0[b], kLevelsPerWord);
   if (l < kLevelsPerWord || kv.words == 1) return l;
   l = word_lcp(kv.w1[a], kv.w1[b], kLevelsPerWord);
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kT) k_bbox_partial(const double *pos, u64 n, d
 
 // Root cube from the reduced box (octree.cpp:184-198); min/max are exact in
 // any order, so the partial boxes are reduced by the whole block.
-__global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, TreeRoot *root) {
+__device__ void root_from_parts(const double *part, int nparts, TreeRoot *root) {
   double v[6];
   for (int a = 0; a < 3; ++a) {
     v[a] = INFINITY;
@@ -214,6 +216,58 @@ __global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, Tre
   int d = 0;
   while (d <= kMaxDepth && __double_as_longlong(root->half_at[d]) >= bound) ++d;
   root->tiny_from = d;
+}
+
+__global__ void __launch_bounds__(kT) k_root(const double *part, int nparts, TreeRoot *root) {
+  root_from_parts(part, nparts, root);
+}
+
+// A forest's boxes: block b covers part of system blk[b].x (rank blk[b].y of
+// its blk[b].z blocks), one partial box each; then one block per system
+// reduces that system's partials (sys_blk: first block, blocks) into its
+// root.
+__global__ void __launch_bounds__(kT)
+    k_bbox_forest(const double *pos, const uint4 *blk, const u32 *start, double *part) {
+  const uint4 q = blk[blockIdx.x];
+  const u64 b0 = start[q.x], b1 = start[q.x + 1];
+  const u64 inf_lo = order_key(INFINITY), inf_hi = order_key(-INFINITY);
+  u64 lo[3] = {inf_lo, inf_lo, inf_lo}, hi[3] = {inf_hi, inf_hi, inf_hi};
+  for (u64 i = b0 + static_cast<u64>(q.y) * kT + threadIdx.x; i < b1;
+       i += static_cast<u64>(q.z) * kT)
+    for (int a = 0; a < 3; ++a) {
+      const u64 k = order_key(pos[3 * i + a]);
+      lo[a] = k < lo[a] ? k : lo[a];
+      hi[a] = k > hi[a] ? k : hi[a];
+    }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o > 0; o >>= 1) {
+      const u64 l = __shfl_xor_sync(kFullMask, lo[a], o), h = __shfl_xor_sync(kFullMask, hi[a], o);
+      lo[a] = l < lo[a] ? l : lo[a];
+      hi[a] = h > hi[a] ? h : hi[a];
+    }
+  __shared__ u64 s[kT / 32][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int a = 0; a < 3; ++a) {
+      s[warp][a] = lo[a];
+      s[warp][3 + a] = hi[a];
+    }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    u64 v = s[0][threadIdx.x];
+    for (int w = 1; w < kT / 32; ++w) {
+      const u64 x = s[w][threadIdx.x];
+      v = threadIdx.x < 3 ? (x < v ? x : v) : (x > v ? x : v);
+    }
+    part[6 * blockIdx.x + threadIdx.x] = from_order_key(v);
+  }
+}
+
+__global__ void __launch_bounds__(kT)
+    k_root_forest(const double *part, const uint2 *sys_blk, TreeRoot *roots) {
+  const uint2 q = sys_blk[blockIdx.x];
+  root_from_parts(part + 6ull * q.x, static_cast<int>(q.y), roots + blockIdx.x);
 }
 
 // ------------------------------------------------------------------- keys
@@ -420,6 +474,68 @@ __global__ void __launch_bounds__(kT)
   tiny[i] = static_cast<u8>(t);
 }
 
+// A forest's first key word: the same levels as k_keys, every centre stepped
+// from the body's own system's root centre (the values k_keys takes from
+// its split table are these same sums).
+__global__ void __launch_bounds__(kT)
+    k_keys_forest(const double *pos, u32 n, const u16 *sys, const TreeRoot *roots, u64 *key,
+                  u32 *idx, u8 *tiny, u32 *error) {
+  const u32 i = blockIdx.x * kT + threadIdx.x;
+  if (i >= n) return;
+  const TreeRoot *root = roots + sys[i];
+  const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
+  if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicOr(error, 4u);
+  const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
+  int dt = root->tiny_from;
+  if (dt <= kLevelsPerWord) {
+    const long long maybe_tiny =
+        __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
+    dt = 0;
+    while (dt <= kLevelsPerWord && __double_as_longlong(root->half_at[dt]) >= maybe_tiny) ++dt;
+  }
+  double cx = root->center[0], cy = root->center[1], cz = root->center[2];
+  u64 k = 0;
+  int t = kNoTiny;
+  for (int d = 0; d < kLevelsPerWord; ++d) {
+    if (d >= dt && t == kNoTiny && tiny_node(root->half_at[d], cx, cy, cz)) t = d;
+    int o = (kx >= order_key(cx) ? 1 : 0) | (ky >= order_key(cy) ? 2 : 0) |
+            (kz >= order_key(cz) ? 4 : 0);
+    if (t != kNoTiny) o = 0;
+    k = (k << 3) | static_cast<u64>(o);
+    step_centre(cx, cy, cz, o, root->half_at[d + 1]);
+  }
+  if (dt <= kLevelsPerWord && t == kNoTiny && tiny_node(root->half_at[kLevelsPerWord], cx, cy, cz))
+    t = kLevelsPerWord;
+  key[i] = k;
+  idx[i] = i;
+  tiny[i] = static_cast<u8>(t);
+}
+
+// A forest's last sort pass, by system: the system of each sorted body as
+// the key, the position as the value; the key words and bodies are copied
+// aside for the gather that follows the pass.
+__global__ void __launch_bounds__(kT)
+    k_forest_sys_keys(const u64 *key, const u32 *idx, const u16 *sys, u32 n, u64 *skey, u32 *spos,
+                      u64 *key_copy, u32 *idx_copy, const u32 *abort = nullptr) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= n || aborted(abort)) return;
+  const u32 i = idx[k];
+  skey[k] = sys[i];
+  spos[k] = k;
+  key_copy[k] = key[k];
+  idx_copy[k] = i;
+}
+
+__global__ void __launch_bounds__(kT)
+    k_forest_gather(const u32 *spos, const u64 *key_copy, const u32 *idx_copy, u32 n, u64 *key,
+                    u32 *idx, const u32 *abort = nullptr) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= n || aborted(abort)) return;
+  const u32 j = spos[k];
+  key[k] = key_copy[j];
+  idx[k] = idx_copy[j];
+}
+
 // Per sorted position: levels shared with the next body, and the leaf depth.
 __global__ void __launch_bounds__(kT)
     k_levels(KeyView kv, const u32 *idx, const u8 *tiny, u32 n, int L, signed char *lcp_next,
@@ -484,6 +600,7 @@ __global__ void __launch_bounds__(kT)
   if (k >= nd) return;
   const u32 b = dpos[k];
   const u32 i = idx[b];
+  if (kv.sys) root += kv.sys[b];  // a forest: the body's system's root
   const int base = kLevelsPerWord * kv.words;
   double cx = root->center[0], cy = root->center[1], cz = root->center[2];
   for (int lvl = 1; lvl <= base; ++lvl) step_centre(cx, cy, cz, digit(kv, b, lvl), root->half_at[lvl]);
@@ -516,7 +633,8 @@ __global__ void __launch_bounds__(kT)
   bool start = k == 0;
   if (!start) {
     const u32 a = dpos[k - 1], b = dpos[k];
-    start = kv.w0[a] != kv.w0[b] || (kv.words > 1 && kv.w1[a] != kv.w1[b]);
+    start = kv.w0[a] != kv.w0[b] || (kv.words > 1 && kv.w1[a] != kv.w1[b]) ||
+            (kv.sys && kv.sys[a] != kv.sys[b]);
   }
   flag[k] = start ? 1u : 0u;
 }
@@ -564,19 +682,29 @@ __global__ void __launch_bounds__(kT)
   const u32 total = sc->n_nodes;
   const u32 first = total - count_scan[b] - c;  // nodes ending after b come first
   const int d0 = lcp_next[b] + 1, ld = leafdepth[b];
-  // centres from the split table down to its last level, stepped below it
+  // centres from the split table down to its last level, stepped below it;
+  // a forest (no table: `root` holds every system's root) steps them all
+  // from the system's root centre
+  const bool table = kv.sys == nullptr;
+  if (!table) root += kv.sys[b];
+  const int table_levels = table ? kSplitLevels : 0;
   const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
   u32 ix = 1, iy = 1, iz = 1;
   double cx = 0.0, cy = 0.0, cz = 0.0;
+  if (!table) {
+    cx = root->center[0];
+    cy = root->center[1];
+    cz = root->center[2];
+  }
   for (int d = 0; d <= ld; ++d) {
     if (d > 0) {
       const int o = digit(kv, b, d);
-      if (d < kSplitLevels) {
+      if (d < table_levels) {
         ix = 2 * ix + (o & 1);
         iy = 2 * iy + ((o >> 1) & 1);
         iz = 2 * iz + (o >> 2);
       } else {
-        if (d == kSplitLevels) {  // the table's deepest centre on this path
+        if (d == table_levels) {  // the table's deepest centre on this path
           cx = __ldg(tx + ix);
           cy = __ldg(ty + iy);
           cz = __ldg(tz + iz);
@@ -585,7 +713,7 @@ __global__ void __launch_bounds__(kT)
       }
     }
     if (d < d0) continue;
-    if (d < kSplitLevels) {
+    if (d < table_levels) {
       cx = __ldg(tx + ix);
       cy = __ldg(ty + iy);
       cz = __ldg(tz + iz);
@@ -604,7 +732,7 @@ __global__ void __launch_bounds__(kT)
   u32 start = b;  // shares at least d levels with b for every d here
   for (int d = ld; d >= d0; --d) {
     u32 lo = 0, hi = start;
-    if (d > 0) {
+    if (d > 0 || !table) {  // (a forest's root starts at its system's first body)
       for (u64 step = 1;; step *= 2) {  // 64-bit: never wraps to 0
         if (step > hi) break;  // lo stays 0
         const u32 cand = hi - static_cast<u32>(step);
@@ -653,6 +781,19 @@ __global__ void __launch_bounds__(kT)
   for (int j = 0; j < k; ++j) parent[ch[j]] = p;
   kids[2ull * p] = make_uint4(ch[0], ch[1], ch[2], ch[3]);
   kids[2ull * p + 1] = make_uint4(ch[4], ch[5], ch[6], ch[7]);
+}
+
+// A forest's roots: system k's root is the first (shallowest) of the nodes
+// ending at its last body, and has no parent.
+__global__ void __launch_bounds__(kT)
+    k_forest_roots(const u32 *start, u32 systems, const u32 *count, const u32 *count_scan,
+                   const Scalars *sc, u32 *root_node, u32 *parent, const u32 *abort = nullptr) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= systems || aborted(abort)) return;
+  const u32 last = start[k + 1] - 1;
+  const u32 r = sc->n_nodes - count_scan[last] - count[last];
+  root_node[k] = r;
+  parent[r] = 0xffffffffu;
 }
 
 // Input order inside each leaf (the reference never splits a leaf's range).
@@ -1082,9 +1223,10 @@ __global__ void __launch_bounds__(kT)
                  const double *delta, const u32 *nbegin, const u32 *nend, const u32 *skip,
                  const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta,
                  WalkRec32 *walk32, WalkRec64 *walk64, float4 *cells, const u32 *m_dev = nullptr,
-                 const u32 *abort = nullptr) {
+                 const u32 *abort = nullptr, const u16 *sys = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || p >= bounded(m, m_dev)) return;
+  if (sys) root += sys[nbegin[p]];  // a forest: relative to the node's system's root
   const Dbl4 g = load_pair(geom, p), c = load_pair(mom, p);
   const double crit = 2.0 * g.w * inv_theta + delta[p];
   WalkRec64 r;
@@ -1121,6 +1263,19 @@ __global__ void __launch_bounds__(kT)
   cells[3 * p + 1] = make_float4(static_cast<float>(qa.x), static_cast<float>(qa.y),
                                  static_cast<float>(qb.x), static_cast<float>(qb.y));
   cells[3 * p + 2] = make_float4(static_cast<float>(qc.x), static_cast<float>(qc.y), 0.0f, 0.0f);
+}
+
+// A forest's FP32 bodies, each relative to its system's root centre.
+__global__ void __launch_bounds__(kT)
+    k_pack_bodies_forest(const double *tpos, const double *tmass, u32 n, const u16 *sys,
+                         const TreeRoot *roots, float4 *bodies, const u32 *abort = nullptr) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= n || aborted(abort)) return;
+  const double *o = roots[sys[k]].center;
+  bodies[k] = make_float4(static_cast<float>(tpos[3ull * k] - o[0]),
+                          static_cast<float>(tpos[3ull * k + 1] - o[1]),
+                          static_cast<float>(tpos[3ull * k + 2] - o[2]),
+                          static_cast<float>(tmass[k]));
 }
 
 // FP32 bodies relative to `origin` (group_lists.cpp:46-50, gravity_backends.cpp:15-23).
@@ -1218,14 +1373,72 @@ namespace {
 // word, rounded up to whole 8-bit passes (21 or more: the whole word), and
 // returns the levels the order is exact for. Bodies that share those levels
 // keep their input order, which is all the tree needs while no leaf lies
-// deeper.
-int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s) {
+// deeper. A forest's pairs are then sorted by system, stably: (system,
+// key), each system at its own bodies' positions.
+int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s,
+                    const u32 *abort = nullptr) {
   const int passes = levels >= kLevelsPerWord ? 8 : (3 * std::max(levels, 1) + 7) / 8;
   const int low = std::max(0, 3 * kLevelsPerWord - 8 * passes);
   ws.sort_passes = passes;
   radix_sort_pairs(ws.key0.as<u64>(), ws.idx.as<u32>(), ws.key0_alt.as<u64>(),
                    ws.idx_alt.as<u32>(), n, 3 * kLevelsPerWord - low, ws.radix, s, low);
+  if (ws.forest) {
+    const ForestView &fv = ws.forest;
+    ws.dkey.ensure(n * 8ull);
+    ws.dkey_alt.ensure(n * 8ull);
+    ws.drec.ensure(n * 4ull);
+    ws.drec_alt.ensure(n * 4ull);
+    u64 *skey = ws.dkey.as<u64>();
+    u32 *spos = ws.drec.as<u32>();
+    const u32 nb = ceil_div(n, kT);
+    k_forest_sys_keys<<<nb, kT, 0, s>>>(ws.key0.as<u64>(), ws.idx.as<u32>(), fv.sys, n, skey,
+                                        spos, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), abort);
+    GTC_LAUNCH_CHECK();
+    int bits = 1;
+    while (bits < 16 && (1u << bits) < fv.systems) ++bits;
+    radix_sort_pairs(skey, spos, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), n, bits, ws.radix,
+                     s);
+    k_forest_gather<<<nb, kT, 0, s>>>(spos, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n,
+                                      ws.key0.as<u64>(), ws.idx.as<u32>(), abort);
+    GTC_LAUNCH_CHECK();
+  }
   return low == 0 ? kLevelsPerWord : (3 * kLevelsPerWord - low) / 3;
+}
+
+// A forest's root cubes (one per system) and first key words.
+void forest_keys(Workspace &ws, const double *pos, u32 n, cudaStream_t s) {
+  const ForestView &fv = ws.forest;
+  ws.bbox_part.ensure(6 * sizeof(double) * fv.bbox_nblocks);
+  k_bbox_forest<<<fv.bbox_nblocks, kT, 0, s>>>(pos, fv.bbox_blocks, fv.start,
+                                               ws.bbox_part.as<double>());
+  GTC_LAUNCH_CHECK();
+  k_root_forest<<<fv.systems, kT, 0, s>>>(ws.bbox_part.as<double>(), fv.sys_blocks, fv.roots);
+  GTC_LAUNCH_CHECK();
+  k_keys_forest<<<ceil_div(n, kT), kT, 0, s>>>(pos, n, fv.sys, fv.roots, ws.key0.as<u64>(),
+                                               ws.idx.as<u32>(), ws.tiny.as<u8>(),
+                                               &ws.scalars.as<Scalars>()->error);
+  GTC_LAUNCH_CHECK();
+}
+
+void forest_roots(Workspace &ws, const u32 *abort, cudaStream_t s) {
+  const ForestView &fv = ws.forest;
+  k_forest_roots<<<ceil_div(fv.systems, kT), kT, 0, s>>>(
+      fv.start, fv.systems, ws.count.as<u32>(), ws.count_scan.as<u32>(),
+      ws.scalars.as<Scalars>(), fv.root_node, ws.parent.as<u32>(), abort);
+  GTC_LAUNCH_CHECK();
+}
+
+void pack_bodies_tree(Workspace &ws, u32 n, const TreeRoot *root, const u32 *abort,
+                      cudaStream_t s) {
+  if (ws.forest) {
+    k_pack_bodies_forest<<<ceil_div(n, kT), kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(),
+                                                        n, ws.forest.sys, ws.forest.roots,
+                                                        ws.bodies.as<float4>(), abort);
+  } else {
+    k_pack_bodies<<<ceil_div(n, kT), kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n,
+                                                 root_centre(root), ws.bodies.as<float4>(), abort);
+  }
+  GTC_LAUNCH_CHECK();
 }
 }  // namespace
 
@@ -1257,19 +1470,21 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
 
   ws.stage(Workspace::kStBuild, s);
-  bbox_root(ws, pos, n, s);
-  const TreeRoot *root = ws.root.as<TreeRoot>();
+  const ForestView &fv = ws.forest;
+  if (fv) forest_keys(ws, pos, n32, s);
+  else bbox_root(ws, pos, n, s);
+  const TreeRoot *root = fv ? fv.roots : ws.root.as<TreeRoot>();
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  make_keys(ws, pos, n32, s);
+  if (!fv) make_keys(ws, pos, n32, s);
   // the levels the last tree needed first; all of them when a leaf lies
   // deeper (sorting the partly sorted pairs again gives the full order)
   ws.stage(Workspace::kStSort0, s);
   const int sorted = sort_top_levels(ws, n32, ws.sort_levels > 0 ? ws.sort_levels : kLevelsPerWord, s);
   ws.stage(Workspace::kStSort1, s);
 
-  KeyView kv{key0, nullptr, nullptr, 1};
+  KeyView kv{key0, nullptr, nullptr, 1, fv.sys};
   signed char *lcp_next = ws.lcp.as<signed char>();
   u8 *leafdepth = ws.leafdepth.as<u8>();
   // Node numbering: count the nodes ending at each sorted position (with
@@ -1387,6 +1602,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, ws.parent.as<u32>(),
                                ws.nchild.as<u8>(), ws.kids.as<uint4>());
   GTC_LAUNCH_CHECK();
+  if (fv) forest_roots(ws, nullptr, s);
   k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), m, idx);
   GTC_LAUNCH_CHECK();
   k_tree_order<<<nb, kT, 0, s>>>(pos, mass, idx, n32, ws.tpos.as<double>(), ws.tmass.as<double>());
@@ -1427,12 +1643,11 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                                   ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                                   ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
                                   1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
-                                  ws.walk64.as<WalkRec64>(), ws.cells.as<float4>());
+                                  ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), nullptr,
+                                  nullptr, fv.sys);
   GTC_LAUNCH_CHECK();
   ws.stage(Workspace::kStMom1, ms);
-  k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
-                                  root_centre(root), ws.bodies.as<float4>());
-  GTC_LAUNCH_CHECK();
+  pack_bodies_tree(ws, n32, root, nullptr, s);
 }
 
 void moments32(Workspace &ws, float4 *cells32, float *delta32, double2 *rootmom,
@@ -1464,15 +1679,17 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   Scalars *sc = ws.scalars.as<Scalars>();
   u32 *abort = &sc->abort;
   GTC_CUDA(cudaMemsetAsync(sc, 0, sizeof(Scalars), s));
-  bbox_root(ws, pos, n, s);
-  const TreeRoot *root = ws.root.as<TreeRoot>();
+  const ForestView &fv = ws.forest;
+  if (fv) forest_keys(ws, pos, n32, s);
+  else bbox_root(ws, pos, n, s);
+  const TreeRoot *root = fv ? fv.roots : ws.root.as<TreeRoot>();
   u64 *key0 = ws.key0.as<u64>();
   u32 *idx = ws.idx.as<u32>();
   u8 *tiny = ws.tiny.as<u8>();
-  make_keys(ws, pos, n32, s);
+  if (!fv) make_keys(ws, pos, n32, s);
   // the levels the captured depth allows: a deeper tree aborts the replay
   const int sorted = sort_top_levels(ws, n32, caps.depth + 1, s);
-  const KeyView kv{key0, nullptr, nullptr, 1};
+  const KeyView kv{key0, nullptr, nullptr, 1, fv.sys};
   signed char *lcp_next = ws.lcp.as<signed char>();
   u8 *leafdepth = ws.leafdepth.as<u8>();
   k_levels<<<nb, kT, 0, s>>>(kv, idx, tiny, n32, L, lcp_next, leafdepth, sc);
@@ -1491,6 +1708,7 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, ws.parent.as<u32>(),
                                ws.nchild.as<u8>(), ws.kids.as<uint4>(), m_dev, abort);
   GTC_LAUNCH_CHECK();
+  if (fv) forest_roots(ws, abort, s);
   k_leaf_order<<<mb, kT, 0, s>>>(ws.isleaf.as<u8>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(), mcap,
                                  idx, m_dev, abort);
   GTC_LAUNCH_CHECK();
@@ -1529,11 +1747,10 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
                                  ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
                                  ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, root,
                                  1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
-                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), m_dev, abort);
+                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), m_dev, abort,
+                                 fv.sys);
   GTC_LAUNCH_CHECK();
-  k_pack_bodies<<<nb, kT, 0, s>>>(ws.tpos.as<double>(), ws.tmass.as<double>(), n32,
-                                  root_centre(root), ws.bodies.as<float4>(), abort);
-  GTC_LAUNCH_CHECK();
+  pack_bodies_tree(ws, n32, root, abort, s);
 }
 
 }  // namespace gtc

@@ -170,6 +170,8 @@ def run_shard(models, mine, args, device):
         ens.set_system(k, g["pos"].data_ptr(), g["vel"].data_ptr(), g["mass"].data_ptr(),
                        g["acc"].data_ptr(), g["pot"].data_ptr(), g["n"], **kw)
         ens.context(k).set_option("walk_warps", g["walk_warps"])
+    ens.set_option("forest", args.forest)
+    torch.cuda.synchronize(dev)
     ens.leapfrog(args.dt, 2, prime=True, graph=True)  # capture and warm up
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -210,6 +212,8 @@ def main():
     ap.add_argument("--dt", type=float, default=0.01)
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--sample", type=int, default=1024)
+    ap.add_argument("--forest", type=int, default=-1, choices=(-1, 0, 1),
+                    help="the ensemble as one forest: -1 when eligible, 0 never, 1 always")
     args = ap.parse_args()
     args.rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

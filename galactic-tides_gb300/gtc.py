@@ -136,6 +136,7 @@ def _load():
         "gtc_ensemble_set_system": (I, [V, U32, P, P, P, P, P, U64, C.POINTER(GravityParams)]),
         "gtc_ensemble_leapfrog": (I, [V, D, U64, I, I]),
         "gtc_ensemble_context": (V, [V, U32]),
+        "gtc_ensemble_set_option": (I, [V, C.c_char_p, D]),
         "gtc_autotune_group": (I, [V, P, P, U64, C.POINTER(GravityParams),
                                    C.POINTER(GravityParams), C.POINTER(C.c_double),
                                    C.POINTER(C.c_int)]),
@@ -547,6 +548,11 @@ class Ensemble:
 
     def context(self, i):
         return _Borrowed(lib.gtc_ensemble_context(self.h, i))
+
+    def set_option(self, name, value):
+        """Ensemble options: "forest" (-1 when eligible, 0 never, 1 always)
+        and "walk_warps" (the forest walk: -1 by group count, 0, 1)."""
+        self._check(lib.gtc_ensemble_set_option(self.h, name.encode(), float(value)))
 
     def close(self):
         if self.h:

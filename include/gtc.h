@@ -309,10 +309,16 @@ gtc_status gtc_diagnostics_device(gtc_context *ctx, const double *pos, const dou
 
 /* ---- batched ensembles (no reference counterpart) ---------------------- */
 
-/* Independent systems (galaxies) advanced together: each has its own
- * context (stream, workspace), and with graph = 1 one CUDA graph launch
- * replays every system's whole step (kick, drift, rebuild, evaluation,
- * kick), the systems' kernel chains running concurrently. */
+/* Independent systems (galaxies) advanced together. When their G, theta,
+ * eps, quadrupole flag and leaf size agree (group size and packing may
+ * differ), as one forest: every system's bodies in one arena, one tree per
+ * system, and each stage of the step (kick and drift, boxes, keys, sort,
+ * topology, moments, groups, walk, evaluation, scatter, kick) one launch
+ * for all systems; each system moves to the same doubles as on its own.
+ * Otherwise (or with option "forest" 0) each system has its own context
+ * (stream, workspace), and with graph = 1 one CUDA graph launch replays
+ * every system's whole step, the systems' kernel chains running
+ * concurrently. */
 typedef struct gtc_ensemble gtc_ensemble;
 gtc_status gtc_ensemble_create(gtc_ensemble **e, int device, uint32_t systems);
 void gtc_ensemble_destroy(gtc_ensemble *e);
@@ -326,8 +332,14 @@ gtc_status gtc_ensemble_set_system(gtc_ensemble *e, uint32_t i, double *pos, dou
 /* gtc_leapfrog_device for every system: prime, then `steps` steps of dt. */
 gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int prime,
                                  int graph);
-/* System i's context (its stats, exports and options). */
+/* System i's context (its stats, exports and options). After a forest
+ * leapfrog its stats hold the system's interaction counts, group count and
+ * longest list of the last step (no times, no exports). */
 gtc_context *gtc_ensemble_context(gtc_ensemble *e, uint32_t i);
+/* Ensemble options: "forest" (-1 as one forest when eligible, the default;
+ * 1 always, an error when not eligible; 0 never) and "walk_warps" (the
+ * forest walk: -1 by group count, the default; 0 threads; 1 warps). */
+gtc_status gtc_ensemble_set_option(gtc_ensemble *e, const char *name, double value);
 
 /* The autotuner: times the grouped solver (theta criterion) on these bodies
  * (device arrays) for group_size 8, 16, 24, 32, each with sibling packing

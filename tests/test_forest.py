@@ -1,0 +1,116 @@
+"""The batched ensemble as one forest (csrc/forest.cu): every system's
+bodies in one arena, one tree per system, each stage one launch for all
+systems. Each system must move to the same doubles as on its own: the
+forest against the same ensemble stepped system by system (option
+"forest" 0), bitwise, over systems that exercise every branch of the
+build -- galaxies of uneven N with their own group size and packing, a
+clump deeper than one key word, coincident bodies (the tiny-node rule),
+and systems smaller than a group or a leaf."""
+
+import numpy as np
+import pytest
+
+from native import coincident_system, lopsided_sphere
+
+gpu = pytest.mark.gpu
+
+SOLVER = dict(G=1.0, theta=0.75, eps=0.025, quadrupole=True, leaf_size=8)
+
+
+def systems(gtc):
+    """(pos, vel, mass, group_size, pack) of each system."""
+    rng = np.random.default_rng(31)
+    out = []
+    for n, seed, gs, pack in [(12_000, 1, 32, 1), (30_000, 2, 16, 0), (8_000, 3, 24, 12)]:
+        pos, vel, mass, _ = gtc.make_galaxy(n, seed=seed)
+        out.append((pos, vel, mass, gs, pack))
+    wide = rng.normal(size=(3000, 3)) * 10.0
+    clump = np.concatenate([wide, 1.0 + rng.normal(size=(300, 3)) * 1e-7])
+    out.append((clump, rng.normal(size=clump.shape) * 0.1, rng.random(len(clump)) + 0.5, 8, 6))
+    pos, mass = coincident_system()
+    out.append((pos, np.zeros_like(pos), mass, 32, 1))
+    pos, mass = lopsided_sphere(5000, 7)
+    out.append((pos, rng.normal(size=pos.shape) * 0.05, mass, 16, 1))
+    for n in (1, 9):
+        pos, mass = lopsided_sphere(n, n + 40)
+        out.append((pos, np.zeros_like(pos), mass, 8, 1))
+    return out
+
+
+def run(gtc, specs, forest, walk, steps, prime=True):
+    import torch
+    d = torch.device("cuda", 0)
+    bufs = []
+    stats = []
+    with gtc.Ensemble(len(specs)) as ens:
+        for i, (pos, vel, mass, gs, pack) in enumerate(specs):
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(d)
+            n = len(mass)
+            b = dict(pos=t(pos), vel=t(vel), mass=t(mass),
+                     acc=torch.zeros((n, 3), dtype=torch.float64, device=d),
+                     pot=torch.zeros(n, dtype=torch.float64, device=d))
+            bufs.append(b)
+            ens.set_system(i, b["pos"].data_ptr(), b["vel"].data_ptr(), b["mass"].data_ptr(),
+                           b["acc"].data_ptr(), b["pot"].data_ptr(), n,
+                           **dict(SOLVER, group_size=gs, pack=pack))
+            ens.context(i).set_option("walk_warps", walk)
+        ens.set_option("forest", forest)
+        ens.set_option("walk_warps", walk)
+        torch.cuda.synchronize()  # the arrays are written on torch's stream
+        ens.leapfrog(0.01, steps, prime=prime, graph=False)
+        torch.cuda.synchronize()
+        for i in range(len(specs)):
+            st = ens.context(i).stats()
+            stats.append((st["cell_interactions"], st["body_interactions"], st["n_groups"]))
+    return [{k: v.cpu().numpy() for k, v in b.items()} for b in bufs], stats
+
+
+@gpu
+@pytest.mark.parametrize("walk", [0, 1])
+def test_forest_steps_equal_each_system_stepped_alone(gtc, walk):
+    specs = systems(gtc)
+    got, got_stats = run(gtc, specs, forest=1, walk=walk, steps=3)
+    want, want_stats = run(gtc, specs, forest=0, walk=walk, steps=3)
+    for i, (g, w) in enumerate(zip(got, want)):
+        for k in ("pos", "vel", "acc", "pot"):
+            assert np.array_equal(g[k], w[k]), (i, k)
+        assert np.all(np.isfinite(g["acc"]))
+    assert got_stats == want_stats
+
+
+@gpu
+def test_forest_force_evaluation_alone_equals_group_force(gtc):
+    """A prime with no steps is one forest force evaluation: each system's
+    forces are its own group_force's (walk by threads, the reference's list
+    order), bitwise."""
+    specs = systems(gtc)[:6]
+    got, _ = run(gtc, specs, forest=1, walk=0, steps=0)
+    with gtc.Context(0) as c:
+        c.set_option("walk_warps", 0)
+        for i, (pos, _, mass, gs, pack) in enumerate(specs):
+            acc, pot = c.group_force(pos, mass, group_size=gs, pack=pack, **SOLVER)
+            assert np.array_equal(got[i]["acc"], acc), i
+            assert np.array_equal(got[i]["pot"], pot), i
+
+
+@gpu
+def test_forest_refuses_mixed_parameters(gtc):
+    import torch
+    d = torch.device("cuda", 0)
+    pos, vel, mass, _ = gtc.make_galaxy(2000, seed=3)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(d)
+    arrays = [[t(pos), t(vel), t(mass), t(np.zeros((2000, 3))), t(np.zeros(2000))]
+              for _ in range(2)]
+    with gtc.Ensemble(2) as ens:
+        for i, (dp, dv, dm, da, dpt) in enumerate(arrays):
+            kw = dict(SOLVER, group_size=16, pack=1, theta=0.75 if i == 0 else 0.6)
+            ens.set_system(i, dp.data_ptr(), dv.data_ptr(), dm.data_ptr(), da.data_ptr(),
+                           dpt.data_ptr(), 2000, **kw)
+        ens.set_option("forest", 1)
+        with pytest.raises(gtc.GtcInvalidArgument, match="forest"):
+            ens.leapfrog(0.01, 1, prime=True, graph=False)
+        ens.set_option("forest", -1)  # not eligible: system by system
+        ens.leapfrog(0.01, 1, prime=True, graph=False)
+    with pytest.raises(gtc.GtcInvalidArgument):
+        with gtc.Ensemble(1) as ens:
+            ens.set_option("forest", 2)

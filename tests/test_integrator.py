@@ -216,9 +216,11 @@ def test_encounter_energy_drift(gtc):
 
 
 @gpu
-def test_ensemble_step_graph_equals_each_system_alone(gtc):
-    """Three galaxies advanced together (one graph launch per step, tuned-like
-    parameters per system) give bitwise the trajectories each gives alone."""
+@pytest.mark.parametrize("forest", [0, 1])
+def test_ensemble_step_graph_equals_each_system_alone(gtc, forest):
+    """Three galaxies advanced together, with tuned-like parameters per
+    system -- one graph launch per step of every system's kernel chains, or
+    as one forest -- give bitwise the trajectories each gives alone."""
     import torch
     specs = [(12_000, 1, 32, True), (30_000, 2, 16, False), (8_000, 3, 24, True)]
     alone = []
@@ -238,10 +240,12 @@ def test_ensemble_step_graph_equals_each_system_alone(gtc):
             kw = dict(SOLVER, group_size=gs, pack=pack)
             ens.set_system(i, dpos.data_ptr(), dvel.data_ptr(), dmass.data_ptr(), dacc.data_ptr(),
                            dpot.data_ptr(), n, **kw)
+        ens.set_option("forest", forest)
         ens.leapfrog(0.01, 5, prime=True, graph=True)
         torch.cuda.synchronize()
-        for i in range(len(specs)):
-            assert ens.context(i).stats()["graph_steps"] == 5
+        if not forest:
+            for i in range(len(specs)):
+                assert ens.context(i).stats()["graph_steps"] == 5
     for (dpos, dvel, dacc, dpot, _), want in zip(bufs, alone):
         assert np.array_equal(dpos.cpu().numpy(), want[0])
         assert np.array_equal(dvel.cpu().numpy(), want[1])
