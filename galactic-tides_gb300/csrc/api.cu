@@ -256,6 +256,75 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   ctx->last = sp;
 }
 
+// The capacities of a captured solve of n bodies and the buffers they need:
+// the last eager solve's sizes (hs, ws) with headroom (list slots with
+// twice the headroom: the longest of many lists moves more than the totals
+// do); offsets stay below 2^32 (a replay that needs more aborts).
+void reserve_graph(gtc::Workspace &ws, const gtc::Scalars &hs, double headroom, u64 n,
+                   gtc::GraphCaps &caps) {
+  const double f = 1.0 + headroom;
+  const u64 pad = headroom > 0 ? 1024 : 0;
+  caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
+  caps.depth = std::min<int>(gtc::kMaxDepth, static_cast<int>(hs.depth) + (pad ? 2 : 0));
+  // list slots: the last walk's group count, and its longest lists with
+  // twice the headroom (the longest of many lists moves more than the
+  // totals do); offsets stay below 2^32 (a replay that needs more aborts)
+  caps.groups = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_groups * f) + pad, n));
+  caps.groups = std::max<u32>(caps.groups, 1);
+  const double fs = 1.0 + 2.0 * headroom;
+  auto slot = [&](u32 longest) {
+    const u64 v = (static_cast<u64>(longest * fs) + (pad ? 64 : 0) + 31) & ~31ull;
+    const u64 most = (0xffffffffull / caps.groups / 2) & ~31ull;  // two slot arrays
+    return static_cast<u32>(std::max<u64>(32, std::min(v, most)));
+  };
+  // (the last walk split: rest and near field; the two passes: whole lists)
+  const bool split = ws.list_passes == 1;
+  caps.slot_cells = slot(hs.max_cells);
+  caps.slot_bodies = slot(hs.max_bodies);
+  caps.slot_near_cells = slot(split ? hs.max_near_cells : hs.max_cells);
+  caps.slot_near_bodies = slot(split ? hs.max_near_bodies : hs.max_bodies);
+  auto pool = [&](u32 rest, u32 near) {
+    const u64 used = static_cast<u64>(caps.groups) * (static_cast<u64>(rest) + near);
+    const u64 room = used < 0xffffffffull ? 0xffffffffull - used : 0;
+    return std::min<u64>(gtc::Workspace::pool_for(caps.groups, rest + near), room);
+  };
+  caps.pool_cells = pool(caps.slot_cells, caps.slot_near_cells);
+  caps.pool_bodies = pool(caps.slot_bodies, caps.slot_near_bodies);
+  const u64 m = caps.nodes;
+  ws.geom.ensure(m * 2 * sizeof(double2));
+  ws.mom.ensure(m * 2 * sizeof(double2));
+  ws.quad.ensure(m * 3 * sizeof(double2));
+  ws.delta.ensure(m * 8);
+  ws.nbegin.ensure(m * 4);
+  ws.nend.ensure(m * 4);
+  ws.skip.ensure(m * 4);
+  ws.parent.ensure(m * 4);
+  ws.depth.ensure(m);
+  ws.nchild.ensure(m);
+  ws.kids.ensure(m * 8 * sizeof(u32));
+  ws.isleaf.ensure(m);
+  ws.bucket.ensure(m * 4);
+  ws.walk32.ensure(m * sizeof(gtc::WalkRec32));
+  ws.walk64.ensure(m * sizeof(gtc::WalkRec64));
+  ws.cells.ensure(m * 3 * sizeof(float4));
+  if (!ws.forest) ws.split.ensure(3ull * gtc::kSplitSize * sizeof(double));  // (a forest steps)
+  ws.flags.ensure(std::max<u64>(n, m) * 4);
+  ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
+  ws.gcells.ensure(2 * n * 8);
+  ws.gbodies.ensure(2 * n * 8);
+  ws.gcell_off.ensure((n + 1) * 8);
+  ws.gbody_off.ensure((n + 1) * 8);
+  ws.groups.ensure(n * gtc::kGroupRecWords * 4);
+  ws.cell_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_cells + caps.slot_near_cells) +
+                       caps.pool_cells) * 4);
+  ws.body_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_bodies + caps.slot_near_bodies) +
+                       caps.pool_bodies) * 4);
+  ws.spill.ensure(2 * n * sizeof(u32));
+  ws.splitpt.ensure(2 * n * sizeof(u32));
+  ws.out.ensure(n * sizeof(float4));
+  gtc::reserve_scans(ws.scan_tmp, std::max<u64>(n, m));
+}
+
 // One system's leapfrog step inside a captured CUDA graph: kick and drift,
 // the whole grouped solve (tree, groups, walk, evaluation, scatter) and the
 // closing kick, with no host synchronisation inside. reserve() sizes the
@@ -274,70 +343,9 @@ struct GraphStep {
 
   void reserve() {
     gtc::Workspace &ws = ctx->ws;
-    const gtc::Scalars &hs = *ctx->host_sc;
-    const double f = 1.0 + ctx->graph_headroom;
-    const u64 pad = ctx->graph_headroom > 0 ? 1024 : 0;
-    caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
-    caps.depth = std::min<int>(gtc::kMaxDepth, static_cast<int>(hs.depth) + (pad ? 2 : 0));
-    // list slots: the last walk's group count, and its longest lists with
-    // twice the headroom (the longest of many lists moves more than the
-    // totals do); offsets stay below 2^32 (a replay that needs more aborts)
-    caps.groups = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_groups * f) + pad, n));
-    caps.groups = std::max<u32>(caps.groups, 1);
-    const double fs = 1.0 + 2.0 * ctx->graph_headroom;
-    auto slot = [&](u32 longest) {
-      const u64 v = (static_cast<u64>(longest * fs) + (pad ? 64 : 0) + 31) & ~31ull;
-      const u64 most = (0xffffffffull / caps.groups / 2) & ~31ull;  // two slot arrays
-      return static_cast<u32>(std::max<u64>(32, std::min(v, most)));
-    };
-    // (the last walk split: rest and near field; the two passes: whole lists)
-    const bool split = ws.list_passes == 1;
-    caps.slot_cells = slot(hs.max_cells);
-    caps.slot_bodies = slot(hs.max_bodies);
-    caps.slot_near_cells = slot(split ? hs.max_near_cells : hs.max_cells);
-    caps.slot_near_bodies = slot(split ? hs.max_near_bodies : hs.max_bodies);
-    auto pool = [&](u32 rest, u32 near) {
-      const u64 used = static_cast<u64>(caps.groups) * (static_cast<u64>(rest) + near);
-      const u64 room = used < 0xffffffffull ? 0xffffffffull - used : 0;
-      return std::min<u64>(gtc::Workspace::pool_for(caps.groups, rest + near), room);
-    };
-    caps.pool_cells = pool(caps.slot_cells, caps.slot_near_cells);
-    caps.pool_bodies = pool(caps.slot_bodies, caps.slot_near_bodies);
-    const u64 m = caps.nodes;
-    ws.geom.ensure(m * 2 * sizeof(double2));
-    ws.mom.ensure(m * 2 * sizeof(double2));
-    ws.quad.ensure(m * 3 * sizeof(double2));
-    ws.delta.ensure(m * 8);
-    ws.nbegin.ensure(m * 4);
-    ws.nend.ensure(m * 4);
-    ws.skip.ensure(m * 4);
-    ws.parent.ensure(m * 4);
-    ws.depth.ensure(m);
-    ws.nchild.ensure(m);
-    ws.kids.ensure(m * 8 * sizeof(u32));
-    ws.isleaf.ensure(m);
-    ws.bucket.ensure(m * 4);
-    ws.walk32.ensure(m * sizeof(gtc::WalkRec32));
-    ws.walk64.ensure(m * sizeof(gtc::WalkRec64));
-    ws.cells.ensure(m * 3 * sizeof(float4));
-    ws.split.ensure(3ull * gtc::kSplitSize * sizeof(double));
-    ws.flags.ensure(std::max<u64>(n, m) * 4);
-    ws.flags_scan.ensure(std::max<u64>(n, m) * 4);
-    ws.gcells.ensure(2 * n * 8);
-    ws.gbodies.ensure(2 * n * 8);
-    ws.gcell_off.ensure((n + 1) * 8);
-    ws.gbody_off.ensure((n + 1) * 8);
-    ws.groups.ensure(n * gtc::kGroupRecWords * 4);
-    ws.cell_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_cells + caps.slot_near_cells) +
-                         caps.pool_cells) * 4);
-    ws.body_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_bodies + caps.slot_near_bodies) +
-                         caps.pool_bodies) * 4);
-    ws.spill.ensure(2 * n * sizeof(u32));
-    ws.splitpt.ensure(2 * n * sizeof(u32));
-    ws.out.ensure(n * sizeof(float4));
+    reserve_graph(ws, *ctx->host_sc, ctx->graph_headroom, n, caps);
     ctx->counter.ensure(sizeof(u32));
     if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));
-    gtc::reserve_scans(ws.scan_tmp, std::max<u64>(n, m));
     gtc::write_root_task(ws, ctx->stream);
   }
 
@@ -626,6 +634,7 @@ struct gtc_ensemble {
   std::string error;
   int forest_mode = -1;  // option "forest": 1 always, 0 never, -1 when eligible
   int forest_walk = -1;  // option "walk_warps" of the forest's walk
+  double forest_headroom = 0.25;  // option "graph_headroom" of the forest's step graph
   std::unique_ptr<gtc::ForestRun> forest;
 };
 
@@ -650,18 +659,116 @@ gtc_status ensemble_guarded(gtc_ensemble *e, F &&f) {
   }
 }
 
-// The ensemble's leapfrog as one forest; afterwards each system's context
-// holds its interaction counts of the last step's lists.
+// The forest's leapfrog step inside a captured CUDA graph, as GraphStep
+// for one system: kick and drift of every system, the forest's build,
+// walk, evaluation and scatter with the closing kick, no host
+// synchronisation inside. A replay that outgrew the captured sizes (or
+// needs a second key word) aborts: its step is redone eagerly and the
+// graph captured again.
+struct ForestGraph {
+  gtc::ForestRun *f = nullptr;
+  double headroom = 0.25;
+  gtc::GraphCaps caps{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+
+  void drop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+
+  void record(double dt, cudaStream_t s) {
+    gtc::Workspace &ws = f->ws;
+    gtc::Scalars *sc = ws.scalars.as<gtc::Scalars>();
+    const double h = 0.5 * dt;
+    f->kick_drift(h, dt, s);
+    gtc::build_tree_graph(ws, f->apos.as<double>(), f->amass.as<double>(), f->n, f->sp, caps, s);
+    gtc::build_lists_graph(ws, f->sp, caps, s);
+    gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
+                              ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
+                              ws.groups.as<uint4>(), f->n, sc, static_cast<float>(f->sp.G),
+                              static_cast<float>(f->sp.eps * f->sp.eps), f->sp.quadrupole != 0,
+                              ws.out.as<float4>(), f->counter.as<u32>(), s);
+    f->scatter(1, h, &sc->abort, s);
+    GTC_CUDA(cudaMemcpyAsync(f->host_sc, sc, sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
+  }
+
+  void capture(double dt, cudaStream_t s) {
+    reserve_graph(f->ws, *f->host_sc, headroom, f->n, caps);
+    GTC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      record(dt, s);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      (void)cudaGetLastError();
+      throw;
+    }
+    GTC_CUDA(cudaStreamEndCapture(s, &graph));
+    GTC_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  }
+
+  // After a replay and its synchronisation: true if the step was redone
+  // eagerly (the graph must be captured again).
+  bool finish(double dt, cudaStream_t s) {
+    gtc::Workspace &ws = f->ws;
+    const gtc::Scalars &hs = *f->host_sc;
+    if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
+    if (hs.error)
+      throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                              std::to_string(hs.error) + ")");
+    if (hs.abort) {
+      f->solve(1, 0.5 * dt, s);
+      return true;
+    }
+    ws.n_nodes = hs.n_nodes;
+    ws.n_groups = hs.n_groups;
+    ws.n_cell_list = hs.n_cell_list;
+    ws.n_body_list = hs.n_body_list;
+    ws.gapped = true;  // replays walk once into the captured slots
+    ws.lists_unordered = ws.walk_warps;
+    ws.list_passes = 1;
+    return false;
+  }
+};
+
+// The ensemble's leapfrog as one forest, eager or with every step replayed
+// from one CUDA graph; afterwards each system's context holds its
+// interaction counts of the last step's lists.
 void leapfrog_forest(gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs, double dt,
                      u64 steps, bool prime, bool graph) {
-  (void)graph;
   if (!e->forest) e->forest = std::make_unique<gtc::ForestRun>();
   gtc::ForestRun &f = *e->forest;
   cudaStream_t s = e->main;
   f.setup(fs, s);
   f.ws.walk_mode = e->forest_walk;
-  if (prime) f.solve(0, 0.0, s);
-  for (u64 k = 0; k < steps; ++k) f.step(dt, s);
+  u64 replays = 0;
+  if (!graph) {
+    if (prime) f.solve(0, 0.0, s);
+    for (u64 k = 0; k < steps; ++k) f.step(dt, s);
+  } else {
+    // an eager solve sizes the buffers (with prime, the priming forces)
+    f.solve(0, 0.0, s, prime);
+    ForestGraph fg;
+    fg.f = &f;
+    fg.headroom = e->forest_headroom;
+    try {
+      for (u64 k = 0; k < steps; ++k) {
+        if (!fg.exec) fg.capture(dt, s);
+        GTC_CUDA(cudaGraphLaunch(fg.exec, s));
+        GTC_CUDA(cudaStreamSynchronize(s));
+        if (fg.finish(dt, s)) fg.drop();
+        else ++replays;
+      }
+    } catch (...) {
+      fg.drop();
+      throw;
+    }
+    fg.drop();
+  }
   const std::vector<gtc::ForestSystemStats> st = f.system_stats(s);
   for (std::size_t k = 0; k < e->ctx.size(); ++k) {
     gtc_stats &c = e->ctx[k]->stats;
@@ -672,7 +779,7 @@ void leapfrog_forest(gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs, 
     c.max_list = st[k].max_list;
     c.criterion_used = GTC_CRITERION_THETA;
     c.list_passes = f.ws.list_passes;
-    c.graph_steps = 0;
+    c.graph_steps = static_cast<u32>(replays);
     e->ctx[k]->have_group = false;  // the lists are the forest's
   }
 }
@@ -1364,6 +1471,9 @@ gtc_status gtc_ensemble_set_option(gtc_ensemble *e, const char *name, double val
       if (value != -1 && value != 0 && value != 1)
         throw gtc::InvalidArgument("walk_warps is -1 (by group count), 0 or 1");
       e->forest_walk = static_cast<int>(value);
+    } else if (opt == "graph_headroom") {
+      if (!(value >= 0 && value <= 4)) throw gtc::InvalidArgument("graph_headroom is 0..4");
+      e->forest_headroom = value;
     } else {
       throw gtc::InvalidArgument("unknown ensemble option: " + opt);
     }

@@ -223,7 +223,7 @@ void ForestRun::scatter(int kick, double h, const u32 *abort, cudaStream_t s) {
   GTC_LAUNCH_CHECK();
 }
 
-void ForestRun::solve(int kick, double h, cudaStream_t s) {
+void ForestRun::solve(int kick, double h, cudaStream_t s, bool write) {
   if (n == 0) return;
   {
     const SideJoin side_join{ws, s};
@@ -235,7 +235,7 @@ void ForestRun::solve(int kick, double h, cudaStream_t s) {
                  ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
                  static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
                  sp.quadrupole != 0, ws.out.as<float4>(), counter.as<u32>(), s);
-  scatter(kick, h, nullptr, s);
+  if (write) scatter(kick, h, nullptr, s);
   GTC_CUDA(cudaMemcpyAsync(host_sc, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
   if (host_sc->error & 4u) throw InvalidArgument("cuda: positions must be finite");

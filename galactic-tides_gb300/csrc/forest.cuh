@@ -47,8 +47,9 @@ struct ForestRun {
   // positions and masses.
   void setup(const std::vector<ForestSystem> &systems, cudaStream_t s);
   // One force evaluation of every system into its acc and pot (with kick:
-  // then v += h a).
-  void solve(int kick, double h, cudaStream_t s);
+  // then v += h a); without write, the systems' arrays are left as they are
+  // (a solve that only sizes the buffers).
+  void solve(int kick, double h, cudaStream_t s, bool write = true);
   // One leapfrog step of every system (integrator.cpp:5-17).
   void step(double dt, cudaStream_t s);
   void kick_drift(double h, double dt, cudaStream_t s);

@@ -141,19 +141,22 @@ def run_shard(models, mine, args, device):
     tuner = gtc.Context(device)
     t0 = time.perf_counter()
     for g in gal:
-        gs, pack, ms, walk = tuner.autotune_group(g["pos"].data_ptr(), g["mass"].data_ptr(),
-                                                  g["n"], **SOLVER)
+        if args.tune:
+            gs, pack, ms, walk = tuner.autotune_group(g["pos"].data_ptr(), g["mass"].data_ptr(),
+                                                      g["n"], **SOLVER)
+        else:  # the benchmark's defaults
+            gs, pack, ms, walk = SOLVER["group_size"], 1, 0.0, -1
         g.update(group_size=gs, pack=pack, tuned_ms=ms, walk_warps=walk)
     shard["autotune_seconds"] = time.perf_counter() - t0
 
     # one after another, default parameters, eager: the unbatched baseline
-    for g in gal:
+    for g in (gal if args.sequential else []):
         tuner.group_force_device(g["pos"].data_ptr(), g["mass"].data_ptr(), g["n"],
                                  g["acc"].data_ptr(), g["pot"].data_ptr(), **SOLVER)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     seq_inter = 0
-    for g in gal:
+    for g in (gal if args.sequential else []):
         tuner.group_force_device(g["pos"].data_ptr(), g["mass"].data_ptr(), g["n"],
                                  g["acc"].data_ptr(), g["pot"].data_ptr(), **SOLVER)
         st = tuner.stats()
@@ -214,6 +217,10 @@ def main():
     ap.add_argument("--sample", type=int, default=1024)
     ap.add_argument("--forest", type=int, default=-1, choices=(-1, 0, 1),
                     help="the ensemble as one forest: -1 when eligible, 0 never, 1 always")
+    ap.add_argument("--tune", type=int, default=1, choices=(0, 1),
+                    help="0: the benchmark's group size and packing for every galaxy")
+    ap.add_argument("--sequential", type=int, default=1, choices=(0, 1),
+                    help="0: no one-after-another baseline")
     args = ap.parse_args()
     args.rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -229,7 +236,8 @@ def main():
         out = combine(shards, args.steps)
         seq_t = sum(s.get("sequential_seconds", 0.0) for s in shards)
         out["sequential_interactions_per_s"] = (
-            sum(s.get("sequential_interactions", 0) for s in shards) / seq_t if seq_t else None)
+            sum(s.get("sequential_interactions", 0) for s in shards) / seq_t
+            if seq_t and args.sequential else None)
         out["autotune_seconds"] = round(max(s.get("autotune_seconds", 0.0) for s in shards), 2)
         out["note"] = ("ensemble steps include kicks and drifts; the sequential baseline is one "
                        "force evaluation per galaxy with default group_size 32, packing on")

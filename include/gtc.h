@@ -337,8 +337,11 @@ gtc_status gtc_ensemble_leapfrog(gtc_ensemble *e, double dt, uint64_t steps, int
  * longest list of the last step (no times, no exports). */
 gtc_context *gtc_ensemble_context(gtc_ensemble *e, uint32_t i);
 /* Ensemble options: "forest" (-1 as one forest when eligible, the default;
- * 1 always, an error when not eligible; 0 never) and "walk_warps" (the
- * forest walk: -1 by group count, the default; 0 threads; 1 warps). */
+ * 1 always, an error when not eligible; 0 never), "walk_warps" (the forest
+ * walk: -1 by group count, the default; 0 threads; 1 warps) and
+ * "graph_headroom" (the forest's step graph: buffer headroom over the last
+ * sizes, default 0.25; a replay that outgrows it, or whose tree needs a
+ * second key word, is redone eagerly and the graph captured again). */
 gtc_status gtc_ensemble_set_option(gtc_ensemble *e, const char *name, double value);
 
 /* The autotuner: times the grouped solver (theta criterion) on these bodies

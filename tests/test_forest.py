@@ -37,7 +37,7 @@ def systems(gtc):
     return out
 
 
-def run(gtc, specs, forest, walk, steps, prime=True):
+def run(gtc, specs, forest, walk, steps, prime=True, graph=False, headroom=None):
     import torch
     d = torch.device("cuda", 0)
     bufs = []
@@ -56,12 +56,15 @@ def run(gtc, specs, forest, walk, steps, prime=True):
             ens.context(i).set_option("walk_warps", walk)
         ens.set_option("forest", forest)
         ens.set_option("walk_warps", walk)
+        if headroom is not None:
+            ens.set_option("graph_headroom", headroom)
         torch.cuda.synchronize()  # the arrays are written on torch's stream
-        ens.leapfrog(0.01, steps, prime=prime, graph=False)
+        ens.leapfrog(0.01, steps, prime=prime, graph=graph)
         torch.cuda.synchronize()
         for i in range(len(specs)):
             st = ens.context(i).stats()
-            stats.append((st["cell_interactions"], st["body_interactions"], st["n_groups"]))
+            stats.append((st["cell_interactions"], st["body_interactions"], st["n_groups"],
+                          st["graph_steps"]))
     return [{k: v.cpu().numpy() for k, v in b.items()} for b in bufs], stats
 
 
@@ -76,6 +79,28 @@ def test_forest_steps_equal_each_system_stepped_alone(gtc, walk):
             assert np.array_equal(g[k], w[k]), (i, k)
         assert np.all(np.isfinite(g["acc"]))
     assert got_stats == want_stats
+
+
+@gpu
+@pytest.mark.parametrize("deep, headroom", [(False, 0.25), (False, 0.0), (True, 0.25)])
+def test_forest_graph_steps_equal_eager_steps(gtc, deep, headroom):
+    """Every step replayed from one captured graph of the whole forest step
+    gives bitwise the eager steps. With no headroom most replays outgrow the
+    captured sizes, and a tree that needs a second key word aborts every
+    replay: those steps are redone eagerly, to the same doubles."""
+    specs = [s for i, s in enumerate(systems(gtc)) if deep or i not in (3, 4)]  # (deeper than 21)
+    got, got_stats = run(gtc, specs, forest=1, walk=0, steps=4, graph=True, headroom=headroom)
+    want, want_stats = run(gtc, specs, forest=1, walk=0, steps=4)
+    for i, (g, w) in enumerate(zip(got, want)):
+        for k in ("pos", "vel", "acc", "pot"):
+            assert np.array_equal(g[k], w[k]), (i, k)
+    assert [s[:3] for s in got_stats] == [s[:3] for s in want_stats]
+    replays = got_stats[0][3]
+    if deep:
+        assert replays == 0
+    elif headroom > 0:
+        assert replays == 4
+    assert all(s[3] == replays for s in got_stats)
 
 
 @gpu

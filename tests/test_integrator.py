@@ -243,9 +243,8 @@ def test_ensemble_step_graph_equals_each_system_alone(gtc, forest):
         ens.set_option("forest", forest)
         ens.leapfrog(0.01, 5, prime=True, graph=True)
         torch.cuda.synchronize()
-        if not forest:
-            for i in range(len(specs)):
-                assert ens.context(i).stats()["graph_steps"] == 5
+        for i in range(len(specs)):
+            assert ens.context(i).stats()["graph_steps"] == 5
     for (dpos, dvel, dacc, dpot, _), want in zip(bufs, alone):
         assert np.array_equal(dpos.cpu().numpy(), want[0])
         assert np.array_equal(dvel.cpu().numpy(), want[1])
