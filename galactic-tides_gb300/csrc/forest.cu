@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kT)
 ForestRun::~ForestRun() {
   ws.release_all();
   DeviceBuffer *own[] = {&tables, &sysid, &roots, &root_node, &group_root, &apos, &amass, &stats,
-                         &counter};
+                         &counter, &split_flags};
   for (DeviceBuffer *b : own) b->release();
   if (host_sc) cudaFreeHost(host_sc);
 }
@@ -182,6 +182,9 @@ void ForestRun::setup(const std::vector<ForestSystem> &systems, cudaStream_t s) 
   apos.ensure(std::max<u64>(1, n) * 24);
   amass.ensure(std::max<u64>(1, n) * 8);
   stats.ensure(k * sizeof(ForestSystemStats));
+  split_flags.ensure(k * sizeof(u32));
+  int T = kLevelsPerWord;
+  while (T > 1 && 3ull * k * (1ull << T) * sizeof(double) > kSplitBudget) --T;
   counter.ensure(sizeof(u32));
   if (!host_sc) GTC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host_sc), sizeof(Scalars)));
   char *t = tables.as<char>();
@@ -197,6 +200,8 @@ void ForestRun::setup(const std::vector<ForestSystem> &systems, cudaStream_t s) 
   fv.bbox_blocks = reinterpret_cast<const uint4 *>(t + off_blk);
   fv.sys_blocks = reinterpret_cast<const uint2 *>(t + off_sblk);
   fv.bbox_nblocks = static_cast<u32>(blk.size());
+  fv.split_levels = T;
+  fv.split_unsorted = split_flags.as<u32>();
   ptrs_dev = reinterpret_cast<const ForestSystemPtrs *>(t + off_ptrs);
   if (n == 0) return;
   k_forest_sys<<<ceil_div(n, kT), kT, 0, s>>>(fv.start, k, static_cast<u32>(n), sysid.as<u16>());

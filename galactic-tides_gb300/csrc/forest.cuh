@@ -31,7 +31,11 @@ struct ForestRun {
   std::vector<ForestSystem> sys;
   SolverParams sp{};            // the shared parameters (group size and packing per system)
   u64 n = 0;                    // bodies in all
-  DeviceBuffer tables, sysid, roots, root_node, group_root, apos, amass, stats, counter;
+  DeviceBuffer tables, sysid, roots, root_node, group_root, apos, amass, stats, counter,
+      split_flags;
+  // Memory for the systems' split tables: each gets levels 0..T-1 (3 x 2^T
+  // doubles), T the most levels (up to the 21 of one key word) within it.
+  static constexpr u64 kSplitBudget = 256ull << 20;
   const ForestSystemPtrs *ptrs_dev = nullptr;
   Scalars *host_sc = nullptr;   // pinned
 

@@ -720,6 +720,8 @@ __global__ void __launch_bounds__(kT)
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort)) return;
   const bool valid = g < bounded(ng, ng_dev);
+  // (a replay's grid covers every body: warps past the groups leave at once)
+  if (__ballot_sync(kFullMask, valid) == 0) return;
   u64 t = 0, rc = 0, rb = 0, nc = 0, nb = 0;
   if (valid) {
     rc = out.ncells[g];

@@ -80,6 +80,8 @@ struct ForestView {
   const u8 *group_size = nullptr;  // per system: group size
   const u8 *pack = nullptr;        // per system: packing (0 off, 1 a group's worth, k >= 2 threshold)
   u32 *group_root = nullptr;       // per group: its system's root node
+  int split_levels = 0;            // levels T of each system's split table (2^T per axis)
+  u32 *split_unsorted = nullptr;   // per system: its table's in-order values decrease somewhere
   const uint4 *bbox_blocks = nullptr;  // bounding-box blocks: (system, rank, blocks, 0)
   const uint2 *sys_blocks = nullptr;   // per system: (first bounding-box block, blocks)
   u32 bbox_nblocks = 0;

@@ -474,15 +474,110 @@ __global__ void __launch_bounds__(kT)
   tiny[i] = static_cast<u8>(t);
 }
 
-// A forest's first key word: the same levels as k_keys, every centre stepped
-// from the body's own system's root centre (the values k_keys takes from
-// its split table are these same sums).
+// A forest's split tables: per system and axis, levels 0..T-1 of the same
+// table as above (heap order, 2^T entries, the system's own root), T set by
+// the forest's memory budget. Built by the same operations as the
+// single-system table: levels 0..min(T, kSplitTop)-1 by one block per
+// (system, axis), the rest by subtrees of 4, 2 or 1 levels.
+__global__ void __launch_bounds__(1024)
+    k_split_top_forest(const TreeRoot *roots, double *split, u32 size, int top) {
+  const u32 sa = blockIdx.x;  // system * 3 + axis
+  const TreeRoot *root = roots + sa / 3;
+  double *t = split + static_cast<u64>(sa) * size;
+  if (threadIdx.x == 0) t[1] = root->center[sa % 3];
+  __syncthreads();
+  for (int d = 1; d < top; ++d) {
+    const double h = root->half_at[d];
+    for (u32 j = threadIdx.x; j < (1u << d); j += blockDim.x) {
+      const u32 k = (1u << d) + j;
+      const double c = t[k >> 1];
+      t[k] = c + ((k & 1u) ? h : -h);  // step_centre's operation
+    }
+    __syncthreads();
+  }
+}
+
+template <int Levels>
 __global__ void __launch_bounds__(kT)
-    k_keys_forest(const double *pos, u32 n, const u16 *sys, const TreeRoot *roots, u64 *key,
-                  u32 *idx, u8 *tiny, u32 *error) {
+    k_split_sub_forest(const TreeRoot *roots, double *split, u32 size, u32 tables, int from) {
+  const u32 per_axis = 1u << from;
+  const u64 tid = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (tid >= static_cast<u64>(tables) * per_axis) return;
+  const u32 sa = static_cast<u32>(tid / per_axis);
+  const TreeRoot *root = roots + sa / 3;
+  double *t = split + static_cast<u64>(sa) * size;
+  const u32 base = per_axis + static_cast<u32>(tid % per_axis);
+  double v[2 << Levels];
+  v[1] = t[base];
+#pragma unroll
+  for (int l = 1; l <= Levels; ++l) {
+    const double h = root->half_at[from + l];
+#pragma unroll
+    for (int j = 0; j < (1 << l); ++j) {
+      const int k = (1 << l) + j;
+      v[k] = v[k >> 1] + ((k & 1) ? h : -h);
+      t[(static_cast<u64>(base) << l) + j] = v[k];
+    }
+  }
+}
+
+// Heap index of in-order position p in a table of `levels` levels.
+__device__ __forceinline__ u32 split_heap_at(u32 p, int levels) {
+  const u32 q = p + 1;
+  const int tz = __ffs(q) - 1;
+  return (1u << (levels - 1 - tz)) + (q >> (tz + 1));
+}
+
+// k_split_check per (system, axis) table; a system whose in-order values
+// decrease somewhere gets its flag set (its keys then walk the table level
+// by level).
+__global__ void __launch_bounds__(kT)
+    k_split_check_forest(const double *split, u32 size, int levels, u32 tables, u32 *unsorted) {
+  const u32 leaves = 1u << (levels - 1);
+  const u64 t = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
+  if (t >= static_cast<u64>(tables) * leaves) return;
+  const u32 sa = static_cast<u32>(t / leaves);
+  const double *s = split + static_cast<u64>(sa) * size;
+  const u32 j = static_cast<u32>(t % leaves), p = 2 * j, values = size - 1;
+  const u64 v = order_key(s[leaves + j]);
+  bool bad = false;
+  if (j > 0) bad |= order_key(s[split_heap_at(p - 1, levels)]) > v;
+  if (p + 1 < values) bad |= v > order_key(s[split_heap_at(p + 1, levels)]);
+  if (bad) atomicOr(unsorted + sa / 3, 1u);
+}
+
+// split_rank on a table of `levels` levels (values = 2^levels - 1).
+__device__ __forceinline__ bool split_rank_at(const double *table, u64 kx, double x,
+                                              double lo_edge, float inv_w, int levels,
+                                              u32 &r) {
+  const u32 values = (1u << levels) - 1;
+  const float g = static_cast<float>(x - lo_edge) * inv_w;
+  int v = g > 0.f ? static_cast<int>(fminf(g, static_cast<float>(values))) : 0;
+  for (int it = 0; it < 4; ++it) {
+    if (v > 0 && kx < order_key(__ldg(table + split_heap_at(v - 1, levels)))) {
+      --v;
+    } else if (v < static_cast<int>(values) &&
+               kx >= order_key(__ldg(table + split_heap_at(v, levels)))) {
+      ++v;
+    } else {
+      r = static_cast<u32>(v);
+      return true;
+    }
+  }
+  return false;
+}
+
+// A forest's first key word: k_keys with each body's own system's root and
+// table of T levels (levels below T stepped as the reference does).
+__global__ void __launch_bounds__(kT)
+    k_keys_forest(const double *pos, u32 n, const u16 *sys, const TreeRoot *roots,
+                  const double *split, u32 size, int T, const u32 *unsorted, u64 *key, u32 *idx,
+                  u8 *tiny, u32 *error) {
   const u32 i = blockIdx.x * kT + threadIdx.x;
   if (i >= n) return;
-  const TreeRoot *root = roots + sys[i];
+  const u32 s = sys[i];
+  const TreeRoot *root = roots + s;
+  const double *half_at = root->half_at;
   const double x = pos[3ull * i], y = pos[3ull * i + 1], z = pos[3ull * i + 2];
   if (!isfinite(x) || !isfinite(y) || !isfinite(z)) atomicOr(error, 4u);
   const u64 kx = order_key(x), ky = order_key(y), kz = order_key(z);
@@ -491,20 +586,54 @@ __global__ void __launch_bounds__(kT)
     const long long maybe_tiny =
         __double_as_longlong(2e-12 * (fabs(x) + fabs(y) + fabs(z) + 1e-300));
     dt = 0;
-    while (dt <= kLevelsPerWord && __double_as_longlong(root->half_at[dt]) >= maybe_tiny) ++dt;
+    while (dt <= kLevelsPerWord && __double_as_longlong(half_at[dt]) >= maybe_tiny) ++dt;
   }
-  double cx = root->center[0], cy = root->center[1], cz = root->center[2];
+  const double *tx = split + 3ull * s * size, *ty = tx + size, *tz = ty + size;
+  u32 ix = 1, iy = 1, iz = 1;
+  double cx = 0.0, cy = 0.0, cz = 0.0;
   u64 k = 0;
   int t = kNoTiny;
-  for (int d = 0; d < kLevelsPerWord; ++d) {
-    if (d >= dt && t == kNoTiny && tiny_node(root->half_at[d], cx, cy, cz)) t = d;
+  auto level = [&](int d, bool test) {
+    if (d < T) {
+      cx = __ldg(tx + ix);
+      cy = __ldg(ty + iy);
+      cz = __ldg(tz + iz);
+    }
+    if (test && t == kNoTiny && tiny_node(half_at[d], cx, cy, cz)) t = d;
     int o = (kx >= order_key(cx) ? 1 : 0) | (ky >= order_key(cy) ? 2 : 0) |
             (kz >= order_key(cz) ? 4 : 0);
     if (t != kNoTiny) o = 0;
     k = (k << 3) | static_cast<u64>(o);
-    step_centre(cx, cy, cz, o, root->half_at[d + 1]);
+    if (d + 1 < T) {
+      ix = 2 * ix + (o & 1);
+      iy = 2 * iy + ((o >> 1) & 1);
+      iz = 2 * iz + (o >> 2);
+    } else {
+      step_centre(cx, cy, cz, o, half_at[d + 1]);
+    }
+  };
+  int d = 0;
+  if (unsorted[s] == 0 && dt >= T) {
+    // no tiny test within the table's levels: its levels by rank, then the
+    // centre of level T (the path's deepest table centre, stepped once)
+    const float inv_w = 1.0f / static_cast<float>(half_at[T - 1]);
+    u32 rx, ry, rz;
+    if (split_rank_at(tx, kx, x, root->center[0] - half_at[0], inv_w, T, rx) &&
+        split_rank_at(ty, ky, y, root->center[1] - half_at[0], inv_w, T, ry) &&
+        split_rank_at(tz, kz, z, root->center[2] - half_at[0], inv_w, T, rz)) {
+      k = spread3(rx) | (spread3(ry) << 1) | (spread3(rz) << 2);
+      const u32 leaves = 1u << (T - 1);
+      cx = __ldg(tx + leaves + (rx >> 1));
+      cy = __ldg(ty + leaves + (ry >> 1));
+      cz = __ldg(tz + leaves + (rz >> 1));
+      const int o = static_cast<int>((rx & 1u) | ((ry & 1u) << 1) | ((rz & 1u) << 2));
+      step_centre(cx, cy, cz, o, half_at[T]);
+      d = T;
+    }
   }
-  if (dt <= kLevelsPerWord && t == kNoTiny && tiny_node(root->half_at[kLevelsPerWord], cx, cy, cz))
+  for (; d < kLevelsPerWord && d < dt; ++d) level(d, false);
+  for (; d < kLevelsPerWord; ++d) level(d, true);
+  if (dt <= kLevelsPerWord && t == kNoTiny && tiny_node(half_at[kLevelsPerWord], cx, cy, cz))
     t = kLevelsPerWord;
   key[i] = k;
   idx[i] = i;
@@ -674,7 +803,8 @@ __global__ void __launch_bounds__(kT)
     k_nodes(KeyView kv, const signed char *lcp_next, const u8 *leafdepth, const u32 *count,
             const u32 *count_scan, u32 n, const Scalars *sc, const TreeRoot *root,
             const double *split, double2 *geom, u32 *nbegin, u32 *nend, u32 *skip, u8 *depth,
-            u8 *isleaf, const u32 *abort = nullptr) {
+            u8 *isleaf, const u32 *abort = nullptr, u32 table_size = kSplitSize,
+            int table_levels = kSplitLevels) {
   const u32 b = blockIdx.x * kT + threadIdx.x;
   if (b >= n || aborted(abort)) return;
   const u32 c = count[b];
@@ -682,20 +812,15 @@ __global__ void __launch_bounds__(kT)
   const u32 total = sc->n_nodes;
   const u32 first = total - count_scan[b] - c;  // nodes ending after b come first
   const int d0 = lcp_next[b] + 1, ld = leafdepth[b];
-  // centres from the split table down to its last level, stepped below it;
-  // a forest (no table: `root` holds every system's root) steps them all
-  // from the system's root centre
-  const bool table = kv.sys == nullptr;
-  if (!table) root += kv.sys[b];
-  const int table_levels = table ? kSplitLevels : 0;
-  const double *tx = split, *ty = split + kSplitSize, *tz = split + 2ull * kSplitSize;
+  // centres from the split table down to its last level, stepped below it
+  // (a forest: `root` and `split` hold every system's root and table)
+  const bool forest = kv.sys != nullptr;
+  const u32 sys = forest ? kv.sys[b] : 0u;
+  root += sys;
+  const double *tx = split + 3ull * sys * table_size, *ty = tx + table_size,
+               *tz = ty + table_size;
   u32 ix = 1, iy = 1, iz = 1;
   double cx = 0.0, cy = 0.0, cz = 0.0;
-  if (!table) {
-    cx = root->center[0];
-    cy = root->center[1];
-    cz = root->center[2];
-  }
   for (int d = 0; d <= ld; ++d) {
     if (d > 0) {
       const int o = digit(kv, b, d);
@@ -732,7 +857,7 @@ __global__ void __launch_bounds__(kT)
   u32 start = b;  // shares at least d levels with b for every d here
   for (int d = ld; d >= d0; --d) {
     u32 lo = 0, hi = start;
-    if (d > 0 || !table) {  // (a forest's root starts at its system's first body)
+    if (d > 0 || forest) {  // (a forest's root starts at its system's first body)
       for (u64 step = 1;; step *= 2) {  // 64-bit: never wraps to 0
         if (step > hi) break;  // lo stays 0
         const u32 cand = hi - static_cast<u32>(step);
@@ -1405,7 +1530,7 @@ int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s,
   return low == 0 ? kLevelsPerWord : (3 * kLevelsPerWord - low) / 3;
 }
 
-// A forest's root cubes (one per system) and first key words.
+// A forest's root cubes (one per system), split tables and first key words.
 void forest_keys(Workspace &ws, const double *pos, u32 n, cudaStream_t s) {
   const ForestView &fv = ws.forest;
   ws.bbox_part.ensure(6 * sizeof(double) * fv.bbox_nblocks);
@@ -1414,7 +1539,28 @@ void forest_keys(Workspace &ws, const double *pos, u32 n, cudaStream_t s) {
   GTC_LAUNCH_CHECK();
   k_root_forest<<<fv.systems, kT, 0, s>>>(ws.bbox_part.as<double>(), fv.sys_blocks, fv.roots);
   GTC_LAUNCH_CHECK();
-  k_keys_forest<<<ceil_div(n, kT), kT, 0, s>>>(pos, n, fv.sys, fv.roots, ws.key0.as<u64>(),
+  const int T = fv.split_levels;
+  const u32 size = 1u << T, tables = 3 * fv.systems;
+  ws.split.ensure(static_cast<u64>(tables) * size * sizeof(double));
+  double *split = ws.split.as<double>();
+  const int top = std::min(T, kSplitTop);
+  k_split_top_forest<<<tables, 1024, 0, s>>>(fv.roots, split, size, top);
+  GTC_LAUNCH_CHECK();
+  for (int lv = top; lv < T;) {  // levels lv.. below the nodes of level lv - 1
+    const int L = T - lv >= 4 ? 4 : (T - lv >= 2 ? 2 : 1);
+    const u32 blocks = ceil_div(static_cast<u64>(tables) << (lv - 1), kT);
+    if (L == 4) k_split_sub_forest<4><<<blocks, kT, 0, s>>>(fv.roots, split, size, tables, lv - 1);
+    else if (L == 2) k_split_sub_forest<2><<<blocks, kT, 0, s>>>(fv.roots, split, size, tables, lv - 1);
+    else k_split_sub_forest<1><<<blocks, kT, 0, s>>>(fv.roots, split, size, tables, lv - 1);
+    GTC_LAUNCH_CHECK();
+    lv += L;
+  }
+  GTC_CUDA(cudaMemsetAsync(fv.split_unsorted, 0, fv.systems * sizeof(u32), s));
+  k_split_check_forest<<<ceil_div(static_cast<u64>(tables) << (T - 1), kT), kT, 0, s>>>(
+      split, size, T, tables, fv.split_unsorted);
+  GTC_LAUNCH_CHECK();
+  k_keys_forest<<<ceil_div(n, kT), kT, 0, s>>>(pos, n, fv.sys, fv.roots, split, size, T,
+                                               fv.split_unsorted, ws.key0.as<u64>(),
                                                ws.idx.as<u32>(), ws.tiny.as<u8>(),
                                                &ws.scalars.as<Scalars>()->error);
   GTC_LAUNCH_CHECK();
@@ -1596,7 +1742,9 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
 
   k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
                             ws.split.as<double>(), ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>());
+                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), nullptr,
+                            fv ? 1u << fv.split_levels : kSplitSize,
+                            fv ? fv.split_levels : kSplitLevels);
   GTC_LAUNCH_CHECK();
   ws.kids.ensure(static_cast<u64>(m) * 8 * sizeof(u32));
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, ws.parent.as<u32>(),
@@ -1703,7 +1851,9 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
   const u32 *m_dev = &sc->n_nodes;
   k_nodes<<<nb, kT, 0, s>>>(kv, lcp_next, leafdepth, count, cscan, n32, sc, root,
                             ws.split.as<double>(), ws.geom.as<double2>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), abort);
+                            ws.skip.as<u32>(), ws.depth.as<u8>(), ws.isleaf.as<u8>(), abort,
+                            fv ? 1u << fv.split_levels : kSplitSize,
+                            fv ? fv.split_levels : kSplitLevels);
   GTC_LAUNCH_CHECK();
   k_children<<<mb, kT, 0, s>>>(ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, ws.parent.as<u32>(),
                                ws.nchild.as<u8>(), ws.kids.as<uint4>(), m_dev, abort);
