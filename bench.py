@@ -544,7 +544,9 @@ def main():
     if args.only_steps:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": round(value, 4), "unit": "ms",
-                              "n": n, "steps": args.steps, "only_steps": True}), flush=True)
+                              "n": n, "steps": args.steps, "only_steps": True,
+                              "eval_kernel_ms": round(statistics.mean(
+                                  s["eval_kernel_ms"] for s in stats), 4)}), flush=True)
         ctx.close()
         return
     st = stats[-1]

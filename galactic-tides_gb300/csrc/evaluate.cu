@@ -226,6 +226,13 @@ constexpr int kPairCellF4 = 5;   // float4 per staged cell pair
 constexpr int kPairBodyF4 = 2;   // float4 per staged body pair
 constexpr u32 kMaxSlices = 16;   // slices per group at most
 constexpr u32 kPassCost = 24;    // a pass's fixed cost, in staged entries per lane
+// Staged pairs a lane works per inner-loop iteration: the pairs' arithmetic
+// is independent up to the accumulation, which stays in list order, so
+// results do not depend on it; more pairs per iteration give each warp more
+// independent work to hide the rsqrt and shared-load latencies. A round's
+// 2W staged entries (2W a multiple of 4) are padded with far dummies, so an
+// iteration never reads past them.
+constexpr int kEvalPairsPerIter = 2;
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
@@ -243,6 +250,7 @@ __device__ __forceinline__ u32 choose_slices(u32 T, u32 ec, u32 eb, int lane) {
   return (__reduce_min_sync(kFullMask, key) & 15u) + 1u;
 }
 
+template <int kU>
 __global__ void __launch_bounds__(kT)
     k_eval_pairs(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
                  const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
@@ -329,9 +337,11 @@ __global__ void __launch_bounds__(kT)
           const u32 base = m0 + 2 * r * W;
           const u32 cnt = computes && base < m1 ? min(2 * W, m1 - base) : 0u;
           const float4 *mine = &sc[warp][area * cstride];
-          for (u32 j = 0; j < cnt; j += 2) {
-            const float4 s0 = mine[0], s1 = mine[1], s2 = mine[2], s3 = mine[3], s4 = mine[4];
-            mine += kPairCellF4;
+          for (u32 j = 0; j < cnt; j += 2 * kU) {
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+            const float4 s0 = mine[5 * u], s1 = mine[5 * u + 1], s2 = mine[5 * u + 2],
+                         s3 = mine[5 * u + 3], s4 = mine[5 * u + 4];
             // s0 = -cx, -cy  s1 = -cz, -Gm  s2 = Qxx, Qyy  s3 = Qzz, Qxy  s4 = Qxz, Qyz (pairs)
             const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
                          dz = __fadd2_rn(pz, f2(s1.x, s1.y));
@@ -352,6 +362,8 @@ __global__ void __launch_bounds__(kT)
             ay = __ffma2_rn(along, dy, __ffma2_rn(qy, inv5, ay));
             az = __ffma2_rn(along, dz, __ffma2_rn(qz, inv5, az));
             pot = __ffma2_rn(mhalf, rqr5, __ffma2_rn(ngm, inv, pot));
+            }
+            mine += kPairCellF4 * kU;
           }
           __syncwarp();
         }
@@ -388,9 +400,10 @@ __global__ void __launch_bounds__(kT)
           const u32 base = m0 + 2 * r * W;
           const u32 cnt = computes && base < m1 ? min(2 * W, m1 - base) : 0u;
           const float4 *mine = &sb[warp][area * bstride];
-          for (u32 j = 0; j < cnt; j += 2) {
-            const float4 s0 = mine[0], s1 = mine[1];
-            mine += kPairBodyF4;
+          for (u32 j = 0; j < cnt; j += 2 * kU) {
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+            const float4 s0 = mine[2 * u], s1 = mine[2 * u + 1];
             const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
                          dz = __fadd2_rn(pz, f2(s1.x, s1.y));
             const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
@@ -401,6 +414,8 @@ __global__ void __launch_bounds__(kT)
             ay = __ffma2_rn(gm3, dy, ay);
             az = __ffma2_rn(gm3, dz, az);
             pot = __fadd2_rn(pot, gm);
+            }
+            mine += kPairBodyF4 * kU;
           }
           __syncwarp();
         }
@@ -451,9 +466,10 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
   GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<kQuad, kSoft>, kT, 0));
   const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
   if (kQuad && kSoft) {
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_pairs, kT, 0));
+    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, k_eval_pairs<kEvalPairsPerIter>, kT, 0));
     const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
-    k_eval_pairs<<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
+    k_eval_pairs<kEvalPairsPerIter><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
                                      static_cast<u32>(n_groups), G, eps2, out, counter,
                                      sc ? &sc->n_groups : nullptr, sc ? &sc->abort : nullptr);
   } else {
