@@ -261,7 +261,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
 // twice the headroom: the longest of many lists moves more than the totals
 // do); offsets stay below 2^32 (a replay that needs more aborts).
 void reserve_graph(gtc::Workspace &ws, const gtc::Scalars &hs, double headroom, u64 n,
-                   gtc::GraphCaps &caps) {
+                   gtc::GraphCaps &caps, bool sized_lists = false) {
   const double f = 1.0 + headroom;
   const u64 pad = headroom > 0 ? 1024 : 0;
   caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
@@ -315,10 +315,13 @@ void reserve_graph(gtc::Workspace &ws, const gtc::Scalars &hs, double headroom, 
   ws.gcell_off.ensure((n + 1) * 8);
   ws.gbody_off.ensure((n + 1) * 8);
   ws.groups.ensure(n * gtc::kGroupRecWords * 4);
-  ws.cell_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_cells + caps.slot_near_cells) +
-                       caps.pool_cells) * 4);
-  ws.body_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_bodies + caps.slot_near_bodies) +
-                       caps.pool_bodies) * 4);
+  caps.sys_slots = nullptr;
+  if (!ws.forest || !sized_lists) {  // (a forest sizes them per system, when it can)
+    ws.cell_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_cells + caps.slot_near_cells) +
+                         caps.pool_cells) * 4);
+    ws.body_list.ensure((static_cast<u64>(caps.groups) * (caps.slot_bodies + caps.slot_near_bodies) +
+                         caps.pool_bodies) * 4);
+  }
   ws.spill.ensure(2 * n * sizeof(u32));
   ws.splitpt.ensure(2 * n * sizeof(u32));
   ws.out.ensure(n * sizeof(float4));
@@ -696,7 +699,18 @@ struct ForestGraph {
   }
 
   void capture(double dt, cudaStream_t s) {
-    reserve_graph(f->ws, *f->host_sc, headroom, f->n, caps);
+    // the list slots per system when they fit 32-bit offsets, else one size
+    // for every group
+    gtc::GraphCaps probe{};
+    const bool per_system = f->size_graph_slots(probe, headroom, s);
+    reserve_graph(f->ws, *f->host_sc, headroom, f->n, caps, per_system);
+    if (per_system) {
+      caps.sys_slots = probe.sys_slots;
+      caps.pool_at_cells = probe.pool_at_cells;
+      caps.pool_at_bodies = probe.pool_at_bodies;
+      caps.pool_cells = probe.pool_cells;
+      caps.pool_bodies = probe.pool_bodies;
+    }
     GTC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
       record(dt, s);

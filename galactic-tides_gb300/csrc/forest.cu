@@ -112,9 +112,10 @@ __global__ void __launch_bounds__(kT)
 ForestRun::~ForestRun() {
   ws.release_all();
   DeviceBuffer *own[] = {&tables, &sysid, &roots, &root_node, &group_root, &apos, &amass, &stats,
-                         &counter, &split_flags};
+                         &counter, &split_flags, &sys_groups, &sys_max, &slot_plan, &graph_slots};
   for (DeviceBuffer *b : own) b->release();
   if (host_sc) cudaFreeHost(host_sc);
+  if (host_lists) cudaFreeHost(host_lists);
 }
 
 bool ForestRun::eligible(const std::vector<ForestSystem> &systems, std::string *why) {
@@ -183,6 +184,17 @@ void ForestRun::setup(const std::vector<ForestSystem> &systems, cudaStream_t s) 
   amass.ensure(std::max<u64>(1, n) * 8);
   stats.ensure(k * sizeof(ForestSystemStats));
   split_flags.ensure(k * sizeof(u32));
+  sys_groups.ensure(k * sizeof(u32));
+  sys_max.ensure(4ull * k * sizeof(u32));
+  slot_plan.ensure(std::max<u64>(1, n) * 2 * sizeof(uint4));
+  graph_slots.ensure(k * sizeof(SysSlots));
+  if (host_systems < k) {
+    if (host_lists) cudaFreeHost(host_lists);
+    host_lists = nullptr;
+    host_systems = 0;
+    GTC_CUDA(cudaMallocHost(reinterpret_cast<void **>(&host_lists), 5ull * k * sizeof(u32)));
+    host_systems = k;
+  }
   int T = kLevelsPerWord;
   while (T > 1 && 3ull * k * (1ull << T) * sizeof(double) > kSplitBudget) --T;
   counter.ensure(sizeof(u32));
@@ -202,6 +214,11 @@ void ForestRun::setup(const std::vector<ForestSystem> &systems, cudaStream_t s) 
   fv.bbox_nblocks = static_cast<u32>(blk.size());
   fv.split_levels = T;
   fv.split_unsorted = split_flags.as<u32>();
+  fv.sys_groups = sys_groups.as<u32>();
+  fv.sys_max = sys_max.as<u32>();
+  fv.host_groups = host_lists;
+  fv.host_max = host_lists + k;
+  fv.slot_plan = slot_plan.as<uint4>();
   ptrs_dev = reinterpret_cast<const ForestSystemPtrs *>(t + off_ptrs);
   if (n == 0) return;
   k_forest_sys<<<ceil_div(n, kT), kT, 0, s>>>(fv.start, k, static_cast<u32>(n), sysid.as<u16>());
@@ -253,6 +270,58 @@ void ForestRun::step(double dt, cudaStream_t s) {
   const double h = 0.5 * dt;
   kick_drift(h, dt, s);
   solve(1, h, s);
+}
+
+bool ForestRun::size_graph_slots(GraphCaps &caps, double headroom, cudaStream_t s) {
+  const ForestView &fv = ws.forest;
+  const u32 k = fv.systems;
+  const double f = 1.0 + headroom, fs = 1.0 + 2.0 * headroom;
+  const bool pad = headroom > 0;
+  auto slot = [&](u32 longest) {
+    const u64 v = (static_cast<u64>(longest * fs) + (pad ? 64 : 0) + 31) & ~31ull;
+    return std::max<u64>(32, v);
+  };
+  std::vector<SysSlots> tab(k);
+  u64 at_c = 0, at_b = 0, most_c = 0, most_b = 0;
+  for (u32 j = 0; j < k; ++j) {
+    const u32 *mx = fv.host_max + 4ull * j;
+    const u64 groups = std::min<u64>(sys[j].n, static_cast<u64>(fv.host_groups[j] * f) +
+                                                   (pad ? 16 : 0));
+    const u64 rc = slot(mx[0]), rb = slot(mx[1]), nc = slot(mx[2]), nb = slot(mx[3]);
+    if (rc + nc > 0xffffffffull || rb + nb > 0xffffffffull) return false;
+    SysSlots &S = tab[j];
+    S = SysSlots{};
+    S.groups = static_cast<u32>(std::max<u64>(groups, 1));
+    S.rc = static_cast<u32>(rc);
+    S.rb = static_cast<u32>(rb);
+    S.nc = static_cast<u32>(nc);
+    S.nb = static_cast<u32>(nb);
+    // rest slots of every group, then near slots, per system
+    const u64 rc_at = at_c, nc_at = at_c + S.groups * rc;
+    const u64 rb_at = at_b, nb_at = at_b + S.groups * rb;
+    at_c = nc_at + S.groups * nc;
+    at_b = nb_at + S.groups * nb;
+    if (at_c > 0xffffffffull || at_b > 0xffffffffull) return false;
+    S.rc_at = static_cast<u32>(rc_at);
+    S.nc_at = static_cast<u32>(nc_at);
+    S.rb_at = static_cast<u32>(rb_at);
+    S.nb_at = static_cast<u32>(nb_at);
+    most_c = std::max(most_c, rc + nc);
+    most_b = std::max(most_b, rb + nb);
+  }
+  const u64 pool_c = at_c / 16 + 4 * most_c, pool_b = at_b / 16 + 4 * most_b;
+  if (at_c + pool_c > 0xffffffffull || at_b + pool_b > 0xffffffffull) return false;
+  GTC_CUDA(cudaMemcpyAsync(graph_slots.ptr, tab.data(), k * sizeof(SysSlots),
+                           cudaMemcpyHostToDevice, s));
+  GTC_CUDA(cudaStreamSynchronize(s));
+  ws.cell_list.ensure((at_c + pool_c) * 4);
+  ws.body_list.ensure((at_b + pool_b) * 4);
+  caps.sys_slots = graph_slots.as<SysSlots>();
+  caps.pool_at_cells = at_c;
+  caps.pool_at_bodies = at_b;
+  caps.pool_cells = pool_c;
+  caps.pool_bodies = pool_b;
+  return true;
 }
 
 std::vector<ForestSystemStats> ForestRun::system_stats(cudaStream_t s) {

@@ -32,7 +32,9 @@ struct ForestRun {
   SolverParams sp{};            // the shared parameters (group size and packing per system)
   u64 n = 0;                    // bodies in all
   DeviceBuffer tables, sysid, roots, root_node, group_root, apos, amass, stats, counter,
-      split_flags;
+      split_flags, sys_groups, sys_max, slot_plan, graph_slots;
+  u32 *host_lists = nullptr;    // pinned: per-system group counts, then list maxima
+  u32 host_systems = 0;         // systems host_lists holds
   // Memory for the systems' split tables: each gets levels 0..T-1 (3 x 2^T
   // doubles), T the most levels (up to the 21 of one key word) within it.
   static constexpr u64 kSplitBudget = 256ull << 20;
@@ -60,6 +62,12 @@ struct ForestRun {
   void scatter(int kick, double h, const u32 *abort, cudaStream_t s);
   // Per-system interaction counts of the current lists.
   std::vector<ForestSystemStats> system_stats(cudaStream_t s);
+  // Per-system list slots for a captured step (caps: the uniform capacities
+  // from the last eager solve; headroom as there), sized from each system's
+  // group count and longest lists of that solve; sets caps.sys_slots and the
+  // pools and sizes the list arrays. False (caps unchanged) when even
+  // these do not fit 32-bit list offsets.
+  bool size_graph_slots(GraphCaps &caps, double headroom, cudaStream_t s);
 };
 
 }  // namespace gtc

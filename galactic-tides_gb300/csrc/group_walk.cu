@@ -398,7 +398,91 @@ struct SplitOut {
   u64 near_cells_at, near_bodies_at;  // the near parts' slots start here (the rest's at 0)
   u32 slot_cells, slot_bodies, slot_near_cells, slot_near_bodies;
   u32 cap;                 // groups the count arrays hold per part
+  // a forest: per-group slots (starts, then sizes; null: the uniform slots
+  // above), and the per-system maxima the records keep (with the body
+  // systems they are indexed by)
+  const uint4 *plan = nullptr;
+  const u16 *sys = nullptr;
+  u32 *sys_max = nullptr;
 };
+
+// Group g's slots: starts (rest cells, rest bodies, near cells, near
+// bodies) and sizes, from the plan or the uniform layout.
+struct GroupSlots {
+  u64 rc_at, rb_at, nc_at, nb_at;
+  u32 rc, rb, nc, nb;
+};
+__device__ __forceinline__ GroupSlots group_slots(const SplitOut &o, u32 g) {
+  if (o.plan) {
+    const uint4 st = o.plan[2ull * g], cp = o.plan[2ull * g + 1];
+    return GroupSlots{st.x, st.y, st.z, st.w, cp.x, cp.y, cp.z, cp.w};
+  }
+  return GroupSlots{static_cast<u64>(g) * o.slot_cells, static_cast<u64>(g) * o.slot_bodies,
+                    o.near_cells_at + static_cast<u64>(g) * o.slot_near_cells,
+                    o.near_bodies_at + static_cast<u64>(g) * o.slot_near_bodies, o.slot_cells,
+                    o.slot_bodies, o.slot_near_cells, o.slot_near_bodies};
+}
+
+// A forest's group count of each system: its groups are contiguous, and
+// the group choice's scan at its first body is its first group.
+__global__ void __launch_bounds__(kT)
+    k_sys_groups(const u32 *mscan, const u32 *start, u32 systems, const Scalars *sc,
+                 u32 *groups) {
+  const u32 k = blockIdx.x * kT + threadIdx.x;
+  if (k >= systems) return;
+  const u32 next = k + 1 < systems ? mscan[start[k + 1]] : sc->n_groups;
+  groups[k] = next - mscan[start[k]];
+}
+
+// Each group's slots from its system's table; a group past the system's
+// capacity gets none (its lists go to the overflow pools).
+__global__ void __launch_bounds__(kT)
+    k_slot_plan(const u32 *gbegin, u32 ng_cap, const u32 *ng_dev, const u32 *abort,
+                const u16 *sys, const u32 *start, const u32 *mscan, const SysSlots *slots,
+                uint4 *plan) {
+  const u32 g = blockIdx.x * kT + threadIdx.x;
+  if (aborted(abort) || g >= bounded(ng_cap, ng_dev)) return;
+  const u16 k = sys[gbegin[g]];
+  const SysSlots S = slots[k];
+  const u32 j = g - mscan[start[k]];
+  if (j < S.groups) {
+    plan[2ull * g] = make_uint4(S.rc_at + j * S.rc, S.rb_at + j * S.rb, S.nc_at + j * S.nc,
+                                S.nb_at + j * S.nb);
+    plan[2ull * g + 1] = make_uint4(S.rc, S.rb, S.nc, S.nb);
+  } else {
+    plan[2ull * g] = make_uint4(0u, 0u, 0u, 0u);
+    plan[2ull * g + 1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+// A forest's per-system maxima of four list lengths (every lane of the
+// warp calls it): one atomic per value when the warp's valid lanes share a
+// system, the usual case (a system's groups are contiguous), else one per
+// lane.
+__device__ __forceinline__ void sys_max_warp(u32 *sys_max, const u16 *sys, bool valid, u32 b0,
+                                             u32 a, u32 b, u32 c, u32 d) {
+  const u32 key = valid ? sys[b0] : 0xffffffffu;
+  const unsigned vm = __ballot_sync(kFullMask, valid);
+  if (vm == 0) return;
+  const u32 key0 = __shfl_sync(kFullMask, key, __ffs(vm) - 1);
+  if (__all_sync(kFullMask, !valid || key == key0)) {
+    const u32 ma = __reduce_max_sync(kFullMask, valid ? a : 0u),
+              mb = __reduce_max_sync(kFullMask, valid ? b : 0u),
+              mc = __reduce_max_sync(kFullMask, valid ? c : 0u),
+              md = __reduce_max_sync(kFullMask, valid ? d : 0u);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&sys_max[4ull * key0], ma);
+      atomicMax(&sys_max[4ull * key0 + 1], mb);
+      atomicMax(&sys_max[4ull * key0 + 2], mc);
+      atomicMax(&sys_max[4ull * key0 + 3], md);
+    }
+  } else if (valid) {
+    atomicMax(&sys_max[4ull * key], a);
+    atomicMax(&sys_max[4ull * key + 1], b);
+    atomicMax(&sys_max[4ull * key + 2], c);
+    atomicMax(&sys_max[4ull * key + 3], d);
+  }
+}
 
 // The child of `root` that holds targets [b0, b1), or kNone.
 __device__ __forceinline__ u32 near_child(u32 root, u32 b0, u32 b1, const uint4 *kids,
@@ -434,10 +518,11 @@ __global__ void __launch_bounds__(kWalkThreads)
   // (a leaf root has no children: nchild 0)
   const u32 near = near_child(root, gbegin[g], gend[g], kids, nchild, nbegin, nend);
   const u32 near_end = near == kNone ? 0u : load32(walk32, near).skip;
-  const u32 cap_c = part ? out.slot_near_cells : out.slot_cells;
-  const u32 cap_b = part ? out.slot_near_bodies : out.slot_bodies;
-  u32 *cl = out.cell_list + (part ? out.near_cells_at : 0ull) + static_cast<u64>(g) * cap_c;
-  u32 *bl = out.body_list + (part ? out.near_bodies_at : 0ull) + static_cast<u64>(g) * cap_b;
+  const GroupSlots gsl = group_slots(out, g);
+  const u32 cap_c = part ? gsl.nc : gsl.rc;
+  const u32 cap_b = part ? gsl.nb : gsl.rb;
+  u32 *cl = out.cell_list + (part ? gsl.nc_at : gsl.rc_at);
+  u32 *bl = out.body_list + (part ? gsl.nb_at : gsl.rb_at);
   u32 nc = 0, nb = 0, exact = 0, visits = 0, split_c = 0, split_b = 0;
   bool jumped = false;
   u32 i = 0, end = 0;
@@ -522,6 +607,7 @@ struct WarpWalkOut {
   const u32 *spill_cells, *spill_bodies;  // kSpill
   u32 *split;                     // kSlots: the split walk's split points (all lists: part 0)
   u32 slot_cells, slot_bodies, cap;
+  const uint4 *plan = nullptr;    // kSlots, a forest: per-group slots (starts, sizes)
 };
 
 __device__ __forceinline__ u32 warp_excl_scan(u32 v, int lane, u32 &total) {
@@ -558,10 +644,18 @@ __global__ void __launch_bounds__(kWarpWalkThreads)
       cl = out.cell_list + out.cell_off[g];
       bl = out.body_list + out.body_off[g];
     } else if (kMode == kSlots) {
-      cap_c = out.slot_cells;
-      cap_b = out.slot_bodies;
-      cl = out.cell_list + static_cast<u64>(g) * cap_c;
-      bl = out.body_list + static_cast<u64>(g) * cap_b;
+      if (out.plan) {
+        const uint4 st = out.plan[2ull * g], cp = out.plan[2ull * g + 1];
+        cap_c = cp.x;
+        cap_b = cp.y;
+        cl = out.cell_list + st.x;
+        bl = out.body_list + st.y;
+      } else {
+        cap_c = out.slot_cells;
+        cap_b = out.slot_bodies;
+        cl = out.cell_list + static_cast<u64>(g) * cap_c;
+        bl = out.body_list + static_cast<u64>(g) * cap_b;
+      }
     } else if (kMode == kSpill) {
       if (out.spill_cells[g] == kNoSpill) continue;
       cl = out.cell_list + out.spill_cells[g];
@@ -693,8 +787,8 @@ __global__ void __launch_bounds__(kT)
   const u64 rc = out.ncells[g], rb = out.nbodies[g];
   const u64 nc = out.ncells[static_cast<u64>(out.cap) + g], nb = out.nbodies[static_cast<u64>(out.cap) + g];
   u32 oc = kNoSpill, ob = kNoSpill;
-  if (rc > out.slot_cells || rb > out.slot_bodies || nc > out.slot_near_cells ||
-      nb > out.slot_near_bodies) {
+  const GroupSlots gsl = group_slots(out, g);
+  if (rc > gsl.rc || rb > gsl.rb || nc > gsl.nc || nb > gsl.nb) {
     const u64 tc = rc + nc, tb = rb + nb;
     const u64 c = atomicAdd(&sc->spill_used[0], static_cast<unsigned long long>(tc));
     const u64 b = atomicAdd(&sc->spill_used[1], static_cast<unsigned long long>(tb));
@@ -735,9 +829,8 @@ __global__ void __launch_bounds__(kT)
       bs = one_segment(spill_bodies[g], rb + nb);
     } else {
       const u32 sc_ = out.split[2ull * g], sb_ = out.split[2ull * g + 1];
-      const u64 r0 = static_cast<u64>(g) * out.slot_cells, q0 = static_cast<u64>(g) * out.slot_bodies;
-      const u64 n0 = out.near_cells_at + static_cast<u64>(g) * out.slot_near_cells;
-      const u64 m0 = out.near_bodies_at + static_cast<u64>(g) * out.slot_near_bodies;
+      const GroupSlots gsl = group_slots(out, g);
+      const u64 r0 = gsl.rc_at, q0 = gsl.rb_at, n0 = gsl.nc_at, m0 = gsl.nb_at;
       cs.start[0] = static_cast<u32>(r0);
       cs.count[0] = sc_;
       cs.start[1] = static_cast<u32>(n0);
@@ -763,6 +856,9 @@ __global__ void __launch_bounds__(kT)
     atomicMax(&sc->max_near_cells, m_nc);
     atomicMax(&sc->max_near_bodies, m_nb);
   }
+  if (out.sys_max)
+    sys_max_warp(out.sys_max, out.sys, valid, valid ? gbegin[g] : 0u, clamp(rc), clamp(rb),
+                 clamp(nc), clamp(nb));
 }
 
 // Walk tasks: nodes at depth `split` (0..2), and leaves above it, in node
@@ -791,8 +887,8 @@ __global__ void __launch_bounds__(kT)
 // GTGroup records from the per-task offsets, and the list counters.
 __global__ void __launch_bounds__(kT)
     k_group_records(const u32 *gbegin, const u32 *gend, u32 ng, u32 ntasks, const u64 *cell_off,
-                    const u64 *body_off, uint4 *groups, Scalars *sc,
-                    const u32 *ng_dev = nullptr) {
+                    const u64 *body_off, uint4 *groups, Scalars *sc, const u32 *ng_dev = nullptr,
+                    const u16 *sys = nullptr, u32 *sys_max = nullptr) {
   const u32 g = blockIdx.x * kT + threadIdx.x;
   if (sc->abort) return;
   const bool valid = g < bounded(ng, ng_dev);
@@ -809,6 +905,11 @@ __global__ void __launch_bounds__(kT)
     nb = b1 - b0;
   }
   group_stats_warp(sc, valid, t, nc, nb, false);
+  if (sys_max) {  // whole lists: they size both parts' slots
+    const u32 c = static_cast<u32>(nc < 0xffffffffull ? nc : 0xffffffffull);
+    const u32 b = static_cast<u32>(nb < 0xffffffffull ? nb : 0xffffffffull);
+    sys_max_warp(sys_max, sys, valid, valid ? gbegin[g] : 0u, c, b, c, b);
+  }
 }
 
 
@@ -920,6 +1021,13 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_LAUNCH_CHECK();
   k_last_end<<<1, 1, 0, s>>>(sc, n32, gend);
   GTC_LAUNCH_CHECK();
+  if (fv) {  // each system's group count, read back with the total
+    k_sys_groups<<<ceil_div(fv.systems, kT), kT, 0, s>>>(mscan, fv.start, fv.systems, sc,
+                                                         fv.sys_groups);
+    GTC_LAUNCH_CHECK();
+    GTC_CUDA(cudaMemcpyAsync(fv.host_groups, fv.sys_groups, fv.systems * sizeof(u32),
+                             cudaMemcpyDeviceToHost, s));
+  }
   GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, 3 * sizeof(unsigned long long), s));
@@ -955,6 +1063,16 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.gbodies.ensure(slots * 8);
   GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
   const u32 tb = ceil_div(slots, kT);
+  // a forest's per-system maxima of the lists, read back after the walk
+  auto clear_sys_max = [&] {
+    if (fv) GTC_CUDA(cudaMemsetAsync(fv.sys_max, 0, 4ull * fv.systems * sizeof(u32), s));
+  };
+  auto read_sys_max = [&] {
+    if (fv)
+      GTC_CUDA(cudaMemcpyAsync(fv.host_max, fv.sys_max, 4ull * fv.systems * sizeof(u32),
+                               cudaMemcpyDeviceToHost, s));
+  };
+  clear_sys_max();
 
   // One pass into per-group slots when the last walk sized them and they
   // fit 32-bit offsets and sixteen times the lists' own size or 2^28
@@ -985,9 +1103,11 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     GTC_CUDA(cudaMemsetAsync(sc->spill_used, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->spilled, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
-    const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
-                      ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
-                      sl_c, sl_b, sn_c, sn_b, ng};
+    SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
+                ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
+                sl_c, sl_b, sn_c, sn_b, ng};
+    so.sys = fv.sys;
+    so.sys_max = fv.sys_max;
     const WarpWalkOut wwo{so.ncells, so.nbodies, nullptr, nullptr, ws.cell_list.as<u32>(),
                           ws.body_list.as<u32>(), spill_c, spill_b, so.split, sl_c, sl_b, ng};
     if (ws.walk_warps) {
@@ -1014,6 +1134,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
                                       ws.groups.as<uint4>(), sc);
     GTC_LAUNCH_CHECK();
     ws.stage(Workspace::kStWalk1, s);
+    read_sys_max();
     read_scalars(ws, host, s);
     size_slots(ws, *host, true);
     if (!host->list_overflow) {
@@ -1030,6 +1151,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->fp64_tests, 0, sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
+    clear_sys_max();
   }
 
   // count pass, offsets, fill pass
@@ -1053,8 +1175,9 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   GTC_CUDA(cudaMemcpyAsync(&sc->n_cell_list, cell_off + slots, 8, cudaMemcpyDeviceToDevice, s));
   GTC_CUDA(cudaMemcpyAsync(&sc->n_body_list, body_off + slots, 8, cudaMemcpyDeviceToDevice, s));
   k_group_records<<<gb, kT, 0, s>>>(gbegin, gend, ng, ntasks, cell_off, body_off,
-                                    ws.groups.as<uint4>(), sc);
+                                    ws.groups.as<uint4>(), sc, nullptr, fv.sys, fv.sys_max);
   GTC_LAUNCH_CHECK();
+  read_sys_max();
   read_scalars(ws, host, s);
   if (host->n_cell_list > 0xffffffffull || host->n_body_list > 0xffffffffull)
     throw RuntimeError("interaction lists too long for 32 bit offsets");
@@ -1109,8 +1232,10 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   GTC_LAUNCH_CHECK();
   // one pass into the captured slots (near field and rest), outgrown groups
   // again into the pools
-  k_check_groups_graph<<<1, 1, 0, s>>>(sc, caps.groups);
-  GTC_LAUNCH_CHECK();
+  if (!caps.sys_slots) {  // (per-system slots: a system past its capacity spills)
+    k_check_groups_graph<<<1, 1, 0, s>>>(sc, caps.groups);
+    GTC_LAUNCH_CHECK();
+  }
   GTC_CUDA(cudaMemsetAsync(&sc->n_cell_list, 0, 2 * sizeof(u64), s));
   GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
   GTC_CUDA(cudaMemsetAsync(&sc->max_cells, 0, 4 * sizeof(u32), s));
@@ -1121,15 +1246,29 @@ void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &c
   ws.walk_warps = ws.warps_for(caps.groups);  // the replays' walk, chosen at capture
   const u64 near_c = static_cast<u64>(caps.groups) * caps.slot_cells;
   const u64 near_b = static_cast<u64>(caps.groups) * caps.slot_bodies;
-  const u64 pool_at_c = near_c + static_cast<u64>(caps.groups) * caps.slot_near_cells;
-  const u64 pool_at_b = near_b + static_cast<u64>(caps.groups) * caps.slot_near_bodies;
-  const SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
-                    ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
-                    caps.slot_cells, caps.slot_bodies, caps.slot_near_cells,
-                    caps.slot_near_bodies, n32};
-  const WarpWalkOut wwo{so.ncells, so.nbodies, nullptr, nullptr, ws.cell_list.as<u32>(),
-                        ws.body_list.as<u32>(), spill_c, spill_b, so.split, caps.slot_cells,
-                        caps.slot_bodies, n32};
+  u64 pool_at_c = near_c + static_cast<u64>(caps.groups) * caps.slot_near_cells;
+  u64 pool_at_b = near_b + static_cast<u64>(caps.groups) * caps.slot_near_bodies;
+  SplitOut so{ws.gcells.as<u64>(), ws.gbodies.as<u64>(), ws.splitpt.as<u32>(),
+              ws.cell_list.as<u32>(), ws.body_list.as<u32>(), near_c, near_b,
+              caps.slot_cells, caps.slot_bodies, caps.slot_near_cells,
+              caps.slot_near_bodies, n32};
+  WarpWalkOut wwo{so.ncells, so.nbodies, nullptr, nullptr, ws.cell_list.as<u32>(),
+                  ws.body_list.as<u32>(), spill_c, spill_b, so.split, caps.slot_cells,
+                  caps.slot_bodies, n32};
+  if (fv) {
+    so.sys = fv.sys;
+    so.sys_max = fv.sys_max;
+    GTC_CUDA(cudaMemsetAsync(fv.sys_max, 0, 4ull * fv.systems * sizeof(u32), s));
+    if (caps.sys_slots) {  // each system's own slots (and the pools after them)
+      k_slot_plan<<<nb, kT, 0, s>>>(gbegin, n32, &sc->n_groups, abort, fv.sys, fv.start, mscan,
+                                    caps.sys_slots, fv.slot_plan);
+      GTC_LAUNCH_CHECK();
+      so.plan = fv.slot_plan;
+      wwo.plan = fv.slot_plan;
+      pool_at_c = caps.pool_at_cells;
+      pool_at_b = caps.pool_at_bodies;
+    }
+  }
   if (ws.walk_warps) {
     launch_warp_walk<kSlots>(ws, wwo, n32, sc, s, &sc->n_groups, abort);
   } else {

@@ -64,6 +64,19 @@ struct SolverParams {
   double alpha;  // learned criterion's tolerance
 };
 
+// A forest's per-system list slots for the one-pass walk: system k's groups
+// get slots sized from that system's own group count and longest lists (one
+// size for every group would give the small systems' groups the largest
+// system's slots). Group j of the system has its rest slots at rc_at + j rc
+// (cells) and rb_at + j rb (bodies), its near-field slots at nc_at + j nc
+// and nb_at + j nb.
+struct alignas(16) SysSlots {
+  u32 groups;                      // groups of the system the slots cover
+  u32 rc, rb, nc, nb;              // slot sizes
+  u32 rc_at, rb_at, nc_at, nb_at;  // the system's first slots
+  u32 pad[3];
+};
+
 // A forest: the bodies of several independent systems back to back (system
 // k at [start[k], start[k + 1])), each with its own root cube and tree, built
 // and walked by the same launches as one system. Sorted by (system, key),
@@ -80,6 +93,13 @@ struct ForestView {
   const u8 *group_size = nullptr;  // per system: group size
   const u8 *pack = nullptr;        // per system: packing (0 off, 1 a group's worth, k >= 2 threshold)
   u32 *group_root = nullptr;       // per group: its system's root node
+  u32 *sys_groups = nullptr;       // per system: groups of the current choice
+  u32 *sys_max = nullptr;          // per system: longest rest cells, rest bodies, near
+                                   // cells, near bodies of the last walk (whole lists
+                                   // after count + fill)
+  u32 *host_groups = nullptr;      // pinned copies of both, read back by eager builds
+  u32 *host_max = nullptr;
+  uint4 *slot_plan = nullptr;      // per group: slot starts, then sizes (per-system slots)
   int split_levels = 0;            // levels T of each system's split table (2^T per axis)
   u32 *split_unsorted = nullptr;   // per system: its table's in-order values decrease somewhere
   const uint4 *bbox_blocks = nullptr;  // bounding-box blocks: (system, rank, blocks, 0)
@@ -328,6 +348,10 @@ struct GraphCaps {
   u32 slot_cells, slot_bodies;  // each group's list slots (one-pass walk, its rest)
   u32 slot_near_cells, slot_near_bodies;  // ... and its near-field walk
   u64 pool_cells, pool_bodies;  // overflow pools behind the slots
+  // a forest: per-system slots (device table; null: the sizes above for
+  // every group), and where the pools start
+  const SysSlots *sys_slots = nullptr;
+  u64 pool_at_cells = 0, pool_at_bodies = 0;
 };
 // Both stages without a host synchronisation, for stream capture: grids
 // sized by the capacities, counts read on the device. One key word only (a
