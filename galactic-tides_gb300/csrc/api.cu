@@ -623,6 +623,10 @@ __global__ void k_unpack_direct(const float4 *out, u32 n, double *acc, double *p
 }
 }  // namespace gtc
 
+namespace {
+struct ForestGraph;
+}
+
 // Independent systems advanced together. As one forest (every stage one
 // launch for all systems, forest.cu) when their shared parameters agree, or
 // with one context (stream, workspace) per system and every system's step
@@ -639,6 +643,11 @@ struct gtc_ensemble {
   int forest_walk = -1;  // option "walk_warps" of the forest's walk
   double forest_headroom = 0.25;  // option "graph_headroom" of the forest's step graph
   std::unique_ptr<gtc::ForestRun> forest;
+  // The forest's step graph, kept for the next call on the same systems,
+  // parameters and dt (forest_key): that call replays it at once.
+  std::unique_ptr<ForestGraph> forest_graph;
+  std::vector<u64> forest_key;
+  ~gtc_ensemble();
 };
 
 namespace {
@@ -674,6 +683,11 @@ struct ForestGraph {
   gtc::GraphCaps caps{};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+
+  ForestGraph() = default;
+  ForestGraph(const ForestGraph &) = delete;
+  ForestGraph &operator=(const ForestGraph &) = delete;
+  ~ForestGraph() { drop(); }
 
   void drop() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -749,26 +763,70 @@ struct ForestGraph {
   }
 };
 
+// What a kept forest graph depends on: the systems' arrays, sizes and
+// parameters, dt and the forest options.
+std::vector<u64> forest_key(const gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs,
+                            double dt) {
+  std::vector<u64> k;
+  auto d = [&](double v) {
+    u64 b;
+    std::memcpy(&b, &v, sizeof b);
+    k.push_back(b);
+  };
+  d(dt);
+  d(e->forest_headroom);
+  k.push_back(static_cast<u64>(static_cast<int64_t>(e->forest_walk)));
+  for (const gtc::ForestSystem &f : fs) {
+    for (const void *p : {static_cast<const void *>(f.pos), static_cast<const void *>(f.vel),
+                          static_cast<const void *>(f.acc), static_cast<const void *>(f.pot),
+                          static_cast<const void *>(f.mass)})
+      k.push_back(reinterpret_cast<std::uintptr_t>(p));
+    k.push_back(f.n);
+    d(f.sp.G);
+    d(f.sp.theta);
+    d(f.sp.eps);
+    k.push_back((static_cast<u64>(f.sp.quadrupole) << 48) ^ (static_cast<u64>(f.sp.group_size) << 32) ^
+                (static_cast<u64>(f.sp.leaf_size) << 16) ^ static_cast<u64>(f.sp.pack));
+  }
+  return k;
+}
+
 // The ensemble's leapfrog as one forest, eager or with every step replayed
 // from one CUDA graph; afterwards each system's context holds its
-// interaction counts of the last step's lists.
+// interaction counts of the last step's lists. A graph is kept for the next
+// call: one on the same systems, parameters and dt without priming replays
+// it at once (its positions and masses gathered again); any eager solve
+// first drops it, as the buffers it points into may be reallocated.
 void leapfrog_forest(gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs, double dt,
                      u64 steps, bool prime, bool graph) {
   if (!e->forest) e->forest = std::make_unique<gtc::ForestRun>();
   gtc::ForestRun &f = *e->forest;
   cudaStream_t s = e->main;
-  f.setup(fs, s);
-  f.ws.walk_mode = e->forest_walk;
+  std::vector<u64> key = forest_key(e, fs, dt);
+  const bool kept = graph && !prime && e->forest_graph && e->forest_graph->exec &&
+                    e->forest_key == key;
+  if (!kept) {
+    e->forest_graph.reset();
+    e->forest_key.clear();
+    f.setup(fs, s);
+    f.ws.walk_mode = e->forest_walk;
+  } else {
+    f.gather(s);
+  }
   u64 replays = 0;
   if (!graph) {
     if (prime) f.solve(0, 0.0, s);
     for (u64 k = 0; k < steps; ++k) f.step(dt, s);
   } else {
-    // an eager solve sizes the buffers (with prime, the priming forces)
-    f.solve(0, 0.0, s, prime);
-    ForestGraph fg;
-    fg.f = &f;
-    fg.headroom = e->forest_headroom;
+    if (!kept) {
+      // an eager solve sizes the buffers (with prime, the priming forces)
+      f.solve(0, 0.0, s, prime);
+      e->forest_graph = std::make_unique<ForestGraph>();
+      e->forest_graph->f = &f;
+      e->forest_graph->headroom = e->forest_headroom;
+      e->forest_key = std::move(key);
+    }
+    ForestGraph &fg = *e->forest_graph;
     try {
       for (u64 k = 0; k < steps; ++k) {
         if (!fg.exec) fg.capture(dt, s);
@@ -778,10 +836,10 @@ void leapfrog_forest(gtc_ensemble *e, const std::vector<gtc::ForestSystem> &fs, 
         else ++replays;
       }
     } catch (...) {
-      fg.drop();
+      e->forest_graph.reset();
+      e->forest_key.clear();
       throw;
     }
-    fg.drop();
   }
   const std::vector<gtc::ForestSystemStats> st = f.system_stats(s);
   for (std::size_t k = 0; k < e->ctx.size(); ++k) {
@@ -1395,10 +1453,13 @@ gtc_status gtc_learned_predict(gtc_context *ctx, const float *feat, uint64_t n, 
 
 // ---------------------------------------------------- ensembles and tuning
 
+gtc_ensemble::~gtc_ensemble() = default;
+
 void gtc_ensemble_destroy(gtc_ensemble *e) {
   if (!e) return;
   cudaSetDevice(e->device);
   if (e->main) cudaStreamSynchronize(e->main);
+  e->forest_graph.reset();  // before the forest whose buffers it points into
   for (gtc_context *c : e->ctx) gtc_destroy(c);
   for (cudaEvent_t ev : e->joins)
     if (ev) cudaEventDestroy(ev);

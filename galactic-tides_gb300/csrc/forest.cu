@@ -229,6 +229,14 @@ void ForestRun::setup(const std::vector<ForestSystem> &systems, cudaStream_t s) 
   GTC_LAUNCH_CHECK();
 }
 
+void ForestRun::gather(cudaStream_t s) {
+  if (n == 0) return;
+  k_forest_gather_bodies<<<ceil_div(n, kT), kT, 0, s>>>(ptrs_dev, ws.forest.sys, ws.forest.start,
+                                                        static_cast<u32>(n), apos.as<double>(),
+                                                        amass.as<double>());
+  GTC_LAUNCH_CHECK();
+}
+
 void ForestRun::kick_drift(double h, double dt, cudaStream_t s) {
   if (n == 0) return;
   k_forest_kick_drift<<<ceil_div(n, kT), kT, 0, s>>>(ptrs_dev, ws.forest.sys, ws.forest.start,

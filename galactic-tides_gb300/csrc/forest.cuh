@@ -59,6 +59,8 @@ struct ForestRun {
   // One leapfrog step of every system (integrator.cpp:5-17).
   void step(double dt, cudaStream_t s);
   void kick_drift(double h, double dt, cudaStream_t s);
+  // The systems' positions and masses into the arena again.
+  void gather(cudaStream_t s);
   void scatter(int kick, double h, const u32 *abort, cudaStream_t s);
   // Per-system interaction counts of the current lists.
   std::vector<ForestSystemStats> system_stats(cudaStream_t s);

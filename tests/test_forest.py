@@ -139,3 +139,35 @@ def test_forest_refuses_mixed_parameters(gtc):
     with pytest.raises(gtc.GtcInvalidArgument):
         with gtc.Ensemble(1) as ens:
             ens.set_option("forest", 2)
+
+
+@gpu
+def test_forest_graph_kept_across_calls(gtc):
+    """A second call on the same systems and dt (no priming) replays the
+    graph the first call captured: two calls of two steps give bitwise the
+    four eager steps."""
+    import torch
+    d = torch.device("cuda", 0)
+    specs = [s for i, s in enumerate(systems(gtc)) if i not in (3, 4)]
+    want, _ = run(gtc, specs, forest=1, walk=0, steps=4)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(d)
+    bufs = []
+    with gtc.Ensemble(len(specs)) as ens:
+        for i, (pos, vel, mass, gs, pack) in enumerate(specs):
+            n = len(mass)
+            b = dict(pos=t(pos), vel=t(vel), mass=t(mass), acc=t(np.zeros((n, 3))),
+                     pot=t(np.zeros(n)))
+            bufs.append(b)
+            ens.set_system(i, b["pos"].data_ptr(), b["vel"].data_ptr(), b["mass"].data_ptr(),
+                           b["acc"].data_ptr(), b["pot"].data_ptr(), n,
+                           **dict(SOLVER, group_size=gs, pack=pack))
+        ens.set_option("forest", 1)
+        ens.set_option("walk_warps", 0)
+        torch.cuda.synchronize()
+        ens.leapfrog(0.01, 2, prime=True, graph=True)
+        ens.leapfrog(0.01, 2, prime=False, graph=True)
+        torch.cuda.synchronize()
+        assert ens.context(0).stats()["graph_steps"] == 2
+    for i, (b, w) in enumerate(zip(bufs, want)):
+        for k in ("pos", "vel", "acc", "pot"):
+            assert np.array_equal(b[k].cpu().numpy(), w[k]), (i, k)
