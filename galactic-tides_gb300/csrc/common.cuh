@@ -62,6 +62,20 @@ struct DeviceBuffer {
 
 inline u32 ceil_div(u64 a, u64 b) { return static_cast<u32>((a + b - 1) / b); }
 
+#ifdef __CUDACC__
+// 1/sqrt(x) of a positive normal float (r^2 with softening: r^2 >= eps^2):
+// the SFU's rsqrt (PTX rsqrt.approx.ftz.f32) without the subnormal-input
+// handling around rsqrtf, which costs FMA-pipe instructions in the
+// evaluators' inner loops. It returns rsqrtf's value bit for bit on every
+// positive normal float (tests/test_rsqrt_normal.py checks all of them); a
+// subnormal input is taken as 0 (result +inf) where rsqrtf scales it.
+__device__ __forceinline__ float rsqrt_normal(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+#endif
+
 // --------------------------------------------------------------- scans
 // Exclusive prefix sums over n elements on `s`. `tmp` is grown as needed.
 // The total is written to *total_dev (device memory, may be null).

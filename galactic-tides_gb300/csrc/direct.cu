@@ -33,7 +33,9 @@ __device__ __forceinline__ void add_pair(const float4 s0, const float4 s1, const
   const float2 dy = __fadd2_rn(f2(s0.z, s0.w), ny);
   const float2 dz = __fadd2_rn(f2(s1.x, s1.y), nz);
   const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-  float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+  // (r^2 >= eps^2; without softening only pairs closer than ~1e-19 could
+  // give a subnormal r^2, whose 1/r is meaningless either way)
+  float2 inv = f2(rsqrt_normal(r2.x), rsqrt_normal(r2.y));
   if (kMask) {
     inv.x = skip0 ? 0.f : inv.x;
     inv.y = skip1 ? 0.f : inv.y;

@@ -4,7 +4,9 @@
 // include/galactic_tides/kernels/gravity_kernels.h:71-135) and the same
 // order -- all cells in list order, then all bodies in list order, skipping
 // the target itself (gt_group_accel, :162-170) -- with FMA contraction and
-// the SFU reciprocal square root (rsqrtf) instead of 1/sqrt.
+// the SFU reciprocal square root (rsqrtf; in the packed kernel the SFU
+// instruction itself, rsqrt_normal, as every softened r^2 is a normal
+// float) instead of 1/sqrt.
 //
 // Lane l of a warp owns target begin + l of its group. The warp walks the
 // list 32 entries at a time: each lane loads one entry (coalesced index
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(kT)
                          dz = __fadd2_rn(pz, f2(s1.x, s1.y));
             const float2 ngm = f2(s1.z, s1.w);
             const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-            const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 inv = f2(rsqrt_normal(r2.x), rsqrt_normal(r2.y));
             const float2 inv2 = __fmul2_rn(inv, inv), inv3 = __fmul2_rn(inv, inv2);
             const float2 qxx = f2(s2.x, s2.y), qyy = f2(s2.z, s2.w), qzz = f2(s3.x, s3.y),
                          qxy = f2(s3.z, s3.w), qxz = f2(s4.x, s4.y), qyz = f2(s4.z, s4.w);
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(kT)
             const float2 dx = __fadd2_rn(px, f2(s0.x, s0.y)), dy = __fadd2_rn(py, f2(s0.z, s0.w)),
                          dz = __fadd2_rn(pz, f2(s1.x, s1.y));
             const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-            const float2 inv = f2(rsqrtf(r2.x), rsqrtf(r2.y));
+            const float2 inv = f2(rsqrt_normal(r2.x), rsqrt_normal(r2.y));
             const float2 gm = __fmul2_rn(f2(s1.z, s1.w), inv);       // -G m / r
             const float2 gm3 = __fmul2_rn(gm, __fmul2_rn(inv, inv));  // -G m / r^3
             ax = __ffma2_rn(gm3, dx, ax);
