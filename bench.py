@@ -546,7 +546,9 @@ def main():
             print(json.dumps({"metric": METRIC, "value": round(value, 4), "unit": "ms",
                               "n": n, "steps": args.steps, "only_steps": True,
                               "eval_kernel_ms": round(statistics.mean(
-                                  s["eval_kernel_ms"] for s in stats), 4)}), flush=True)
+                                  s["eval_kernel_ms"] for s in stats), 4),
+                              "lists_ms": round(statistics.mean(
+                                  s["lists_ms"] for s in stats), 4)}), flush=True)
         ctx.close()
         return
     st = stats[-1]

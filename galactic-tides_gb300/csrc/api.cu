@@ -68,7 +68,7 @@ void Workspace::release_all() {
                          &nend, &skip, &parent, &depth, &nchild, &isleaf, &kids, &arrive, &bucket, &walk32, &walk64, &cells,
                          &tasks, &gbegin, &gend, &gbox, &gboxf, &gcells, &gbodies, &gcell_off, &gbody_off,
                          &groups, &cell_list, &body_list, &spill, &splitpt, &root, &bbox_part, &scalars, &split, &scan_tmp,
-                         &direct_part, &walk_next, &radix.counts, &radix.scan_tmp};
+                         &direct_part, &up_arrive, &walk_next, &radix.counts, &radix.scan_tmp};
   for (DeviceBuffer *b : all) b->release();
   if (side) {
     cudaStreamSynchronize(side);
@@ -904,7 +904,12 @@ gtc_status gtc_create(gtc_context **out, int device) {
     if (prop.major < 10)
       throw gtc::RuntimeError(std::string("cuda: this build needs an sm_103 GPU, found ") +
                               prop.name);
-    GTC_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    // The context's stream at the greatest priority: work it queues runs
+    // before its side stream's (the FP64 moments, which a learned walk on
+    // this stream need not wait for) when both have blocks ready.
+    int least = 0, greatest = 0;
+    GTC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    GTC_CUDA(cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest));
     for (auto &ev : ctx->ev) GTC_CUDA(cudaEventCreate(&ev));
     GTC_CUDA(cudaHostAlloc(&ctx->host_sc, sizeof(gtc::Scalars), cudaHostAllocDefault));
     std::memset(ctx->host_sc, 0, sizeof(gtc::Scalars));

@@ -128,6 +128,7 @@ struct Workspace {
   DeviceBuffer root, bbox_part, scalars, split;
   DeviceBuffer scan_tmp;
   DeviceBuffer direct_part;               // direct sum: per-slice partial sums
+  DeviceBuffer up_arrive;                 // bottom-up FP32 moments: children finished, per node
   int direct_targets = 2;                 // direct sum: targets per thread (2 or 4)
   RadixScratch radix;
 

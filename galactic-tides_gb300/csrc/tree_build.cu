@@ -1131,13 +1131,21 @@ __device__ void leaf_moments32(const Moment32Arrays &a, u32 p) {
   finish_moments32(a, p, m, cx, cy, cz, q);
 }
 
+// Children's cells written by other threads of the same launch are read
+// from L2 (kL2): an SM's L1 may hold an older copy of the line.
+template <bool kL2>
+__device__ __forceinline__ float4 cell32(const float4 *p) {
+  return kL2 ? __ldcg(p) : *p;
+}
+
+template <bool kL2 = false>
 __device__ void node_moments32(const Moment32Arrays &a, u32 p) {
   const uint4 k0 = a.kids[2ull * p], k1 = a.kids[2ull * p + 1];
   const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
   const int nc = a.nchild[p];
   float m = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   for (int j = nc - 1; j >= 0; --j) {
-    const float4 c = a.cells[3 * ch[j]];
+    const float4 c = cell32<kL2>(&a.cells[3 * ch[j]]);
     m += c.w;
     cx += c.w * c.x;
     cy += c.w * c.y;
@@ -1155,7 +1163,8 @@ __device__ void node_moments32(const Moment32Arrays &a, u32 p) {
   }
   float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int j = nc - 1; j >= 0; --j) {
-    const float4 c = a.cells[3 * ch[j]], qa = a.cells[3 * ch[j] + 1], qb = a.cells[3 * ch[j] + 2];
+    const float4 c = cell32<kL2>(&a.cells[3 * ch[j]]), qa = cell32<kL2>(&a.cells[3 * ch[j] + 1]),
+                 qb = cell32<kL2>(&a.cells[3 * ch[j] + 2]);
     const float dx = c.x - cx, dy = c.y - cy, dz = c.z - cz;
     const float r2 = dx * dx + dy * dy + dz * dz;
     q[0] += qa.x + c.w * (3.f * dx * dx - r2);
@@ -1308,22 +1317,31 @@ __global__ void __launch_bounds__(32)
   }
 }
 
+// All of the FP32 moments in one launch, bottom-up: a thread per leaf (in
+// the leaf buckets' order) computes its leaf, then climbs while it is the
+// last child of its parent to finish, computing that parent from its
+// children in child order as node_moments32 does. So every node is computed
+// once, after all its children, with the same operations as the per-depth
+// launches; the climb ends at the root or at a parent a sibling will
+// finish (at most kMaxDepth steps).
 __global__ void __launch_bounds__(kT)
-    k_leaf_moments32(Moment32Arrays a, const u32 *bucket, const u32 *meta) {
+    k_moments32_up(Moment32Arrays a, const u32 *bucket, const u32 *meta, const u32 *parent,
+                   u32 *arrive) {
   u32 count = 0;
   for (int b = kLeafBucket; b < kLeafBucket + kLeafClasses; ++b) count += meta[b];
   const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k < count) leaf_moments32(a, bucket[meta[kBuckets + kLeafBucket] + k]);
-}
-
-// One depth's inner nodes, one thread each (FP32: no need to spread them).
-__global__ void __launch_bounds__(kT)
-    k_node_moments32(Moment32Arrays a, const u32 *bucket, const u32 *meta, int b0, int nb) {
-  u32 count = 0;
-  for (int b = b0; b < b0 + nb; ++b) count += meta[b];
-  const u32 off = meta[kBuckets + b0];
-  for (u32 k = blockIdx.x * kT + threadIdx.x; k < count; k += gridDim.x * kT)
-    node_moments32(a, bucket[off + k]);
+  if (k >= count) return;
+  u32 p = bucket[meta[kBuckets + kLeafBucket] + k];
+  leaf_moments32(a, p);
+  for (int step = 0; step <= kMaxDepth; ++step) {
+    const u32 q = parent[p];
+    if (q == 0xffffffffu) return;
+    __threadfence();  // this node's values before its parent's count
+    if (atomicAdd(&arrive[q], 1u) + 1u != a.nchild[q]) return;
+    __threadfence();  // the siblings' values, counted before this, are visible
+    node_moments32<true>(a, q);
+    p = q;
+  }
 }
 
 __global__ void k_root_mass(const float4 *cells32, double2 *rootmom) {
@@ -1806,13 +1824,11 @@ void moments32(Workspace &ws, float4 *cells32, float *delta32, double2 *rootmom,
                          ws.nchild.as<u8>(),   ws.kids.as<uint4>(), ws.bodies.as<float4>(),
                          ws.root.as<TreeRoot>(), cells32, delta32};
   const u32 *meta = ws.arrive.as<u32>(), *bucket = ws.bucket.as<u32>();
-  k_leaf_moments32<<<ceil_div(m, kT), kT, 0, s>>>(a, bucket, meta);
+  ws.up_arrive.ensure(m * sizeof(u32));
+  GTC_CUDA(cudaMemsetAsync(ws.up_arrive.ptr, 0, m * sizeof(u32), s));
+  k_moments32_up<<<ceil_div(m, kT), kT, 0, s>>>(a, bucket, meta, ws.parent.as<u32>(),
+                                                ws.up_arrive.as<u32>());
   GTC_LAUNCH_CHECK();
-  for (int d = ws.tree_depth - 1; d >= 0; --d) {
-    k_node_moments32<<<ceil_div(std::max<u32>(1, m / 4), kT), kT, 0, s>>>(
-        a, bucket, meta, d * kSizeClasses, kSizeClasses);
-    GTC_LAUNCH_CHECK();
-  }
   k_root_mass<<<1, 1, 0, s>>>(cells32, rootmom);
   GTC_LAUNCH_CHECK();
 }
