@@ -85,6 +85,15 @@ void Workspace::release_all() {
   }
 }
 
+void check_device_error(u32 code) {
+  if (code == 0) return;
+  if (code & 4u) throw InvalidArgument("cuda: positions must be finite");
+  if (code & 8u) throw RuntimeError("cuda: the learned walk's count and fill passes disagree");
+  if (code & 16u) throw RuntimeError("cuda: the radix sort's look-back outwaited its bound");
+  throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
+                     std::to_string(code) + ")");
+}
+
 void Workspace::stage(int k, cudaStream_t s) {
   if (!stage_on) return;
   if (!stage_ev[k]) GTC_CUDA(cudaEventCreate(&stage_ev[k]));
@@ -218,13 +227,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
                            cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
-  if (ctx->host_sc->error & 4u)
-    throw gtc::InvalidArgument("cuda: positions must be finite");
-  if (ctx->host_sc->error & 8u)
-    throw gtc::RuntimeError("cuda: the learned walk's count and fill passes disagree");
-  if (ctx->host_sc->error != 0)
-    throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                            std::to_string(ctx->host_sc->error) + ")");
+  gtc::check_device_error(ctx->host_sc->error);
   gtc_stats &st = ctx->stats;
   st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
   st.lists_ms = elapsed(ctx->ev[1], ctx->ev[2]);
@@ -387,10 +390,7 @@ struct GraphStep {
   bool finish(double dt) {
     gtc::Workspace &ws = ctx->ws;
     const gtc::Scalars &hs = *ctx->host_sc;
-    if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
-    if (hs.error)
-      throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                              std::to_string(hs.error) + ")");
+    gtc::check_device_error(hs.error);
     if (hs.abort) {
       group_force(ctx, pos, mass, n, sp, acc, pot);
       gtc::kick(vel, acc, n, 0.5 * dt, ctx->stream);
@@ -592,9 +592,7 @@ void tree_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
                            cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
-  if (ctx->host_sc->error != 0)
-    throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                            std::to_string(ctx->host_sc->error) + ")");
+  gtc::check_device_error(ctx->host_sc->error);
   gtc_stats &st = ctx->stats;
   st.tree_ms = elapsed(ctx->ev[0], ctx->ev[1]);
   st.evaluate_ms = st.eval_kernel_ms = elapsed(ctx->ev[4], ctx->ev[5]);
@@ -744,10 +742,7 @@ struct ForestGraph {
   bool finish(double dt, cudaStream_t s) {
     gtc::Workspace &ws = f->ws;
     const gtc::Scalars &hs = *f->host_sc;
-    if (hs.error & 4u) throw gtc::InvalidArgument("cuda: positions must be finite");
-    if (hs.error)
-      throw gtc::RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                              std::to_string(hs.error) + ")");
+    gtc::check_device_error(hs.error);
     if (hs.abort) {
       f->solve(1, 0.5 * dt, s);
       return true;

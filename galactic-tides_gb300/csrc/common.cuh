@@ -88,13 +88,16 @@ void reserve_scans(DeviceBuffer &tmp, u64 n);
 
 // ---------------------------------------------------------- radix sort
 // Stable LSD radix sort of (key, value) pairs on `bits` bits of the key from
-// bit `low_bit` up, 8 bits a pass. The sorted pairs end up back in
-// keys/vals; alt_* are scratch of n elements each.
+// bit `low_bit` up, 8 bits a pass, one launch per pass. The sorted pairs end
+// up back in keys/vals; alt_* are scratch of n elements each. A look-back
+// that outwaits its bound sets bit 16 of *error (device word; null: a word
+// of the scratch).
 struct RadixScratch {
   DeviceBuffer counts, scan_tmp;
 };
 void radix_sort_pairs(u64 *keys, u32 *vals, u64 *alt_keys, u32 *alt_vals, u32 n, int bits,
-                      RadixScratch &scratch, cudaStream_t s, int low_bit = 0);
+                      RadixScratch &scratch, cudaStream_t s, int low_bit = 0,
+                      u32 *error = nullptr);
 
 // ------------------------------------------------------- warp helpers
 constexpr unsigned kFullMask = 0xffffffffu;

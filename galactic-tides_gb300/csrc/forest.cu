@@ -268,10 +268,7 @@ void ForestRun::solve(int kick, double h, cudaStream_t s, bool write) {
   if (write) scatter(kick, h, nullptr, s);
   GTC_CUDA(cudaMemcpyAsync(host_sc, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));
-  if (host_sc->error & 4u) throw InvalidArgument("cuda: positions must be finite");
-  if (host_sc->error)
-    throw RuntimeError("cuda: inconsistent tree detected on the device (code " +
-                       std::to_string(host_sc->error) + ")");
+  check_device_error(host_sc->error);
 }
 
 void ForestRun::step(double dt, cudaStream_t s) {

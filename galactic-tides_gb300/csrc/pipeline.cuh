@@ -409,6 +409,12 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
                       cudaStream_t s);
 void bbox_root(Workspace &ws, const double *pos, u64 n, cudaStream_t s);
 
+// Throws for a device-detected failure code (Scalars::error; 0: none): bit 4
+// non-finite positions (InvalidArgument), 8 the learned walk's count and fill
+// passes disagree, 16 a radix-sort look-back outwaited its bound, 1 (and any
+// other) an inconsistent tree.
+void check_device_error(u32 code);
+
 // FP32 FMA throughput of the device (TFLOP/s), by a dense FMA kernel on every SM.
 double fp32_peak_tflops(cudaStream_t s);
 

@@ -1523,8 +1523,9 @@ int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s,
   const int passes = levels >= kLevelsPerWord ? 8 : (3 * std::max(levels, 1) + 7) / 8;
   const int low = std::max(0, 3 * kLevelsPerWord - 8 * passes);
   ws.sort_passes = passes;
+  u32 *err = &ws.scalars.as<Scalars>()->error;
   radix_sort_pairs(ws.key0.as<u64>(), ws.idx.as<u32>(), ws.key0_alt.as<u64>(),
-                   ws.idx_alt.as<u32>(), n, 3 * kLevelsPerWord - low, ws.radix, s, low);
+                   ws.idx_alt.as<u32>(), n, 3 * kLevelsPerWord - low, ws.radix, s, low, err);
   if (ws.forest) {
     const ForestView &fv = ws.forest;
     ws.dkey.ensure(n * 8ull);
@@ -1540,7 +1541,7 @@ int sort_top_levels(Workspace &ws, u32 n, int levels, cudaStream_t s,
     int bits = 1;
     while (bits < 16 && (1u << bits) < fv.systems) ++bits;
     radix_sort_pairs(skey, spos, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), n, bits, ws.radix,
-                     s);
+                     s, 0, err);
     k_forest_gather<<<nb, kT, 0, s>>>(spos, ws.key0_alt.as<u64>(), ws.idx_alt.as<u32>(), n,
                                       ws.key0.as<u64>(), ws.idx.as<u32>(), abort);
     GTC_LAUNCH_CHECK();
@@ -1708,7 +1709,8 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     // then stably by segment number
     u64 *dkey = ws.dkey.as<u64>();
     GTC_CUDA(cudaMemcpyAsync(dkey, dword, nd * 8ull, cudaMemcpyDeviceToDevice, s));
-    radix_sort_pairs(dkey, drec, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), nd, 63, ws.radix, s);
+    radix_sort_pairs(dkey, drec, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), nd, 63, ws.radix, s,
+                     0, &sc->error);
     u32 *sflag = ws.flags.as<u32>(), *sscan = ws.flags_scan.as<u32>();
     k_deep_segments<<<ndb, kT, 0, s>>>(kv, dpos, nd, sflag);
     GTC_LAUNCH_CHECK();
@@ -1719,7 +1721,7 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
     k_seg_keys<<<ndb, kT, 0, s>>>(drec, sscan, sflag, nd, dkey);
     GTC_LAUNCH_CHECK();
     radix_sort_pairs(dkey, drec, ws.dkey_alt.as<u64>(), ws.drec_alt.as<u32>(), nd, seg_bits,
-                     ws.radix, s);
+                     ws.radix, s, 0, &sc->error);
     k_deep_scatter<<<ndb, kT, 0, s>>>(dpos, drec, didx, dword, nd, idx, wbuf.as<u64>());
     GTC_LAUNCH_CHECK();
     if (kv.words == 1) kv.w1 = ws.key1.as<u64>();
