@@ -621,6 +621,104 @@ __device__ __forceinline__ u32 warp_excl_scan(u32 v, int lane, u32 &total) {
   return s - v;
 }
 
+// Walks the ranges on a warp's stack (stk[0..top), each a run of whole
+// subtrees [i, end)) to the end for group g: each step the lanes take the
+// ranges on top, test each range's first node, and push back the rest of
+// its range and, when the node is opened, its children's range (children
+// on top). Cells and bodies go to cl / bl from nc / nb on (kWrite; counting
+// past cap_c / cap_b), in step order, lane order within a step. When the
+// stack is nearly full, lane 0 walks the top range alone, so no step can
+// overflow it. Every lane of the warp calls it; nc and nb are warp-uniform.
+template <bool kWrite>
+__device__ __forceinline__ void walk_ranges_warp(uint2 *stk, u32 top, const WalkRec32 *walk32,
+                                                 const WalkRec64 *walk64, const float *gf,
+                                                 const float *hf, float gbound,
+                                                 const double *gbox, u32 g, u32 *cl, u32 *bl,
+                                                 u64 cap_c, u64 cap_b, u64 &nc, u64 &nb,
+                                                 u32 &exact, u32 &visits, Scalars *sc) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  while (top > 0) {
+    if (top > kWarpStack - 2 * 32) {
+      // nearly full: lane 0 walks the top range alone, without a stack
+      const uint2 e = stk[top - 1];
+      --top;
+      __syncwarp();
+      if (lane == 0) {
+        u32 i = e.x;
+        while (i < e.y) {
+          const WalkRec32 r = load32(walk32, i);
+          ++visits;
+          const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
+          const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+          const bool leaf = (r.nbody_leaf >> 31) != 0;
+          if (verdict == 1 && nbody > kFewBodies) {
+            if (kWrite && nc < cap_c) cl[nc] = i;
+            ++nc;
+          } else if (verdict == 1 || leaf) {
+            for (u32 j = 0; j < nbody; ++j)
+              if (kWrite && nb + j < cap_b) bl[nb + j] = r.begin + j;
+            nb += nbody;
+          }
+          if (verdict == 1 || leaf) {
+            if (r.skip <= i) {  // malformed tree: never loop
+              atomicOr(&sc->error, 1u);
+              break;
+            }
+            i = r.skip;
+          } else {
+            ++i;
+          }
+        }
+      }
+      nc = __shfl_sync(kFullMask, nc, 0);
+      nb = __shfl_sync(kFullMask, nb, 0);
+      continue;
+    }
+    const u32 take = min(32u, top);
+    const bool has = static_cast<u32>(lane) < take;
+    const uint2 e = has ? stk[top - 1 - lane] : make_uint2(0u, 0u);
+    top -= take;
+    __syncwarp();
+    WalkRec32 r{};
+    int verdict = 0;
+    if (has) {
+      r = load32(walk32, e.x);
+      ++visits;
+      verdict = decide(r, walk64, e.x, gf, hf, gbound, gbox, g, exact);
+    }
+    const u32 nbody = r.nbody_leaf & 0x7fffffffu;
+    const bool leaf = (r.nbody_leaf >> 31) != 0;
+    const bool bad = has && r.skip <= e.x;  // malformed tree: never loop
+    if (bad) atomicOr(&sc->error, 1u);
+    const bool cell = has && verdict == 1 && nbody > kFewBodies;
+    const bool bod = has && !cell && (verdict == 1 || leaf);
+    const bool kids = has && !bad && verdict == 0 && !leaf;
+    const bool rest = has && !bad && r.skip < e.y;
+    // cells: one slot per accepting lane, in lane order
+    const unsigned mc = __ballot_sync(kFullMask, cell);
+    if (kWrite && cell) {
+      const u64 pos = nc + __popc(mc & below);
+      if (pos < cap_c) cl[pos] = e.x;
+    }
+    nc += __popc(mc);
+    // bodies: each lane's run after the runs of the lanes before it
+    u32 bt = 0;
+    const u32 boff = warp_excl_scan(bod ? nbody : 0u, lane, bt);
+    if (kWrite && bod)
+      for (u32 j = 0; j < nbody; ++j)
+        if (nb + boff + j < cap_b) bl[nb + boff + j] = r.begin + j;
+    nb += bt;
+    // pushes: each lane its rest, then its children's range (on top)
+    u32 pt = 0;
+    const u32 poff = warp_excl_scan(static_cast<u32>(rest) + static_cast<u32>(kids), lane, pt);
+    if (rest) stk[top + poff] = make_uint2(r.skip, e.y);
+    if (kids) stk[top + poff + (rest ? 1u : 0u)] = make_uint2(e.x + 1, r.skip);
+    top += pt;
+    __syncwarp();
+  }
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(kWarpWalkThreads)
     k_walk_warp(const WalkRec32 *walk32, const WalkRec64 *walk64, const double *gbox,
@@ -631,7 +729,6 @@ __global__ void __launch_bounds__(kWarpWalkThreads)
   const u32 ng = bounded(ng_cap, ng_dev);
   const int lane = threadIdx.x & 31;
   uint2 *stk = stack_all[threadIdx.x >> 5];
-  const unsigned below = (1u << lane) - 1u;
   u32 exact = 0, visits = 0;
   for (;;) {
     u32 g = 0;
@@ -673,85 +770,8 @@ __global__ void __launch_bounds__(kWarpWalkThreads)
     if (lane == 0) stk[0] = make_uint2(root_leaf ? root : root + 1, rr.skip);
     u32 top = 1;
     __syncwarp();
-    while (top > 0) {
-      if (top > kWarpStack - 2 * 32) {
-        // nearly full: lane 0 walks the top range alone, without a stack
-        const uint2 e = stk[top - 1];
-        --top;
-        __syncwarp();
-        if (lane == 0) {
-          u32 i = e.x;
-          while (i < e.y) {
-            const WalkRec32 r = load32(walk32, i);
-            ++visits;
-            const int verdict = decide(r, walk64, i, gf, hf, gbound, gbox, g, exact);
-            const u32 nbody = r.nbody_leaf & 0x7fffffffu;
-            const bool leaf = (r.nbody_leaf >> 31) != 0;
-            if (verdict == 1 && nbody > kFewBodies) {
-              if (kMode != kCount && nc < cap_c) cl[nc] = i;
-              ++nc;
-            } else if (verdict == 1 || leaf) {
-              for (u32 j = 0; j < nbody; ++j)
-                if (kMode != kCount && nb + j < cap_b) bl[nb + j] = r.begin + j;
-              nb += nbody;
-            }
-            if (verdict == 1 || leaf) {
-              if (r.skip <= i) {  // malformed tree: never loop
-                atomicOr(&sc->error, 1u);
-                break;
-              }
-              i = r.skip;
-            } else {
-              ++i;
-            }
-          }
-        }
-        nc = __shfl_sync(kFullMask, nc, 0);
-        nb = __shfl_sync(kFullMask, nb, 0);
-        continue;
-      }
-      const u32 take = min(32u, top);
-      const bool has = static_cast<u32>(lane) < take;
-      const uint2 e = has ? stk[top - 1 - lane] : make_uint2(0u, 0u);
-      top -= take;
-      __syncwarp();
-      WalkRec32 r{};
-      int verdict = 0;
-      if (has) {
-        r = load32(walk32, e.x);
-        ++visits;
-        verdict = decide(r, walk64, e.x, gf, hf, gbound, gbox, g, exact);
-      }
-      const u32 nbody = r.nbody_leaf & 0x7fffffffu;
-      const bool leaf = (r.nbody_leaf >> 31) != 0;
-      const bool bad = has && r.skip <= e.x;  // malformed tree: never loop
-      if (bad) atomicOr(&sc->error, 1u);
-      const bool cell = has && verdict == 1 && nbody > kFewBodies;
-      const bool bod = has && !cell && (verdict == 1 || leaf);
-      const bool kids = has && !bad && verdict == 0 && !leaf;
-      const bool rest = has && !bad && r.skip < e.y;
-      // cells: one slot per accepting lane, in lane order
-      const unsigned mc = __ballot_sync(kFullMask, cell);
-      if (kMode != kCount && cell) {
-        const u64 pos = nc + __popc(mc & below);
-        if (pos < cap_c) cl[pos] = e.x;
-      }
-      nc += __popc(mc);
-      // bodies: each lane's run after the runs of the lanes before it
-      u32 bt = 0;
-      const u32 boff = warp_excl_scan(bod ? nbody : 0u, lane, bt);
-      if (kMode != kCount && bod)
-        for (u32 j = 0; j < nbody; ++j)
-          if (nb + boff + j < cap_b) bl[nb + boff + j] = r.begin + j;
-      nb += bt;
-      // pushes: each lane its rest, then its children's range (on top)
-      u32 pt = 0;
-      const u32 poff = warp_excl_scan(static_cast<u32>(rest) + static_cast<u32>(kids), lane, pt);
-      if (rest) stk[top + poff] = make_uint2(r.skip, e.y);
-      if (kids) stk[top + poff + (rest ? 1u : 0u)] = make_uint2(e.x + 1, r.skip);
-      top += pt;
-      __syncwarp();
-    }
+    walk_ranges_warp<kMode != kCount>(stk, top, walk32, walk64, gf, hf, gbound, gbox, g, cl, bl,
+                                      cap_c, cap_b, nc, nb, exact, visits, sc);
     if (lane == 0) {
       if (kMode == kCount) {
         out.ncells[g] = nc;
