@@ -171,3 +171,24 @@ def test_forest_graph_kept_across_calls(gtc):
     for i, (b, w) in enumerate(zip(bufs, want)):
         for k in ("pos", "vel", "acc", "pot"):
             assert np.array_equal(b[k].cpu().numpy(), w[k]), (i, k)
+
+
+@gpu
+def test_forest_of_many_small_systems(gtc):
+    """300 systems of 20..2000 bodies: the sort's pass by system takes two
+    8-bit digits and each system's split table fewer levels (15 within the
+    budget); each system still moves to the doubles of its own step."""
+    rng = np.random.default_rng(77)
+    specs = []
+    for k in range(300):
+        n = int(rng.integers(20, 2000))
+        pos, mass = lopsided_sphere(n, 1000 + k)
+        pos = pos * rng.uniform(0.1, 10.0) + rng.normal(size=3) * 50.0
+        specs.append((pos, rng.normal(size=pos.shape) * 0.05, mass, int(rng.choice([8, 16, 32])),
+                      int(rng.choice([0, 1]))))
+    got, got_stats = run(gtc, specs, forest=1, walk=0, steps=2)
+    want, want_stats = run(gtc, specs, forest=0, walk=0, steps=2)
+    for i, (g, w) in enumerate(zip(got, want)):
+        for k in ("pos", "vel", "acc", "pot"):
+            assert np.array_equal(g[k], w[k]), (i, k)
+    assert [s[:3] for s in got_stats] == [s[:3] for s in want_stats]
