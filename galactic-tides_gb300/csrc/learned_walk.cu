@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <string>
 #include <vector>
 
@@ -864,7 +865,7 @@ __global__ void __launch_bounds__(kT) k_lgroup_records(const GArgs a, const u32 
   const bool valid = g < a.ng;
   u64 t = 0, nc = 0, nb = 0;
   if (valid) {
-    ListSegs cs, bs;
+    ListSegs cs{}, bs{};  // (segments past kParts stay empty)
     for (int k = 0; k < kParts; ++k) {
       const u64 at = static_cast<u64>(k) * a.ng + g;
       cs.start[k] = static_cast<u32>(a.cells_at[k] + static_cast<u64>(g) * a.slot_cells[k]);
@@ -1010,7 +1011,7 @@ u32 learned_slot(u64 longest) {
 
 void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
                          cudaStream_t s) {
-  static_assert(kParts == kListSegments, "one list segment per part");
+  static_assert(kParts <= kListSegments, "one list segment per part");
   if (ng == 0) return;
   if (ws.n_nodes >= kPairOpen)
     throw RuntimeError("learned walk: too many tree nodes for 32 bit node ranges");
@@ -1085,7 +1086,10 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
     GTC_CUDA(cudaMemsetAsync(&sc->cell_interactions, 0, 3 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_group, 0, sizeof(u32), s));
     GTC_CUDA(cudaMemsetAsync(&sc->list_overflow, 0, sizeof(u32), s));
-    GTC_CUDA(cudaMemsetAsync(sc->lmax_cells, 0, (2 * kParts + 1) * sizeof(u32), s));
+    GTC_CUDA(cudaMemsetAsync(sc->lmax_cells, 0,
+                             offsetof(Scalars, max_pend) + sizeof(u32) -
+                                 offsetof(Scalars, lmax_cells),
+                             s));  // lmax_cells, lmax_bodies, max_pend
     GTC_CUDA(cudaMemsetAsync(&sc->walk_nodes, 0, sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->mlp_rows, 0, 2 * sizeof(unsigned long long), s));
     GTC_CUDA(cudaMemsetAsync(&sc->max_rows, 0, sizeof(u32), s));
