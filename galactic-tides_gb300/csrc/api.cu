@@ -75,10 +75,11 @@ void Workspace::release_all() {
     cudaStreamDestroy(side);
     cudaEventDestroy(side_fork);
     cudaEventDestroy(side_done);
+    cudaEventDestroy(side_walk);
   }
   side = nullptr;
-  side_fork = side_done = nullptr;
-  side_pending = false;
+  side_fork = side_done = side_walk = nullptr;
+  side_pending = walk_pending = false;
   for (cudaEvent_t &e : stage_ev) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
@@ -265,6 +266,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
 // do); offsets stay below 2^32 (a replay that needs more aborts).
 void reserve_graph(gtc::Workspace &ws, const gtc::Scalars &hs, double headroom, u64 n,
                    gtc::GraphCaps &caps, bool sized_lists = false) {
+  gtc::ensure_side(ws);  // the captured build forks the quadrupoles onto it
   const double f = 1.0 + headroom;
   const u64 pad = headroom > 0 ? 1024 : 0;
   caps.nodes = static_cast<u32>(std::min<u64>(static_cast<u64>(ws.n_nodes * f) + pad, 0xfffffff0ull));
@@ -369,6 +371,7 @@ struct GraphStep {
     gtc::build_tree_graph(ws, pos, mass, n, sp, caps, s);
     mark(1, s);
     gtc::build_lists_graph(ws, sp, caps, s);
+    gtc::join_side(ws, s);  // the cells
     mark(2, s);
     mark(4, s);
     gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
@@ -701,6 +704,7 @@ struct ForestGraph {
     f->kick_drift(h, dt, s);
     gtc::build_tree_graph(ws, f->apos.as<double>(), f->amass.as<double>(), f->n, f->sp, caps, s);
     gtc::build_lists_graph(ws, f->sp, caps, s);
+    gtc::join_side(ws, s);  // the cells
     gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
                               ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
                               ws.groups.as<uint4>(), f->n, sc, static_cast<float>(f->sp.G),

@@ -1070,7 +1070,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     join_side(ws, s);
     return;
   }
-  join_side(ws, s);  // the walk reads the node records
+  join_walk(ws, s);  // the walk reads the node records (the cells follow on the side stream)
   ws.stage(Workspace::kStWalk0, s);
 
   const WalkRec32 *w32 = ws.walk32.as<WalkRec32>();
@@ -1158,6 +1158,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     read_scalars(ws, host, s);
     size_slots(ws, *host, true);
     if (!host->list_overflow) {
+      join_side(ws, s);  // the lists' readers read the cells too
       ws.n_cell_list = host->n_cell_list;
       ws.n_body_list = host->n_body_list;
       ws.gapped = true;
@@ -1220,6 +1221,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
   ws.stage(Workspace::kStWalk1, s);
   ws.lists_unordered = warps;
   ws.list_passes = 2;
+  join_side(ws, s);
 }
 
 void build_lists_graph(Workspace &ws, const SolverParams &sp, const GraphCaps &caps,

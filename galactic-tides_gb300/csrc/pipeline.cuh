@@ -163,10 +163,12 @@ struct Workspace {
   u32 list_passes = 0;  // walks of the last list build (1 one pass, 2 count + fill, rounds)
   // The tree's moments and node records run on a side stream once the
   // topology is known, beside the group choice on the main stream; whoever
-  // reads them first makes the main stream wait for `side_done`.
+  // reads them first makes the main stream wait for `side_done`. The walk
+  // records are ready earlier, at `side_walk` (the quadrupoles and the cells
+  // follow them on the side stream).
   cudaStream_t side = nullptr;
-  cudaEvent_t side_fork = nullptr, side_done = nullptr;
-  bool side_pending = false;
+  cudaEvent_t side_fork = nullptr, side_done = nullptr, side_walk = nullptr;
+  bool side_pending = false, walk_pending = false;
   // Optional stage events (context option "stage_events"): CUDA events at
   // the boundaries of the eager build's and walk's stages, for per-stage
   // device times. Off by default.
@@ -307,10 +309,16 @@ __device__ __forceinline__ void warp_add(unsigned long long *total, unsigned lon
 // Fills geometry, moments, ranges, the tree-order permutation (idx), the
 // FP32 bodies and cells and the walk records. Returns the node count.
 // `host` is pinned memory the device scalars are read back into.
+// The side stream and its events (made before a capture uses them).
+void ensure_side(Workspace &ws);
 // The side stream, started after the work queued on s so far.
 cudaStream_t fork_side(Workspace &ws, cudaStream_t s);
 // Work queued on the side stream so far ends before what s runs next.
 void join_side(Workspace &ws, cudaStream_t s);
+// The side stream's walk records (marked by mark_walk_ready) are written
+// before what s runs next; its later work may still run.
+void mark_walk_ready(Workspace &ws, cudaStream_t side);
+void join_walk(Workspace &ws, cudaStream_t s);
 // Joins the side stream when it leaves scope (every exit of a solve).
 struct SideJoin {
   Workspace &ws;

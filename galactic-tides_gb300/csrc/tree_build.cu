@@ -975,7 +975,11 @@ __device__ __forceinline__ void store_pair(double2 *a, u32 p, double x, double y
   a[2 * p + 1] = make_double2(z, w);
 }
 
-__device__ void leaf_moments(const MomentArrays &a, u32 p) {  // octree.cpp:46-72
+// The moments in two passes, with the reference's operations in its order:
+// the centre of mass and delta first (all the walk's records need), the
+// quadrupole after it, from the stored centre of mass. The walk starts
+// after the first pass while the second one runs beside it.
+__device__ void leaf_com(const MomentArrays &a, u32 p) {  // octree.cpp:46-54, 71
   const Dbl4 g = load_pair(a.geom, p);
   const u32 b0 = a.nbegin[p], b1 = a.nend[p];
   double m = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
@@ -995,6 +999,15 @@ __device__ void leaf_moments(const MomentArrays &a, u32 p) {  // octree.cpp:46-7
     cy = g.y;
     cz = g.z;
   }
+  store_pair(a.mom, p, cx, cy, cz, m);
+  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
+  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+__device__ void leaf_quad(const MomentArrays &a, u32 p) {  // octree.cpp:55-70
+  const Dbl4 c = load_pair(a.mom, p);
+  const double cx = c.x, cy = c.y, cz = c.z;
+  const u32 b0 = a.nbegin[p], b1 = a.nend[p];
   double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
   for (u32 k = b0; k < b1; ++k) {
     const double mi = a.tmass[k];
@@ -1008,15 +1021,12 @@ __device__ void leaf_moments(const MomentArrays &a, u32 p) {  // octree.cpp:46-7
     q4 += mi * 3 * dx * dz;
     q5 += mi * 3 * dy * dz;
   }
-  store_pair(a.mom, p, cx, cy, cz, m);
   a.quad[3 * p] = make_double2(q0, q1);
   a.quad[3 * p + 1] = make_double2(q2, q3);
   a.quad[3 * p + 2] = make_double2(q4, q5);
-  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
-  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
 }
 
-__device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-102
+__device__ void node_com(const MomentArrays &a, u32 p) {  // octree.cpp:75-85, 101
   const Dbl4 g = load_pair(a.geom, p);
   const uint4 k0 = a.kids[2ull * p], k1 = a.kids[2ull * p + 1];
   const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};  // last octant first
@@ -1038,6 +1048,17 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
     cy = g.y;
     cz = g.z;
   }
+  store_pair(a.mom, p, cx, cy, cz, m);
+  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
+  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+__device__ void node_quad(const MomentArrays &a, u32 p) {  // octree.cpp:86-100
+  const Dbl4 pc = load_pair(a.mom, p);
+  const double cx = pc.x, cy = pc.y, cz = pc.z;
+  const uint4 k0 = a.kids[2ull * p], k1 = a.kids[2ull * p + 1];
+  const u32 ch[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+  const int nc = a.nchild[p];
   double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
   for (int j = nc - 1; j >= 0; --j) {
     const Dbl4 c = load_pair(a.mom, ch[j]);
@@ -1051,17 +1072,15 @@ __device__ void node_moments(const MomentArrays &a, u32 p) {  // octree.cpp:75-1
     q4 += qc.x + c.w * 3 * dx * dz;
     q5 += qc.y + c.w * 3 * dy * dz;
   }
-  store_pair(a.mom, p, cx, cy, cz, m);
   a.quad[3 * p] = make_double2(q0, q1);
   a.quad[3 * p + 1] = make_double2(q2, q3);
   a.quad[3 * p + 2] = make_double2(q4, q5);
-  const double ex = cx - g.x, ey = cy - g.y, ez = cz - g.z;
-  a.delta[p] = sqrt(ex * ex + ey * ey + ez * ez);
 }
 
 // FP32 estimates of the moments, for the learned walk's decisions only: the
-// same sums as leaf_moments / node_moments, in FP32 on the FP32 bodies
-// (relative to the root centre), written as GTCell-layout cells plus delta.
+// same sums as the FP64 passes (leaf_com and leaf_quad, node_com and
+// node_quad), in FP32 on the FP32 bodies (relative to the root centre),
+// written as GTCell-layout cells plus delta.
 // They take a few tens of microseconds where the FP64 moments take most of a
 // millisecond, so the learned walk starts while the FP64 moments -- which
 // the evaluation reads -- are still being accumulated.
@@ -1278,13 +1297,18 @@ __global__ void __launch_bounds__(kT)
   if (b >= 0) bucket[base[b] + local] = p;
 }
 
+// kQuad: the quadrupole pass, else the centre-of-mass pass.
+template <bool kQuad>
 __global__ void __launch_bounds__(kT)
     k_leaf_moments(MomentArrays a, const u32 *bucket, const u32 *meta) {
   // the leaf buckets' count and first place, from the bucket scan
   u32 count = 0;
   for (int b = kLeafBucket; b < kLeafBucket + kLeafClasses; ++b) count += meta[b];
   const u32 k = blockIdx.x * kT + threadIdx.x;
-  if (k < count) leaf_moments(a, bucket[meta[kBuckets + kLeafBucket] + k]);
+  if (k >= count) return;
+  const u32 p = bucket[meta[kBuckets + kLeafBucket] + k];
+  if (kQuad) leaf_quad(a, p);
+  else leaf_com(a, p);
 }
 
 // Inner-node moments of one depth: one warp per block, `per` nodes to a
@@ -1301,6 +1325,7 @@ __host__ __device__ __forceinline__ u32 nodes_per_warp(u32 count) {
 // Over the device counts of buckets [b0, b0 + nb) (leaves or one depth's
 // inner nodes), grid-stride over kMomentWarps warps: no count is read back,
 // so the launches of every depth queue at once (eager and graph replays).
+template <bool kQuad>
 __global__ void __launch_bounds__(32)
     k_node_moments(MomentArrays a, const u32 *bucket, const u32 *meta, int b0, int nb,
                    const u32 *abort) {
@@ -1312,8 +1337,14 @@ __global__ void __launch_bounds__(32)
   if (threadIdx.x >= per) return;
   for (u64 k = static_cast<u64>(blockIdx.x) * per + threadIdx.x; k < count;
        k += static_cast<u64>(gridDim.x) * per) {
-    if (b0 >= kLeafBucket) leaf_moments(a, bucket[off + k]);
-    else node_moments(a, bucket[off + k]);
+    const u32 p = bucket[off + k];
+    if (b0 >= kLeafBucket) {
+      if (kQuad) leaf_quad(a, p);
+      else leaf_com(a, p);
+    } else {
+      if (kQuad) node_quad(a, p);
+      else node_com(a, p);
+    }
   }
 }
 
@@ -1359,14 +1390,15 @@ __global__ void k_check_tree_graph(Scalars *sc, u32 cap, int sorted_levels) {
 
 // --------------------------------------------------------------- packing
 
-// Walk records (FP32 and FP64) and FP32 cell of every node
-// (group_lists.cpp:52-61).
+// Walk records (FP32 and FP64) of every node (group_lists.cpp:59-61): they
+// need the centres of mass and deltas only, so they are packed after the
+// first moment pass.
 __global__ void __launch_bounds__(kT)
-    k_pack_nodes(const double2 *geom, const double2 *mom, const double2 *quad,
-                 const double *delta, const u32 *nbegin, const u32 *nend, const u32 *skip,
-                 const u8 *isleaf, u32 m, const TreeRoot *root, double inv_theta,
-                 WalkRec32 *walk32, WalkRec64 *walk64, float4 *cells, const u32 *m_dev = nullptr,
-                 const u32 *abort = nullptr, const u16 *sys = nullptr) {
+    k_pack_walk(const double2 *geom, const double2 *mom, const double *delta, const u32 *nbegin,
+                const u32 *nend, const u32 *skip, const u8 *isleaf, u32 m, const TreeRoot *root,
+                double inv_theta, WalkRec32 *walk32, WalkRec64 *walk64,
+                const u32 *m_dev = nullptr, const u32 *abort = nullptr,
+                const u16 *sys = nullptr) {
   const u32 p = blockIdx.x * kT + threadIdx.x;
   if (aborted(abort) || p >= bounded(m, m_dev)) return;
   if (sys) root += sys[nbegin[p]];  // a forest: relative to the node's system's root
@@ -1400,6 +1432,18 @@ __global__ void __launch_bounds__(kT)
                           fmaxf(fabsf(f.my), fabsf(f.mz)));
   f.bound = (mag + f.slack) * (1.0f + 1.0f / (1 << 20));
   walk32[p] = f;
+}
+
+// FP32 cell of every node, after the quadrupole pass (group_lists.cpp:52-58).
+__global__ void __launch_bounds__(kT)
+    k_pack_cells(const double2 *mom, const double2 *quad, const u32 *nbegin, u32 m,
+                 const TreeRoot *root, float4 *cells, const u32 *m_dev = nullptr,
+                 const u32 *abort = nullptr, const u16 *sys = nullptr) {
+  const u32 p = blockIdx.x * kT + threadIdx.x;
+  if (aborted(abort) || p >= bounded(m, m_dev)) return;
+  if (sys) root += sys[nbegin[p]];
+  const Dbl4 c = load_pair(mom, p);
+  const double ox = root->center[0], oy = root->center[1], oz = root->center[2];
   const double2 qa = quad[3 * p], qb = quad[3 * p + 1], qc = quad[3 * p + 2];
   cells[3 * p] = make_float4(static_cast<float>(c.x - ox), static_cast<float>(c.y - oy),
                              static_cast<float>(c.z - oz), static_cast<float>(c.w));
@@ -1465,23 +1509,43 @@ void pack_bodies_bbox(Workspace &ws, const double *pos, const double *mass, u64 
   GTC_LAUNCH_CHECK();
 }
 
+void ensure_side(Workspace &ws) {
+  if (ws.side) return;
+  GTC_CUDA(cudaStreamCreateWithFlags(&ws.side, cudaStreamNonBlocking));
+  GTC_CUDA(cudaEventCreateWithFlags(&ws.side_fork, cudaEventDisableTiming));
+  GTC_CUDA(cudaEventCreateWithFlags(&ws.side_done, cudaEventDisableTiming));
+  GTC_CUDA(cudaEventCreateWithFlags(&ws.side_walk, cudaEventDisableTiming));
+}
+
 cudaStream_t fork_side(Workspace &ws, cudaStream_t s) {
-  if (!ws.side) {
-    GTC_CUDA(cudaStreamCreateWithFlags(&ws.side, cudaStreamNonBlocking));
-    GTC_CUDA(cudaEventCreateWithFlags(&ws.side_fork, cudaEventDisableTiming));
-    GTC_CUDA(cudaEventCreateWithFlags(&ws.side_done, cudaEventDisableTiming));
-  }
+  ensure_side(ws);
   GTC_CUDA(cudaEventRecord(ws.side_fork, s));
   GTC_CUDA(cudaStreamWaitEvent(ws.side, ws.side_fork, 0));
   ws.side_pending = true;
+  ws.walk_pending = false;
   return ws.side;
 }
 
 void join_side(Workspace &ws, cudaStream_t s) {
+  ws.walk_pending = false;
   if (!ws.side_pending) return;
   ws.side_pending = false;
   if (cudaEventRecord(ws.side_done, ws.side) == cudaSuccess)
     cudaStreamWaitEvent(s, ws.side_done, 0);
+}
+
+void mark_walk_ready(Workspace &ws, cudaStream_t side) {
+  GTC_CUDA(cudaEventRecord(ws.side_walk, side));
+  ws.walk_pending = true;
+}
+
+void join_walk(Workspace &ws, cudaStream_t s) {
+  if (!ws.walk_pending) {
+    join_side(ws, s);  // no walk mark: all of the side stream's work
+    return;
+  }
+  ws.walk_pending = false;
+  GTC_CUDA(cudaStreamWaitEvent(s, ws.side_walk, 0));
 }
 
 namespace {
@@ -1798,20 +1862,34 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
   // small depths leave most SMs idle, and the group choice needs none of
   // it. Bucket sizes are read on the device: leaves (at most m), then each
   // depth's inner nodes from the deepest possible one up.
+  // The centres of mass first and the walk records from them (the walk
+  // waits for these only), then the quadrupoles and the cells beside the
+  // walk.
   cudaStream_t ms = fork_side(ws, s);
   ws.stage(Workspace::kStMom0, ms);
-  k_leaf_moments<<<mb, kT, 0, ms>>>(ma, bucket, meta);
+  k_leaf_moments<false><<<mb, kT, 0, ms>>>(ma, bucket, meta);
   GTC_LAUNCH_CHECK();
   for (int d = static_cast<int>(host->depth) - 1; d >= 0; --d) {
-    k_node_moments<<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, d * kSizeClasses,
-                                                 kSizeClasses, &sc->abort);
+    k_node_moments<false><<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, d * kSizeClasses,
+                                                        kSizeClasses, &sc->abort);
     GTC_LAUNCH_CHECK();
   }
-  k_pack_nodes<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
-                                  ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                                  ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
-                                  1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
-                                  ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), nullptr,
+  k_pack_walk<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(),
+                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root, 1.0 / sp.theta,
+                                 ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), nullptr,
+                                 nullptr, fv.sys);
+  GTC_LAUNCH_CHECK();
+  mark_walk_ready(ws, ms);
+  k_leaf_moments<true><<<mb, kT, 0, ms>>>(ma, bucket, meta);
+  GTC_LAUNCH_CHECK();
+  for (int d = static_cast<int>(host->depth) - 1; d >= 0; --d) {
+    k_node_moments<true><<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, d * kSizeClasses,
+                                                       kSizeClasses, &sc->abort);
+    GTC_LAUNCH_CHECK();
+  }
+  k_pack_cells<<<mb, kT, 0, ms>>>(ws.mom.as<double2>(), ws.quad.as<double2>(),
+                                  ws.nbegin.as<u32>(), m, root, ws.cells.as<float4>(), nullptr,
                                   nullptr, fv.sys);
   GTC_LAUNCH_CHECK();
   ws.stage(Workspace::kStMom1, ms);
@@ -1900,23 +1978,35 @@ void build_tree_graph(Workspace &ws, const double *pos, const double *mass, u64 
                   ws.kids.as<uint4>(), ws.tpos.as<double>(), ws.tmass.as<double>(),
                   ws.mom.as<double2>(),
                   ws.quad.as<double2>(), ws.delta.as<double>()};
-  int dev = 0, sms = 0;
-  GTC_CUDA(cudaGetDevice(&dev));
-  GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const u32 gb = std::min<u32>(mb, static_cast<u32>(std::max(1, 8 * sms)));
-  k_node_moments<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses, abort);
+  // the centres of mass and the walk records in line; the quadrupoles and
+  // the cells on the side stream, beside the group choice and the walk (the
+  // caller joins it before the evaluation)
+  k_node_moments<false><<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, kLeafBucket, kLeafClasses,
+                                                     abort);
   GTC_LAUNCH_CHECK();
   for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
-    k_node_moments<<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, d * kSizeClasses, kSizeClasses,
-                                                abort);
+    k_node_moments<false><<<kMomentWarps, 32, 0, s>>>(ma, bucket, meta, d * kSizeClasses,
+                                                       kSizeClasses, abort);
     GTC_LAUNCH_CHECK();
   }
-  k_pack_nodes<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(), ws.quad.as<double2>(),
-                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, root,
-                                 1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
-                                 ws.walk64.as<WalkRec64>(), ws.cells.as<float4>(), m_dev, abort,
-                                 fv.sys);
+  k_pack_walk<<<mb, kT, 0, s>>>(ws.geom.as<double2>(), ws.mom.as<double2>(),
+                                ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                ws.skip.as<u32>(), ws.isleaf.as<u8>(), mcap, root, 1.0 / sp.theta,
+                                ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), m_dev,
+                                abort, fv.sys);
+  GTC_LAUNCH_CHECK();
+  cudaStream_t ms = fork_side(ws, s);
+  k_node_moments<true><<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, kLeafBucket, kLeafClasses,
+                                                     abort);
+  GTC_LAUNCH_CHECK();
+  for (int d = std::min(caps.depth, kMaxDepth); d >= 0; --d) {
+    k_node_moments<true><<<kMomentWarps, 32, 0, ms>>>(ma, bucket, meta, d * kSizeClasses,
+                                                      kSizeClasses, abort);
+    GTC_LAUNCH_CHECK();
+  }
+  k_pack_cells<<<mb, kT, 0, ms>>>(ws.mom.as<double2>(), ws.quad.as<double2>(),
+                                  ws.nbegin.as<u32>(), mcap, root, ws.cells.as<float4>(), m_dev,
+                                  abort, fv.sys);
   GTC_LAUNCH_CHECK();
   pack_bodies_tree(ws, n32, root, abort, s);
 }
