@@ -211,18 +211,15 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   if (n > 0) {
     ws.out.ensure(n * sizeof(float4));
     ctx->counter.ensure(sizeof(u32));
+    if (ctx->have_model) ctx->prev_amag.ensure(n * sizeof(float));  // |a| for the next learned solve
+    const gtc::EvalOut eo{ws.out.as<float4>(), ws.idx.as<u32>(), acc, pot,
+                          ctx->have_model ? ctx->prev_amag.as<float>() : nullptr};
     GTC_CUDA(cudaEventRecord(ctx->ev[4], s));
     gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
                         ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
                         static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
-                        sp.quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+                        sp.quadrupole != 0, eo, ctx->counter.as<u32>(), s);
     GTC_CUDA(cudaEventRecord(ctx->ev[5], s));
-    gtc::scatter_results(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, s);
-    if (ctx->have_model) {  // |a| for the next learned solve
-      ctx->prev_amag.ensure(n * sizeof(float));
-      gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
-                               ctx->prev_amag.as<float>(), s);
-    }
   }
   GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
   GTC_CUDA(cudaMemcpyAsync(ctx->host_sc, ws.scalars.ptr, sizeof(gtc::Scalars),
@@ -374,16 +371,14 @@ struct GraphStep {
     gtc::join_side(ws, s);  // the cells
     mark(2, s);
     mark(4, s);
+    const gtc::EvalOut eo{ws.out.as<float4>(), ws.idx.as<u32>(), acc, pot,
+                          ctx->have_model ? ctx->prev_amag.as<float>() : nullptr};
     gtc::evaluate_lists_graph(ws.bodies.as<float4>(), ws.cells.as<float4>(),
                               ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
                               ws.groups.as<uint4>(), n, sc, static_cast<float>(sp.G),
-                              static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0,
-                              ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+                              static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0, eo,
+                              ctx->counter.as<u32>(), s);
     mark(5, s);
-    gtc::scatter_results_graph(ws.out.as<float4>(), ws.idx.as<u32>(), n, acc, pot, sc, s);
-    if (ctx->have_model)
-      gtc::learned_record_amag(ws.out.as<float4>(), ws.idx.as<u32>(), n,
-                               ctx->prev_amag.as<float>(), s);
     gtc::kick(vel, acc, n, h, s, &sc->abort);
     mark(3, s);
   }
@@ -709,7 +704,7 @@ struct ForestGraph {
                               ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
                               ws.groups.as<uint4>(), f->n, sc, static_cast<float>(f->sp.G),
                               static_cast<float>(f->sp.eps * f->sp.eps), f->sp.quadrupole != 0,
-                              ws.out.as<float4>(), f->counter.as<u32>(), s);
+                              gtc::EvalOut{ws.out.as<float4>()}, f->counter.as<u32>(), s);
     f->scatter(1, h, &sc->abort, s);
     GTC_CUDA(cudaMemcpyAsync(f->host_sc, sc, sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
   }
@@ -1027,7 +1022,8 @@ gtc_status gtc_tree(gtc_context *ctx, const gtc_float4 *bodies, const gtc_cell *
     GTC_CUDA(cudaEventRecord(ctx->ev[2], s));
     gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
                         ws.body_list.as<u32>(), ws.groups.as<uint4>(), ng, p->G, p->eps2,
-                        p->quadrupole != 0, ws.out.as<float4>(), ctx->counter.as<u32>(), s);
+                        p->quadrupole != 0, gtc::EvalOut{ws.out.as<float4>()},
+                        ctx->counter.as<u32>(), s);
     GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
     GTC_CUDA(cudaMemcpyAsync(out, ws.out.ptr, n * 16, cudaMemcpyDeviceToHost, s));
     GTC_CUDA(cudaStreamSynchronize(s));

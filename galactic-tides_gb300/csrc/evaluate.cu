@@ -67,6 +67,19 @@ __device__ __forceinline__ void add_cell(float px, float py, float pz, const Sta
   }
 }
 
+// Target i's results (tree order) into eo: the FP32 record, and the caller's
+// FP64 arrays (FP32 -> FP64 exactly) and |a| when eo asks for them.
+__device__ __forceinline__ void write_target(const EvalOut &eo, u32 i, float4 a) {
+  eo.out[i] = a;
+  if (!eo.acc) return;
+  const u64 j = eo.order[i];
+  eo.acc[3 * j] = a.x;
+  eo.acc[3 * j + 1] = a.y;
+  eo.acc[3 * j + 2] = a.z;
+  eo.pot[j] = a.w;
+  if (eo.amag) eo.amag[j] = sqrtf(__fmaf_rn(a.x, a.x, __fmaf_rn(a.y, a.y, __fmul_rn(a.z, a.z))));
+}
+
 // kSoft: eps2 > 0. Every target appears exactly once in its own group's body
 // list (each body is covered once and no accepted cell holds a target), and
 // with softening its self term adds exactly zero acceleration (d = 0) and a
@@ -77,9 +90,8 @@ template <bool kQuad, bool kSoft>
 __global__ void __launch_bounds__(kT)
     k_eval(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
            const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
-           const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
-           float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev = nullptr,
-           const u32 *abort = nullptr) {
+           const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2, EvalOut eo,
+           u32 *next_group, const u32 *ng_dev = nullptr, const u32 *abort = nullptr) {
   // Staged entries, per warp: slice k's W entries start at float4 k (3W + 1)
   // (cells) and k (W + 1) (bodies); the 16-byte gap puts the slices on
   // different shared-memory banks, so their broadcast loads do not conflict.
@@ -199,7 +211,7 @@ __global__ void __launch_bounds__(kT)
       }
     }
     if (kSoft) pot += G * bi.w * rsqrtf(eps2);  // the self term, added once above
-    if (slice == 0 && t < T) out[i] = make_float4(ax, ay, az, pot);
+    if (slice == 0 && t < T) write_target(eo, i, make_float4(ax, ay, az, pot));
   }
 }
 
@@ -257,8 +269,7 @@ __global__ void __launch_bounds__(kT)
     k_eval_pairs(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
                  const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
                  const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
-                 float4 *__restrict__ out, u32 *next_group, const u32 *ng_dev,
-                 const u32 *abort) {
+                 EvalOut eo, u32 *next_group, const u32 *ng_dev, const u32 *abort) {
   // per warp, staged pairs: each lane stages two entries per round, so area
   // a (2W entries) starts at float4 a * (W * per-pair + 1) (at most 4 areas:
   // 164 and 68 float4); the 16-byte gap puts the areas on different
@@ -439,29 +450,15 @@ __global__ void __launch_bounds__(kT)
       const u32 i = q0.x + static_cast<u32>(lane);
       float4 acc = sacc[warp][lane];
       acc.w += G * bodies[i].w * rsqrtf(eps2);  // the self term (softened), taken back once
-      out[i] = acc;
+      write_target(eo, i, acc);
     }
   }
-}
-
-// Tree order -> caller order, FP32 -> FP64 (gravity_backends.cpp:132-136).
-__global__ void __launch_bounds__(256)
-    k_scatter(const float4 *out, const u32 *order, u32 n, double *acc, double *pot,
-              const u32 *abort = nullptr) {
-  const u32 k = blockIdx.x * 256 + threadIdx.x;
-  if (k >= n || (abort && *abort)) return;
-  const float4 o = out[k];
-  const u64 i = order[k];
-  acc[3 * i] = o.x;
-  acc[3 * i + 1] = o.y;
-  acc[3 * i + 2] = o.z;
-  pot[i] = o.w;
 }
 
 template <bool kQuad, bool kSoft>
 void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                  const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                 float4 *out, u32 *counter, cudaStream_t s, const Scalars *sc = nullptr) {
+                 const EvalOut &eo, u32 *counter, cudaStream_t s, const Scalars *sc = nullptr) {
   int dev = 0, sms = 0, per_sm = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -472,12 +469,12 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
         &per_sm, k_eval_pairs<kEvalPairsPerIter>, kT, 0));
     const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
     k_eval_pairs<kEvalPairsPerIter><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
-                                     static_cast<u32>(n_groups), G, eps2, out, counter,
+                                     static_cast<u32>(n_groups), G, eps2, eo, counter,
                                      sc ? &sc->n_groups : nullptr, sc ? &sc->abort : nullptr);
   } else {
     const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
     k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
-                                             static_cast<u32>(n_groups), G, eps2, out, counter,
+                                             static_cast<u32>(n_groups), G, eps2, eo, counter,
                                              sc ? &sc->n_groups : nullptr,
                                              sc ? &sc->abort : nullptr);
   }
@@ -488,49 +485,35 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
 
 void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                     const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                    bool quadrupole, float4 *out, u32 *counter, cudaStream_t s) {
+                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s) {
   if (n_groups == 0) return;
   GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
   const bool soft = eps2 > 0.0f;
   if (quadrupole && soft)
-    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
   else if (quadrupole)
-    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
   else if (soft)
-    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
   else
-    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, out, counter, s);
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
 }
 
 void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                           const u32 *body_list, const uint4 *groups, u64 max_groups,
-                          const Scalars *sc, float G, float eps2, bool quadrupole, float4 *out,
-                          u32 *counter, cudaStream_t s) {
+                          const Scalars *sc, float G, float eps2, bool quadrupole,
+                          const EvalOut &eo, u32 *counter, cudaStream_t s) {
   if (max_groups == 0) return;
   GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
   const bool soft = eps2 > 0.0f;
   if (quadrupole && soft)
-    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
   else if (quadrupole)
-    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
   else if (soft)
-    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
   else
-    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, out, counter, s, sc);
-}
-
-void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
-                           const Scalars *sc, cudaStream_t s) {
-  if (n == 0) return;
-  k_scatter<<<ceil_div(n, 256), 256, 0, s>>>(out, order, static_cast<u32>(n), acc, pot, &sc->abort);
-  GTC_LAUNCH_CHECK();
-}
-
-void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
-                     cudaStream_t s) {
-  if (n == 0) return;
-  k_scatter<<<ceil_div(n, 256), 256, 0, s>>>(out, order, static_cast<u32>(n), acc, pot);
-  GTC_LAUNCH_CHECK();
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
 }
 
 }  // namespace gtc

@@ -183,9 +183,6 @@ void learned_group_tolerances(Workspace &ws, const LearnedWalk &lw, u32 ng, cuda
 // the interaction counters of the ng groups (inside build_lists).
 void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *host,
                          cudaStream_t s);
-// |a| per body, caller order, from the evaluator's tree-order output.
-void learned_record_amag(const float4 *out, const u32 *order, u64 n, float *amag,
-                         cudaStream_t s);
 // The tensor-core layout of an FP32 model (kModelFloats floats, device).
 void learned_prepare_net(const float *model, LearnedNet *net, cudaStream_t s);
 // The walk's inference on given raw features: predicted log2 error per row.

@@ -243,14 +243,6 @@ __global__ void __launch_bounds__(kT)
   gtol[g] = make_float2(group_feature(hmax, fs), tau);
 }
 
-__global__ void __launch_bounds__(kT)
-    k_record_amag(const float4 *out, const u32 *order, u64 n, float *amag) {
-  const u64 t = static_cast<u64>(blockIdx.x) * kT + threadIdx.x;
-  if (t >= n) return;
-  const float4 o = out[t];
-  amag[order[t]] = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-}
-
 constexpr int kMaxRounds = kMaxDepth + 4;
 
 // Round 0 runs as kParts threads per group, each walking a range of the
@@ -1221,13 +1213,6 @@ void learned_build_lists(Workspace &ws, const LearnedWalk &lw, u32 ng, Scalars *
   ls.slot_pend = learned_slot(host->max_pend);
   ls.rounds = rounds;
   ls.row_cap = learned_slot(host->max_rows);
-}
-
-void learned_record_amag(const float4 *out, const u32 *order, u64 n, float *amag,
-                         cudaStream_t s) {
-  if (n == 0) return;
-  k_record_amag<<<ceil_div(n, kT), kT, 0, s>>>(out, order, n, amag);
-  GTC_LAUNCH_CHECK();
 }
 
 }  // namespace gtc

@@ -337,14 +337,23 @@ struct LearnedWalk;
 void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars *host,
                  const LearnedWalk *lw = nullptr);
 
-// Stage 3: warp-per-group evaluation of the lists into ws.out (tree order),
-// then the scatter into acc/pot in caller order (FP64).
+// Where an evaluation writes each target's acceleration and potential:
+// always out (FP32, tree order); with acc set also acc and pot (FP64, caller
+// order through `order`: the scatter of gravity_backends.cpp:132-136, done
+// by the evaluation's own threads), and with amag set |a| per body (caller
+// order) for the next learned solve.
+struct EvalOut {
+  float4 *out = nullptr;
+  const u32 *order = nullptr;
+  double *acc = nullptr, *pot = nullptr;
+  float *amag = nullptr;
+};
+
+// Stage 3: warp-per-group evaluation of the lists into eo.
 // `counter` is one device word the kernel's work queue uses.
 void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                     const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                    bool quadrupole, float4 *out, u32 *counter, cudaStream_t s);
-void scatter_results(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
-                     cudaStream_t s);
+                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s);
 
 // Capacities of a solve replayed from a CUDA graph: the sizes of the
 // buffers the graph was captured with. A replay whose tree, depth or lists
@@ -376,10 +385,8 @@ void write_root_task(Workspace &ws, cudaStream_t s);
 // after an abort.
 void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                           const u32 *body_list, const uint4 *groups, u64 max_groups,
-                          const Scalars *sc, float G, float eps2, bool quadrupole, float4 *out,
-                          u32 *counter, cudaStream_t s);
-void scatter_results_graph(const float4 *out, const u32 *order, u64 n, double *acc, double *pot,
-                           const Scalars *sc, cudaStream_t s);
+                          const Scalars *sc, float G, float eps2, bool quadrupole,
+                          const EvalOut &eo, u32 *counter, cudaStream_t s);
 
 // Direct summation kernels.
 // FP32 estimates of every node's moments (GTCell layout in cells32, delta in
