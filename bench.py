@@ -234,7 +234,11 @@ def run_reference(args):
 KEYS_B_BODY = 24 + 24 + 13          # box: pos; keys: pos in, key + index + tiny flag out
 SORT_B_BODY_PASS = 24               # key and index in and out per 8-bit pass
 TOPO_B_BODY, TOPO_B_NODE = 118, 88  # levels, node count + scan, nodes, leaf and tree order
-MOM_B_BODY, MOM_B_NODE = 32, 417    # leaf bodies in; moments out, node records packed
+# FP64 moments in two passes: bodies in for each; per node the centres of mass
+# pass reads geometry, children and ranges and writes the centre of mass,
+# delta and both walk records; the quadrupole pass reads centres of mass,
+# children and ranges and writes the quadrupole and the FP32 cell
+MOM_B_BODY, MOM_COM_B_NODE, MOM_QUAD_B_NODE = 32, 230, 169
 PACK_B_BODY = 48                    # FP32 bodies from the tree-order copies
 
 
@@ -275,7 +279,8 @@ def measure_stages(ctx, step, flush, stream, n, hbm_gbs, reps=5):
     b_keys = KEYS_B_BODY * n
     b_sort = SORT_B_BODY_PASS * passes * n
     b_topo = TOPO_B_BODY * n + TOPO_B_NODE * m
-    b_mom = MOM_B_BODY * n + MOM_B_NODE * m
+    b_mom = MOM_B_BODY * n + MOM_COM_B_NODE * m
+    b_quad = MOM_B_BODY * n + MOM_QUAD_B_NODE * m
     b_build = b_keys + b_sort + b_topo + b_mom + PACK_B_BODY * n
     # the walk: node records read once, group boxes and ranges read, lists and
     # group records written; `requested` counts every record test's 48 B
@@ -293,7 +298,9 @@ def measure_stages(ctx, step, flush, stream, n, hbm_gbs, reps=5):
                      f"{reps} solves after the timed steps, L2 flushed before each"),
             "hbm_peak_gbs": hbm_gbs, "sort_passes": passes,
             "keys": rate(b_keys, tm["keys_ms"]), "radix_sort": rate(b_sort, tm["sort_ms"]),
-            "topology": rate(b_topo, tm["topology_ms"]), "moments": rate(b_mom, tm["moments_ms"]),
+            "topology": rate(b_topo, tm["topology_ms"]),
+            "moments_com": rate(b_mom, tm["moments_ms"]),
+            "moments_quad_beside_walk": rate(b_quad, tm["quad_ms"]),
             "tree_build": rate(b_build, tm["build_ms"]), "walk": rate(b_walk, tm["walk_ms"]),
             "walk_record_bytes_requested": 48 * st["walk_nodes"],
             "walk_requested_gbs": (round(48 * st["walk_nodes"] / (tm["walk_ms"] * 1e-3) / 1e9, 1)

@@ -1686,11 +1686,12 @@ gtc_status gtc_get_stage_times(gtc_context *ctx, gtc_stage_times *out) {
     };
     using W = gtc::Workspace;
     *out = gtc_stage_times{};
-    out->build_ms = span(W::kStBuild, W::kStMom1);
+    out->build_ms = span(W::kStBuild, W::kStMomW);
     out->keys_ms = span(W::kStBuild, W::kStSort0);
     out->sort_ms = span(W::kStSort0, W::kStSort1);
     out->topology_ms = span(W::kStSort1, W::kStTopo);
-    out->moments_ms = span(W::kStMom0, W::kStMom1);
+    out->moments_ms = span(W::kStMom0, W::kStMomW);
+    out->quad_ms = span(W::kStMomW, W::kStMom1);
     out->walk_ms = span(W::kStWalk0, W::kStWalk1);
     out->sort_passes = static_cast<uint32_t>(ws.sort_passes);
   });

@@ -172,8 +172,8 @@ struct Workspace {
   // Optional stage events (context option "stage_events"): CUDA events at
   // the boundaries of the eager build's and walk's stages, for per-stage
   // device times. Off by default.
-  enum Stage { kStBuild, kStSort0, kStSort1, kStTopo, kStMom0, kStMom1, kStWalk0, kStWalk1,
-               kStages };
+  enum Stage { kStBuild, kStSort0, kStSort1, kStTopo, kStMom0, kStMomW, kStMom1, kStWalk0,
+               kStWalk1, kStages };
   bool stage_on = false;
   cudaEvent_t stage_ev[kStages] = {};
   bool stage_hit[kStages] = {};

@@ -1535,6 +1535,7 @@ void join_side(Workspace &ws, cudaStream_t s) {
 }
 
 void mark_walk_ready(Workspace &ws, cudaStream_t side) {
+  ws.stage(Workspace::kStMomW, side);
   GTC_CUDA(cudaEventRecord(ws.side_walk, side));
   ws.walk_pending = true;
 }

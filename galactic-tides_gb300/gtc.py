@@ -69,7 +69,8 @@ class Stats(C.Structure):
 class StageTimes(C.Structure):
     _fields_ = [("build_ms", C.c_double), ("keys_ms", C.c_double), ("sort_ms", C.c_double),
                 ("topology_ms", C.c_double), ("moments_ms", C.c_double),
-                ("walk_ms", C.c_double), ("sort_passes", C.c_uint32), ("reserved", C.c_uint32)]
+                ("walk_ms", C.c_double), ("sort_passes", C.c_uint32), ("reserved", C.c_uint32),
+                ("quad_ms", C.c_double)]
 
 
 NODE_DTYPE = np.dtype([

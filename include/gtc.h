@@ -235,14 +235,16 @@ gtc_status gtc_get_stats(const gtc_context *ctx, gtc_stats *out);
  * stage the call did not time). No reference counterpart: the reference's
  * Timings (gravity_backends.h:54-58) stop at tree / lists / evaluate. */
 typedef struct gtc_stage_times {
-  double build_ms;     /* tree build start to the end of the moments (side stream) */
+  double build_ms;     /* tree build start to the walk records (what the walk waits for) */
   double keys_ms;      /* bounding box, split table and keys */
   double sort_ms;      /* the radix sort of the first key word */
   double topology_ms;  /* levels, node count, nodes, children, leaf and tree order */
-  double moments_ms;   /* FP64 moments and node records (beside the group choice) */
+  double moments_ms;   /* FP64 centres of mass and the walk records (side stream, beside
+                          the group choice) */
   double walk_ms;      /* the grouped walk, after the group choice */
   uint32_t sort_passes; /* 8-bit passes of that sort */
   uint32_t reserved;
+  double quad_ms;      /* FP64 quadrupoles and the FP32 cells (side stream, beside the walk) */
 } gtc_stage_times;
 gtc_status gtc_get_stage_times(gtc_context *ctx, gtc_stage_times *out);
 
