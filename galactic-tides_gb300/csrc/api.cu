@@ -158,6 +158,19 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// Makes `main` wait for the learned stream's work when it leaves scope, on
+// every exit of a solve (the walk itself waits for it before it starts).
+struct LearnedJoin {
+  gtc_context *ctx;
+  cudaStream_t main;
+  bool active;
+  ~LearnedJoin() {
+    if (!active) return;
+    if (cudaEventRecord(ctx->ldone, ctx->lstream) == cudaSuccess)
+      cudaStreamWaitEvent(main, ctx->ldone, 0);
+  }
+};
+
 // The grouped solver on device arrays (caller order in and out).
 void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
                  const gtc::SolverParams &sp, double *acc, double *pot) {
@@ -182,13 +195,27 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   const gtc::SideJoin side_join{ws, s};
   gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
   GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
+  LearnedJoin learned_join{ctx, s, false};
   if (learned) {
-    // the walk's inputs from FP32 moment estimates on the main stream: the
-    // walk runs while the side stream accumulates the FP64 moments the
-    // evaluation reads
+    // the walk's inputs from FP32 moment estimates, on their own stream
+    // beside the group choice (the walk waits for them); the walk then runs
+    // while the side stream accumulates the FP64 moments the evaluation reads
+    if (!ctx->lstream) {
+      int least = 0, greatest = 0;
+      GTC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      GTC_CUDA(cudaStreamCreateWithPriority(&ctx->lstream, cudaStreamNonBlocking, greatest));
+      GTC_CUDA(cudaEventCreateWithFlags(&ctx->lfork, cudaEventDisableTiming));
+      GTC_CUDA(cudaEventCreateWithFlags(&ctx->ldone, cudaEventDisableTiming));
+    }
+    GTC_CUDA(cudaEventRecord(ctx->lfork, s));
+    GTC_CUDA(cudaStreamWaitEvent(ctx->lstream, ctx->lfork, 0));
+    learned_join.active = true;
     gtc::learned_walk_inputs(ws, ctx->lscratch, ctx->cfeat,
-                             static_cast<float>(1.0 / ctx->guard_theta), ctx->model_ymean, s);
+                             static_cast<float>(1.0 / ctx->guard_theta), ctx->model_ymean,
+                             ctx->lstream);
+    GTC_CUDA(cudaEventRecord(ctx->ldone, ctx->lstream));
     gtc::LearnedWalk lw;
+    lw.inputs_ready = ctx->ldone;
     lw.net = ctx->net.as<gtc::LearnedNet>();
     lw.cfeat = ctx->cfeat.as<gtc::CellFeat>();
     lw.gtol = &ctx->gtol;
@@ -932,6 +959,12 @@ void gtc_destroy(gtc_context *ctx) {
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->host_sc) cudaFreeHost(ctx->host_sc);
+  if (ctx->lstream) {
+    cudaStreamSynchronize(ctx->lstream);
+    cudaStreamDestroy(ctx->lstream);
+    cudaEventDestroy(ctx->lfork);
+    cudaEventDestroy(ctx->ldone);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -31,6 +31,10 @@ struct gtc_context {
   gtc::LearnedScratch lscratch;     // the learned walk's rounds
   gtc::DeviceBuffer prev_amag;      // |a| per body (caller order) of the last solve
   gtc::u64 prev_n = 0;              // bodies in prev_amag (0: none)
+  // the learned walk's inputs (FP32 moment estimates, node features and
+  // records) run on their own stream, beside the group choice on `stream`
+  cudaStream_t lstream = nullptr;
+  cudaEvent_t lfork = nullptr, ldone = nullptr;
   double guard_theta = 1.5;         // options of the learned walk
   double band_override = -1.0;      // < 0: the model's band
   gtc::u32 walk_budget = gtc::kLearnedWalkBudget;  // learned walk: nodes a thread tests before

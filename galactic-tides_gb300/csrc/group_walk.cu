@@ -1064,6 +1064,7 @@ void build_lists(Workspace &ws, const SolverParams &sp, cudaStream_t s, Scalars 
     // the learned walk decides from FP32 moment estimates: the FP64 moments
     // go on on the side stream, and are joined for the evaluation after it
     ws.stage(Workspace::kStWalk0, s);
+    if (lw->inputs_ready) GTC_CUDA(cudaStreamWaitEvent(s, lw->inputs_ready, 0));
     learned_group_tolerances(ws, *lw, ng, s);
     learned_build_lists(ws, *lw, ng, host, s);
     ws.stage(Workspace::kStWalk1, s);

@@ -163,6 +163,9 @@ struct LearnedWalk {
   // each round by warps, one per group (1), by threads per part (0), or by
   // warps below Workspace::kWarpWalkGroups groups (-1), as the plain walk
   int warps_mode = -1;
+  // recorded after the walk's inputs (learned_walk_inputs) on another
+  // stream: the walk's stream waits for it first (null: same stream)
+  cudaEvent_t inputs_ready = nullptr;
 };
 
 // Per-node features (after build_tree and the FP64 moments: the training
