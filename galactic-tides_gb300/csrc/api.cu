@@ -193,7 +193,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
   for (bool &h : ws.stage_hit) h = false;
   GTC_CUDA(cudaEventRecord(ctx->ev[0], s));
   const gtc::SideJoin side_join{ws, s};
-  gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc);
+  gtc::build_tree(ws, pos, mass, n, sp, s, ctx->host_sc, !learned);
   GTC_CUDA(cudaEventRecord(ctx->ev[1], s));
   LearnedJoin learned_join{ctx, s, false};
   if (learned) {

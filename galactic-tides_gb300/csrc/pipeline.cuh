@@ -326,8 +326,10 @@ struct SideJoin {
   ~SideJoin() { join_side(ws, s); }
 };
 
+// walk_records: pack the theta walk's node records (the learned walk has its
+// own and skips them).
 void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
-                const SolverParams &sp, cudaStream_t s, Scalars *host);
+                const SolverParams &sp, cudaStream_t s, Scalars *host, bool walk_records = true);
 
 struct LearnedWalk;
 

@@ -1673,7 +1673,7 @@ void pack_bodies_tree(Workspace &ws, u32 n, const TreeRoot *root, const u32 *abo
 }  // namespace
 
 void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
-                const SolverParams &sp, cudaStream_t s, Scalars *host) {
+                const SolverParams &sp, cudaStream_t s, Scalars *host, bool walk_records) {
   ws.n = n;
   ws.n_nodes = 0;
   ws.key_words = 1;
@@ -1875,12 +1875,14 @@ void build_tree(Workspace &ws, const double *pos, const double *mass, u64 n,
                                                         kSizeClasses, &sc->abort);
     GTC_LAUNCH_CHECK();
   }
-  k_pack_walk<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(),
-                                 ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
-                                 ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root, 1.0 / sp.theta,
-                                 ws.walk32.as<WalkRec32>(), ws.walk64.as<WalkRec64>(), nullptr,
-                                 nullptr, fv.sys);
-  GTC_LAUNCH_CHECK();
+  if (walk_records) {
+    k_pack_walk<<<mb, kT, 0, ms>>>(ws.geom.as<double2>(), ws.mom.as<double2>(),
+                                   ws.delta.as<double>(), ws.nbegin.as<u32>(), ws.nend.as<u32>(),
+                                   ws.skip.as<u32>(), ws.isleaf.as<u8>(), m, root,
+                                   1.0 / sp.theta, ws.walk32.as<WalkRec32>(),
+                                   ws.walk64.as<WalkRec64>(), nullptr, nullptr, fv.sys);
+    GTC_LAUNCH_CHECK();
+  }
   mark_walk_ready(ws, ms);
   k_leaf_moments<true><<<mb, kT, 0, ms>>>(ma, bucket, meta);
   GTC_LAUNCH_CHECK();
