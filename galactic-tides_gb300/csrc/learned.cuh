@@ -34,7 +34,7 @@ constexpr float kPriorBase = 3.3773f;       // log2(2 * 3^1.5)
 // Node records one thread of the learned walk tests before the rest of its
 // walk goes to a warp: in round 0, and in later rounds (where each deferred
 // pair costs a few dependent loads more than a node).
-constexpr u32 kLearnedWalkBudget = 640, kLearnedPairBudget = 32;
+constexpr u32 kLearnedWalkBudget = 576, kLearnedPairBudget = 48;
 
 // Raw features of a (group, cell) pair, all from FP32 quantities so that
 // training and inference see the same numbers:

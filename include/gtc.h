@@ -379,12 +379,12 @@ gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double
  *                        (default): tests whose centred error prior lies
  *                        further than this from the tolerance are decided by
  *                        it; the rest go to the network (0: prior only).
- *   "learned_walk_budget" whole number >= 0 (default 640): in the learned
+ *   "learned_walk_budget" whole number >= 0 (default 576): in the learned
  *                        walk's first round a thread tests this many nodes
  *                        for its group, then a warp walks the rest 32 nodes
  *                        at a time (0: the thread walks it all). The lists
  *                        hold the same entries; only their order depends on it.
- *   "learned_pair_budget" the same for the later rounds (default 32), which
+ *   "learned_pair_budget" the same for the later rounds (default 48), which
  *                        walk the subtrees of the pairs the network opened.
  *   "learned_read_every_round" 0 (default) or 1: the learned walk first runs
  *                        as many rounds as its last call needed, then reads
