@@ -245,7 +245,7 @@ void group_force(gtc_context *ctx, const double *pos, const double *mass, u64 n,
     gtc::evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
                         ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
                         static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
-                        sp.quadrupole != 0, eo, ctx->counter.as<u32>(), s);
+                        sp.quadrupole != 0, eo, ctx->counter.as<u32>(), s, ws.eval_shape);
     GTC_CUDA(cudaEventRecord(ctx->ev[5], s));
   }
   GTC_CUDA(cudaEventRecord(ctx->ev[3], s));
@@ -404,7 +404,7 @@ struct GraphStep {
                               ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
                               ws.groups.as<uint4>(), n, sc, static_cast<float>(sp.G),
                               static_cast<float>(sp.eps * sp.eps), sp.quadrupole != 0, eo,
-                              ctx->counter.as<u32>(), s);
+                              ctx->counter.as<u32>(), s, ws.eval_shape);
     mark(5, s);
     gtc::kick(vel, acc, n, h, s, &sc->abort);
     mark(3, s);
@@ -731,7 +731,8 @@ struct ForestGraph {
                               ws.cell_list.as<u32>(), ws.body_list.as<u32>(),
                               ws.groups.as<uint4>(), f->n, sc, static_cast<float>(f->sp.G),
                               static_cast<float>(f->sp.eps * f->sp.eps), f->sp.quadrupole != 0,
-                              gtc::EvalOut{ws.out.as<float4>()}, f->counter.as<u32>(), s);
+                              gtc::EvalOut{ws.out.as<float4>()}, f->counter.as<u32>(), s,
+                              ws.eval_shape);
     f->scatter(1, h, &sc->abort, s);
     GTC_CUDA(cudaMemcpyAsync(f->host_sc, sc, sizeof(gtc::Scalars), cudaMemcpyDeviceToHost, s));
   }
@@ -1240,6 +1241,13 @@ gtc_status gtc_set_option(gtc_context *ctx, const char *name, double value) {
         throw gtc::InvalidArgument("walk_warps must be -1, 0 or 1");
       ctx->ws.walk_mode = static_cast<int>(value);
       ctx->ws.slot_cells = 0;  // slots sized by the other walk would not fit: count first
+    } else if (key == "eval_pairs") {
+      if (value != 1 && value != 2) throw gtc::InvalidArgument("eval_pairs must be 1 or 2");
+      ctx->ws.eval_shape.pairs = static_cast<int>(value);
+    } else if (key == "eval_pass_cost") {
+      if (!(value >= 1 && value <= 256 && value == static_cast<double>(static_cast<int>(value))))
+        throw gtc::InvalidArgument("eval_pass_cost must be a whole number in 1..256");
+      ctx->ws.eval_shape.pass_cost = static_cast<gtc::u32>(value);
     } else if (key == "direct_targets") {
       if (value != 2 && value != 4) throw gtc::InvalidArgument("direct_targets must be 2 or 4");
       ctx->ws.direct_targets = static_cast<int>(value);
@@ -1699,6 +1707,42 @@ gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double
     }
     ws.direct_targets = pick;  // the context keeps the winner
     if (targets) *targets = pick;
+    if (best_ms) *best_ms = best_t;
+  });
+}
+
+gtc_status gtc_autotune_eval(gtc_context *ctx, const double *pos, const double *mass,
+                             uint64_t n, const gtc_gravity_params *gp, int *pairs,
+                             int *pass_cost, double *best_ms) {
+  return guarded(ctx, [&] {
+    if (n == 0 || !pos || !mass || !gp) throw gtc::InvalidArgument("pos, mass and gp are required");
+    const gtc::SolverParams sp = check_params(gp, true);
+    if (!sp.quadrupole || !(sp.eps > 0))
+      throw gtc::InvalidArgument("the evaluation's tile shape applies to softened quadrupoles");
+    gtc::Workspace &ws = ctx->ws;
+    ws.acc.ensure(n * 24);
+    ws.pot.ensure(n * 8);
+    // the lists first (and the one-pass walk's slots): a solve with the
+    // current shape, untimed
+    group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+    double best_t = 1e300;
+    gtc::EvalShape pick = ws.eval_shape;
+    for (int k : {2, 1})
+      for (gtc::u32 c : {24u, 8u, 16u, 32u, 48u}) {
+        ws.eval_shape = gtc::EvalShape{k, c};
+        double t = 0;
+        for (int rep = 0; rep < 3; ++rep) {
+          group_force(ctx, pos, mass, n, sp, ws.acc.as<double>(), ws.pot.as<double>());
+          if (rep > 0) t += ctx->stats.eval_kernel_ms;  // the first warms up
+        }
+        if (t / 2 < best_t) {
+          best_t = t / 2;
+          pick = ws.eval_shape;
+        }
+      }
+    ws.eval_shape = pick;  // the context keeps the winner
+    if (pairs) *pairs = pick.pairs;
+    if (pass_cost) *pass_cost = static_cast<int>(pick.pass_cost);
     if (best_ms) *best_ms = best_t;
   });
 }

@@ -239,27 +239,28 @@ constexpr float kFar = 1.0e30f;
 constexpr int kPairCellF4 = 5;   // float4 per staged cell pair
 constexpr int kPairBodyF4 = 2;   // float4 per staged body pair
 constexpr u32 kMaxSlices = 16;   // slices per group at most
-constexpr u32 kPassCost = 24;    // a pass's fixed cost, in staged entries per lane
-// Staged pairs a lane works per inner-loop iteration: the pairs' arithmetic
-// is independent up to the accumulation, which stays in list order, so
-// results do not depend on it; more pairs per iteration give each warp more
-// independent work to hide the rsqrt and shared-load latencies. A round's
-// 2W staged entries (2W a multiple of 4) are padded with far dummies, so an
-// iteration never reads past them.
-constexpr int kEvalPairsPerIter = 2;
+// The tile shape (EvalShape, a context option each and searched by
+// gtc_autotune_eval): the staged pairs a lane works per inner-loop
+// iteration (kU, 1 or 2) -- the pairs' arithmetic is independent up to the
+// accumulation, which stays in list order, so results do not depend on it;
+// more pairs per iteration give each warp more independent work to hide the
+// rsqrt and shared-load latencies; a round's 2W staged entries (2W a
+// multiple of 4) are padded with far dummies, so an iteration never reads
+// past them -- and a pass's fixed cost in staged entries per lane, which
+// sets how many slices a group's lists are cut into (below).
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
 __device__ __forceinline__ u32 even_up(u32 x) { return (x + 1u) & ~1u; }
 
 // Slices for a group of T targets with ec cells and eb bodies (warp-uniform):
-// the ns in 1..16 that minimises passes x (pair steps per pass + kPassCost).
-__device__ __forceinline__ u32 choose_slices(u32 T, u32 ec, u32 eb, int lane) {
+// the ns in 1..16 that minimises passes x (pair steps per pass + pass_cost).
+__device__ __forceinline__ u32 choose_slices(u32 T, u32 ec, u32 eb, int lane, u32 pass_cost) {
   if (T <= 10) return T == 0 ? 1u : min(4u, 32u / T);
   const u32 ns = static_cast<u32>(lane) % kMaxSlices + 1u;
   const u32 passes = (ns * T + 31u) / 32u;
   const u64 cost = static_cast<u64>(passes) *
-                   (even_up((ec + ns - 1) / ns) + even_up((eb + ns - 1) / ns) + kPassCost);
+                   (even_up((ec + ns - 1) / ns) + even_up((eb + ns - 1) / ns) + pass_cost);
   const u32 key = static_cast<u32>(cost < (1ull << 27) ? cost : (1ull << 27) - 1) << 4 | (ns - 1u);
   return (__reduce_min_sync(kFullMask, key) & 15u) + 1u;
 }
@@ -269,7 +270,8 @@ __global__ void __launch_bounds__(kT)
     k_eval_pairs(const float4 *__restrict__ bodies, const float4 *__restrict__ cells,
                  const u32 *__restrict__ cell_list, const u32 *__restrict__ body_list,
                  const uint4 *__restrict__ groups, u32 ngroups, float G, float eps2,
-                 EvalOut eo, u32 *next_group, const u32 *ng_dev, const u32 *abort) {
+                 EvalOut eo, u32 *next_group, const u32 *ng_dev, const u32 *abort,
+                 u32 pass_cost) {
   // per warp, staged pairs: each lane stages two entries per round, so area
   // a (2W entries) starts at float4 a * (W * per-pair + 1) (at most 4 areas:
   // 164 and 68 float4); the 16-byte gap puts the areas on different
@@ -292,7 +294,7 @@ __global__ void __launch_bounds__(kT)
     const u32 T = q0.y - q0.x;
     if (T == 0) continue;
     const u32 ec = q0.z, eb = q0.w;
-    const u32 ns = choose_slices(T, ec, eb, lane);
+    const u32 ns = choose_slices(T, ec, eb, lane, pass_cost);
     const u32 slots = ns * T;
     const u32 passes = (slots + 31u) / 32u;
     if (static_cast<u32>(lane) < T) sacc[warp][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -455,22 +457,37 @@ __global__ void __launch_bounds__(kT)
   }
 }
 
+template <int kU>
+void launch_pairs(const float4 *bodies, const float4 *cells, const u32 *cell_list,
+                  const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
+                  const EvalOut &eo, u32 *counter, cudaStream_t s, const Scalars *sc,
+                  u32 pass_cost, u64 want, int sms) {
+  int per_sm = 0;
+  GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_pairs<kU>, kT, 0));
+  const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
+  k_eval_pairs<kU><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
+                                       static_cast<u32>(n_groups), G, eps2, eo, counter,
+                                       sc ? &sc->n_groups : nullptr, sc ? &sc->abort : nullptr,
+                                       pass_cost);
+}
+
 template <bool kQuad, bool kSoft>
 void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                  const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                 const EvalOut &eo, u32 *counter, cudaStream_t s, const Scalars *sc = nullptr) {
+                 const EvalOut &eo, u32 *counter, cudaStream_t s, const EvalShape &shape,
+                 const Scalars *sc = nullptr) {
   int dev = 0, sms = 0, per_sm = 0;
   GTC_CUDA(cudaGetDevice(&dev));
   GTC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval<kQuad, kSoft>, kT, 0));
   const u64 want = (n_groups + kWarpsPerBlock - 1) / kWarpsPerBlock;
   if (kQuad && kSoft) {
-    GTC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, k_eval_pairs<kEvalPairsPerIter>, kT, 0));
-    const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
-    k_eval_pairs<kEvalPairsPerIter><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
-                                     static_cast<u32>(n_groups), G, eps2, eo, counter,
-                                     sc ? &sc->n_groups : nullptr, sc ? &sc->abort : nullptr);
+    if (shape.pairs == 1)
+      launch_pairs<1>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter,
+                      s, sc, shape.pass_cost, want, sms);
+    else
+      launch_pairs<2>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter,
+                      s, sc, shape.pass_cost, want, sms);
   } else {
     const u32 grid = static_cast<u32>(std::min<u64>(want, static_cast<u64>(sms) * std::max(1, per_sm)));
     k_eval<kQuad, kSoft><<<grid, kT, 0, s>>>(bodies, cells, cell_list, body_list, groups,
@@ -485,35 +502,37 @@ void launch_eval(const float4 *bodies, const float4 *cells, const u32 *cell_list
 
 void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                     const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s) {
+                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s,
+                    const EvalShape &shape) {
   if (n_groups == 0) return;
   GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
   const bool soft = eps2 > 0.0f;
   if (quadrupole && soft)
-    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s, shape);
   else if (quadrupole)
-    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s, shape);
   else if (soft)
-    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s, shape);
   else
-    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s);
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, n_groups, G, eps2, eo, counter, s, shape);
 }
 
 void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                           const u32 *body_list, const uint4 *groups, u64 max_groups,
                           const Scalars *sc, float G, float eps2, bool quadrupole,
-                          const EvalOut &eo, u32 *counter, cudaStream_t s) {
+                          const EvalOut &eo, u32 *counter, cudaStream_t s,
+                          const EvalShape &shape) {
   if (max_groups == 0) return;
   GTC_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
   const bool soft = eps2 > 0.0f;
   if (quadrupole && soft)
-    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
+    launch_eval<true, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, shape, sc);
   else if (quadrupole)
-    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
+    launch_eval<true, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, shape, sc);
   else if (soft)
-    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
+    launch_eval<false, true>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, shape, sc);
   else
-    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, sc);
+    launch_eval<false, false>(bodies, cells, cell_list, body_list, groups, max_groups, G, eps2, eo, counter, s, shape, sc);
 }
 
 }  // namespace gtc

@@ -264,7 +264,8 @@ void ForestRun::solve(int kick, double h, cudaStream_t s, bool write) {
   evaluate_lists(ws.bodies.as<float4>(), ws.cells.as<float4>(), ws.cell_list.as<u32>(),
                  ws.body_list.as<u32>(), ws.groups.as<uint4>(), ws.n_groups,
                  static_cast<float>(sp.G), static_cast<float>(sp.eps * sp.eps),
-                 sp.quadrupole != 0, EvalOut{ws.out.as<float4>()}, counter.as<u32>(), s);
+                 sp.quadrupole != 0, EvalOut{ws.out.as<float4>()}, counter.as<u32>(), s,
+                 ws.eval_shape);
   if (write) scatter(kick, h, nullptr, s);
   GTC_CUDA(cudaMemcpyAsync(host_sc, ws.scalars.ptr, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   GTC_CUDA(cudaStreamSynchronize(s));

@@ -58,6 +58,15 @@ struct alignas(16) WalkRec64 {
   double mx, my, mz, crit2;  // crit = 2 half / theta + delta (group_lists.cpp:59-60)
 };
 
+// Tile shape of the softened quadrupole list evaluation: staged pairs a
+// lane works per inner-loop iteration (1 or 2; the forces do not depend on
+// it), and a pass's fixed cost in staged entries per lane, which sets how
+// many slices a group's lists are cut into (summation order).
+struct EvalShape {
+  int pairs = 2;
+  u32 pass_cost = 24;
+};
+
 struct SolverParams {
   double G, theta, eps;
   int quadrupole, group_size, leaf_size, pack, criterion;
@@ -130,6 +139,7 @@ struct Workspace {
   DeviceBuffer direct_part;               // direct sum: per-slice partial sums
   DeviceBuffer up_arrive;                 // bottom-up FP32 moments: children finished, per node
   int direct_targets = 2;                 // direct sum: targets per thread (2 or 4)
+  EvalShape eval_shape;                   // list evaluation's tile shape
   RadixScratch radix;
 
   // host-side view of the last build
@@ -352,10 +362,12 @@ struct EvalOut {
 };
 
 // Stage 3: warp-per-group evaluation of the lists into eo.
-// `counter` is one device word the kernel's work queue uses.
+// `counter` is one device word the kernel's work queue uses; `shape` the
+// tile shape of the softened quadrupole evaluation.
 void evaluate_lists(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                     const u32 *body_list, const uint4 *groups, u64 n_groups, float G, float eps2,
-                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s);
+                    bool quadrupole, const EvalOut &eo, u32 *counter, cudaStream_t s,
+                    const EvalShape &shape = EvalShape{});
 
 // Capacities of a solve replayed from a CUDA graph: the sizes of the
 // buffers the graph was captured with. A replay whose tree, depth or lists
@@ -388,7 +400,8 @@ void write_root_task(Workspace &ws, cudaStream_t s);
 void evaluate_lists_graph(const float4 *bodies, const float4 *cells, const u32 *cell_list,
                           const u32 *body_list, const uint4 *groups, u64 max_groups,
                           const Scalars *sc, float G, float eps2, bool quadrupole,
-                          const EvalOut &eo, u32 *counter, cudaStream_t s);
+                          const EvalOut &eo, u32 *counter, cudaStream_t s,
+                          const EvalShape &shape = EvalShape{});
 
 // Direct summation kernels.
 // FP32 estimates of every node's moments (GTCell layout in cells32, delta in

@@ -143,6 +143,8 @@ def _load():
                                    C.POINTER(C.c_int)]),
         "gtc_autotune_direct": (I, [V, P, P, U64, C.POINTER(GravityParams), C.POINTER(C.c_int),
                                     C.POINTER(C.c_double)]),
+        "gtc_autotune_eval": (I, [V, P, P, U64, C.POINTER(GravityParams), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_double)]),
         "gtc_group_sizes": (I, [V] + [C.POINTER(C.c_uint64)] * 5),
         "gtc_group_export": (I, [V, P, P, P, P, P, P, P, P]),
     }
@@ -331,6 +333,15 @@ class Context:
         self._check(lib.gtc_autotune_direct(self.h, pos_ptr, mass_ptr, n, C.byref(gp),
                                             C.byref(k), C.byref(ms)))
         return k.value, ms.value
+
+    def autotune_eval(self, pos_ptr, mass_ptr, n, **kw):
+        """gtc_autotune_eval -> (staged pairs per iteration, pass cost,
+        evaluation kernel ms); the context keeps the winner."""
+        gp = gravity_params(**kw)
+        k, c, ms = C.c_int(), C.c_int(), C.c_double()
+        self._check(lib.gtc_autotune_eval(self.h, pos_ptr, mass_ptr, n, C.byref(gp),
+                                          C.byref(k), C.byref(c), C.byref(ms)))
+        return k.value, c.value, ms.value
 
     # ---- time integration ------------------------------------------------------
 

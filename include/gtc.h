@@ -364,6 +364,17 @@ gtc_status gtc_autotune_group(gtc_context *ctx, const double *pos, const double 
 gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double *mass,
                                uint64_t n, const gtc_gravity_params *gp, int *targets,
                                double *best_ms);
+/* The list evaluation's tile shape (softened quadrupole evaluation): times
+ * the evaluation kernel of gtc_group_force_device on these bodies (device
+ * arrays, parameters gp) with 1 and 2 staged pairs per inner iteration and
+ * pass costs 8, 16, 24, 32 and 48 (how many slices a group's lists are cut
+ * into), keeps the fastest in the context (options "eval_pairs" and
+ * "eval_pass_cost") and returns it in *pairs and *pass_cost, its kernel time
+ * in *best_ms. The staged pairs do not change the forces; the pass cost
+ * changes their summation order only. */
+gtc_status gtc_autotune_eval(gtc_context *ctx, const double *pos, const double *mass,
+                             uint64_t n, const gtc_gravity_params *gp, int *pairs,
+                             int *pass_cost, double *best_ms);
 
 /* ---- tuning and diagnostics (no reference counterpart) ------------------ */
 
@@ -403,6 +414,14 @@ gtc_status gtc_autotune_direct(gtc_context *ctx, const double *pos, const double
  *                        warps, one per group (1), or by three threads per
  *                        group with the long walks handed to warps (0, the
  *                        budgets below); -1 picks as "walk_warps" does.
+ *   "eval_pairs"         2 (default) or 1: staged pairs each lane of the list
+ *                        evaluation works per inner iteration (the forces do
+ *                        not depend on it; gtc_autotune_eval picks it).
+ *   "eval_pass_cost"     whole number 1..256 (default 24): a pass's fixed cost
+ *                        in staged entries per lane, from which the list
+ *                        evaluation picks how many slices to cut each group's
+ *                        lists into (summation order only; gtc_autotune_eval
+ *                        picks it).
  *   "direct_targets"     2 (default) or 4: targets per thread of the direct
  *                        kernel (its tile shape; gtc_autotune_direct picks it).
  *   "stage_events"       0 (default) or 1: record CUDA events at the stage

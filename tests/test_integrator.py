@@ -281,6 +281,37 @@ def test_autotuner_returns_a_timed_configuration(ctx, gtc):
 
 
 @gpu
+def test_autotuner_picks_the_evaluation_tile_shape(gtc):
+    """gtc_autotune_eval times the list evaluation's tile shapes and keeps
+    the fastest in the context. Staged pairs per iteration do not change the
+    forces (bitwise); the pass cost changes the slicing, so the summation
+    order only."""
+    pos, _, mass, _ = gtc.make_galaxy(60_000, seed=9)
+    dpos, dmass = _dev(pos, mass)
+    res = {}
+    c = gtc.Context(0)
+    try:
+        k, cost, ms = c.autotune_eval(dpos.data_ptr(), dmass.data_ptr(), len(mass), **SOLVER)
+        assert k in (1, 2) and cost in (8, 16, 24, 32, 48) and ms > 0
+        for pairs, pass_cost in ((2, 24), (1, 24), (2, 8), (1, 48)):
+            c.set_option("eval_pairs", pairs)
+            c.set_option("eval_pass_cost", pass_cost)
+            res[(pairs, pass_cost)] = c.group_force(pos, mass, **SOLVER)
+        with pytest.raises(gtc.GtcInvalidArgument):
+            c.set_option("eval_pairs", 3)
+        with pytest.raises(gtc.GtcInvalidArgument):
+            c.autotune_eval(dpos.data_ptr(), dmass.data_ptr(), len(mass),
+                            **dict(SOLVER, quadrupole=False))
+    finally:
+        c.close()
+    for a, b in zip(res[(2, 24)], res[(1, 24)]):
+        assert np.array_equal(a, b)
+    ref = res[(2, 24)][0]
+    for key in ((2, 8), (1, 48)):
+        assert np.abs(res[key][0] - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@gpu
 def test_packing_threshold_keeps_sibling_runs(ctx):
     """pack = k >= 2 merges small siblings while the run holds at most k
     bodies: groups are still whole nodes, leaf chunks or sibling runs, the
